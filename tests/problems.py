@@ -1,0 +1,271 @@
+"""Seeded two-site problems shared by the parity tests, ``smoke()`` and the
+benchmark: random block-sparse MPS sites with (N, Sz) bond sectors of a given
+bond dimension, their left / right environments for every operator term,
+and the wavefunction layout of the dot.  The same dense data feed the CPU
+oracle (``oracle/``) and the GPU engine (``zmpo_dmrg_gb300``).
+"""
+import numpy
+
+QPHYS = numpy.array([[0., 0.], [1., -0.5], [1., 0.5], [2., 0.]])
+
+
+def _feasible_left(N, Sz, nelec, sz, nrest):
+    ne = nelec - N
+    na = 0.5 * ne + (sz - Sz)
+    nb = 0.5 * ne - (sz - Sz)
+    return 0 <= ne <= 2 * nrest and -1e-9 <= na <= nrest + 1e-9 and -1e-9 <= nb <= nrest + 1e-9 \
+        and abs(na - round(na)) < 1e-9
+
+
+def _pick(cands, D, center, rng, spread):
+    """Sector dimensions of a truncated bond: keep sectors closest to the
+    expected filling, each no larger than its multiplicity."""
+    keys = sorted(cands)
+    w = numpy.array([-((k[0] - center) ** 2) / spread - abs(k[1]) + 0.01 * rng.random() for k in keys])
+    order = numpy.argsort(-w, kind="stable")
+    dims = {}
+    left = D
+    # share proportional to exp(w), bounded by multiplicity, at least 1
+    pw = numpy.exp(w - w.max())
+    share = pw / pw.sum()
+    for i in order:
+        if left <= 0:
+            break
+        k = keys[i]
+        d = int(min(cands[k], max(1, round(share[i] * D * 1.2)), left))
+        if d > 0:
+            dims[k] = d
+            left -= d
+    out = []
+    for k in sorted(dims):
+        out += [list(k)] * dims[k]
+    return numpy.array(out, dtype=float)
+
+
+def bond_structure(K, nelec, sz, D, rng):
+    qnuml = [numpy.array([[0., 0.]])]
+    for i in range(K):
+        cands = {}
+        for ql in map(tuple, qnuml[i]):
+            for qn in map(tuple, QPHYS):
+                k = (ql[0] + qn[0], ql[1] + qn[1])
+                if _feasible_left(k[0], k[1], nelec, sz, K - i - 1):
+                    cands[k] = cands.get(k, 0) + 1
+        qnuml.append(_pick(cands, D, nelec * (i + 1) / K, rng, 2.0 + 0.25 * min(i + 1, K - i - 1)))
+    qnumr = [None] * (K + 1)
+    qnumr[K] = numpy.array([[0., 0.]])
+    for i in range(K - 1, -1, -1):
+        cands = {}
+        for qn in map(tuple, QPHYS):
+            for qr in map(tuple, qnumr[i + 1]):
+                k = (qn[0] + qr[0], qn[1] + qr[1])
+                if _feasible_left(k[0], k[1], nelec, sz, i):
+                    cands[k] = cands.get(k, 0) + 1
+        qnumr[i] = _pick(cands, D, nelec * (K - i) / K, rng, 2.0 + 0.25 * min(i, K - i))
+    return qnuml, qnumr
+
+
+def random_left_site(ql, qr, rng):
+    """Left-canonical A[l, n, r] with q_l + q_n = q_r (QR per r sector)."""
+    A = numpy.zeros((len(ql), 4, len(qr)))
+    qln = (ql[:, None, :] + QPHYS[None, :, :]).reshape(-1, 2)
+    for key in {tuple(x) for x in qr}:
+        cols = numpy.flatnonzero(numpy.all(qr == key, axis=1))
+        rows = numpy.flatnonzero(numpy.all(numpy.abs(qln - key) < 1e-12, axis=1))
+        if rows.size == 0:
+            continue
+        M = rng.standard_normal((rows.size, cols.size))
+        Q, _ = numpy.linalg.qr(M) if rows.size >= cols.size else (M / numpy.sqrt(rows.size), None)
+        A.reshape(-1, len(qr))[numpy.ix_(rows, cols)] = Q[:, :cols.size]
+    return A
+
+
+def random_right_site(ql, qr, rng):
+    """Right-canonical B[l, n, r] with q_l = q_n + q_r (QR per l sector)."""
+    B = numpy.zeros((len(ql), 4, len(qr)))
+    qnr = (QPHYS[:, None, :] + qr[None, :, :]).reshape(-1, 2)
+    for key in {tuple(x) for x in ql}:
+        rows = numpy.flatnonzero(numpy.all(ql == key, axis=1))
+        cols = numpy.flatnonzero(numpy.all(numpy.abs(qnr - key) < 1e-12, axis=1))
+        if cols.size == 0:
+            continue
+        M = rng.standard_normal((cols.size, rows.size))
+        Q, _ = numpy.linalg.qr(M) if cols.size >= rows.size else (M / numpy.sqrt(cols.size), None)
+        B.reshape(len(ql), -1)[numpy.ix_(rows, cols)] = Q[:, :rows.size].T
+    return B
+
+
+class Problem:
+    pass
+
+
+def random_problem(K=6, nelec=6, D=16, isite=2, seed=0, hop=1.0, sz=0.0, device=True,
+                   with_oracle=True):
+    """Two-site dot at (isite, isite+1) with environments of every H_p."""
+    from oracle import integrals as oint
+    rng = numpy.random.default_rng(seed)
+    h1e, eri, _ = oint.synthetic(K, seed, hop)
+    int1e, int2e, _ = oint.to_spin_orbital(h1e, eri)
+    qnuml, qnumr = bond_structure(K, nelec, sz, D, rng)
+    lsites = [random_left_site(qnuml[i], qnuml[i + 1], rng) for i in range(isite + 1)]
+    rsites = {i: random_right_site(qnumr[i], qnumr[i + 1], rng) for i in range(isite + 2, K)}
+    P = Problem()
+    P.K, P.nelec, P.D, P.isite, P.seed = K, nelec, D, isite, seed
+    P.int1e, P.int2e = int1e, int2e
+    P.qnuml, P.qnumr, P.lsites, P.rsites = qnuml, qnumr, lsites, rsites
+    P.key = [float(nelec), float(sz)]
+    if with_oracle:
+        P.o = _oracle_side(P)
+        P.ndim0 = P.o.qtmp.size_allowed
+    if device:
+        P.p = _product_side(P)
+        P.ndim0 = P.p.qtmp.size_allowed
+    return P
+
+
+def _oracle_side(P):
+    from oracle import dmrg as od, kernel as ok
+    from oracle.qtensor import qtensor
+    m = od.mpo_dmrg(seed=P.seed)
+    m.nsite, m.sbas, m.isym, m.ifQt = P.K, 2 * P.K, 2, True
+    m.build()
+    m.partition()
+    m.loadInts(P.int1e, P.int2e)
+    m.dumpMPO()
+    m.qnuml = list(P.qnuml)
+    m.qnumr = list(P.qnumr)
+    fL = m._boundary('lop', -1)
+    for i in range(P.isite):
+        t = qtensor([False, False, True])
+        t.fromDenseTensor(P.lsites[i], [P.qnuml[i], QPHYS, P.qnuml[i + 1]])
+        fN = {}
+        ok.renorm(m, i, 1, [[fL, None]], [[fN]], t, 'L')
+        fL = fN
+    fR = m._boundary('rop', P.K)
+    for i in range(P.K - 1, P.isite + 1, -1):
+        t = qtensor([True, False, False])
+        t.fromDenseTensor(P.rsites[i], [P.qnumr[i], QPHYS, P.qnumr[i + 1]])
+        fN = {}
+        ok.renorm(m, i, 1, [[None, fR]], [[fN]], t, 'R')
+        fR = fN
+    m.flst = [[fL, fR]]
+    m.dims = (len(P.qnuml[P.isite]), 16, len(P.qnumr[P.isite + 2]), 0)
+    m.qlst = [P.qnuml[P.isite], QPHYS, QPHYS, P.qnumr[P.isite + 2]]
+    m.setupQtmpCI(2, P.key)
+    m._hvec_templates = None
+    return m
+
+
+def _product_side(P):
+    from zmpo_dmrg_gb300.mpo_dmrg_class import mpo_dmrg
+    from zmpo_dmrg_gb300.mpo_dmrg_kernel import renorm
+    from zmpo_dmrg_gb300.qtensor import qtensor
+    m = mpo_dmrg(seed=P.seed)
+    m.nsite, m.sbas, m.isym = P.K, 2 * P.K, 2
+    m.build()
+    m.partition()
+    m.loadInts((P.int1e, P.int2e))
+    m.dumpMPO()
+    fL = m.boundary_env()
+    for i in range(P.isite):
+        t = qtensor([False, False, True])
+        t.fromDenseTensor(P.lsites[i], [P.qnuml[i], QPHYS, P.qnuml[i + 1]])
+        fN = [[None]]
+        renorm(m, i, 1, [[fL, None]], fN, t, 'L')
+        fL = fN[0][0]
+    fR = m.boundary_env()
+    for i in range(P.K - 1, P.isite + 1, -1):
+        t = qtensor([True, False, False])
+        t.fromDenseTensor(P.rsites[i], [P.qnumr[i], QPHYS, P.qnumr[i + 1]])
+        fN = [[None]]
+        renorm(m, i, 1, [[None, fR]], fN, t, 'R')
+        fR = fN[0][0]
+    m.flst = [[fL, fR]]
+    m.qnuml, m.qnumr = list(P.qnuml), list(P.qnumr)
+    m.qlst = [P.qnuml[P.isite], QPHYS, QPHYS, P.qnumr[P.isite + 2]]
+    m.setupQtmpCI(2, P.key)
+    return m
+
+
+def oracle_sigma(P, x):
+    from oracle import kernel as ok
+    m = P.o
+    return ok.HVecQt(numpy.asarray(x, dtype=float), [m, P.isite, 2, m.flst, 'L', True], P.ndim0, None)
+
+
+def oracle_hdiag(P):
+    from oracle import kernel as ok
+    m = P.o
+    prj = m.qtmp.prjmap(m.idlstCI)
+    ldim, rdim = len(P.qnuml[P.isite]), len(P.qnumr[P.isite + 2])
+    m.dims = (ldim, 16, rdim, ldim * 16 * rdim)
+    return ok.HDiagQt([m, P.isite, 2, m.flst, 'L', True], P.ndim0, prj)
+
+
+def product_sigma(P, x, precision="fp64"):
+    from zmpo_dmrg_gb300.mpo_dmrg_kernel import HVec
+    m = P.p
+    m.precision = precision
+    return HVec(numpy.asarray(x, dtype=float), [m, P.isite, 2, m.flst, 'L', True], P.ndim0, None)
+
+
+def product_hdiag(P):
+    from zmpo_dmrg_gb300.mpo_dmrg_kernel import HDiag
+    m = P.p
+    return HDiag([m, P.isite, 2, m.flst, 'L', True], P.ndim0, None).cpu().numpy()
+
+
+def _renorm_site(P):
+    """A left site at the dot (status 'L') or a right site (status 'R')."""
+    rng = numpy.random.default_rng(P.seed + 101)
+    i = P.isite
+    return (P.lsites[i],
+            random_right_site(P.qnumr[i + 1], P.qnumr[i + 2], rng))
+
+
+def oracle_renorm(P, status):
+    from oracle import kernel as ok
+    from oracle.qtensor import qtensor
+    m = P.o
+    A, B = _renorm_site(P)
+    fN = {}
+    if status == 'L':
+        t = qtensor([False, False, True])
+        t.fromDenseTensor(A, [P.qnuml[P.isite], QPHYS, P.qnuml[P.isite + 1]])
+        ok.renorm(m, P.isite, 1, m.flst, [[fN]], t, 'L')
+    else:
+        t = qtensor([True, False, False])
+        t.fromDenseTensor(B, [P.qnumr[P.isite + 1], QPHYS, P.qnumr[P.isite + 2]])
+        ok.renorm(m, P.isite, 2, m.flst, [[fN]], t, 'R')
+    out = []
+    for iop in range(m.nops):
+        v = fN['opers%d' % iop]
+        out.append(numpy.zeros(0) if v is None else v.value)
+    return out
+
+
+def product_renorm(P, status, precision="fp64"):
+    from zmpo_dmrg_gb300.mpo_dmrg_kernel import renorm
+    from zmpo_dmrg_gb300.qtensor import qtensor
+    m = P.p
+    m.precision_renorm = precision
+    A, B = _renorm_site(P)
+    fN = [[None]]
+    if status == 'L':
+        t = qtensor([False, False, True])
+        t.fromDenseTensor(A, [P.qnuml[P.isite], QPHYS, P.qnuml[P.isite + 1]])
+        renorm(m, P.isite, 1, m.flst, fN, t, 'L')
+    else:
+        t = qtensor([True, False, False])
+        t.fromDenseTensor(B, [P.qnumr[P.isite + 1], QPHYS, P.qnumr[P.isite + 2]])
+        renorm(m, P.isite, 2, m.flst, fN, t, 'R')
+    E = fN[0][0]
+    buf = E.buf.cpu().numpy()
+    out = []
+    for iop in range(m.nops):
+        if E.off[iop] < 0:
+            out.append(numpy.zeros(0))
+        else:
+            n = E.tensors[iop].size_allowed
+            out.append(buf[E.off[iop]:E.off[iop] + n])
+    return out

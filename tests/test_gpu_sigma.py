@@ -1,0 +1,72 @@
+"""Sigma vector, diagonal and renormalisation on the GPU against the CPU
+oracle (restated HVecQt / HDiagQt / renormQt_H00 of the reference) on seeded
+random block-sparse problems.  Tolerances: FP64 path <= 1e-10 relative,
+split path <= 1e-8 relative (norm of the difference over the norm)."""
+import numpy
+import pytest
+
+from tests.problems import (random_problem, oracle_sigma, product_sigma, oracle_hdiag,
+                            product_hdiag, oracle_renorm, product_renorm)
+
+pytestmark = pytest.mark.gpu
+
+CASES = [dict(K=4, nelec=4, D=8, isite=1, seed=5),
+         dict(K=6, nelec=6, D=16, isite=2, seed=1),
+         dict(K=6, nelec=6, D=24, isite=0, seed=2),
+         dict(K=6, nelec=6, D=24, isite=4, seed=3),
+         dict(K=8, nelec=8, D=32, isite=3, seed=4)]
+
+_cache = {}
+
+
+def prob(c):
+    key = tuple(sorted(c.items()))
+    if key not in _cache:
+        _cache[key] = random_problem(**c)
+    return _cache[key]
+
+
+def rel(a, b):
+    return numpy.linalg.norm(a - b) / max(numpy.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_sigma_fp64(gpu, case):
+    P = prob(case)
+    x = numpy.random.default_rng(7).standard_normal(P.ndim0)
+    assert rel(product_sigma(P, x, "fp64"), oracle_sigma(P, x)) < 1e-10
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("precision,tol", [("split", 1e-8), ("emu64", 1e-10)])
+def test_sigma_split(gpu, case, precision, tol):
+    P = prob(case)
+    x = numpy.random.default_rng(8).standard_normal(P.ndim0)
+    assert rel(product_sigma(P, x, precision), oracle_sigma(P, x)) < tol
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_hdiag(gpu, case):
+    P = prob(case)
+    assert rel(product_hdiag(P), oracle_hdiag(P)) < 1e-12
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("status", ["L", "R"])
+def test_renorm(gpu, case, status):
+    P = prob(case)
+    a = product_renorm(P, status)
+    b = oracle_renorm(P, status)
+    assert len(a) == len(b)
+    for x, y in zip(a, b):
+        assert x.shape == y.shape
+        if y.size:
+            assert numpy.abs(x - y).max() <= 1e-12 * max(1.0, numpy.abs(y).max())
+
+
+def test_sigma_deterministic(gpu):
+    P = prob(CASES[1])
+    x = numpy.random.default_rng(9).standard_normal(P.ndim0)
+    a = product_sigma(P, x, "fp64")
+    b = product_sigma(P, x, "fp64")
+    assert numpy.array_equal(a, b)

@@ -1,0 +1,86 @@
+// Internal declarations shared by the host-side planner (planner.cpp) and the
+// device kernels (kernels.cu) of the GB300 DMRG engine.
+#pragma once
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace zmpo {
+
+// Device task records.  A "group" is one dense output sub-matrix
+// C[m*scm + n*scn] (m < M, n < N) of an output block; it is the sum of its
+// segments, each a strided GEMM alpha * A(m,k) B(k,n) with k < K.  All
+// contributions to an output region live in one group, so every output
+// element has exactly one writer and the sum order is fixed.
+struct Seg {
+  int64_t a_off, b_off;
+  int64_t sam, sak, sbk, sbn;
+  double alpha;
+  int32_t K;
+  int8_t abuf, bbuf, pad0, pad1;
+};
+
+struct Group {
+  int64_t c_off;
+  int64_t scm, scn;
+  int32_t M, N;
+  int32_t seg0, nseg;
+  int32_t cbuf, pad;
+};
+
+struct Work {
+  int32_t group;
+  int32_t mt, nt;   // tile coordinates inside the group
+  int32_t pad;
+};
+
+constexpr int kMaxBufs = 8;
+struct Bufs {
+  double *p[kMaxBufs];
+};
+
+// One launch worth of tasks (device copies + host mirror of sizes).
+struct Step {
+  std::vector<Seg> segs;
+  std::vector<Group> groups;
+  Seg *d_segs = nullptr;
+  Group *d_groups = nullptr;
+  Work *d_work_fp64 = nullptr;   // tiles of kTileFP64
+  Work *d_work_tc = nullptr;     // tiles of the tensor-core kernel
+  int64_t nwork_fp64 = 0, nwork_tc = 0;
+  double flops = 0.0;            // sum of 2*m*n*k of the reference tasks
+  int64_t ntasks = 0;
+  bool uploaded = false;         // device copies are made on first use
+};
+
+// Launchers (kernels.cu)
+int launch_step_fp64(const Step &s, const Bufs &b, void *stream);
+int launch_step_split(const Step &s, const Bufs &b, int nslices, void *stream);
+
+// Diagonal terms for HDiag: out[l, r] += alpha * sum_{a,b,c} Ld[a,l] Wi[a,b]
+// Wj[b,c] Rd[c,r] for one psi block; Ld/Rd are diagonal blocks of the
+// environments (strided), Wi/Wj scalars per (a,b) / (b,c) sector pair.
+struct DiagTerm {
+  int64_t l_off, r_off, wi_off, wj_off;  // element offsets of the blocks
+  int64_t l_sa, l_sl;                     // L block strides for (a, l)
+  int64_t r_sc, r_sr;                     // R block strides for (c, r)
+  int64_t wi_sa, wi_sb;                   // Wi strides for (a, b)
+  int64_t wj_sb, wj_sc;                   // Wj strides for (b, c)
+  double alpha;
+  int32_t da, db, dc;
+  int32_t ncsite;                         // 1: no Wj factor (dc unused)
+};
+struct DiagBlock {
+  int64_t out_off;
+  int32_t dl, dr;
+  int32_t t0, nt;
+};
+int launch_hdiag(const DiagBlock *blocks, int64_t nblocks, const DiagTerm *terms,
+                 const Bufs &b, double *out, int max_ac, int max_ar, void *stream);
+
+// error recording shared by both translation units
+int record_cuda_error(const char *where, int cuda_err);
+int record_arg_error(const char *msg);
+
+}  // namespace zmpo

@@ -1,0 +1,1180 @@
+// Host side of the GB300 DMRG engine: block layouts, symbolic block-sparse
+// contraction (task lists), GEMM mapping of each block task, sigma / renorm /
+// HDiag plans and the C ABI declared in include/zmpo_gb300.h.
+//
+// The symbolic part restates the reference's qtensor.fromQsyms
+// (source/qtensor/qtensor.py:272-346), the C rule symAllowed
+// (ctypes/qsym.c:5-480) and qtensor.tensordotSYM (qtensor.py:563-637) as
+// plain C++ over integer sector indices.  The numeric part (tensordotCAL,
+// qtensor.py:642-659) becomes grouped GEMM launches in kernels.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/zmpo_gb300.h"
+#include "engine.h"
+
+namespace zmpo {
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+
+int record_cuda_error(const char *where, int cuda_err) {
+  return fail(ZMPO_E_CUDA, std::string(where) + ": " + cudaGetErrorString((cudaError_t)cuda_err));
+}
+
+int record_arg_error(const char *msg) { return fail(ZMPO_E_ARG, msg); }
+
+#define CUDA_TRY(x)                                                      \
+  do {                                                                   \
+    cudaError_t _e = (x);                                                \
+    if (_e != cudaSuccess)                                               \
+      return fail(_e == cudaErrorMemoryAllocation ? ZMPO_E_NOMEM         \
+                                                  : ZMPO_E_CUDA,         \
+                  std::string(#x) + ": " + cudaGetErrorString(_e));      \
+  } while (0)
+
+// ------------------------------------------------------------------ layouts
+struct Packing {
+  int64_t nblks = 0;
+  int64_t size = 0;
+  std::vector<int64_t> flat;     // allowed blocks, ascending flat index
+  std::vector<int64_t> off;      // packed offset of each allowed block
+  std::vector<int32_t> lookup;   // flat -> ordinal, -1 if not allowed
+};
+
+struct Layout {
+  int rank = 0, nq = 0;
+  std::vector<int> nsec;
+  std::vector<std::vector<double>> q;     // [leg][sec*nq + k]
+  std::vector<std::vector<int64_t>> dim;  // [leg][sec]
+  std::vector<int> status;
+  std::shared_ptr<Packing> pk;
+
+  int64_t secstride(int leg) const {
+    int64_t s = 1;
+    for (int j = rank - 1; j > leg; --j) s *= nsec[j];
+    return s;
+  }
+  void sectors(int64_t flat, int *sec) const {
+    for (int j = rank - 1; j >= 0; --j) {
+      sec[j] = (int)(flat % nsec[j]);
+      flat /= nsec[j];
+    }
+  }
+  int64_t ravel(const int *sec) const {
+    int64_t f = 0;
+    for (int j = 0; j < rank; ++j) f = f * nsec[j] + sec[j];
+    return f;
+  }
+  void block_dims(int64_t ord, int64_t *d) const {
+    int sec[16];
+    sectors(pk->flat[ord], sec);
+    for (int j = 0; j < rank; ++j) d[j] = dim[j][sec[j]];
+  }
+};
+
+// allowed iff sum_k |sum_{status 0} q_k - sum_{status 1} q_k| < 1e-10
+static void build_packing(Layout &L) {
+  auto pk = std::make_shared<Packing>();
+  int64_t nb = 1;
+  for (int j = 0; j < L.rank; ++j) nb *= L.nsec[j];
+  pk->nblks = nb;
+  pk->lookup.assign((size_t)nb, -1);
+  std::vector<int> sec(L.rank, 0);
+  std::vector<double> diff(L.nq);
+  int64_t off = 0;
+  for (int64_t f = 0; f < nb; ++f) {
+    if (L.rank > 0) {
+      int64_t t = f;
+      for (int j = L.rank - 1; j >= 0; --j) {
+        sec[j] = (int)(t % L.nsec[j]);
+        t /= L.nsec[j];
+      }
+    }
+    std::fill(diff.begin(), diff.end(), 0.0);
+    for (int j = 0; j < L.rank; ++j) {
+      const double *qq = &L.q[j][(size_t)sec[j] * L.nq];
+      double sg = L.status[j] ? -1.0 : 1.0;
+      for (int k = 0; k < L.nq; ++k) diff[k] += sg * qq[k];
+    }
+    double dtot = 0.0;
+    for (int k = 0; k < L.nq; ++k) dtot += std::fabs(diff[k]);
+    if (dtot < 1e-10) {
+      int64_t n = 1;
+      for (int j = 0; j < L.rank; ++j) n *= L.dim[j][sec[j]];
+      pk->lookup[(size_t)f] = (int32_t)pk->flat.size();
+      pk->flat.push_back(f);
+      pk->off.push_back(off);
+      off += n;
+    }
+  }
+  pk->size = off;
+  L.pk = pk;
+}
+
+// ------------------------------------------------------------ contractions
+struct Task {
+  int32_t ob, ab, bb;
+};
+
+struct Contraction {
+  int lay_a = -1, lay_b = -1, lay_out = -1;
+  std::vector<int> e1, i1, e2, i2;
+  std::vector<Task> tasks;  // sorted by output block
+  std::vector<int64_t> task_start;  // [nout+1] CSR over output blocks
+};
+
+// Steps are built from "output works": one output block region and the list
+// of block products that sum into it.
+struct TaskRef {
+  const Contraction *c;
+  const Layout *la, *lb, *lo;
+  int32_t ab, bb;
+  int64_t a_base, b_base;
+  int abuf, bbuf;
+  double alpha;
+};
+struct OutWork {
+  const Layout *lo;
+  int32_t ob;
+  int64_t c_base;
+  int cbuf;
+  std::vector<TaskRef> tasks;
+};
+
+struct Plan {
+  int kind = 0;  // 1 contract, 2 sigma, 3 renorm
+  std::vector<Step> steps;
+  int64_t ws_elems = 0;
+  double flops = 0.0;
+  int64_t ntasks = 0;
+  // contract
+  int lay_out = -1;
+  // renorm
+  std::vector<int> out_lay;
+  std::vector<int64_t> out_off;
+  int64_t out_total = 0;
+  int status = 0;
+  // sigma: the psi size (checked at call time) and HDiag tables
+  int64_t ndim0 = 0;
+  std::vector<DiagBlock> dblocks;
+  std::vector<DiagTerm> dterms;
+  DiagBlock *d_dblocks = nullptr;
+  DiagTerm *d_dterms = nullptr;
+  int64_t max_ac = 0, max_ar = 0;
+  bool diag_uploaded = false;
+};
+
+}  // namespace zmpo
+
+using namespace zmpo;
+
+struct zmpo_engine {
+  int device = 0;
+  std::vector<std::unique_ptr<Layout>> layouts;
+  std::vector<std::unique_ptr<Contraction>> contractions;
+  std::vector<std::unique_ptr<Plan>> plans;
+};
+
+namespace zmpo {
+
+static Layout *get_layout(zmpo_engine *e, int id) {
+  if (!e || id < 0 || id >= (int)e->layouts.size() || !e->layouts[id]) return nullptr;
+  return e->layouts[id].get();
+}
+
+static int add_layout(zmpo_engine *e, std::unique_ptr<Layout> L) {
+  e->layouts.push_back(std::move(L));
+  return (int)e->layouts.size() - 1;
+}
+
+static bool same_q(const Layout &A, int la, const Layout &B, int lb) {
+  if (A.nsec[la] != B.nsec[lb] || A.nq != B.nq) return false;
+  for (size_t i = 0; i < A.q[la].size(); ++i)
+    if (A.q[la][i] != B.q[lb][i]) return false;
+  for (int s = 0; s < A.nsec[la]; ++s)
+    if (A.dim[la][s] != B.dim[lb][s]) return false;
+  return true;
+}
+
+// tensordotSYM: output layout + task list (qtensor.py:563-637)
+static int build_contraction(zmpo_engine *e, int ia, int ib, int naxes, const int *ax_a,
+                             const int *ax_b, int *out_layout, int *out_contr) {
+  Layout *A = get_layout(e, ia), *B = get_layout(e, ib);
+  if (!A || !B) return fail(ZMPO_E_ID, "contract: unknown layout");
+  auto C = std::make_unique<Contraction>();
+  C->lay_a = ia;
+  C->lay_b = ib;
+  std::vector<char> ina(A->rank, 0), inb(B->rank, 0);
+  for (int k = 0; k < naxes; ++k) {
+    if (ax_a[k] < 0 || ax_a[k] >= A->rank || ax_b[k] < 0 || ax_b[k] >= B->rank)
+      return fail(ZMPO_E_ARG, "contract: axis out of range");
+    ina[ax_a[k]] = 1;
+    inb[ax_b[k]] = 1;
+    C->i1.push_back(ax_a[k]);
+    C->i2.push_back(ax_b[k]);
+    if (!same_q(*A, ax_a[k], *B, ax_b[k]))
+      return fail(ZMPO_E_SYM, "contract: contracted legs have different sectors");
+  }
+  for (int j = 0; j < A->rank; ++j)
+    if (!ina[j]) C->e1.push_back(j);
+  for (int j = 0; j < B->rank; ++j)
+    if (!inb[j]) C->e2.push_back(j);
+  std::vector<int> exts2;
+  for (int j : C->e2) exts2.push_back(B->status[j]);
+  if (naxes > 0) {
+    bool flip = A->status[C->i1[0]] == B->status[C->i2[0]];
+    for (int k = 0; k < naxes; ++k) {
+      int s2 = B->status[C->i2[k]] ^ (flip ? 1 : 0);
+      if (A->status[C->i1[k]] == s2)
+        return fail(ZMPO_E_SYM, "contract: inconsistent leg directions");
+    }
+    if (flip)
+      for (auto &s : exts2) s ^= 1;
+  }
+  auto O = std::make_unique<Layout>();
+  O->nq = A->nq;
+  for (int j : C->e1) {
+    O->nsec.push_back(A->nsec[j]);
+    O->q.push_back(A->q[j]);
+    O->dim.push_back(A->dim[j]);
+    O->status.push_back(A->status[j]);
+  }
+  for (size_t t = 0; t < C->e2.size(); ++t) {
+    int j = C->e2[t];
+    O->nsec.push_back(B->nsec[j]);
+    O->q.push_back(B->q[j]);
+    O->dim.push_back(B->dim[j]);
+    O->status.push_back(exts2[t]);
+  }
+  O->rank = (int)O->nsec.size();
+  build_packing(*O);
+  // index A's allowed blocks by their external sector tuple
+  const int ne1 = (int)C->e1.size(), ne2 = (int)C->e2.size();
+  std::unordered_map<int64_t, std::vector<std::pair<int64_t, int32_t>>> amap;
+  {
+    int sec[16];
+    for (size_t ob = 0; ob < A->pk->flat.size(); ++ob) {
+      A->sectors(A->pk->flat[ob], sec);
+      int64_t ef = 0, inf = 0;
+      for (int j : C->e1) ef = ef * A->nsec[j] + sec[j];
+      for (int j : C->i1) inf = inf * A->nsec[j] + sec[j];
+      amap[ef].push_back({inf, (int32_t)ob});
+    }
+    for (auto &kv : amap) std::sort(kv.second.begin(), kv.second.end());
+  }
+  C->task_start.assign(O->pk->flat.size() + 1, 0);
+  int osec[16], bsec[16], isec[16];
+  for (size_t ob = 0; ob < O->pk->flat.size(); ++ob) {
+    C->task_start[ob] = (int64_t)C->tasks.size();
+    O->sectors(O->pk->flat[ob], osec);
+    int64_t ef = 0;
+    for (int t = 0; t < ne1; ++t) ef = ef * A->nsec[C->e1[t]] + osec[t];
+    auto it = amap.find(ef);
+    if (it == amap.end()) continue;
+    for (auto &pr : it->second) {
+      // internal sector indices from the A internal flat
+      int64_t inf = pr.first;
+      for (int k = naxes - 1; k >= 0; --k) {
+        isec[k] = (int)(inf % A->nsec[C->i1[k]]);
+        inf /= A->nsec[C->i1[k]];
+      }
+      for (int k = 0; k < naxes; ++k) bsec[C->i2[k]] = isec[k];
+      for (int t = 0; t < ne2; ++t) bsec[C->e2[t]] = osec[ne1 + t];
+      int64_t bf = B->ravel(bsec);
+      int32_t bo = B->pk->lookup[(size_t)bf];
+      if (bo < 0) continue;
+      C->tasks.push_back({(int32_t)ob, pr.second, bo});
+    }
+  }
+  C->task_start[O->pk->flat.size()] = (int64_t)C->tasks.size();
+  int lo = add_layout(e, std::move(O));
+  C->lay_out = lo;
+  e->contractions.push_back(std::move(C));
+  *out_layout = lo;
+  *out_contr = (int)e->contractions.size() - 1;
+  return ZMPO_OK;
+}
+
+// ------------------------------------------------------------ GEMM mapping
+struct Leg2 {
+  int64_t d, s0, s1;
+};
+
+static void rowmajor_strides(const int64_t *d, int r, int64_t *st) {
+  int64_t s = 1;
+  for (int j = r - 1; j >= 0; --j) {
+    st[j] = s;
+    s *= d[j];
+  }
+}
+
+// merge adjacent legs (outer first) when contiguous in both operands
+static std::vector<Leg2> merge_legs(const std::vector<Leg2> &in) {
+  std::vector<Leg2> out;
+  for (const auto &l : in) {
+    if (l.d == 1) continue;
+    if (!out.empty()) {
+      Leg2 &o = out.back();
+      if (o.s0 == l.d * l.s0 && o.s1 == l.d * l.s1) {
+        o.d *= l.d;
+        o.s0 = l.s0;
+        o.s1 = l.s1;
+        continue;
+      }
+    }
+    out.push_back(l);
+  }
+  return out;
+}
+
+// Expand all output works of one launch into groups / segments.
+static int build_step(std::vector<OutWork> &works, Step &st) {
+  st.segs.clear();
+  st.groups.clear();
+  for (auto &w : works) {
+    const Layout &O = *w.lo;
+    int64_t od[16], ost[16];
+    O.block_dims(w.ob, od);
+    rowmajor_strides(od, O.rank, ost);
+    const int64_t c0 = w.c_base + O.pk->off[w.ob];
+    // legs of the output block; M legs are e1 of each task's contraction, N
+    // legs e2.  All tasks of one output work share the split (ne1 fixed).
+    int ne1 = w.tasks.empty() ? O.rank : (int)w.tasks[0].c->e1.size();
+    for (auto &t : w.tasks)
+      if ((int)t.c->e1.size() != ne1) return fail(ZMPO_E_ARG, "mixed contraction split");
+    // Determine M decomposition valid for C and every task's A; likewise N.
+    // Represent each merged leg by its range of original legs.
+    auto decompose = [&](int j0, int j1, bool isM, std::vector<std::pair<int, int>> &ranges) {
+      ranges.clear();
+      int start = -1;
+      for (int j = j0; j < j1; ++j) {
+        if (od[j] == 1) continue;
+        if (start < 0) {
+          start = j;
+          ranges.push_back({j, j + 1});
+          continue;
+        }
+        auto &rg = ranges.back();
+        int outer = rg.second - 1;
+        // find previous non-unit leg in the range
+        while (outer >= rg.first && od[outer] == 1) --outer;
+        bool ok = ost[outer] == od[j] * ost[j];
+        for (auto &t : w.tasks) {
+          if (!ok) break;
+          const Layout &X = isM ? *t.la : *t.lb;
+          int32_t xb = isM ? t.ab : t.bb;
+          int64_t xd[16], xs[16];
+          X.block_dims(xb, xd);
+          rowmajor_strides(xd, X.rank, xs);
+          const std::vector<int> &ex = isM ? t.c->e1 : t.c->e2;
+          int jo = isM ? outer : outer - ne1, ji = isM ? j : j - ne1;
+          ok = xs[ex[jo]] == od[j] * xs[ex[ji]];
+        }
+        if (ok)
+          rg.second = j + 1;
+        else
+          ranges.push_back({j, j + 1});
+      }
+    };
+    std::vector<std::pair<int, int>> mr, nr;
+    decompose(0, ne1, true, mr);
+    decompose(ne1, O.rank, false, nr);
+    auto rdim = [&](const std::pair<int, int> &r) {
+      int64_t d = 1;
+      for (int j = r.first; j < r.second; ++j) d *= od[j];
+      return d;
+    };
+    auto innermost = [&](const std::pair<int, int> &r) {
+      int j = r.second - 1;
+      while (j > r.first && od[j] == 1) --j;
+      return j;
+    };
+    // primary M / N range = largest; the others become sub-region loops
+    int pm = -1, pn = -1;
+    for (int i = 0; i < (int)mr.size(); ++i)
+      if (pm < 0 || rdim(mr[i]) > rdim(mr[pm])) pm = i;
+    for (int i = 0; i < (int)nr.size(); ++i)
+      if (pn < 0 || rdim(nr[i]) > rdim(nr[pn])) pn = i;
+    std::vector<std::pair<int, int>> loops;  // (range index, isM)
+    for (int i = 0; i < (int)mr.size(); ++i)
+      if (i != pm) loops.push_back({i, 1});
+    for (int i = 0; i < (int)nr.size(); ++i)
+      if (i != pn) loops.push_back({i, 0});
+    int64_t nsub = 1;
+    for (auto &lp : loops) nsub *= rdim(lp.second ? mr[lp.first] : nr[lp.first]);
+    const int64_t M = pm >= 0 ? rdim(mr[pm]) : 1;
+    const int64_t N = pn >= 0 ? rdim(nr[pn]) : 1;
+    const int64_t scm = pm >= 0 ? ost[innermost(mr[pm])] : 0;
+    const int64_t scn = pn >= 0 ? ost[innermost(nr[pn])] : 0;
+    if (M > INT32_MAX || N > INT32_MAX) return fail(ZMPO_E_SIZE, "block too large");
+    for (int64_t sub = 0; sub < nsub; ++sub) {
+      // multi-index of the sub-region over the loop ranges; each range is a
+      // merged leg so its index maps linearly with the innermost stride
+      std::vector<int64_t> lidx(loops.size());
+      int64_t t = sub;
+      for (int i = (int)loops.size() - 1; i >= 0; --i) {
+        int64_t d = rdim(loops[i].second ? mr[loops[i].first] : nr[loops[i].first]);
+        lidx[i] = t % d;
+        t /= d;
+      }
+      int64_t coff = c0;
+      for (size_t i = 0; i < loops.size(); ++i) {
+        auto &rg = loops[i].second ? mr[loops[i].first] : nr[loops[i].first];
+        coff += lidx[i] * ost[innermost(rg)];
+      }
+      Group g;
+      g.c_off = coff;
+      g.scm = scm;
+      g.scn = scn;
+      g.M = (int32_t)M;
+      g.N = (int32_t)N;
+      g.seg0 = (int32_t)st.segs.size();
+      g.cbuf = w.cbuf;
+      g.pad = 0;
+      for (auto &tk : w.tasks) {
+        const Layout &A = *tk.la, &B = *tk.lb;
+        int64_t ad[16], as[16], bd[16], bs[16];
+        A.block_dims(tk.ab, ad);
+        B.block_dims(tk.bb, bd);
+        rowmajor_strides(ad, A.rank, as);
+        rowmajor_strides(bd, B.rank, bs);
+        const auto &e1 = tk.c->e1, &e2 = tk.c->e2, &i1 = tk.c->i1, &i2 = tk.c->i2;
+        // reference work unit: 2 * m * n * k of the full block product
+        if (sub == 0) {
+          double m = 1, n = 1, k = 1;
+          for (int j : e1) m *= (double)ad[j];
+          for (int j : e2) n *= (double)bd[j];
+          for (int j : i1) k *= (double)ad[j];
+          st.flops += 2.0 * m * n * k;
+          st.ntasks += 1;
+        }
+        int64_t a0 = tk.a_base + A.pk->off[tk.ab];
+        int64_t b0 = tk.b_base + B.pk->off[tk.bb];
+        for (size_t i = 0; i < loops.size(); ++i) {
+          auto &rg = loops[i].second ? mr[loops[i].first] : nr[loops[i].first];
+          int jj = innermost(rg);
+          if (loops[i].second)
+            a0 += lidx[i] * as[e1[jj]];
+          else
+            b0 += lidx[i] * bs[e2[jj - ne1]];
+        }
+        int64_t sam = pm >= 0 ? as[e1[innermost(mr[pm])]] : 0;
+        int64_t sbn = pn >= 0 ? bs[e2[innermost(nr[pn]) - ne1]] : 0;
+        // K legs: sort by A stride (descending), merge where contiguous in both
+        std::vector<Leg2> kl;
+        for (size_t k = 0; k < i1.size(); ++k) kl.push_back({ad[i1[k]], as[i1[k]], bs[i2[k]]});
+        std::sort(kl.begin(), kl.end(), [](const Leg2 &x, const Leg2 &y) { return x.s0 > y.s0; });
+        kl = merge_legs(kl);
+        int pk = -1;
+        for (int i = 0; i < (int)kl.size(); ++i)
+          if (pk < 0 || kl[i].d > kl[pk].d) pk = i;
+        int64_t K = pk >= 0 ? kl[pk].d : 1;
+        int64_t sak = pk >= 0 ? kl[pk].s0 : 0, sbk = pk >= 0 ? kl[pk].s1 : 0;
+        std::vector<Leg2> kloops;
+        for (int i = 0; i < (int)kl.size(); ++i)
+          if (i != pk) kloops.push_back(kl[i]);
+        int64_t nk = 1;
+        for (auto &l : kloops) nk *= l.d;
+        for (int64_t ki = 0; ki < nk; ++ki) {
+          int64_t aa = a0, bb = b0, tt = ki;
+          for (int i = (int)kloops.size() - 1; i >= 0; --i) {
+            int64_t x = tt % kloops[i].d;
+            tt /= kloops[i].d;
+            aa += x * kloops[i].s0;
+            bb += x * kloops[i].s1;
+          }
+          Seg s;
+          s.a_off = aa;
+          s.b_off = bb;
+          s.sam = sam;
+          s.sak = sak;
+          s.sbk = sbk;
+          s.sbn = sbn;
+          s.alpha = tk.alpha;
+          s.K = (int32_t)K;
+          s.abuf = (int8_t)tk.abuf;
+          s.bbuf = (int8_t)tk.bbuf;
+          s.pad0 = s.pad1 = 0;
+          st.segs.push_back(s);
+        }
+      }
+      g.nseg = (int32_t)st.segs.size() - g.seg0;
+      st.groups.push_back(g);
+    }
+  }
+  return ZMPO_OK;
+}
+
+// tile sizes of the two kernels (must match kernels.cu)
+constexpr int kTileFP64M = 32, kTileFP64N = 32;
+constexpr int kTileTCM = 32, kTileTCN = 32;
+
+static int upload_step(Step &st) {
+  if (st.uploaded) return ZMPO_OK;
+  std::vector<Work> w64, wtc;
+  // order groups by cost (longest first) for load balance
+  std::vector<int> order(st.groups.size());
+  std::iota(order.begin(), order.end(), 0);
+  std::vector<int64_t> cost(st.groups.size(), 0);
+  for (size_t g = 0; g < st.groups.size(); ++g) {
+    int64_t c = 0;
+    for (int s = 0; s < st.groups[g].nseg; ++s) c += st.segs[st.groups[g].seg0 + s].K + 16;
+    cost[g] = c;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  for (int g : order) {
+    const Group &G = st.groups[g];
+    for (int mt = 0; mt * kTileFP64M < G.M; ++mt)
+      for (int nt = 0; nt * kTileFP64N < G.N; ++nt) w64.push_back({g, mt, nt, 0});
+    for (int mt = 0; mt * kTileTCM < G.M; ++mt)
+      for (int nt = 0; nt * kTileTCN < G.N; ++nt) wtc.push_back({g, mt, nt, 0});
+  }
+  st.nwork_fp64 = (int64_t)w64.size();
+  st.nwork_tc = (int64_t)wtc.size();
+  auto up = [](auto **dptr, const auto &v) -> cudaError_t {
+    using T = typename std::remove_reference<decltype(v)>::type::value_type;
+    if (v.empty()) {
+      *dptr = nullptr;
+      return cudaSuccess;
+    }
+    cudaError_t e = cudaMalloc((void **)dptr, v.size() * sizeof(T));
+    if (e != cudaSuccess) return e;
+    return cudaMemcpy(*dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+  };
+  CUDA_TRY(up(&st.d_segs, st.segs));
+  CUDA_TRY(up(&st.d_groups, st.groups));
+  CUDA_TRY(up(&st.d_work_fp64, w64));
+  CUDA_TRY(up(&st.d_work_tc, wtc));
+  // keep the host mirror of groups (sizes) but free the bulky segment copy
+  std::vector<Seg>().swap(st.segs);
+  st.uploaded = true;
+  return ZMPO_OK;
+}
+
+static void free_step(Step &st) {
+  cudaFree(st.d_segs);
+  cudaFree(st.d_groups);
+  cudaFree(st.d_work_fp64);
+  cudaFree(st.d_work_tc);
+  st.d_segs = nullptr;
+  st.d_groups = nullptr;
+  st.d_work_fp64 = st.d_work_tc = nullptr;
+}
+
+static int run_step(Step &st, const Bufs &b, int precision, void *stream) {
+  int rc = upload_step(st);
+  if (rc) return rc;
+  if (precision == ZMPO_PREC_FP64) return launch_step_fp64(st, b, stream);
+  if (precision == ZMPO_PREC_SPLIT) return launch_step_split(st, b, 4, stream);
+  if (precision == ZMPO_PREC_EMU64) return launch_step_split(st, b, 7, stream);
+  return fail(ZMPO_E_ARG, "unknown precision");
+}
+
+static Plan *get_plan(zmpo_engine *e, int id, int kind) {
+  if (!e || id < 0 || id >= (int)e->plans.size() || !e->plans[id]) return nullptr;
+  if (kind && e->plans[id]->kind != kind) return nullptr;
+  return e->plans[id].get();
+}
+
+// per-class chain of contractions, instantiated per operator
+struct ChainStep {
+  int contr;  // contraction id
+  int lay;    // output layout
+};
+
+}  // namespace zmpo
+
+// ====================================================================== C ABI
+extern "C" {
+
+int zmpo_last_error(char *buf, size_t len) {
+  if (!buf || len == 0) return ZMPO_E_ARG;
+  std::snprintf(buf, len, "%s", g_err.c_str());
+  return ZMPO_OK;
+}
+
+int zmpo_version(void) { return 1; }
+
+int symAllowed(int rank, int nqnum, int *ndims, int *status, int *allowed, double *a0,
+               double *a1, double *a2, double *a3, double *a4, double *a5, double *a6,
+               double *a7) {
+  if (rank < 1 || rank > 8 || nqnum < 1 || !ndims || !status || !allowed)
+    return fail(ZMPO_E_ARG, "symAllowed: rank must be 1..8");
+  double *qs[8] = {a0, a1, a2, a3, a4, a5, a6, a7};
+  int64_t nb = 1;
+  for (int j = 0; j < rank; ++j) {
+    if (!qs[j] || ndims[j] < 0) return fail(ZMPO_E_ARG, "symAllowed: missing leg");
+    nb *= ndims[j];
+  }
+  int sec[8] = {0};
+  std::vector<double> diff(nqnum);
+  for (int64_t f = 0; f < nb; ++f) {
+    int64_t t = f;
+    for (int j = rank - 1; j >= 0; --j) {
+      sec[j] = (int)(t % ndims[j]);
+      t /= ndims[j];
+    }
+    std::fill(diff.begin(), diff.end(), 0.0);
+    for (int j = 0; j < rank; ++j) {
+      const double *q = qs[j] + (size_t)sec[j] * nqnum;
+      for (int k = 0; k < nqnum; ++k) diff[k] += status[j] == 0 ? q[k] : -q[k];
+    }
+    double dtot = 0.0;
+    for (int k = 0; k < nqnum; ++k) dtot += std::fabs(diff[k]);
+    allowed[f] = dtot < 1.e-10;
+  }
+  return ZMPO_OK;
+}
+
+int zmpo_engine_create(zmpo_engine **out, int device) {
+  if (!out) return fail(ZMPO_E_ARG, "engine_create: null out");
+  *out = new zmpo_engine();
+  (*out)->device = device;
+  return ZMPO_OK;
+}
+
+int zmpo_engine_destroy(zmpo_engine *e) {
+  if (!e) return ZMPO_OK;
+  for (auto &p : e->plans) {
+    if (!p) continue;
+    for (auto &s : p->steps) free_step(s);
+    cudaFree(p->d_dblocks);
+    cudaFree(p->d_dterms);
+  }
+  delete e;
+  return ZMPO_OK;
+}
+
+int zmpo_layout_create(zmpo_engine *e, int rank, int nqnum, const int *nsec,
+                       const double *qsyms, const int64_t *dims, const int *status,
+                       int *layout_id) {
+  if (!e || !layout_id || rank < 0 || rank > 12 || nqnum < 1 || (rank > 0 && (!nsec || !qsyms || !dims || !status)))
+    return fail(ZMPO_E_ARG, "layout_create: bad arguments");
+  auto L = std::make_unique<Layout>();
+  L->rank = rank;
+  L->nq = nqnum;
+  size_t qo = 0, dof = 0;
+  int64_t nb = 1;
+  for (int j = 0; j < rank; ++j) {
+    if (nsec[j] < 1) return fail(ZMPO_E_ARG, "layout_create: empty leg");
+    L->nsec.push_back(nsec[j]);
+    L->q.emplace_back(qsyms + qo, qsyms + qo + (size_t)nsec[j] * nqnum);
+    L->dim.emplace_back(dims + dof, dims + dof + nsec[j]);
+    for (int s = 0; s < nsec[j]; ++s)
+      if (dims[dof + s] < 1) return fail(ZMPO_E_ARG, "layout_create: sector dim < 1");
+    L->status.push_back(status[j] ? 1 : 0);
+    qo += (size_t)nsec[j] * nqnum;
+    dof += nsec[j];
+    nb *= nsec[j];
+    if (nb > (int64_t)1 << 31) return fail(ZMPO_E_SIZE, "layout_create: too many blocks");
+  }
+  build_packing(*L);
+  *layout_id = add_layout(e, std::move(L));
+  return ZMPO_OK;
+}
+
+int zmpo_layout_derive(zmpo_engine *e, int src, const double *qsyms, const int *status,
+                       int *layout_id) {
+  Layout *S = get_layout(e, src);
+  if (!S || !qsyms || !status || !layout_id) return fail(ZMPO_E_ARG, "layout_derive: bad arguments");
+  auto L = std::make_unique<Layout>(*S);
+  size_t qo = 0;
+  for (int j = 0; j < L->rank; ++j) {
+    L->q[j].assign(qsyms + qo, qsyms + qo + (size_t)L->nsec[j] * L->nq);
+    qo += (size_t)L->nsec[j] * L->nq;
+    L->status[j] = status[j] ? 1 : 0;
+  }
+  *layout_id = add_layout(e, std::move(L));
+  return ZMPO_OK;
+}
+
+int zmpo_layout_info(zmpo_engine *e, int id, int64_t *size_allowed, int64_t *nblocks, int *rank) {
+  Layout *L = get_layout(e, id);
+  if (!L) return fail(ZMPO_E_ID, "layout_info: unknown layout");
+  if (size_allowed) *size_allowed = L->pk->size;
+  if (nblocks) *nblocks = (int64_t)L->pk->flat.size();
+  if (rank) *rank = L->rank;
+  return ZMPO_OK;
+}
+
+int zmpo_layout_blocks(zmpo_engine *e, int id, int64_t *flat, int64_t *off) {
+  Layout *L = get_layout(e, id);
+  if (!L) return fail(ZMPO_E_ID, "layout_blocks: unknown layout");
+  for (size_t i = 0; i < L->pk->flat.size(); ++i) {
+    if (flat) flat[i] = L->pk->flat[i];
+    if (off) off[i] = L->pk->off[i];
+  }
+  return ZMPO_OK;
+}
+
+int zmpo_contract_plan(zmpo_engine *e, int lay_a, int lay_b, int naxes, const int *axes_a,
+                       const int *axes_b, int *lay_out, int *plan_id) {
+  if (!e || !lay_out || !plan_id || naxes < 0 || (naxes > 0 && (!axes_a || !axes_b)))
+    return fail(ZMPO_E_ARG, "contract_plan: bad arguments");
+  int lo, ci;
+  int rc = build_contraction(e, lay_a, lay_b, naxes, axes_a, axes_b, &lo, &ci);
+  if (rc) return rc;
+  auto P = std::make_unique<Plan>();
+  P->kind = 1;
+  P->lay_out = lo;
+  const Contraction *C = e->contractions[ci].get();
+  const Layout *A = get_layout(e, lay_a), *B = get_layout(e, lay_b), *O = get_layout(e, lo);
+  std::vector<OutWork> works(O->pk->flat.size());
+  for (size_t ob = 0; ob < O->pk->flat.size(); ++ob) {
+    OutWork &w = works[ob];
+    w.lo = O;
+    w.ob = (int32_t)ob;
+    w.c_base = 0;
+    w.cbuf = 4;
+    for (int64_t t = C->task_start[ob]; t < C->task_start[ob + 1]; ++t)
+      w.tasks.push_back({C, A, B, O, C->tasks[t].ab, C->tasks[t].bb, 0, 0, 0, 1, 1.0});
+  }
+  P->steps.emplace_back();
+  rc = build_step(works, P->steps.back());
+  if (rc) return rc;
+  P->flops = P->steps.back().flops;
+  P->ntasks = P->steps.back().ntasks;
+  e->plans.push_back(std::move(P));
+  *lay_out = lo;
+  *plan_id = (int)e->plans.size() - 1;
+  return ZMPO_OK;
+}
+
+int zmpo_contract_exec(zmpo_engine *e, int plan_id, const double *d_a, const double *d_b,
+                       double *d_out, int precision, void *stream) {
+  Plan *P = get_plan(e, plan_id, 1);
+  if (!P) return fail(ZMPO_E_ID, "contract_exec: unknown plan");
+  Bufs b{};
+  b.p[0] = const_cast<double *>(d_a);
+  b.p[1] = const_cast<double *>(d_b);
+  b.p[4] = d_out;
+  return run_step(P->steps[0], b, precision, stream);
+}
+
+int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
+  if (!e || !d || !plan_id || d->nop < 0 || d->nclass < 1 || (d->ncsite != 1 && d->ncsite != 2))
+    return fail(ZMPO_E_ARG, "sigma_plan: bad descriptor");
+  const Layout *Psi = get_layout(e, d->lay_psi);
+  if (!Psi) return fail(ZMPO_E_ID, "sigma_plan: unknown psi layout");
+  // per-class symbolic chain (the reference caches the same per icase0,
+  // mpo_dmrg_kernelQt.py:199-204)
+  struct ClassChain {
+    bool built = false, empty = false;
+    std::vector<ChainStep> c;
+  };
+  std::vector<ClassChain> chains(d->nclass);
+  static const int ax1a[1] = {2}, ax1b[1] = {0};
+  static const int ax2a[2] = {0, 2}, ax2b[2] = {0, 3};
+  static const int ax3a[2] = {1, 3}, ax3b[2] = {3, 0};
+  static const int ax4a[2] = {1, 3}, ax4b[2] = {2, 0};
+  static const int ax3a1[2] = {1, 2}, ax3b1[2] = {2, 0};
+  for (int op = 0; op < d->nop; ++op) {
+    int c = d->op_class[op];
+    if (c < 0 || c >= d->nclass) return fail(ZMPO_E_ARG, "sigma_plan: bad class");
+    ClassChain &ch = chains[c];
+    if (ch.built) continue;
+    ch.built = true;
+    int lo, ci, rc;
+    rc = build_contraction(e, d->lay_L[c], d->lay_psi, 1, ax1a, ax1b, &lo, &ci);
+    if (rc) return rc;
+    ch.c.push_back({ci, lo});
+    rc = build_contraction(e, lo, d->lay_Wi[c], 2, ax2a, ax2b, &lo, &ci);
+    if (rc) return rc;
+    ch.c.push_back({ci, lo});
+    if (d->ncsite == 2) {
+      rc = build_contraction(e, lo, d->lay_Wj[c], 2, ax3a, ax3b, &lo, &ci);
+      if (rc) return rc;
+      ch.c.push_back({ci, lo});
+      rc = build_contraction(e, lo, d->lay_Rf[c], 2, ax4a, ax4b, &lo, &ci);
+    } else {
+      rc = build_contraction(e, lo, d->lay_Rf[c], 2, ax3a1, ax3b1, &lo, &ci);
+    }
+    if (rc) return rc;
+    ch.c.push_back({ci, lo});
+    const Layout *Out = get_layout(e, lo);
+    if (Out->pk->flat != Psi->pk->flat || Out->pk->size != Psi->pk->size)
+      return fail(ZMPO_E_SYM, "sigma_plan: H.psi layout differs from psi layout");
+  }
+  auto P = std::make_unique<Plan>();
+  P->kind = 2;
+  P->ndim0 = Psi->pk->size;
+  const int nstep = d->ncsite == 2 ? 4 : 3;
+  // workspace offsets: per op, intermediates of steps 0..nstep-2
+  std::vector<std::vector<int64_t>> ws_off(d->nop, std::vector<int64_t>(nstep - 1, 0));
+  int64_t ws = 0;
+  for (int op = 0; op < d->nop; ++op) {
+    const ClassChain &ch = chains[d->op_class[op]];
+    for (int s = 0; s < nstep - 1; ++s) {
+      ws_off[op][s] = ws;
+      ws += get_layout(e, ch.c[s].lay)->pk->size;
+      ws = (ws + 31) & ~int64_t(31);
+    }
+  }
+  P->ws_elems = ws;
+  // buffers: 0 L, 1 R, 2 W, 3 x, 4 y, 5 workspace
+  for (int s = 0; s < nstep; ++s) {
+    std::vector<OutWork> works;
+    if (s < nstep - 1) {
+      for (int op = 0; op < d->nop; ++op) {
+        const ClassChain &ch = chains[d->op_class[op]];
+        const Contraction *C = e->contractions[ch.c[s].contr].get();
+        const Layout *A = get_layout(e, C->lay_a), *B = get_layout(e, C->lay_b),
+                     *O = get_layout(e, C->lay_out);
+        int abuf, bbuf;
+        int64_t abase, bbase;
+        if (s == 0) {
+          abuf = 0; abase = d->off_L[op];
+          bbuf = 3; bbase = 0;
+        } else {
+          abuf = 5; abase = ws_off[op][s - 1];
+          bbuf = 2; bbase = (s == 1) ? d->off_Wi[op] : d->off_Wj[op];
+        }
+        for (size_t ob = 0; ob < O->pk->flat.size(); ++ob) {
+          OutWork w;
+          w.lo = O;
+          w.ob = (int32_t)ob;
+          w.c_base = ws_off[op][s];
+          w.cbuf = 5;
+          for (int64_t t = C->task_start[ob]; t < C->task_start[ob + 1]; ++t)
+            w.tasks.push_back({C, A, B, O, C->tasks[t].ab, C->tasks[t].bb, abase, bbase, abuf, bbuf, 1.0});
+          works.push_back(std::move(w));
+        }
+      }
+    } else {
+      // last step: every op contributes to the same psi blocks
+      works.resize(Psi->pk->flat.size());
+      for (size_t ob = 0; ob < works.size(); ++ob) {
+        works[ob].lo = Psi;
+        works[ob].ob = (int32_t)ob;
+        works[ob].c_base = 0;
+        works[ob].cbuf = 4;
+      }
+      for (int op = 0; op < d->nop; ++op) {
+        const ClassChain &ch = chains[d->op_class[op]];
+        const Contraction *C = e->contractions[ch.c[s].contr].get();
+        const Layout *A = get_layout(e, C->lay_a), *B = get_layout(e, C->lay_b),
+                     *O = get_layout(e, C->lay_out);
+        for (size_t ob = 0; ob < O->pk->flat.size(); ++ob)
+          for (int64_t t = C->task_start[ob]; t < C->task_start[ob + 1]; ++t)
+            works[ob].tasks.push_back({C, A, B, O, C->tasks[t].ab, C->tasks[t].bb,
+                                       ws_off[op][s - 1], d->off_R[op], 5, 1, d->wts[op]});
+      }
+    }
+    P->steps.emplace_back();
+    int rc = build_step(works, P->steps.back());
+    if (rc) return rc;
+    P->flops += P->steps.back().flops;
+    P->ntasks += P->steps.back().ntasks;
+  }
+  // ---- HDiag terms: out[l,r] += w * sum Ld[a,l] Wi[a,b] (Wj[b,c]) Rd[c,r]
+  {
+    int psec[16];
+    for (size_t ob = 0; ob < Psi->pk->flat.size(); ++ob) {
+      Psi->sectors(Psi->pk->flat[ob], psec);
+      DiagBlock db;
+      db.out_off = Psi->pk->off[ob];
+      db.dl = (int32_t)Psi->dim[0][psec[0]];
+      db.dr = (int32_t)Psi->dim[Psi->rank - 1][psec[Psi->rank - 1]];
+      db.t0 = (int32_t)P->dterms.size();
+      const int sl = psec[0], sr = psec[Psi->rank - 1];
+      const int n1 = psec[1], n2 = d->ncsite == 2 ? psec[2] : -1;
+      for (int op = 0; op < d->nop; ++op) {
+        int c = d->op_class[op];
+        const Layout *L = get_layout(e, d->lay_L[c]), *R = get_layout(e, d->lay_Rf[c]);
+        const Layout *Wi = get_layout(e, d->lay_Wi[c]);
+        const Layout *Wj = d->ncsite == 2 ? get_layout(e, d->lay_Wj[c]) : nullptr;
+        for (int sa = 0; sa < L->nsec[0]; ++sa) {
+          int ls[3] = {sa, sl, sl};
+          int32_t lb = L->pk->lookup[(size_t)L->ravel(ls)];
+          if (lb < 0) continue;
+          for (int sb = 0; sb < Wi->nsec[1]; ++sb) {
+            int ws1[4] = {sa, sb, n1, n1};
+            int32_t wib = Wi->pk->lookup[(size_t)Wi->ravel(ws1)];
+            if (wib < 0) continue;
+            int nsc = d->ncsite == 2 ? Wj->nsec[1] : 1;
+            for (int sc = 0; sc < nsc; ++sc) {
+              int32_t wjb = -1;
+              int rs0 = sb;
+              if (d->ncsite == 2) {
+                int ws2[4] = {sb, sc, n2, n2};
+                wjb = Wj->pk->lookup[(size_t)Wj->ravel(ws2)];
+                if (wjb < 0) continue;
+                rs0 = sc;
+              }
+              int rsec[3] = {rs0, sr, sr};
+              int32_t rb = R->pk->lookup[(size_t)R->ravel(rsec)];
+              if (rb < 0) continue;
+              DiagTerm t;
+              int64_t ld[3], rd[3], wid[4], wjd[4];
+              L->block_dims(lb, ld);
+              R->block_dims(rb, rd);
+              Wi->block_dims(wib, wid);
+              t.l_off = d->off_L[op] + L->pk->off[lb];
+              t.l_sa = ld[1] * ld[2];
+              t.l_sl = ld[2] + 1;
+              t.r_off = d->off_R[op] + R->pk->off[rb];
+              t.r_sc = rd[1] * rd[2];
+              t.r_sr = rd[2] + 1;
+              t.wi_off = d->off_Wi[op] + Wi->pk->off[wib];
+              t.wi_sa = wid[1];
+              t.wi_sb = 1;
+              t.da = (int32_t)ld[0];
+              t.db = (int32_t)wid[1];
+              if (d->ncsite == 2) {
+                Wj->block_dims(wjb, wjd);
+                t.wj_off = d->off_Wj[op] + Wj->pk->off[wjb];
+                t.wj_sb = wjd[1];
+                t.wj_sc = 1;
+                t.dc = (int32_t)wjd[1];
+              } else {
+                t.wj_off = 0;
+                t.wj_sb = t.wj_sc = 0;
+                t.dc = (int32_t)wid[1];
+              }
+              t.alpha = d->wts[op];
+              t.ncsite = d->ncsite;
+              P->dterms.push_back(t);
+            }
+          }
+        }
+      }
+      db.nt = (int32_t)P->dterms.size() - db.t0;
+      P->dblocks.push_back(db);
+    }
+    for (const auto &t : P->dterms) {
+      P->max_ac = std::max<int64_t>(P->max_ac, (int64_t)t.da * t.dc);
+    }
+    for (const auto &b : P->dblocks) {
+      int64_t mda = 0;
+      for (int i = 0; i < b.nt; ++i) mda = std::max<int64_t>(mda, P->dterms[b.t0 + i].da);
+      P->max_ar = std::max<int64_t>(P->max_ar, mda * b.dr);
+    }
+  }
+  e->plans.push_back(std::move(P));
+  *plan_id = (int)e->plans.size() - 1;
+  return ZMPO_OK;
+}
+
+int zmpo_sigma_workspace(zmpo_engine *e, int plan_id, int64_t *bytes) {
+  Plan *P = get_plan(e, plan_id, 0);
+  if (!P || !bytes) return fail(ZMPO_E_ID, "workspace: unknown plan");
+  *bytes = P->ws_elems * (int64_t)sizeof(double);
+  return ZMPO_OK;
+}
+
+int zmpo_plan_stats(zmpo_engine *e, int plan_id, double *flops, int64_t *ntasks, int *nlaunch) {
+  Plan *P = get_plan(e, plan_id, 0);
+  if (!P) return fail(ZMPO_E_ID, "plan_stats: unknown plan");
+  if (flops) *flops = P->flops;
+  if (ntasks) *ntasks = P->ntasks;
+  if (nlaunch) *nlaunch = (int)P->steps.size();
+  return ZMPO_OK;
+}
+
+int zmpo_sigma(zmpo_engine *e, int plan_id, const double *d_L, const double *d_R,
+               const double *d_W, const double *d_x, double *d_y, void *d_workspace,
+               int precision, void *stream) {
+  Plan *P = get_plan(e, plan_id, 2);
+  if (!P) return fail(ZMPO_E_ID, "sigma: unknown plan");
+  if (P->ws_elems > 0 && !d_workspace) return fail(ZMPO_E_ARG, "sigma: workspace required");
+  Bufs b{};
+  b.p[0] = const_cast<double *>(d_L);
+  b.p[1] = const_cast<double *>(d_R);
+  b.p[2] = const_cast<double *>(d_W);
+  b.p[3] = const_cast<double *>(d_x);
+  b.p[4] = d_y;
+  b.p[5] = (double *)d_workspace;
+  for (auto &s : P->steps) {
+    int rc = run_step(s, b, precision, stream);
+    if (rc) return rc;
+  }
+  return ZMPO_OK;
+}
+
+int zmpo_hdiag(zmpo_engine *e, int plan_id, const double *d_L, const double *d_R,
+               const double *d_W, double *d_diag, void *stream) {
+  Plan *P = get_plan(e, plan_id, 2);
+  if (!P) return fail(ZMPO_E_ID, "hdiag: unknown plan");
+  if (!P->diag_uploaded) {
+    if (!P->dblocks.empty()) {
+      CUDA_TRY(cudaMalloc((void **)&P->d_dblocks, P->dblocks.size() * sizeof(DiagBlock)));
+      CUDA_TRY(cudaMemcpy(P->d_dblocks, P->dblocks.data(), P->dblocks.size() * sizeof(DiagBlock),
+                          cudaMemcpyHostToDevice));
+    }
+    if (!P->dterms.empty()) {
+      CUDA_TRY(cudaMalloc((void **)&P->d_dterms, P->dterms.size() * sizeof(DiagTerm)));
+      CUDA_TRY(cudaMemcpy(P->d_dterms, P->dterms.data(), P->dterms.size() * sizeof(DiagTerm),
+                          cudaMemcpyHostToDevice));
+    }
+    std::vector<DiagTerm>().swap(P->dterms);
+    P->diag_uploaded = true;
+  }
+  Bufs b{};
+  b.p[0] = const_cast<double *>(d_L);
+  b.p[1] = const_cast<double *>(d_R);
+  b.p[2] = const_cast<double *>(d_W);
+  return launch_hdiag(P->d_dblocks, (int64_t)P->dblocks.size(), P->d_dterms, b, d_diag,
+                      (int)P->max_ac, (int)P->max_ar, stream);
+}
+
+int zmpo_renorm_plan(zmpo_engine *e, const zmpo_renorm_desc *d, int *plan_id) {
+  if (!e || !d || !plan_id || d->nop < 0 || d->nclass < 1 || (d->status != 0 && d->status != 1))
+    return fail(ZMPO_E_ARG, "renorm_plan: bad descriptor");
+  // reference chains (mpo_dmrg_kernelQt.py:665-667 for 'L', 727-729 for 'R')
+  static const int La1[1] = {0}, Lb1[1] = {1};
+  static const int La2[2] = {0, 2}, Lb2[2] = {2, 0};
+  static const int La3[2] = {1, 3}, Lb3[2] = {1, 0};
+  static const int Ra1[1] = {2}, Rb1[1] = {1};
+  static const int Ra2[2] = {1, 2}, Rb2[2] = {2, 1};
+  static const int Ra3[2] = {1, 3}, Rb3[2] = {1, 2};
+  struct Ch {
+    bool built = false;
+    int c1 = -1, c2 = -1, c3 = -1, l1 = -1, l2 = -1, l3 = -1;
+  };
+  std::vector<Ch> ch(d->nclass);
+  for (int op = 0; op < d->nop; ++op) {
+    int c = d->op_class[op];
+    if (c < 0 || c >= d->nclass) return fail(ZMPO_E_ARG, "renorm_plan: bad class");
+    if (ch[c].built) continue;
+    ch[c].built = true;
+    int rc;
+    if (d->status == 0) {
+      rc = build_contraction(e, d->lay_site, d->lay_env[c], 1, La1, Lb1, &ch[c].l1, &ch[c].c1);
+      if (rc) return rc;
+      rc = build_contraction(e, d->lay_W[c], ch[c].l1, 2, La2, Lb2, &ch[c].l2, &ch[c].c2);
+      if (rc) return rc;
+      rc = build_contraction(e, ch[c].l2, d->lay_site, 2, La3, Lb3, &ch[c].l3, &ch[c].c3);
+    } else {
+      rc = build_contraction(e, d->lay_site, d->lay_env[c], 1, Ra1, Rb1, &ch[c].l1, &ch[c].c1);
+      if (rc) return rc;
+      rc = build_contraction(e, d->lay_W[c], ch[c].l1, 2, Ra2, Rb2, &ch[c].l2, &ch[c].c2);
+      if (rc) return rc;
+      rc = build_contraction(e, ch[c].l2, d->lay_site, 2, Ra3, Rb3, &ch[c].l3, &ch[c].c3);
+    }
+    if (rc) return rc;
+  }
+  auto P = std::make_unique<Plan>();
+  P->kind = 3;
+  P->status = d->status;
+  P->out_lay.assign(d->nclass, -1);
+  P->out_off.assign(d->nop, -1);
+  for (int c = 0; c < d->nclass; ++c)
+    if (ch[c].built && get_layout(e, ch[c].l3)->pk->size > 0) P->out_lay[c] = ch[c].l3;
+  int64_t tot = 0, ws = 0;
+  std::vector<int64_t> w1(d->nop, 0), w2(d->nop, 0);
+  for (int op = 0; op < d->nop; ++op) {
+    int c = d->op_class[op];
+    if (P->out_lay[c] < 0) continue;
+    P->out_off[op] = tot;
+    tot += get_layout(e, ch[c].l3)->pk->size;
+    w1[op] = ws;
+    ws += get_layout(e, ch[c].l1)->pk->size;
+    ws = (ws + 31) & ~int64_t(31);
+    w2[op] = ws;
+    ws += get_layout(e, ch[c].l2)->pk->size;
+    ws = (ws + 31) & ~int64_t(31);
+  }
+  P->out_total = tot;
+  P->ws_elems = ws;
+  // buffers: 0 env, 2 W, 3 site, 4 out, 5 workspace
+  for (int s = 0; s < 3; ++s) {
+    std::vector<OutWork> works;
+    for (int op = 0; op < d->nop; ++op) {
+      int c = d->op_class[op];
+      if (P->out_lay[c] < 0) continue;
+      int ci = s == 0 ? ch[c].c1 : (s == 1 ? ch[c].c2 : ch[c].c3);
+      const Contraction *C = e->contractions[ci].get();
+      const Layout *A = get_layout(e, C->lay_a), *B = get_layout(e, C->lay_b),
+                   *O = get_layout(e, C->lay_out);
+      int abuf, bbuf, cbuf;
+      int64_t abase, bbase, cbase;
+      if (s == 0) {
+        abuf = 3; abase = 0; bbuf = 0; bbase = d->off_env[op]; cbuf = 5; cbase = w1[op];
+      } else if (s == 1) {
+        abuf = 2; abase = d->off_W[op]; bbuf = 5; bbase = w1[op]; cbuf = 5; cbase = w2[op];
+      } else {
+        abuf = 5; abase = w2[op]; bbuf = 3; bbase = 0; cbuf = 4; cbase = P->out_off[op];
+      }
+      for (size_t ob = 0; ob < O->pk->flat.size(); ++ob) {
+        OutWork w;
+        w.lo = O;
+        w.ob = (int32_t)ob;
+        w.c_base = cbase;
+        w.cbuf = cbuf;
+        for (int64_t t = C->task_start[ob]; t < C->task_start[ob + 1]; ++t)
+          w.tasks.push_back({C, A, B, O, C->tasks[t].ab, C->tasks[t].bb, abase, bbase, abuf, bbuf, 1.0});
+        works.push_back(std::move(w));
+      }
+    }
+    P->steps.emplace_back();
+    int rc = build_step(works, P->steps.back());
+    if (rc) return rc;
+    P->flops += P->steps.back().flops;
+    P->ntasks += P->steps.back().ntasks;
+  }
+  e->plans.push_back(std::move(P));
+  *plan_id = (int)e->plans.size() - 1;
+  return ZMPO_OK;
+}
+
+int zmpo_renorm_outputs(zmpo_engine *e, int plan_id, int *lay_out, int64_t *off_out, int64_t *total) {
+  Plan *P = get_plan(e, plan_id, 3);
+  if (!P) return fail(ZMPO_E_ID, "renorm_outputs: unknown plan");
+  if (lay_out)
+    for (size_t c = 0; c < P->out_lay.size(); ++c) lay_out[c] = P->out_lay[c];
+  if (off_out)
+    for (size_t i = 0; i < P->out_off.size(); ++i) off_out[i] = P->out_off[i];
+  if (total) *total = P->out_total;
+  return ZMPO_OK;
+}
+
+int zmpo_renorm_workspace(zmpo_engine *e, int plan_id, int64_t *bytes) {
+  return zmpo_sigma_workspace(e, plan_id, bytes);
+}
+
+int zmpo_renorm(zmpo_engine *e, int plan_id, const double *d_env, const double *d_W,
+                const double *d_site, double *d_out, void *d_workspace, int precision,
+                void *stream) {
+  Plan *P = get_plan(e, plan_id, 3);
+  if (!P) return fail(ZMPO_E_ID, "renorm: unknown plan");
+  if (P->ws_elems > 0 && !d_workspace) return fail(ZMPO_E_ARG, "renorm: workspace required");
+  Bufs b{};
+  b.p[0] = const_cast<double *>(d_env);
+  b.p[2] = const_cast<double *>(d_W);
+  b.p[3] = const_cast<double *>(d_site);
+  b.p[4] = d_out;
+  b.p[5] = (double *)d_workspace;
+  for (auto &s : P->steps) {
+    int rc = run_step(s, b, precision, stream);
+    if (rc) return rc;
+  }
+  return ZMPO_OK;
+}
+
+int zmpo_plan_destroy(zmpo_engine *e, int plan_id) {
+  Plan *P = get_plan(e, plan_id, 0);
+  if (!P) return fail(ZMPO_E_ID, "plan_destroy: unknown plan");
+  for (auto &s : P->steps) free_step(s);
+  cudaFree(P->d_dblocks);
+  cudaFree(P->d_dterms);
+  e->plans[plan_id].reset();
+  return ZMPO_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,177 @@
+"""Python handle on the GB300 engine: layouts, plans and device launches.
+
+Device memory is owned by torch tensors; the engine receives raw pointers and
+the current CUDA stream.  Only block structure (layouts, task lists) lives in
+the engine.
+"""
+import ctypes
+
+import numpy
+
+from . import _lib
+from ._lib import check, as_i32, as_i64, as_f64, iptr, lptr, dptr
+
+_ENGINES = {}
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def device_ptr(t):
+    """Raw device pointer of a contiguous float64 torch tensor."""
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise RuntimeError("engine buffers must be CUDA tensors")
+    if t.dtype != _torch().float64 or not t.is_contiguous():
+        raise RuntimeError("engine buffers must be contiguous float64")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def current_stream():
+    torch = _torch()
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class Engine:
+    def __init__(self, device=0):
+        self.device = device
+        h = ctypes.c_void_p()
+        check(_lib.lib().zmpo_engine_create(ctypes.byref(h), device), "engine_create")
+        self.h = h
+        self._layout_cache = {}
+
+    def __del__(self):
+        try:
+            if self.h:
+                _lib.lib().zmpo_engine_destroy(self.h)
+        except Exception:
+            pass
+
+    # ----------------------------------------------------------- layouts
+    def layout(self, qsyms, ndims, status):
+        """Layout id of a block-sparse tensor (cached on its structure)."""
+        rank = len(qsyms)
+        nq = int(numpy.asarray(qsyms[0]).reshape(len(ndims[0]), -1).shape[1]) if rank else 1
+        q = [as_f64(numpy.asarray(x, dtype=float).reshape(len(d), nq)) for x, d in zip(qsyms, ndims)]
+        key = (tuple(x.tobytes() for x in q), tuple(tuple(int(v) for v in d) for d in ndims),
+               tuple(int(bool(s)) for s in status))
+        lid = self._layout_cache.get(key)
+        if lid is not None:
+            return lid
+        nsec = as_i32([len(d) for d in ndims])
+        qcat = as_f64(numpy.concatenate([x.reshape(-1) for x in q]) if rank else numpy.zeros(1))
+        dcat = as_i64(numpy.concatenate([numpy.asarray(d, dtype=numpy.int64) for d in ndims])
+                      if rank else numpy.zeros(1))
+        st = as_i32([1 if s else 0 for s in status] or [0])
+        out = ctypes.c_int()
+        check(_lib.lib().zmpo_layout_create(self.h, rank, nq, iptr(nsec), dptr(qcat), lptr(dcat),
+                                            iptr(st), ctypes.byref(out)), "layout_create")
+        self._layout_cache[key] = out.value
+        return out.value
+
+    def derive(self, src, qsyms, status):
+        q = as_f64(numpy.concatenate([numpy.asarray(x, dtype=float).reshape(-1) for x in qsyms]))
+        st = as_i32([1 if s else 0 for s in status])
+        out = ctypes.c_int()
+        check(_lib.lib().zmpo_layout_derive(self.h, src, dptr(q), iptr(st), ctypes.byref(out)),
+              "layout_derive")
+        return out.value
+
+    def layout_blocks(self, lid):
+        size = ctypes.c_int64()
+        nb = ctypes.c_int64()
+        rank = ctypes.c_int()
+        check(_lib.lib().zmpo_layout_info(self.h, lid, ctypes.byref(size), ctypes.byref(nb),
+                                          ctypes.byref(rank)), "layout_info")
+        flat = numpy.zeros(max(nb.value, 1), dtype=numpy.int64)
+        off = numpy.zeros(max(nb.value, 1), dtype=numpy.int64)
+        check(_lib.lib().zmpo_layout_blocks(self.h, lid, lptr(flat), lptr(off)), "layout_blocks")
+        return int(size.value), flat[:nb.value], off[:nb.value]
+
+    # ---------------------------------------------------------- contraction
+    def contract_plan(self, lay_a, lay_b, axes):
+        ax1 = as_i32(list(axes[0]) or [0])
+        ax2 = as_i32(list(axes[1]) or [0])
+        lo = ctypes.c_int()
+        pid = ctypes.c_int()
+        check(_lib.lib().zmpo_contract_plan(self.h, lay_a, lay_b, len(axes[0]), iptr(ax1), iptr(ax2),
+                                            ctypes.byref(lo), ctypes.byref(pid)), "contract_plan")
+        return lo.value, pid.value
+
+    def contract_exec(self, pid, a, b, out, precision="fp64"):
+        check(_lib.lib().zmpo_contract_exec(self.h, pid, device_ptr(a), device_ptr(b), device_ptr(out),
+                                            _lib.PREC[precision], current_stream()), "contract_exec")
+
+    def plan_stats(self, pid):
+        fl = ctypes.c_double()
+        nt = ctypes.c_int64()
+        nl = ctypes.c_int()
+        check(_lib.lib().zmpo_plan_stats(self.h, pid, ctypes.byref(fl), ctypes.byref(nt),
+                                         ctypes.byref(nl)), "plan_stats")
+        return fl.value, nt.value, nl.value
+
+    def destroy_plan(self, pid):
+        check(_lib.lib().zmpo_plan_destroy(self.h, pid), "plan_destroy")
+
+    # --------------------------------------------------------------- sigma
+    def sigma_plan(self, ncsite, op_class, lay_L, lay_Wi, lay_Wj, lay_Rf, lay_psi, off_L, off_R,
+                   off_Wi, off_Wj, wts):
+        keep = dict(op_class=as_i32(op_class), lay_L=as_i32(lay_L), lay_Wi=as_i32(lay_Wi),
+                    lay_Wj=as_i32(lay_Wj if lay_Wj is not None else lay_Wi), lay_Rf=as_i32(lay_Rf),
+                    off_L=as_i64(off_L), off_R=as_i64(off_R), off_Wi=as_i64(off_Wi),
+                    off_Wj=as_i64(off_Wj if off_Wj is not None else off_Wi), wts=as_f64(wts))
+        d = _lib.SigmaDesc(ncsite, len(op_class), len(lay_L), iptr(keep["op_class"]),
+                           iptr(keep["lay_L"]), iptr(keep["lay_Wi"]), iptr(keep["lay_Wj"]),
+                           iptr(keep["lay_Rf"]), lay_psi, lptr(keep["off_L"]), lptr(keep["off_R"]),
+                           lptr(keep["off_Wi"]), lptr(keep["off_Wj"]), dptr(keep["wts"]))
+        pid = ctypes.c_int()
+        check(_lib.lib().zmpo_sigma_plan(self.h, ctypes.byref(d), ctypes.byref(pid)), "sigma_plan")
+        ws = ctypes.c_int64()
+        check(_lib.lib().zmpo_sigma_workspace(self.h, pid.value, ctypes.byref(ws)), "sigma_workspace")
+        return pid.value, ws.value
+
+    def sigma(self, pid, L, R, W, x, y, workspace, precision="fp64"):
+        check(_lib.lib().zmpo_sigma(self.h, pid, device_ptr(L), device_ptr(R), device_ptr(W),
+                                    device_ptr(x), device_ptr(y),
+                                    device_ptr(workspace) if workspace is not None else None,
+                                    _lib.PREC[precision], current_stream()), "sigma")
+
+    def hdiag(self, pid, L, R, W, diag):
+        check(_lib.lib().zmpo_hdiag(self.h, pid, device_ptr(L), device_ptr(R), device_ptr(W),
+                                    device_ptr(diag), current_stream()), "hdiag")
+
+    # -------------------------------------------------------------- renorm
+    def renorm_plan(self, status, op_class, lay_env, lay_W, lay_site, off_env, off_W):
+        keep = dict(op_class=as_i32(op_class), lay_env=as_i32(lay_env), lay_W=as_i32(lay_W),
+                    off_env=as_i64(off_env), off_W=as_i64(off_W))
+        d = _lib.RenormDesc(0 if status == 'L' else 1, len(op_class), len(lay_env),
+                            iptr(keep["op_class"]), iptr(keep["lay_env"]), iptr(keep["lay_W"]),
+                            lay_site, lptr(keep["off_env"]), lptr(keep["off_W"]))
+        pid = ctypes.c_int()
+        check(_lib.lib().zmpo_renorm_plan(self.h, ctypes.byref(d), ctypes.byref(pid)), "renorm_plan")
+        lay_out = numpy.zeros(len(lay_env), dtype=numpy.int32)
+        off_out = numpy.zeros(len(op_class), dtype=numpy.int64)
+        tot = ctypes.c_int64()
+        check(_lib.lib().zmpo_renorm_outputs(self.h, pid.value, iptr(lay_out), lptr(off_out),
+                                             ctypes.byref(tot)), "renorm_outputs")
+        ws = ctypes.c_int64()
+        check(_lib.lib().zmpo_renorm_workspace(self.h, pid.value, ctypes.byref(ws)), "renorm_ws")
+        return pid.value, lay_out, off_out, tot.value, ws.value
+
+    def renorm(self, pid, env, W, site, out, workspace, precision="fp64"):
+        check(_lib.lib().zmpo_renorm(self.h, pid, device_ptr(env), device_ptr(W), device_ptr(site),
+                                     device_ptr(out),
+                                     device_ptr(workspace) if workspace is not None else None,
+                                     _lib.PREC[precision], current_stream()), "renorm")
+
+
+def get(device=0):
+    """Process-wide engine for ``device``."""
+    eng = _ENGINES.get(device)
+    if eng is None:
+        eng = Engine(device)
+        _ENGINES[device] = eng
+    return eng

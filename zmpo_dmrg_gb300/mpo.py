@@ -1,0 +1,168 @@
+"""MPO site tensors of H = sum_p a_p^+ V_p for the engine.
+
+The bond-index layout is the reference's MPO format (it fixes the structure
+of every environment, so it has to be the same): spin-orbital site ``k`` of
+``nsite`` spin orbitals carries a bond of dimension 2(nsite+1) ordered as
+``mpo_dmrg_opers.genWfacSpin`` (source/mpo_dmrg_opers.py:91-194) orders it;
+H_p = a_p^+ V_p (``genHfacSpin`` 197-203); a spatial site joins spin sites
+(2i, 2i+1) (``linkTwoOpers`` 43-49); spin projection multiplies the ket leg by
+exp(-i theta S_y) (``genHRfacSpatial`` 253-260).  The block-sparse form sorts
+the bond quantum numbers and collects equal ones into sectors, with physical
+legs uncollected (``qtensor_opers.genHRfacSpatialQt`` 358-408); the bond
+order inside a sector is ascending in the (N, Sz) label.
+"""
+import math
+
+import numpy
+
+from .qtensor import qtensor
+
+# local 2x2 operators on [|0>, |1>] of one spin orbital
+_I = numpy.eye(2)
+_Z = numpy.diag([1.0, -1.0])      # Jordan-Wigner sign (also the "idnt" string)
+_C = numpy.array([[0.0, 0.0], [1.0, 0.0]])   # creation
+_A = numpy.array([[0.0, 1.0], [0.0, 0.0]])   # annihilation
+_N = numpy.array([[0.0, 0.0], [0.0, 1.0]])   # number
+
+
+def spin_site(nsite, k, h, v):
+    """V_p MPO on spin orbital ``k``: ``h[q]`` = h_pq, ``v[q,r,s]`` = V_pqrs."""
+    nl = 1 if k == 0 else 2 * (nsite + 1)
+    nr = 1 if k == nsite - 1 else 2 * (nsite + 1)
+    W = numpy.zeros((nl, nr, 2, 2))
+    L = k                 # spin orbitals left of k
+    R = nsite - k - 1     # spin orbitals right of k
+    right = numpy.arange(k + 1, nsite)
+    left = numpy.arange(k)
+    last = nr - 1
+    if k == nsite - 1:
+        W[0, 0] = h[k] * _A
+        W[1, 0] = _C
+        W[2, 0] = _A
+        W[3 + left, 0] = v[k, left, k][:, None, None] * _N
+        W[nl - 1, 0] = _I
+        return W
+    # first row: string, V(k,k,r) n_k, -a_k, a+_k, h_k a_k
+    W[0, 0] = _Z
+    W[0, 1 + R + numpy.arange(R)] = v[k, k, right][:, None, None] * (-_N)
+    W[0, 1 + 2 * R + L] = -_A
+    W[0, 2 + 2 * R + 2 * L] = _C
+    W[0, last] = h[k] * _A
+    if k == 0:
+        return W
+    W[1, last] = _C
+    W[2 + numpy.arange(R), 1 + numpy.arange(R)] = _Z
+    W[2 + R, last] = _A
+    W[3 + R + numpy.arange(R), 1 + R + numpy.arange(R)] = _Z
+    o6 = 3 + 2 * R
+    for li in range(L):
+        W[o6 + li, 1 + numpy.arange(R)] = -v[right, li, k][:, None, None] * (-_A)
+        W[o6 + li, 1 + R + numpy.arange(R)] = v[k, li, right][:, None, None] * _C
+        W[o6 + li, 1 + 2 * R + li] = _I
+        W[o6 + li, last] = v[k, li, k] * _N
+    o7 = 3 + 2 * R + L
+    for li in range(L):
+        W[o7 + li, 1 + R + numpy.arange(R)] = v[li, k, right][:, None, None] * (-_A)
+        W[o7 + li, 2 + 2 * R + L + li] = _I
+    W[nl - 1, last] = _I
+    return W
+
+
+def _elem(p, k):
+    if k < p:
+        return _Z
+    return _C if k == p else _I
+
+
+def hp_spin_site(p, nsite, k, h, v):
+    """a_p^+ V_p on spin orbital k: the local a_p^+ factor acts after V_p."""
+    W = spin_site(nsite, k, h, v)
+    return numpy.einsum('ij,abjk->abik', _elem(p, k), W)
+
+
+def link(W1, W2):
+    """Join two sites: [a,b,i,j] x [b,c,k,l] -> [a,c,(ik),(jl)]."""
+    t = numpy.einsum('abij,bckl->acikjl', W1, W2)
+    s = t.shape
+    return t.reshape(s[0], s[1], s[2] * s[3], s[4] * s[5])
+
+
+def ry_matrix(phi):
+    """exp(-i phi S_y) on the spatial basis [0, b, a, ab]."""
+    m = numpy.eye(4)
+    c, s = math.cos(0.5 * phi), math.sin(0.5 * phi)
+    m[1, 1], m[1, 2], m[2, 1], m[2, 2] = c, s, -s, c
+    return m
+
+
+def hp_spatial_site(pindx, nspin, isite, int1e, int2e, qpts=None, pdic=None):
+    p, ipt = pindx
+    idx = p if pdic is None else pdic[p]
+    W = link(hp_spin_site(p, nspin, 2 * isite, int1e[idx], int2e[idx]),
+             hp_spin_site(p, nspin, 2 * isite + 1, int1e[idx], int2e[idx]))
+    if ipt is not None:
+        W = numpy.einsum('abij,jk->abik', W, ry_matrix(qpts[ipt]))
+    return W
+
+
+# --------------------------------------------------------- quantum numbers
+_SPIN = (0.5, -0.5)
+
+
+def _bond_right(nsite, k, sz):
+    """(N, Sz) labels of the right bond of spin orbital k for V_p with
+    Sz(p) = sz (qtensor_opers.genWfacSpinQnumsRight, qtensor_opers.py:161)."""
+    q = [[0.0, 0.0]]
+    q += [[-2.0, -sz - _SPIN[i % 2]] for i in range(k + 1, nsite)]
+    q += [[0.0, -sz + _SPIN[i % 2]] for i in range(k + 1, nsite)]
+    q += [[-1.0, -_SPIN[i % 2]] for i in range(k + 1)]
+    q += [[1.0, _SPIN[i % 2]] for i in range(k + 1)]
+    q += [[-1.0, -sz]]
+    return numpy.array(q)
+
+
+def _elem_q(p, k):
+    """Label change of the a_p^+ factor across spin orbital k."""
+    d = numpy.array([1.0, _SPIN[p % 2]])
+    left = d if k > p else numpy.zeros(2)
+    right = d if k >= p else numpy.zeros(2)
+    return left, right
+
+
+def spatial_bond_qnums(p, nspin, isite):
+    """Left / right bond labels of H_p at spatial site ``isite``."""
+    sz = _SPIN[p % 2]
+    k0, k1 = 2 * isite, 2 * isite + 1
+    ql = numpy.zeros((1, 2)) if k0 == 0 else _bond_right(nspin, k0 - 1, sz)
+    qr = numpy.array([[-1.0, -sz]]) if k1 == nspin - 1 else _bond_right(nspin, k1, sz)
+    el, _ = _elem_q(p, k0)
+    _, er = _elem_q(p, k1)
+    return ql + el, qr + er
+
+
+def hp_spatial_qt(pindx, nspin, isite, int1e, int2e, qpts=None, pdic=None):
+    """Block-sparse site tensor of H_p with bond sectors collected."""
+    W = hp_spatial_site(pindx, nspin, isite, int1e, int2e, qpts, pdic)
+    ql, qr = spatial_bond_qnums(pindx[0], nspin, isite)
+    qphys = numpy.array([[0.0, 0.0], [1.0, -0.5], [1.0, 0.5], [2.0, 0.0]])
+    if pindx[1] is not None:
+        ql, qr, qphys = ql[:, :1], qr[:, :1], qphys[:, :1]
+    il = numpy.lexsort(ql.T[::-1])
+    ir = numpy.lexsort(qr.T[::-1])
+    W = W[numpy.ix_(il, ir)]
+    qt = qtensor([False, True, False, True])
+    qt.fromDenseTensor(W, [ql[il], qr[ir], qphys, qphys], ifcollect=[1, 1, 0, 0])
+    return qt
+
+
+def op_class(p, isite, ncsite=1):
+    """Layout class of H_p relative to the dot (qtensor_opers.case, qtensor_opers.py:72)."""
+    i = p // 2
+    odd = p % 2
+    if i < isite:
+        return odd
+    if i == isite:
+        return 2 + odd
+    if ncsite == 1 or i == isite + 1:
+        return 4 + odd
+    return 6 + odd

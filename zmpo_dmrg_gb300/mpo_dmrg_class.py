@@ -1,0 +1,534 @@
+"""DMRG driver object with the reference's API, running the hot path on the GPU.
+
+Interface of ``source/mpo_dmrg_class.py`` (``mpo_dmrg``: attributes 47-192,
+``partition`` 206, ``loadInts`` 249, ``dumpMPO`` 254, ``build`` 279,
+``initStates`` 299, ``default`` 329, ``checkMPS`` 470) together with the sweep
+of ``mpo_dmrg_opt.py`` (``sweep`` 31, ``checkOpers`` 153, ``updateSite`` 313,
+``updateBoundary`` 347), the local solver of ``mpo_dmrg_dot.ci_solver`` 24 and
+the decimation / guess of ``mpo_dmrg_dotutil.py`` (288-559).
+
+GB300 design: the MPO, every environment L_p / R_p of every operator term and
+the Davidson basis live in device memory (no files, no MPI); H.psi, diag(H) and
+the renormalisation are engine launches over all terms at once; the density
+matrix decimation and the guess run on the host (they are O(D^3) once per
+site).  Storage is always block-sparse (the reference's "Qt" form).
+Engine options on the object: ``precision`` ('fp64', 'split' or 'emu64') for
+the sigma vector, ``precision_renorm`` for the environments.
+"""
+import copy
+import time
+
+import numpy
+
+from . import mpo as _mpo
+from . import pdvdson
+from .mpo_dmrg_kernel import EnvSet, MPOStore, HVec, HDiag, renorm
+from .qtensor import qtensor, fromQnums
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def vacuum(isym=2):
+    return [[0.]] if isym == 1 else [[0., 0.]]
+
+
+def dpt(q1, q2):
+    """Labels of a direct product, first index slowest (mpo_dmrg_qphys.dpt)."""
+    a = numpy.asarray(q1, dtype=float)
+    b = numpy.asarray(q2, dtype=float)
+    return (a[:, None, :] + b[None, :, :]).reshape(-1, a.shape[1])
+
+
+def init_spatial_orb(norb, isym=2):
+    q = numpy.array([[0., 0.], [1., -0.5], [1., 0.5], [2., 0.]])
+    if isym == 1:
+        q = q[:, :1]
+    return [q.copy() for _ in range(norb)]
+
+
+def rdm_blkdiag(rho0, classes, thresh, Dcut=-1):
+    """Block eigen-decomposition of the reduced density matrix by sector and
+    truncation (mpo_dmrg_qparser.rdm_blkdiag, mpo_dmrg_qparser.py:106-183)."""
+    import scipy.linalg
+    cls = numpy.asarray(classes, dtype=float)
+    keys, first, inv = numpy.unique(cls, axis=0, return_index=True, return_inverse=True)
+    inv = inv.reshape(-1)
+    order = numpy.argsort(first, kind="stable")
+    nrows = rho0.shape[0]
+    qsymL, cols, sigs = [], [], []
+    for k in order:
+        rows = numpy.flatnonzero(inv == k)
+        s2, u = scipy.linalg.eigh(rho0[numpy.ix_(rows, rows)])
+        s2 = numpy.abs(s2)
+        ucol = numpy.zeros((nrows, len(rows)))
+        ucol[rows, :] = u
+        cols.append(ucol)
+        sigs.append(s2)
+        qsymL += [list(keys[k])] * len(rows)
+    rotL = numpy.hstack(cols)
+    sigs = numpy.hstack(sigs)
+    sigs = sigs / numpy.sum(sigs)
+    indx = numpy.argsort(sigs, kind="stable")[::-1]
+    nres = len(sigs)
+    ts = sigs[indx]
+    below = numpy.flatnonzero(ts < thresh * 1.01)
+    if below.size:
+        nres = int(below[0])
+    nres = max(nres, 1)
+    if Dcut > 0:
+        nres = min(nres, Dcut)
+    indx = indx[:nres]
+    sigs = sigs[indx]
+    dwts = 1.0 - numpy.sum(sigs)
+    qsymL = [qsymL[i] for i in indx]
+    rotL = rotL[:, indx]
+    o = sorted(range(nres), key=lambda x: qsymL[x])
+    return dwts, numpy.array([qsymL[i] for i in o]), rotL[:, o].copy(), sigs[o].copy()
+
+
+class mpo_dmrg:
+    def __init__(self, seed=0):
+        self.iprt = 0
+        self.nsite = None
+        self.sbas = None
+        self.occun = None
+        self.crit_vec = 1.e-8
+        self.thresh = -1.e-14
+        self.ifdvdnz = True
+        self.Dcut = None
+        self.Dmax = None
+        self.crit_e = 1.e-10
+        self.noise = 1.e-4
+        self.inoise = 0
+        self.ifprecond = True
+        self.ifguess = True
+        self.psi0 = None
+        self.ncsite = None
+        self.status = None
+        self.isym = 2
+        self.qphys = None
+        self.dphys = None
+        self.qnuml = None
+        self.qnumr = None
+        self.nelec = 0.0
+        self.sz = 0.0
+        self.neig = None
+        self.wts = None
+        self.qsectors = None
+        self.const = 0.0
+        self.ifs2proj = False
+        self.npts = None
+        self.qwts = None
+        self.qpts = None
+        self.opers = []
+        self.nops = None
+        self.ifQt = True
+        self.qkey = None
+        self.qlst = None
+        self.qtmp = None
+        self.idlstCI = None
+        self.maxslc = 1
+        self.int1e = None
+        self.int2e = None
+        self.hpwts = None
+        # engine options
+        self.precision = "fp64"
+        self.precision_renorm = "fp64"
+        self.rng = numpy.random.default_rng(seed)
+        # device state
+        self.mpo_store = None
+        self.envs = {}
+        self.flmps = {}
+        self.frmps = {}
+        self.nmvp = []
+        self.eav = []
+        self.dwt = []
+        self.esweeps = []
+        self.timings = []
+
+    # ------------------------------------------------------------ set-up
+    def build(self):
+        if self.nsite < 2:
+            raise ValueError('mps is not supported for nsite < 2')
+        assert self.isym in (1, 2)
+        self.qphys = init_spatial_orb(self.nsite, self.isym)
+        self.dphys = [len(x) for x in self.qphys]
+        self.qnuml = [None] * (self.nsite + 1)
+        self.qnuml[0] = numpy.array(vacuum(self.isym))
+        self.qnumr = [None] * (self.nsite + 1)
+        self.qnumr[-1] = numpy.array(vacuum(self.isym))
+        return 0
+
+    def s2quad(self, sval=0, sz=0):
+        from .spinproj import s2quad
+        s2quad(self, sval, sz)
+        return 0
+
+    def partition(self):
+        if self.sbas is None:
+            raise ValueError('sbas is not defined')
+        if self.npts is None:
+            self.opers = [[x, None] for x in range(self.sbas)]
+            self.hpwts = numpy.ones(self.sbas)
+        else:
+            self.opers = [[x // self.npts, x % self.npts] for x in range(self.npts * self.sbas)]
+            self.hpwts = numpy.array([self.qwts[x[1]] for x in self.opers])
+        self.nops = len(self.opers)
+        self.pidx = sorted(set(x[0] for x in self.opers))
+        self.pdic = dict((p, i) for i, p in enumerate(self.pidx))
+        return 0
+
+    def loadInts(self, mol):
+        """``mol`` carries spin-orbital ``int1e`` [p,q] and ``int2e`` [p,q,r,s]
+        = V_pqrs (the arrays the reference reads from mole.h5), or is the pair."""
+        if isinstance(mol, (tuple, list)):
+            int1e, int2e = mol
+        else:
+            int1e, int2e = mol.int1e, mol.int2e
+        self.int1e = numpy.asarray(int1e)[self.pidx]
+        self.int2e = numpy.asarray(int2e)[self.pidx]
+        return 0
+
+    def dumpMPO(self):
+        """Build every W_p(i) in block-sparse form and upload them at once."""
+        torch = _torch()
+        tens = [[None] * self.nops for _ in range(self.nsite)]
+        off = numpy.zeros((self.nsite, self.nops), dtype=numpy.int64)
+        vals = []
+        pos = 0
+        for isite in range(self.nsite):
+            for iop in range(self.nops):
+                t = _mpo.hp_spatial_qt(self.opers[iop], self.sbas, isite, self.int1e, self.int2e,
+                                       self.qpts, self.pdic)
+                tens[isite][iop] = t
+                off[isite, iop] = pos
+                vals.append(t.value)
+                pos += t.size_allowed
+        buf = torch.from_numpy(numpy.concatenate(vals)).cuda()
+        self.mpo_store = MPOStore(buf, off, tens)
+        return 0
+
+    def initStates(self):
+        if self.qsectors is None:
+            if self.neig is None:
+                raise ValueError('no state is specified')
+            key = str([self.nelec]) if self.isym == 1 else str([self.nelec, self.sz])
+            self.qsectors = {key: self.neig}
+        self.neig = sum(self.qsectors.values())
+        if self.wts is None:
+            self.wts = numpy.ones(self.neig) / float(self.neig)
+        return 0
+
+    # ------------------------------------------------------- environments
+    def boundary_env(self):
+        """Environment of the empty block: 1 for every term
+        (mpo_dmrg_initQt.genBopsQt, mpo_dmrg_initQt.py:49-85)."""
+        torch = _torch()
+        q = [[0.]] if (self.isym == 1 or self.ifs2proj) else [[0., 0.]]
+        t = qtensor([True, False, True])
+        t.fromQsyms(3, [q, q, q], [[1], [1], [1]], ifallocate=False)
+        buf = torch.ones(self.nops, dtype=torch.float64, device="cuda")
+        return EnvSet(buf, numpy.arange(self.nops, dtype=numpy.int64),
+                      numpy.full(self.nops, t.layout, dtype=numpy.int64), [t] * self.nops)
+
+    def site_qt(self, isite, dense, qnums, status):
+        t = qtensor(status)
+        t.fromDenseTensor(dense, qnums)
+        return t
+
+    def product_mps(self):
+        """Left-canonical product state from ``occun`` (mpo_dmrg_util.mps0occun,
+        mpo_dmrg_util.py:118-155) in block-sparse form."""
+        nsite = self.nsite
+        fmps = {'nsite': nsite}
+        qn = [numpy.array([[0., 0.]])]
+        ne, ms = 0.0, 0.0
+        for i in range(nsite):
+            na, nb = self.occun[2 * i], self.occun[2 * i + 1]
+            idx = int(round(na)) * 2 + int(round(nb))
+            ne += round(na) + round(nb)
+            ms += 0.5 * (round(na) - round(nb))
+            site = numpy.zeros((1, 4, 1))
+            site[0, idx, 0] = 1.0
+            qn.append(numpy.array([[ne, ms]]))
+            fmps['site%d' % i] = self.site_qt(i, site, [qn[i], self.qphys[i], qn[i + 1]],
+                                              [False, False, True])
+        for i in range(nsite + 1):
+            fmps['qnum%d' % i] = qn[i]
+        return fmps
+
+    def genHops(self, fmps, kind='lop'):
+        """All left (or right) environments of an MPS and <H_p> at the end."""
+        nsite = self.nsite
+        if kind == 'lop':
+            self.envs[('lop', -1)] = self.boundary_env()
+            order = range(nsite)
+        else:
+            self.envs[('rop', nsite)] = self.boundary_env()
+            order = range(nsite - 1, -1, -1)
+        for isite in order:
+            site = fmps['site%d' % isite]
+            if kind == 'lop':
+                flst = [[self.envs[('lop', isite - 1)], None]]
+            else:
+                flst = [[None, self.envs[('rop', isite + 1)]]]
+            fN = [[None]]
+            renorm(self, isite, 1, flst, fN, site, 'L' if kind == 'lop' else 'R')
+            self.envs[(kind, isite)] = fN[0][0]
+        last = self.envs[(kind, nsite - 1 if kind == 'lop' else 0)]
+        vals = last.buf.cpu().numpy()
+        exphop = numpy.zeros(self.nops)
+        for iop in range(self.nops):
+            if last.off[iop] >= 0:
+                exphop[iop] = vals[last.off[iop]]
+        return exphop
+
+    def initOps(self, fmps):
+        self.envs[('rop', self.nsite)] = self.boundary_env()
+        self.genHops(fmps, 'lop')
+        return 0
+
+    def checkMPS(self, fbra=None):
+        """Energy sum_p w_p <H_p> of the left-canonical MPS (checkMPS 470-558)."""
+        fmps = self.flmps if fbra is None else fbra
+        exphop = self.genHops(fmps, 'lop')
+        esum = float(numpy.dot(self.hpwts, exphop))
+        return esum, esum, 1.0, None
+
+    # ----------------------------------------------------------- local solver
+    def _qlst(self, isite, ncsite):
+        q = [numpy.asarray(self.qnuml[isite]), self.qphys[isite]]
+        if ncsite == 2:
+            q.append(self.qphys[isite + 1])
+        q.append(numpy.asarray(self.qnumr[isite + ncsite]))
+        return q
+
+    def setupQtmpCI(self, ncsite, key):
+        self.qkey = numpy.array(key, dtype=float)
+        qn = list(self.qlst[:-1]) + [self.qkey - self.qlst[-1]]
+        self.qtmp = qtensor([False] * (len(qn) - 1) + [True])
+        rank, qsyms, ndims, idlst = fromQnums(qn)
+        self.qtmp.fromQsyms(rank, qsyms, ndims, ifallocate=False)
+        self.idlstCI = idlst
+        self.qtmp_psi_layout = self.qtmp.layout
+        return 0
+
+    def ci_solver(self, isite, ncsite, actlst, flst, status, ifsym=True):
+        torch = _torch()
+        cdim = self.dphys[isite] * (self.dphys[isite + 1] if ncsite == 2 else 1)
+        ldim = len(self.qnuml[isite])
+        rdim = len(self.qnumr[isite + ncsite])
+        ndim = ldim * cdim * rdim
+        self.dims = (ldim, cdim, rdim, ndim)
+        self.qlst = self._qlst(isite, ncsite)
+        info = [self, isite, ncsite, flst, status, ifsym]
+        ioff = 0
+        eigs, civecs = [], []
+        nmvps = 0
+        for qkey in self.qsectors:
+            neig = self.qsectors[qkey]
+            key = [float(x) for x in eval(qkey)]
+            self.setupQtmpCI(ncsite, key)
+            prjmap = self.qtmp.prjmap(self.idlstCI)
+            ndim0 = self.qtmp.size_allowed
+            if ndim0 == 0:
+                raise RuntimeError('no basis in symmetry sector %s' % qkey)
+            if self.ifprecond:
+                diag = HDiag(info, ndim0, prjmap)
+            else:
+                diag = torch.ones(ndim0, dtype=torch.float64, device="cuda")
+            solver = pdvdson.eigenSolver(self.rng)
+            solver.HVec = pdvdson.mask([info, ndim0, prjmap], HVec).matvec
+            solver.crit_e = self.crit_e
+            solver.crit_vec = self.crit_vec
+            solver.ndim = ndim0
+            solver.neig = neig
+            solver.diag = diag
+            solver.noise = self.ifdvdnz and (self.noise > 1.e-10)
+            v0 = None
+            if self.psi0 is not None:
+                v0 = self.psi0[ioff:ioff + neig][:, prjmap].copy()
+            eig, vec, nmvp = solver.solve_iter(v0=v0, iop=4)
+            civec = numpy.zeros((neig, ndim))
+            civec[:, prjmap] = vec.cpu().numpy()
+            civecs.append(civec)
+            eigs += list(eig)
+            nmvps += nmvp
+            ioff += neig
+        civecs = numpy.vstack(civecs)
+        eigs = numpy.array(eigs)
+        sigs, dwts, qred, site, srotR = self.decimation(civecs, info)
+        if self.ifguess:
+            self.genGuess(isite, ncsite, actlst, civecs, srotR, status)
+        return nmvps, eigs, sigs, dwts, qred, site, srotR
+
+    def decimation(self, civecs, info):
+        dmrg, isite, ncsite, flst, status, ifsym = info
+        ldim, cdim, rdim, ndim = self.dims
+        neig = civecs.shape[0]
+        if status == 'L':
+            dim = self.dphys[isite]
+            cdimc = cdim // dim
+            lcdim, crdim = ldim * dim, cdimc * rdim
+        else:
+            jsite = isite + ncsite - 1
+            dim = self.dphys[jsite]
+            cdimc = cdim // dim
+            lcdim, crdim = ldim * cdimc, dim * rdim
+        if self.noise >= 1.e-10:
+            if self.inoise == 1:
+                civecs = civecs + self.rng.uniform(-1, 1, size=civecs.shape) * 10.0 * self.noise
+            else:
+                raise NotImplementedError(
+                    "perturbative (pRDM) noise is not available in this engine; use a schedule "
+                    "with zero noise or inoise = 1")
+        mats = civecs.reshape(neig, lcdim, crdim)
+        if status == 'L':
+            rdm1 = numpy.einsum('eij,ekj->ik', mats, mats)
+        else:
+            rdm1 = numpy.einsum('eji,ejk->ik', mats, mats)
+        tr = numpy.trace(rdm1)
+        if tr < -1e-12:
+            raise RuntimeError('RDM should be positive definite')
+        rdm1 = rdm1 + numpy.identity(rdm1.shape[0]) / rdm1.shape[0] if tr < 1e-12 else rdm1 / tr
+        Dcut = self.Dmax
+        if ncsite == 1 and ((status == 'L' and isite == self.nsite - 1) or (status == 'R' and isite == 0)):
+            Dcut = 1
+        if status == 'L':
+            if self.Dcut is not None:
+                Dcut = self.Dcut[isite + 1]
+            classes = dpt(self.qnuml[isite], self.qphys[isite])
+            dwts, qred, rotL, sigs = rdm_blkdiag(rdm1, classes, self.thresh, Dcut)
+            nres = len(qred)
+            site = rotL.reshape(ldim, dim, nres).copy()
+            srotR = numpy.einsum('ia,eij->eaj', rotL, mats).reshape(neig, nres, cdimc, rdim)
+        else:
+            jsite = isite + ncsite - 1
+            if self.Dcut is not None:
+                Dcut = self.Dcut[jsite]
+            classes = dpt(self.qphys[jsite], self.qnumr[jsite + 1])
+            dwts, qred, rotL, sigs = rdm_blkdiag(rdm1, classes, self.thresh, Dcut)
+            nres = len(qred)
+            site = rotL.reshape(dim, rdim, nres).transpose(2, 0, 1).copy()
+            srotR = numpy.einsum('eij,ja->eia', mats, rotL).reshape(neig, ldim, cdimc, nres)
+        return sigs, dwts, qred, site, srotR
+
+    def genGuess(self, isite, ncsite, actlst, civecs, srotR, status):
+        if isite == actlst[-1]:
+            self.psi0 = civecs.copy()
+            return 0
+        if status == 'R':
+            t = self.flmps.get('site%d' % (isite - 1))
+            if t is not None:
+                d = t.toDenseTensor(t.idlst)
+                self.psi0 = numpy.array([numpy.tensordot(d, srotR[e], axes=([2], [0])).reshape(-1)
+                                         for e in range(self.neig)])
+        else:
+            t = self.frmps.get('site%d' % (isite + ncsite))
+            if t is not None:
+                d = t.toDenseTensor(t.idlst)
+                self.psi0 = numpy.array([numpy.tensordot(srotR[e], d, axes=([2], [0])).reshape(-1)
+                                         for e in range(self.neig)])
+        return 0
+
+    # ----------------------------------------------------------------- sweep
+    def checkOpers(self, sitelst, ncsite, status):
+        if status == 'L':
+            return [i - ncsite for i in range(sitelst[0] + ncsite, min(self.nsite, sitelst[-1] + ncsite) + 1)]
+        lst = list(range(max(-1, sitelst[0] - ncsite), sitelst[-1] - ncsite + 1))
+        return [i + 1 for i in lst[::-1]]
+
+    def updateSite(self, isite, ncsite, qred, site, status):
+        if status == 'L':
+            self.qnuml[isite + 1] = qred.copy()
+            t = self.site_qt(isite, site, [self.qlst[0], self.qlst[1], qred], [False, False, True])
+            self.flmps['qnum%d' % (isite + 1)] = qred.copy()
+            self.flmps['site%d' % isite] = t
+        else:
+            jsite = isite + ncsite - 1
+            self.qnumr[jsite] = qred.copy()
+            t = self.site_qt(jsite, site, [qred, self.qlst[-2], self.qlst[-1]], [True, False, False])
+            self.frmps['qnum%d' % jsite] = qred.copy()
+            self.frmps['site%d' % jsite] = t
+        return t
+
+    def updateBoundary(self, ncsite, sitelst, qred, srotR, status):
+        if ncsite != 2:
+            return 0
+        key = numpy.array([float(x) for x in eval(next(iter(self.qsectors)))])
+        smat = srotR[0] / numpy.linalg.norm(srotR[0])
+        if status == 'L' and sitelst[-1] == self.nsite - 1:
+            self.flmps['qnum%d' % self.nsite] = key[None, :]
+            self.flmps['site%d' % (self.nsite - 1)] = self.site_qt(
+                self.nsite - 1, smat, [qred, self.qphys[self.nsite - 1], key[None, :]], [False, False, True])
+        elif status == 'R' and sitelst[0] == 0:
+            self.frmps['qnum0'] = key[None, :]
+            self.frmps['site0'] = self.site_qt(0, smat, [key[None, :], self.qphys[0], qred],
+                                               [True, False, False])
+        return 0
+
+    def sweep(self, sitelst, ncsite, status, ifsym=True):
+        torch = _torch()
+        actlst = self.checkOpers(sitelst, ncsite, status)
+        elst, dlst = [], []
+        nmvp = 0
+        for isite in actlst:
+            t0 = time.perf_counter()
+            flst = [[self.envs[('lop', isite - 1)], self.envs[('rop', isite + ncsite)]]]
+            nmvps, eigs, sigs, dwts, qred, site, srotR = self.ci_solver(isite, ncsite, actlst, flst, status, ifsym)
+            t1 = time.perf_counter()
+            nmvp += nmvps
+            elst.append(eigs)
+            dlst.append(dwts)
+            siteN = self.updateSite(isite, ncsite, qred, site, status)
+            fN = [[None]]
+            renorm(self, isite, ncsite, flst, fN, siteN, status)
+            if status == 'L':
+                self.envs[('lop', isite)] = fN[0][0]
+            else:
+                self.envs[('rop', isite + ncsite - 1)] = fN[0][0]
+            torch.cuda.synchronize()
+            self.timings.append((status, isite, t1 - t0, time.perf_counter() - t1, nmvps))
+        self.updateBoundary(ncsite, sitelst, qred, srotR, status)
+        eavs = numpy.array(elst).dot(self.wts)
+        indx = int(numpy.argmin(eavs))
+        return nmvp, indx, eavs[indx], dlst[indx], elst, dlst
+
+    def default(self, sc, fmps=None):
+        """Standard DMRG following the schedule (mpo_dmrg_class.py:329-434)."""
+        self.schedule = sc
+        self.crit_tol = sc.tol
+        self.initStates()
+        self.flmps = {'nsite': self.nsite, 'qnum0': self.qnuml[0]}
+        self.frmps = {'nsite': self.nsite, 'qnum%d' % self.nsite: self.qnumr[-1]}
+        if fmps is None:
+            fmps = self.product_mps()
+        self.qnuml = [numpy.asarray(fmps['qnum%d' % i]) for i in range(self.nsite + 1)]
+        self.flmps.update(fmps)
+        self.initOps(fmps)
+        self.psi0 = None
+        sitelst = list(range(self.nsite))
+        eold, deltaE, ifconv, isweep = 1.e3, 1.e3, False, -1
+        for isweep in range(sc.maxiter):
+            self.isweep = isweep
+            sc.getParameters(self, isweep)
+            r1 = self.sweep(sitelst, self.ncsite, 'R')
+            r2 = self.sweep(sitelst, self.ncsite, 'L')
+            self.nmvp.append(r1[0] + r2[0])
+            self.esweeps += r1[4] + r2[4]
+            eav, dwt = (r1[2], r1[3]) if r1[2] < r2[2] else (r2[2], r2[3])
+            self.eav.append(eav)
+            self.dwt.append(dwt)
+            self.Energy = eav
+            deltaE = eav - eold
+            ifconv = sc.checkConv(self, isweep, deltaE)
+            eold = eav
+            if ifconv:
+                break
+        self.ifconv = ifconv
+        self.nsweep = isweep + 1
+        self.deltaE = deltaE
+        return 0

@@ -1,0 +1,231 @@
+"""Drop-in replacements for the reference's hot-path kernels, on the GPU.
+
+Same call signatures as ``source/mpo_dmrg_kernel.py``:
+  ``HVec(vec0, info, ndim0, prjmap)``   (117-136; Qt body HVecQt,
+                                         mpo_dmrg_kernelQt.py:153-319)
+  ``HDiag(info, ndim0, prjmap)``         (41-51; HDiagQt 30-127)
+  ``renorm(dmrg, isite, ncsite, flst, flstN, site, status)`` (347-377;
+                                         renormQt_H00 633-768)
+with ``info = [dmrg, isite, ncsite, flst, status, ifsym]``.  ``flst[0][0:2]``
+are the left / right environment sets (``EnvSet``: one device buffer holding
+L_p or R_p for every operator term, in the reference's packed block order),
+``dmrg.qtmp`` is the wavefunction layout and ``dmrg.qkey`` its target label.
+Vectors may be NumPy (copied to and from the device) or float64 CUDA tensors
+(kept on the device).  Every product runs in the engine; there is no host
+fallback.
+"""
+import numpy
+
+from . import engine as _engine
+from .qtensor import qtensor
+
+
+class EnvSet:
+    """Environments of all operator terms at one bond (replaces the reference's
+    per-site HDF5 file ``lop_site_i`` / ``rop_site_i`` with datasets ``opers{p}``)."""
+
+    def __init__(self, buf, off, layouts, tensors):
+        self.buf = buf            # torch float64 CUDA tensor
+        self.off = off            # [nop] element offsets (-1: absent)
+        self.layouts = layouts    # [nop] engine layout ids (-1: absent)
+        self.tensors = tensors    # [nop] host qtensor structure (value unset)
+
+    def present(self, iop):
+        return self.off[iop] >= 0
+
+
+class MPOStore:
+    """All MPO site tensors on the device (replaces the reference's ``hop`` file)."""
+
+    def __init__(self, buf, off, tensors):
+        self.buf = buf            # torch float64 CUDA tensor
+        self.off = off            # off[isite][iop]
+        self.tensors = tensors    # tensors[isite][iop] host qtensor
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _to_device(v):
+    torch = _torch()
+    if isinstance(v, numpy.ndarray):
+        return torch.from_numpy(numpy.ascontiguousarray(v, dtype=numpy.float64)).cuda(), True
+    return v.contiguous(), False
+
+
+def _flip_layout(dmrg, t):
+    """Right environment with the reference's label flip (kernelQt.py:301)."""
+    qkey = numpy.asarray(dmrg.qkey, dtype=float)
+    if dmrg.ifs2proj:
+        qkey = qkey[:1]
+    key = (t.layout, tuple(qkey.tolist()))
+    cache = dmrg.__dict__.setdefault("_flip_cache", {})
+    lid = cache.get(key)
+    if lid is None:
+        lid = _engine.get().derive(t.layout, [-t.qsyms[0], qkey - t.qsyms[1], qkey - t.qsyms[2]],
+                                   t.status)
+        cache[key] = lid
+    return lid
+
+
+class SigmaPlan:
+    def __init__(self, dmrg, isite, ncsite, fL, fR):
+        from .mpo import op_class
+        eng = _engine.get()
+        mpo = dmrg.mpo_store
+        ops = [iop for iop in range(dmrg.nops) if fL.present(iop) and fR.present(iop)]
+        classes = {}
+        op_cls, lay_L, lay_Wi, lay_Wj, lay_Rf = [], [], [], [], []
+        off_L, off_R, off_Wi, off_Wj, wts = [], [], [], [], []
+        for iop in ops:
+            c0 = op_class(dmrg.opers[iop][0], isite, ncsite)
+            if c0 not in classes:
+                classes[c0] = len(classes)
+                lay_L.append(fL.layouts[iop])
+                lay_Wi.append(mpo.tensors[isite][iop].layout)
+                lay_Wj.append(mpo.tensors[isite + 1][iop].layout if ncsite == 2 else -1)
+                lay_Rf.append(_flip_layout(dmrg, fR.tensors[iop]))
+            c = classes[c0]
+            op_cls.append(c)
+            off_L.append(fL.off[iop])
+            off_R.append(fR.off[iop])
+            off_Wi.append(mpo.off[isite][iop])
+            off_Wj.append(mpo.off[isite + 1][iop] if ncsite == 2 else 0)
+            wts.append(dmrg.hpwts[iop])
+        self.nops = len(ops)
+        if self.nops == 0:
+            self.pid = None
+            return
+        self.pid, ws = eng.sigma_plan(ncsite, op_cls, lay_L, lay_Wi, lay_Wj if ncsite == 2 else None,
+                                      lay_Rf, dmrg.qtmp_psi_layout, off_L, off_R, off_Wi,
+                                      off_Wj if ncsite == 2 else None, wts)
+        torch = _torch()
+        self.workspace = torch.empty(max(ws // 8, 1), dtype=torch.float64, device="cuda")
+        self.flops, self.ntasks, self.nlaunch = eng.plan_stats(self.pid)
+        self.fL, self.fR = fL, fR
+
+    def release(self):
+        if self.pid is not None:
+            _engine.get().destroy_plan(self.pid)
+            self.pid = None
+
+
+def _sigma_plan(info):
+    dmrg, isite, ncsite, flst, status, ifsym = info
+    fL, fR = flst[0][0:2]
+    key = (id(fL), id(fR), isite, ncsite, dmrg.qtmp_psi_layout)
+    cur = getattr(dmrg, "_sigma_plan", None)
+    if cur is None or cur[0] != key:
+        if cur is not None:
+            cur[1].release()
+        cur = (key, SigmaPlan(dmrg, isite, ncsite, fL, fR))
+        dmrg._sigma_plan = cur
+    return cur[1]
+
+
+def HVec(vec0, info, ndim0, prjmap):
+    """y = H x over every operator term of the dot, on the GPU."""
+    dmrg = info[0]
+    torch = _torch()
+    plan = _sigma_plan(info)
+    x, was_host = _to_device(vec0)
+    y = torch.empty(ndim0, dtype=torch.float64, device=x.device)
+    if plan.pid is None:
+        y.zero_()
+    else:
+        _engine.get().sigma(plan.pid, plan.fL.buf, plan.fR.buf, dmrg.mpo_store.buf, x, y,
+                            plan.workspace, getattr(dmrg, "precision", "fp64"))
+    return y.cpu().numpy() if was_host else y
+
+
+def HDiag(info, ndim0, prjmap):
+    """diag(H) in the packed wavefunction order (Davidson preconditioner)."""
+    dmrg = info[0]
+    torch = _torch()
+    plan = _sigma_plan(info)
+    d = torch.zeros(ndim0, dtype=torch.float64, device="cuda")
+    if plan.pid is not None:
+        _engine.get().hdiag(plan.pid, plan.fL.buf, plan.fR.buf, dmrg.mpo_store.buf, d)
+    return d
+
+
+def renorm(dmrg, isite, ncsite, flst, flstN, site, status):
+    """New environments of every operator term after the site update; the
+    result EnvSet is stored in ``flstN[0][0]`` (a one-element list)."""
+    from .mpo import op_class
+    eng = _engine.get()
+    torch = _torch()
+    mpo = dmrg.mpo_store
+    qsite = site
+    if status == 'L':
+        fE = flst[0][0]
+        jsite = isite
+    else:
+        fE = flst[0][1]
+        jsite = isite + ncsite - 1
+    ops = [iop for iop in range(dmrg.nops) if fE.present(iop)]
+    classes = {}
+    op_cls, lay_env, lay_W, off_env, off_W = [], [], [], [], []
+    for iop in ops:
+        c0 = op_class(dmrg.opers[iop][0], jsite)
+        if c0 not in classes:
+            classes[c0] = len(classes)
+            lay_env.append(fE.layouts[iop])
+            wt = mpo.tensors[jsite][iop]
+            if status == 'L':
+                lay_W.append(wt.layout)
+            else:
+                st = wt.status.copy()
+                st[0], st[1] = not st[0], not st[1]
+                lay_W.append(eng.derive(wt.layout, [-wt.qsyms[0], -wt.qsyms[1], wt.qsyms[2],
+                                                    wt.qsyms[3]], st))
+        op_cls.append(classes[c0])
+        off_env.append(fE.off[iop])
+        off_W.append(mpo.off[jsite][iop])
+    nop = dmrg.nops
+    off = numpy.full(nop, -1, dtype=numpy.int64)
+    lays = numpy.full(nop, -1, dtype=numpy.int64)
+    tens = [None] * nop
+    if not ops:
+        buf = torch.zeros(1, dtype=torch.float64, device="cuda")
+    else:
+        pid, lay_out, off_out, total, ws = eng.renorm_plan(status, op_cls, lay_env, lay_W,
+                                                           qsite.layout, off_env, off_W)
+        buf = torch.empty(max(total, 1), dtype=torch.float64, device="cuda")
+        work = torch.empty(max(ws // 8, 1), dtype=torch.float64, device="cuda")
+        sval, _ = _to_device(qsite.value)
+        eng.renorm(pid, fE.buf, mpo.buf, sval, buf, work, getattr(dmrg, "precision_renorm", "fp64"))
+        # host structure of each output (layout id per class)
+        struct = {}
+        for k, iop in enumerate(ops):
+            c = op_cls[k]
+            if lay_out[c] < 0 or off_out[k] < 0:
+                continue
+            if c not in struct:
+                struct[c] = _env_structure(dmrg, status, qsite, mpo.tensors[jsite][iop], fE.tensors[iop],
+                                           int(lay_out[c]))
+            off[iop] = off_out[k]
+            lays[iop] = struct[c].layout
+            tens[iop] = struct[c]
+        eng.destroy_plan(pid)
+    flstN[0][0] = EnvSet(buf, off, lays, tens)
+    return 0
+
+
+def _env_structure(dmrg, status, qsite, wt, env, lay_out):
+    """Host qtensor describing a renormalised environment block structure:
+    legs [b, bra, ket] with the reference's labels (status [T, F, T])."""
+    t = qtensor([True, False, True])
+    if status == 'L':
+        q = [wt.qsyms[1], qsite.qsyms[2], qsite.qsyms[2]]
+        d = [wt.ndims[1], qsite.ndims[2], qsite.ndims[2]]
+    else:
+        q = [-wt.qsyms[0], qsite.qsyms[0], qsite.qsyms[0]]
+        d = [wt.ndims[0], qsite.ndims[0], qsite.ndims[0]]
+    t.fromQsyms(3, q, d, ifallocate=False)
+    size, flat, _ = _engine.get().layout_blocks(lay_out)
+    if size != t.size_allowed or not numpy.array_equal(flat, t.blk_flat):
+        raise RuntimeError("renormalised environment layout mismatch")
+    return t
