@@ -1,0 +1,325 @@
+"""Benchmark of the DMRG sigma-vector hot path on one GB300.
+
+One step = one two-site H.psi over every operator term H_p (48 terms) at the
+middle dot of K=24 spatial orbitals, 24 electrons, Sz=0, bond dimension
+D=512, (N,Sz) block-sparse, in the split-precision tensor-core path.  Inputs
+are seeded synthetic integrals (the configuration's generator) and a seeded
+random block-sparse MPS with realistic sector sizes; the environments of all
+terms are built on the GPU by the engine's renormalisation.
+
+Printed (one JSON line, rank 0): ``value`` = F_ref / t with F_ref the
+reference's algorithmic FLOPs of one H.psi (sum of 2mnk over its block task
+lists) and t the device time per step with inputs resident in HBM; ``e2e`` =
+the same through the C ABI with host input/output vectors (H2D + D2H inside
+the timed region); ``roofline`` for the dominant launch; ``cpu_baseline`` =
+the oracle (the reference's NumPy kernel restated) on a bounded sample of the
+same workload.  ``--impl reference`` times only that CPU path.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+WORKLOAD = dict(K=24, nelec=24, D=512, isite=11, seed=2024)
+SMALL = dict(K=12, nelec=12, D=128, isite=5, seed=2024)
+METRIC = "sweep s & sigma-vec TFLOP/s, split-BF16 vs FP64 on 1 GB300 at ΔE≤1e-8 Eh"
+
+
+def peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p["hbm_gbs"], p["bf16_tflops"], "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.p = None
+        self.path = os.path.join(HERE, "gpurun_out", "clocks_bench.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                       "-i", "0", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(numpy.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_problem(with_oracle=False, small=False):
+    from tests.problems import random_problem
+    t0 = time.perf_counter()
+    P = random_problem(device=True, with_oracle=with_oracle, **(SMALL if small else WORKLOAD))
+    return P, time.perf_counter() - t0
+
+
+def oracle_sample(P, nops_sample=2, budget_s=25.0):
+    """Time the oracle's HVecQt on a bounded subset of operator terms built
+    from the GPU environments (same packed values), F_ref / t."""
+    from oracle import dmrg as od, kernel as ok, qtensor as oq
+    m = od.mpo_dmrg(seed=0)
+    m.nsite, m.sbas, m.isym, m.ifQt = P.K, 2 * P.K, 2, True
+    m.build()
+    m.partition()
+    m.loadInts(P.int1e, P.int2e)
+    pm = P.p
+    isite = P.isite
+    fL, fR = pm.flst[0]
+    Lb = fL.buf.cpu().numpy()
+    Rb = fR.buf.cpu().numpy()
+    from oracle import qtensor_opers
+    # pick operator terms from distinct classes, up to nops_sample
+    chosen, seen = [], set()
+    for iop in range(m.nops):
+        c = qtensor_opers.case(m.opers[iop][0], isite, 2)
+        if c not in seen and fL.present(iop) and fR.present(iop):
+            seen.add(c)
+            chosen.append(iop)
+        if len(chosen) >= nops_sample:
+            break
+    m.fhop = {'nops': len(chosen)}
+    m.opers = [m.opers[i] for i in chosen]
+    m.hpwts = numpy.ones(len(chosen))
+    fLo, fRo = {}, {}
+    for k, iop in enumerate(chosen):
+        for src, dst, buf in ((fL, fLo, Lb), (fR, fRo, Rb)):
+            t = src.tensors[iop]
+            q = oq.qtensor(t.status)
+            q.fromQsyms(3, t.qsyms, t.ndims)
+            q.value = buf[src.off[iop]:src.off[iop] + q.size_allowed].copy()
+            q.idlst = None
+            dst['opers%d' % k] = q
+        for s in (isite, isite + 1):
+            m.fhop['site%d/op%d' % (s, k)] = qtensor_opers.genHRfacSpatialQt(
+                m.opers[k], m.sbas, s, m.int1e, m.int2e, None, m.pdic)
+    m.qlst = [P.qnuml[isite], pm.qlst[1], pm.qlst[2], P.qnumr[isite + 2]]
+    m.setupQtmpCI(2, P.key)
+    x = numpy.random.default_rng(1).standard_normal(m.qtmp.size_allowed)
+    info = [m, isite, 2, [[fLo, fRo]], 'L', True]
+    oq.reset_flops()
+    t0 = time.perf_counter()
+    m._hvec_templates = None
+    ok.HVecQt(x, info, m.qtmp.size_allowed, None)
+    dt = time.perf_counter() - t0
+    return oq.FLOPS["count"], dt, chosen
+
+
+def cpu_threads():
+    return os.cpu_count() or 1
+
+
+def run_reference(args):
+    """--impl reference: the oracle (reference algorithm) on host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import torch
+    torch.cuda.set_device(0)
+    P, _ = build_problem()
+    vals = []
+    for i in range(args.warmup + args.steps):
+        fl, dt, ch = oracle_sample(P)
+        if i >= args.warmup:
+            vals.append(fl / dt / 1e12)
+    v = float(numpy.mean(vals))
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+           "config": {"workload": "two-site H.psi, K=24 N=24 Sz=0 D=512, 48 terms, (N,Sz) blocks"},
+           "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": cpu_threads(), "kind": "port",
+                            "sample": "oracle HVecQt (reference NumPy algorithm) over %d of 48 operator "
+                                      "terms per step, F_ref/t" % len(ch)},
+           "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine")
+    ap.add_argument("--precision", default="split")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--small", action="store_true", help="K=12, D=128 case (profiling)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from zmpo_dmrg_gb300 import build as _b
+    _b.build()
+    from zmpo_dmrg_gb300 import engine as E
+    from zmpo_dmrg_gb300.mpo_dmrg_kernel import HVec, _sigma_plan
+
+    P, t_build = build_problem(small=args.small)
+    pm = P.p
+    info = [pm, P.isite, 2, pm.flst, 'L', True]
+    eng = E.get()
+    plan = _sigma_plan(info)
+    flops = plan.flops
+    n = P.ndim0
+    x_host = numpy.random.default_rng(5).standard_normal(n)
+    x = torch.from_numpy(x_host).cuda()
+    y = torch.empty(n, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step(prec):
+        eng.sigma(plan.pid, plan.fL.buf, plan.fR.buf, pm.mpo_store.buf, x, y, plan.workspace, prec)
+
+    def timed(prec, steps, warmup):
+        for _ in range(warmup):
+            step(prec)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            step(prec)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        return e0.elapsed_time(e1) / 1e3 / steps
+
+    # accuracy of both paths against FP64 on this workload
+    step("fp64")
+    y64 = y.clone()
+    step(args.precision)
+    err_split = float(torch.linalg.norm(y - y64) / torch.linalg.norm(y64))
+
+    clocks = Clocks()
+    clocks.start()
+    t_split = timed(args.precision, args.steps, max(args.warmup, 3))
+    clocks_rec = clocks.stop()
+    t_fp64 = timed("fp64", max(2, args.steps // 10), 1)
+
+    # per-launch durations (engine tracing: CUDA events around each launch on
+    # its stream) and the algorithmic bytes of each launch
+    L = plan.fL.buf
+    R = plan.fR.buf
+    W = pm.mpo_store.buf
+    eng.profile(True)
+    eng.launch_times(plan.pid)
+    nprof = max(5, args.steps // 2)
+    for _ in range(nprof):
+        step(args.precision)
+    torch.cuda.synchronize()
+    ms, abytes, ncalls = eng.launch_times(plan.pid)
+    eng.profile(False)
+    launches = [{"launch": i, "ms": float(ms[i]), "alg_bytes": float(abytes[i]),
+                 "GBs": float(abytes[i] / (ms[i] * 1e-3) / 1e9) if ms[i] > 0 else None}
+                for i in range(plan.nlaunch)]
+    top = max(range(plan.nlaunch), key=lambda i: ms[i])
+    # e2e through the C ABI with host vectors
+    xh = torch.from_numpy(x_host).pin_memory()
+    yh = torch.empty(n, dtype=torch.float64).pin_memory()
+    for _ in range(3):
+        xd = xh.cuda(non_blocking=True)
+        eng.sigma(plan.pid, L, R, W, xd, y, plan.workspace, args.precision)
+        yh.copy_(y, non_blocking=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ne2e = max(3, args.steps // 2)
+    for _ in range(ne2e):
+        xd = xh.cuda(non_blocking=True)
+        eng.sigma(plan.pid, L, R, W, xd, y, plan.workspace, args.precision)
+        yh.copy_(y, non_blocking=True)
+        torch.cuda.synchronize()
+    t_e2e = (time.perf_counter() - t0) / ne2e
+
+    # algorithmic bytes of one step: every operand block read once, outputs written once
+    hbm, bf16, peak_kind = peaks()
+    value = flops / t_split / 1e12
+    tmax = t_split
+    if dist:
+        tt = torch.tensor([t_split], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        tmax = float(tt.item())
+        value = world * flops / tmax / 1e12
+    result = {
+        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": tmax * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 (bf16 digit slices, fp32 accumulate)",
+        "data": "synthetic (seeded integrals + seeded random block-sparse MPS)",
+        "config": {"workload": "two-site H.psi, K=24 N=24 Sz=0 D=512, 48 terms, (N,Sz) blocks",
+                   "ndim0": n, "F_ref_flops": flops, "tasks": plan.ntasks, "precision": args.precision,
+                   "l2": "inputs larger than L2 (environments %.2f GB)" % ((L.numel() + R.numel()) * 8 / 1e9),
+                   "build_s": t_build},
+        "fp64": {"value": flops / t_fp64 / 1e12, "ms_per_step": t_fp64 * 1e3},
+        "split_vs_fp64_rel_err": err_split,
+        "e2e": {"value": flops / t_e2e / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": n * 8,
+                "d2h_bytes_per_step": n * 8},
+        "gpu_launches": args.steps * plan.nlaunch,
+        "clocks": clocks_rec,
+        "launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "k_step_split<4> launch %d of %d" % (top, plan.nlaunch),
+                     "achieved": launches[top]["GBs"], "peak": hbm, "unit": "GB/s",
+                     "frac": (launches[top]["GBs"] or 0.0) / hbm, "traffic": None,
+                     "peak_source": peak_kind},
+    }
+    if rank == 0 and not args.no_cpu:
+        fl, dt, ch = oracle_sample(P)
+        result["cpu_baseline"] = {"value": fl / dt / 1e12, "unit": "TFLOP/s", "cores": cpu_threads(),
+                                  "kind": "port",
+                                  "sample": "oracle HVecQt over %d of 48 operator terms (%.1f s), F_ref/t" %
+                                            (len(ch), dt)}
+    if rank == 0:
+        print(json.dumps(result))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -155,6 +155,15 @@ int zmpo_renorm(zmpo_engine *e, int plan_id, const double *d_env,
                 const double *d_W, const double *d_site, double *d_out,
                 void *d_workspace, int precision, void *stream);
 
+/* Tracing: when on, every launch of a plan is bracketed by CUDA events on
+ * its stream; zmpo_plan_launch_times returns, per launch of the plan, the
+ * average device time (ms) since the last read, the algorithmic bytes of
+ * that launch (each operand tensor read once, each output written once) and
+ * the number of timed calls, then resets the counters. */
+int zmpo_profile(zmpo_engine *e, int on);
+int zmpo_plan_launch_times(zmpo_engine *e, int plan_id, int nmax, double *ms_avg,
+                           double *alg_bytes, int64_t *ncalls);
+
 /* Release a contraction / sigma / renorm plan. */
 int zmpo_plan_destroy(zmpo_engine *e, int plan_id);
 

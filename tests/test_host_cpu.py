@@ -1,0 +1,202 @@
+"""Host-side logic of the product on the CPU (no GPU calls): the C ABI
+library loads and exports every declared symbol, its block rule, layouts and
+task lists agree with the oracle, and the product's MPO / integrals /
+schedule / decimation agree with the oracle's restatement."""
+import ctypes
+import os
+import re
+
+import numpy
+import pytest
+
+from oracle import integrals as oint, mpo as omp, qtensor as oq, qtensor_opers as oqo, dmrg as od
+from zmpo_dmrg_gb300 import _lib, engine as E, mpo as pm, integrals as pint
+from zmpo_dmrg_gb300.mpo_dmrg_schedule import schedule as pschedule
+from zmpo_dmrg_gb300.mpo_dmrg_class import rdm_blkdiag as p_rdm_blkdiag
+from zmpo_dmrg_gb300.qtensor import qtensor as pq
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "zmpo_gb300.h")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from zmpo_dmrg_gb300 import build
+    build.build()
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*int\s+(\w+)\s*\(", text, flags=re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(_lib.LIBPATH)
+    names = declared_symbols()
+    assert "zmpo_sigma" in names and "symAllowed" in names
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) <= set(_lib.EXPORTS)
+    assert _lib.lib().zmpo_version() == 1
+
+
+def test_symallowed_export_matches_reference_golden():
+    z = numpy.load(os.path.join(ROOT, "tests", "golden", "qsym_reference.npz"))
+    lib = _lib.lib()
+    for c in range(int(z["ncase"])):
+        nsyms = z["c%d_nsyms" % c].astype(numpy.int32)
+        status = z["c%d_status" % c].astype(numpy.int32)
+        nq = int(z["c%d_nq" % c])
+        qs = [numpy.ascontiguousarray(z["c%d_q%d" % (c, i)]) for i in range(len(nsyms))]
+        out = numpy.zeros(int(numpy.prod(nsyms)), dtype=numpy.int32)
+        args = [q.ctypes.data_as(ctypes.c_void_p) for q in qs] + [None] * (8 - len(qs))
+        assert lib.symAllowed(len(nsyms), nq, _lib.iptr(nsyms), _lib.iptr(status), _lib.iptr(out), *args) == 0
+        assert numpy.array_equal(out, z["c%d_allowed" % c])
+
+
+def test_error_convention():
+    eng = E.get()
+    with pytest.raises(RuntimeError, match="unknown"):
+        eng.layout_blocks(10 ** 6)
+    assert "unknown layout" in _lib.last_error()
+
+
+def test_integrals_match_oracle():
+    for K, seed, hop in [(4, 1, 1.0), (6, 9, 0.7)]:
+        a = pint.synthetic(K, seed, hop)
+        b = oint.synthetic(K, seed, hop)
+        assert numpy.array_equal(a[0], b[0]) and numpy.allclose(a[1], b[1], atol=1e-15, rtol=0)
+        p1, p2 = pint.spin_orbital(a[0], a[1])
+        o1, o2, _ = oint.to_spin_orbital(b[0], b[1])
+        assert numpy.array_equal(p1, o1) and numpy.allclose(p2, o2, atol=1e-15, rtol=0)
+    fd = os.path.join(ROOT, "tests", "golden", "h6p_doublet_fcidump.npz")
+    z = numpy.load(fd)
+    # round trip through the FCIDUMP text format
+    path = os.path.join(ROOT, "_work", "rt.FCIDUMP")
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    n = z["h1e"].shape[0]
+    with open(path, "w") as f:
+        f.write(" &FCI NORB=%d,NELEC=%d,MS2=%d,\n  ORBSYM=%s\n  ISYM=1,\n &END\n"
+                % (n, int(z["nelec"]), int(z["ms2"]), "1," * n))
+        for i in range(n):
+            for j in range(i + 1):
+                for k in range(n):
+                    for l in range(k + 1):
+                        if i * (i + 1) // 2 + j >= k * (k + 1) // 2 + l and z["eri"][i, j, k, l] != 0:
+                            f.write("%.16e %d %d %d %d\n" % (z["eri"][i, j, k, l], i + 1, j + 1, k + 1, l + 1))
+        for i in range(n):
+            for j in range(i + 1):
+                f.write("%.16e %d %d 0 0\n" % (z["h1e"][i, j], i + 1, j + 1))
+        f.write("%.16e 0 0 0 0\n" % float(z["ecore"]))
+    a = pint.read_fcidump(path)
+    b = oint.read_fcidump(path)
+    assert numpy.array_equal(a["eri"], b["eri"]) and numpy.array_equal(a["h1e"], b["h1e"])
+    assert a["ecore"] == b["ecore"] and a["norb"] == b["norb"] == n
+    assert numpy.allclose(a["eri"], z["eri"], atol=1e-15)
+
+
+def test_mpo_matches_oracle():
+    K = 5
+    h, eri, _ = oint.synthetic(K, 4)
+    i1, i2, _ = oint.to_spin_orbital(h, eri)
+    pdic = {q: q for q in range(2 * K)}
+    for p in range(2 * K):
+        for i in range(K):
+            a = omp.genHRfacSpatial([p, None], 2 * K, i, i1, i2, None, pdic)
+            b = pm.hp_spatial_site([p, None], 2 * K, i, i1, i2)
+            assert numpy.array_equal(a, b)
+            qa = oqo.genHRfacSpatialQt([p, None], 2 * K, i, i1, i2, None, pdic)
+            qb = pm.hp_spatial_qt([p, None], 2 * K, i, i1, i2)
+            assert numpy.array_equal(qa.value, qb.value)
+            assert all(numpy.array_equal(x, y) for x, y in zip(qa.qsyms, qb.qsyms))
+            assert oqo.case(p, i, 2) == pm.op_class(p, i, 2) and oqo.case(p, i) == pm.op_class(p, i)
+
+
+def test_spin_projected_mpo_matches_oracle():
+    K = 3
+    h, eri, _ = oint.synthetic(K, 8)
+    i1, i2, _ = oint.to_spin_orbital(h, eri)
+    qpts = [0.3, 1.7]
+    pdic = {q: q for q in range(2 * K)}
+    for p in range(2 * K):
+        for ip in range(2):
+            for i in range(K):
+                qa = oqo.genHRfacSpatialQt([p, ip], 2 * K, i, i1, i2, qpts, pdic)
+                qb = pm.hp_spatial_qt([p, ip], 2 * K, i, i1, i2, qpts, pdic)
+                assert numpy.allclose(qa.value, qb.value, atol=1e-15, rtol=0)
+
+
+def test_layouts_and_task_lists_match_oracle():
+    """Engine packing == oracle fromQsyms; engine sigma task lists give the
+    oracle's F_ref (sum of 2mnk over its tensordotSYM tasks)."""
+    from tests.problems import random_problem, oracle_sigma
+    P = random_problem(K=6, nelec=6, D=16, isite=2, seed=1, device=False)
+    m = P.o
+    eng = E.get()
+    fL, fR = m.flst[0]
+
+    def lay(t):
+        return eng.layout(t.qsyms, t.ndims, t.status)
+
+    for iop in range(m.nops):
+        for t in (fL['opers%d' % iop], fR['opers%d' % iop]):
+            size, flat, off = eng.layout_blocks(lay(t))
+            assert size == t.size_allowed
+            assert numpy.array_equal(flat, t.idx_allowed)
+            assert numpy.array_equal(off, t.ioff_allowed[t.idx_allowed])
+    classes, op_cls, lL, lWi, lWj, lRf = {}, [], [], [], [], []
+    for iop in range(m.nops):
+        c0 = pm.op_class(m.opers[iop][0], P.isite, 2)
+        if c0 not in classes:
+            classes[c0] = len(classes)
+            R = fR['opers%d' % iop]
+            lL.append(lay(fL['opers%d' % iop]))
+            lWi.append(lay(m.fhop['site%d/op%d' % (P.isite, iop)]))
+            lWj.append(lay(m.fhop['site%d/op%d' % (P.isite + 1, iop)]))
+            lRf.append(eng.derive(lay(R), [-R.qsyms[0], m.qkey - R.qsyms[1], m.qkey - R.qsyms[2]], R.status))
+        op_cls.append(classes[c0])
+    n = m.nops
+    pid, ws = eng.sigma_plan(2, op_cls, lL, lWi, lWj, lRf, lay(m.qtmp), [0] * n, [0] * n, [0] * n, [0] * n,
+                             [1.0] * n)
+    oq.reset_flops()
+    oracle_sigma(P, numpy.ones(P.ndim0))
+    flops, ntasks, nl = eng.plan_stats(pid)
+    assert flops == oq.FLOPS["count"] and nl == 4 and ws > 0
+
+
+def test_product_qtensor_dense_roundtrip_and_prjmap():
+    rng = numpy.random.default_rng(3)
+    ql = numpy.array([[0, 0], [1, .5], [1, -.5], [1, .5], [2, 0]], dtype=float)
+    qp = numpy.array([[0., 0.], [1., -0.5], [1., 0.5], [2., 0.]])
+    qr = numpy.array([[1, .5], [2, 0], [2, 0], [3, .5]], dtype=float)
+    A = rng.standard_normal((5, 4, 4))
+    a = pq([False, False, True])
+    a.fromDenseTensor(A, [ql, qp, qr])
+    b = oq.qtensor([False, False, True])
+    b.fromDenseTensor(A, [ql, qp, qr])
+    assert numpy.array_equal(a.value, b.value)
+    assert numpy.array_equal(a.prjmap(a.idlst), b.prjmap(b.idlst))
+    assert numpy.array_equal(a.toDenseTensor(a.idlst), b.toDenseTensor(b.idlst))
+
+
+def test_schedule_matches_oracle():
+    for maxM, tol in [(64, 1e-9), (512, 1e-8), (1000, 1e-7)]:
+        a = pschedule(maxM=maxM, tol=tol)
+        a.normal()
+        b = od.schedule(maxM=maxM, tol=tol)
+        b.normal()
+        assert (a.MaxMs, a.Tols, a.Noises, a.change) == (b.MaxMs, b.Tols, b.Noises, b.change)
+
+
+def test_rdm_blkdiag_matches_oracle():
+    rng = numpy.random.default_rng(5)
+    classes = [[0., 0.], [1., .5], [1., -.5], [2., 0.]] * 6
+    X = rng.standard_normal((24, 30))
+    rho = X @ X.T
+    for cut in (5, 12, -1):
+        a = p_rdm_blkdiag(rho, classes, -1e-14, cut)
+        b = od.rdm_blkdiag(rho, classes, -1e-14, cut)
+        assert abs(a[0] - b[0]) < 1e-13
+        assert numpy.array_equal(numpy.array(a[1]), numpy.array(b[1]))
+        assert numpy.allclose(numpy.abs(a[2]), numpy.abs(b[2]), atol=1e-10)

@@ -1,0 +1,143 @@
+"""Pins of the CPU oracle against the reference: its own C block rule, the
+exact Hamiltonian, its Qt-vs-dense MPO self-test, its HVec/HDiag debug check,
+its Davidson self-test and the BLOCK energy recorded for the K=6 FCIDUMP."""
+import ctypes
+import os
+
+import numpy
+import pytest
+
+from oracle import integrals, mpo, qtensor as oq, qtensor_opers as oqo, dmrg as od, kernel as ok
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+REF_LIB = os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "_ref", "libqsym.so")
+
+
+def _golden_qsym():
+    z = numpy.load(os.path.join(GOLD, "qsym_reference.npz"))
+    for c in range(int(z["ncase"])):
+        nsyms = z["c%d_nsyms" % c]
+        yield (nsyms, z["c%d_status" % c], int(z["c%d_nq" % c]),
+               [z["c%d_q%d" % (c, i)] for i in range(len(nsyms))], z["c%d_allowed" % c])
+
+
+def test_blks_allowed_vs_reference_golden():
+    """Restated rule == outputs of the reference's compiled symAllowed."""
+    for nsyms, status, nq, qs, allowed in _golden_qsym():
+        nb = int(numpy.prod(nsyms))
+        got = oq.blks_allowed(nb, len(nsyms), nq, nsyms, status.astype(bool), qs)
+        assert numpy.array_equal(got, allowed)
+        got0 = oq.blks_allowed0(nb, len(nsyms), nq, nsyms, status.astype(bool), qs)
+        assert numpy.array_equal(got0, allowed)
+
+
+@pytest.mark.skipif(not os.path.exists(REF_LIB), reason="reference qsym.c not built here")
+def test_blks_allowed_vs_reference_live():
+    lib = ctypes.CDLL(REF_LIB)
+    rng = numpy.random.default_rng(7)
+    for _ in range(50):
+        rank = int(rng.integers(2, 8))
+        nq = 2
+        nsyms = rng.integers(1, 5, size=rank).astype(numpy.int32)
+        status = rng.integers(0, 2, size=rank).astype(numpy.int32)
+        qs = [numpy.ascontiguousarray(rng.integers(-2, 3, size=(n, nq)) * 0.5) for n in nsyms]
+        nb = int(numpy.prod(nsyms))
+        ref = numpy.zeros(nb, dtype=numpy.int32)
+        args = [q.ctypes.data_as(ctypes.c_void_p) for q in qs] + [ctypes.c_void_p()] * (8 - rank)
+        lib.symAllowed(rank, nq, nsyms.ctypes.data_as(ctypes.c_void_p), status.ctypes.data_as(ctypes.c_void_p),
+                       ref.ctypes.data_as(ctypes.c_void_p), *args)
+        assert numpy.array_equal(oq.blks_allowed(nb, rank, nq, nsyms, status.astype(bool), qs), ref)
+
+
+def _mpo_chain(K, p, int1e, int2e):
+    T = mpo.genHfacSpatial(p, 2 * K, 0, int1e[p], int2e[p])[0].transpose(1, 2, 0)
+    for i in range(1, K):
+        W = mpo.genHfacSpatial(p, 2 * K, i, int1e[p], int2e[p])
+        T = numpy.tensordot(T, W, axes=([-1], [0])).transpose(0, 3, 1, 4, 2)
+        s = T.shape
+        T = T.reshape(s[0] * s[1], s[2] * s[3], s[4])
+    return T[:, :, 0]
+
+
+@pytest.mark.parametrize("K", [2, 3])
+def test_mpo_sum_equals_exact_hamiltonian(K):
+    h, eri, _ = integrals.synthetic(K, 11)
+    i1, i2, g = integrals.to_spin_orbital(h, eri)
+    H = sum(_mpo_chain(K, p, i1, i2) for p in range(2 * K))
+    Hf = integrals.fci_hamiltonian(i1, g).toarray()
+    assert numpy.linalg.norm(H - Hf) < 1e-12 * numpy.linalg.norm(Hf)
+
+
+def test_qt_mpo_matches_dense():
+    """qtensor_opers.testHRfacSpatial (qtensor_opers.py:907-960): Qt == dense."""
+    K = 4
+    h, eri, _ = integrals.synthetic(K, 2)
+    i1, i2, _ = integrals.to_spin_orbital(h, eri)
+    pdic = {q: q for q in range(2 * K)}
+    for p in range(2 * K):
+        for i in range(K):
+            qt = oqo.genHRfacSpatialQt([p, None], 2 * K, i, i1, i2, None, pdic)
+            dense = mpo.genHRfacSpatial([p, None], 2 * K, i, i1, i2, None, pdic)
+            ql, qr = oqo.bond_qnums(p, 2 * K, i)
+            il = oqo.sortQnums(ql)
+            ir = oqo.sortQnums(qr)
+            assert numpy.abs(qt.toDenseTensor(qt.idlst) - dense[numpy.ix_(il, ir)]).max() < 1e-14
+
+
+def test_hvec_hermitian_and_diag():
+    """checkDiagQt (mpo_dmrg_kernelQt.py:129-150) on a seeded problem."""
+    from tests.problems import random_problem, oracle_sigma, oracle_hdiag
+    P = random_problem(K=4, nelec=4, D=6, isite=1, seed=3, device=False)
+    n = P.ndim0
+    H = numpy.array([oracle_sigma(P, e) for e in numpy.identity(n)]).T
+    assert numpy.linalg.norm(H - H.T) < 1e-10 * numpy.linalg.norm(H)
+    assert numpy.linalg.norm(numpy.diag(H) - oracle_hdiag(P)) < 1e-10
+
+
+def test_davidson_vs_eigh():
+    """tools/pdvdson.py:396-429 self-test (random 100x100, seed 0)."""
+    numpy.random.seed(0)
+    mat = numpy.random.uniform(-1, 1, size=(100, 100))
+    mat = 0.5 * (mat + mat.T)
+    efull = numpy.linalg.eigvalsh(mat)
+    s = od.eigenSolver(numpy.random.default_rng(0))
+    s.crit_vec = 1.e-7
+    s.maxcycle = 200
+    s.ndim = 100
+    s.neig = 2
+    s.diag = numpy.diag(mat).copy()
+    s.HVec = mat.dot
+    eigs, vecs, _ = s.solve_iter(iop=4)
+    assert numpy.abs(eigs - efull[:2]).max() < 1e-8
+
+
+def _fcidump():
+    z = numpy.load(os.path.join(GOLD, "h6p_doublet_fcidump.npz"))
+    return z
+
+
+def test_fcidump_fci_matches_block():
+    z = _fcidump()
+    i1, i2, g = integrals.to_spin_orbital(z["h1e"], z["eri"])
+    e = integrals.fci_energy(i1, g, int(z["nelec"]), 0.5 * int(z["ms2"]))[0] + float(z["ecore"])
+    assert abs(e - float(z["e_block"])) < 5e-9
+
+
+def test_oracle_dmrg_reaches_fci_on_fcidump():
+    z = _fcidump()
+    K = z["h1e"].shape[0]
+    i1, i2, g = integrals.to_spin_orbital(z["h1e"], z["eri"])
+    efci = integrals.fci_energy(i1, g, int(z["nelec"]), 0.0)[0]
+    m = od.mpo_dmrg(seed=1)
+    m.nsite, m.sbas, m.isym = K, 2 * K, 2
+    m.build()
+    m.occun = numpy.array([1., 1.] * 3 + [0., 0.] * 3)
+    m.qsectors = {str([6.0, 0.0]): 1}
+    m.partition()
+    m.loadInts(i1, i2)
+    m.dumpMPO()
+    sc = od.schedule(maxM=64, tol=1e-9, maxiter=8)
+    sc.normal(2)
+    m.default(sc)
+    assert abs(m.Energy - efci) < 1e-9
+    assert abs(m.Energy + float(z["ecore"]) - float(z["e_block"])) < 5e-9

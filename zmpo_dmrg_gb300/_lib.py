@@ -61,6 +61,9 @@ EXPORTS = {
     "zmpo_renorm_workspace": ([c_void_p, ctypes.c_int, c_i64_p], ctypes.c_int),
     "zmpo_renorm": ([c_void_p, ctypes.c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                      ctypes.c_int, c_void_p], ctypes.c_int),
+    "zmpo_profile": ([c_void_p, ctypes.c_int], ctypes.c_int),
+    "zmpo_plan_launch_times": ([c_void_p, ctypes.c_int, ctypes.c_int, c_dbl_p, c_dbl_p, c_i64_p],
+                               ctypes.c_int),
     "zmpo_plan_destroy": ([c_void_p, ctypes.c_int], ctypes.c_int),
 }
 

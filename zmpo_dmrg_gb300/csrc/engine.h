@@ -52,6 +52,12 @@ struct Step {
   double flops = 0.0;            // sum of 2*m*n*k of the reference tasks
   int64_t ntasks = 0;
   bool uploaded = false;         // device copies are made on first use
+  double alg_bytes = 0.0;        // each operand tensor read once + output written once
+  // profiling (zmpo_profile): events around the launch, accumulated time
+  void *ev0 = nullptr, *ev1 = nullptr;
+  bool ev_pending = false;
+  double ms_total = 0.0;
+  int64_t ncalls = 0;
 };
 
 // Launchers (kernels.cu)

@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <memory>
 #include <mutex>
 #include <numeric>
@@ -347,6 +348,25 @@ static std::vector<Leg2> merge_legs(const std::vector<Leg2> &in) {
 static int build_step(std::vector<OutWork> &works, Step &st) {
   st.segs.clear();
   st.groups.clear();
+  {
+    // algorithmic traffic: every distinct operand tensor once, every output block once
+    std::map<std::tuple<int, int64_t, const Layout *>, int64_t> seen;
+    double out_elems = 0.0;
+    for (auto &w : works) {
+      int64_t od[16];
+      w.lo->block_dims(w.ob, od);
+      double n = 1;
+      for (int j = 0; j < w.lo->rank; ++j) n *= (double)od[j];
+      out_elems += n;
+      for (auto &t : w.tasks) {
+        seen[std::make_tuple(t.abuf, t.a_base, t.la)] = t.la->pk->size;
+        seen[std::make_tuple(t.bbuf, t.b_base, t.lb)] = t.lb->pk->size;
+      }
+    }
+    double in_elems = 0.0;
+    for (auto &kv : seen) in_elems += (double)kv.second;
+    st.alg_bytes = 8.0 * (in_elems + out_elems);
+  }
   for (auto &w : works) {
     const Layout &O = *w.lo;
     int64_t od[16], ost[16];
@@ -568,6 +588,9 @@ static int upload_step(Step &st) {
 }
 
 static void free_step(Step &st) {
+  if (st.ev0) cudaEventDestroy((cudaEvent_t)st.ev0);
+  if (st.ev1) cudaEventDestroy((cudaEvent_t)st.ev1);
+  st.ev0 = st.ev1 = nullptr;
   cudaFree(st.d_segs);
   cudaFree(st.d_groups);
   cudaFree(st.d_work_fp64);
@@ -577,13 +600,43 @@ static void free_step(Step &st) {
   st.d_work_fp64 = st.d_work_tc = nullptr;
 }
 
+static bool g_profile = false;
+
+static void profile_collect(Step &st) {
+  if (!st.ev_pending) return;
+  cudaEventSynchronize((cudaEvent_t)st.ev1);
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, (cudaEvent_t)st.ev0, (cudaEvent_t)st.ev1) == cudaSuccess) {
+    st.ms_total += ms;
+    st.ncalls += 1;
+  }
+  st.ev_pending = false;
+}
+
 static int run_step(Step &st, const Bufs &b, int precision, void *stream) {
   int rc = upload_step(st);
   if (rc) return rc;
-  if (precision == ZMPO_PREC_FP64) return launch_step_fp64(st, b, stream);
-  if (precision == ZMPO_PREC_SPLIT) return launch_step_split(st, b, 4, stream);
-  if (precision == ZMPO_PREC_EMU64) return launch_step_split(st, b, 7, stream);
-  return fail(ZMPO_E_ARG, "unknown precision");
+  if (g_profile) {
+    profile_collect(st);
+    if (!st.ev0) {
+      cudaEventCreate((cudaEvent_t *)&st.ev0);
+      cudaEventCreate((cudaEvent_t *)&st.ev1);
+    }
+    cudaEventRecord((cudaEvent_t)st.ev0, (cudaStream_t)stream);
+  }
+  if (precision == ZMPO_PREC_FP64)
+    rc = launch_step_fp64(st, b, stream);
+  else if (precision == ZMPO_PREC_SPLIT)
+    rc = launch_step_split(st, b, 4, stream);
+  else if (precision == ZMPO_PREC_EMU64)
+    rc = launch_step_split(st, b, 7, stream);
+  else
+    return fail(ZMPO_E_ARG, "unknown precision");
+  if (g_profile && rc == ZMPO_OK) {
+    cudaEventRecord((cudaEvent_t)st.ev1, (cudaStream_t)stream);
+    st.ev_pending = true;
+  }
+  return rc;
 }
 
 static Plan *get_plan(zmpo_engine *e, int id, int kind) {
@@ -1163,6 +1216,28 @@ int zmpo_renorm(zmpo_engine *e, int plan_id, const double *d_env, const double *
   for (auto &s : P->steps) {
     int rc = run_step(s, b, precision, stream);
     if (rc) return rc;
+  }
+  return ZMPO_OK;
+}
+
+int zmpo_profile(zmpo_engine *e, int on) {
+  if (!e) return fail(ZMPO_E_ARG, "profile: null engine");
+  g_profile = on != 0;
+  return ZMPO_OK;
+}
+
+int zmpo_plan_launch_times(zmpo_engine *e, int plan_id, int nmax, double *ms_avg, double *alg_bytes,
+                           int64_t *ncalls) {
+  Plan *P = get_plan(e, plan_id, 0);
+  if (!P) return fail(ZMPO_E_ID, "launch_times: unknown plan");
+  for (int s = 0; s < (int)P->steps.size() && s < nmax; ++s) {
+    Step &st = P->steps[s];
+    profile_collect(st);
+    if (ms_avg) ms_avg[s] = st.ncalls ? st.ms_total / (double)st.ncalls : 0.0;
+    if (alg_bytes) alg_bytes[s] = st.alg_bytes;
+    if (ncalls) ncalls[s] = st.ncalls;
+    st.ms_total = 0.0;
+    st.ncalls = 0;
   }
   return ZMPO_OK;
 }

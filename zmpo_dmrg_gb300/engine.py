@@ -113,6 +113,17 @@ class Engine:
                                          ctypes.byref(nl)), "plan_stats")
         return fl.value, nt.value, nl.value
 
+    def profile(self, on=True):
+        check(_lib.lib().zmpo_profile(self.h, 1 if on else 0), "profile")
+
+    def launch_times(self, pid, nmax=8):
+        ms = numpy.zeros(nmax)
+        by = numpy.zeros(nmax)
+        nc = numpy.zeros(nmax, dtype=numpy.int64)
+        check(_lib.lib().zmpo_plan_launch_times(self.h, pid, nmax, dptr(ms), dptr(by), lptr(nc)),
+              "launch_times")
+        return ms, by, nc
+
     def destroy_plan(self, pid):
         check(_lib.lib().zmpo_plan_destroy(self.h, pid), "plan_destroy")
 
