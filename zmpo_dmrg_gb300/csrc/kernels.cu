@@ -104,35 +104,51 @@ int launch_step_fp64(const Step &s, const Bufs &b, void *stream) {
 }
 
 // ------------------------------------------------------- split (tensor core)
-constexpr int S_TM = 32, S_TN = 32, S_TK = 32, S_NT = 128;
-constexpr int S_PAD = 40;  // bf16 row stride of a digit plane (bank-conflict free)
+// Tile: 128 rows (one thread per row of A) x TN (8 or 16) columns, K packed
+// in chunks of 32 slots: consecutive segments of the group fill the slots of
+// a chunk (a short block product does not waste a whole chunk).  Per chunk:
+// shared power-of-two scale per row of A / column of B over the chunk, S
+// exact 8-bit digit planes in shared memory, digit products per level on the
+// BF16 tensor cores (exact in FP32: level sums < 2^24), level sums scaled and
+// added to a two-float accumulator.  Integer->float conversions stay 32-bit:
+// 64-bit conversions issue on the FP64 pipe, which is narrow on GB300.
+constexpr int T_TM = 128, T_TK = 32, T_NT = 128, T_PAD = 40;
 
 // biased exponent of a double (0 for zero / denormal)
 __device__ __forceinline__ int dexp(double x) {
-  return (int)((__double_as_longlong(x) >> 52) & 0x7ff);
+  return (int)(((unsigned)__double2hiint(x) >> 20) & 0x7ffu);
 }
 
-// 8-bit digits of |x| * 2^(8S - (E - 1022)) where E >= biased exponent of x;
-// returns the signed digits (most significant first) as floats.
+// small non-negative integer (< 2^23) to float without a conversion unit
+__device__ __forceinline__ float small_u2f(unsigned d) {
+  return __uint_as_float(0x4B000000u | d) - 8388608.0f;
+}
+
+// S signed 8-bit digits of |x| / 2^(E-1022), most significant first, packed
+// as bf16 (exact: |digit| <= 255).
 template <int S>
-__device__ __forceinline__ void digits(double x, int E, float *d) {
-  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-  const int e = (int)((bits >> 52) & 0x7ff);
-  const float sg = (bits >> 63) ? -1.f : 1.f;
+__device__ __forceinline__ void digits_bf16(double x, int E, __nv_bfloat16 *d, int stride) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const int e = (int)((hi >> 20) & 0x7ffu);
   unsigned long long X = 0ull;
   if (e != 0) {
-    const unsigned long long mant = (bits & 0xfffffffffffffull) | (1ull << 52);
-    const int sh = e - E + 8 * S - 53;  // X = mant * 2^sh, X < 2^(8S)
+    const unsigned long long mant = ((unsigned long long)((hi & 0xfffffu) | 0x100000u) << 32) | lo;
+    const int sh = e - E + 8 * S - 53;
     if (sh >= 0)
       X = mant << sh;
     else if (sh > -64)
       X = mant >> (-sh);
   }
+  const unsigned sgn = hi & 0x80000000u;
 #pragma unroll
-  for (int s = 0; s < S; ++s) d[s] = sg * (float)((X >> (8 * (S - 1 - s))) & 0xffull);
+  for (int s = 0; s < S; ++s) {
+    const unsigned dig = (unsigned)(X >> (8 * (S - 1 - s))) & 0xffu;
+    const float f = __uint_as_float(__float_as_uint(small_u2f(dig)) | sgn);
+    d[s * stride] = __float2bfloat16_rn(f);
+  }
 }
 
-// exact power of two 2^k as a float scale applied in two steps
+// exact power of two 2^k times v (two steps below the normal range)
 __device__ __forceinline__ float scale_pow2(float v, int k) {
   if (k >= -126) {
     if (k > 127) k = 127;
@@ -158,175 +174,218 @@ __device__ __forceinline__ void mma_bf16(float *c, const uint32_t *a, const uint
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-template <int S>
-__global__ void __launch_bounds__(S_NT)
-k_step_split(const Work *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
-             const Seg *__restrict__ segs, Bufs bufs) {
+struct Slot {
+  const double *a;  // A(row 0, k) of the slot's segment
+  const double *b;  // B(k, col 0)
+  int64_t sam, sbn;
+  double alpha;
+};
+
+template <int S, int TN>
+__global__ void __launch_bounds__(T_NT)
+k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
+          const Seg *__restrict__ segs, Bufs bufs) {
+  constexpr int NTL = TN / 8;  // n8 tiles per warp
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double *Ad = reinterpret_cast<double *>(smem_raw);            // [TM][TK]
-  double *Bd = Ad + S_TM * S_TK;                                // [TN][TK]
-  __nv_bfloat16 *Ap = reinterpret_cast<__nv_bfloat16 *>(Bd + S_TN * S_TK);  // [S][TM][PAD]
-  __nv_bfloat16 *Bp = Ap + S * S_TM * S_PAD;                    // [S][TN][PAD]
-  int *Ea = reinterpret_cast<int *>(Bp + S * S_TN * S_PAD);     // [TM]
-  int *Eb = Ea + S_TM;                                          // [TN]
+  __nv_bfloat16 *Ap = reinterpret_cast<__nv_bfloat16 *>(smem_raw);  // [S][TM][PAD]
+  __nv_bfloat16 *Bp = Ap + S * T_TM * T_PAD;                        // [S][TN][PAD]
+  int *Ea = reinterpret_cast<int *>(Bp + S * TN * T_PAD);           // [TM]
+  int *Eb = Ea + T_TM;                                              // [TN]
+  Slot *slots = reinterpret_cast<Slot *>(Eb + 16);                  // [TK]
+  int *ctl = reinterpret_cast<int *>(slots + T_TK);                 // nslot, si, ki
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = (warp >> 1) * 16, wn = (warp & 1) * 16;  // warp tile origin
+  const int wm = warp * 32;  // 32 rows (two m16 tiles) per warp
   const int gq = lane >> 2, tq = lane & 3;
 
   for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
     const Work wk = work[w];
     const Group g = groups[wk.group];
-    const int m0 = wk.mt * S_TM, n0 = wk.nt * S_TN;
-    // two-float accumulators: [ntile 0..1][c 0..3]
-    float hi[8], lo[8];
+    const int m0 = wk.mt * T_TM, n0 = wk.nt * TN;
+    float hi[2][NTL][4], lo[2][NTL][4];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) hi[i] = lo[i] = 0.f;
-
-    for (int si = 0; si < g.nseg; ++si) {
-      const Seg s = segs[g.seg0 + si];
-      const double *A = bufs.p[s.abuf] + s.a_off;
-      const double *B = bufs.p[s.bbuf] + s.b_off;
-      const bool a_kfast = s.sak == 1, b_nfast = s.sbn == 1;
-      const bool unit_alpha = s.alpha == 1.0;
-      const float ahi = (float)s.alpha;
-      const float alo = (float)(s.alpha - (double)ahi);
-      for (int k0 = 0; k0 < s.K; k0 += S_TK) {
-        // 1. stage FP64 operands
-        for (int e = tid; e < S_TM * S_TK; e += S_NT) {
-          int r, k;
-          if (a_kfast) { r = e / S_TK; k = e % S_TK; } else { r = e % S_TM; k = e / S_TM; }
-          double v = 0.0;
-          if (m0 + r < g.M && k0 + k < s.K) v = A[(int64_t)(m0 + r) * s.sam + (int64_t)(k0 + k) * s.sak];
-          Ad[r * S_TK + k] = v;
-        }
-        for (int e = tid; e < S_TN * S_TK; e += S_NT) {
-          int c, k;
-          if (b_nfast) { k = e / S_TN; c = e % S_TN; } else { c = e / S_TK; k = e % S_TK; }
-          double v = 0.0;
-          if (n0 + c < g.N && k0 + k < s.K) v = B[(int64_t)(k0 + k) * s.sbk + (int64_t)(n0 + c) * s.sbn];
-          Bd[c * S_TK + k] = v;
-        }
-        __syncthreads();
-        // 2. shared exponent per row of A / column of B (4 threads per line)
-        {
-          const int line = tid >> 2, part = tid & 3;
-          int ea = 0, eb = 0;
+    for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-          for (int k = part * 8; k < part * 8 + 8; ++k) {
-            ea = max(ea, dexp(Ad[line * S_TK + k]));
-            eb = max(eb, dexp(Bd[line * S_TK + k]));
+      for (int nt = 0; nt < NTL; ++nt)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) hi[mt][nt][i] = lo[mt][nt][i] = 0.f;
+    if (tid == 0) {
+      ctl[1] = 0;
+      ctl[2] = 0;
+    }
+    __syncthreads();
+    while (ctl[1] < g.nseg) {
+      // 1. slot table for this chunk (one thread; at most 32 entries)
+      if (tid == 0) {
+        int si = ctl[1], ki = ctl[2], j = 0;
+        while (j < T_TK && si < g.nseg) {
+          const Seg sg = segs[g.seg0 + si];
+          const double *A = bufs.p[sg.abuf] + sg.a_off;
+          const double *B = bufs.p[sg.bbuf] + sg.b_off;
+          const int take = min(T_TK - j, sg.K - ki);
+          for (int t = 0; t < take; ++t) {
+            slots[j + t].a = A + (int64_t)(ki + t) * sg.sak;
+            slots[j + t].b = B + (int64_t)(ki + t) * sg.sbk;
+            slots[j + t].sam = sg.sam;
+            slots[j + t].sbn = sg.sbn;
+            slots[j + t].alpha = sg.alpha;
           }
-          ea = max(ea, __shfl_xor_sync(0xffffffffu, ea, 1));
-          ea = max(ea, __shfl_xor_sync(0xffffffffu, ea, 2));
-          eb = max(eb, __shfl_xor_sync(0xffffffffu, eb, 1));
-          eb = max(eb, __shfl_xor_sync(0xffffffffu, eb, 2));
-          if (part == 0) {
-            Ea[line] = ea;
-            Eb[line] = eb;
+          j += take;
+          ki += take;
+          if (ki >= sg.K) {
+            ++si;
+            ki = 0;
           }
         }
-        __syncthreads();
-        // 3. digit planes
-        for (int e = tid; e < S_TM * S_TK; e += S_NT) {
-          const int r = e / S_TK, k = e % S_TK;
-          float d[S];
-          digits<S>(Ad[e], Ea[r], d);
+        ctl[0] = j;
+        ctl[1] = si;
+        ctl[2] = ki;
+      }
+      __syncthreads();
+      const int nslot = ctl[0];
+      // 2. A: thread = row; chunk max exponent then digit planes
+      {
+        const int row = m0 + tid;
+        double v[T_TK];
+        int emax = 0;
 #pragma unroll
-          for (int p = 0; p < S; ++p) Ap[(p * S_TM + r) * S_PAD + k] = __float2bfloat16_rn(d[p]);
-          digits<S>(Bd[e], Eb[r], d);
-#pragma unroll
-          for (int p = 0; p < S; ++p) Bp[(p * S_TN + r) * S_PAD + k] = __float2bfloat16_rn(d[p]);
+        for (int j = 0; j < T_TK; ++j) {
+          double x = 0.0;
+          if (j < nslot && row < g.M) {
+            const Slot &sl = slots[j];
+            x = __ldg(sl.a + (int64_t)row * sl.sam);
+            if (sl.alpha != 1.0) x *= sl.alpha;
+          }
+          v[j] = x;
+          emax = max(emax, dexp(x));
         }
-        __syncthreads();
-        // 4. digit products per level l = s + t (levels 0..S-1 here), exact
-        float acc[S][8];
+        Ea[tid] = emax;
 #pragma unroll
-        for (int l = 0; l < S; ++l)
+        for (int j = 0; j < T_TK; ++j) digits_bf16<S>(v[j], emax, Ap + tid * T_PAD + j, T_TM * T_PAD);
+      }
+      // 3. B: TN columns, 128/TN threads per column share the 32 slots
+      {
+        constexpr int TPC = T_NT / TN;  // threads per column
+        constexpr int KPT = T_TK / TPC; // slots per thread
+        const int c = tid / TPC, part = tid % TPC;
+        const int col = n0 + c;
+        double v[KPT];
+        int emax = 0;
 #pragma unroll
-          for (int i = 0; i < 8; ++i) acc[l][i] = 0.f;
+        for (int t = 0; t < KPT; ++t) {
+          const int j = part * KPT + t;
+          double x = 0.0;
+          if (j < nslot && col < g.N) x = __ldg(slots[j].b + (int64_t)col * slots[j].sbn);
+          v[t] = x;
+          emax = max(emax, dexp(x));
+        }
 #pragma unroll
-        for (int kk = 0; kk < S_TK; kk += 16) {
+        for (int o = 1; o < TPC; o <<= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        if (part == 0) Eb[c] = emax;
 #pragma unroll
-          for (int sa = 0; sa < S; ++sa) {
+        for (int t = 0; t < KPT; ++t)
+          digits_bf16<S>(v[t], emax, Bp + c * T_PAD + part * KPT + t, TN * T_PAD);
+      }
+      __syncthreads();
+      // 4. digit products per level, exact in FP32
+      float acc[S][2][NTL][4];
+#pragma unroll
+      for (int l = 0; l < S; ++l)
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+          for (int nt = 0; nt < NTL; ++nt)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) acc[l][mt][nt][i] = 0.f;
+#pragma unroll
+      for (int kk = 0; kk < T_TK; kk += 16) {
+        uint32_t bf[S][NTL][2];
+#pragma unroll
+        for (int sb = 0; sb < S; ++sb)
+#pragma unroll
+          for (int nt = 0; nt < NTL; ++nt) {
+            const __nv_bfloat16 *bp = Bp + (sb * TN + nt * 8 + gq) * T_PAD + kk;
+            bf[sb][nt][0] = *reinterpret_cast<const uint32_t *>(bp + 2 * tq);
+            bf[sb][nt][1] = *reinterpret_cast<const uint32_t *>(bp + 2 * tq + 8);
+          }
+#pragma unroll
+        for (int sa = 0; sa < S; ++sa) {
+#pragma unroll
+          for (int mt = 0; mt < 2; ++mt) {
             uint32_t af[4];
-            const __nv_bfloat16 *ap = Ap + (sa * S_TM + wm) * S_PAD + kk;
-            af[0] = *reinterpret_cast<const uint32_t *>(ap + gq * S_PAD + 2 * tq);
-            af[1] = *reinterpret_cast<const uint32_t *>(ap + (gq + 8) * S_PAD + 2 * tq);
-            af[2] = *reinterpret_cast<const uint32_t *>(ap + gq * S_PAD + 2 * tq + 8);
-            af[3] = *reinterpret_cast<const uint32_t *>(ap + (gq + 8) * S_PAD + 2 * tq + 8);
+            const __nv_bfloat16 *ap = Ap + (sa * T_TM + wm + mt * 16) * T_PAD + kk;
+            af[0] = *reinterpret_cast<const uint32_t *>(ap + gq * T_PAD + 2 * tq);
+            af[1] = *reinterpret_cast<const uint32_t *>(ap + (gq + 8) * T_PAD + 2 * tq);
+            af[2] = *reinterpret_cast<const uint32_t *>(ap + gq * T_PAD + 2 * tq + 8);
+            af[3] = *reinterpret_cast<const uint32_t *>(ap + (gq + 8) * T_PAD + 2 * tq + 8);
 #pragma unroll
-            for (int sb = 0; sb + sa < S; ++sb) {
+            for (int sb = 0; sb + sa < S; ++sb)
 #pragma unroll
-              for (int nt = 0; nt < 2; ++nt) {
-                uint32_t bf[2];
-                const __nv_bfloat16 *bp = Bp + (sb * S_TN + wn + nt * 8 + gq) * S_PAD + kk;
-                bf[0] = *reinterpret_cast<const uint32_t *>(bp + 2 * tq);
-                bf[1] = *reinterpret_cast<const uint32_t *>(bp + 2 * tq + 8);
-                mma_bf16(&acc[sa + sb][nt * 4], af, bf);
-              }
-            }
+              for (int nt = 0; nt < NTL; ++nt) mma_bf16(acc[sa + sb][mt][nt], af, bf[sb][nt]);
           }
         }
-        // 5. scale each level by 2^(Ea + Eb - 2044 - 8(l+2)) and accumulate
+      }
+      // 5. scale levels by 2^(Ea + Eb - 2044 - 8(l+2)) into the two-float sums
 #pragma unroll
-        for (int nt = 0; nt < 2; ++nt) {
+      for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < NTL; ++nt)
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
-            const int r = wm + gq + (i >> 1) * 8;
-            const int c = wn + nt * 8 + 2 * tq + (i & 1);
-            const int base = Ea[r] + Eb[c] - 2044;
-            if (Ea[r] == 0 || Eb[c] == 0) continue;
+            const int r = wm + mt * 16 + gq + (i >> 1) * 8;
+            const int c = nt * 8 + 2 * tq + (i & 1);
+            const int ea = Ea[r], eb = Eb[c];
+            if (ea == 0 || eb == 0) continue;
+            const int base = ea + eb - 2044;
 #pragma unroll
-            for (int l = 0; l < S; ++l) {
-              const float x = scale_pow2(acc[l][nt * 4 + i], base - 8 * (l + 2));
-              if (unit_alpha) {
-                two_sum_acc(hi[nt * 4 + i], lo[nt * 4 + i], x);
-              } else {
-                const float p = x * ahi;
-                const float pe = fmaf(x, ahi, -p) + x * alo;
-                two_sum_acc(hi[nt * 4 + i], lo[nt * 4 + i], p);
-                lo[nt * 4 + i] += pe;
-              }
-            }
+            for (int l = 0; l < S; ++l)
+              two_sum_acc(hi[mt][nt][i], lo[mt][nt][i], scale_pow2(acc[l][mt][nt][i], base - 8 * (l + 2)));
           }
-        }
-        __syncthreads();
-      }
+      __syncthreads();
     }
     double *C = bufs.p[g.cbuf] + g.c_off;
 #pragma unroll
-    for (int nt = 0; nt < 2; ++nt) {
+    for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const int r = m0 + wm + gq + (i >> 1) * 8;
-        const int c = n0 + wn + nt * 8 + 2 * tq + (i & 1);
-        if (r < g.M && c < g.N)
-          C[(int64_t)r * g.scm + (int64_t)c * g.scn] = (double)hi[nt * 4 + i] + (double)lo[nt * 4 + i];
-      }
-    }
+      for (int nt = 0; nt < NTL; ++nt)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int r = m0 + wm + mt * 16 + gq + (i >> 1) * 8;
+          const int c = n0 + nt * 8 + 2 * tq + (i & 1);
+          if (r < g.M && c < g.N)
+            C[(int64_t)r * g.scm + (int64_t)c * g.scn] = (double)hi[mt][nt][i] + (double)lo[mt][nt][i];
+        }
+    __syncthreads();
   }
 }
 
-template <int S>
-static int launch_split_t(const Step &s, const Bufs &b, void *stream) {
-  const size_t smem = (size_t)(S_TM + S_TN) * S_TK * sizeof(double) +
-                      (size_t)S * (S_TM + S_TN) * S_PAD * sizeof(__nv_bfloat16) +
-                      (size_t)(S_TM + S_TN) * sizeof(int);
+template <int S, int TN>
+static int launch_tc_t(const Work *work, int64_t nwork, const Step &s, const Bufs &b, void *stream) {
+  if (nwork == 0) return ZMPO_OK;
+  const size_t smem = (size_t)S * (T_TM + TN) * T_PAD * sizeof(__nv_bfloat16) +
+                      (size_t)(T_TM + 16) * sizeof(int) + T_TK * sizeof(Slot) + 4 * sizeof(int) + 16;
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_step_split<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_step_tc<S, TN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = true;
   }
-  k_step_split<S><<<grid_for(s.nwork_tc, 8), S_NT, smem, (cudaStream_t)stream>>>(
-      s.d_work_tc, s.nwork_tc, s.d_groups, s.d_segs, b);
-  return launch_error("k_step_split");
+  k_step_tc<S, TN><<<grid_for(nwork, 8), T_NT, smem, (cudaStream_t)stream>>>(work, nwork, s.d_groups,
+                                                                             s.d_segs, b);
+  return launch_error("k_step_tc");
 }
 
 int launch_step_split(const Step &s, const Bufs &b, int nslices, void *stream) {
-  if (s.nwork_tc == 0) return ZMPO_OK;
-  if (nslices == 4) return launch_split_t<4>(s, b, stream);
-  if (nslices == 7) return launch_split_t<7>(s, b, stream);
+  int rc;
+  if (nslices == 4) {
+    rc = launch_tc_t<4, 8>(s.d_work_tc8, s.nwork_tc8, s, b, stream);
+    if (rc) return rc;
+    return launch_tc_t<4, 16>(s.d_work_tc16, s.nwork_tc16, s, b, stream);
+  }
+  if (nslices == 7) {
+    rc = launch_tc_t<7, 8>(s.d_work_tc8, s.nwork_tc8, s, b, stream);
+    if (rc) return rc;
+    return launch_tc_t<7, 16>(s.d_work_tc16, s.nwork_tc16, s, b, stream);
+  }
   return record_arg_error("unsupported slice count");
 }
 

@@ -162,7 +162,8 @@ struct Plan {
   int kind = 0;  // 1 contract, 2 sigma, 3 renorm
   std::vector<Step> steps;
   int64_t ws_elems = 0;
-  double flops = 0.0;
+  double flops = 0.0;       // reference work F_ref (its task lists)
+  double exec_flops = 0.0;  // work of the executed task lists
   int64_t ntasks = 0;
   // contract
   int lay_out = -1;
@@ -310,6 +311,24 @@ static int build_contraction(zmpo_engine *e, int ia, int ib, int naxes, const in
   *out_layout = lo;
   *out_contr = (int)e->contractions.size() - 1;
   return ZMPO_OK;
+}
+
+// 2*m*n*k summed over the block tasks of a contraction (the reference's
+// tensordotCAL work on the same task list)
+static double contraction_flops(zmpo_engine *e, const Contraction *C) {
+  const Layout *A = get_layout(e, C->lay_a), *B = get_layout(e, C->lay_b);
+  double f = 0.0;
+  int64_t ad[16], bd[16];
+  for (const auto &t : C->tasks) {
+    A->block_dims(t.ab, ad);
+    B->block_dims(t.bb, bd);
+    double m = 1, n = 1, k = 1;
+    for (int j : C->e1) m *= (double)ad[j];
+    for (int j : C->e2) n *= (double)bd[j];
+    for (int j : C->i1) k *= (double)ad[j];
+    f += 2.0 * m * n * k;
+  }
+  return f;
 }
 
 // ------------------------------------------------------------ GEMM mapping
@@ -543,11 +562,11 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
 
 // tile sizes of the two kernels (must match kernels.cu)
 constexpr int kTileFP64M = 32, kTileFP64N = 32;
-constexpr int kTileTCM = 32, kTileTCN = 32;
+constexpr int kTileTCM = 128;
 
 static int upload_step(Step &st) {
   if (st.uploaded) return ZMPO_OK;
-  std::vector<Work> w64, wtc;
+  std::vector<Work> w64, wtc8, wtc16;
   // order groups by cost (longest first) for load balance
   std::vector<int> order(st.groups.size());
   std::iota(order.begin(), order.end(), 0);
@@ -562,11 +581,14 @@ static int upload_step(Step &st) {
     const Group &G = st.groups[g];
     for (int mt = 0; mt * kTileFP64M < G.M; ++mt)
       for (int nt = 0; nt * kTileFP64N < G.N; ++nt) w64.push_back({g, mt, nt, 0});
+    const int tn = G.N <= 8 ? 8 : 16;
+    auto &wl = tn == 8 ? wtc8 : wtc16;
     for (int mt = 0; mt * kTileTCM < G.M; ++mt)
-      for (int nt = 0; nt * kTileTCN < G.N; ++nt) wtc.push_back({g, mt, nt, 0});
+      for (int nt = 0; nt * tn < G.N; ++nt) wl.push_back({g, mt, nt, 0});
   }
   st.nwork_fp64 = (int64_t)w64.size();
-  st.nwork_tc = (int64_t)wtc.size();
+  st.nwork_tc8 = (int64_t)wtc8.size();
+  st.nwork_tc16 = (int64_t)wtc16.size();
   auto up = [](auto **dptr, const auto &v) -> cudaError_t {
     using T = typename std::remove_reference<decltype(v)>::type::value_type;
     if (v.empty()) {
@@ -580,7 +602,8 @@ static int upload_step(Step &st) {
   CUDA_TRY(up(&st.d_segs, st.segs));
   CUDA_TRY(up(&st.d_groups, st.groups));
   CUDA_TRY(up(&st.d_work_fp64, w64));
-  CUDA_TRY(up(&st.d_work_tc, wtc));
+  CUDA_TRY(up(&st.d_work_tc8, wtc8));
+  CUDA_TRY(up(&st.d_work_tc16, wtc16));
   // keep the host mirror of groups (sizes) but free the bulky segment copy
   std::vector<Seg>().swap(st.segs);
   st.uploaded = true;
@@ -594,10 +617,11 @@ static void free_step(Step &st) {
   cudaFree(st.d_segs);
   cudaFree(st.d_groups);
   cudaFree(st.d_work_fp64);
-  cudaFree(st.d_work_tc);
+  cudaFree(st.d_work_tc8);
+  cudaFree(st.d_work_tc16);
   st.d_segs = nullptr;
   st.d_groups = nullptr;
-  st.d_work_fp64 = st.d_work_tc = nullptr;
+  st.d_work_fp64 = st.d_work_tc8 = st.d_work_tc16 = nullptr;
 }
 
 static bool g_profile = false;
@@ -825,11 +849,16 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
     return fail(ZMPO_E_ARG, "sigma_plan: bad descriptor");
   const Layout *Psi = get_layout(e, d->lay_psi);
   if (!Psi) return fail(ZMPO_E_ID, "sigma_plan: unknown psi layout");
-  // per-class symbolic chain (the reference caches the same per icase0,
-  // mpo_dmrg_kernelQt.py:199-204)
+  // Per-class symbolic chains (the reference caches the same per icase0,
+  // mpo_dmrg_kernelQt.py:199-204).  The reference's two-site chain is
+  //   T1 = L.psi, T2 = T1.Wi, T3 = T2.Wj, sigma = T3.R   (kernelQt.py:270-306)
+  // and its tasks define the reported work F_ref.  The engine executes
+  //   O = Wi.Wj (over the shared MPO bond), T1 = L.psi, T3 = T1.O, sigma = T3.R
+  // which gives the same T3 layout without materialising T2.
   struct ClassChain {
-    bool built = false, empty = false;
-    std::vector<ChainStep> c;
+    bool built = false;
+    std::vector<ChainStep> c;  // executed steps
+    double ref_flops = 0.0;
   };
   std::vector<ClassChain> chains(d->nclass);
   static const int ax1a[1] = {2}, ax1b[1] = {0};
@@ -837,28 +866,48 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
   static const int ax3a[2] = {1, 3}, ax3b[2] = {3, 0};
   static const int ax4a[2] = {1, 3}, ax4b[2] = {2, 0};
   static const int ax3a1[2] = {1, 2}, ax3b1[2] = {2, 0};
+  static const int axOa[1] = {1}, axOb[1] = {0};
+  static const int axTa[3] = {0, 2, 3}, axTb[3] = {0, 2, 5};
   for (int op = 0; op < d->nop; ++op) {
     int c = d->op_class[op];
     if (c < 0 || c >= d->nclass) return fail(ZMPO_E_ARG, "sigma_plan: bad class");
     ClassChain &ch = chains[c];
     if (ch.built) continue;
     ch.built = true;
-    int lo, ci, rc;
-    rc = build_contraction(e, d->lay_L[c], d->lay_psi, 1, ax1a, ax1b, &lo, &ci);
+    int lo, ci, rc, l1, c1;
+    rc = build_contraction(e, d->lay_L[c], d->lay_psi, 1, ax1a, ax1b, &l1, &c1);
     if (rc) return rc;
-    ch.c.push_back({ci, lo});
-    rc = build_contraction(e, lo, d->lay_Wi[c], 2, ax2a, ax2b, &lo, &ci);
-    if (rc) return rc;
-    ch.c.push_back({ci, lo});
+    ch.ref_flops += contraction_flops(e, e->contractions[c1].get());
     if (d->ncsite == 2) {
-      rc = build_contraction(e, lo, d->lay_Wj[c], 2, ax3a, ax3b, &lo, &ci);
+      int l2, c2, l3, c3;
+      rc = build_contraction(e, l1, d->lay_Wi[c], 2, ax2a, ax2b, &l2, &c2);
       if (rc) return rc;
+      rc = build_contraction(e, l2, d->lay_Wj[c], 2, ax3a, ax3b, &l3, &c3);
+      if (rc) return rc;
+      ch.ref_flops += contraction_flops(e, e->contractions[c2].get()) +
+                      contraction_flops(e, e->contractions[c3].get());
+      int lO, cO;
+      rc = build_contraction(e, d->lay_Wi[c], d->lay_Wj[c], 1, axOa, axOb, &lO, &cO);
+      if (rc) return rc;
+      ch.c.push_back({cO, lO});
+      ch.c.push_back({c1, l1});
+      rc = build_contraction(e, l1, lO, 3, axTa, axTb, &lo, &ci);
+      if (rc) return rc;
+      const Layout *T3a = get_layout(e, l3), *T3b = get_layout(e, lo);
+      if (T3a->pk->flat != T3b->pk->flat || T3a->pk->size != T3b->pk->size)
+        return fail(ZMPO_E_SYM, "sigma_plan: fused MPO step layout differs");
       ch.c.push_back({ci, lo});
       rc = build_contraction(e, lo, d->lay_Rf[c], 2, ax4a, ax4b, &lo, &ci);
     } else {
+      ch.c.push_back({c1, l1});
+      rc = build_contraction(e, l1, d->lay_Wi[c], 2, ax2a, ax2b, &lo, &ci);
+      if (rc) return rc;
+      ch.ref_flops += contraction_flops(e, e->contractions[ci].get());
+      ch.c.push_back({ci, lo});
       rc = build_contraction(e, lo, d->lay_Rf[c], 2, ax3a1, ax3b1, &lo, &ci);
     }
     if (rc) return rc;
+    ch.ref_flops += contraction_flops(e, e->contractions[ci].get());
     ch.c.push_back({ci, lo});
     const Layout *Out = get_layout(e, lo);
     if (Out->pk->flat != Psi->pk->flat || Out->pk->size != Psi->pk->size)
@@ -867,9 +916,9 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
   auto P = std::make_unique<Plan>();
   P->kind = 2;
   P->ndim0 = Psi->pk->size;
-  const int nstep = d->ncsite == 2 ? 4 : 3;
-  // workspace offsets: per op, intermediates of steps 0..nstep-2
-  std::vector<std::vector<int64_t>> ws_off(d->nop, std::vector<int64_t>(nstep - 1, 0));
+  const int nstep = (int)chains[d->op_class[0 < d->nop ? 0 : 0]].c.size();
+  // workspace: per op, outputs of steps 0..nstep-2
+  std::vector<std::vector<int64_t>> ws_off(d->nop, std::vector<int64_t>(nstep, 0));
   int64_t ws = 0;
   for (int op = 0; op < d->nop; ++op) {
     const ClassChain &ch = chains[d->op_class[op]];
@@ -878,11 +927,28 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
       ws += get_layout(e, ch.c[s].lay)->pk->size;
       ws = (ws + 31) & ~int64_t(31);
     }
+    P->flops += ch.ref_flops;
   }
   P->ws_elems = ws;
   // buffers: 0 L, 1 R, 2 W, 3 x, 4 y, 5 workspace
+  // operand sources per executed step (two-site: O, T1, T3, sigma)
   for (int s = 0; s < nstep; ++s) {
     std::vector<OutWork> works;
+    auto src = [&](int op, bool isA, int &buf, int64_t &base) {
+      if (d->ncsite == 2) {
+        switch (s) {
+          case 0: buf = 2; base = isA ? d->off_Wi[op] : d->off_Wj[op]; return;
+          case 1: if (isA) { buf = 0; base = d->off_L[op]; } else { buf = 3; base = 0; } return;
+          case 2: buf = 5; base = isA ? ws_off[op][1] : ws_off[op][0]; return;
+          default: if (isA) { buf = 5; base = ws_off[op][2]; } else { buf = 1; base = d->off_R[op]; } return;
+        }
+      }
+      switch (s) {
+        case 0: if (isA) { buf = 0; base = d->off_L[op]; } else { buf = 3; base = 0; } return;
+        case 1: if (isA) { buf = 5; base = ws_off[op][0]; } else { buf = 2; base = d->off_Wi[op]; } return;
+        default: if (isA) { buf = 5; base = ws_off[op][1]; } else { buf = 1; base = d->off_R[op]; } return;
+      }
+    };
     if (s < nstep - 1) {
       for (int op = 0; op < d->nop; ++op) {
         const ClassChain &ch = chains[d->op_class[op]];
@@ -891,13 +957,8 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
                      *O = get_layout(e, C->lay_out);
         int abuf, bbuf;
         int64_t abase, bbase;
-        if (s == 0) {
-          abuf = 0; abase = d->off_L[op];
-          bbuf = 3; bbase = 0;
-        } else {
-          abuf = 5; abase = ws_off[op][s - 1];
-          bbuf = 2; bbase = (s == 1) ? d->off_Wi[op] : d->off_Wj[op];
-        }
+        src(op, true, abuf, abase);
+        src(op, false, bbuf, bbase);
         for (size_t ob = 0; ob < O->pk->flat.size(); ++ob) {
           OutWork w;
           w.lo = O;
@@ -923,16 +984,20 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
         const Contraction *C = e->contractions[ch.c[s].contr].get();
         const Layout *A = get_layout(e, C->lay_a), *B = get_layout(e, C->lay_b),
                      *O = get_layout(e, C->lay_out);
+        int abuf, bbuf;
+        int64_t abase, bbase;
+        src(op, true, abuf, abase);
+        src(op, false, bbuf, bbase);
         for (size_t ob = 0; ob < O->pk->flat.size(); ++ob)
           for (int64_t t = C->task_start[ob]; t < C->task_start[ob + 1]; ++t)
-            works[ob].tasks.push_back({C, A, B, O, C->tasks[t].ab, C->tasks[t].bb,
-                                       ws_off[op][s - 1], d->off_R[op], 5, 1, d->wts[op]});
+            works[ob].tasks.push_back({C, A, B, O, C->tasks[t].ab, C->tasks[t].bb, abase, bbase, abuf,
+                                       bbuf, d->wts[op]});
       }
     }
     P->steps.emplace_back();
     int rc = build_step(works, P->steps.back());
     if (rc) return rc;
-    P->flops += P->steps.back().flops;
+    P->exec_flops += P->steps.back().flops;
     P->ntasks += P->steps.back().ntasks;
   }
   // ---- HDiag terms: out[l,r] += w * sum Ld[a,l] Wi[a,b] (Wj[b,c]) Rd[c,r]
