@@ -14,10 +14,14 @@ Vectors may be NumPy (copied to and from the device) or float64 CUDA tensors
 (kept on the device).  Every product runs in the engine; there is no host
 fallback.
 """
+import itertools
+
 import numpy
 
 from . import engine as _engine
 from .qtensor import qtensor
+
+_serial = itertools.count()
 
 
 class EnvSet:
@@ -25,6 +29,7 @@ class EnvSet:
     per-site HDF5 file ``lop_site_i`` / ``rop_site_i`` with datasets ``opers{p}``)."""
 
     def __init__(self, buf, off, layouts, tensors):
+        self.uid = next(_serial)  # plan caches key on this, never on id()
         self.buf = buf            # torch float64 CUDA tensor
         self.off = off            # [nop] element offsets (-1: absent)
         self.layouts = layouts    # [nop] engine layout ids (-1: absent)
@@ -38,6 +43,7 @@ class MPOStore:
     """All MPO site tensors on the device (replaces the reference's ``hop`` file)."""
 
     def __init__(self, buf, off, tensors):
+        self.uid = next(_serial)
         self.buf = buf            # torch float64 CUDA tensor
         self.off = off            # off[isite][iop]
         self.tensors = tensors    # tensors[isite][iop] host qtensor
@@ -115,7 +121,7 @@ class SigmaPlan:
 def _sigma_plan(info):
     dmrg, isite, ncsite, flst, status, ifsym = info
     fL, fR = flst[0][0:2]
-    key = (id(fL), id(fR), isite, ncsite, dmrg.qtmp_psi_layout)
+    key = (fL.uid, fR.uid, isite, ncsite, dmrg.qtmp_psi_layout, dmrg.mpo_store.uid)
     cur = getattr(dmrg, "_sigma_plan", None)
     if cur is None or cur[0] != key:
         if cur is not None:
