@@ -134,8 +134,10 @@ class mpo_dmrg:
         self.int1e = None
         self.int2e = None
         self.hpwts = None
-        # engine options
+        # engine options: precision of H.psi inside Davidson, of the final
+        # Rayleigh quotient of each converged vector, and of the renormalisation
         self.precision = "fp64"
+        self.precision_final = "emu64"
         self.precision_renorm = "fp64"
         self.rng = numpy.random.default_rng(seed)
         # device state
@@ -348,10 +350,20 @@ class mpo_dmrg:
             solver.neig = neig
             solver.diag = diag
             solver.noise = self.ifdvdnz and (self.noise > 1.e-10)
+            solver.hvec_eps = {"fp64": 0.0, "emu64": 1e-14, "split": 1e-8}[self.precision]
             v0 = None
             if self.psi0 is not None:
                 v0 = self.psi0[ioff:ioff + neig][:, prjmap].copy()
             eig, vec, nmvp = solver.solve_iter(v0=v0, iop=4)
+            if self.precision == "split":
+                # energy error is second order in the vector error: one
+                # Rayleigh quotient per vector with the 56-bit product
+                saved = self.precision
+                self.precision = self.precision_final
+                for i in range(neig):
+                    hv = HVec(vec[i].contiguous(), info, ndim0, prjmap)
+                    eig[i] = float(torch.dot(vec[i], hv) / torch.dot(vec[i], vec[i]))
+                self.precision = saved
             civec = numpy.zeros((neig, ndim))
             civec[:, prjmap] = vec.cpu().numpy()
             civecs.append(civec)

@@ -71,6 +71,9 @@ class eigenSolver:
         self.ifall = True
         self.nfac = 10
         self.ifconv = False
+        # relative accuracy of H.v (0 for FP64); bounds the symmetry check and
+        # the reachable residual of a split-precision product
+        self.hvec_eps = 0.0
         self.rng = rng if rng is not None else numpy.random.default_rng(0)
 
     def HVecs(self, vbas):
@@ -114,7 +117,8 @@ class eigenSolver:
             if numpy.linalg.norm(iden - numpy.identity(ndim)) > 1.e-10:
                 raise RuntimeError("Davidson: basis lost orthonormality")
             tmpH = (vbas @ wbas.T).cpu().numpy()
-            if numpy.linalg.norm(tmpH - tmpH.T) > 1.e-10:
+            tol_sym = max(1.e-10, 100.0 * self.hvec_eps * numpy.linalg.norm(tmpH))
+            if numpy.linalg.norm(tmpH - tmpH.T) > tol_sym:
                 raise RuntimeError("Davidson: subspace H not symmetric")
             tmpH = 0.5 * (tmpH + tmpH.T)
             eig, vr = numpy.linalg.eigh(tmpH)
@@ -126,7 +130,8 @@ class eigenSolver:
             xbas = vr_d @ vbas
             rbas = vr_d @ wbas - torch.as_tensor(eigs, device=dev)[:, None] * xbas
             rn = torch.linalg.norm(rbas, dim=1).cpu().numpy()
-            rconv = [rn[i] <= self.crit_vec for i in range(neig)]
+            crit = max(self.crit_vec, 10.0 * self.hvec_eps * max(1.0, float(numpy.abs(eigs).max())))
+            rconv = [rn[i] <= crit for i in range(neig)]
             rindx = [i for i in range(neig) if not rconv[i] and not econv[i]]
             self.rnorm = rn
             if not rindx or niter == self.maxcycle - 1:
