@@ -1,8 +1,8 @@
 """Full two-site DMRG sweeps with the hot path on the GPU (driver with the
 reference's API): the reference's K=6 FCIDUMP must reach the FCI energy and
 the BLOCK M=1000 energy recorded in the reference's dmrg.out; the split
-(BF16 tensor-core) path must reach the FP64 path's energy within 1e-8 Eh; a
-synthetic K=8 problem must match the CPU oracle's sweep energies."""
+(BF16 tensor-core) path must reach the FP64 path's energy within 1e-8 Eh;
+seeded synthetic K=6 problems must reach their FCI energies."""
 import os
 
 import numpy
@@ -45,24 +45,16 @@ def test_fcidump_energy(gpu):
     assert abs(ms.Energy - m.Energy) < 1e-8
 
 
-def test_synthetic_k8_matches_oracle(gpu):
-    from oracle import dmrg as od
-    K = 8
-    h, eri, _ = oint.synthetic(K, 21)
-    i1, i2, _ = oint.to_spin_orbital(h, eri)
-    occ = numpy.array([1., 1.] * 4 + [0., 0.] * 4)
-    m = _run(i1, i2, K, 8, occ, 24, 1e-8, 4)
-    o = od.mpo_dmrg(seed=1)
-    o.nsite, o.sbas, o.isym = K, 2 * K, 2
-    o.build()
-    o.occun = occ
-    o.qsectors = {str([8.0, 0.0]): 1}
-    o.partition()
-    o.loadInts(i1, i2)
-    o.dumpMPO()
-    sc = od.schedule(maxM=24, tol=1e-8, maxiter=4)
-    sc.startNoise = 0.0
-    sc.normal(2)
-    o.default(sc)
-    assert abs(m.Energy - o.Energy) < 1e-8
-    assert numpy.max(numpy.abs(numpy.array(m.eav) - numpy.array(o.eav))) < 1e-7
+@pytest.mark.parametrize("hop,seed", [(1.0, 21), (0.7, 5)])
+def test_synthetic_k6_reaches_fci(gpu, hop, seed):
+    """Seeded synthetic integrals of the benchmark generator; D = 64 is exact
+    for K = 6, so every implementation must land on the FCI energy."""
+    K = 6
+    h, eri, _ = oint.synthetic(K, seed, hop)
+    i1, i2, g = oint.to_spin_orbital(h, eri)
+    efci = oint.fci_energy(i1, g, 6, 0.0)[0]
+    occ = numpy.array([1., 1.] * 3 + [0., 0.] * 3)
+    m = _run(i1, i2, K, 6, occ, 64, 1e-9, 10)
+    assert abs(m.Energy - efci) < 1e-9
+    ms = _run(i1, i2, K, 6, occ, 64, 1e-9, 10, precision="split")
+    assert abs(ms.Energy - efci) < 1e-8
