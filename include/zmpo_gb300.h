@@ -164,6 +164,12 @@ int zmpo_profile(zmpo_engine *e, int on);
 int zmpo_plan_launch_times(zmpo_engine *e, int plan_id, int nmax, double *ms_avg,
                            double *alg_bytes, int64_t *ncalls);
 
+/* Introspection of a launch of a plan before its first execution: number of
+ * output groups and, when M is non-NULL, per group its rows, columns, number
+ * of block products and summed K (used to choose tile shapes). */
+int zmpo_plan_groups(zmpo_engine *e, int plan_id, int step, int64_t *ngroups,
+                     int32_t *M, int32_t *N, int32_t *nseg, int64_t *ktot);
+
 /* Release a contraction / sigma / renorm plan. */
 int zmpo_plan_destroy(zmpo_engine *e, int plan_id);
 

@@ -64,6 +64,8 @@ EXPORTS = {
     "zmpo_profile": ([c_void_p, ctypes.c_int], ctypes.c_int),
     "zmpo_plan_launch_times": ([c_void_p, ctypes.c_int, ctypes.c_int, c_dbl_p, c_dbl_p, c_i64_p],
                                ctypes.c_int),
+    "zmpo_plan_groups": ([c_void_p, ctypes.c_int, ctypes.c_int, c_i64_p, c_int_p, c_int_p, c_int_p,
+                          c_i64_p], ctypes.c_int),
     "zmpo_plan_destroy": ([c_void_p, ctypes.c_int], ctypes.c_int),
 }
 

@@ -29,6 +29,17 @@ struct Group {
   int32_t cbuf, pad;
 };
 
+// Split-K: a long group is cut into parts written to plan-owned scratch and
+// summed in part order by k_reduce (deterministic).
+struct Reduction {
+  int64_t c_off;        // destination (buffer cbuf)
+  int64_t scm, scn;
+  int64_t part_off;     // first partial (scratch), parts consecutive, M*N each
+  int32_t M, N;
+  int32_t nparts, cbuf;
+  int64_t elem0;        // prefix of M*N over reductions (thread mapping)
+};
+
 struct Work {
   int32_t group;
   int32_t mt, nt;   // tile coordinates inside the group
@@ -36,6 +47,7 @@ struct Work {
 };
 
 constexpr int kMaxBufs = 8;
+constexpr int kPartialBuf = 6;   // buffer slot of the split-K scratch
 struct Bufs {
   double *p[kMaxBufs];
 };
@@ -53,6 +65,11 @@ struct Step {
   double flops = 0.0;            // sum of 2*m*n*k of the reference tasks
   int64_t ntasks = 0;
   bool uploaded = false;         // device copies are made on first use
+  std::vector<Reduction> reds;   // split-K reductions (host)
+  Reduction *d_reds = nullptr;
+  int64_t red_elems = 0;         // total output elements of the reductions
+  int64_t part_elems = 0;        // scratch size (doubles)
+  double *d_part = nullptr;      // split-K scratch, owned by the step
   double alg_bytes = 0.0;        // each operand tensor read once + output written once
   // profiling (zmpo_profile): events around the launch, accumulated time
   void *ev0 = nullptr, *ev1 = nullptr;
@@ -64,6 +81,7 @@ struct Step {
 // Launchers (kernels.cu)
 int launch_step_fp64(const Step &s, const Bufs &b, void *stream);
 int launch_step_split(const Step &s, const Bufs &b, int nslices, void *stream);
+int launch_reduce(const Step &s, const Bufs &b, void *stream);
 
 // Diagonal terms for HDiag: out[l, r] += alpha * sum_{a,b,c} Ld[a,l] Wi[a,b]
 // Wj[b,c] Rd[c,r] for one psi block; Ld/Rd are diagonal blocks of the

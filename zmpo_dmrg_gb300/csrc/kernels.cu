@@ -215,31 +215,64 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
     }
     __syncthreads();
     while (ctl[1] < g.nseg) {
-      // 1. slot table for this chunk (one thread; at most 32 entries)
-      if (tid == 0) {
-        int si = ctl[1], ki = ctl[2], j = 0;
-        while (j < T_TK && si < g.nseg) {
-          const Seg sg = segs[g.seg0 + si];
+      // 1. slot table of this chunk, built by warp 0: lane l looks at segment
+      //    cur+l, an inclusive warp scan of the slots each segment can still
+      //    provide places every segment's k range inside the 32 slots.
+      if (warp == 0) {
+        const int cur = ctl[1], curk = ctl[2];
+        const int sidx = cur + lane;
+        Seg sg;
+        int avail = 0;
+        if (sidx < g.nseg) {
+          sg = segs[g.seg0 + sidx];
+          avail = sg.K - (lane == 0 ? curk : 0);
+        }
+        int incl = avail;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += t;
+        }
+        const int excl = incl - avail;
+        if (avail > 0 && excl < T_TK) {
           const double *A = bufs.p[sg.abuf] + sg.a_off;
           const double *B = bufs.p[sg.bbuf] + sg.b_off;
-          const int take = min(T_TK - j, sg.K - ki);
-          for (int t = 0; t < take; ++t) {
-            slots[j + t].a = A + (int64_t)(ki + t) * sg.sak;
-            slots[j + t].b = B + (int64_t)(ki + t) * sg.sbk;
-            slots[j + t].sam = sg.sam;
-            slots[j + t].sbn = sg.sbn;
-            slots[j + t].alpha = sg.alpha;
-          }
-          j += take;
-          ki += take;
-          if (ki >= sg.K) {
-            ++si;
-            ki = 0;
+          const int k0 = lane == 0 ? curk : 0;
+          const int jend = min(incl, T_TK);
+          for (int j = excl; j < jend; ++j) {
+            const int kk = k0 + (j - excl);
+            slots[j].a = A + (int64_t)kk * sg.sak;
+            slots[j].b = B + (int64_t)kk * sg.sbk;
+            slots[j].sam = sg.sam;
+            slots[j].sbn = sg.sbn;
+            slots[j].alpha = sg.alpha;
           }
         }
-        ctl[0] = j;
-        ctl[1] = si;
-        ctl[2] = ki;
+        // where the chunk ends: first lane whose inclusive sum reaches 32
+        const unsigned reach = __ballot_sync(0xffffffffu, incl >= T_TK && avail > 0);
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        const int lstop = reach ? (__ffs(reach) - 1) : -1;
+        const int stop_incl = __shfl_sync(0xffffffffu, incl, lstop < 0 ? 31 : lstop);
+        const int stop_excl = __shfl_sync(0xffffffffu, excl, lstop < 0 ? 31 : lstop);
+        if (lane == 0) {
+          if (lstop < 0) {           // every remaining segment fits (or the 32 lanes ran out)
+            const int nseen = min(32, g.nseg - cur);
+            ctl[0] = min(total, T_TK);
+            ctl[1] = cur + nseen;
+            ctl[2] = 0;
+          } else {
+            ctl[0] = T_TK;
+            const int used = T_TK - stop_excl;             // slots taken from segment cur+lstop
+            const int base = lstop == 0 ? curk : 0;
+            if (stop_incl == T_TK) {
+              ctl[1] = cur + lstop + 1;
+              ctl[2] = 0;
+            } else {
+              ctl[1] = cur + lstop;
+              ctl[2] = base + used;
+            }
+          }
+        }
       }
       __syncthreads();
       const int nslot = ctl[0];
@@ -387,6 +420,37 @@ int launch_step_split(const Step &s, const Bufs &b, int nslices, void *stream) {
     return launch_tc_t<7, 16>(s.d_work_tc16, s.nwork_tc16, s, b, stream);
   }
   return record_arg_error("unsupported slice count");
+}
+
+// ------------------------------------------------------------- split-K sum
+__global__ void __launch_bounds__(256)
+k_reduce(const Reduction *__restrict__ reds, int nred, int64_t total, Bufs bufs) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = nred - 1;
+    while (lo < hi) {  // last reduction with elem0 <= i
+      const int mid = (lo + hi + 1) >> 1;
+      if (reds[mid].elem0 <= i) lo = mid; else hi = mid - 1;
+    }
+    const Reduction r = reds[lo];
+    const int64_t e = i - r.elem0;
+    const int m = (int)(e / r.N), n = (int)(e % r.N);
+    const double *P = bufs.p[kPartialBuf] + r.part_off + e;
+    const int64_t stride = (int64_t)r.M * r.N;
+    double acc = 0.0;
+    for (int t = 0; t < r.nparts; ++t) acc += P[t * stride];
+    bufs.p[r.cbuf][r.c_off + (int64_t)m * r.scm + (int64_t)n * r.scn] = acc;
+  }
+}
+
+int launch_reduce(const Step &s, const Bufs &b, void *stream) {
+  if (s.red_elems == 0) return ZMPO_OK;
+  Bufs bb = b;
+  bb.p[kPartialBuf] = s.d_part;
+  const int64_t blocks = (s.red_elems + 255) / 256;
+  k_reduce<<<(int)(blocks < 152 * 16 ? blocks : 152 * 16), 256, 0, (cudaStream_t)stream>>>(
+      s.d_reds, (int)s.reds.size(), s.red_elems, bb);
+  return launch_error("k_reduce");
 }
 
 // ----------------------------------------------------------------- HDiag

@@ -564,8 +564,86 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
 constexpr int kTileFP64M = 32, kTileFP64N = 32;
 constexpr int kTileTCM = 128;
 
+// Cut groups whose summed K exceeds kSplitK into parts of about kSplitK (at
+// segment boundaries, or inside a long segment); parts go to scratch and a
+// reduction sums them in order.
+constexpr int64_t kSplitK = 2048;
+
+static void split_long_groups(Step &st) {
+  std::vector<Group> out;
+  std::vector<Seg> segs;
+  out.reserve(st.groups.size());
+  segs.reserve(st.segs.size());
+  int64_t part = 0;
+  for (const Group &G : st.groups) {
+    int64_t ktot = 0;
+    for (int i = 0; i < G.nseg; ++i) ktot += st.segs[G.seg0 + i].K;
+    if (ktot <= kSplitK || G.M == 0 || G.N == 0) {
+      Group g = G;
+      g.seg0 = (int32_t)segs.size();
+      for (int i = 0; i < G.nseg; ++i) segs.push_back(st.segs[G.seg0 + i]);
+      out.push_back(g);
+      continue;
+    }
+    Reduction r;
+    r.c_off = G.c_off;
+    r.scm = G.scm;
+    r.scn = G.scn;
+    r.M = G.M;
+    r.N = G.N;
+    r.cbuf = G.cbuf;
+    r.part_off = part;
+    r.nparts = 0;
+    const int64_t mn = (int64_t)G.M * G.N;
+    Group cur{};
+    auto open_part = [&]() {
+      cur = Group{};
+      cur.c_off = part;
+      cur.scm = G.N;
+      cur.scn = 1;
+      cur.M = G.M;
+      cur.N = G.N;
+      cur.cbuf = kPartialBuf;
+      cur.seg0 = (int32_t)segs.size();
+      cur.nseg = 0;
+      part += mn;
+      r.nparts += 1;
+    };
+    open_part();
+    int64_t kin = 0;
+    for (int i = 0; i < G.nseg; ++i) {
+      Seg sgm = st.segs[G.seg0 + i];
+      int64_t k0 = 0;
+      while (k0 < sgm.K) {
+        if (kin >= kSplitK) {
+          out.push_back(cur);
+          open_part();
+          kin = 0;
+        }
+        const int64_t take = std::min<int64_t>(sgm.K - k0, kSplitK - kin);
+        Seg piece = sgm;
+        piece.a_off = sgm.a_off + k0 * sgm.sak;
+        piece.b_off = sgm.b_off + k0 * sgm.sbk;
+        piece.K = (int32_t)take;
+        segs.push_back(piece);
+        cur.nseg += 1;
+        kin += take;
+        k0 += take;
+      }
+    }
+    out.push_back(cur);
+    r.elem0 = st.red_elems;
+    st.red_elems += mn;
+    st.reds.push_back(r);
+  }
+  st.groups.swap(out);
+  st.segs.swap(segs);
+  st.part_elems = part;
+}
+
 static int upload_step(Step &st) {
   if (st.uploaded) return ZMPO_OK;
+  split_long_groups(st);
   std::vector<Work> w64, wtc8, wtc16;
   // order groups by cost (longest first) for load balance
   std::vector<int> order(st.groups.size());
@@ -604,6 +682,8 @@ static int upload_step(Step &st) {
   CUDA_TRY(up(&st.d_work_fp64, w64));
   CUDA_TRY(up(&st.d_work_tc8, wtc8));
   CUDA_TRY(up(&st.d_work_tc16, wtc16));
+  CUDA_TRY(up(&st.d_reds, st.reds));
+  if (st.part_elems > 0) CUDA_TRY(cudaMalloc((void **)&st.d_part, st.part_elems * sizeof(double)));
   // keep the host mirror of groups (sizes) but free the bulky segment copy
   std::vector<Seg>().swap(st.segs);
   st.uploaded = true;
@@ -619,6 +699,10 @@ static void free_step(Step &st) {
   cudaFree(st.d_work_fp64);
   cudaFree(st.d_work_tc8);
   cudaFree(st.d_work_tc16);
+  cudaFree(st.d_reds);
+  cudaFree(st.d_part);
+  st.d_reds = nullptr;
+  st.d_part = nullptr;
   st.d_segs = nullptr;
   st.d_groups = nullptr;
   st.d_work_fp64 = st.d_work_tc8 = st.d_work_tc16 = nullptr;
@@ -648,14 +732,17 @@ static int run_step(Step &st, const Bufs &b, int precision, void *stream) {
     }
     cudaEventRecord((cudaEvent_t)st.ev0, (cudaStream_t)stream);
   }
+  Bufs bb = b;
+  bb.p[kPartialBuf] = st.d_part;
   if (precision == ZMPO_PREC_FP64)
-    rc = launch_step_fp64(st, b, stream);
+    rc = launch_step_fp64(st, bb, stream);
   else if (precision == ZMPO_PREC_SPLIT)
-    rc = launch_step_split(st, b, 4, stream);
+    rc = launch_step_split(st, bb, 4, stream);
   else if (precision == ZMPO_PREC_EMU64)
-    rc = launch_step_split(st, b, 7, stream);
+    rc = launch_step_split(st, bb, 7, stream);
   else
     return fail(ZMPO_E_ARG, "unknown precision");
+  if (rc == ZMPO_OK) rc = launch_reduce(st, bb, stream);
   if (g_profile && rc == ZMPO_OK) {
     cudaEventRecord((cudaEvent_t)st.ev1, (cudaStream_t)stream);
     st.ev_pending = true;
@@ -1303,6 +1390,30 @@ int zmpo_plan_launch_times(zmpo_engine *e, int plan_id, int nmax, double *ms_avg
     if (ncalls) ncalls[s] = st.ncalls;
     st.ms_total = 0.0;
     st.ncalls = 0;
+  }
+  return ZMPO_OK;
+}
+
+int zmpo_plan_groups(zmpo_engine *e, int plan_id, int step, int64_t *ngroups, int32_t *M,
+                     int32_t *N, int32_t *nseg, int64_t *ktot) {
+  Plan *P = get_plan(e, plan_id, 0);
+  if (!P || step < 0 || step >= (int)P->steps.size() || !ngroups)
+    return fail(ZMPO_E_ID, "plan_groups: unknown plan or step");
+  const Step &st = P->steps[step];
+  *ngroups = (int64_t)st.groups.size();
+  if (!M) return ZMPO_OK;
+  if (st.segs.empty() && !st.groups.empty() && st.uploaded)
+    return fail(ZMPO_E_ARG, "plan_groups: segment list already moved to the device");
+  for (size_t g = 0; g < st.groups.size(); ++g) {
+    const Group &G = st.groups[g];
+    M[g] = G.M;
+    N[g] = G.N;
+    if (nseg) nseg[g] = G.nseg;
+    if (ktot) {
+      int64_t k = 0;
+      for (int i = 0; i < G.nseg; ++i) k += st.segs[G.seg0 + i].K;
+      ktot[g] = k;
+    }
   }
   return ZMPO_OK;
 }

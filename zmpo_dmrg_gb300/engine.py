@@ -124,6 +124,19 @@ class Engine:
               "launch_times")
         return ms, by, nc
 
+    def plan_groups(self, pid, step):
+        n = ctypes.c_int64()
+        check(_lib.lib().zmpo_plan_groups(self.h, pid, step, ctypes.byref(n), None, None, None, None),
+              "plan_groups")
+        M = numpy.zeros(max(n.value, 1), dtype=numpy.int32)
+        N = numpy.zeros_like(M)
+        S = numpy.zeros_like(M)
+        Kt = numpy.zeros(max(n.value, 1), dtype=numpy.int64)
+        check(_lib.lib().zmpo_plan_groups(self.h, pid, step, ctypes.byref(n), iptr(M), iptr(N), iptr(S),
+                                          lptr(Kt)), "plan_groups")
+        k = n.value
+        return M[:k], N[:k], S[:k], Kt[:k]
+
     def destroy_plan(self, pid):
         check(_lib.lib().zmpo_plan_destroy(self.h, pid), "plan_destroy")
 
