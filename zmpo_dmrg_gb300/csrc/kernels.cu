@@ -59,12 +59,16 @@ k_step_fp64(const Work *__restrict__ work, int64_t nwork, const Group *__restric
       const double *A = bufs.p[s.abuf] + s.a_off;
       const double *B = bufs.p[s.bbuf] + s.b_off;
       const bool a_kfast = s.sak == 1, b_nfast = s.sbn == 1;
+      const bool scaled = s.alpha != 1.0;
       for (int k0 = 0; k0 < s.K; k0 += F_TK) {
         for (int e = tid; e < F_TM * F_TK; e += F_NT) {
           int r, k;
           if (a_kfast) { r = e / F_TK; k = e % F_TK; } else { r = e % F_TM; k = e / F_TM; }
           double v = 0.0;
-          if (m0 + r < g.M && k0 + k < s.K) v = s.alpha * A[(int64_t)(m0 + r) * s.sam + (int64_t)(k0 + k) * s.sak];
+          if (m0 + r < g.M && k0 + k < s.K) {
+            v = A[(int64_t)(m0 + r) * s.sam + (int64_t)(k0 + k) * s.sak];
+            if (scaled) v *= s.alpha;
+          }
           As[k][r] = v;
         }
         for (int e = tid; e < F_TK * F_TN; e += F_NT) {
@@ -112,7 +116,7 @@ int launch_step_fp64(const Step &s, const Bufs &b, void *stream) {
 // BF16 tensor cores (exact in FP32: level sums < 2^24), level sums scaled and
 // added to a two-float accumulator.  Integer->float conversions stay 32-bit:
 // 64-bit conversions issue on the FP64 pipe, which is narrow on GB300.
-constexpr int T_TM = 128, T_TK = 32, T_NT = 128, T_PAD = 40;
+constexpr int T_TM = 128, T_TK = 32, T_NT = 256, T_PAD = 40;
 
 // biased exponent of a double (0 for zero / denormal)
 __device__ __forceinline__ int dexp(double x) {
@@ -179,10 +183,12 @@ struct Slot {
   const double *b;  // B(k, col 0)
   int64_t sam, sbn;
   double alpha;
+  int scaled;       // alpha != 1 (decided once per slot, not per element)
+  int pad;
 };
 
 template <int S, int TN>
-__global__ void __launch_bounds__(T_NT)
+__global__ void __launch_bounds__(T_NT, (S <= 4 ? 3 : 2))
 k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
           const Seg *__restrict__ segs, Bufs bufs) {
   constexpr int NTL = TN / 8;  // n8 tiles per warp
@@ -195,16 +201,17 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
   int *ctl = reinterpret_cast<int *>(slots + T_TK);                 // nslot, si, ki
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = warp * 32;  // 32 rows (two m16 tiles) per warp
+  const int wm = warp * 16;  // one m16 tile per warp
   const int gq = lane >> 2, tq = lane & 3;
+  constexpr int MT = 1;
 
   for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
     const Work wk = work[w];
     const Group g = groups[wk.group];
     const int m0 = wk.mt * T_TM, n0 = wk.nt * TN;
-    float hi[2][NTL][4], lo[2][NTL][4];
+    float hi[MT][NTL][4], lo[MT][NTL][4];
 #pragma unroll
-    for (int mt = 0; mt < 2; ++mt)
+    for (int mt = 0; mt < MT; ++mt)
 #pragma unroll
       for (int nt = 0; nt < NTL; ++nt)
 #pragma unroll
@@ -246,6 +253,7 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
             slots[j].sam = sg.sam;
             slots[j].sbn = sg.sbn;
             slots[j].alpha = sg.alpha;
+            slots[j].scaled = sg.alpha != 1.0;
           }
         }
         // where the chunk ends: first lane whose inclusive sum reaches 32
@@ -276,25 +284,31 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
       }
       __syncthreads();
       const int nslot = ctl[0];
-      // 2. A: thread = row; chunk max exponent then digit planes
+      // 2. A: two threads per row (16 slots each, partner = lane ^ 1);
+      //    chunk max exponent of the row, then digit planes
       {
-        const int row = m0 + tid;
-        double v[T_TK];
+        constexpr int HK = T_TK / 2;
+        const int r = tid >> 1, half = tid & 1;
+        const int row = m0 + r;
+        double v[HK];
         int emax = 0;
 #pragma unroll
-        for (int j = 0; j < T_TK; ++j) {
+        for (int t = 0; t < HK; ++t) {
+          const int j = half * HK + t;
           double x = 0.0;
           if (j < nslot && row < g.M) {
             const Slot &sl = slots[j];
             x = __ldg(sl.a + (int64_t)row * sl.sam);
-            if (sl.alpha != 1.0) x *= sl.alpha;
+            if (sl.scaled) x *= sl.alpha;
           }
-          v[j] = x;
+          v[t] = x;
           emax = max(emax, dexp(x));
         }
-        Ea[tid] = emax;
+        emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
+        if (half == 0) Ea[r] = emax;
 #pragma unroll
-        for (int j = 0; j < T_TK; ++j) digits_bf16<S>(v[j], emax, Ap + tid * T_PAD + j, T_TM * T_PAD);
+        for (int t = 0; t < HK; ++t)
+          digits_bf16<S>(v[t], emax, Ap + r * T_PAD + half * HK + t, T_TM * T_PAD);
       }
       // 3. B: TN columns, 128/TN threads per column share the 32 slots
       {
@@ -321,11 +335,11 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
       }
       __syncthreads();
       // 4. digit products per level, exact in FP32
-      float acc[S][2][NTL][4];
+      float acc[S][MT][NTL][4];
 #pragma unroll
       for (int l = 0; l < S; ++l)
 #pragma unroll
-        for (int mt = 0; mt < 2; ++mt)
+        for (int mt = 0; mt < MT; ++mt)
 #pragma unroll
           for (int nt = 0; nt < NTL; ++nt)
 #pragma unroll
@@ -344,7 +358,7 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
 #pragma unroll
         for (int sa = 0; sa < S; ++sa) {
 #pragma unroll
-          for (int mt = 0; mt < 2; ++mt) {
+          for (int mt = 0; mt < MT; ++mt) {
             uint32_t af[4];
             const __nv_bfloat16 *ap = Ap + (sa * T_TM + wm + mt * 16) * T_PAD + kk;
             af[0] = *reinterpret_cast<const uint32_t *>(ap + gq * T_PAD + 2 * tq);
@@ -360,7 +374,7 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
       }
       // 5. scale levels by 2^(Ea + Eb - 2044 - 8(l+2)) into the two-float sums
 #pragma unroll
-      for (int mt = 0; mt < 2; ++mt)
+      for (int mt = 0; mt < MT; ++mt)
 #pragma unroll
         for (int nt = 0; nt < NTL; ++nt)
 #pragma unroll
@@ -378,7 +392,7 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
     }
     double *C = bufs.p[g.cbuf] + g.c_off;
 #pragma unroll
-    for (int mt = 0; mt < 2; ++mt)
+    for (int mt = 0; mt < MT; ++mt)
 #pragma unroll
       for (int nt = 0; nt < NTL; ++nt)
 #pragma unroll
