@@ -89,6 +89,26 @@ int zmpo_contract_exec(zmpo_engine *e, int plan_id, const double *d_a,
                        const double *d_b, double *d_out, int precision,
                        void *stream);
 
+/* Allocation-free variant of zmpo_contract_exec (no counterpart in the
+ * reference).  For callers that cannot allocate device memory when they run
+ * a contraction -- code recorded into a CUDA graph by stream capture, where
+ * cudaMalloc is not allowed, or a host framework that hands out all device
+ * memory itself -- the split-K partial sums go to a fixed 8 MiB array
+ * (1048576 float64) compiled into this library instead of memory the plan
+ * allocates.  Every GPU that loads the library holds that array until the
+ * process exits.  The call allocates nothing: the plan must have run once
+ * through zmpo_contract_exec during set-up (that call builds the plan's device
+ * task lists), and a plan that needs more scratch than the array holds is
+ * rejected with ZMPO_E_SIZE.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress, with that device current); make that
+ * first call before any stream capture.  All calls share the one array and it
+ * keeps the last call's contents (every partial is overwritten before it is
+ * read, nothing needs clearing); calls whose launches overlap on the GPU race
+ * on it, so order them on one stream. */
+int zmpo_contract_exec_noalloc(zmpo_engine *e, int plan_id, const double *d_a,
+                               const double *d_b, double *d_out, int precision,
+                               void *stream);
+
 /* Sigma vector H.psi over all operator terms p of one dot
  * (replaces mpo_dmrg_kernelQt.HVecQt, mpo_dmrg_kernelQt.py:153-319, and the
  * Reduce over ranks, tools/pdvdson.py:75).  Operators of one class share

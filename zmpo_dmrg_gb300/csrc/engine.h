@@ -107,5 +107,6 @@ int launch_hdiag(const DiagBlock *blocks, int64_t nblocks, const DiagTerm *terms
 // error recording shared by both translation units
 int record_cuda_error(const char *where, int cuda_err);
 int record_arg_error(const char *msg);
+int record_size_error(const char *msg);
 
 }  // namespace zmpo

@@ -539,3 +539,68 @@ int launch_hdiag(const DiagBlock *blocks, int64_t nblocks, const DiagTerm *terms
 }
 
 }  // namespace zmpo
+
+// =================================================== allocation-free variant
+// zmpo_contract_exec_noalloc: the split-K partial sums of a contraction live in
+// this fixed device array instead of memory the plan allocates, for callers
+// that must not allocate device memory at the time of the call (see the
+// declaration in include/zmpo_gb300.h).  Every device that loads the library
+// holds the array until the process exits.
+namespace zmpo {
+int contract_step_for(zmpo_engine *e, int plan_id, Step **out);
+}
+
+constexpr int64_t kNoAllocScratchElems = int64_t(1) << 20;  // 8 MiB of float64
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchElems];
+constexpr int kNoAllocMaxDevices = 64;
+static double *g_noalloc_ptr[kNoAllocMaxDevices];  // device address of the array, per device
+
+// split-K sum that reads the partials from the scratch pointer it is given
+static int launch_reduce_given_scratch(const zmpo::Step &s, const zmpo::Bufs &b, void *stream) {
+  if (s.red_elems == 0) return ZMPO_OK;
+  const int64_t blocks = (s.red_elems + 255) / 256;
+  zmpo::k_reduce<<<(int)(blocks < 152 * 16 ? blocks : 152 * 16), 256, 0, (cudaStream_t)stream>>>(
+      s.d_reds, (int)s.reds.size(), s.red_elems, b);
+  return zmpo::launch_error("k_reduce (static scratch)");
+}
+
+extern "C" int zmpo_contract_exec_noalloc(zmpo_engine *e, int plan_id, const double *d_a,
+                                          const double *d_b, double *d_out, int precision,
+                                          void *stream) {
+  zmpo::Step *st = nullptr;
+  int rc = zmpo::contract_step_for(e, plan_id, &st);
+  if (rc) return rc;
+  if (st->part_elems > kNoAllocScratchElems)
+    return zmpo::record_size_error(
+        "contract_exec_noalloc: the plan needs more split-K scratch than the fixed 8 MiB "
+        "(1048576 float64) array holds; use zmpo_contract_exec");
+  int dev = -1;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess) return zmpo::record_cuda_error("contract_exec_noalloc: cudaGetDevice", (int)ce);
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return zmpo::record_size_error("contract_exec_noalloc: device ordinal beyond 63");
+  if (g_noalloc_ptr[dev] == nullptr) {
+    // one-time set-up on this device (the device is current): the array's
+    // name is a host-side stand-in, the kernels need its device address
+    void *p = nullptr;
+    ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (ce != cudaSuccess)
+      return zmpo::record_cuda_error("contract_exec_noalloc: cudaGetSymbolAddress", (int)ce);
+    g_noalloc_ptr[dev] = static_cast<double *>(p);
+  }
+  zmpo::Bufs b{};
+  b.p[0] = const_cast<double *>(d_a);
+  b.p[1] = const_cast<double *>(d_b);
+  b.p[4] = d_out;
+  b.p[zmpo::kPartialBuf] = g_noalloc_ptr[dev];
+  if (precision == ZMPO_PREC_FP64)
+    rc = zmpo::launch_step_fp64(*st, b, stream);
+  else if (precision == ZMPO_PREC_SPLIT)
+    rc = zmpo::launch_step_split(*st, b, 4, stream);
+  else if (precision == ZMPO_PREC_EMU64)
+    rc = zmpo::launch_step_split(*st, b, 7, stream);
+  else
+    return zmpo::record_arg_error("contract_exec_noalloc: unknown precision");
+  if (rc) return rc;
+  return launch_reduce_given_scratch(*st, b, stream);
+}

@@ -40,6 +40,8 @@ int record_cuda_error(const char *where, int cuda_err) {
 
 int record_arg_error(const char *msg) { return fail(ZMPO_E_ARG, msg); }
 
+int record_size_error(const char *msg) { return fail(ZMPO_E_SIZE, msg); }
+
 #define CUDA_TRY(x)                                                      \
   do {                                                                   \
     cudaError_t _e = (x);                                                \
@@ -762,6 +764,21 @@ struct ChainStep {
   int lay;    // output layout
 };
 
+}  // namespace zmpo
+
+namespace zmpo {
+// The single launch of a contraction plan whose device task lists exist
+// (used by the allocation-free entry point in kernels.cu).
+int contract_step_for(zmpo_engine *e, int plan_id, Step **out) {
+  Plan *P = get_plan(e, plan_id, 1);
+  if (!P) return fail(ZMPO_E_ID, "contract_exec_noalloc: unknown contraction plan");
+  if (!P->steps[0].uploaded)
+    return fail(ZMPO_E_ARG,
+                "contract_exec_noalloc: the plan has no device task lists yet; run it once "
+                "through zmpo_contract_exec during set-up");
+  *out = &P->steps[0];
+  return ZMPO_OK;
+}
 }  // namespace zmpo
 
 // ====================================================================== C ABI
