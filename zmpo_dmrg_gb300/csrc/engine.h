@@ -59,9 +59,10 @@ struct Step {
   Seg *d_segs = nullptr;
   Group *d_groups = nullptr;
   Work *d_work_fp64 = nullptr;   // tiles of kTileFP64
-  Work *d_work_tc8 = nullptr;    // 128 x 8 tiles of the tensor-core kernel
-  Work *d_work_tc16 = nullptr;   // 128 x 16 tiles
-  int64_t nwork_fp64 = 0, nwork_tc8 = 0, nwork_tc16 = 0;
+  // tensor-core tiles: [rows 32 / 64 / 128][columns 8 / 16]
+  Work *d_work_tc[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+  int64_t nwork_fp64 = 0;
+  int64_t nwork_tc[3][2] = {{0, 0}, {0, 0}, {0, 0}};
   double flops = 0.0;            // sum of 2*m*n*k of the reference tasks
   int64_t ntasks = 0;
   bool uploaded = false;         // device copies are made on first use

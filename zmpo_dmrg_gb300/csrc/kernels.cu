@@ -116,7 +116,7 @@ int launch_step_fp64(const Step &s, const Bufs &b, void *stream) {
 // BF16 tensor cores (exact in FP32: level sums < 2^24), level sums scaled and
 // added to a two-float accumulator.  Integer->float conversions stay 32-bit:
 // 64-bit conversions issue on the FP64 pipe, which is narrow on GB300.
-constexpr int T_TM = 128, T_TK = 32, T_NT = 256, T_PAD = 40;
+constexpr int T_TK = 32, T_PAD = 40;
 
 // biased exponent of a double (0 for zero / denormal)
 __device__ __forceinline__ int dexp(double x) {
@@ -187,10 +187,11 @@ struct Slot {
   int pad;
 };
 
-template <int S, int TN>
-__global__ void __launch_bounds__(T_NT, (S <= 4 ? 3 : 2))
+template <int S, int TM, int TN>
+__global__ void __launch_bounds__(2 * TM, (S <= 4 ? 768 : 512) / (2 * TM))
 k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
           const Seg *__restrict__ segs, Bufs bufs) {
+  constexpr int T_TM = TM, T_NT = 2 * TM;  // two threads per row, one m16 tile per warp
   constexpr int NTL = TN / 8;  // n8 tiles per warp
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __nv_bfloat16 *Ap = reinterpret_cast<__nv_bfloat16 *>(smem_raw);  // [S][TM][PAD]
@@ -406,33 +407,35 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
   }
 }
 
-template <int S, int TN>
+template <int S, int TM, int TN>
 static int launch_tc_t(const Work *work, int64_t nwork, const Step &s, const Bufs &b, void *stream) {
   if (nwork == 0) return ZMPO_OK;
-  const size_t smem = (size_t)S * (T_TM + TN) * T_PAD * sizeof(__nv_bfloat16) +
-                      (size_t)(T_TM + 16) * sizeof(int) + T_TK * sizeof(Slot) + 4 * sizeof(int) + 16;
+  const size_t smem = (size_t)S * (TM + TN) * T_PAD * sizeof(__nv_bfloat16) +
+                      (size_t)(TM + 16) * sizeof(int) + T_TK * sizeof(Slot) + 4 * sizeof(int) + 16;
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_step_tc<S, TN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_step_tc<S, TM, TN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = true;
   }
-  k_step_tc<S, TN><<<grid_for(nwork, 8), T_NT, smem, (cudaStream_t)stream>>>(work, nwork, s.d_groups,
-                                                                             s.d_segs, b);
+  k_step_tc<S, TM, TN><<<grid_for(nwork, 3 * 256 / TM), 2 * TM, smem, (cudaStream_t)stream>>>(
+      work, nwork, s.d_groups, s.d_segs, b);
   return launch_error("k_step_tc");
 }
 
-int launch_step_split(const Step &s, const Bufs &b, int nslices, void *stream) {
+template <int S>
+static int launch_split_all(const Step &s, const Bufs &b, void *stream) {
   int rc;
-  if (nslices == 4) {
-    rc = launch_tc_t<4, 8>(s.d_work_tc8, s.nwork_tc8, s, b, stream);
-    if (rc) return rc;
-    return launch_tc_t<4, 16>(s.d_work_tc16, s.nwork_tc16, s, b, stream);
-  }
-  if (nslices == 7) {
-    rc = launch_tc_t<7, 8>(s.d_work_tc8, s.nwork_tc8, s, b, stream);
-    if (rc) return rc;
-    return launch_tc_t<7, 16>(s.d_work_tc16, s.nwork_tc16, s, b, stream);
-  }
+  if ((rc = launch_tc_t<S, 128, 8>(s.d_work_tc[2][0], s.nwork_tc[2][0], s, b, stream))) return rc;
+  if ((rc = launch_tc_t<S, 128, 16>(s.d_work_tc[2][1], s.nwork_tc[2][1], s, b, stream))) return rc;
+  if ((rc = launch_tc_t<S, 64, 8>(s.d_work_tc[1][0], s.nwork_tc[1][0], s, b, stream))) return rc;
+  if ((rc = launch_tc_t<S, 64, 16>(s.d_work_tc[1][1], s.nwork_tc[1][1], s, b, stream))) return rc;
+  if ((rc = launch_tc_t<S, 32, 8>(s.d_work_tc[0][0], s.nwork_tc[0][0], s, b, stream))) return rc;
+  return launch_tc_t<S, 32, 16>(s.d_work_tc[0][1], s.nwork_tc[0][1], s, b, stream);
+}
+
+int launch_step_split(const Step &s, const Bufs &b, int nslices, void *stream) {
+  if (nslices == 4) return launch_split_all<4>(s, b, stream);
+  if (nslices == 7) return launch_split_all<7>(s, b, stream);
   return record_arg_error("unsupported slice count");
 }
 

@@ -564,7 +564,6 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
 
 // tile sizes of the two kernels (must match kernels.cu)
 constexpr int kTileFP64M = 32, kTileFP64N = 32;
-constexpr int kTileTCM = 128;
 
 // Cut groups whose summed K exceeds kSplitK into parts of about kSplitK (at
 // segment boundaries, or inside a long segment); parts go to scratch and a
@@ -646,7 +645,7 @@ static void split_long_groups(Step &st) {
 static int upload_step(Step &st) {
   if (st.uploaded) return ZMPO_OK;
   split_long_groups(st);
-  std::vector<Work> w64, wtc8, wtc16;
+  std::vector<Work> w64, wtc[3][2];
   // order groups by cost (longest first) for load balance
   std::vector<int> order(st.groups.size());
   std::iota(order.begin(), order.end(), 0);
@@ -661,14 +660,15 @@ static int upload_step(Step &st) {
     const Group &G = st.groups[g];
     for (int mt = 0; mt * kTileFP64M < G.M; ++mt)
       for (int nt = 0; nt * kTileFP64N < G.N; ++nt) w64.push_back({g, mt, nt, 0});
-    const int tn = G.N <= 8 ? 8 : 16;
-    auto &wl = tn == 8 ? wtc8 : wtc16;
-    for (int mt = 0; mt * kTileTCM < G.M; ++mt)
+    const int tni = G.N <= 8 ? 0 : 1, tn = tni ? 16 : 8;
+    const int tmi = G.M <= 32 ? 0 : (G.M <= 64 ? 1 : 2), tm = 32 << tmi;
+    auto &wl = wtc[tmi][tni];
+    for (int mt = 0; mt * tm < G.M; ++mt)
       for (int nt = 0; nt * tn < G.N; ++nt) wl.push_back({g, mt, nt, 0});
   }
   st.nwork_fp64 = (int64_t)w64.size();
-  st.nwork_tc8 = (int64_t)wtc8.size();
-  st.nwork_tc16 = (int64_t)wtc16.size();
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 2; ++j) st.nwork_tc[i][j] = (int64_t)wtc[i][j].size();
   auto up = [](auto **dptr, const auto &v) -> cudaError_t {
     using T = typename std::remove_reference<decltype(v)>::type::value_type;
     if (v.empty()) {
@@ -682,8 +682,8 @@ static int upload_step(Step &st) {
   CUDA_TRY(up(&st.d_segs, st.segs));
   CUDA_TRY(up(&st.d_groups, st.groups));
   CUDA_TRY(up(&st.d_work_fp64, w64));
-  CUDA_TRY(up(&st.d_work_tc8, wtc8));
-  CUDA_TRY(up(&st.d_work_tc16, wtc16));
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 2; ++j) CUDA_TRY(up(&st.d_work_tc[i][j], wtc[i][j]));
   CUDA_TRY(up(&st.d_reds, st.reds));
   if (st.part_elems > 0) CUDA_TRY(cudaMalloc((void **)&st.d_part, st.part_elems * sizeof(double)));
   // keep the host mirror of groups (sizes) but free the bulky segment copy
@@ -699,15 +699,18 @@ static void free_step(Step &st) {
   cudaFree(st.d_segs);
   cudaFree(st.d_groups);
   cudaFree(st.d_work_fp64);
-  cudaFree(st.d_work_tc8);
-  cudaFree(st.d_work_tc16);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 2; ++j) {
+      cudaFree(st.d_work_tc[i][j]);
+      st.d_work_tc[i][j] = nullptr;
+    }
   cudaFree(st.d_reds);
   cudaFree(st.d_part);
   st.d_reds = nullptr;
   st.d_part = nullptr;
   st.d_segs = nullptr;
   st.d_groups = nullptr;
-  st.d_work_fp64 = st.d_work_tc8 = st.d_work_tc16 = nullptr;
+  st.d_work_fp64 = nullptr;
 }
 
 static bool g_profile = false;
