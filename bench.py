@@ -146,6 +146,42 @@ def oracle_sample(P, nops_sample=2, budget_s=25.0):
     return oq.FLOPS["count"], dt, chosen
 
 
+def sweep_metrics(K=10, nelec=10, D=64, nsweep=4, seed=2024):
+    """Seconds per two-site sweep of the GPU driver on the small configuration
+    (K=10, 10 electrons, Sz=0, D=64, 4 sweeps, seeded synthetic integrals),
+    FP64 vs split path, and the difference of their final energies."""
+    import torch
+    from zmpo_dmrg_gb300 import integrals as I
+    from zmpo_dmrg_gb300.mpo_dmrg_class import mpo_dmrg
+    from zmpo_dmrg_gb300.mpo_dmrg_schedule import schedule
+    h, eri, _ = I.synthetic(K, seed)
+    i1, i2 = I.spin_orbital(h, eri)
+    out = {"workload": "K=%d N=%d Sz=0 D=%d, %d two-site sweeps from the Aufbau product state" % (K, nelec, D, nsweep)}
+    for prec in ("fp64", "split"):
+        m = mpo_dmrg(seed=1)
+        m.nsite, m.sbas, m.isym = K, 2 * K, 2
+        m.build()
+        m.occun = I.closed_shell_occun(K, nelec)
+        m.qsectors = {str([float(nelec), 0.0]): 1}
+        m.precision = prec
+        m.use_graph = True
+        m.partition()
+        m.loadInts((i1, i2))
+        m.dumpMPO()
+        sc = schedule(maxM=D, tol=1e-12, maxiter=nsweep)
+        sc.fixed(ncsite=2, maxM=D, tol=1e-12, maxiter=nsweep, noise=0.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m.default(sc)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out[prec] = {"s_per_sweep": dt / max(m.nsweep, 1), "sweeps": m.nsweep, "energy": float(m.Energy),
+                     "matvecs": int(sum(m.nmvp))}
+    out["dE_split_fp64"] = abs(out["split"]["energy"] - out["fp64"]["energy"])
+    out["sweep_speedup_split_vs_fp64"] = out["fp64"]["s_per_sweep"] / out["split"]["s_per_sweep"]
+    return out
+
+
 def cpu_threads():
     return os.cpu_count() or 1
 
@@ -183,6 +219,7 @@ def main():
     ap.add_argument("--impl", default="engine")
     ap.add_argument("--precision", default="split")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--small", action="store_true", help="K=12, D=128 case (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -308,6 +345,8 @@ def main():
                      "frac": (launches[top]["GBs"] or 0.0) / hbm, "traffic": None,
                      "peak_source": peak_kind},
     }
+    if rank == 0 and not args.no_sweep:
+        result["sweep"] = sweep_metrics()
     if rank == 0 and not args.no_cpu:
         fl, dt, ch = oracle_sample(P)
         result["cpu_baseline"] = {"value": fl / dt / 1e12, "unit": "TFLOP/s", "cores": cpu_threads(),

@@ -70,3 +70,19 @@ def test_sigma_deterministic(gpu):
     a = product_sigma(P, x, "fp64")
     b = product_sigma(P, x, "fp64")
     assert numpy.array_equal(a, b)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_sigma_graph_replay(gpu, precision):
+    """The site's launches recorded in a CUDA graph give the eager result."""
+    P = prob(CASES[1])
+    x = numpy.random.default_rng(10).standard_normal(P.ndim0)
+    eager = product_sigma(P, x, precision)
+    P.p.use_graph = True
+    try:
+        a = product_sigma(P, x, precision)
+        b = product_sigma(P, 2.0 * x, precision)
+    finally:
+        P.p.use_graph = False
+    assert numpy.array_equal(a, eager)
+    assert numpy.allclose(b, 2.0 * eager, rtol=1e-12, atol=1e-12)

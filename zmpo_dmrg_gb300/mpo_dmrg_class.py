@@ -139,6 +139,8 @@ class mpo_dmrg:
         self.precision = "fp64"
         self.precision_final = "emu64"
         self.precision_renorm = "fp64"
+        # replay each site's H.psi launches from a CUDA graph
+        self.use_graph = False
         self.rng = numpy.random.default_rng(seed)
         # device state
         self.mpo_store = None

@@ -111,8 +111,38 @@ class SigmaPlan:
         self.workspace = torch.empty(max(ws // 8, 1), dtype=torch.float64, device="cuda")
         self.flops, self.ntasks, self.nlaunch = eng.plan_stats(self.pid)
         self.fL, self.fR = fL, fR
+        self.graphs = {}
+
+    def run(self, dmrg, x, y, precision, use_graph=False):
+        """y = H x.  With ``use_graph`` the launches of this plan are recorded
+        once into a CUDA graph (per precision) over staging vectors and
+        replayed on every later call of the site."""
+        eng = _engine.get()
+        W = dmrg.mpo_store.buf
+        if not use_graph:
+            eng.sigma(self.pid, self.fL.buf, self.fR.buf, W, x, y, self.workspace, precision)
+            return
+        torch = _torch()
+        rec = self.graphs.get(precision)
+        if rec is None:
+            xs = torch.empty_like(x)
+            ys = torch.empty_like(y)
+            xs.copy_(x)
+            # warm-up outside capture: builds the device task lists
+            eng.sigma(self.pid, self.fL.buf, self.fR.buf, W, xs, ys, self.workspace, precision)
+            torch.cuda.synchronize()
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph):
+                eng.sigma(self.pid, self.fL.buf, self.fR.buf, W, xs, ys, self.workspace, precision)
+            rec = (graph, xs, ys)
+            self.graphs[precision] = rec
+        graph, xs, ys = rec
+        xs.copy_(x)
+        graph.replay()
+        y.copy_(ys)
 
     def release(self):
+        self.graphs = {}
         if self.pid is not None:
             _engine.get().destroy_plan(self.pid)
             self.pid = None
@@ -141,8 +171,7 @@ def HVec(vec0, info, ndim0, prjmap):
     if plan.pid is None:
         y.zero_()
     else:
-        _engine.get().sigma(plan.pid, plan.fL.buf, plan.fR.buf, dmrg.mpo_store.buf, x, y,
-                            plan.workspace, getattr(dmrg, "precision", "fp64"))
+        plan.run(dmrg, x, y, getattr(dmrg, "precision", "fp64"), getattr(dmrg, "use_graph", False))
     return y.cpu().numpy() if was_host else y
 
 
