@@ -95,6 +95,30 @@ def SVecQt(vec0, info, ndim0, prjmap):
     return svec
 
 
+def SDiagQt(info, ndim0, prjmap):
+    """diag(S) from the dense diagonals of the P environments and R(theta)
+    (mpo_dmrg_kernelQt.py:322-370)."""
+    dmrg, isite, ncsite, flst, status, ifsym = info
+    fLp, fRp = flst[0][2:4]
+    ldim, cdim, rdim, ndim = dmrg.dims
+    diag = numpy.zeros(ndim)
+    for iop in range(dmrg.npts):
+        cop = dmrg.fpop['op%d' % iop]
+        lop = fLp['opers%d' % iop]
+        rop = fRp['opers%d' % iop]
+        cdiag = cop.toDenseDiag(cop.idlst)
+        ldiag = lop.toDenseDiag(lop.idlst)
+        rdiag = rop.toDenseDiag(rop.idlst)
+        tmp = numpy.tensordot(ldiag, cdiag, axes=([0], [0]))
+        if ncsite == 1:
+            tmp = numpy.tensordot(tmp, rdiag, axes=([1], [0]))
+        else:
+            tmp = numpy.tensordot(tmp, cdiag, axes=([1], [0]))
+            tmp = numpy.tensordot(tmp, rdiag, axes=([2], [0]))
+        diag += dmrg.qwts[iop] * tmp.reshape(ndim)
+    return diag[prjmap].real.copy()
+
+
 def renormQt_S00(dmrg, isite, ncsite, flst, flstN, site, status):
     """New P environments for every quadrature point."""
     qsite = site.reduceQsymsToN()

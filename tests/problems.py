@@ -100,8 +100,11 @@ class Problem:
 
 
 def random_problem(K=6, nelec=6, D=16, isite=2, seed=0, hop=1.0, sz=0.0, device=True,
-                   with_oracle=True):
-    """Two-site dot at (isite, isite+1) with environments of every H_p."""
+                   with_oracle=True, npts=None, sval=0.0):
+    """Two-site dot at (isite, isite+1) with environments of every H_p.
+    With ``npts`` the problem is spin-projected: terms [p, g] over ``npts``
+    Gauss-Legendre points for <S^2> = sval(sval+1), N-labelled environments
+    and the P_g environments."""
     from oracle import integrals as oint
     rng = numpy.random.default_rng(seed)
     h1e, eri, _ = oint.synthetic(K, seed, hop)
@@ -114,6 +117,7 @@ def random_problem(K=6, nelec=6, D=16, isite=2, seed=0, hop=1.0, sz=0.0, device=
     P.int1e, P.int2e = int1e, int2e
     P.qnuml, P.qnumr, P.lsites, P.rsites = qnuml, qnumr, lsites, rsites
     P.key = [float(nelec), float(sz)]
+    P.npts, P.sval, P.sz = npts, sval, sz
     if with_oracle:
         P.o = _oracle_side(P)
         P.ndim0 = P.o.qtmp.size_allowed
@@ -126,29 +130,46 @@ def random_problem(K=6, nelec=6, D=16, isite=2, seed=0, hop=1.0, sz=0.0, device=
 def _oracle_side(P):
     from oracle import dmrg as od, kernel as ok
     from oracle.qtensor import qtensor
+    from oracle import spinproj as osp
     m = od.mpo_dmrg(seed=P.seed)
     m.nsite, m.sbas, m.isym, m.ifQt = P.K, 2 * P.K, 2, True
+    sp = P.npts is not None
+    if sp:
+        m.ifs2proj, m.npts = True, P.npts
+        osp.s2quad(m, P.sval, P.sz)
     m.build()
     m.partition()
     m.loadInts(P.int1e, P.int2e)
     m.dumpMPO()
+    if sp:
+        osp.dumpMPO_R(m)
     m.qnuml = list(P.qnuml)
     m.qnumr = list(P.qnumr)
     fL = m._boundary('lop', -1)
+    fLp = osp.boundary_pops(m) if sp else None
     for i in range(P.isite):
         t = qtensor([False, False, True])
         t.fromDenseTensor(P.lsites[i], [P.qnuml[i], QPHYS, P.qnuml[i + 1]])
         fN = {}
         ok.renorm(m, i, 1, [[fL, None]], [[fN]], t, 'L')
         fL = fN
+        if sp:
+            fNp = {}
+            osp.renormQt_S00(m, i, 1, [[None, None, fLp, None]], [[None, fNp]], t, 'L')
+            fLp = fNp
     fR = m._boundary('rop', P.K)
+    fRp = osp.boundary_pops(m) if sp else None
     for i in range(P.K - 1, P.isite + 1, -1):
         t = qtensor([True, False, False])
         t.fromDenseTensor(P.rsites[i], [P.qnumr[i], QPHYS, P.qnumr[i + 1]])
         fN = {}
         ok.renorm(m, i, 1, [[None, fR]], [[fN]], t, 'R')
         fR = fN
-    m.flst = [[fL, fR]]
+        if sp:
+            fNp = {}
+            osp.renormQt_S00(m, i, 1, [[None, None, None, fRp]], [[None, fNp]], t, 'R')
+            fRp = fNp
+    m.flst = [[fL, fR, fLp, fRp]] if sp else [[fL, fR]]
     m.dims = (len(P.qnuml[P.isite]), 16, len(P.qnumr[P.isite + 2]), 0)
     m.qlst = [P.qnuml[P.isite], QPHYS, QPHYS, P.qnumr[P.isite + 2]]
     m.setupQtmpCI(2, P.key)
@@ -160,27 +181,34 @@ def _product_side(P):
     from zmpo_dmrg_gb300.mpo_dmrg_class import mpo_dmrg
     from zmpo_dmrg_gb300.mpo_dmrg_kernel import renorm
     from zmpo_dmrg_gb300.qtensor import qtensor
+    from zmpo_dmrg_gb300 import spinproj
     m = mpo_dmrg(seed=P.seed)
     m.nsite, m.sbas, m.isym = P.K, 2 * P.K, 2
+    sp = P.npts is not None
+    if sp:
+        m.ifs2proj, m.npts = True, P.npts
+        m.s2quad(P.sval, P.sz)
     m.build()
     m.partition()
     m.loadInts((P.int1e, P.int2e))
     m.dumpMPO()
     fL = m.boundary_env()
+    fLp = spinproj.boundary_pops(m) if sp else None
     for i in range(P.isite):
         t = qtensor([False, False, True])
         t.fromDenseTensor(P.lsites[i], [P.qnuml[i], QPHYS, P.qnuml[i + 1]])
-        fN = [[None]]
-        renorm(m, i, 1, [[fL, None]], fN, t, 'L')
-        fL = fN[0][0]
+        fN = [[None, None]]
+        renorm(m, i, 1, [[fL, None, fLp, None]], fN, t, 'L')
+        fL, fLp = fN[0][0], fN[0][1]
     fR = m.boundary_env()
+    fRp = spinproj.boundary_pops(m) if sp else None
     for i in range(P.K - 1, P.isite + 1, -1):
         t = qtensor([True, False, False])
         t.fromDenseTensor(P.rsites[i], [P.qnumr[i], QPHYS, P.qnumr[i + 1]])
-        fN = [[None]]
-        renorm(m, i, 1, [[None, fR]], fN, t, 'R')
-        fR = fN[0][0]
-    m.flst = [[fL, fR]]
+        fN = [[None, None]]
+        renorm(m, i, 1, [[None, fR, None, fRp]], fN, t, 'R')
+        fR, fRp = fN[0][0], fN[0][1]
+    m.flst = [[fL, fR, fLp, fRp]] if sp else [[fL, fR]]
     m.qnuml, m.qnumr = list(P.qnuml), list(P.qnumr)
     m.qlst = [P.qnuml[P.isite], QPHYS, QPHYS, P.qnumr[P.isite + 2]]
     m.setupQtmpCI(2, P.key)
@@ -223,28 +251,37 @@ def _renorm_site(P):
             random_right_site(P.qnumr[i + 1], P.qnumr[i + 2], rng))
 
 
-def oracle_renorm(P, status):
+def oracle_renorm(P, status, which=0):
+    """New environments of the H_p terms (which=0) or, for a spin-projected
+    problem, of the P_g points (which=1)."""
     from oracle import kernel as ok
+    from oracle import spinproj as osp
     from oracle.qtensor import qtensor
     m = P.o
     A, B = _renorm_site(P)
     fN = {}
+    fNp = {}
     if status == 'L':
         t = qtensor([False, False, True])
         t.fromDenseTensor(A, [P.qnuml[P.isite], QPHYS, P.qnuml[P.isite + 1]])
         ok.renorm(m, P.isite, 1, m.flst, [[fN]], t, 'L')
+        if which == 1:
+            osp.renormQt_S00(m, P.isite, 1, m.flst, [[fN, fNp]], t, 'L')
     else:
         t = qtensor([True, False, False])
         t.fromDenseTensor(B, [P.qnumr[P.isite + 1], QPHYS, P.qnumr[P.isite + 2]])
         ok.renorm(m, P.isite, 2, m.flst, [[fN]], t, 'R')
+        if which == 1:
+            osp.renormQt_S00(m, P.isite, 2, m.flst, [[fN, fNp]], t, 'R')
+    f = fNp if which == 1 else fN
     out = []
-    for iop in range(m.nops):
-        v = fN['opers%d' % iop]
+    for iop in range(m.npts if which == 1 else m.nops):
+        v = f['opers%d' % iop]
         out.append(numpy.zeros(0) if v is None else v.value)
     return out
 
 
-def product_renorm(P, status, precision="fp64"):
+def product_renorm(P, status, precision="fp64", which=0):
     from zmpo_dmrg_gb300.mpo_dmrg_kernel import renorm
     from zmpo_dmrg_gb300.qtensor import qtensor
     m = P.p
@@ -259,13 +296,71 @@ def product_renorm(P, status, precision="fp64"):
         t = qtensor([True, False, False])
         t.fromDenseTensor(B, [P.qnumr[P.isite + 1], QPHYS, P.qnumr[P.isite + 2]])
         renorm(m, P.isite, 2, m.flst, fN, t, 'R')
-    E = fN[0][0]
+    E = fN[0][which]
     buf = E.buf.cpu().numpy()
     out = []
-    for iop in range(m.nops):
+    for iop in range(m.npts if which == 1 else m.nops):
         if E.off[iop] < 0:
             out.append(numpy.zeros(0))
         else:
             n = E.tensors[iop].size_allowed
             out.append(buf[E.off[iop]:E.off[iop] + n])
     return out
+
+
+def _random_civec(P, seed):
+    m = P.o
+    rng = numpy.random.default_rng(seed)
+    m.qtmp.value = rng.standard_normal(m.qtmp.size_allowed)
+    dense = m.qtmp.toDenseTensor(m.idlstCI)          # (ldim, 4, 4, rdim)
+    return dense / numpy.linalg.norm(dense)
+
+
+def prdm_inputs(P, status, seed=0):
+    c = _random_civec(P, seed)
+    ldim, rdim = c.shape[0], c.shape[3]
+    if status == 'L':
+        return c.reshape(1, ldim, 4, 4 * rdim)
+    return c.reshape(1, ldim * 4, 4, rdim)
+
+
+def oracle_prdm(P, status, noise=1e-4, seed=0):
+    from oracle import dmrg as od
+    m = P.o
+    m.noise, m.inoise = noise, 0
+    return od.pRDM(prdm_inputs(P, status, seed), [m, P.isite, 2, m.flst, status, True])
+
+
+def product_prdm(P, status, noise=1e-4, seed=0):
+    from zmpo_dmrg_gb300 import prdm
+    m = P.p
+    m.noise, m.inoise = noise, 0
+    m.qkey = numpy.array(P.key)
+    return prdm.pRDM(prdm_inputs(P, status, seed), [m, P.isite, 2, m.flst, status, True])
+
+
+def oracle_svec(P, x):
+    from oracle import spinproj as osp
+    m = P.o
+    return osp.SVecQt(numpy.asarray(x, dtype=float), [m, P.isite, 2, m.flst, 'L', True], P.ndim0, None)
+
+
+def product_svec(P, x):
+    from zmpo_dmrg_gb300.mpo_dmrg_kernel import SVec
+    m = P.p
+    return SVec(numpy.asarray(x, dtype=float), [m, P.isite, 2, m.flst, 'L', True], P.ndim0, None)
+
+
+def oracle_sdiag(P):
+    from oracle import spinproj as osp
+    m = P.o
+    prj = m.qtmp.prjmap(m.idlstCI)
+    ldim, rdim = len(P.qnuml[P.isite]), len(P.qnumr[P.isite + 2])
+    m.dims = (ldim, 16, rdim, ldim * 16 * rdim)
+    return osp.SDiagQt([m, P.isite, 2, m.flst, 'L', True], P.ndim0, prj)
+
+
+def product_sdiag(P):
+    from zmpo_dmrg_gb300.mpo_dmrg_kernel import SDiag
+    m = P.p
+    return SDiag([m, P.isite, 2, m.flst, 'L', True], P.ndim0, None).cpu().numpy()

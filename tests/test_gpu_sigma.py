@@ -6,7 +6,8 @@ import numpy
 import pytest
 
 from tests.problems import (random_problem, oracle_sigma, product_sigma, oracle_hdiag,
-                            product_hdiag, oracle_renorm, product_renorm)
+                            product_hdiag, oracle_renorm, product_renorm, oracle_prdm,
+                            product_prdm)
 
 pytestmark = pytest.mark.gpu
 
@@ -86,3 +87,16 @@ def test_sigma_graph_replay(gpu, precision):
         P.p.use_graph = False
     assert numpy.array_equal(a, eager)
     assert numpy.allclose(b, 2.0 * eager, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("case", CASES[1:4])
+@pytest.mark.parametrize("status", ["L", "R"])
+def test_perturbed_rdm(gpu, case, status):
+    """Noise density matrix of the decimation (pRDMQt) on the GPU."""
+    P = prob(case)
+    a = product_prdm(P, status)
+    b = oracle_prdm(P, status)
+    assert a.shape == b.shape
+    assert numpy.abs(a - b).max() <= 1e-12 * max(1.0, numpy.abs(b).max())
+    noise_part = oracle_prdm(P, status, noise=1.0) - oracle_prdm(P, status, noise=0.0)
+    assert numpy.abs(noise_part).max() > 1e-6   # the noise term is exercised

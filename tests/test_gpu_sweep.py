@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
 
 
-def _run(int1e, int2e, K, nelec, occ, maxM, tol, maxiter, precision="fp64", seed=1):
+def _run(int1e, int2e, K, nelec, occ, maxM, tol, maxiter, precision="fp64", seed=1, noise=0.0):
     from zmpo_dmrg_gb300.mpo_dmrg_class import mpo_dmrg
     from zmpo_dmrg_gb300.mpo_dmrg_schedule import schedule
     m = mpo_dmrg(seed=seed)
@@ -27,7 +27,7 @@ def _run(int1e, int2e, K, nelec, occ, maxM, tol, maxiter, precision="fp64", seed
     m.loadInts((int1e, int2e))
     m.dumpMPO()
     sc = schedule(maxM=maxM, tol=tol, maxiter=maxiter)
-    sc.startNoise = 0.0
+    sc.startNoise = noise
     sc.normal(2)
     m.default(sc)
     return m
@@ -58,3 +58,29 @@ def test_synthetic_k6_reaches_fci(gpu, hop, seed):
     assert abs(m.Energy - efci) < 1e-9
     ms = _run(i1, i2, K, 6, occ, 64, 1e-9, 10, precision="split")
     assert abs(ms.Energy - efci) < 1e-8
+
+
+def test_default_noise_schedule_k8(gpu):
+    """The reference's default schedule (perturbed density-matrix noise 1e-4 in
+    the first sweeps) with truncation: FP64 and split runs reach the same
+    energy, and the oracle with the same schedule agrees."""
+    from oracle import dmrg as od
+    K = 8
+    h, eri, _ = oint.synthetic(K, 21)
+    i1, i2, _ = oint.to_spin_orbital(h, eri)
+    occ = numpy.array([1., 1.] * 4 + [0., 0.] * 4)
+    m = _run(i1, i2, K, 8, occ, 48, 1e-9, 10, noise=1e-4)
+    ms = _run(i1, i2, K, 8, occ, 48, 1e-9, 10, precision="split", noise=1e-4)
+    assert abs(ms.Energy - m.Energy) < 1e-8
+    o = od.mpo_dmrg(seed=1)
+    o.nsite, o.sbas, o.isym = K, 2 * K, 2
+    o.build()
+    o.occun = occ
+    o.qsectors = {str([8.0, 0.0]): 1}
+    o.partition()
+    o.loadInts(i1, i2)
+    o.dumpMPO()
+    sc = od.schedule(maxM=48, tol=1e-9, maxiter=10)
+    sc.normal(2)
+    o.default(sc)
+    assert abs(o.Energy - m.Energy) < 1e-7

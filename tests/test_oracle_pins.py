@@ -141,3 +141,84 @@ def test_oracle_dmrg_reaches_fci_on_fcidump():
     m.default(sc)
     assert abs(m.Energy - efci) < 1e-9
     assert abs(m.Energy + float(z["ecore"]) - float(z["e_block"])) < 5e-9
+
+
+def _dense_spin_ops(K, npts, sval, sz):
+    """Exact Fock-space P = sum_g w_g exp(-i beta_g S_y) from the JW operators."""
+    import scipy.linalg
+    from oracle import spinproj as osp
+    a = integrals._jw_ops(2 * K)
+    sp = sum((a[2 * i].T @ a[2 * i + 1]) for i in range(K)).toarray()
+    gen = sp - sp.T
+
+    class Q:
+        pass
+    q = Q()
+    q.npts = npts
+    osp.s2quad(q, sval, sz)
+    P = sum(w * scipy.linalg.expm(-0.5 * b * gen) for b, w in zip(q.qpts, q.qwts))
+    return P, gen
+
+
+def test_spin_projection_exact_projector():
+    """The restated quadrature (smalld + s2quad) gives the exact spin projector
+    on the M = 0 sector of a K=4 Fock space: idempotent, and S^2 = S(S+1) on it."""
+    K, npts = 4, 4
+    P, gen = _dense_spin_ops(K, npts, 0, 0)
+    idx = integrals.sector_indices(2 * K, 4, 0.0)
+    Pm = P[numpy.ix_(idx, idx)]
+    assert numpy.abs(Pm @ Pm - Pm).max() < 1e-12
+    a = integrals._jw_ops(2 * K)
+    sp = sum((a[2 * i].T @ a[2 * i + 1]) for i in range(K)).toarray()
+    nup = sum((a[2 * i].T @ a[2 * i]) for i in range(K)).toarray()
+    ndn = sum((a[2 * i + 1].T @ a[2 * i + 1]) for i in range(K)).toarray()
+    szm = 0.5 * (nup - ndn)
+    s2 = sp.T @ sp + szm @ szm + szm
+    assert numpy.abs((s2 @ P)[numpy.ix_(idx, idx)]).max() < 1e-12
+    assert numpy.trace(Pm) > 0.5
+
+
+def test_spin_projected_kernels_equal_dense_operators():
+    """Oracle HVecQt / SVecQt / SDiagQt of a spin-projected two-site dot equal
+    U^T H P U x, U^T P U x and diag(U^T P U), with U the MPS basis of the dot
+    (K=4, N=4, S=0, 4 Gauss-Legendre points): pins the N-only relabelling,
+    the projection back on (N, Sz), the R(beta) site tensors and the P
+    environments built by renormQt_S00."""
+    import sys
+    sys.path.insert(0, os.path.dirname(__file__))
+    import problems
+    from oracle import spinproj as osp
+    K, nelec = 4, 4
+    P = problems.random_problem(K=K, nelec=nelec, D=16, isite=1, seed=5, device=False, npts=4)
+    m = P.o
+    h1e, eri, _ = integrals.synthetic(K, P.seed, 1.0)
+    _, _, gphys = integrals.to_spin_orbital(h1e, eri)
+    H = integrals.fci_hamiltonian(P.int1e, gphys).toarray()
+    Pd, _ = _dense_spin_ops(K, 4, 0, 0)
+    A0 = P.lsites[0][0]            # (4, ldim)
+    B3 = P.rsites[3][:, :, 0]      # (rdim, 4)
+
+    def up(x):
+        m.qtmp.value = numpy.asarray(x, dtype=float).copy()
+        psi = m.qtmp.toDenseTensor(m.idlstCI)
+        return numpy.einsum('al,lcdr,rb->acdb', A0, psi, B3).reshape(-1)
+
+    def down(f):
+        psi = numpy.einsum('al,acdb,rb->lcdr', A0, f.reshape(4, 4, 4, 4), B3)
+        t = oq.qtensor(m.qtmp.status)
+        t.fromQsyms(m.qtmp.rank, m.qtmp.qsyms, m.qtmp.ndims)
+        t.fromDense(psi, m.idlstCI)
+        return t.value
+
+    rng = numpy.random.default_rng(11)
+    x = rng.standard_normal(P.ndim0)
+    hx = ok.HVecQt(x, [m, 1, 2, m.flst, 'L', True], P.ndim0, None)
+    sx = osp.SVecQt(x, [m, 1, 2, m.flst, 'L', True], P.ndim0, None)
+    hx_ref = down(H @ (Pd @ up(x)))
+    sx_ref = down(Pd @ up(x))
+    assert numpy.abs(hx - hx_ref).max() < 1e-10 * numpy.abs(hx_ref).max()
+    assert numpy.abs(sx - sx_ref).max() < 1e-10 * numpy.abs(sx_ref).max()
+    sd = problems.oracle_sdiag(P)
+    eye = numpy.eye(P.ndim0)
+    sd_ref = numpy.array([down(Pd @ up(eye[i]))[i] for i in range(P.ndim0)])
+    assert numpy.abs(sd - sd_ref).max() < 1e-10

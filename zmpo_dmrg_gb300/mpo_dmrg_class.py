@@ -22,6 +22,7 @@ import numpy
 
 from . import mpo as _mpo
 from . import pdvdson
+from . import prdm
 from .mpo_dmrg_kernel import EnvSet, MPOStore, HVec, HDiag, renorm
 from .qtensor import qtensor, fromQnums
 
@@ -392,18 +393,14 @@ class mpo_dmrg:
             dim = self.dphys[jsite]
             cdimc = cdim // dim
             lcdim, crdim = ldim * cdimc, dim * rdim
-        if self.noise >= 1.e-10:
-            if self.inoise == 1:
-                civecs = civecs + self.rng.uniform(-1, 1, size=civecs.shape) * 10.0 * self.noise
-            else:
-                raise NotImplementedError(
-                    "perturbative (pRDM) noise is not available in this engine; use a schedule "
-                    "with zero noise or inoise = 1")
+        if self.noise >= 1.e-10 and self.inoise == 1:
+            civecs = civecs + self.rng.uniform(-1, 1, size=civecs.shape) * 10.0 * self.noise
         mats = civecs.reshape(neig, lcdim, crdim)
         if status == 'L':
-            rdm1 = numpy.einsum('eij,ekj->ik', mats, mats)
+            shaped = civecs.reshape(neig, ldim, dim, crdim)
         else:
-            rdm1 = numpy.einsum('eji,ejk->ik', mats, mats)
+            shaped = civecs.reshape(neig, lcdim, dim, rdim)
+        rdm1 = prdm.pRDM(shaped, info)
         tr = numpy.trace(rdm1)
         if tr < -1e-12:
             raise RuntimeError('RDM should be positive definite')
