@@ -160,3 +160,37 @@ def fci_energy(int1e, gphys, nelec, sz, nroots=1):
     Hs = H[idx][:, idx].toarray()
     e = numpy.linalg.eigvalsh(Hs)
     return e[:nroots]
+
+
+def spin_ops(sbas):
+    """S+ and S_z (sparse) with alpha = even spin orbital."""
+    a = _jw_ops(sbas)
+    K = sbas // 2
+    sp = a[0].T @ a[1]
+    for i in range(1, K):
+        sp = sp + a[2 * i].T @ a[2 * i + 1]
+    nup = a[0].T @ a[0]
+    ndn = a[1].T @ a[1]
+    for i in range(1, K):
+        nup = nup + a[2 * i].T @ a[2 * i]
+        ndn = ndn + a[2 * i + 1].T @ a[2 * i + 1]
+    return sp.tocsr(), (0.5 * (nup - ndn)).tocsr()
+
+
+def fci_spin_energy(int1e, gphys, nelec, sz, sval, nroots=1):
+    """Lowest eigenvalues of H restricted to S^2 = sval(sval+1) in the
+    (nelec, sz) sector (H and S^2 are diagonalised jointly)."""
+    sbas = int1e.shape[0]
+    H = fci_hamiltonian(int1e, gphys)
+    sp, szm = spin_ops(sbas)
+    s2 = (sp.T @ sp + szm @ szm + szm).tocsr()
+    idx = sector_indices(sbas, nelec, sz)
+    Hs = H[idx][:, idx].toarray()
+    S2 = s2[idx][:, idx].toarray()
+    w, v = numpy.linalg.eigh(S2)
+    sel = numpy.abs(w - sval * (sval + 1.0)) < 1e-8
+    if not numpy.any(sel):
+        return numpy.zeros(0)
+    u = v[:, sel]
+    e = numpy.linalg.eigvalsh(u.T @ Hs @ u)
+    return e[:nroots]

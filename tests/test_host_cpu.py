@@ -200,3 +200,66 @@ def test_rdm_blkdiag_matches_oracle():
         assert abs(a[0] - b[0]) < 1e-13
         assert numpy.array_equal(numpy.array(a[1]), numpy.array(b[1]))
         assert numpy.allclose(numpy.abs(a[2]), numpy.abs(b[2]), atol=1e-10)
+
+
+def test_generalised_davidson_matches_eigh():
+    """The generalised Davidson (pgdvdson restated, basis as torch tensors; CPU
+    here) reaches scipy's eigh(H, S) with restarts, S-normalised vectors."""
+    import scipy.linalg
+    import torch
+    from zmpo_dmrg_gb300 import pgdvdson
+    rng = numpy.random.default_rng(3)
+    n = 200
+    A = rng.standard_normal((n, n))
+    H = (A + A.T) / 2 + numpy.diag(numpy.arange(n) * 0.5)
+    B = rng.standard_normal((n, n)) * 0.05
+    S = numpy.eye(n) + B @ B.T
+    e_ref = scipy.linalg.eigh(H, S, eigvals_only=True)[:2]
+    Ht, St = torch.tensor(H), torch.tensor(S)
+    sol = pgdvdson.eigenSolver(numpy.random.default_rng(0))
+    sol.HVec = lambda v: Ht @ v
+    sol.SVec = lambda v: St @ v
+    sol.ndim, sol.neig = n, 2
+    sol.diag = torch.diag(Ht).clone()
+    sol.maxcycle = 200
+    sol.crit_e, sol.crit_vec = 1e-12, 1e-9
+    e, x, nmvp = sol.solve_iter()
+    assert sol.ifconv and nmvp > 2 * sol.nfac * sol.neig   # restarted at least once
+    assert numpy.abs(e - e_ref).max() < 1e-9
+    assert float(((x @ St) @ x.T - torch.eye(2, dtype=torch.float64)).abs().max()) < 1e-12
+
+
+def test_n_only_relabel_matches_oracle():
+    """Product N-only scatter / gather maps == the oracle's reduceQsymsToN and
+    projectionNMs on a spin-projected dot (bit-exact), and the quadrature
+    points and weights agree."""
+    import torch
+    from tests.problems import random_problem
+    from zmpo_dmrg_gb300 import spinproj
+    from zmpo_dmrg_gb300.qtensor import qtensor as pqt, fromQnums
+    from oracle import spinproj as osp
+    P = random_problem(K=6, nelec=5, D=16, isite=2, seed=2, device=False, npts=4, sval=0.5, sz=0.5)
+    m = P.o
+    qn = [m.qlst[0], m.qlst[1], m.qlst[2], m.qkey - m.qlst[3]]
+    t = pqt([False, False, False, True])
+    rank, qsyms, ndims, _ = fromQnums(qn)
+    t.fromQsyms(rank, qsyms, ndims, ifallocate=False)
+    qN, idx = spinproj.n_only_map(t)
+    x = numpy.random.default_rng(1).standard_normal(m.qtmp.size_allowed)
+    m.qtmp.value = x.copy()
+    red = m.qtmp.reduceQsymsToN()
+    assert qN.size_allowed == red.size_allowed
+    xN = numpy.zeros(qN.size_allowed)
+    xN[idx] = x
+    assert numpy.array_equal(xN, red.value)
+    y = numpy.random.default_rng(2).standard_normal(qN.size_allowed)
+    red.value = y.copy()
+    assert numpy.array_equal(y[idx], red.projectionNMs(m.qtmp.qsyms).value)
+
+    class Q:
+        npts = 6
+    a, b = Q(), Q()
+    spinproj.s2quad(a, 1.5, 0.5)
+    osp.s2quad(b, 1.5, 0.5)
+    assert numpy.abs(a.qpts - b.qpts).max() < 1e-14
+    assert numpy.abs(a.qwts - b.qwts).max() < 1e-13

@@ -22,8 +22,10 @@ import numpy
 
 from . import mpo as _mpo
 from . import pdvdson
+from . import pgdvdson
 from . import prdm
-from .mpo_dmrg_kernel import EnvSet, MPOStore, HVec, HDiag, renorm
+from . import spinproj
+from .mpo_dmrg_kernel import EnvSet, MPOStore, HVec, HDiag, SVec, renorm
 from .qtensor import qtensor, fromQnums
 
 
@@ -145,6 +147,8 @@ class mpo_dmrg:
         self.rng = numpy.random.default_rng(seed)
         # device state
         self.mpo_store = None
+        self.pop_store = None
+        self.exppop = None
         self.envs = {}
         self.flmps = {}
         self.frmps = {}
@@ -214,6 +218,8 @@ class mpo_dmrg:
                 pos += t.size_allowed
         buf = torch.from_numpy(numpy.concatenate(vals)).cuda()
         self.mpo_store = MPOStore(buf, off, tens)
+        if self.ifs2proj:
+            spinproj.dumpMPO_R(self)
         return 0
 
     def initStates(self):
@@ -265,42 +271,70 @@ class mpo_dmrg:
             fmps['qnum%d' % i] = qn[i]
         return fmps
 
+    def _flst(self, lsite, rsite):
+        """Environments of a dot: [L, R] or, spin-projected, [L, R, L_P, R_P]."""
+        f = [self.envs.get(('lop', lsite)), self.envs.get(('rop', rsite))]
+        if self.ifs2proj:
+            f += [self.envs.get(('lpop', lsite)), self.envs.get(('rpop', rsite))]
+        return [f]
+
+    def _store_envs(self, kind, isite, fN):
+        self.envs[(kind, isite)] = fN[0][0]
+        if self.ifs2proj:
+            self.envs[(kind[0] + 'pop', isite)] = fN[0][1]
+
+    @staticmethod
+    def _scalars(env, n):
+        vals = env.buf.cpu().numpy()
+        out = numpy.zeros(n)
+        for iop in range(n):
+            if env.off[iop] >= 0:
+                out[iop] = vals[env.off[iop]]
+        return out
+
     def genHops(self, fmps, kind='lop'):
-        """All left (or right) environments of an MPS and <H_p> at the end."""
+        """All left (or right) environments of an MPS and <H_p> at the end
+        (with spin projection also the P_g environments and <P_g>)."""
         nsite = self.nsite
         if kind == 'lop':
-            self.envs[('lop', -1)] = self.boundary_env()
-            order = range(nsite)
+            bnd, order = -1, range(nsite)
         else:
-            self.envs[('rop', nsite)] = self.boundary_env()
-            order = range(nsite - 1, -1, -1)
+            bnd, order = nsite, range(nsite - 1, -1, -1)
+        self.envs[(kind, bnd)] = self.boundary_env()
+        if self.ifs2proj:
+            self.envs[(kind[0] + 'pop', bnd)] = spinproj.boundary_pops(self)
         for isite in order:
             site = fmps['site%d' % isite]
             if kind == 'lop':
-                flst = [[self.envs[('lop', isite - 1)], None]]
+                flst = self._flst(isite - 1, None)
             else:
-                flst = [[None, self.envs[('rop', isite + 1)]]]
-            fN = [[None]]
+                flst = self._flst(None, isite + 1)
+            fN = [[None, None]]
             renorm(self, isite, 1, flst, fN, site, 'L' if kind == 'lop' else 'R')
-            self.envs[(kind, isite)] = fN[0][0]
-        last = self.envs[(kind, nsite - 1 if kind == 'lop' else 0)]
-        vals = last.buf.cpu().numpy()
-        exphop = numpy.zeros(self.nops)
-        for iop in range(self.nops):
-            if last.off[iop] >= 0:
-                exphop[iop] = vals[last.off[iop]]
+            self._store_envs(kind, isite, fN)
+        iend = nsite - 1 if kind == 'lop' else 0
+        exphop = self._scalars(self.envs[(kind, iend)], self.nops)
+        self.exppop = None
+        if self.ifs2proj:
+            self.exppop = self._scalars(self.envs[(kind[0] + 'pop', iend)], self.npts)
         return exphop
 
     def initOps(self, fmps):
         self.envs[('rop', self.nsite)] = self.boundary_env()
+        if self.ifs2proj:
+            self.envs[('rpop', self.nsite)] = spinproj.boundary_pops(self)
         self.genHops(fmps, 'lop')
         return 0
 
     def checkMPS(self, fbra=None):
-        """Energy sum_p w_p <H_p> of the left-canonical MPS (checkMPS 470-558)."""
+        """Energy sum_p w_p <H_p> (over sum_g w_g <P_g> with spin projection)
+        of the left-canonical MPS (checkMPS 470-558): (energy, <H(P)>, ovlp, <P>)."""
         fmps = self.flmps if fbra is None else fbra
         exphop = self.genHops(fmps, 'lop')
         esum = float(numpy.dot(self.hpwts, exphop))
+        if self.ifs2proj:
+            psum = float(numpy.dot(self.qwts, self.exppop))
+            return esum / psum, esum, 1.0, psum
         return esum, esum, 1.0, None
 
     # ----------------------------------------------------------- local solver
@@ -345,8 +379,13 @@ class mpo_dmrg:
                 diag = HDiag(info, ndim0, prjmap)
             else:
                 diag = torch.ones(ndim0, dtype=torch.float64, device="cuda")
-            solver = pdvdson.eigenSolver(self.rng)
-            solver.HVec = pdvdson.mask([info, ndim0, prjmap], HVec).matvec
+            if not self.ifs2proj:
+                solver = pdvdson.eigenSolver(self.rng)
+                solver.HVec = pdvdson.mask([info, ndim0, prjmap], HVec).matvec
+            else:
+                solver = pgdvdson.eigenSolver(self.rng)
+                solver.HVec = pgdvdson.mask([info, ndim0, prjmap], HVec).matvec
+                solver.SVec = pgdvdson.mask([info, ndim0, prjmap], SVec).matvec
             solver.crit_e = self.crit_e
             solver.crit_vec = self.crit_vec
             solver.ndim = ndim0
@@ -364,8 +403,10 @@ class mpo_dmrg:
                 saved = self.precision
                 self.precision = self.precision_final
                 for i in range(neig):
-                    hv = HVec(vec[i].contiguous(), info, ndim0, prjmap)
-                    eig[i] = float(torch.dot(vec[i], hv) / torch.dot(vec[i], vec[i]))
+                    v = vec[i].contiguous()
+                    hv = HVec(v, info, ndim0, prjmap)
+                    sv = SVec(v, info, ndim0, prjmap) if self.ifs2proj else v
+                    eig[i] = float(torch.dot(v, hv) / torch.dot(v, sv))
                 self.precision = saved
             civec = numpy.zeros((neig, ndim))
             civec[:, prjmap] = vec.cpu().numpy()
@@ -488,19 +529,19 @@ class mpo_dmrg:
         nmvp = 0
         for isite in actlst:
             t0 = time.perf_counter()
-            flst = [[self.envs[('lop', isite - 1)], self.envs[('rop', isite + ncsite)]]]
+            flst = self._flst(isite - 1, isite + ncsite)
             nmvps, eigs, sigs, dwts, qred, site, srotR = self.ci_solver(isite, ncsite, actlst, flst, status, ifsym)
             t1 = time.perf_counter()
             nmvp += nmvps
             elst.append(eigs)
             dlst.append(dwts)
             siteN = self.updateSite(isite, ncsite, qred, site, status)
-            fN = [[None]]
+            fN = [[None, None]]
             renorm(self, isite, ncsite, flst, fN, siteN, status)
             if status == 'L':
-                self.envs[('lop', isite)] = fN[0][0]
+                self._store_envs('lop', isite, fN)
             else:
-                self.envs[('rop', isite + ncsite - 1)] = fN[0][0]
+                self._store_envs('rop', isite + ncsite - 1, fN)
             torch.cuda.synchronize()
             self.timings.append((status, isite, t1 - t0, time.perf_counter() - t1, nmvps))
         self.updateBoundary(ncsite, sitelst, qred, srotR, status)

@@ -104,10 +104,19 @@ class SigmaPlan:
         if self.nops == 0:
             self.pid = None
             return
-        self.pid, ws = eng.sigma_plan(ncsite, op_cls, lay_L, lay_Wi, lay_Wj if ncsite == 2 else None,
-                                      lay_Rf, dmrg.qtmp_psi_layout, off_L, off_R, off_Wi,
-                                      off_Wj if ncsite == 2 else None, wts)
         torch = _torch()
+        lay_psi = dmrg.qtmp_psi_layout
+        self.nmap = None
+        if dmrg.ifs2proj:
+            # psi relabelled by N (reduceQsymsToN): same sectors, more allowed
+            # blocks; the result is read back on the (N, Sz) blocks only
+            from .spinproj import n_only_map
+            qN, idx = n_only_map(dmrg.qtmp)
+            lay_psi = qN.layout
+            self.nmap = (torch.as_tensor(idx, device="cuda"), qN.size_allowed)
+        self.pid, ws = eng.sigma_plan(ncsite, op_cls, lay_L, lay_Wi, lay_Wj if ncsite == 2 else None,
+                                      lay_Rf, lay_psi, off_L, off_R, off_Wi,
+                                      off_Wj if ncsite == 2 else None, wts)
         self.workspace = torch.empty(max(ws // 8, 1), dtype=torch.float64, device="cuda")
         self.flops, self.ntasks, self.nlaunch = eng.plan_stats(self.pid)
         self.fL, self.fR = fL, fR
@@ -119,6 +128,18 @@ class SigmaPlan:
         replayed on every later call of the site."""
         eng = _engine.get()
         W = dmrg.mpo_store.buf
+        if self.nmap is not None:
+            torch = _torch()
+            idx, nN = self.nmap
+            xN = torch.zeros(nN, dtype=torch.float64, device=x.device)
+            xN[idx] = x
+            yN = torch.empty_like(xN)
+            self._run(eng, W, xN, yN, precision, use_graph)
+            torch.index_select(yN, 0, idx, out=y)
+            return
+        self._run(eng, W, x, y, precision, use_graph)
+
+    def _run(self, eng, W, x, y, precision, use_graph):
         if not use_graph:
             eng.sigma(self.pid, self.fL.buf, self.fR.buf, W, x, y, self.workspace, precision)
             return
@@ -181,8 +202,15 @@ def HDiag(info, ndim0, prjmap):
     torch = _torch()
     plan = _sigma_plan(info)
     d = torch.zeros(ndim0, dtype=torch.float64, device="cuda")
-    if plan.pid is not None:
-        _engine.get().hdiag(plan.pid, plan.fL.buf, plan.fR.buf, dmrg.mpo_store.buf, d)
+    if plan.pid is None:
+        return d
+    if plan.nmap is not None:
+        idx, nN = plan.nmap
+        dN = torch.zeros(nN, dtype=torch.float64, device="cuda")
+        _engine.get().hdiag(plan.pid, plan.fL.buf, plan.fR.buf, dmrg.mpo_store.buf, dN)
+        torch.index_select(dN, 0, idx, out=d)
+        return d
+    _engine.get().hdiag(plan.pid, plan.fL.buf, plan.fR.buf, dmrg.mpo_store.buf, d)
     return d
 
 
@@ -194,6 +222,9 @@ def renorm(dmrg, isite, ncsite, flst, flstN, site, status):
     torch = _torch()
     mpo = dmrg.mpo_store
     qsite = site
+    if dmrg.ifs2proj:
+        from .spinproj import reduce_site
+        qsite = reduce_site(site)
     if status == 'L':
         fE = flst[0][0]
         jsite = isite
@@ -246,7 +277,21 @@ def renorm(dmrg, isite, ncsite, flst, flstN, site, status):
             tens[iop] = struct[c]
         eng.destroy_plan(pid)
     flstN[0][0] = EnvSet(buf, off, lays, tens)
+    if dmrg.ifs2proj:
+        from .spinproj import renorm_S00
+        renorm_S00(dmrg, isite, ncsite, flst, flstN, site, status)
     return 0
+
+
+def SVec(vec0, info, ndim0, prjmap):
+    """S psi for the spin-projected problem (``mpo_dmrg_kernel.SVec``, 226-231)."""
+    from .spinproj import SVec as _svec
+    return _svec(vec0, info, ndim0, prjmap)
+
+
+def SDiag(info, ndim0, prjmap):
+    from .spinproj import SDiag as _sdiag
+    return _sdiag(info, ndim0, prjmap)
 
 
 def _env_structure(dmrg, status, qsite, wt, env, lay_out):

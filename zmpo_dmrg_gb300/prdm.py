@@ -59,8 +59,8 @@ def pRDM(civecs, info):
         rho = numpy.einsum('eji,ejk->ik', mats, mats)
     if not (dmrg.inoise == 0 and dmrg.noise >= 1.e-10):
         return rho
-    if ncsite != 2 or dmrg.ifs2proj:
-        raise NotImplementedError("perturbed RDM is built for the two-site dot without spin projection")
+    if ncsite != 2:
+        raise NotImplementedError("perturbed RDM is built for the two-site dot")
     eng = _engine.get()
     qkey = numpy.asarray(dmrg.qkey, dtype=float)
     ql, qc1, qc2, qr = dmrg.qlst
@@ -77,6 +77,12 @@ def pRDM(civecs, info):
     psi = qtensor([False, False, True])
     rank, qsyms, ndims, idlst = fromQnums(qn)
     psi.fromQsyms(rank, qsyms, ndims, ifallocate=False)
+    lay_psi, nmap = psi.layout, None
+    if dmrg.ifs2proj:
+        # spin projection: the terms carry N-only labels (reduceQsymsToN)
+        from .spinproj import n_only_map
+        psiN, idx = n_only_map(psi)
+        lay_psi, nmap = psiN.layout, (idx, psiN.size_allowed)
     mpo = dmrg.mpo_store
     from .mpo import op_class
     chains = {}
@@ -95,7 +101,7 @@ def pRDM(civecs, info):
                 st = et.status.copy()
                 st[1] = not st[1]
                 lay_env = eng.derive(et.layout, [-et.qsyms[0], et.qsyms[1] - q0, q0 - et.qsyms[2]], st)
-            chains[c0] = _Chain(eng, lay_env, wt.layout, psi.layout, status)
+            chains[c0] = _Chain(eng, lay_env, wt.layout, lay_psi, status)
         ch = chains[c0]
         if acc is None:
             acc = torch.zeros(ch.sizes[2], dtype=torch.float64, device="cuda")
@@ -105,7 +111,11 @@ def pRDM(civecs, info):
         w_view = mpo.buf.narrow(0, int(mpo.off[jsite][iop]), mpo.tensors[jsite][iop].size_allowed)
         for e in range(neig):
             psi.fromDense(civecs[e], idlst)
-            x = torch.from_numpy(psi.value).cuda()
+            xv = psi.value
+            if nmap is not None:
+                xv = numpy.zeros(nmap[1])
+                xv[nmap[0]] = psi.value
+            x = torch.from_numpy(xv).cuda()
             t1 = torch.empty(max(ch.sizes[0], 1), dtype=torch.float64, device="cuda")
             t2 = torch.empty(max(ch.sizes[1], 1), dtype=torch.float64, device="cuda")
             if status == 'L':
