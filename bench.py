@@ -29,6 +29,7 @@ sys.path.insert(0, HERE)
 
 WORKLOAD = dict(K=24, nelec=24, D=512, isite=11, seed=2024)
 SMALL = dict(K=12, nelec=12, D=128, isite=5, seed=2024)
+MEDIUM = dict(K=16, nelec=16, D=256, isite=7, seed=2024)
 METRIC = "sweep s & sigma-vec TFLOP/s, split-BF16 vs FP64 on 1 GB300 at ΔE≤1e-8 Eh"
 
 
@@ -88,10 +89,11 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def build_problem(with_oracle=False, small=False):
+def build_problem(with_oracle=False, small=False, medium=False):
     from tests.problems import random_problem
     t0 = time.perf_counter()
-    P = random_problem(device=True, with_oracle=with_oracle, **(SMALL if small else WORKLOAD))
+    cfg = SMALL if small else (MEDIUM if medium else WORKLOAD)
+    P = random_problem(device=True, with_oracle=with_oracle, **cfg)
     return P, time.perf_counter() - t0
 
 
@@ -221,6 +223,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--small", action="store_true", help="K=12, D=128 case (profiling)")
+    ap.add_argument("--medium", action="store_true", help="K=16, D=256 case (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -238,7 +241,7 @@ def main():
     from zmpo_dmrg_gb300 import engine as E
     from zmpo_dmrg_gb300.mpo_dmrg_kernel import HVec, _sigma_plan
 
-    P, t_build = build_problem(small=args.small)
+    P, t_build = build_problem(small=args.small, medium=args.medium)
     pm = P.p
     info = [pm, P.isite, 2, pm.flst, 'L', True]
     eng = E.get()
@@ -329,7 +332,8 @@ def main():
         "warmup": max(args.warmup, 3), "ms_per_step": tmax * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 (bf16 digit slices, fp32 accumulate)",
         "data": "synthetic (seeded integrals + seeded random block-sparse MPS)",
-        "config": {"workload": "two-site H.psi, K=24 N=24 Sz=0 D=512, 48 terms, (N,Sz) blocks",
+        "config": {"workload": "two-site H.psi, K=%d N=%d Sz=0 D=%d, %d terms, (N,Sz) blocks" %
+                               (P.K, P.nelec, P.D, pm.nops),
                    "ndim0": n, "F_ref_flops": flops, "tasks": plan.ntasks, "precision": args.precision,
                    "l2": "inputs larger than L2 (environments %.2f GB)" % ((L.numel() + R.numel()) * 8 / 1e9),
                    "build_s": t_build},
@@ -337,10 +341,10 @@ def main():
         "split_vs_fp64_rel_err": err_split,
         "e2e": {"value": flops / t_e2e / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": n * 8,
                 "d2h_bytes_per_step": n * 8},
-        "gpu_launches": args.steps * plan.nlaunch,
+        "gpu_launches": args.steps * eng.kernel_count(plan.pid, args.precision),
         "clocks": clocks_rec,
         "launches": launches,
-        "roofline": {"bound": "hbm", "kernel": "k_step_split<4> launch %d of %d" % (top, plan.nlaunch),
+        "roofline": {"bound": "hbm", "kernel": "k_step_tc (all tile shapes) of step %d of %d" % (top, plan.nlaunch),
                      "achieved": launches[top]["GBs"], "peak": hbm, "unit": "GB/s",
                      "frac": (launches[top]["GBs"] or 0.0) / hbm, "traffic": None,
                      "peak_source": peak_kind},

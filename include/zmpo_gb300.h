@@ -138,6 +138,10 @@ int zmpo_sigma_workspace(zmpo_engine *e, int plan_id, int64_t *bytes);
  * task lists), and the number of tasks / launches. */
 int zmpo_plan_stats(zmpo_engine *e, int plan_id, double *flops,
                     int64_t *ntasks, int *nlaunch);
+/* Number of kernel launches one execution of the plan issues at this
+ * precision (grouped GEMM launches per tile shape plus split-K sums).  No
+ * reference counterpart: it reports what the engine will launch. */
+int zmpo_plan_kernel_count(zmpo_engine *e, int plan_id, int precision, int *count);
 /* y = H x (ndim0 = size of lay_psi).  d_x, d_y device vectors. */
 int zmpo_sigma(zmpo_engine *e, int plan_id, const double *d_L,
                const double *d_R, const double *d_W, const double *d_x,

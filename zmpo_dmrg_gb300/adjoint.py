@@ -1,0 +1,223 @@
+"""Energy gradient with respect to the integrals at a converged MPS.
+
+E(h1e, eri) = sum_p w_p <psi| H_p(h1e, eri) |psi> / <psi|psi> at a fixed MPS
+psi (at a converged state the Hellmann-Feynman gradient).  E is linear in
+every MPO site tensor W_p(j), so
+
+    dE/dW_p(j)[a,b,n',n] = sum L_p(j-1)[a,l,l'] A_j[l,n',r] A_j[l',n,r'] R_p(j+1)[b,r,r']
+
+with L and R the environments of the same MPS (exact for any gauge: the
+left-canonical sites of the last sweep serve for both sides).  These site
+gradients are engine contractions (three per term and site, block-sparse,
+FP64 on the GPU); the chain rule through the MPO construction and the
+spin-orbital expansion of the integrals is the torch autograd of the same
+builder (``mpo.hp_spatial_site`` with torch tensors).  ``EnergyGradient`` is
+the ``torch.autograd.Function`` wrapping it: forward returns E, backward
+dE/dh1e (K x K) and dE/d(pq|rs) (K^4).
+
+For the reference, dE/dh1e is the spin-summed one-particle density matrix
+(``properties/mpo_dmrg_propsItrf.eval_rdm1BF``, propsItrf.py:204-263) and
+dE/d(pq|rs) half the two-particle one (``genMPO_Apqrs`` with ``evalProps``,
+propsMPO.py:73-113).
+"""
+import numpy
+
+from . import engine as _engine
+from . import mpo as _mpo
+from .mpo import op_class
+from .qtensor import qtensor
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def spin_orbital_torch(h1e, eri):
+    """Differentiable copy of ``integrals.spin_orbital`` (torch tensors)."""
+    torch = _torch()
+    K = h1e.shape[0]
+    n = 2 * K
+    int1e = torch.zeros((n, n), dtype=h1e.dtype, device=h1e.device)
+    int1e[0::2, 0::2] = h1e
+    int1e[1::2, 1::2] = h1e
+    chem = torch.zeros((n, n, n, n), dtype=eri.dtype, device=eri.device)
+    for s in (0, 1):
+        for t in (0, 1):
+            chem[s::2, s::2, t::2, t::2] = eri
+    g = chem.permute(0, 2, 1, 3)
+    int2e = -0.5 * (g - g.permute(0, 1, 3, 2))
+    return int1e, int2e
+
+
+def _right_convention(site, qkey):
+    """A left-canonical site [l, n, r] (status F,F,T) relabelled as a site of
+    the right block (status T,F,F; labels qkey - q on both bonds): the same
+    allowed blocks and packing, so the values carry over unchanged."""
+    t = qtensor([True, False, False])
+    q = [qkey - site.qsyms[0], site.qsyms[1], qkey - site.qsyms[2]]
+    t.fromQsyms(3, q, site.ndims, ifallocate=False)
+    if t.size_allowed != site.size_allowed or not numpy.array_equal(t.blk_flat, site.blk_flat):
+        raise RuntimeError("site relabelling changed the block structure")
+    t.value = site.value
+    t.idlst = site.idlst
+    return t
+
+
+class _GradChain:
+    """Three contractions of one operator class at one site:
+    t1 = A . L over the bra left bond, u = t1 . A over the ket left bond,
+    G = u . Rf over both right bonds -> G[n', a, n, b]."""
+
+    def __init__(self, eng, lay_site, lay_L, lay_Rf):
+        lo1, self.p1 = eng.contract_plan(lay_site, lay_L, ([0], [1]))
+        lo2, self.p2 = eng.contract_plan(lo1, lay_site, ([3], [0]))
+        self.lay_out, self.p3 = eng.contract_plan(lo2, lay_Rf, ([1, 4], [1, 2]))
+        self.sizes = [eng.layout_blocks(x)[0] for x in (lo1, lo2, self.lay_out)]
+
+    def release(self, eng):
+        for p in (self.p1, self.p2, self.p3):
+            eng.destroy_plan(p)
+
+
+def right_environments(dmrg, fmps):
+    """R_p(j) for j = nsite-1 .. 0 from the left-canonical sites."""
+    from .mpo_dmrg_kernel import renorm
+    nsite = dmrg.nsite
+    qkey = numpy.asarray(fmps['qnum%d' % nsite], dtype=float)[0]
+    envs = {nsite: dmrg.boundary_env()}
+    for j in range(nsite - 1, -1, -1):
+        site = _right_convention(fmps['site%d' % j], qkey)
+        fN = [[None, None]]
+        renorm(dmrg, j, 1, [[None, envs[j + 1]]], fN, site, 'R')
+        envs[j] = fN[0][0]
+    return envs, qkey
+
+
+def site_gradients(dmrg, fmps=None):
+    """dE/dW_p(j) for every site j and term p as dense [Dw_l, Dw_r, 4, 4]
+    arrays in the builder's bond order, and <H> and <psi|psi> of the MPS."""
+    torch = _torch()
+    if dmrg.ifs2proj:
+        raise NotImplementedError("energy gradient of the spin-projected energy")
+    fmps = dmrg.flmps if fmps is None else fmps
+    eng = _engine.get()
+    nsite = dmrg.nsite
+    exphop = dmrg.genHops(fmps, 'lop')
+    esum = float(numpy.dot(dmrg.hpwts, exphop))
+    last = fmps['site%d' % (nsite - 1)]
+    norm2 = float(numpy.dot(last.value, last.value))
+    Lenv = {j: dmrg.envs[('lop', j)] for j in range(-1, nsite)}
+    Renv, qkey = right_environments(dmrg, fmps)
+    mpo = dmrg.mpo_store
+    grads = [[None] * dmrg.nops for _ in range(nsite)]
+    for j in range(nsite):
+        site = fmps['site%d' % j]
+        sval = torch.from_numpy(numpy.ascontiguousarray(site.value)).cuda()
+        fL, fR = Lenv[j - 1], Renv[j + 1]
+        chains = {}
+        for iop in range(dmrg.nops):
+            if not (fL.present(iop) and fR.present(iop)):
+                continue
+            c0 = op_class(dmrg.opers[iop][0], j)
+            if c0 not in chains:
+                rt = fR.tensors[iop]
+                lay_rf = eng.derive(rt.layout, [-rt.qsyms[0], qkey - rt.qsyms[1], qkey - rt.qsyms[2]],
+                                    rt.status)
+                chains[c0] = _GradChain(eng, site.layout, fL.layouts[iop], lay_rf)
+            ch = chains[c0]
+            lv = fL.buf.narrow(0, int(fL.off[iop]), fL.tensors[iop].size_allowed)
+            rv = fR.buf.narrow(0, int(fR.off[iop]), fR.tensors[iop].size_allowed)
+            t1 = torch.empty(max(ch.sizes[0], 1), dtype=torch.float64, device="cuda")
+            t2 = torch.empty(max(ch.sizes[1], 1), dtype=torch.float64, device="cuda")
+            g = torch.empty(max(ch.sizes[2], 1), dtype=torch.float64, device="cuda")
+            eng.contract_exec(ch.p1, sval, lv, t1)
+            eng.contract_exec(ch.p2, t1, sval, t2)
+            eng.contract_exec(ch.p3, t2, rv, g)
+            wt = mpo.tensors[j][iop]
+            # legs [n', a, n, b]: directions follow the contraction (bra
+            # site against the bra leg of L, ket legs against ket legs)
+            out = qtensor([False, False, True, True])
+            out.fromQsyms(4, [site.qsyms[1], wt.qsyms[0], site.qsyms[1], wt.qsyms[1]],
+                          [site.ndims[1], wt.ndims[0], site.ndims[1], wt.ndims[1]], ifallocate=False)
+            size, flat, _ = eng.layout_blocks(ch.lay_out)
+            if size != out.size_allowed or not numpy.array_equal(flat, out.blk_flat):
+                raise RuntimeError("site gradient layout mismatch")
+            out.value = g[:size].cpu().numpy()
+            dense = out.toDenseTensor([site.idlst[1], wt.idlst[0], site.idlst[1], wt.idlst[1]])
+            gq = dense.transpose(1, 3, 0, 2)            # [a, b, n', n] in sorted bond order
+            il, ir = _mpo.bond_order(dmrg.opers[iop], dmrg.sbas, j)
+            gb = numpy.zeros_like(gq)
+            gb[numpy.ix_(il, ir)] = gq
+            grads[j][iop] = dmrg.hpwts[iop] * gb / norm2
+        for ch in chains.values():
+            ch.release(eng)
+    return grads, esum / norm2, norm2
+
+
+def integral_gradients(dmrg, h1e, eri, grads):
+    """Chain rule from the site gradients to dE/dh1e and dE/d(pq|rs)
+    (spatial orbitals) through the torch build of every W_p(j)."""
+    torch = _torch()
+    with torch.enable_grad():   # also when called from a Function's backward
+        h = torch.tensor(numpy.asarray(h1e, dtype=float), requires_grad=True)
+        g = torch.tensor(numpy.asarray(eri, dtype=float), requires_grad=True)
+        int1e, int2e = spin_orbital_torch(h, g)
+        int1e = int1e[dmrg.pidx]
+        int2e = int2e[dmrg.pidx]
+        total = torch.zeros((), dtype=torch.float64)
+        for j in range(dmrg.nsite):
+            for iop in range(dmrg.nops):
+                G = grads[j][iop]
+                if G is None:
+                    continue
+                W = _mpo.hp_spatial_site(dmrg.opers[iop], dmrg.sbas, j, int1e, int2e, None, dmrg.pdic)
+                total = total + (W * torch.from_numpy(G)).sum()
+        total.backward()
+    return h.grad.numpy().copy(), g.grad.numpy().copy()
+
+
+def symmetrize_eri_gradient(d):
+    """Average over the eight index permutations that leave (pq|rs) invariant."""
+    perms = [(0, 1, 2, 3), (1, 0, 2, 3), (0, 1, 3, 2), (1, 0, 3, 2),
+             (2, 3, 0, 1), (3, 2, 0, 1), (2, 3, 1, 0), (3, 2, 1, 0)]
+    return sum(d.transpose(p) for p in perms) / 8.0
+
+
+def _make_function():
+    torch = _torch()
+
+    class EnergyGradient(torch.autograd.Function):
+        """E(h1e, eri) at the MPS held by ``dmrg``; backward is the adjoint of
+        the H.psi contraction (site gradients) chained through the builder."""
+
+        @staticmethod
+        def forward(ctx, h1e, eri, dmrg):
+            from .integrals import spin_orbital
+            int1e, int2e = spin_orbital(h1e.detach().cpu().numpy(), eri.detach().cpu().numpy())
+            dmrg.loadInts((int1e, int2e))
+            dmrg.dumpMPO()
+            grads, energy, _ = site_gradients(dmrg)
+            ctx.saved = (dmrg, h1e.detach().cpu().numpy(), eri.detach().cpu().numpy(), grads)
+            return torch.tensor(energy, dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, gout):
+            dmrg, h1e, eri, grads = ctx.saved
+            dh, dg = integral_gradients(dmrg, h1e, eri, grads)
+            s = float(gout)
+            return torch.from_numpy(dh * s), torch.from_numpy(dg * s), None
+
+    return EnergyGradient
+
+
+_FN = None
+
+
+def energy(h1e, eri, dmrg):
+    """E at the MPS of ``dmrg`` as a differentiable function of the spatial
+    integrals (torch float64 tensors)."""
+    global _FN
+    if _FN is None:
+        _FN = _make_function()
+    return _FN.apply(h1e, eri, dmrg)

@@ -152,6 +152,61 @@ __device__ __forceinline__ void digits_bf16(double x, int E, __nv_bfloat16 *d, i
   }
 }
 
+// S = 4: the 32 most significant bits of |x|'s significand aligned to the
+// chunk exponent E (E >= exponent of x), truncated -- the same bits the
+// 64-bit path keeps -- using 32-bit integer operations only.  Its four bytes
+// are the four digits, most significant first.
+__device__ __forceinline__ uint32_t aligned32(double x, int E) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const int e = (int)((hi >> 20) & 0x7ffu);
+  const uint32_t top = e ? ((((hi & 0xfffffu) | 0x100000u) << 11) | (lo >> 21)) : 0u;
+  return __funnelshift_rc(top, 0u, (unsigned)(E - e));
+}
+
+// byte k of X as the bit pattern of the float 2^23 + byte (PRMT), then the
+// exact float value of the byte (one FADD)
+template <int K>
+__device__ __forceinline__ float byte_to_float(uint32_t X) {
+  return __uint_as_float(__byte_perm(X, 0x4B000000u, 0x7440u | K)) - 8388608.0f;
+}
+
+// four digit planes of two neighbouring elements (same row, k and k+1) as
+// packed bf16 pairs: the bf16 of a byte-valued float is its upper half
+__device__ __forceinline__ void digits4_pair(double x0, double x1, int E, uint32_t *d, int stride_u32) {
+  const uint32_t X0 = aligned32(x0, E), X1 = aligned32(x1, E);
+  const uint32_t sg = ((unsigned)__double2hiint(x0) >> 16 & 0x8000u) | ((unsigned)__double2hiint(x1) & 0x80000000u);
+  d[0] = __byte_perm(__float_as_uint(byte_to_float<3>(X0)), __float_as_uint(byte_to_float<3>(X1)), 0x7632u) | sg;
+  d[stride_u32] = __byte_perm(__float_as_uint(byte_to_float<2>(X0)), __float_as_uint(byte_to_float<2>(X1)), 0x7632u) | sg;
+  d[2 * stride_u32] = __byte_perm(__float_as_uint(byte_to_float<1>(X0)), __float_as_uint(byte_to_float<1>(X1)), 0x7632u) | sg;
+  d[3 * stride_u32] = __byte_perm(__float_as_uint(byte_to_float<0>(X0)), __float_as_uint(byte_to_float<0>(X1)), 0x7632u) | sg;
+}
+
+// single element variant (one bf16 per plane)
+__device__ __forceinline__ void digits4_one(double x, int E, __nv_bfloat16 *d, int stride) {
+  const uint32_t X = aligned32(x, E);
+  const unsigned short sg = (unsigned short)((unsigned)__double2hiint(x) >> 16 & 0x8000u);
+  unsigned short *u = reinterpret_cast<unsigned short *>(d);
+  u[0] = (unsigned short)(__float_as_uint(byte_to_float<3>(X)) >> 16) | sg;
+  u[stride] = (unsigned short)(__float_as_uint(byte_to_float<2>(X)) >> 16) | sg;
+  u[2 * stride] = (unsigned short)(__float_as_uint(byte_to_float<1>(X)) >> 16) | sg;
+  u[3 * stride] = (unsigned short)(__float_as_uint(byte_to_float<0>(X)) >> 16) | sg;
+}
+
+// 2^k as a float for k in the float range (subnormal powers of two are exact;
+// below 2^-149 the contribution is dropped)
+__device__ __forceinline__ float pow2f(int k) {
+  if (k > 127) k = 127;
+  if (k >= -126) return __int_as_float((k + 127) << 23);
+  if (k >= -149) return __int_as_float(1 << (k + 149));
+  return 0.f;
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float z = s - a;
+  e = (a - (s - z)) + (b - z);
+}
+
 // exact power of two 2^k times v (two steps below the normal range)
 __device__ __forceinline__ float scale_pow2(float v, int k) {
   if (k >= -126) {
@@ -187,223 +242,247 @@ struct Slot {
   int pad;
 };
 
+// Slot table of the next chunk, built by warp 0: lane l looks at segment
+// cur+l; an inclusive warp scan of the slots each segment can still provide
+// places every segment's k range inside the 32 slots.  cursor[0] = next
+// segment, cursor[1] = k offset inside it; *nslot = slots filled (0 = done).
+__device__ __forceinline__ void build_slots(const Group &g, const Seg *__restrict__ segs,
+                                            const Bufs &bufs, Slot *slots, int *cursor,
+                                            int *nslot, int lane) {
+  const int cur = cursor[0], curk = cursor[1];
+  if (cur >= g.nseg) {
+    if (lane == 0) *nslot = 0;
+    return;
+  }
+  const int sidx = cur + lane;
+  Seg sg;
+  int avail = 0;
+  if (sidx < g.nseg) {
+    sg = segs[g.seg0 + sidx];
+    avail = sg.K - (lane == 0 ? curk : 0);
+  }
+  int incl = avail;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int excl = incl - avail;
+  if (avail > 0 && excl < T_TK) {
+    const double *A = bufs.p[sg.abuf] + sg.a_off;
+    const double *B = bufs.p[sg.bbuf] + sg.b_off;
+    const int k0 = lane == 0 ? curk : 0;
+    const int jend = min(incl, T_TK);
+    for (int j = excl; j < jend; ++j) {
+      const int kk = k0 + (j - excl);
+      slots[j].a = A + (int64_t)kk * sg.sak;
+      slots[j].b = B + (int64_t)kk * sg.sbk;
+      slots[j].sam = sg.sam;
+      slots[j].sbn = sg.sbn;
+      slots[j].alpha = sg.alpha;
+      slots[j].scaled = sg.alpha != 1.0;
+    }
+  }
+  // where the chunk ends: first lane whose inclusive sum reaches 32
+  const unsigned reach = __ballot_sync(0xffffffffu, incl >= T_TK && avail > 0);
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  const int lstop = reach ? (__ffs(reach) - 1) : -1;
+  const int stop_incl = __shfl_sync(0xffffffffu, incl, lstop < 0 ? 31 : lstop);
+  const int stop_excl = __shfl_sync(0xffffffffu, excl, lstop < 0 ? 31 : lstop);
+  if (lane == 0) {
+    if (lstop < 0) {  // every remaining segment fits (or the 32 lanes ran out)
+      const int nseen = min(32, g.nseg - cur);
+      *nslot = min(total, T_TK);
+      cursor[0] = cur + nseen;
+      cursor[1] = 0;
+    } else {
+      *nslot = T_TK;
+      const int used = T_TK - stop_excl;  // slots taken from segment cur+lstop
+      const int base = lstop == 0 ? curk : 0;
+      if (stop_incl == T_TK) {
+        cursor[0] = cur + lstop + 1;
+        cursor[1] = 0;
+      } else {
+        cursor[0] = cur + lstop;
+        cursor[1] = base + used;
+      }
+    }
+  }
+}
+
+// One CTA per output tile of TM rows x TN columns; warps tile it in m16 x n8
+// pieces (TM/16 x TN/8 warps), so each thread holds one m16n8 accumulator
+// per digit level.  A chunk of 32 k slots is cut by TPR threads per row of A
+// and TPC threads per column of B.  Per chunk: slot table (warp 0), operands
+// to digit planes, digit products, scaled sums; three barriers.
 template <int S, int TM, int TN>
-__global__ void __launch_bounds__(2 * TM, (S <= 4 ? 768 : 512) / (2 * TM))
+struct TcShape {
+  static constexpr int WM = TM / 16, WN = TN / 8;
+  static constexpr int NT = 32 * WM * WN;     // threads per CTA
+  static constexpr int TPR = NT / TM;         // threads per row of A
+  static constexpr int KPA = T_TK / TPR;      // A slots per thread
+  static constexpr int TPC = NT / TN;         // threads per column of B
+  static constexpr int KPB = T_TK / TPC;      // B slots per thread
+  // resident threads per SM the register budget is sized for (16 A slots
+  // per thread need more registers than 8)
+  static constexpr int THREADS_SM = KPA > 8 ? 768 : 1024;
+  static_assert(TPR >= 1 && KPA >= 1 && TPC >= 1 && KPB >= 1, "tile shape");
+};
+
+template <int S, int TM, int TN>
+__global__ void __launch_bounds__(TcShape<S, TM, TN>::NT, TcShape<S, TM, TN>::THREADS_SM / TcShape<S, TM, TN>::NT)
 k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
           const Seg *__restrict__ segs, Bufs bufs) {
-  constexpr int T_TM = TM, T_NT = 2 * TM;  // two threads per row, one m16 tile per warp
-  constexpr int NTL = TN / 8;  // n8 tiles per warp
+  using Sh = TcShape<S, TM, TN>;
+  constexpr int TPR = Sh::TPR, KPA = Sh::KPA, TPC = Sh::TPC, KPB = Sh::KPB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __nv_bfloat16 *Ap = reinterpret_cast<__nv_bfloat16 *>(smem_raw);  // [S][TM][PAD]
-  __nv_bfloat16 *Bp = Ap + S * T_TM * T_PAD;                        // [S][TN][PAD]
+  __nv_bfloat16 *Bp = Ap + S * TM * T_PAD;                          // [S][TN][PAD]
   int *Ea = reinterpret_cast<int *>(Bp + S * TN * T_PAD);           // [TM]
-  int *Eb = Ea + T_TM;                                              // [TN]
+  int *Eb = Ea + TM;                                                // [TN]
   Slot *slots = reinterpret_cast<Slot *>(Eb + 16);                  // [TK]
-  int *ctl = reinterpret_cast<int *>(slots + T_TK);                 // nslot, si, ki
+  int *ctl = reinterpret_cast<int *>(slots + T_TK);                 // cursor[2], nslot
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = warp * 16;  // one m16 tile per warp
+  const int wm = (warp % Sh::WM) * 16, wn = (warp / Sh::WM) * 8;  // this warp's m16n8 piece
   const int gq = lane >> 2, tq = lane & 3;
-  constexpr int MT = 1;
+  const int ra = tid / TPR, parta = tid % TPR;  // A: row, part of the chunk
+  const int cb = tid / TPC, partb = tid % TPC;  // B: column, part of the chunk
 
   for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
     const Work wk = work[w];
     const Group g = groups[wk.group];
-    const int m0 = wk.mt * T_TM, n0 = wk.nt * TN;
-    float hi[MT][NTL][4], lo[MT][NTL][4];
-#pragma unroll
-    for (int mt = 0; mt < MT; ++mt)
-#pragma unroll
-      for (int nt = 0; nt < NTL; ++nt)
-#pragma unroll
-        for (int i = 0; i < 4; ++i) hi[mt][nt][i] = lo[mt][nt][i] = 0.f;
+    const int m0 = wk.mt * TM, n0 = wk.nt * TN;
+    const int rowa = m0 + ra, colb = n0 + cb;
+    float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
     if (tid == 0) {
+      ctl[0] = 0;
       ctl[1] = 0;
-      ctl[2] = 0;
     }
     __syncthreads();
-    while (ctl[1] < g.nseg) {
-      // 1. slot table of this chunk, built by warp 0: lane l looks at segment
-      //    cur+l, an inclusive warp scan of the slots each segment can still
-      //    provide places every segment's k range inside the 32 slots.
-      if (warp == 0) {
-        const int cur = ctl[1], curk = ctl[2];
-        const int sidx = cur + lane;
-        Seg sg;
-        int avail = 0;
-        if (sidx < g.nseg) {
-          sg = segs[g.seg0 + sidx];
-          avail = sg.K - (lane == 0 ? curk : 0);
-        }
-        int incl = avail;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int t = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += t;
-        }
-        const int excl = incl - avail;
-        if (avail > 0 && excl < T_TK) {
-          const double *A = bufs.p[sg.abuf] + sg.a_off;
-          const double *B = bufs.p[sg.bbuf] + sg.b_off;
-          const int k0 = lane == 0 ? curk : 0;
-          const int jend = min(incl, T_TK);
-          for (int j = excl; j < jend; ++j) {
-            const int kk = k0 + (j - excl);
-            slots[j].a = A + (int64_t)kk * sg.sak;
-            slots[j].b = B + (int64_t)kk * sg.sbk;
-            slots[j].sam = sg.sam;
-            slots[j].sbn = sg.sbn;
-            slots[j].alpha = sg.alpha;
-            slots[j].scaled = sg.alpha != 1.0;
-          }
-        }
-        // where the chunk ends: first lane whose inclusive sum reaches 32
-        const unsigned reach = __ballot_sync(0xffffffffu, incl >= T_TK && avail > 0);
-        const int total = __shfl_sync(0xffffffffu, incl, 31);
-        const int lstop = reach ? (__ffs(reach) - 1) : -1;
-        const int stop_incl = __shfl_sync(0xffffffffu, incl, lstop < 0 ? 31 : lstop);
-        const int stop_excl = __shfl_sync(0xffffffffu, excl, lstop < 0 ? 31 : lstop);
-        if (lane == 0) {
-          if (lstop < 0) {           // every remaining segment fits (or the 32 lanes ran out)
-            const int nseen = min(32, g.nseg - cur);
-            ctl[0] = min(total, T_TK);
-            ctl[1] = cur + nseen;
-            ctl[2] = 0;
-          } else {
-            ctl[0] = T_TK;
-            const int used = T_TK - stop_excl;             // slots taken from segment cur+lstop
-            const int base = lstop == 0 ? curk : 0;
-            if (stop_incl == T_TK) {
-              ctl[1] = cur + lstop + 1;
-              ctl[2] = 0;
-            } else {
-              ctl[1] = cur + lstop;
-              ctl[2] = base + used;
-            }
-          }
-        }
-      }
+    while (true) {
+      if (warp == 0) build_slots(g, segs, bufs, slots, ctl, ctl + 2, lane);
       __syncthreads();
-      const int nslot = ctl[0];
-      // 2. A: two threads per row (16 slots each, partner = lane ^ 1);
-      //    chunk max exponent of the row, then digit planes
-      {
-        constexpr int HK = T_TK / 2;
-        const int r = tid >> 1, half = tid & 1;
-        const int row = m0 + r;
-        double v[HK];
+      const int ns = ctl[2];
+      if (ns == 0) break;
+      {  // A: chunk max exponent of the row over its TPR threads, digit planes
+        double v[KPA];
         int emax = 0;
 #pragma unroll
-        for (int t = 0; t < HK; ++t) {
-          const int j = half * HK + t;
+        for (int t = 0; t < KPA; ++t) {
+          const int j = parta * KPA + t;
           double x = 0.0;
-          if (j < nslot && row < g.M) {
+          if (j < ns && rowa < g.M) {
             const Slot &sl = slots[j];
-            x = __ldg(sl.a + (int64_t)row * sl.sam);
+            x = __ldg(sl.a + (int64_t)rowa * sl.sam);
             if (sl.scaled) x *= sl.alpha;
           }
           v[t] = x;
           emax = max(emax, dexp(x));
         }
-        emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
-        if (half == 0) Ea[r] = emax;
 #pragma unroll
-        for (int t = 0; t < HK; ++t)
-          digits_bf16<S>(v[t], emax, Ap + r * T_PAD + half * HK + t, T_TM * T_PAD);
+        for (int o = 1; o < TPR; o <<= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        if (parta == 0) Ea[ra] = emax;
+        if constexpr (S == 4 && KPA % 2 == 0) {
+          uint32_t *ap = reinterpret_cast<uint32_t *>(Ap + ra * T_PAD + parta * KPA);
+#pragma unroll
+          for (int t = 0; t < KPA; t += 2) digits4_pair(v[t], v[t + 1], emax, ap + t / 2, TM * T_PAD / 2);
+        } else if constexpr (S == 4) {
+#pragma unroll
+          for (int t = 0; t < KPA; ++t) digits4_one(v[t], emax, Ap + ra * T_PAD + parta * KPA + t, TM * T_PAD);
+        } else {
+#pragma unroll
+          for (int t = 0; t < KPA; ++t) digits_bf16<S>(v[t], emax, Ap + ra * T_PAD + parta * KPA + t, TM * T_PAD);
+        }
       }
-      // 3. B: TN columns, 128/TN threads per column share the 32 slots
-      {
-        constexpr int TPC = T_NT / TN;  // threads per column
-        constexpr int KPT = T_TK / TPC; // slots per thread
-        const int c = tid / TPC, part = tid % TPC;
-        const int col = n0 + c;
-        double v[KPT];
+      {  // B: TPC threads per column share the 32 slots
+        double v[KPB];
         int emax = 0;
 #pragma unroll
-        for (int t = 0; t < KPT; ++t) {
-          const int j = part * KPT + t;
+        for (int t = 0; t < KPB; ++t) {
+          const int j = partb * KPB + t;
           double x = 0.0;
-          if (j < nslot && col < g.N) x = __ldg(slots[j].b + (int64_t)col * slots[j].sbn);
+          if (j < ns && colb < g.N) x = __ldg(slots[j].b + (int64_t)colb * slots[j].sbn);
           v[t] = x;
           emax = max(emax, dexp(x));
         }
 #pragma unroll
         for (int o = 1; o < TPC; o <<= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
-        if (part == 0) Eb[c] = emax;
+        if (partb == 0) Eb[cb] = emax;
+        if constexpr (S == 4 && KPB % 2 == 0) {
+          uint32_t *bp = reinterpret_cast<uint32_t *>(Bp + cb * T_PAD + partb * KPB);
 #pragma unroll
-        for (int t = 0; t < KPT; ++t)
-          digits_bf16<S>(v[t], emax, Bp + c * T_PAD + part * KPT + t, TN * T_PAD);
+          for (int t = 0; t < KPB; t += 2) digits4_pair(v[t], v[t + 1], emax, bp + t / 2, TN * T_PAD / 2);
+        } else if constexpr (S == 4) {
+#pragma unroll
+          for (int t = 0; t < KPB; ++t) digits4_one(v[t], emax, Bp + cb * T_PAD + partb * KPB + t, TN * T_PAD);
+        } else {
+#pragma unroll
+          for (int t = 0; t < KPB; ++t) digits_bf16<S>(v[t], emax, Bp + cb * T_PAD + partb * KPB + t, TN * T_PAD);
+        }
       }
       __syncthreads();
-      // 4. digit products per level, exact in FP32
-      float acc[S][MT][NTL][4];
+      // digit products per level, exact in FP32
+      float acc[S][4];
 #pragma unroll
       for (int l = 0; l < S; ++l)
 #pragma unroll
-        for (int mt = 0; mt < MT; ++mt)
-#pragma unroll
-          for (int nt = 0; nt < NTL; ++nt)
-#pragma unroll
-            for (int i = 0; i < 4; ++i) acc[l][mt][nt][i] = 0.f;
+        for (int i = 0; i < 4; ++i) acc[l][i] = 0.f;
 #pragma unroll
       for (int kk = 0; kk < T_TK; kk += 16) {
-        uint32_t bf[S][NTL][2];
+        uint32_t bf[S][2];
 #pragma unroll
-        for (int sb = 0; sb < S; ++sb)
-#pragma unroll
-          for (int nt = 0; nt < NTL; ++nt) {
-            const __nv_bfloat16 *bp = Bp + (sb * TN + nt * 8 + gq) * T_PAD + kk;
-            bf[sb][nt][0] = *reinterpret_cast<const uint32_t *>(bp + 2 * tq);
-            bf[sb][nt][1] = *reinterpret_cast<const uint32_t *>(bp + 2 * tq + 8);
-          }
+        for (int sb = 0; sb < S; ++sb) {
+          const __nv_bfloat16 *bp = Bp + (sb * TN + wn + gq) * T_PAD + kk;
+          bf[sb][0] = *reinterpret_cast<const uint32_t *>(bp + 2 * tq);
+          bf[sb][1] = *reinterpret_cast<const uint32_t *>(bp + 2 * tq + 8);
+        }
 #pragma unroll
         for (int sa = 0; sa < S; ++sa) {
+          uint32_t af[4];
+          const __nv_bfloat16 *ap = Ap + (sa * TM + wm) * T_PAD + kk;
+          af[0] = *reinterpret_cast<const uint32_t *>(ap + gq * T_PAD + 2 * tq);
+          af[1] = *reinterpret_cast<const uint32_t *>(ap + (gq + 8) * T_PAD + 2 * tq);
+          af[2] = *reinterpret_cast<const uint32_t *>(ap + gq * T_PAD + 2 * tq + 8);
+          af[3] = *reinterpret_cast<const uint32_t *>(ap + (gq + 8) * T_PAD + 2 * tq + 8);
 #pragma unroll
-          for (int mt = 0; mt < MT; ++mt) {
-            uint32_t af[4];
-            const __nv_bfloat16 *ap = Ap + (sa * T_TM + wm + mt * 16) * T_PAD + kk;
-            af[0] = *reinterpret_cast<const uint32_t *>(ap + gq * T_PAD + 2 * tq);
-            af[1] = *reinterpret_cast<const uint32_t *>(ap + (gq + 8) * T_PAD + 2 * tq);
-            af[2] = *reinterpret_cast<const uint32_t *>(ap + gq * T_PAD + 2 * tq + 8);
-            af[3] = *reinterpret_cast<const uint32_t *>(ap + (gq + 8) * T_PAD + 2 * tq + 8);
-#pragma unroll
-            for (int sb = 0; sb + sa < S; ++sb)
-#pragma unroll
-              for (int nt = 0; nt < NTL; ++nt) mma_bf16(acc[sa + sb][mt][nt], af, bf[sb][nt]);
-          }
+          for (int sb = 0; sb + sa < S; ++sb) mma_bf16(acc[sa + sb], af, bf[sb]);
         }
       }
-      // 5. scale levels by 2^(Ea + Eb - 2044 - 8(l+2)) into the two-float sums
+      // scale the levels by 2^(Ea + Eb - 2044 - 8(l+2)) into the two-float sums
 #pragma unroll
-      for (int mt = 0; mt < MT; ++mt)
+      for (int i = 0; i < 4; ++i) {
+        const int r = wm + gq + (i >> 1) * 8;
+        const int c = wn + 2 * tq + (i & 1);
+        const int ea = Ea[r], eb = Eb[c];
+        if (ea == 0 || eb == 0) continue;
+        const int base = ea + eb - 2044;
+        if constexpr (S == 4) {
+          // levels are exact integers below 2^24: level 0 + level 1 / 2^8 as
+          // an exact pair, levels 2 and 3 into its low part, one scale
+          float h, e;
+          two_sum(acc[0][i], acc[1][i] * 0x1p-8f, h, e);
+          e = fmaf(acc[2][i], 0x1p-16f, e);
+          e = fmaf(acc[3][i], 0x1p-24f, e);
+          const float sc = pow2f(base - 16);
+          float s2, e2;
+          two_sum(hi[i], h * sc, s2, e2);
+          hi[i] = s2;
+          lo[i] += e2 + e * sc;
+        } else {
 #pragma unroll
-        for (int nt = 0; nt < NTL; ++nt)
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            const int r = wm + mt * 16 + gq + (i >> 1) * 8;
-            const int c = nt * 8 + 2 * tq + (i & 1);
-            const int ea = Ea[r], eb = Eb[c];
-            if (ea == 0 || eb == 0) continue;
-            const int base = ea + eb - 2044;
-#pragma unroll
-            for (int l = 0; l < S; ++l)
-              two_sum_acc(hi[mt][nt][i], lo[mt][nt][i], scale_pow2(acc[l][mt][nt][i], base - 8 * (l + 2)));
-          }
+          for (int l = 0; l < S; ++l) two_sum_acc(hi[i], lo[i], scale_pow2(acc[l][i], base - 8 * (l + 2)));
+        }
+      }
       __syncthreads();
     }
     double *C = bufs.p[g.cbuf] + g.c_off;
 #pragma unroll
-    for (int mt = 0; mt < MT; ++mt)
-#pragma unroll
-      for (int nt = 0; nt < NTL; ++nt)
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const int r = m0 + wm + mt * 16 + gq + (i >> 1) * 8;
-          const int c = n0 + nt * 8 + 2 * tq + (i & 1);
-          if (r < g.M && c < g.N)
-            C[(int64_t)r * g.scm + (int64_t)c * g.scn] = (double)hi[mt][nt][i] + (double)lo[mt][nt][i];
-        }
-    __syncthreads();
+    for (int i = 0; i < 4; ++i) {
+      const int r = m0 + wm + gq + (i >> 1) * 8;
+      const int c = n0 + wn + 2 * tq + (i & 1);
+      if (r < g.M && c < g.N) C[(int64_t)r * g.scm + (int64_t)c * g.scn] = (double)hi[i] + (double)lo[i];
+    }
   }
 }
 
@@ -417,7 +496,8 @@ static int launch_tc_t(const Work *work, int64_t nwork, const Step &s, const Buf
     cudaFuncSetAttribute(k_step_tc<S, TM, TN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = true;
   }
-  k_step_tc<S, TM, TN><<<grid_for(nwork, 3 * 256 / TM), 2 * TM, smem, (cudaStream_t)stream>>>(
+  constexpr int NT = TcShape<S, TM, TN>::NT;
+  k_step_tc<S, TM, TN><<<grid_for(nwork, TcShape<S, TM, TN>::THREADS_SM / NT), NT, smem, (cudaStream_t)stream>>>(
       work, nwork, s.d_groups, s.d_segs, b);
   return launch_error("k_step_tc");
 }

@@ -1212,6 +1212,26 @@ int zmpo_plan_stats(zmpo_engine *e, int plan_id, double *flops, int64_t *ntasks,
   return ZMPO_OK;
 }
 
+int zmpo_plan_kernel_count(zmpo_engine *e, int plan_id, int precision, int *count) {
+  Plan *P = get_plan(e, plan_id, 0);
+  if (!P) return fail(ZMPO_E_ID, "plan_kernel_count: unknown plan");
+  if (!count) return fail(ZMPO_E_ARG, "plan_kernel_count: null output");
+  int n = 0;
+  for (auto &s : P->steps) {
+    int rc = upload_step(s);
+    if (rc) return rc;
+    if (precision == ZMPO_PREC_FP64) {
+      n += s.nwork_fp64 > 0;
+    } else {
+      for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 2; ++c) n += s.nwork_tc[a][c] > 0;
+    }
+    n += s.red_elems > 0;
+  }
+  *count = n;
+  return ZMPO_OK;
+}
+
 int zmpo_sigma(zmpo_engine *e, int plan_id, const double *d_L, const double *d_R,
                const double *d_W, const double *d_x, double *d_y, void *d_workspace,
                int precision, void *stream) {

@@ -113,6 +113,13 @@ class Engine:
                                          ctypes.byref(nl)), "plan_stats")
         return fl.value, nt.value, nl.value
 
+    def kernel_count(self, pid, precision="split"):
+        """Kernel launches one execution of the plan issues at ``precision``."""
+        n = ctypes.c_int()
+        check(_lib.lib().zmpo_plan_kernel_count(self.h, pid, _lib.PREC[precision], ctypes.byref(n)),
+              "plan_kernel_count")
+        return n.value
+
     def profile(self, on=True):
         check(_lib.lib().zmpo_profile(self.h, 1 if on else 0), "profile")
 

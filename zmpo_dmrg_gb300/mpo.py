@@ -25,46 +25,79 @@ _A = numpy.array([[0.0, 1.0], [0.0, 0.0]])   # annihilation
 _N = numpy.array([[0.0, 0.0], [0.0, 1.0]])   # number
 
 
+class _Backend:
+    """Array operations for the builder: NumPy (the site tensors the engine
+    uploads) or torch (the same tensors as a differentiable function of the
+    integrals, for the energy gradient)."""
+
+    def __init__(self, like):
+        self.torch = not isinstance(like, numpy.ndarray)
+        if self.torch:
+            import torch
+            self.t = torch
+            kw = dict(dtype=like.dtype, device=like.device)
+            self.kw = kw
+            self.I, self.Z, self.C, self.A, self.N = (torch.as_tensor(x, **kw) for x in (_I, _Z, _C, _A, _N))
+        else:
+            self.I, self.Z, self.C, self.A, self.N = _I, _Z, _C, _A, _N
+
+    def zeros(self, shape):
+        return self.t.zeros(shape, **self.kw) if self.torch else numpy.zeros(shape)
+
+    def arange(self, a, b=None):
+        if b is None:
+            a, b = 0, a
+        if self.torch:
+            return self.t.arange(a, b, device=self.kw["device"])
+        return numpy.arange(a, b)
+
+    def matmul(self, a, b):
+        return self.t.matmul(a, b) if self.torch else numpy.matmul(a, b)
+
+
 def spin_site(nsite, k, h, v):
-    """V_p MPO on spin orbital ``k``: ``h[q]`` = h_pq, ``v[q,r,s]`` = V_pqrs."""
+    """V_p MPO on spin orbital ``k``: ``h[q]`` = h_pq, ``v[q,r,s]`` = V_pqrs
+    (NumPy arrays, or float64 torch tensors for a differentiable build)."""
+    B = _Backend(h)
     nl = 1 if k == 0 else 2 * (nsite + 1)
     nr = 1 if k == nsite - 1 else 2 * (nsite + 1)
-    W = numpy.zeros((nl, nr, 2, 2))
+    W = B.zeros((nl, nr, 2, 2))
     L = k                 # spin orbitals left of k
     R = nsite - k - 1     # spin orbitals right of k
-    right = numpy.arange(k + 1, nsite)
-    left = numpy.arange(k)
+    right = B.arange(k + 1, nsite)
+    left = B.arange(k)
+    rr = B.arange(R)
     last = nr - 1
     if k == nsite - 1:
-        W[0, 0] = h[k] * _A
-        W[1, 0] = _C
-        W[2, 0] = _A
-        W[3 + left, 0] = v[k, left, k][:, None, None] * _N
-        W[nl - 1, 0] = _I
+        W[0, 0] = h[k] * B.A
+        W[1, 0] = B.C
+        W[2, 0] = B.A
+        W[3 + left, 0] = v[k, left, k][:, None, None] * B.N
+        W[nl - 1, 0] = B.I
         return W
     # first row: string, V(k,k,r) n_k, -a_k, a+_k, h_k a_k
-    W[0, 0] = _Z
-    W[0, 1 + R + numpy.arange(R)] = v[k, k, right][:, None, None] * (-_N)
-    W[0, 1 + 2 * R + L] = -_A
-    W[0, 2 + 2 * R + 2 * L] = _C
-    W[0, last] = h[k] * _A
+    W[0, 0] = B.Z
+    W[0, 1 + R + rr] = v[k, k, right][:, None, None] * (-B.N)
+    W[0, 1 + 2 * R + L] = -B.A
+    W[0, 2 + 2 * R + 2 * L] = B.C
+    W[0, last] = h[k] * B.A
     if k == 0:
         return W
-    W[1, last] = _C
-    W[2 + numpy.arange(R), 1 + numpy.arange(R)] = _Z
-    W[2 + R, last] = _A
-    W[3 + R + numpy.arange(R), 1 + R + numpy.arange(R)] = _Z
+    W[1, last] = B.C
+    W[2 + rr, 1 + rr] = B.Z
+    W[2 + R, last] = B.A
+    W[3 + R + rr, 1 + R + rr] = B.Z
     o6 = 3 + 2 * R
     for li in range(L):
-        W[o6 + li, 1 + numpy.arange(R)] = -v[right, li, k][:, None, None] * (-_A)
-        W[o6 + li, 1 + R + numpy.arange(R)] = v[k, li, right][:, None, None] * _C
-        W[o6 + li, 1 + 2 * R + li] = _I
-        W[o6 + li, last] = v[k, li, k] * _N
+        W[o6 + li, 1 + rr] = -v[right, li, k][:, None, None] * (-B.A)
+        W[o6 + li, 1 + R + rr] = v[k, li, right][:, None, None] * B.C
+        W[o6 + li, 1 + 2 * R + li] = B.I
+        W[o6 + li, last] = v[k, li, k] * B.N
     o7 = 3 + 2 * R + L
     for li in range(L):
-        W[o7 + li, 1 + R + numpy.arange(R)] = v[li, k, right][:, None, None] * (-_A)
-        W[o7 + li, 2 + 2 * R + L + li] = _I
-    W[nl - 1, last] = _I
+        W[o7 + li, 1 + R + rr] = v[li, k, right][:, None, None] * (-B.A)
+        W[o7 + li, 2 + 2 * R + L + li] = B.I
+    W[nl - 1, last] = B.I
     return W
 
 
@@ -77,11 +110,20 @@ def _elem(p, k):
 def hp_spin_site(p, nsite, k, h, v):
     """a_p^+ V_p on spin orbital k: the local a_p^+ factor acts after V_p."""
     W = spin_site(nsite, k, h, v)
-    return numpy.matmul(_elem(p, k), W)
+    B = _Backend(h)
+    e = _elem(p, k)
+    if B.torch:
+        e = B.t.as_tensor(e, **B.kw)
+    return B.matmul(e, W)
 
 
 def link(W1, W2):
     """Join two sites: [a,b,i,j] x [b,c,k,l] -> [a,c,(ik),(jl)] (one GEMM over b)."""
+    if not isinstance(W1, numpy.ndarray):
+        import torch
+        t = torch.tensordot(W1, W2, dims=([1], [0])).permute(0, 3, 1, 4, 2, 5)
+        s = t.shape
+        return t.reshape(s[0], s[1], s[2] * s[3], s[4] * s[5])
     t = numpy.tensordot(W1, W2, axes=([1], [0]))        # a,i,j,c,k,l
     t = t.transpose(0, 3, 1, 4, 2, 5)
     s = t.shape
@@ -141,15 +183,28 @@ def spatial_bond_qnums(p, nspin, isite):
     return ql + el, qr + er
 
 
+def _bond_labels(pindx, nspin, isite):
+    ql, qr = spatial_bond_qnums(pindx[0], nspin, isite)
+    if pindx[1] is not None:
+        ql, qr = ql[:, :1], qr[:, :1]
+    return ql, qr
+
+
+def bond_order(pindx, nspin, isite):
+    """Permutations (left, right) from the builder's bond order to the
+    block-sparse tensor's order (ascending label, stable)."""
+    ql, qr = _bond_labels(pindx, nspin, isite)
+    return numpy.lexsort(ql.T[::-1]), numpy.lexsort(qr.T[::-1])
+
+
 def hp_spatial_qt(pindx, nspin, isite, int1e, int2e, qpts=None, pdic=None):
     """Block-sparse site tensor of H_p with bond sectors collected."""
     W = hp_spatial_site(pindx, nspin, isite, int1e, int2e, qpts, pdic)
-    ql, qr = spatial_bond_qnums(pindx[0], nspin, isite)
+    ql, qr = _bond_labels(pindx, nspin, isite)
     qphys = numpy.array([[0.0, 0.0], [1.0, -0.5], [1.0, 0.5], [2.0, 0.0]])
     if pindx[1] is not None:
-        ql, qr, qphys = ql[:, :1], qr[:, :1], qphys[:, :1]
-    il = numpy.lexsort(ql.T[::-1])
-    ir = numpy.lexsort(qr.T[::-1])
+        qphys = qphys[:, :1]
+    il, ir = bond_order(pindx, nspin, isite)
     W = W[numpy.ix_(il, ir)]
     qt = qtensor([False, True, False, True])
     qt.fromDenseTensor(W, [ql[il], qr[ir], qphys, qphys], ifcollect=[1, 1, 0, 0])
