@@ -116,7 +116,6 @@ int launch_step_fp64(const Step &s, const Bufs &b, void *stream) {
 // BF16 tensor cores (exact in FP32: level sums < 2^24), level sums scaled and
 // added to a two-float accumulator.  Integer->float conversions stay 32-bit:
 // 64-bit conversions issue on the FP64 pipe, which is narrow on GB300.
-constexpr int T_TK = 32, T_PAD = 40;
 
 // biased exponent of a double (0 for zero / denormal)
 __device__ __forceinline__ int dexp(double x) {
@@ -246,6 +245,7 @@ struct Slot {
 // cur+l; an inclusive warp scan of the slots each segment can still provide
 // places every segment's k range inside the 32 slots.  cursor[0] = next
 // segment, cursor[1] = k offset inside it; *nslot = slots filled (0 = done).
+template <int TK>
 __device__ __forceinline__ void build_slots(const Group &g, const Seg *__restrict__ segs,
                                             const Bufs &bufs, Slot *slots, int *cursor,
                                             int *nslot, int lane) {
@@ -268,11 +268,11 @@ __device__ __forceinline__ void build_slots(const Group &g, const Seg *__restric
     if (lane >= o) incl += t;
   }
   const int excl = incl - avail;
-  if (avail > 0 && excl < T_TK) {
+  if (avail > 0 && excl < TK) {
     const double *A = bufs.p[sg.abuf] + sg.a_off;
     const double *B = bufs.p[sg.bbuf] + sg.b_off;
     const int k0 = lane == 0 ? curk : 0;
-    const int jend = min(incl, T_TK);
+    const int jend = min(incl, TK);
     for (int j = excl; j < jend; ++j) {
       const int kk = k0 + (j - excl);
       slots[j].a = A + (int64_t)kk * sg.sak;
@@ -284,7 +284,7 @@ __device__ __forceinline__ void build_slots(const Group &g, const Seg *__restric
     }
   }
   // where the chunk ends: first lane whose inclusive sum reaches 32
-  const unsigned reach = __ballot_sync(0xffffffffu, incl >= T_TK && avail > 0);
+  const unsigned reach = __ballot_sync(0xffffffffu, incl >= TK && avail > 0);
   const int total = __shfl_sync(0xffffffffu, incl, 31);
   const int lstop = reach ? (__ffs(reach) - 1) : -1;
   const int stop_incl = __shfl_sync(0xffffffffu, incl, lstop < 0 ? 31 : lstop);
@@ -292,14 +292,14 @@ __device__ __forceinline__ void build_slots(const Group &g, const Seg *__restric
   if (lane == 0) {
     if (lstop < 0) {  // every remaining segment fits (or the 32 lanes ran out)
       const int nseen = min(32, g.nseg - cur);
-      *nslot = min(total, T_TK);
+      *nslot = min(total, TK);
       cursor[0] = cur + nseen;
       cursor[1] = 0;
     } else {
-      *nslot = T_TK;
-      const int used = T_TK - stop_excl;  // slots taken from segment cur+lstop
+      *nslot = TK;
+      const int used = TK - stop_excl;  // slots taken from segment cur+lstop
       const int base = lstop == 0 ? curk : 0;
-      if (stop_incl == T_TK) {
+      if (stop_incl == TK) {
         cursor[0] = cur + lstop + 1;
         cursor[1] = 0;
       } else {
@@ -317,15 +317,21 @@ __device__ __forceinline__ void build_slots(const Group &g, const Seg *__restric
 // to digit planes, digit products, scaled sums; three barriers.
 template <int S, int TM, int TN>
 struct TcShape {
+  // k slots per chunk.  A level sums at most S products of at most 255^2 per
+  // k, so S = 4 stays exact in FP32 (< 2^24) up to 64 slots and S = 7 up to
+  // 32; 64-slot chunks were measured slower (more registers per thread), so
+  // both use 32.
+  static constexpr int TK = 32;
+  static constexpr int PAD = TK + 8;          // bf16 per plane row in shared memory
   static constexpr int WM = TM / 16, WN = TN / 8;
   static constexpr int NT = 32 * WM * WN;     // threads per CTA
   static constexpr int TPR = NT / TM;         // threads per row of A
-  static constexpr int KPA = T_TK / TPR;      // A slots per thread
+  static constexpr int KPA = TK / TPR;        // A slots per thread
   static constexpr int TPC = NT / TN;         // threads per column of B
-  static constexpr int KPB = T_TK / TPC;      // B slots per thread
+  static constexpr int KPB = TK / TPC;        // B slots per thread
   // resident threads per SM the register budget is sized for (16 A slots
   // per thread need more registers than 8)
-  static constexpr int THREADS_SM = KPA > 8 ? 768 : 1024;
+  static constexpr int THREADS_SM = (KPA > 8 && NT < 512) ? 768 : 1024;
   static_assert(TPR >= 1 && KPA >= 1 && TPC >= 1 && KPB >= 1, "tile shape");
 };
 
@@ -335,13 +341,14 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
           const Seg *__restrict__ segs, Bufs bufs) {
   using Sh = TcShape<S, TM, TN>;
   constexpr int TPR = Sh::TPR, KPA = Sh::KPA, TPC = Sh::TPC, KPB = Sh::KPB;
+  constexpr int TK = Sh::TK, T_PAD = Sh::PAD;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __nv_bfloat16 *Ap = reinterpret_cast<__nv_bfloat16 *>(smem_raw);  // [S][TM][PAD]
   __nv_bfloat16 *Bp = Ap + S * TM * T_PAD;                          // [S][TN][PAD]
   int *Ea = reinterpret_cast<int *>(Bp + S * TN * T_PAD);           // [TM]
   int *Eb = Ea + TM;                                                // [TN]
-  Slot *slots = reinterpret_cast<Slot *>(Eb + 16);                  // [TK]
-  int *ctl = reinterpret_cast<int *>(slots + T_TK);                 // cursor[2], nslot
+  Slot *slots = reinterpret_cast<Slot *>(Eb + (TN < 16 ? 16 : TN));  // [TK] (Eb holds TN ints)
+  int *ctl = reinterpret_cast<int *>(slots + TK);                 // cursor[2], nslot
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wm = (warp % Sh::WM) * 16, wn = (warp / Sh::WM) * 8;  // this warp's m16n8 piece
@@ -361,7 +368,7 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
     }
     __syncthreads();
     while (true) {
-      if (warp == 0) build_slots(g, segs, bufs, slots, ctl, ctl + 2, lane);
+      if (warp == 0) build_slots<TK>(g, segs, bufs, slots, ctl, ctl + 2, lane);
       __syncthreads();
       const int ns = ctl[2];
       if (ns == 0) break;
@@ -429,7 +436,7 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
 #pragma unroll
         for (int i = 0; i < 4; ++i) acc[l][i] = 0.f;
 #pragma unroll
-      for (int kk = 0; kk < T_TK; kk += 16) {
+      for (int kk = 0; kk < TK; kk += 16) {
         uint32_t bf[S][2];
 #pragma unroll
         for (int sb = 0; sb < S; ++sb) {
@@ -489,8 +496,10 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
 template <int S, int TM, int TN>
 static int launch_tc_t(const Work *work, int64_t nwork, const Step &s, const Bufs &b, void *stream) {
   if (nwork == 0) return ZMPO_OK;
-  const size_t smem = (size_t)S * (TM + TN) * T_PAD * sizeof(__nv_bfloat16) +
-                      (size_t)(TM + 16) * sizeof(int) + T_TK * sizeof(Slot) + 4 * sizeof(int) + 16;
+  using Sh = TcShape<S, TM, TN>;
+  const size_t smem = (size_t)S * (TM + TN) * Sh::PAD * sizeof(__nv_bfloat16) +
+                      (size_t)(TM + (TN < 16 ? 16 : TN)) * sizeof(int) + Sh::TK * sizeof(Slot) +
+                      4 * sizeof(int) + 16;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_step_tc<S, TM, TN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -510,7 +519,10 @@ static int launch_split_all(const Step &s, const Bufs &b, void *stream) {
   if ((rc = launch_tc_t<S, 64, 8>(s.d_work_tc[1][0], s.nwork_tc[1][0], s, b, stream))) return rc;
   if ((rc = launch_tc_t<S, 64, 16>(s.d_work_tc[1][1], s.nwork_tc[1][1], s, b, stream))) return rc;
   if ((rc = launch_tc_t<S, 32, 8>(s.d_work_tc[0][0], s.nwork_tc[0][0], s, b, stream))) return rc;
-  return launch_tc_t<S, 32, 16>(s.d_work_tc[0][1], s.nwork_tc[0][1], s, b, stream);
+  if ((rc = launch_tc_t<S, 32, 16>(s.d_work_tc[0][1], s.nwork_tc[0][1], s, b, stream))) return rc;
+  if ((rc = launch_tc_t<S, 128, 32>(s.d_work_tc[2][2], s.nwork_tc[2][2], s, b, stream))) return rc;
+  if ((rc = launch_tc_t<S, 64, 32>(s.d_work_tc[1][2], s.nwork_tc[1][2], s, b, stream))) return rc;
+  return launch_tc_t<S, 32, 32>(s.d_work_tc[0][2], s.nwork_tc[0][2], s, b, stream);
 }
 
 int launch_step_split(const Step &s, const Bufs &b, int nslices, void *stream) {
