@@ -138,6 +138,14 @@ int zmpo_sigma_workspace(zmpo_engine *e, int plan_id, int64_t *bytes);
  * task lists), and the number of tasks / launches. */
 int zmpo_plan_stats(zmpo_engine *e, int plan_id, double *flops,
                     int64_t *ntasks, int *nlaunch);
+/* Host copy of one step's task records before the plan's first execution
+ * (afterwards they live on the device): counts[4] = groups, segments, column
+ * blocks, per-(segment, column block) B parts; each output pointer may be NULL
+ * and receives the records in the engine's internal layout (csrc/engine.h:
+ * Group 56 bytes, Seg 64, ColBlock 32, SegB 24).  For inspection and tests;
+ * no reference counterpart. */
+int zmpo_plan_step_tasks(zmpo_engine *e, int plan_id, int step, int64_t *counts,
+                         void *groups, void *segs, void *cblocks, void *segb);
 /* Number of kernel launches one execution of the plan issues at this
  * precision (grouped GEMM launches per tile shape plus split-K sums).  No
  * reference counterpart: it reports what the engine will launch. */

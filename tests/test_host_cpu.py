@@ -263,3 +263,91 @@ def test_n_only_relabel_matches_oracle():
     osp.s2quad(b, 1.5, 0.5)
     assert numpy.abs(a.qpts - b.qpts).max() < 1e-14
     assert numpy.abs(a.qwts - b.qwts).max() < 1e-13
+
+
+def _run_tasks_on_host(eng, pid, nsteps, bufs):
+    """Execute a plan's task records with NumPy (test-only model of the
+    kernels' semantics, incl. column-block groups); returns the buffers."""
+    for st in range(nsteps):
+        groups, segs, cbl, segb = eng.step_tasks(pid, st)
+        for g in groups:
+            M, N = int(g["M"]), int(g["N"])
+            acc = numpy.zeros((M, N))
+            mi = numpy.arange(M)
+            for si in range(int(g["nseg"])):
+                s = segs[g["seg0"] + si]
+                K = int(s["K"])
+                ki = numpy.arange(K)
+                A = bufs[int(s["abuf"])][s["a_off"] + mi[:, None] * s["sam"] + ki[None, :] * s["sak"]]
+                if g["ncb"] == 0:
+                    ni = numpy.arange(N)
+                    B = bufs[int(s["bbuf"])][s["b_off"] + ki[:, None] * s["sbk"] + ni[None, :] * s["sbn"]]
+                else:
+                    B = numpy.zeros((K, N))
+                    for j in range(int(g["ncb"])):
+                        cb = cbl[g["cb0"] + j]
+                        sb = segb[g["sb0"] + si * g["ncb"] + j]
+                        if sb["b_off"] < 0:
+                            continue
+                        ni = numpy.arange(int(cb["n"]))
+                        B[:, cb["n0"]:cb["n0"] + cb["n"]] = bufs[int(s["bbuf"])][
+                            sb["b_off"] + ki[:, None] * sb["sbk"] + ni[None, :] * sb["sbn"]]
+                acc += s["alpha"] * (A @ B)
+            out = bufs[int(g["cbuf"])]
+            if g["ncb"] == 0:
+                ni = numpy.arange(N)
+                out[g["c_off"] + mi[:, None] * g["scm"] + ni[None, :] * g["scn"]] = acc
+            else:
+                for j in range(int(g["ncb"])):
+                    cb = cbl[g["cb0"] + j]
+                    ni = numpy.arange(int(cb["n"]))
+                    out[cb["c_off"] + mi[:, None] * cb["scm"] + ni[None, :] * cb["scn"]] = \
+                        acc[:, cb["n0"]:cb["n0"] + cb["n"]]
+    return bufs
+
+
+def test_sigma_task_lists_compute_the_oracle_sigma():
+    """The engine's sigma plan (O = Wi.Wj, T1 = L.psi, T3 = T1.O, sigma = T3.R
+    with column-block groups) executed from its task records by a NumPy model
+    of the kernels equals the oracle's HVecQt (FP64, 1e-12): checks the
+    planner's addressing on the CPU, before any kernel runs."""
+    from tests.problems import random_problem, oracle_sigma
+    P = random_problem(K=6, nelec=6, D=16, isite=2, seed=1, device=False)
+    m = P.o
+    eng = E.get()
+    fL, fR = m.flst[0]
+
+    def lay(t):
+        return eng.layout(t.qsyms, t.ndims, t.status)
+
+    nops = m.nops
+    Lv, Rv, Wv = [], [], []
+    offL, offR, offWi, offWj = [], [], [], []
+    classes, op_cls, lL, lWi, lWj, lRf = {}, [], [], [], [], []
+    pos = {"L": 0, "R": 0, "W": 0}
+    for iop in range(nops):
+        Lt, Rt = fL['opers%d' % iop], fR['opers%d' % iop]
+        Wi = m.fhop['site%d/op%d' % (P.isite, iop)]
+        Wj = m.fhop['site%d/op%d' % (P.isite + 1, iop)]
+        offL.append(pos["L"]); Lv.append(Lt.value); pos["L"] += Lt.value.size
+        offR.append(pos["R"]); Rv.append(Rt.value); pos["R"] += Rt.value.size
+        offWi.append(pos["W"]); Wv.append(Wi.value); pos["W"] += Wi.value.size
+        offWj.append(pos["W"]); Wv.append(Wj.value); pos["W"] += Wj.value.size
+        c0 = pm.op_class(m.opers[iop][0], P.isite, 2)
+        if c0 not in classes:
+            classes[c0] = len(classes)
+            lL.append(lay(Lt)); lWi.append(lay(Wi)); lWj.append(lay(Wj))
+            lRf.append(eng.derive(lay(Rt), [-Rt.qsyms[0], m.qkey - Rt.qsyms[1], m.qkey - Rt.qsyms[2]], Rt.status))
+        op_cls.append(classes[c0])
+    pid, ws = eng.sigma_plan(2, op_cls, lL, lWi, lWj, lRf, lay(m.qtmp), offL, offR, offWi, offWj,
+                             m.hpwts)
+    x = numpy.random.default_rng(3).standard_normal(P.ndim0)
+    bufs = [numpy.concatenate(Lv), numpy.concatenate(Rv), numpy.concatenate(Wv), x,
+            numpy.zeros(P.ndim0), numpy.zeros(max(ws // 8, 1)), numpy.zeros(1), numpy.zeros(1)]
+    _, _, nl = eng.plan_stats(pid)
+    groups_all = [eng.step_tasks(pid, st)[0] for st in range(nl)]
+    assert any((g["ncb"] > 0).any() for g in groups_all)      # column-block groups are in use
+    y = _run_tasks_on_host(eng, pid, nl, bufs)[4]
+    ref = oracle_sigma(P, x)
+    assert numpy.linalg.norm(y - ref) <= 1e-12 * numpy.linalg.norm(ref)
+    eng.destroy_plan(pid)

@@ -26,7 +26,25 @@ struct Group {
   int64_t scm, scn;
   int32_t M, N;
   int32_t seg0, nseg;
-  int32_t cbuf, pad;
+  int32_t cbuf;
+  // ncb = 0: one output block (c_off, scm, scn; B part in each Seg).
+  // ncb > 0: "column-block group": the output blocks that share the same A
+  // rows are side by side in N (ColBlock cb0 .. cb0+ncb-1), the segments are
+  // the union of their A parts, and SegB[sb0 + s * ncb + j] is the B part of
+  // segment s for column block j (b_off < 0: that pair does not exist, zero).
+  // A is then cut into digit planes once per column tile of the whole row
+  // instead of once per output block.
+  int32_t ncb;
+  int32_t cb0, sb0;
+};
+
+struct ColBlock {
+  int64_t c_off, scm, scn;  // output block (buffer Group::cbuf)
+  int32_t n0, n;            // its columns inside the group
+};
+
+struct SegB {
+  int64_t b_off, sbk, sbn;
 };
 
 // Split-K: a long group is cut into parts written to plan-owned scratch and
@@ -56,8 +74,12 @@ struct Bufs {
 struct Step {
   std::vector<Seg> segs;
   std::vector<Group> groups;
+  std::vector<ColBlock> cblocks;
+  std::vector<SegB> segb;
   Seg *d_segs = nullptr;
   Group *d_groups = nullptr;
+  ColBlock *d_cblocks = nullptr;
+  SegB *d_segb = nullptr;
   Work *d_work_fp64 = nullptr;   // tiles of kTileFP64
   // tensor-core tiles: [rows 32 / 64 / 128][columns 8 / 16]
   Work *d_work_tc[3][3] = {};  // [row tile 32/64/128][column tile 8/16/32]

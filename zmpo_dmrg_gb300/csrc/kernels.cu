@@ -40,19 +40,65 @@ static int grid_for(int64_t nwork, int per_sm) {
   return (int)(g < 1 ? 1 : g);
 }
 
+// column block of column col of a column-block group, and col relative to it
+// (binary search: the blocks of a group are in ascending n0)
+__device__ __forceinline__ int find_cblock(const ColBlock *__restrict__ cbl, const Group &g, int col,
+                                           int &colrel) {
+  colrel = 0;
+  if (g.ncb <= 0 || col < 0 || col >= g.N) return -1;
+  int lo = 0, hi = g.ncb - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (cbl[g.cb0 + mid].n0 <= col) lo = mid; else hi = mid - 1;
+  }
+  const ColBlock c = cbl[g.cb0 + lo];
+  if (col < c.n0 || col >= c.n0 + c.n) return -1;
+  colrel = col - c.n0;
+  return lo;
+}
+
+// column-block map of the tile's columns n0 .. n0+tn-1 into shared memory
+// (one binary search per column instead of one per access); needs a barrier
+// before use
+__device__ __forceinline__ void tile_cblocks(const ColBlock *__restrict__ cbl, const Group &g, int n0, int tn,
+                                             int *cbj, int *cbrel) {
+  for (int c = threadIdx.x; c < tn; c += blockDim.x) {
+    int rel;
+    cbj[c] = find_cblock(cbl, g, n0 + c, rel);
+    cbrel[c] = rel;
+  }
+}
+
+// C(r, c) of a group; column-block groups use the tile's map (c - n0 indexes it)
+__device__ __forceinline__ void store_c(const Bufs &bufs, const ColBlock *__restrict__ cbl, const Group &g,
+                                        int r, int c, int n0, const int *cbj, const int *cbrel, double v) {
+  if (g.ncb == 0) {
+    bufs.p[g.cbuf][g.c_off + (int64_t)r * g.scm + (int64_t)c * g.scn] = v;
+    return;
+  }
+  const int j = cbj[c - n0];
+  if (j < 0) return;
+  const ColBlock cb = cbl[g.cb0 + j];
+  bufs.p[g.cbuf][cb.c_off + (int64_t)r * cb.scm + (int64_t)cbrel[c - n0] * cb.scn] = v;
+}
+
 // ------------------------------------------------------------------ FP64
 constexpr int F_TM = 32, F_TN = 32, F_TK = 16, F_NT = 256;
 
 __global__ void __launch_bounds__(F_NT)
 k_step_fp64(const Work *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
-            const Seg *__restrict__ segs, Bufs bufs) {
+            const Seg *__restrict__ segs, const ColBlock *__restrict__ cbl, const SegB *__restrict__ segb,
+            Bufs bufs) {
   __shared__ double As[F_TK][F_TM + 1];
   __shared__ double Bs[F_TK][F_TN + 1];
+  __shared__ int cbj[F_TN], cbrel[F_TN];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
     const Work wk = work[w];
     const Group g = groups[wk.group];
     const int m0 = wk.mt * F_TM, n0 = wk.nt * F_TN;
+    if (g.ncb) tile_cblocks(cbl, g, n0, F_TN, cbj, cbrel);
+    __syncthreads();
     double c00 = 0.0, c01 = 0.0, c10 = 0.0, c11 = 0.0;
     for (int si = 0; si < g.nseg; ++si) {
       const Seg s = segs[g.seg0 + si];
@@ -75,7 +121,18 @@ k_step_fp64(const Work *__restrict__ work, int64_t nwork, const Group *__restric
           int k, c;
           if (b_nfast) { k = e / F_TN; c = e % F_TN; } else { c = e / F_TK; k = e % F_TK; }
           double v = 0.0;
-          if (n0 + c < g.N && k0 + k < s.K) v = B[(int64_t)(k0 + k) * s.sbk + (int64_t)(n0 + c) * s.sbn];
+          if (n0 + c < g.N && k0 + k < s.K) {
+            if (g.ncb == 0) {
+              v = B[(int64_t)(k0 + k) * s.sbk + (int64_t)(n0 + c) * s.sbn];
+            } else {
+              const int j = cbj[c];
+              if (j >= 0) {
+                const SegB sb = segb[g.sb0 + (int64_t)si * g.ncb + j];
+                if (sb.b_off >= 0)
+                  v = bufs.p[s.bbuf][sb.b_off + (int64_t)(k0 + k) * sb.sbk + (int64_t)cbrel[c] * sb.sbn];
+              }
+            }
+          }
           Bs[k][c] = v;
         }
         __syncthreads();
@@ -91,19 +148,19 @@ k_step_fp64(const Work *__restrict__ work, int64_t nwork, const Group *__restric
         __syncthreads();
       }
     }
-    double *C = bufs.p[g.cbuf] + g.c_off;
     const int r0 = m0 + ty, r1 = m0 + ty + 16, q0 = n0 + tx, q1 = n0 + tx + 16;
-    if (r0 < g.M && q0 < g.N) C[(int64_t)r0 * g.scm + (int64_t)q0 * g.scn] = c00;
-    if (r0 < g.M && q1 < g.N) C[(int64_t)r0 * g.scm + (int64_t)q1 * g.scn] = c01;
-    if (r1 < g.M && q0 < g.N) C[(int64_t)r1 * g.scm + (int64_t)q0 * g.scn] = c10;
-    if (r1 < g.M && q1 < g.N) C[(int64_t)r1 * g.scm + (int64_t)q1 * g.scn] = c11;
+    if (r0 < g.M && q0 < g.N) store_c(bufs, cbl, g, r0, q0, n0, cbj, cbrel, c00);
+    if (r0 < g.M && q1 < g.N) store_c(bufs, cbl, g, r0, q1, n0, cbj, cbrel, c01);
+    if (r1 < g.M && q0 < g.N) store_c(bufs, cbl, g, r1, q0, n0, cbj, cbrel, c10);
+    if (r1 < g.M && q1 < g.N) store_c(bufs, cbl, g, r1, q1, n0, cbj, cbrel, c11);
+    __syncthreads();  // the column map is rewritten by the next tile
   }
 }
 
 int launch_step_fp64(const Step &s, const Bufs &b, void *stream) {
   if (s.nwork_fp64 == 0) return ZMPO_OK;
   k_step_fp64<<<grid_for(s.nwork_fp64, 8), F_NT, 0, (cudaStream_t)stream>>>(
-      s.d_work_fp64, s.nwork_fp64, s.d_groups, s.d_segs, b);
+      s.d_work_fp64, s.nwork_fp64, s.d_groups, s.d_segs, s.d_cblocks, s.d_segb, b);
   return launch_error("k_step_fp64");
 }
 
@@ -234,12 +291,25 @@ __device__ __forceinline__ void mma_bf16(float *c, const uint32_t *a, const uint
 
 struct Slot {
   const double *a;  // A(row 0, k) of the slot's segment
-  const double *b;  // B(k, col 0)
+  const double *b;  // B(k, col 0); column-block groups: B buffer base
   int64_t sam, sbn;
   double alpha;
   int scaled;       // alpha != 1 (decided once per slot, not per element)
+  int seg;          // column-block groups: segment index inside the group
+  int kk;           // and k inside the segment
   int pad;
 };
+
+// B(k, col) of a column-block group for the thread's column block jb
+// (jb < 0: column outside the group) -- zero where the pair has no B part
+__device__ __forceinline__ double load_b_cb(const Slot &sl, const SegB *__restrict__ segb, const Group &g,
+                                            int jb, int colrel) {
+  if (jb < 0) return 0.0;
+  const SegB sb = segb[g.sb0 + (int64_t)sl.seg * g.ncb + jb];
+  if (sb.b_off < 0) return 0.0;
+  return __ldg(sl.b + sb.b_off + (int64_t)sl.kk * sb.sbk + (int64_t)colrel * sb.sbn);
+}
+
 
 // Slot table of the next chunk, built by warp 0: lane l looks at segment
 // cur+l; an inclusive warp scan of the slots each segment can still provide
@@ -270,17 +340,19 @@ __device__ __forceinline__ void build_slots(const Group &g, const Seg *__restric
   const int excl = incl - avail;
   if (avail > 0 && excl < TK) {
     const double *A = bufs.p[sg.abuf] + sg.a_off;
-    const double *B = bufs.p[sg.bbuf] + sg.b_off;
+    const double *B = g.ncb ? bufs.p[sg.bbuf] : bufs.p[sg.bbuf] + sg.b_off;
     const int k0 = lane == 0 ? curk : 0;
     const int jend = min(incl, TK);
     for (int j = excl; j < jend; ++j) {
       const int kk = k0 + (j - excl);
       slots[j].a = A + (int64_t)kk * sg.sak;
-      slots[j].b = B + (int64_t)kk * sg.sbk;
+      slots[j].b = g.ncb ? B : B + (int64_t)kk * sg.sbk;
       slots[j].sam = sg.sam;
       slots[j].sbn = sg.sbn;
       slots[j].alpha = sg.alpha;
       slots[j].scaled = sg.alpha != 1.0;
+      slots[j].seg = sidx;
+      slots[j].kk = kk;
     }
   }
   // where the chunk ends: first lane whose inclusive sum reaches 32
@@ -338,7 +410,8 @@ struct TcShape {
 template <int S, int TM, int TN>
 __global__ void __launch_bounds__(TcShape<S, TM, TN>::NT, TcShape<S, TM, TN>::THREADS_SM / TcShape<S, TM, TN>::NT)
 k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
-          const Seg *__restrict__ segs, Bufs bufs) {
+          const Seg *__restrict__ segs, const ColBlock *__restrict__ cbl, const SegB *__restrict__ segb,
+          Bufs bufs) {
   using Sh = TcShape<S, TM, TN>;
   constexpr int TPR = Sh::TPR, KPA = Sh::KPA, TPC = Sh::TPC, KPB = Sh::KPB;
   constexpr int TK = Sh::TK, T_PAD = Sh::PAD;
@@ -350,6 +423,7 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
   Slot *slots = reinterpret_cast<Slot *>(Eb + (TN < 16 ? 16 : TN));  // [TK] (Eb holds TN ints)
   int *ctl = reinterpret_cast<int *>(slots + TK);                 // cursor[2], nslot
 
+  __shared__ int cbj[TN], cbrel[TN];  // column-block map of the tile
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wm = (warp % Sh::WM) * 16, wn = (warp / Sh::WM) * 8;  // this warp's m16n8 piece
   const int gq = lane >> 2, tq = lane & 3;
@@ -366,7 +440,9 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
       ctl[0] = 0;
       ctl[1] = 0;
     }
+    if (g.ncb) tile_cblocks(cbl, g, n0, TN, cbj, cbrel);
     __syncthreads();
+    const int jb = g.ncb ? cbj[cb] : -1, colrel = g.ncb ? cbrel[cb] : 0;
     while (true) {
       if (warp == 0) build_slots<TK>(g, segs, bufs, slots, ctl, ctl + 2, lane);
       __syncthreads();
@@ -409,7 +485,8 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
         for (int t = 0; t < KPB; ++t) {
           const int j = partb * KPB + t;
           double x = 0.0;
-          if (j < ns && colb < g.N) x = __ldg(slots[j].b + (int64_t)colb * slots[j].sbn);
+          if (j < ns && colb < g.N)
+            x = g.ncb ? load_b_cb(slots[j], segb, g, jb, colrel) : __ldg(slots[j].b + (int64_t)colb * slots[j].sbn);
           v[t] = x;
           emax = max(emax, dexp(x));
         }
@@ -483,13 +560,13 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
       }
       __syncthreads();
     }
-    double *C = bufs.p[g.cbuf] + g.c_off;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int r = m0 + wm + gq + (i >> 1) * 8;
       const int c = n0 + wn + 2 * tq + (i & 1);
-      if (r < g.M && c < g.N) C[(int64_t)r * g.scm + (int64_t)c * g.scn] = (double)hi[i] + (double)lo[i];
+      if (r < g.M && c < g.N) store_c(bufs, cbl, g, r, c, n0, cbj, cbrel, (double)hi[i] + (double)lo[i]);
     }
+    __syncthreads();  // the column map is rewritten by the next tile
   }
 }
 
@@ -507,7 +584,7 @@ static int launch_tc_t(const Work *work, int64_t nwork, const Step &s, const Buf
   }
   constexpr int NT = TcShape<S, TM, TN>::NT;
   k_step_tc<S, TM, TN><<<grid_for(nwork, TcShape<S, TM, TN>::THREADS_SM / NT), NT, smem, (cudaStream_t)stream>>>(
-      work, nwork, s.d_groups, s.d_segs, b);
+      work, nwork, s.d_groups, s.d_segs, s.d_cblocks, s.d_segb, b);
   return launch_error("k_step_tc");
 }
 

@@ -366,6 +366,127 @@ static std::vector<Leg2> merge_legs(const std::vector<Leg2> &in) {
 }
 
 // Expand all output works of one launch into groups / segments.
+constexpr int64_t kSplitK = 2048;
+
+// Column-block groups: output blocks of one step whose groups read the same A
+// rows (same output layout, same row-leg sectors, same A tensor and term) are
+// joined side by side in N.  Their segments become the union of the A parts;
+// each (segment, column block) pair keeps its own B part, or none.  Only
+// groups made of one region with one segment per task take part, and only
+// while the joined K stays below the split-K length.
+struct MergeInfo {
+  bool ok = false;
+  std::string key;
+};
+
+static void merge_column_blocks(Step &st, const std::vector<MergeInfo> &info) {
+  std::unordered_map<std::string, std::vector<int>> buckets;
+  std::vector<int> order_keys;
+  for (size_t g = 0; g < st.groups.size(); ++g)
+    if (info[g].ok) buckets[info[g].key].push_back((int)g);
+  std::vector<Group> groups;
+  std::vector<Seg> segs;
+  std::vector<char> done(st.groups.size(), 0);
+  auto emit_plain = [&](int gi) {
+    Group g = st.groups[gi];
+    const int32_t s0 = g.seg0;
+    g.seg0 = (int32_t)segs.size();
+    for (int i = 0; i < g.nseg; ++i) segs.push_back(st.segs[s0 + i]);
+    groups.push_back(g);
+  };
+  for (size_t gi = 0; gi < st.groups.size(); ++gi) {
+    if (done[gi]) continue;
+    if (!info[gi].ok) {
+      emit_plain((int)gi);
+      continue;
+    }
+    const std::vector<int> &bk = buckets[info[gi].key];
+    for (int x : bk) done[x] = 1;
+    if (bk.size() < 2) {
+      emit_plain((int)gi);
+      continue;
+    }
+    // union of A parts, in first-seen order
+    struct PartKey {
+      int64_t a_off, sam, sak;
+      double alpha;
+      int32_t K;
+      int8_t abuf;
+      bool operator<(const PartKey &o) const {
+        return std::tie(a_off, sam, sak, alpha, K, abuf) < std::tie(o.a_off, o.sam, o.sak, o.alpha, o.K, o.abuf);
+      }
+    };
+    std::map<PartKey, int> pidx;
+    std::vector<Seg> parts;
+    struct Use {
+      int part, blk;
+      SegB b;
+    };
+    std::vector<Use> uses;
+    bool ok = true;
+    int64_t ntot = 0, ktot = 0;
+    const Group &G0 = st.groups[bk[0]];
+    const int8_t bbuf = st.segs[G0.seg0].bbuf;
+    for (size_t j = 0; j < bk.size() && ok; ++j) {
+      const Group &G = st.groups[bk[j]];
+      if (G.M != G0.M || G.cbuf != G0.cbuf) ok = false;
+      ntot += G.N;
+      for (int i = 0; i < G.nseg && ok; ++i) {
+        const Seg &sg = st.segs[G.seg0 + i];
+        if (sg.bbuf != bbuf) {
+          ok = false;
+          break;
+        }
+        PartKey k{sg.a_off, sg.sam, sg.sak, sg.alpha, sg.K, sg.abuf};
+        auto it = pidx.find(k);
+        int p;
+        if (it == pidx.end()) {
+          p = (int)parts.size();
+          pidx[k] = p;
+          parts.push_back(sg);
+          ktot += sg.K;
+        } else {
+          p = it->second;
+        }
+        uses.push_back({p, (int)j, {sg.b_off, sg.sbk, sg.sbn}});
+      }
+    }
+    if (!ok || ktot > kSplitK || ntot > INT32_MAX) {
+      for (int x : bk) emit_plain(x);
+      continue;
+    }
+    Group mg{};
+    mg.c_off = 0;
+    mg.scm = mg.scn = 0;
+    mg.M = G0.M;
+    mg.N = (int32_t)ntot;
+    mg.seg0 = (int32_t)segs.size();
+    mg.nseg = (int32_t)parts.size();
+    mg.cbuf = G0.cbuf;
+    mg.ncb = (int32_t)bk.size();
+    mg.cb0 = (int32_t)st.cblocks.size();
+    mg.sb0 = (int32_t)st.segb.size();
+    int32_t n0 = 0;
+    for (int x : bk) {
+      const Group &G = st.groups[x];
+      st.cblocks.push_back({G.c_off, G.scm, G.scn, n0, G.N});
+      n0 += G.N;
+    }
+    const size_t sb_base = st.segb.size();
+    st.segb.resize(sb_base + parts.size() * bk.size(), SegB{-1, 0, 0});
+    for (auto &u : uses) st.segb[sb_base + (size_t)u.part * bk.size() + u.blk] = u.b;
+    for (auto &p : parts) {
+      Seg sg = p;
+      sg.b_off = -1;
+      sg.sbk = sg.sbn = 0;
+      segs.push_back(sg);
+    }
+    groups.push_back(mg);
+  }
+  st.groups.swap(groups);
+  st.segs.swap(segs);
+}
+
 static int build_step(std::vector<OutWork> &works, Step &st) {
   st.segs.clear();
   st.groups.clear();
@@ -388,6 +509,7 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
     for (auto &kv : seen) in_elems += (double)kv.second;
     st.alg_bytes = 8.0 * (in_elems + out_elems);
   }
+  std::vector<MergeInfo> minfo;
   for (auto &w : works) {
     const Layout &O = *w.lo;
     int64_t od[16], ost[16];
@@ -464,6 +586,21 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
     const int64_t scm = pm >= 0 ? ost[innermost(mr[pm])] : 0;
     const int64_t scn = pn >= 0 ? ost[innermost(nr[pn])] : 0;
     if (M > INT32_MAX || N > INT32_MAX) return fail(ZMPO_E_SIZE, "block too large");
+    // key of the A rows this output block reads (column-block groups)
+    MergeInfo mi;
+    mi.ok = nsub == 1 && !w.tasks.empty();
+    if (mi.ok) {
+      int sec[16];
+      O.sectors(O.pk->flat[w.ob], sec);
+      const auto &t0 = w.tasks[0];
+      char buf[64];
+      snprintf(buf, sizeof(buf), "%p|%p|%d|%d|%lld|%lld|", (const void *)w.lo, (const void *)t0.la, t0.abuf,
+               w.cbuf, (long long)t0.a_base, (long long)M);
+      mi.key = buf;
+      for (int j = 0; j < ne1; ++j) mi.key += std::to_string(sec[j]) + ",";
+      for (auto &t : w.tasks)
+        if (t.la != t0.la || t.abuf != t0.abuf || t.a_base != t0.a_base) mi.ok = false;
+    }
     for (int64_t sub = 0; sub < nsub; ++sub) {
       // multi-index of the sub-region over the loop ranges; each range is a
       // merged leg so its index maps linearly with the innermost stride
@@ -487,7 +624,7 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
       g.N = (int32_t)N;
       g.seg0 = (int32_t)st.segs.size();
       g.cbuf = w.cbuf;
-      g.pad = 0;
+      g.ncb = g.cb0 = g.sb0 = 0;
       for (auto &tk : w.tasks) {
         const Layout &A = *tk.la, &B = *tk.lb;
         int64_t ad[16], as[16], bd[16], bs[16];
@@ -532,6 +669,7 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
           if (i != pk) kloops.push_back(kl[i]);
         int64_t nk = 1;
         for (auto &l : kloops) nk *= l.d;
+        if (nk != 1) mi.ok = false;
         for (int64_t ki = 0; ki < nk; ++ki) {
           int64_t aa = a0, bb = b0, tt = ki;
           for (int i = (int)kloops.size() - 1; i >= 0; --i) {
@@ -557,8 +695,10 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
       }
       g.nseg = (int32_t)st.segs.size() - g.seg0;
       st.groups.push_back(g);
+      minfo.push_back(mi);
     }
   }
+  merge_column_blocks(st, minfo);
   return ZMPO_OK;
 }
 
@@ -568,7 +708,6 @@ constexpr int kTileFP64M = 32, kTileFP64N = 32;
 // Cut groups whose summed K exceeds kSplitK into parts of about kSplitK (at
 // segment boundaries, or inside a long segment); parts go to scratch and a
 // reduction sums them in order.
-constexpr int64_t kSplitK = 2048;
 
 static void split_long_groups(Step &st) {
   std::vector<Group> out;
@@ -681,6 +820,8 @@ static int upload_step(Step &st) {
   };
   CUDA_TRY(up(&st.d_segs, st.segs));
   CUDA_TRY(up(&st.d_groups, st.groups));
+  CUDA_TRY(up(&st.d_cblocks, st.cblocks));
+  CUDA_TRY(up(&st.d_segb, st.segb));
   CUDA_TRY(up(&st.d_work_fp64, w64));
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) CUDA_TRY(up(&st.d_work_tc[i][j], wtc[i][j]));
@@ -698,6 +839,10 @@ static void free_step(Step &st) {
   st.ev0 = st.ev1 = nullptr;
   cudaFree(st.d_segs);
   cudaFree(st.d_groups);
+  cudaFree(st.d_cblocks);
+  cudaFree(st.d_segb);
+  st.d_cblocks = nullptr;
+  st.d_segb = nullptr;
   cudaFree(st.d_work_fp64);
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) {
@@ -1455,6 +1600,24 @@ int zmpo_plan_groups(zmpo_engine *e, int plan_id, int step, int64_t *ngroups, in
       ktot[g] = k;
     }
   }
+  return ZMPO_OK;
+}
+
+int zmpo_plan_step_tasks(zmpo_engine *e, int plan_id, int step, int64_t *counts, void *groups, void *segs,
+                         void *cblocks, void *segb) {
+  Plan *P = get_plan(e, plan_id, 0);
+  if (!P || step < 0 || step >= (int)P->steps.size() || !counts)
+    return fail(ZMPO_E_ID, "plan_step_tasks: unknown plan or step");
+  const Step &st = P->steps[step];
+  if (st.uploaded) return fail(ZMPO_E_ARG, "plan_step_tasks: task lists already moved to the device");
+  counts[0] = (int64_t)st.groups.size();
+  counts[1] = (int64_t)st.segs.size();
+  counts[2] = (int64_t)st.cblocks.size();
+  counts[3] = (int64_t)st.segb.size();
+  if (groups) memcpy(groups, st.groups.data(), st.groups.size() * sizeof(Group));
+  if (segs) memcpy(segs, st.segs.data(), st.segs.size() * sizeof(Seg));
+  if (cblocks) memcpy(cblocks, st.cblocks.data(), st.cblocks.size() * sizeof(ColBlock));
+  if (segb) memcpy(segb, st.segb.data(), st.segb.size() * sizeof(SegB));
   return ZMPO_OK;
 }
 

@@ -113,6 +113,29 @@ class Engine:
                                          ctypes.byref(nl)), "plan_stats")
         return fl.value, nt.value, nl.value
 
+    # task records of csrc/engine.h (C layout)
+    GROUP = numpy.dtype([("c_off", "i8"), ("scm", "i8"), ("scn", "i8"), ("M", "i4"), ("N", "i4"),
+                         ("seg0", "i4"), ("nseg", "i4"), ("cbuf", "i4"), ("ncb", "i4"), ("cb0", "i4"),
+                         ("sb0", "i4")], align=True)
+    SEG = numpy.dtype([("a_off", "i8"), ("b_off", "i8"), ("sam", "i8"), ("sak", "i8"), ("sbk", "i8"),
+                       ("sbn", "i8"), ("alpha", "f8"), ("K", "i4"), ("abuf", "i1"), ("bbuf", "i1"),
+                       ("pad0", "i1"), ("pad1", "i1")], align=True)
+    COLBLOCK = numpy.dtype([("c_off", "i8"), ("scm", "i8"), ("scn", "i8"), ("n0", "i4"), ("n", "i4")],
+                           align=True)
+    SEGB = numpy.dtype([("b_off", "i8"), ("sbk", "i8"), ("sbn", "i8")], align=True)
+
+    def step_tasks(self, pid, step):
+        """Host copy of a step's task records (before its first execution)."""
+        cnt = numpy.zeros(4, dtype=numpy.int64)
+        check(_lib.lib().zmpo_plan_step_tasks(self.h, pid, step, lptr(cnt), None, None, None, None),
+              "plan_step_tasks")
+        arrs = [numpy.zeros(int(n), dtype=d) for n, d in zip(cnt, (self.GROUP, self.SEG, self.COLBLOCK,
+                                                                   self.SEGB))]
+        check(_lib.lib().zmpo_plan_step_tasks(self.h, pid, step, lptr(cnt), *[a.ctypes.data_as(ctypes.c_void_p)
+                                                                               for a in arrs]),
+              "plan_step_tasks")
+        return arrs
+
     def kernel_count(self, pid, precision="split"):
         """Kernel launches one execution of the plan issues at ``precision``."""
         n = ctypes.c_int()
