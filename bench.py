@@ -30,6 +30,15 @@ sys.path.insert(0, HERE)
 WORKLOAD = dict(K=24, nelec=24, D=512, isite=11, seed=2024)
 SMALL = dict(K=12, nelec=12, D=128, isite=5, seed=2024)
 MEDIUM = dict(K=16, nelec=16, D=256, isite=7, seed=2024)
+# the large batched configuration (hopping 0.7), run with a workspace budget
+LARGE = dict(K=36, nelec=36, D=1024, isite=17, seed=2024, hop=0.7)
+LARGE_WORKSPACE = 64e9
+# DRAM bytes (read + write) over algorithmic bytes of the T3 step, measured
+# with ncu (dram__bytes_read.sum + dram__bytes_write.sum of every launch in
+# the step's NVTX range) on the K=16, D=256 two-site dot: 1.896 GB against
+# 1.934 GB.  The full-size traffic is this ratio times the step's algorithmic
+# bytes (the step's traffic grows with the operand and output sizes).
+T3_TRAFFIC_RATIO = 1.896 / 1.934
 METRIC = "sweep s & sigma-vec TFLOP/s, split-BF16 vs FP64 on 1 GB300 at ΔE≤1e-8 Eh"
 
 
@@ -89,10 +98,10 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def build_problem(with_oracle=False, small=False, medium=False):
+def build_problem(with_oracle=False, small=False, medium=False, large=False):
     from tests.problems import random_problem
     t0 = time.perf_counter()
-    cfg = SMALL if small else (MEDIUM if medium else WORKLOAD)
+    cfg = SMALL if small else (MEDIUM if medium else (LARGE if large else WORKLOAD))
     P = random_problem(device=True, with_oracle=with_oracle, **cfg)
     return P, time.perf_counter() - t0
 
@@ -187,6 +196,57 @@ def sweep_metrics(K=10, nelec=10, D=64, nsweep=10, seed=2024):
     return out
 
 
+def gradient_metrics(K=16, nelec=16, D=256, seed=2024):
+    """Energy gradient (dE/dh1e, dE/d(pq|rs)) at a seeded random left-canonical
+    MPS of K=16, 16 electrons, D=256 (the adjoint configuration's sizes; the
+    cost does not depend on convergence): seconds for the site gradients
+    (engine contractions) and for the chain rule, and a central-difference
+    check (step 1e-5) of the fixed-MPS energy along a random symmetric direction."""
+    import torch
+    from tests.problems import bond_structure, random_left_site, QPHYS
+    from zmpo_dmrg_gb300 import integrals as I, adjoint
+    from zmpo_dmrg_gb300.mpo_dmrg_class import mpo_dmrg
+    from zmpo_dmrg_gb300.qtensor import qtensor
+    rng = numpy.random.default_rng(seed)
+    h, eri, _ = I.synthetic(K, seed)
+    m = mpo_dmrg(seed=1)
+    m.nsite, m.sbas, m.isym = K, 2 * K, 2
+    m.build()
+    m.partition()
+    m.loadInts(I.spin_orbital(h, eri))
+    m.dumpMPO()
+    qnuml, _ = bond_structure(K, nelec, 0.0, D, rng)
+    fmps = {'nsite': K}
+    for i in range(K):
+        t = qtensor([False, False, True])
+        t.fromDenseTensor(random_left_site(qnuml[i], qnuml[i + 1], rng), [qnuml[i], QPHYS, qnuml[i + 1]])
+        fmps['site%d' % i] = t
+    for i in range(K + 1):
+        fmps['qnum%d' % i] = qnuml[i]
+    m.flmps = fmps
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    grads, energy, _ = adjoint.site_gradients(m)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    dh, dg = adjoint.integral_gradients(m, h, eri, grads)
+    t2 = time.perf_counter()
+    dH = rng.standard_normal((K, K))
+    dH = dH + dH.T
+    dG = adjoint.symmetrize_eri_gradient(rng.standard_normal((K, K, K, K)))
+    eps = 1e-5
+    es = []
+    for sgn in (1, -1):
+        m.loadInts(I.spin_orbital(h + sgn * eps * dH, eri + sgn * eps * dG))
+        m.dumpMPO()
+        es.append(m.checkMPS()[0])
+    fd = (es[0] - es[1]) / (2 * eps)
+    an = float((dh * dH).sum() + (dg * dG).sum())
+    return {"workload": "K=%d N=%d D=%d random left-canonical MPS, %d terms" % (K, nelec, D, m.nops),
+            "s_site_gradients": t1 - t0, "s_chain_rule": t2 - t1, "energy": energy,
+            "fd_directional": fd, "adjoint_directional": an, "abs_diff": abs(fd - an)}
+
+
 def cpu_threads():
     return os.cpu_count() or 1
 
@@ -227,6 +287,10 @@ def main():
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--small", action="store_true", help="K=12, D=128 case (profiling)")
     ap.add_argument("--medium", action="store_true", help="K=16, D=256 case (profiling)")
+    ap.add_argument("--gradient", action="store_true",
+                    help="also time the energy gradient at K=16, D=256 (adjoint configuration)")
+    ap.add_argument("--large", action="store_true",
+                    help="K=36, D=1024, hopping 0.7 (terms in batches under a 64 GB workspace)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -244,8 +308,11 @@ def main():
     from zmpo_dmrg_gb300 import engine as E
     from zmpo_dmrg_gb300.mpo_dmrg_kernel import HVec, _sigma_plan
 
-    P, t_build = build_problem(small=args.small, medium=args.medium)
+    P, t_build = build_problem(small=args.small, medium=args.medium, large=args.large)
     pm = P.p
+    if args.large:
+        pm.workspace_budget = LARGE_WORKSPACE
+        pm._sigma_plan = None
     info = [pm, P.isite, 2, pm.flst, 'L', True]
     eng = E.get()
     plan = _sigma_plan(info)
@@ -257,7 +324,7 @@ def main():
     stream = torch.cuda.current_stream()
 
     def step(prec):
-        eng.sigma(plan.pid, plan.fL.buf, plan.fR.buf, pm.mpo_store.buf, x, y, plan.workspace, prec)
+        plan.run(pm, x, y, prec)
 
     def timed(prec, steps, warmup):
         for _ in range(warmup):
@@ -293,12 +360,16 @@ def main():
     R = plan.fR.buf
     W = pm.mpo_store.buf
     eng.profile(True)
-    eng.launch_times(plan.pid)
+    for pid in plan.pids:
+        eng.launch_times(pid)
     nprof = max(5, args.steps // 2)
     for _ in range(nprof):
         step(args.precision)
     torch.cuda.synchronize()
     ms, abytes, ncalls = eng.launch_times(plan.pid)
+    for pid in plan.pids[1:]:   # term batches: the same steps, summed
+        ms2, ab2, _ = eng.launch_times(pid)
+        ms, abytes = ms + ms2, abytes + ab2
     eng.profile(False)
     launches = [{"launch": i, "ms": float(ms[i]), "alg_bytes": float(abytes[i]),
                  "GBs": float(abytes[i] / (ms[i] * 1e-3) / 1e9) if ms[i] > 0 else None}
@@ -309,14 +380,14 @@ def main():
     yh = torch.empty(n, dtype=torch.float64).pin_memory()
     for _ in range(3):
         xd = xh.cuda(non_blocking=True)
-        eng.sigma(plan.pid, L, R, W, xd, y, plan.workspace, args.precision)
+        plan.run(pm, xd, y, args.precision)
         yh.copy_(y, non_blocking=True)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     ne2e = max(3, args.steps // 2)
     for _ in range(ne2e):
         xd = xh.cuda(non_blocking=True)
-        eng.sigma(plan.pid, L, R, W, xd, y, plan.workspace, args.precision)
+        plan.run(pm, xd, y, args.precision)
         yh.copy_(y, non_blocking=True)
         torch.cuda.synchronize()
     t_e2e = (time.perf_counter() - t0) / ne2e
@@ -338,22 +409,29 @@ def main():
         "config": {"workload": "two-site H.psi, K=%d N=%d Sz=0 D=%d, %d terms, (N,Sz) blocks" %
                                (P.K, P.nelec, P.D, pm.nops),
                    "ndim0": n, "F_ref_flops": flops, "tasks": plan.ntasks, "precision": args.precision,
+                   "term_batches": len(plan.pids),
                    "l2": "inputs larger than L2 (environments %.2f GB)" % ((L.numel() + R.numel()) * 8 / 1e9),
                    "build_s": t_build},
         "fp64": {"value": flops / t_fp64 / 1e12, "ms_per_step": t_fp64 * 1e3},
         "split_vs_fp64_rel_err": err_split,
         "e2e": {"value": flops / t_e2e / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": n * 8,
                 "d2h_bytes_per_step": n * 8},
-        "gpu_launches": args.steps * eng.kernel_count(plan.pid, args.precision),
+        "gpu_launches": args.steps * sum(eng.kernel_count(pid, args.precision) for pid in plan.pids),
         "clocks": clocks_rec,
         "launches": launches,
         "roofline": {"bound": "hbm", "kernel": "k_step_tc (all tile shapes) of step %d of %d" % (top, plan.nlaunch),
                      "achieved": launches[top]["GBs"], "peak": hbm, "unit": "GB/s",
-                     "frac": (launches[top]["GBs"] or 0.0) / hbm, "traffic": None,
+                     "frac": (launches[top]["GBs"] or 0.0) / hbm,
+                     "traffic": (T3_TRAFFIC_RATIO * launches[top]["alg_bytes"] / len(plan.pids)
+                                 if top == 2 and args.precision == "split" else None),
+                     "traffic_note": "bytes per launch of the step, scaled from the ncu capture of the K=16 D=256 "
+                                     "dot (ratio %.3f to algorithmic bytes)" % T3_TRAFFIC_RATIO,
                      "peak_source": peak_kind},
     }
     if rank == 0 and not args.no_sweep:
         result["sweep"] = sweep_metrics()
+    if rank == 0 and args.gradient:
+        result["gradient"] = gradient_metrics()
     if rank == 0 and not args.no_cpu:
         fl, dt, ch = oracle_sample(P)
         result["cpu_baseline"] = {"value": fl / dt / 1e12, "unit": "TFLOP/s", "cores": cpu_threads(),

@@ -100,3 +100,34 @@ def test_perturbed_rdm(gpu, case, status):
     assert numpy.abs(a - b).max() <= 1e-12 * max(1.0, numpy.abs(b).max())
     noise_part = oracle_prdm(P, status, noise=1.0) - oracle_prdm(P, status, noise=0.0)
     assert numpy.abs(noise_part).max() > 1e-6   # the noise term is exercised
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_sigma_term_batches(gpu, precision):
+    """With a workspace budget the terms run in batches (summed on the
+    device); sigma and diag(H) agree with the single-plan result."""
+    from zmpo_dmrg_gb300.mpo_dmrg_kernel import HVec, HDiag
+    P = prob(CASES[4])
+    m = P.p
+    x = numpy.random.default_rng(12).standard_normal(P.ndim0)
+    info = [m, P.isite, 2, m.flst, 'L', True]
+    m.precision = precision
+    m._sigma_plan = None
+    y1 = HVec(x, info, P.ndim0, None)
+    d1 = HDiag(info, P.ndim0, None).cpu().numpy()
+    ws1 = m._sigma_plan[1].workspace.numel() * 8
+    m._sigma_plan[1].release()
+    m._sigma_plan = None
+    m.workspace_budget = ws1 // 3
+    try:
+        y2 = HVec(x, info, P.ndim0, None)
+        d2 = HDiag(info, P.ndim0, None).cpu().numpy()
+        assert len(m._sigma_plan[1].pids) >= 3
+    finally:
+        m._sigma_plan[1].release()
+        m._sigma_plan = None
+        m.workspace_budget = None
+        m.precision = "fp64"
+    tol = 1e-12 if precision == "fp64" else 1e-8
+    assert rel(y2, y1) < tol
+    assert rel(d2, d1) < 1e-12

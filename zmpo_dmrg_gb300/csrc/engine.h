@@ -72,6 +72,7 @@ struct Bufs {
 
 // One launch worth of tasks (device copies + host mirror of sizes).
 struct Step {
+  int idx = 0;                   // position in its plan's chain
   std::vector<Seg> segs;
   std::vector<Group> groups;
   std::vector<ColBlock> cblocks;

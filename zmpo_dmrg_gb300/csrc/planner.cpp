@@ -22,6 +22,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
 #include "../../include/zmpo_gb300.h"
 #include "engine.h"
 
@@ -874,6 +875,14 @@ static void profile_collect(Step &st) {
 static int run_step(Step &st, const Bufs &b, int precision, void *stream) {
   int rc = upload_step(st);
   if (rc) return rc;
+  // one NVTX range per step ("zmpo.step<i>"), so a profiler can select the
+  // launches of one step of a chain
+  static const char *kRange[] = {"zmpo.step0", "zmpo.step1", "zmpo.step2", "zmpo.step3",
+                                 "zmpo.step4", "zmpo.step5", "zmpo.step6", "zmpo.step7"};
+  nvtxRangePushA(kRange[st.idx & 7]);
+  struct Pop {
+    ~Pop() { nvtxRangePop(); }
+  } pop;
   if (g_profile) {
     profile_collect(st);
     if (!st.ev0) {
@@ -1075,6 +1084,7 @@ int zmpo_contract_plan(zmpo_engine *e, int lay_a, int lay_b, int naxes, const in
       w.tasks.push_back({C, A, B, O, C->tasks[t].ab, C->tasks[t].bb, 0, 0, 0, 1, 1.0});
   }
   P->steps.emplace_back();
+  P->steps.back().idx = (int)P->steps.size() - 1;
   rc = build_step(works, P->steps.back());
   if (rc) return rc;
   P->flops = P->steps.back().flops;
@@ -1247,6 +1257,7 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
       }
     }
     P->steps.emplace_back();
+    P->steps.back().idx = (int)P->steps.size() - 1;
     int rc = build_step(works, P->steps.back());
     if (rc) return rc;
     P->exec_flops += P->steps.back().flops;
@@ -1513,6 +1524,7 @@ int zmpo_renorm_plan(zmpo_engine *e, const zmpo_renorm_desc *d, int *plan_id) {
       }
     }
     P->steps.emplace_back();
+    P->steps.back().idx = (int)P->steps.size() - 1;
     int rc = build_step(works, P->steps.back());
     if (rc) return rc;
     P->flops += P->steps.back().flops;

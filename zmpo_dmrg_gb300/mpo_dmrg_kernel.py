@@ -103,6 +103,7 @@ class SigmaPlan:
         self.nops = len(ops)
         if self.nops == 0:
             self.pid = None
+            self.pids = []
             return
         torch = _torch()
         lay_psi = dmrg.qtmp_psi_layout
@@ -114,11 +115,39 @@ class SigmaPlan:
             qN, idx = n_only_map(dmrg.qtmp)
             lay_psi = qN.layout
             self.nmap = (torch.as_tensor(idx, device="cuda"), qN.size_allowed)
-        self.pid, ws = eng.sigma_plan(ncsite, op_cls, lay_L, lay_Wi, lay_Wj if ncsite == 2 else None,
-                                      lay_Rf, lay_psi, off_L, off_R, off_Wi,
-                                      off_Wj if ncsite == 2 else None, wts)
-        self.workspace = torch.empty(max(ws // 8, 1), dtype=torch.float64, device="cuda")
-        self.flops, self.ntasks, self.nlaunch = eng.plan_stats(self.pid)
+        # the terms' intermediates live in one workspace; with a budget
+        # (dmrg.workspace_budget, bytes) the terms are cut into consecutive
+        # batches whose workspace fits, run one after the other
+        budget = getattr(dmrg, "workspace_budget", None)
+        nb = 1
+        while True:
+            cuts = numpy.linspace(0, self.nops, nb + 1).round().astype(int)
+            pids, wss = [], []
+            for b in range(nb):
+                sl = slice(cuts[b], cuts[b + 1])
+                if sl.start == sl.stop:
+                    continue
+                used = sorted(set(op_cls[sl]))
+                remap = {c: i for i, c in enumerate(used)}
+                pid, ws = eng.sigma_plan(ncsite, [remap[c] for c in op_cls[sl]], [lay_L[c] for c in used],
+                                         [lay_Wi[c] for c in used],
+                                         [lay_Wj[c] for c in used] if ncsite == 2 else None,
+                                         [lay_Rf[c] for c in used], lay_psi, off_L[sl], off_R[sl],
+                                         off_Wi[sl], off_Wj[sl] if ncsite == 2 else None, wts[sl])
+                pids.append(pid)
+                wss.append(ws)
+            if budget is None or max(wss) <= budget or nb >= self.nops:
+                break
+            for pid in pids:
+                eng.destroy_plan(pid)
+            nb *= 2
+        self.pids = pids
+        self.pid = pids[0]
+        self.workspace = torch.empty(max(max(wss) // 8, 1), dtype=torch.float64, device="cuda")
+        stats = [eng.plan_stats(pid) for pid in pids]
+        self.flops = sum(x[0] for x in stats)
+        self.ntasks = sum(x[1] for x in stats)
+        self.nlaunch = stats[0][2]
         self.fL, self.fR = fL, fR
         self.graphs = {}
 
@@ -140,6 +169,13 @@ class SigmaPlan:
         self._run(eng, W, x, y, precision, use_graph)
 
     def _run(self, eng, W, x, y, precision, use_graph):
+        if len(self.pids) > 1:
+            tmp = _torch().empty_like(y)
+            eng.sigma(self.pids[0], self.fL.buf, self.fR.buf, W, x, y, self.workspace, precision)
+            for pid in self.pids[1:]:
+                eng.sigma(pid, self.fL.buf, self.fR.buf, W, x, tmp, self.workspace, precision)
+                y += tmp
+            return
         if not use_graph:
             eng.sigma(self.pid, self.fL.buf, self.fR.buf, W, x, y, self.workspace, precision)
             return
@@ -162,11 +198,23 @@ class SigmaPlan:
         graph.replay()
         y.copy_(ys)
 
+    def hdiag(self, dmrg, d):
+        eng = _engine.get()
+        W = dmrg.mpo_store.buf
+        eng.hdiag(self.pids[0], self.fL.buf, self.fR.buf, W, d)
+        if len(self.pids) > 1:
+            tmp = _torch().empty_like(d)
+            for pid in self.pids[1:]:
+                eng.hdiag(pid, self.fL.buf, self.fR.buf, W, tmp)
+                d += tmp
+
     def release(self):
         self.graphs = {}
         if self.pid is not None:
-            _engine.get().destroy_plan(self.pid)
+            for pid in self.pids:
+                _engine.get().destroy_plan(pid)
             self.pid = None
+            self.pids = []
 
 
 def _sigma_plan(info):
@@ -207,10 +255,10 @@ def HDiag(info, ndim0, prjmap):
     if plan.nmap is not None:
         idx, nN = plan.nmap
         dN = torch.zeros(nN, dtype=torch.float64, device="cuda")
-        _engine.get().hdiag(plan.pid, plan.fL.buf, plan.fR.buf, dmrg.mpo_store.buf, dN)
+        plan.hdiag(dmrg, dN)
         torch.index_select(dN, 0, idx, out=d)
         return d
-    _engine.get().hdiag(plan.pid, plan.fL.buf, plan.fR.buf, dmrg.mpo_store.buf, d)
+    plan.hdiag(dmrg, d)
     return d
 
 
