@@ -216,6 +216,7 @@ def gradient_metrics(K=16, nelec=16, D=256, seed=2024):
     m.loadInts(I.spin_orbital(h, eri))
     m.dumpMPO()
     qnuml, _ = bond_structure(K, nelec, 0.0, D, rng)
+    qnuml[K] = numpy.array([[float(nelec), 0.0]])   # one state at the right end
     fmps = {'nsite': K}
     for i in range(K):
         t = qtensor([False, False, True])

@@ -83,9 +83,9 @@ struct Step {
   SegB *d_segb = nullptr;
   Work *d_work_fp64 = nullptr;   // tiles of kTileFP64
   // tensor-core tiles: [rows 32 / 64 / 128][columns 8 / 16]
-  Work *d_work_tc[3][3] = {};  // [row tile 32/64/128][column tile 8/16/32]
+  Work *d_work_tc[3][4] = {};  // [row tile 32/64/128][column tile 8/16/32/64]
   int64_t nwork_fp64 = 0;
-  int64_t nwork_tc[3][3] = {};
+  int64_t nwork_tc[3][4] = {};
   double flops = 0.0;            // sum of 2*m*n*k of the reference tasks
   int64_t ntasks = 0;
   bool uploaded = false;         // device copies are made on first use

@@ -391,9 +391,11 @@ template <int S, int TM, int TN>
 struct TcShape {
   // k slots per chunk.  A level sums at most S products of at most 255^2 per
   // k, so S = 4 stays exact in FP32 (< 2^24) up to 64 slots and S = 7 up to
-  // 32; 64-slot chunks were measured slower (more registers per thread), so
-  // both use 32.
-  static constexpr int TK = 32;
+  // 32.  The 64-column tiles (16 threads per row of A, 4 slots each) take
+  // 64-slot chunks with S = 4: half the barriers and level folds per k.  The
+  // narrower tiles keep 32 (64 slots there mean more registers per thread,
+  // measured slower).
+  static constexpr int TK = (S == 4 && TN == 64) ? 64 : 32;
   static constexpr int PAD = TK + 8;          // bf16 per plane row in shared memory
   static constexpr int WM = TM / 16, WN = TN / 8;
   static constexpr int NT = 32 * WM * WN;     // threads per CTA
@@ -599,7 +601,9 @@ static int launch_split_all(const Step &s, const Bufs &b, void *stream) {
   if ((rc = launch_tc_t<S, 32, 16>(s.d_work_tc[0][1], s.nwork_tc[0][1], s, b, stream))) return rc;
   if ((rc = launch_tc_t<S, 128, 32>(s.d_work_tc[2][2], s.nwork_tc[2][2], s, b, stream))) return rc;
   if ((rc = launch_tc_t<S, 64, 32>(s.d_work_tc[1][2], s.nwork_tc[1][2], s, b, stream))) return rc;
-  return launch_tc_t<S, 32, 32>(s.d_work_tc[0][2], s.nwork_tc[0][2], s, b, stream);
+  if ((rc = launch_tc_t<S, 32, 32>(s.d_work_tc[0][2], s.nwork_tc[0][2], s, b, stream))) return rc;
+  if ((rc = launch_tc_t<S, 64, 64>(s.d_work_tc[1][3], s.nwork_tc[1][3], s, b, stream))) return rc;
+  return launch_tc_t<S, 32, 64>(s.d_work_tc[0][3], s.nwork_tc[0][3], s, b, stream);
 }
 
 int launch_step_split(const Step &s, const Bufs &b, int nslices, void *stream) {

@@ -785,7 +785,7 @@ static void split_long_groups(Step &st) {
 static int upload_step(Step &st) {
   if (st.uploaded) return ZMPO_OK;
   split_long_groups(st);
-  std::vector<Work> w64, wtc[3][3];
+  std::vector<Work> w64, wtc[3][4];
   // order groups by cost (longest first) for load balance
   std::vector<int> order(st.groups.size());
   std::iota(order.begin(), order.end(), 0);
@@ -800,15 +800,17 @@ static int upload_step(Step &st) {
     const Group &G = st.groups[g];
     for (int mt = 0; mt * kTileFP64M < G.M; ++mt)
       for (int nt = 0; nt * kTileFP64N < G.N; ++nt) w64.push_back({g, mt, nt, 0});
-    const int tni = G.N <= 8 ? 0 : (G.N <= 16 ? 1 : 2), tn = 8 << tni;
-    const int tmi = G.M <= 32 ? 0 : (G.M <= 64 ? 1 : 2), tm = 32 << tmi;
+    const int tni = G.N <= 8 ? 0 : (G.N <= 16 ? 1 : (G.N <= 32 ? 2 : 3)), tn = 8 << tni;
+    int tmi = G.M <= 32 ? 0 : (G.M <= 64 ? 1 : 2);
+    if (tni == 3 && tmi == 2) tmi = 1;  // 64-column tiles: 32 or 64 rows (1024 threads at most)
+    const int tm = 32 << tmi;
     auto &wl = wtc[tmi][tni];
     for (int mt = 0; mt * tm < G.M; ++mt)
       for (int nt = 0; nt * tn < G.N; ++nt) wl.push_back({g, mt, nt, 0});
   }
   st.nwork_fp64 = (int64_t)w64.size();
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) st.nwork_tc[i][j] = (int64_t)wtc[i][j].size();
+    for (int j = 0; j < 4; ++j) st.nwork_tc[i][j] = (int64_t)wtc[i][j].size();
   auto up = [](auto **dptr, const auto &v) -> cudaError_t {
     using T = typename std::remove_reference<decltype(v)>::type::value_type;
     if (v.empty()) {
@@ -825,7 +827,7 @@ static int upload_step(Step &st) {
   CUDA_TRY(up(&st.d_segb, st.segb));
   CUDA_TRY(up(&st.d_work_fp64, w64));
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) CUDA_TRY(up(&st.d_work_tc[i][j], wtc[i][j]));
+    for (int j = 0; j < 4; ++j) CUDA_TRY(up(&st.d_work_tc[i][j], wtc[i][j]));
   CUDA_TRY(up(&st.d_reds, st.reds));
   if (st.part_elems > 0) CUDA_TRY(cudaMalloc((void **)&st.d_part, st.part_elems * sizeof(double)));
   // keep the host mirror of groups (sizes) but free the bulky segment copy
@@ -846,7 +848,7 @@ static void free_step(Step &st) {
   st.d_segb = nullptr;
   cudaFree(st.d_work_fp64);
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 0; j < 4; ++j) {
       cudaFree(st.d_work_tc[i][j]);
       st.d_work_tc[i][j] = nullptr;
     }
@@ -1380,7 +1382,7 @@ int zmpo_plan_kernel_count(zmpo_engine *e, int plan_id, int precision, int *coun
       n += s.nwork_fp64 > 0;
     } else {
       for (int a = 0; a < 3; ++a)
-        for (int c = 0; c < 3; ++c) n += s.nwork_tc[a][c] > 0;
+        for (int c = 0; c < 4; ++c) n += s.nwork_tc[a][c] > 0;
     }
     n += s.red_elems > 0;
   }
