@@ -257,6 +257,32 @@ __device__ __forceinline__ float pow2f(int k) {
   return 0.f;
 }
 
+// hi + lo (two floats) as a double with integer operations only: both become
+// signed fixed-point numbers on the larger exponent (29 guard bits), are added
+// in 64 bits and the sum is normalised into the double's fields (bits below
+// the 53rd are truncated).  The FP64 pipe, narrow on GB300, is not used.
+__device__ __forceinline__ double two_float_to_double(float hi, float lo) {
+  const uint32_t bh = __float_as_uint(hi), bl = __float_as_uint(lo);
+  int eh = (int)((bh >> 23) & 0xffu), el = (int)((bl >> 23) & 0xffu);
+  long long mh = (long long)((bh & 0x7fffffu) | (eh ? 0x800000u : 0u));
+  long long ml = (long long)((bl & 0x7fffffu) | (el ? 0x800000u : 0u));
+  eh = eh ? eh : 1;  // subnormal floats: exponent 1 without the leading bit
+  el = el ? el : 1;
+  if (bh >> 31) mh = -mh;
+  if (bl >> 31) ml = -ml;
+  const int E = max(eh, el);
+  const int dh = min(E - eh, 63), dl = min(E - el, 63);
+  const long long S = ((mh << 29) >> dh) + ((ml << 29) >> dl);  // value S * 2^(E - 150 - 29)
+  if (S == 0) return 0.0;
+  const unsigned long long sign = S < 0 ? 0x8000000000000000ull : 0ull;
+  const unsigned long long A = (unsigned long long)(S < 0 ? -S : S);
+  const int n = 63 - __clzll((long long)A);  // position of the leading bit (<= 53)
+  const unsigned long long mant = n >= 52 ? (A >> (n - 52)) : (A << (52 - n));
+  const long long ebits = (long long)(E - 150 - 29 + n + 1023);  // always a normal double here
+  return __longlong_as_double((long long)(sign | ((unsigned long long)ebits << 52) |
+                                          (mant & 0xfffffffffffffull)));
+}
+
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
   s = a + b;
   const float z = s - a;
@@ -566,7 +592,7 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
     for (int i = 0; i < 4; ++i) {
       const int r = m0 + wm + gq + (i >> 1) * 8;
       const int c = n0 + wn + 2 * tq + (i & 1);
-      if (r < g.M && c < g.N) store_c(bufs, cbl, g, r, c, n0, cbj, cbrel, (double)hi[i] + (double)lo[i]);
+      if (r < g.M && c < g.N) store_c(bufs, cbl, g, r, c, n0, cbj, cbrel, two_float_to_double(hi[i], lo[i]));
     }
     __syncthreads();  // the column map is rewritten by the next tile
   }
