@@ -33,6 +33,9 @@ MEDIUM = dict(K=16, nelec=16, D=256, isite=7, seed=2024)
 # the large batched configuration (hopping 0.7), run with a workspace budget
 LARGE = dict(K=36, nelec=36, D=1024, isite=17, seed=2024, hop=0.7)
 LARGE_WORKSPACE = 64e9
+# the spin-projected configuration: singlet projection with 8 Gauss-Legendre
+# points (320 terms [p, g]), H.psi with the N-only relabelling
+SPCFG = dict(K=20, nelec=20, D=512, isite=9, seed=2024, npts=8, sval=0.0)
 # DRAM bytes (read + write) over algorithmic bytes of the T3 step, measured
 # with ncu (dram__bytes_read.sum + dram__bytes_write.sum of every launch in
 # the step's NVTX range) on the K=16, D=256 two-site dot: 1.896 GB against
@@ -98,10 +101,10 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def build_problem(with_oracle=False, small=False, medium=False, large=False):
+def build_problem(with_oracle=False, small=False, medium=False, large=False, sp=False):
     from tests.problems import random_problem
     t0 = time.perf_counter()
-    cfg = SMALL if small else (MEDIUM if medium else (LARGE if large else WORKLOAD))
+    cfg = SMALL if small else (MEDIUM if medium else (LARGE if large else (SPCFG if sp else WORKLOAD)))
     P = random_problem(device=True, with_oracle=with_oracle, **cfg)
     return P, time.perf_counter() - t0
 
@@ -178,6 +181,7 @@ def sweep_metrics(K=10, nelec=10, D=64, nsweep=10, seed=2024):
         m.occun = I.closed_shell_occun(K, nelec)
         m.qsectors = {str([float(nelec), 0.0]): 1}
         m.precision = prec
+        m.precision_renorm = "emu64" if prec == "split" else "fp64"
         m.use_graph = True
         m.partition()
         m.loadInts((i1, i2))
@@ -248,6 +252,74 @@ def gradient_metrics(K=16, nelec=16, D=256, seed=2024):
             "fd_directional": fd, "adjoint_directional": an, "abs_diff": abs(fd - an)}
 
 
+def sweep_large(K=24, nelec=24, D=512, seed=2024):
+    """One right-to-left two-site sweep (K-1 dots) at K=24, 24 electrons,
+    D=512 from the same seeded random left-canonical MPS, FP64 vs split
+    (schedule: D=512, Davidson crit_e 1e-9, no noise): seconds, matvecs and
+    the energies reached."""
+    import torch
+    from tests.problems import bond_structure, random_left_site, QPHYS
+    from zmpo_dmrg_gb300 import integrals as I
+    from zmpo_dmrg_gb300.mpo_dmrg_class import mpo_dmrg
+    from zmpo_dmrg_gb300.mpo_dmrg_schedule import schedule
+    from zmpo_dmrg_gb300.qtensor import qtensor
+    h, eri, _ = I.synthetic(K, seed)
+    ints = I.spin_orbital(h, eri)
+    out = {"workload": "K=%d N=%d Sz=0 D=%d, one right-to-left two-site sweep (%d dots) from a seeded random "
+                       "left-canonical MPS, Davidson crit_e 1e-9, no noise" % (K, nelec, D, K - 1)}
+    for prec in ("split", "fp64"):
+        rng = numpy.random.default_rng(seed)
+        qnuml, _ = bond_structure(K, nelec, 0.0, D, rng)
+        qnuml[K] = numpy.array([[float(nelec), 0.0]])
+        m = mpo_dmrg(seed=1)
+        m.nsite, m.sbas, m.isym = K, 2 * K, 2
+        m.build()
+        m.qsectors = {str([float(nelec), 0.0]): 1}
+        m.initStates()
+        m.precision = prec
+        # the split configuration renormalises with the 7-slice emulation
+        # (~2^-56 relative), the FP64 configuration with FP64
+        m.precision_renorm = "emu64" if prec == "split" else "fp64"
+        m.partition()
+        m.loadInts(ints)
+        m.dumpMPO()
+        fmps = {'nsite': K}
+        for i in range(K):
+            t = qtensor([False, False, True])
+            t.fromDenseTensor(random_left_site(qnuml[i], qnuml[i + 1], rng), [qnuml[i], QPHYS, qnuml[i + 1]])
+            fmps['site%d' % i] = t
+        for i in range(K + 1):
+            fmps['qnum%d' % i] = qnuml[i]
+        m.flmps = {'nsite': K, 'qnum0': qnuml[0]}
+        m.frmps = {'nsite': K, 'qnum%d' % K: m.qnumr[-1]}
+        m.qnuml = [numpy.asarray(fmps['qnum%d' % i]) for i in range(K + 1)]
+        m.flmps.update(fmps)
+        m.initOps(fmps)
+        m.psi0 = None
+        sc = schedule(maxM=D, tol=1e-9, maxiter=1)
+        sc.fixed(ncsite=2, maxM=D, tol=1e-9, maxiter=1, noise=0.0)
+        sc.getParameters(m, 0)
+        m.crit_e = 1e-9
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = m.sweep(list(range(K)), 2, 'R')
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        tdav = sum(x[2] for x in m.timings)
+        tren = sum(x[3] for x in m.timings)
+        out[prec] = {"s_per_half_sweep": dt, "s_local_solver": tdav, "s_renorm": tren, "matvecs": int(r[0]),
+                     "energy": float(r[2]), "energy_first_dot": float(numpy.asarray(r[4][0]).ravel()[0])}
+        del m
+        torch.cuda.empty_cache()
+    out["dE_split_fp64"] = abs(out["split"]["energy"] - out["fp64"]["energy"])
+    # the first dot sees identical environments in both runs: its energy
+    # difference is the precision effect alone; later dots inherit different
+    # truncations of a far-from-converged random state
+    out["dE_first_dot"] = abs(out["split"]["energy_first_dot"] - out["fp64"]["energy_first_dot"])
+    out["speedup_split_vs_fp64"] = out["fp64"]["s_per_half_sweep"] / out["split"]["s_per_half_sweep"]
+    return out
+
+
 def cpu_threads():
     return os.cpu_count() or 1
 
@@ -288,8 +360,12 @@ def main():
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--small", action="store_true", help="K=12, D=128 case (profiling)")
     ap.add_argument("--medium", action="store_true", help="K=16, D=256 case (profiling)")
+    ap.add_argument("--sweep-large", action="store_true",
+                    help="also time one two-site sweep at K=24, D=512 (split vs FP64)")
     ap.add_argument("--gradient", action="store_true",
                     help="also time the energy gradient at K=16, D=256 (adjoint configuration)")
+    ap.add_argument("--sp", action="store_true",
+                    help="spin-projected H.psi, K=20, D=512, 8 quadrature points (terms in batches)")
     ap.add_argument("--large", action="store_true",
                     help="K=36, D=1024, hopping 0.7 (terms in batches under a 64 GB workspace)")
     args = ap.parse_args()
@@ -309,9 +385,9 @@ def main():
     from zmpo_dmrg_gb300 import engine as E
     from zmpo_dmrg_gb300.mpo_dmrg_kernel import HVec, _sigma_plan
 
-    P, t_build = build_problem(small=args.small, medium=args.medium, large=args.large)
+    P, t_build = build_problem(small=args.small, medium=args.medium, large=args.large, sp=args.sp)
     pm = P.p
-    if args.large:
+    if args.large or args.sp:
         pm.workspace_budget = LARGE_WORKSPACE
         pm._sigma_plan = None
     info = [pm, P.isite, 2, pm.flst, 'L', True]
@@ -407,8 +483,10 @@ def main():
         "warmup": max(args.warmup, 3), "ms_per_step": tmax * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 (bf16 digit slices, fp32 accumulate)",
         "data": "synthetic (seeded integrals + seeded random block-sparse MPS)",
-        "config": {"workload": "two-site H.psi, K=%d N=%d Sz=0 D=%d, %d terms, (N,Sz) blocks" %
-                               (P.K, P.nelec, P.D, pm.nops),
+        "config": {"workload": ("two-site H.psi, K=%d N=%d Sz=0 D=%d, %d terms, (N,Sz) blocks" %
+                                (P.K, P.nelec, P.D, pm.nops)) +
+                               (", spin-projected S=0 with %d quadrature points (N-only terms)" % pm.npts
+                                if pm.ifs2proj else ""),
                    "ndim0": n, "F_ref_flops": flops, "tasks": plan.ntasks, "precision": args.precision,
                    "term_batches": len(plan.pids),
                    "l2": "inputs larger than L2 (environments %.2f GB)" % ((L.numel() + R.numel()) * 8 / 1e9),
@@ -433,6 +511,8 @@ def main():
         result["sweep"] = sweep_metrics()
     if rank == 0 and args.gradient:
         result["gradient"] = gradient_metrics()
+    if rank == 0 and args.sweep_large:
+        result["sweep_large"] = sweep_large()
     if rank == 0 and not args.no_cpu:
         fl, dt, ch = oracle_sample(P)
         result["cpu_baseline"] = {"value": fl / dt / 1e12, "unit": "TFLOP/s", "cores": cpu_threads(),

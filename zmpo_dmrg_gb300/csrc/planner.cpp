@@ -20,6 +20,7 @@
 #include <numeric>
 #include <string>
 #include <unordered_map>
+#include <thread>
 #include <vector>
 
 #include <nvtx3/nvToolsExt.h>
@@ -1108,6 +1109,28 @@ int zmpo_contract_exec(zmpo_engine *e, int plan_id, const double *d_a, const dou
   return run_step(P->steps[0], b, precision, stream);
 }
 
+// The steps of a chain have independent task lists: their GEMM mappings are
+// built on one host thread per step (error text is per thread, so it is
+// carried back to the caller's thread).
+static int build_steps_parallel(Plan *P, std::vector<std::vector<OutWork>> &step_works) {
+  const int nstep = (int)step_works.size();
+  P->steps.resize(nstep);
+  std::vector<int> rcs(nstep, ZMPO_OK);
+  std::vector<std::string> msgs(nstep);
+  std::vector<std::thread> pool;
+  for (int s = 0; s < nstep; ++s) {
+    P->steps[s].idx = s;
+    pool.emplace_back([&, s]() {
+      rcs[s] = build_step(step_works[s], P->steps[s]);
+      if (rcs[s]) msgs[s] = g_err;
+    });
+  }
+  for (auto &t : pool) t.join();
+  for (int s = 0; s < nstep; ++s)
+    if (rcs[s]) return fail(rcs[s], msgs[s]);
+  return ZMPO_OK;
+}
+
 int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
   if (!e || !d || !plan_id || d->nop < 0 || d->nclass < 1 || (d->ncsite != 1 && d->ncsite != 2))
     return fail(ZMPO_E_ARG, "sigma_plan: bad descriptor");
@@ -1195,9 +1218,12 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
   }
   P->ws_elems = ws;
   // buffers: 0 L, 1 R, 2 W, 3 x, 4 y, 5 workspace
-  // operand sources per executed step (two-site: O, T1, T3, sigma)
+  // operand sources per executed step (two-site: O, T1, T3, sigma).  The
+  // steps' task lists are independent: their output works are collected
+  // first and the GEMM mappings built on one host thread per step.
+  std::vector<std::vector<OutWork>> step_works(nstep);
   for (int s = 0; s < nstep; ++s) {
-    std::vector<OutWork> works;
+    std::vector<OutWork> &works = step_works[s];
     auto src = [&](int op, bool isA, int &buf, int64_t &base) {
       if (d->ncsite == 2) {
         switch (s) {
@@ -1229,8 +1255,11 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
           w.ob = (int32_t)ob;
           w.c_base = ws_off[op][s];
           w.cbuf = 5;
+          // the term weight goes on the per-term MPO product O = w Wi.Wj
+          // (two-site), so the sum over terms reads unscaled operands
+          const double wgt = (d->ncsite == 2 && s == 0) ? d->wts[op] : 1.0;
           for (int64_t t = C->task_start[ob]; t < C->task_start[ob + 1]; ++t)
-            w.tasks.push_back({C, A, B, O, C->tasks[t].ab, C->tasks[t].bb, abase, bbase, abuf, bbuf, 1.0});
+            w.tasks.push_back({C, A, B, O, C->tasks[t].ab, C->tasks[t].bb, abase, bbase, abuf, bbuf, wgt});
           works.push_back(std::move(w));
         }
       }
@@ -1255,15 +1284,17 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
         for (size_t ob = 0; ob < O->pk->flat.size(); ++ob)
           for (int64_t t = C->task_start[ob]; t < C->task_start[ob + 1]; ++t)
             works[ob].tasks.push_back({C, A, B, O, C->tasks[t].ab, C->tasks[t].bb, abase, bbase, abuf,
-                                       bbuf, d->wts[op]});
+                                       bbuf, d->ncsite == 2 ? 1.0 : d->wts[op]});
       }
     }
-    P->steps.emplace_back();
-    P->steps.back().idx = (int)P->steps.size() - 1;
-    int rc = build_step(works, P->steps.back());
+  }
+  {
+    int rc = build_steps_parallel(P.get(), step_works);
     if (rc) return rc;
-    P->exec_flops += P->steps.back().flops;
-    P->ntasks += P->steps.back().ntasks;
+    for (auto &st : P->steps) {
+      P->exec_flops += st.flops;
+      P->ntasks += st.ntasks;
+    }
   }
   // ---- HDiag terms: out[l,r] += w * sum Ld[a,l] Wi[a,b] (Wj[b,c]) Rd[c,r]
   {
@@ -1496,8 +1527,9 @@ int zmpo_renorm_plan(zmpo_engine *e, const zmpo_renorm_desc *d, int *plan_id) {
   P->out_total = tot;
   P->ws_elems = ws;
   // buffers: 0 env, 2 W, 3 site, 4 out, 5 workspace
+  std::vector<std::vector<OutWork>> step_works(3);
   for (int s = 0; s < 3; ++s) {
-    std::vector<OutWork> works;
+    std::vector<OutWork> &works = step_works[s];
     for (int op = 0; op < d->nop; ++op) {
       int c = d->op_class[op];
       if (P->out_lay[c] < 0) continue;
@@ -1525,12 +1557,14 @@ int zmpo_renorm_plan(zmpo_engine *e, const zmpo_renorm_desc *d, int *plan_id) {
         works.push_back(std::move(w));
       }
     }
-    P->steps.emplace_back();
-    P->steps.back().idx = (int)P->steps.size() - 1;
-    int rc = build_step(works, P->steps.back());
+  }
+  {
+    int rc = build_steps_parallel(P.get(), step_works);
     if (rc) return rc;
-    P->flops += P->steps.back().flops;
-    P->ntasks += P->steps.back().ntasks;
+    for (auto &st : P->steps) {
+      P->flops += st.flops;
+      P->ntasks += st.ntasks;
+    }
   }
   e->plans.push_back(std::move(P));
   *plan_id = (int)e->plans.size() - 1;
