@@ -209,6 +209,15 @@ static int add_layout(zmpo_engine *e, std::unique_ptr<Layout> L) {
   return (int)e->layouts.size() - 1;
 }
 
+// A plan keeps only its task lists: the symbolic contractions and the
+// intermediate layouts made while building it are dropped afterwards (layout
+// ids handed to the caller are kept), so long sweeps do not accumulate them.
+static void drop_internal(zmpo_engine *e, size_t c0, size_t l0, const std::vector<int> &keep) {
+  for (size_t i = c0; i < e->contractions.size(); ++i) e->contractions[i].reset();
+  for (size_t i = l0; i < e->layouts.size(); ++i)
+    if (std::find(keep.begin(), keep.end(), (int)i) == keep.end()) e->layouts[i].reset();
+}
+
 static bool same_q(const Layout &A, int la, const Layout &B, int lb) {
   if (A.nsec[la] != B.nsec[lb] || A.nq != B.nq) return false;
   for (size_t i = 0; i < A.q[la].size(); ++i)
@@ -494,7 +503,15 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
   st.groups.clear();
   {
     // algorithmic traffic: every distinct operand tensor once, every output block once
-    std::map<std::tuple<int, int64_t, const Layout *>, int64_t> seen;
+    struct Operand {
+      const Layout *l;
+      int64_t base;
+      int buf;
+      bool operator<(const Operand &o) const { return std::tie(l, base, buf) < std::tie(o.l, o.base, o.buf); }
+      bool operator==(const Operand &o) const { return l == o.l && base == o.base && buf == o.buf; }
+    };
+    std::vector<Operand> seen;
+    Operand lastA{nullptr, -1, -1}, lastB{nullptr, -1, -1};
     double out_elems = 0.0;
     for (auto &w : works) {
       int64_t od[16];
@@ -503,12 +520,17 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
       for (int j = 0; j < w.lo->rank; ++j) n *= (double)od[j];
       out_elems += n;
       for (auto &t : w.tasks) {
-        seen[std::make_tuple(t.abuf, t.a_base, t.la)] = t.la->pk->size;
-        seen[std::make_tuple(t.bbuf, t.b_base, t.lb)] = t.lb->pk->size;
+        const Operand a{t.la, t.a_base, t.abuf}, b{t.lb, t.b_base, t.bbuf};
+        // consecutive tasks mostly read the same tensors: skip repeats early
+        // (the sort below removes the rest)
+        if (!(a == lastA)) seen.push_back(lastA = a);
+        if (!(b == lastB)) seen.push_back(lastB = b);
       }
     }
+    std::sort(seen.begin(), seen.end());
+    seen.erase(std::unique(seen.begin(), seen.end()), seen.end());
     double in_elems = 0.0;
-    for (auto &kv : seen) in_elems += (double)kv.second;
+    for (auto &o : seen) in_elems += (double)o.l->pk->size;
     st.alg_bytes = 8.0 * (in_elems + out_elems);
   }
   std::vector<MergeInfo> minfo;
@@ -595,11 +617,17 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
       int sec[16];
       O.sectors(O.pk->flat[w.ob], sec);
       const auto &t0 = w.tasks[0];
-      char buf[64];
-      snprintf(buf, sizeof(buf), "%p|%p|%d|%d|%lld|%lld|", (const void *)w.lo, (const void *)t0.la, t0.abuf,
-               w.cbuf, (long long)t0.a_base, (long long)M);
-      mi.key = buf;
-      for (int j = 0; j < ne1; ++j) mi.key += std::to_string(sec[j]) + ",";
+      // binary key: output layout, A tensor (layout, buffer, base), output
+      // buffer, M and the row-leg sectors
+      int64_t kw[8 + 16];
+      kw[0] = (int64_t)(intptr_t)w.lo;
+      kw[1] = (int64_t)(intptr_t)t0.la;
+      kw[2] = t0.abuf;
+      kw[3] = w.cbuf;
+      kw[4] = t0.a_base;
+      kw[5] = M;
+      for (int j = 0; j < ne1; ++j) kw[6 + j] = sec[j];
+      mi.key.assign(reinterpret_cast<const char *>(kw), (size_t)(6 + ne1) * sizeof(int64_t));
       for (auto &t : w.tasks)
         if (t.la != t0.la || t.abuf != t0.abuf || t.a_base != t0.a_base) mi.ok = false;
     }
@@ -657,24 +685,38 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
         int64_t sam = pm >= 0 ? as[e1[innermost(mr[pm])]] : 0;
         int64_t sbn = pn >= 0 ? bs[e2[innermost(nr[pn]) - ne1]] : 0;
         // K legs: sort by A stride (descending), merge where contiguous in both
-        std::vector<Leg2> kl;
-        for (size_t k = 0; k < i1.size(); ++k) kl.push_back({ad[i1[k]], as[i1[k]], bs[i2[k]]});
-        std::sort(kl.begin(), kl.end(), [](const Leg2 &x, const Leg2 &y) { return x.s0 > y.s0; });
-        kl = merge_legs(kl);
+        // (fixed-size arrays: this runs once per block task)
+        Leg2 kraw[16], kl[16], kloops[16];
+        int nraw = 0, nkl = 0, nkloop = 0;
+        for (size_t k = 0; k < i1.size(); ++k) kraw[nraw++] = {ad[i1[k]], as[i1[k]], bs[i2[k]]};
+        std::sort(kraw, kraw + nraw, [](const Leg2 &x, const Leg2 &y) { return x.s0 > y.s0; });
+        for (int i = 0; i < nraw; ++i) {
+          const Leg2 &l = kraw[i];
+          if (l.d == 1) continue;
+          if (nkl > 0) {
+            Leg2 &o = kl[nkl - 1];
+            if (o.s0 == l.d * l.s0 && o.s1 == l.d * l.s1) {
+              o.d *= l.d;
+              o.s0 = l.s0;
+              o.s1 = l.s1;
+              continue;
+            }
+          }
+          kl[nkl++] = l;
+        }
         int pk = -1;
-        for (int i = 0; i < (int)kl.size(); ++i)
+        for (int i = 0; i < nkl; ++i)
           if (pk < 0 || kl[i].d > kl[pk].d) pk = i;
         int64_t K = pk >= 0 ? kl[pk].d : 1;
         int64_t sak = pk >= 0 ? kl[pk].s0 : 0, sbk = pk >= 0 ? kl[pk].s1 : 0;
-        std::vector<Leg2> kloops;
-        for (int i = 0; i < (int)kl.size(); ++i)
-          if (i != pk) kloops.push_back(kl[i]);
+        for (int i = 0; i < nkl; ++i)
+          if (i != pk) kloops[nkloop++] = kl[i];
         int64_t nk = 1;
-        for (auto &l : kloops) nk *= l.d;
+        for (int i = 0; i < nkloop; ++i) nk *= kloops[i].d;
         if (nk != 1) mi.ok = false;
         for (int64_t ki = 0; ki < nk; ++ki) {
           int64_t aa = a0, bb = b0, tt = ki;
-          for (int i = (int)kloops.size() - 1; i >= 0; --i) {
+          for (int i = nkloop - 1; i >= 0; --i) {
             int64_t x = tt % kloops[i].d;
             tt /= kloops[i].d;
             aa += x * kloops[i].s0;
@@ -1069,6 +1111,7 @@ int zmpo_contract_plan(zmpo_engine *e, int lay_a, int lay_b, int naxes, const in
   if (!e || !lay_out || !plan_id || naxes < 0 || (naxes > 0 && (!axes_a || !axes_b)))
     return fail(ZMPO_E_ARG, "contract_plan: bad arguments");
   int lo, ci;
+  const size_t c0 = e->contractions.size(), l0 = e->layouts.size();
   int rc = build_contraction(e, lay_a, lay_b, naxes, axes_a, axes_b, &lo, &ci);
   if (rc) return rc;
   auto P = std::make_unique<Plan>();
@@ -1093,6 +1136,7 @@ int zmpo_contract_plan(zmpo_engine *e, int lay_a, int lay_b, int naxes, const in
   P->flops = P->steps.back().flops;
   P->ntasks = P->steps.back().ntasks;
   e->plans.push_back(std::move(P));
+  drop_internal(e, c0, l0, {lo});
   *lay_out = lo;
   *plan_id = (int)e->plans.size() - 1;
   return ZMPO_OK;
@@ -1136,6 +1180,7 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
     return fail(ZMPO_E_ARG, "sigma_plan: bad descriptor");
   const Layout *Psi = get_layout(e, d->lay_psi);
   if (!Psi) return fail(ZMPO_E_ID, "sigma_plan: unknown psi layout");
+  const size_t c0 = e->contractions.size(), l0 = e->layouts.size();
   // Per-class symbolic chains (the reference caches the same per icase0,
   // mpo_dmrg_kernelQt.py:199-204).  The reference's two-site chain is
   //   T1 = L.psi, T2 = T1.Wi, T3 = T2.Wj, sigma = T3.R   (kernelQt.py:270-306)
@@ -1381,6 +1426,7 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
     }
   }
   e->plans.push_back(std::move(P));
+  drop_internal(e, c0, l0, {});
   *plan_id = (int)e->plans.size() - 1;
   return ZMPO_OK;
 }
@@ -1470,6 +1516,7 @@ int zmpo_hdiag(zmpo_engine *e, int plan_id, const double *d_L, const double *d_R
 int zmpo_renorm_plan(zmpo_engine *e, const zmpo_renorm_desc *d, int *plan_id) {
   if (!e || !d || !plan_id || d->nop < 0 || d->nclass < 1 || (d->status != 0 && d->status != 1))
     return fail(ZMPO_E_ARG, "renorm_plan: bad descriptor");
+  const size_t c0 = e->contractions.size(), l0 = e->layouts.size();
   // reference chains (mpo_dmrg_kernelQt.py:665-667 for 'L', 727-729 for 'R')
   static const int La1[1] = {0}, Lb1[1] = {1};
   static const int La2[2] = {0, 2}, Lb2[2] = {2, 0};
@@ -1567,6 +1614,12 @@ int zmpo_renorm_plan(zmpo_engine *e, const zmpo_renorm_desc *d, int *plan_id) {
     }
   }
   e->plans.push_back(std::move(P));
+  {
+    std::vector<int> keep;  // the output layouts go back to the caller
+    for (int c = 0; c < d->nclass; ++c)
+      if (ch[c].built) keep.push_back(ch[c].l3);
+    drop_internal(e, c0, l0, keep);
+  }
   *plan_id = (int)e->plans.size() - 1;
   return ZMPO_OK;
 }
