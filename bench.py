@@ -20,6 +20,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy
@@ -61,7 +62,9 @@ class Clocks:
 
     def __init__(self):
         self.p = None
-        self.path = os.path.join(HERE, "gpurun_out", "clocks_bench.csv")
+        # raw samples; the summary goes into the JSON line
+        self.path = os.environ.get("ZMPO_CLOCKS_CSV",
+                                   os.path.join(tempfile.gettempdir(), "zmpo_clocks_bench.csv"))
 
     def start(self):
         try:

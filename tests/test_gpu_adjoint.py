@@ -123,3 +123,17 @@ def test_gradient_matches_fci_energy_differences(converged):
     fd = (efci(h + eps * dh, eri + eps * dg) - efci(h - eps * dh, eri - eps * dg)) / (2 * eps)
     an = float((converged["dh"] * dh).sum() + (converged["dg"] * dg).sum())
     assert abs(fd - an) < 1e-7 * max(1.0, abs(an))
+
+
+def test_rdm12_properties(converged):
+    """The property routine returns the FCI state's 1- and 2-particle
+    densities (the reference's eval_rdm1BF / genMPO_Apqrs quantities)."""
+    from zmpo_dmrg_gb300 import properties, adjoint
+    import torch
+    m, h, eri = converged["m"], converged["h"], converged["eri"]
+    adjoint.energy(torch.tensor(h), torch.tensor(eri), m)   # MPO of these integrals
+    g1, g2 = properties.rdm12(m, h, eri)
+    _, one, two = _fci_rdms(converged["i1"], converged["gphys"], 6, 0.0)
+    assert abs(g1.trace() - 6.0) < 1e-9
+    assert numpy.abs(g1 - one).max() < 1e-8
+    assert numpy.abs(g2 - two).max() < 1e-8
