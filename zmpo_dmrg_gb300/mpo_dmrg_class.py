@@ -456,7 +456,7 @@ class mpo_dmrg:
             dwts, qred, rotL, sigs = rdm_blkdiag(rdm1, classes, self.thresh, Dcut)
             nres = len(qred)
             site = rotL.reshape(ldim, dim, nres).copy()
-            srotR = numpy.einsum('ia,eij->eaj', rotL, mats).reshape(neig, nres, cdimc, rdim)
+            srotR = numpy.matmul(rotL.T, mats).reshape(neig, nres, cdimc, rdim)
         else:
             jsite = isite + ncsite - 1
             if self.Dcut is not None:
@@ -465,7 +465,7 @@ class mpo_dmrg:
             dwts, qred, rotL, sigs = rdm_blkdiag(rdm1, classes, self.thresh, Dcut)
             nres = len(qred)
             site = rotL.reshape(dim, rdim, nres).transpose(2, 0, 1).copy()
-            srotR = numpy.einsum('eij,ja->eia', mats, rotL).reshape(neig, ldim, cdimc, nres)
+            srotR = numpy.matmul(mats, rotL).reshape(neig, ldim, cdimc, nres)
         return sigs, dwts, qred, site, srotR
 
     def genGuess(self, isite, ncsite, actlst, civecs, srotR, status):

@@ -51,12 +51,14 @@ def pRDM(civecs, info):
     dmrg, isite, ncsite, flst, status, ifsym = info
     torch = _torch()
     neig, diml, dimc, dimr = civecs.shape
+    # sum_e C_e C_e^T as one BLAS product (the states side by side)
     if status == 'L':
         mats = civecs.reshape(neig, diml * dimc, dimr)
-        rho = numpy.einsum('eij,ekj->ik', mats, mats)
+        cat = mats.transpose(1, 0, 2).reshape(diml * dimc, neig * dimr)
+        rho = cat @ cat.T
     else:
-        mats = civecs.reshape(neig, diml, dimc * dimr)
-        rho = numpy.einsum('eji,ejk->ik', mats, mats)
+        mats = civecs.reshape(neig * diml, dimc * dimr)
+        rho = mats.T @ mats
     if not (dmrg.inoise == 0 and dmrg.noise >= 1.e-10):
         return rho
     if ncsite != 2:
@@ -85,6 +87,15 @@ def pRDM(civecs, info):
         lay_psi, nmap = psiN.layout, (idx, psiN.size_allowed)
     mpo = dmrg.mpo_store
     from .mpo import op_class
+    # the packed wavefunction of every state, on the device once
+    xs = []
+    for e in range(neig):
+        psi.fromDense(civecs[e], idlst)
+        xv = psi.value
+        if nmap is not None:
+            xv = numpy.zeros(nmap[1])
+            xv[nmap[0]] = psi.value
+        xs.append(torch.from_numpy(numpy.ascontiguousarray(xv)).cuda())
     chains = {}
     acc = None
     for iop in range(dmrg.nops):
@@ -109,15 +120,9 @@ def pRDM(civecs, info):
         n_env = env.tensors[iop].size_allowed
         e_view = env.buf.narrow(0, int(env.off[iop]), n_env)
         w_view = mpo.buf.narrow(0, int(mpo.off[jsite][iop]), mpo.tensors[jsite][iop].size_allowed)
-        for e in range(neig):
-            psi.fromDense(civecs[e], idlst)
-            xv = psi.value
-            if nmap is not None:
-                xv = numpy.zeros(nmap[1])
-                xv[nmap[0]] = psi.value
-            x = torch.from_numpy(xv).cuda()
-            t1 = torch.empty(max(ch.sizes[0], 1), dtype=torch.float64, device="cuda")
-            t2 = torch.empty(max(ch.sizes[1], 1), dtype=torch.float64, device="cuda")
+        t1 = torch.empty(max(ch.sizes[0], 1), dtype=torch.float64, device="cuda")
+        t2 = torch.empty(max(ch.sizes[1], 1), dtype=torch.float64, device="cuda")
+        for x in xs:
             if status == 'L':
                 eng.contract_exec(ch.p1, e_view, x, t1)
                 eng.contract_exec(ch.p2, t1, w_view, t2)
