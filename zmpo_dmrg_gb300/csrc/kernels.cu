@@ -337,17 +337,19 @@ __device__ __forceinline__ double load_b_cb(const Slot &sl, const SegB *__restri
 }
 
 
-// Slot table of the next chunk, built by warp 0: lane l looks at segment
-// cur+l; an inclusive warp scan of the slots each segment can still provide
-// places every segment's k range inside the 32 slots.  cursor[0] = next
-// segment, cursor[1] = k offset inside it; *nslot = slots filled (0 = done).
-template <int TK>
-__device__ __forceinline__ void build_slots(const Group &g, const Seg *__restrict__ segs,
-                                            const Bufs &bufs, Slot *slots, int *cursor,
-                                            int *nslot, int lane) {
+// Slot tables of up to NCH chunks in one pass of warp 0 (lane l looks at
+// segment cur+l; the inclusive scan places every segment's k range in the
+// slot sequence, chunk c holding slots [c*TK, (c+1)*TK)).  A chunk may be
+// shorter than TK (end of the 32 segments a pass sees): sums are unchanged.
+// nslot[c] = slots of chunk c; *nchunk = chunks filled (0 = done).
+template <int TK, int NCH>
+__device__ __forceinline__ void build_slots_multi(const Group &g, const Seg *__restrict__ segs,
+                                                  const Bufs &bufs, Slot *slots, int *cursor,
+                                                  int *nslot, int *nchunk, int lane) {
+  constexpr int CAP = TK * NCH;
   const int cur = cursor[0], curk = cursor[1];
   if (cur >= g.nseg) {
-    if (lane == 0) *nslot = 0;
+    if (lane == 0) *nchunk = 0;
     return;
   }
   const int sidx = cur + lane;
@@ -364,40 +366,40 @@ __device__ __forceinline__ void build_slots(const Group &g, const Seg *__restric
     if (lane >= o) incl += t;
   }
   const int excl = incl - avail;
-  if (avail > 0 && excl < TK) {
+  if (avail > 0 && excl < CAP) {
     const double *A = bufs.p[sg.abuf] + sg.a_off;
     const double *B = g.ncb ? bufs.p[sg.bbuf] : bufs.p[sg.bbuf] + sg.b_off;
     const int k0 = lane == 0 ? curk : 0;
-    const int jend = min(incl, TK);
+    const int jend = min(incl, CAP);
     for (int j = excl; j < jend; ++j) {
       const int kk = k0 + (j - excl);
-      slots[j].a = A + (int64_t)kk * sg.sak;
-      slots[j].b = g.ncb ? B : B + (int64_t)kk * sg.sbk;
-      slots[j].sam = sg.sam;
-      slots[j].sbn = sg.sbn;
-      slots[j].alpha = sg.alpha;
-      slots[j].scaled = sg.alpha != 1.0;
-      slots[j].seg = sidx;
-      slots[j].kk = kk;
+      Slot &sl = slots[j];
+      sl.a = A + (int64_t)kk * sg.sak;
+      sl.b = g.ncb ? B : B + (int64_t)kk * sg.sbk;
+      sl.sam = sg.sam;
+      sl.sbn = sg.sbn;
+      sl.alpha = sg.alpha;
+      sl.scaled = sg.alpha != 1.0;
+      sl.seg = sidx;
+      sl.kk = kk;
     }
   }
-  // where the chunk ends: first lane whose inclusive sum reaches 32
-  const unsigned reach = __ballot_sync(0xffffffffu, incl >= TK && avail > 0);
+  const unsigned reach = __ballot_sync(0xffffffffu, incl >= CAP && avail > 0);
   const int total = __shfl_sync(0xffffffffu, incl, 31);
   const int lstop = reach ? (__ffs(reach) - 1) : -1;
   const int stop_incl = __shfl_sync(0xffffffffu, incl, lstop < 0 ? 31 : lstop);
   const int stop_excl = __shfl_sync(0xffffffffu, excl, lstop < 0 ? 31 : lstop);
   if (lane == 0) {
-    if (lstop < 0) {  // every remaining segment fits (or the 32 lanes ran out)
-      const int nseen = min(32, g.nseg - cur);
-      *nslot = min(total, TK);
-      cursor[0] = cur + nseen;
+    int filled;
+    if (lstop < 0) {  // every segment the lanes saw fits
+      filled = min(total, CAP);
+      cursor[0] = cur + min(32, g.nseg - cur);
       cursor[1] = 0;
     } else {
-      *nslot = TK;
-      const int used = TK - stop_excl;  // slots taken from segment cur+lstop
+      filled = CAP;
+      const int used = CAP - stop_excl;  // slots taken from segment cur+lstop
       const int base = lstop == 0 ? curk : 0;
-      if (stop_incl == TK) {
+      if (stop_incl == CAP) {
         cursor[0] = cur + lstop + 1;
         cursor[1] = 0;
       } else {
@@ -405,6 +407,9 @@ __device__ __forceinline__ void build_slots(const Group &g, const Seg *__restric
         cursor[1] = base + used;
       }
     }
+    const int nch = (filled + TK - 1) / TK;
+    for (int c = 0; c < nch; ++c) nslot[c] = min(TK, filled - c * TK);
+    *nchunk = nch;
   }
 }
 
@@ -423,6 +428,7 @@ struct TcShape {
   // measured slower).
   static constexpr int TK = (S == 4 && TN == 64) ? 64 : 32;
   static constexpr int PAD = TK + 8;          // bf16 per plane row in shared memory
+  static constexpr int NCH = 4;               // chunks per slot-table pass
   static constexpr int WM = TM / 16, WN = TN / 8;
   static constexpr int NT = 32 * WM * WN;     // threads per CTA
   static constexpr int TPR = NT / TM;         // threads per row of A
@@ -448,8 +454,8 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
   __nv_bfloat16 *Bp = Ap + S * TM * T_PAD;                          // [S][TN][PAD]
   int *Ea = reinterpret_cast<int *>(Bp + S * TN * T_PAD);           // [TM]
   int *Eb = Ea + TM;                                                // [TN]
-  Slot *slots = reinterpret_cast<Slot *>(Eb + (TN < 16 ? 16 : TN));  // [TK] (Eb holds TN ints)
-  int *ctl = reinterpret_cast<int *>(slots + TK);                 // cursor[2], nslot
+  Slot *slots = reinterpret_cast<Slot *>(Eb + (TN < 16 ? 16 : TN));  // [NCH][TK] (Eb holds TN ints)
+  int *ctl = reinterpret_cast<int *>(slots + Sh::NCH * TK);  // cursor[2], nchunk, nslot[NCH]
 
   __shared__ int cbj[TN], cbrel[TN];  // column-block map of the tile
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -472,10 +478,13 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
     __syncthreads();
     const int jb = g.ncb ? cbj[cb] : -1, colrel = g.ncb ? cbrel[cb] : 0;
     while (true) {
-      if (warp == 0) build_slots<TK>(g, segs, bufs, slots, ctl, ctl + 2, lane);
+      if (warp == 0) build_slots_multi<TK, Sh::NCH>(g, segs, bufs, slots, ctl, ctl + 3, ctl + 2, lane);
       __syncthreads();
-      const int ns = ctl[2];
-      if (ns == 0) break;
+      const int nch = ctl[2];
+      if (nch == 0) break;
+      for (int ch = 0; ch < nch; ++ch) {
+      const int ns = ctl[3 + ch];
+      const Slot *slt = slots + ch * TK;
       {  // A: chunk max exponent of the row over its TPR threads, digit planes
         double v[KPA];
         int emax = 0;
@@ -484,7 +493,7 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
           const int j = parta * KPA + t;
           double x = 0.0;
           if (j < ns && rowa < g.M) {
-            const Slot &sl = slots[j];
+            const Slot &sl = slt[j];
             x = __ldg(sl.a + (int64_t)rowa * sl.sam);
             if (sl.scaled) x *= sl.alpha;
           }
@@ -514,7 +523,7 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
           const int j = partb * KPB + t;
           double x = 0.0;
           if (j < ns && colb < g.N)
-            x = g.ncb ? load_b_cb(slots[j], segb, g, jb, colrel) : __ldg(slots[j].b + (int64_t)colb * slots[j].sbn);
+            x = g.ncb ? load_b_cb(slt[j], segb, g, jb, colrel) : __ldg(slt[j].b + (int64_t)colb * slt[j].sbn);
           v[t] = x;
           emax = max(emax, dexp(x));
         }
@@ -587,6 +596,7 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
         }
       }
       __syncthreads();
+      }
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -603,8 +613,8 @@ static int launch_tc_t(const Work *work, int64_t nwork, const Step &s, const Buf
   if (nwork == 0) return ZMPO_OK;
   using Sh = TcShape<S, TM, TN>;
   const size_t smem = (size_t)S * (TM + TN) * Sh::PAD * sizeof(__nv_bfloat16) +
-                      (size_t)(TM + (TN < 16 ? 16 : TN)) * sizeof(int) + Sh::TK * sizeof(Slot) +
-                      4 * sizeof(int) + 16;
+                      (size_t)(TM + (TN < 16 ? 16 : TN)) * sizeof(int) + Sh::NCH * Sh::TK * sizeof(Slot) +
+                      (3 + Sh::NCH) * sizeof(int) + 16;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_step_tc<S, TM, TN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
