@@ -428,7 +428,7 @@ struct TcShape {
   // measured slower).
   static constexpr int TK = (S == 4 && TN == 64) ? 64 : 32;
   static constexpr int PAD = TK + 8;          // bf16 per plane row in shared memory
-  static constexpr int NCH = 4;               // chunks per slot-table pass
+  static constexpr int NCH = 8;               // chunks per slot-table pass (4, 8, 16 measured: 8 best)
   static constexpr int WM = TM / 16, WN = TN / 8;
   static constexpr int NT = 32 * WM * WN;     // threads per CTA
   static constexpr int TPR = NT / TM;         // threads per row of A

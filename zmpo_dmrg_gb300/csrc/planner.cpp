@@ -832,18 +832,27 @@ static int upload_step(Step &st) {
   // order groups by cost (longest first) for load balance
   std::vector<int> order(st.groups.size());
   std::iota(order.begin(), order.end(), 0);
-  std::vector<int64_t> cost(st.groups.size(), 0);
+  std::vector<int64_t> cost(st.groups.size(), 0), ktot(st.groups.size(), 0);
   for (size_t g = 0; g < st.groups.size(); ++g) {
-    int64_t c = 0;
-    for (int s = 0; s < st.groups[g].nseg; ++s) c += st.segs[st.groups[g].seg0 + s].K + 16;
+    int64_t c = 0, k = 0;
+    for (int s = 0; s < st.groups[g].nseg; ++s) {
+      c += st.segs[st.groups[g].seg0 + s].K + 16;
+      k += st.segs[st.groups[g].seg0 + s].K;
+    }
     cost[g] = c;
+    ktot[g] = k;
   }
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
   for (int g : order) {
     const Group &G = st.groups[g];
     for (int mt = 0; mt * kTileFP64M < G.M; ++mt)
       for (int nt = 0; nt * kTileFP64N < G.N; ++nt) w64.push_back({g, mt, nt, 0});
-    const int tni = G.N <= 8 ? 0 : (G.N <= 16 ? 1 : (G.N <= 32 ? 2 : 3)), tn = 8 << tni;
+    int tni = G.N <= 8 ? 0 : (G.N <= 16 ? 1 : (G.N <= 32 ? 2 : 3));
+    // 64-column tiles cut K in 64-slot chunks: a group with K <= 32 would
+    // leave half of every chunk empty, so it takes 32-column tiles (32-slot
+    // chunks, up to 128 rows) instead
+    if (tni == 3 && ktot[g] <= 32) tni = 2;
+    const int tn = 8 << tni;
     int tmi = G.M <= 32 ? 0 : (G.M <= 64 ? 1 : 2);
     if (tni == 3 && tmi == 2) tmi = 1;  // 64-column tiles: 32 or 64 rows (1024 threads at most)
     const int tm = 32 << tmi;
