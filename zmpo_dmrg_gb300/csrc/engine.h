@@ -82,10 +82,16 @@ struct Step {
   ColBlock *d_cblocks = nullptr;
   SegB *d_segb = nullptr;
   Work *d_work_fp64 = nullptr;   // tiles of kTileFP64
-  // tensor-core tiles: [rows 32 / 64 / 128][columns 8 / 16]
+  // tensor-core tiles of every group (7 digit slices)
   Work *d_work_tc[3][4] = {};  // [row tile 32/64/128][column tile 8/16/32/64]
+  // 4 digit slices: the groups of the B-resident kernel (Work: column tile
+  // nt, row tiles mt .. mt+pad-1) and the tiles of all other groups
+  Work *d_work_tcb[2] = {};    // [64 x 64 tiles, 128 x 32 tiles]
+  Work *d_work_tc4[3][4] = {};
   int64_t nwork_fp64 = 0;
   int64_t nwork_tc[3][4] = {};
+  int64_t nwork_tcb[2] = {};
+  int64_t nwork_tc4[3][4] = {};
   double flops = 0.0;            // sum of 2*m*n*k of the reference tasks
   int64_t ntasks = 0;
   bool uploaded = false;         // device copies are made on first use

@@ -441,6 +441,131 @@ struct TcShape {
   static_assert(TPR >= 1 && KPA >= 1 && TPC >= 1 && KPB >= 1, "tile shape");
 };
 
+// Cut of one chunk of A: TPR threads per row, KPA slots each; the row's
+// chunk exponent (max over its TPR threads) and its S digit planes.
+template <int S, int TM, int TPR, int KPA, int T_PAD>
+__device__ __forceinline__ void cut_a(const Slot *slt, int ns, int rowa, int M, __nv_bfloat16 *Ap, int *Ea,
+                                      int ra, int parta) {
+  double v[KPA];
+  int emax = 0;
+#pragma unroll
+  for (int t = 0; t < KPA; ++t) {
+    const int j = parta * KPA + t;
+    double x = 0.0;
+    if (j < ns && rowa < M) {
+      const Slot &sl = slt[j];
+      x = __ldg(sl.a + (int64_t)rowa * sl.sam);
+      if (sl.scaled) x *= sl.alpha;
+    }
+    v[t] = x;
+    emax = max(emax, dexp(x));
+  }
+#pragma unroll
+  for (int o = 1; o < TPR; o <<= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+  if (parta == 0) Ea[ra] = emax;
+  if constexpr (S == 4 && KPA % 2 == 0) {
+    uint32_t *ap = reinterpret_cast<uint32_t *>(Ap + ra * T_PAD + parta * KPA);
+#pragma unroll
+    for (int t = 0; t < KPA; t += 2) digits4_pair(v[t], v[t + 1], emax, ap + t / 2, TM * T_PAD / 2);
+  } else if constexpr (S == 4) {
+#pragma unroll
+    for (int t = 0; t < KPA; ++t) digits4_one(v[t], emax, Ap + ra * T_PAD + parta * KPA + t, TM * T_PAD);
+  } else {
+#pragma unroll
+    for (int t = 0; t < KPA; ++t) digits_bf16<S>(v[t], emax, Ap + ra * T_PAD + parta * KPA + t, TM * T_PAD);
+  }
+}
+
+// Cut of one chunk of B: TPC threads per column, KPB slots each.
+template <int S, int TN, int TPC, int KPB, int T_PAD>
+__device__ __forceinline__ void cut_b(const Slot *slt, int ns, int colb, const Group &g,
+                                      const SegB *__restrict__ segb, int jb, int colrel, __nv_bfloat16 *Bp,
+                                      int *Eb, int cb, int partb) {
+  double v[KPB];
+  int emax = 0;
+#pragma unroll
+  for (int t = 0; t < KPB; ++t) {
+    const int j = partb * KPB + t;
+    double x = 0.0;
+    if (j < ns && colb < g.N)
+      x = g.ncb ? load_b_cb(slt[j], segb, g, jb, colrel) : __ldg(slt[j].b + (int64_t)colb * slt[j].sbn);
+    v[t] = x;
+    emax = max(emax, dexp(x));
+  }
+#pragma unroll
+  for (int o = 1; o < TPC; o <<= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+  if (partb == 0) Eb[cb] = emax;
+  if constexpr (S == 4 && KPB % 2 == 0) {
+    uint32_t *bp = reinterpret_cast<uint32_t *>(Bp + cb * T_PAD + partb * KPB);
+#pragma unroll
+    for (int t = 0; t < KPB; t += 2) digits4_pair(v[t], v[t + 1], emax, bp + t / 2, TN * T_PAD / 2);
+  } else if constexpr (S == 4) {
+#pragma unroll
+    for (int t = 0; t < KPB; ++t) digits4_one(v[t], emax, Bp + cb * T_PAD + partb * KPB + t, TN * T_PAD);
+  } else {
+#pragma unroll
+    for (int t = 0; t < KPB; ++t) digits_bf16<S>(v[t], emax, Bp + cb * T_PAD + partb * KPB + t, TN * T_PAD);
+  }
+}
+
+// Digit products of one chunk for this warp's m16 x n8 piece (exact in FP32
+// per level), then the levels scaled by 2^(Ea + Eb - 2044 - 8(l+2)) into the
+// two-float sums.
+template <int S, int TM, int TN, int TK, int T_PAD>
+__device__ __forceinline__ void mma_fold(const __nv_bfloat16 *Ap, const __nv_bfloat16 *Bp, const int *Ea,
+                                         const int *Eb, int wm, int wn, int gq, int tq, float *hi, float *lo) {
+  float acc[S][4];
+#pragma unroll
+  for (int l = 0; l < S; ++l)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) acc[l][i] = 0.f;
+#pragma unroll
+  for (int kk = 0; kk < TK; kk += 16) {
+    uint32_t bf[S][2];
+#pragma unroll
+    for (int sb = 0; sb < S; ++sb) {
+      const __nv_bfloat16 *bp = Bp + (sb * TN + wn + gq) * T_PAD + kk;
+      bf[sb][0] = *reinterpret_cast<const uint32_t *>(bp + 2 * tq);
+      bf[sb][1] = *reinterpret_cast<const uint32_t *>(bp + 2 * tq + 8);
+    }
+#pragma unroll
+    for (int sa = 0; sa < S; ++sa) {
+      uint32_t af[4];
+      const __nv_bfloat16 *ap = Ap + (sa * TM + wm) * T_PAD + kk;
+      af[0] = *reinterpret_cast<const uint32_t *>(ap + gq * T_PAD + 2 * tq);
+      af[1] = *reinterpret_cast<const uint32_t *>(ap + (gq + 8) * T_PAD + 2 * tq);
+      af[2] = *reinterpret_cast<const uint32_t *>(ap + gq * T_PAD + 2 * tq + 8);
+      af[3] = *reinterpret_cast<const uint32_t *>(ap + (gq + 8) * T_PAD + 2 * tq + 8);
+#pragma unroll
+      for (int sb = 0; sb + sa < S; ++sb) mma_bf16(acc[sa + sb], af, bf[sb]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = wm + gq + (i >> 1) * 8;
+    const int c = wn + 2 * tq + (i & 1);
+    const int ea = Ea[r], eb = Eb[c];
+    if (ea == 0 || eb == 0) continue;
+    const int base = ea + eb - 2044;
+    if constexpr (S == 4) {
+      // levels are exact integers below 2^24: level 0 + level 1 / 2^8 as an
+      // exact pair, levels 2 and 3 into its low part, one scale
+      float h, e;
+      two_sum(acc[0][i], acc[1][i] * 0x1p-8f, h, e);
+      e = fmaf(acc[2][i], 0x1p-16f, e);
+      e = fmaf(acc[3][i], 0x1p-24f, e);
+      const float sc = pow2f(base - 16);
+      float s2, e2;
+      two_sum(hi[i], h * sc, s2, e2);
+      hi[i] = s2;
+      lo[i] += e2 + e * sc;
+    } else {
+#pragma unroll
+      for (int l = 0; l < S; ++l) two_sum_acc(hi[i], lo[i], scale_pow2(acc[l][i], base - 8 * (l + 2)));
+    }
+  }
+}
+
 template <int S, int TM, int TN>
 __global__ void __launch_bounds__(TcShape<S, TM, TN>::NT, TcShape<S, TM, TN>::THREADS_SM / TcShape<S, TM, TN>::NT)
 k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
@@ -483,119 +608,13 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
       const int nch = ctl[2];
       if (nch == 0) break;
       for (int ch = 0; ch < nch; ++ch) {
-      const int ns = ctl[3 + ch];
-      const Slot *slt = slots + ch * TK;
-      {  // A: chunk max exponent of the row over its TPR threads, digit planes
-        double v[KPA];
-        int emax = 0;
-#pragma unroll
-        for (int t = 0; t < KPA; ++t) {
-          const int j = parta * KPA + t;
-          double x = 0.0;
-          if (j < ns && rowa < g.M) {
-            const Slot &sl = slt[j];
-            x = __ldg(sl.a + (int64_t)rowa * sl.sam);
-            if (sl.scaled) x *= sl.alpha;
-          }
-          v[t] = x;
-          emax = max(emax, dexp(x));
-        }
-#pragma unroll
-        for (int o = 1; o < TPR; o <<= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
-        if (parta == 0) Ea[ra] = emax;
-        if constexpr (S == 4 && KPA % 2 == 0) {
-          uint32_t *ap = reinterpret_cast<uint32_t *>(Ap + ra * T_PAD + parta * KPA);
-#pragma unroll
-          for (int t = 0; t < KPA; t += 2) digits4_pair(v[t], v[t + 1], emax, ap + t / 2, TM * T_PAD / 2);
-        } else if constexpr (S == 4) {
-#pragma unroll
-          for (int t = 0; t < KPA; ++t) digits4_one(v[t], emax, Ap + ra * T_PAD + parta * KPA + t, TM * T_PAD);
-        } else {
-#pragma unroll
-          for (int t = 0; t < KPA; ++t) digits_bf16<S>(v[t], emax, Ap + ra * T_PAD + parta * KPA + t, TM * T_PAD);
-        }
-      }
-      {  // B: TPC threads per column share the 32 slots
-        double v[KPB];
-        int emax = 0;
-#pragma unroll
-        for (int t = 0; t < KPB; ++t) {
-          const int j = partb * KPB + t;
-          double x = 0.0;
-          if (j < ns && colb < g.N)
-            x = g.ncb ? load_b_cb(slt[j], segb, g, jb, colrel) : __ldg(slt[j].b + (int64_t)colb * slt[j].sbn);
-          v[t] = x;
-          emax = max(emax, dexp(x));
-        }
-#pragma unroll
-        for (int o = 1; o < TPC; o <<= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
-        if (partb == 0) Eb[cb] = emax;
-        if constexpr (S == 4 && KPB % 2 == 0) {
-          uint32_t *bp = reinterpret_cast<uint32_t *>(Bp + cb * T_PAD + partb * KPB);
-#pragma unroll
-          for (int t = 0; t < KPB; t += 2) digits4_pair(v[t], v[t + 1], emax, bp + t / 2, TN * T_PAD / 2);
-        } else if constexpr (S == 4) {
-#pragma unroll
-          for (int t = 0; t < KPB; ++t) digits4_one(v[t], emax, Bp + cb * T_PAD + partb * KPB + t, TN * T_PAD);
-        } else {
-#pragma unroll
-          for (int t = 0; t < KPB; ++t) digits_bf16<S>(v[t], emax, Bp + cb * T_PAD + partb * KPB + t, TN * T_PAD);
-        }
-      }
-      __syncthreads();
-      // digit products per level, exact in FP32
-      float acc[S][4];
-#pragma unroll
-      for (int l = 0; l < S; ++l)
-#pragma unroll
-        for (int i = 0; i < 4; ++i) acc[l][i] = 0.f;
-#pragma unroll
-      for (int kk = 0; kk < TK; kk += 16) {
-        uint32_t bf[S][2];
-#pragma unroll
-        for (int sb = 0; sb < S; ++sb) {
-          const __nv_bfloat16 *bp = Bp + (sb * TN + wn + gq) * T_PAD + kk;
-          bf[sb][0] = *reinterpret_cast<const uint32_t *>(bp + 2 * tq);
-          bf[sb][1] = *reinterpret_cast<const uint32_t *>(bp + 2 * tq + 8);
-        }
-#pragma unroll
-        for (int sa = 0; sa < S; ++sa) {
-          uint32_t af[4];
-          const __nv_bfloat16 *ap = Ap + (sa * TM + wm) * T_PAD + kk;
-          af[0] = *reinterpret_cast<const uint32_t *>(ap + gq * T_PAD + 2 * tq);
-          af[1] = *reinterpret_cast<const uint32_t *>(ap + (gq + 8) * T_PAD + 2 * tq);
-          af[2] = *reinterpret_cast<const uint32_t *>(ap + gq * T_PAD + 2 * tq + 8);
-          af[3] = *reinterpret_cast<const uint32_t *>(ap + (gq + 8) * T_PAD + 2 * tq + 8);
-#pragma unroll
-          for (int sb = 0; sb + sa < S; ++sb) mma_bf16(acc[sa + sb], af, bf[sb]);
-        }
-      }
-      // scale the levels by 2^(Ea + Eb - 2044 - 8(l+2)) into the two-float sums
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const int r = wm + gq + (i >> 1) * 8;
-        const int c = wn + 2 * tq + (i & 1);
-        const int ea = Ea[r], eb = Eb[c];
-        if (ea == 0 || eb == 0) continue;
-        const int base = ea + eb - 2044;
-        if constexpr (S == 4) {
-          // levels are exact integers below 2^24: level 0 + level 1 / 2^8 as
-          // an exact pair, levels 2 and 3 into its low part, one scale
-          float h, e;
-          two_sum(acc[0][i], acc[1][i] * 0x1p-8f, h, e);
-          e = fmaf(acc[2][i], 0x1p-16f, e);
-          e = fmaf(acc[3][i], 0x1p-24f, e);
-          const float sc = pow2f(base - 16);
-          float s2, e2;
-          two_sum(hi[i], h * sc, s2, e2);
-          hi[i] = s2;
-          lo[i] += e2 + e * sc;
-        } else {
-#pragma unroll
-          for (int l = 0; l < S; ++l) two_sum_acc(hi[i], lo[i], scale_pow2(acc[l][i], base - 8 * (l + 2)));
-        }
-      }
-      __syncthreads();
+        const int ns = ctl[3 + ch];
+        const Slot *slt = slots + ch * TK;
+        cut_a<S, TM, TPR, KPA, T_PAD>(slt, ns, rowa, g.M, Ap, Ea, ra, parta);
+        cut_b<S, TN, TPC, KPB, T_PAD>(slt, ns, colb, g, segb, jb, colrel, Bp, Eb, cb, partb);
+        __syncthreads();
+        mma_fold<S, TM, TN, TK, T_PAD>(Ap, Bp, Ea, Eb, wm, wn, gq, tq, hi, lo);
+        __syncthreads();
       }
     }
 #pragma unroll
@@ -606,6 +625,101 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
     }
     __syncthreads();  // the column map is rewritten by the next tile
   }
+}
+
+// B-resident variant for groups whose whole K fits in CHB chunks of one
+// slot-table pass (at most 32 segments): a work item is one column tile and
+// a run of up to MB row tiles (Work::pad of them).  The column tile's B is cut
+// into digit planes once, for every chunk, and stays in shared memory while
+// the row tiles stream through: B is cut once per run instead of once per row
+// tile.
+template <int TM, int TN>
+struct TcbShape {
+  using Sh = TcShape<4, TM, TN>;
+  static constexpr int CHB = 192 / Sh::TK;      // K up to 192
+  static constexpr int EBN = TN < 16 ? 16 : TN;
+  static constexpr size_t smem() {
+    return (size_t)4 * TM * Sh::PAD * 2 + (size_t)CHB * 4 * TN * Sh::PAD * 2 + (size_t)TM * 4 +
+           (size_t)CHB * EBN * 4 + (size_t)CHB * Sh::TK * sizeof(Slot) + (3 + CHB) * 4 + 16;
+  }
+};
+
+template <int TM, int TN>
+__global__ void __launch_bounds__(TcShape<4, TM, TN>::NT, TcShape<4, TM, TN>::THREADS_SM / TcShape<4, TM, TN>::NT)
+k_step_tcb(const Work *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
+           const Seg *__restrict__ segs, const ColBlock *__restrict__ cbl, const SegB *__restrict__ segb,
+           Bufs bufs) {
+  constexpr int S = 4;
+  using Sh = TcShape<S, TM, TN>;
+  using Bh = TcbShape<TM, TN>;
+  constexpr int TPR = Sh::TPR, KPA = Sh::KPA, TPC = Sh::TPC, KPB = Sh::KPB;
+  constexpr int TK = Sh::TK, T_PAD = Sh::PAD, CHB = Bh::CHB, EBN = Bh::EBN;
+  constexpr int BPL = S * TN * T_PAD;  // bf16 per chunk of B planes
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __nv_bfloat16 *Ap = reinterpret_cast<__nv_bfloat16 *>(smem_raw);  // [S][TM][PAD]
+  __nv_bfloat16 *Bp = Ap + S * TM * T_PAD;                          // [CHB][S][TN][PAD]
+  int *Ea = reinterpret_cast<int *>(Bp + CHB * BPL);                // [TM]
+  int *Eb = Ea + TM;                                                // [CHB][EBN]
+  Slot *slots = reinterpret_cast<Slot *>(Eb + CHB * EBN);          // [CHB][TK]
+  int *ctl = reinterpret_cast<int *>(slots + CHB * TK);             // cursor[2], nchunk, nslot[CHB]
+
+  __shared__ int cbj[TN], cbrel[TN];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = (warp % Sh::WM) * 16, wn = (warp / Sh::WM) * 8;
+  const int gq = lane >> 2, tq = lane & 3;
+  const int ra = tid / TPR, parta = tid % TPR;
+  const int cb = tid / TPC, partb = tid % TPC;
+
+  for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const Work wk = work[w];
+    const Group g = groups[wk.group];
+    const int n0 = wk.nt * TN, colb = n0 + cb;
+    if (tid == 0) {
+      ctl[0] = 0;
+      ctl[1] = 0;
+    }
+    if (g.ncb) tile_cblocks(cbl, g, n0, TN, cbj, cbrel);
+    __syncthreads();
+    const int jb = g.ncb ? cbj[cb] : -1, colrel = g.ncb ? cbrel[cb] : 0;
+    if (warp == 0) build_slots_multi<TK, CHB>(g, segs, bufs, slots, ctl, ctl + 3, ctl + 2, lane);
+    __syncthreads();
+    const int nch = ctl[2];  // the planner routes only groups that one pass covers
+    for (int ch = 0; ch < nch; ++ch)
+      cut_b<S, TN, TPC, KPB, T_PAD>(slots + ch * TK, ctl[3 + ch], colb, g, segb, jb, colrel, Bp + ch * BPL,
+                                    Eb + ch * EBN, cb, partb);
+    for (int mi = 0; mi < wk.pad; ++mi) {
+      const int m0 = (wk.mt + mi) * TM, rowa = m0 + ra;
+      float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int ch = 0; ch < nch; ++ch) {
+        cut_a<S, TM, TPR, KPA, T_PAD>(slots + ch * TK, ctl[3 + ch], rowa, g.M, Ap, Ea, ra, parta);
+        __syncthreads();
+        mma_fold<S, TM, TN, TK, T_PAD>(Ap, Bp + ch * BPL, Ea, Eb + ch * EBN, wm, wn, gq, tq, hi, lo);
+        __syncthreads();
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int r = m0 + wm + gq + (i >> 1) * 8;
+        const int c = n0 + wn + 2 * tq + (i & 1);
+        if (r < g.M && c < g.N) store_c(bufs, cbl, g, r, c, n0, cbj, cbrel, two_float_to_double(hi[i], lo[i]));
+      }
+    }
+    __syncthreads();  // slot tables, B planes and the column map are rewritten by the next item
+  }
+}
+
+template <int TM, int TN>
+static int launch_tcb_t(const Work *work, int64_t nwork, const Step &s, const Bufs &b, void *stream) {
+  if (nwork == 0) return ZMPO_OK;
+  const size_t smem = TcbShape<TM, TN>::smem();
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_step_tcb<TM, TN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  constexpr int NT = TcShape<4, TM, TN>::NT;
+  k_step_tcb<TM, TN><<<grid_for(nwork, TcShape<4, TM, TN>::THREADS_SM / NT), NT, smem, (cudaStream_t)stream>>>(
+      work, nwork, s.d_groups, s.d_segs, s.d_cblocks, s.d_segb, b);
+  return launch_error("k_step_tcb");
 }
 
 template <int S, int TM, int TN>
@@ -629,17 +743,25 @@ static int launch_tc_t(const Work *work, int64_t nwork, const Step &s, const Buf
 template <int S>
 static int launch_split_all(const Step &s, const Bufs &b, void *stream) {
   int rc;
-  if ((rc = launch_tc_t<S, 128, 8>(s.d_work_tc[2][0], s.nwork_tc[2][0], s, b, stream))) return rc;
-  if ((rc = launch_tc_t<S, 128, 16>(s.d_work_tc[2][1], s.nwork_tc[2][1], s, b, stream))) return rc;
-  if ((rc = launch_tc_t<S, 64, 8>(s.d_work_tc[1][0], s.nwork_tc[1][0], s, b, stream))) return rc;
-  if ((rc = launch_tc_t<S, 64, 16>(s.d_work_tc[1][1], s.nwork_tc[1][1], s, b, stream))) return rc;
-  if ((rc = launch_tc_t<S, 32, 8>(s.d_work_tc[0][0], s.nwork_tc[0][0], s, b, stream))) return rc;
-  if ((rc = launch_tc_t<S, 32, 16>(s.d_work_tc[0][1], s.nwork_tc[0][1], s, b, stream))) return rc;
-  if ((rc = launch_tc_t<S, 128, 32>(s.d_work_tc[2][2], s.nwork_tc[2][2], s, b, stream))) return rc;
-  if ((rc = launch_tc_t<S, 64, 32>(s.d_work_tc[1][2], s.nwork_tc[1][2], s, b, stream))) return rc;
-  if ((rc = launch_tc_t<S, 32, 32>(s.d_work_tc[0][2], s.nwork_tc[0][2], s, b, stream))) return rc;
-  if ((rc = launch_tc_t<S, 64, 64>(s.d_work_tc[1][3], s.nwork_tc[1][3], s, b, stream))) return rc;
-  return launch_tc_t<S, 32, 64>(s.d_work_tc[0][3], s.nwork_tc[0][3], s, b, stream);
+  // S = 4: the groups routed to the B-resident kernel are not in the S = 4
+  // lists; S = 7 (no B-resident variant) uses the lists of every group
+  Work *const(*wl)[4] = S == 4 ? s.d_work_tc4 : s.d_work_tc;
+  const int64_t(*nw)[4] = S == 4 ? s.nwork_tc4 : s.nwork_tc;
+  if (S == 4) {
+    if ((rc = launch_tcb_t<64, 64>(s.d_work_tcb[0], s.nwork_tcb[0], s, b, stream))) return rc;
+    if ((rc = launch_tcb_t<128, 32>(s.d_work_tcb[1], s.nwork_tcb[1], s, b, stream))) return rc;
+  }
+  if ((rc = launch_tc_t<S, 128, 8>(wl[2][0], nw[2][0], s, b, stream))) return rc;
+  if ((rc = launch_tc_t<S, 128, 16>(wl[2][1], nw[2][1], s, b, stream))) return rc;
+  if ((rc = launch_tc_t<S, 64, 8>(wl[1][0], nw[1][0], s, b, stream))) return rc;
+  if ((rc = launch_tc_t<S, 64, 16>(wl[1][1], nw[1][1], s, b, stream))) return rc;
+  if ((rc = launch_tc_t<S, 32, 8>(wl[0][0], nw[0][0], s, b, stream))) return rc;
+  if ((rc = launch_tc_t<S, 32, 16>(wl[0][1], nw[0][1], s, b, stream))) return rc;
+  if ((rc = launch_tc_t<S, 128, 32>(wl[2][2], nw[2][2], s, b, stream))) return rc;
+  if ((rc = launch_tc_t<S, 64, 32>(wl[1][2], nw[1][2], s, b, stream))) return rc;
+  if ((rc = launch_tc_t<S, 32, 32>(wl[0][2], nw[0][2], s, b, stream))) return rc;
+  if ((rc = launch_tc_t<S, 64, 64>(wl[1][3], nw[1][3], s, b, stream))) return rc;
+  return launch_tc_t<S, 32, 64>(wl[0][3], nw[0][3], s, b, stream);
 }
 
 int launch_step_split(const Step &s, const Bufs &b, int nslices, void *stream) {

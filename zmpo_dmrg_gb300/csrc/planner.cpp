@@ -748,6 +748,9 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
 
 // tile sizes of the two kernels (must match kernels.cu)
 constexpr int kTileFP64M = 32, kTileFP64N = 32;
+// B-resident kernel (kernels.cu, k_step_tcb): largest K it holds (three
+// 64-slot or six 32-slot chunks) and the row tiles of one work item
+constexpr int kBresMaxK = 192, kBresRun = 8;
 
 // Cut groups whose summed K exceeds kSplitK into parts of about kSplitK (at
 // segment boundaries, or inside a long segment); parts go to scratch and a
@@ -828,7 +831,7 @@ static void split_long_groups(Step &st) {
 static int upload_step(Step &st) {
   if (st.uploaded) return ZMPO_OK;
   split_long_groups(st);
-  std::vector<Work> w64, wtc[3][4];
+  std::vector<Work> w64, wtc[3][4], wtc4[3][4], wtcb[2];
   // order groups by cost (longest first) for load balance
   std::vector<int> order(st.groups.size());
   std::iota(order.begin(), order.end(), 0);
@@ -857,12 +860,29 @@ static int upload_step(Step &st) {
     if (tni == 3 && tmi == 2) tmi = 1;  // 64-column tiles: 32 or 64 rows (1024 threads at most)
     const int tm = 32 << tmi;
     auto &wl = wtc[tmi][tni];
-    for (int mt = 0; mt * tm < G.M; ++mt)
-      for (int nt = 0; nt * tn < G.N; ++nt) wl.push_back({g, mt, nt, 0});
+    const int nmt = (G.M + tm - 1) / tm, nnt = (G.N + tn - 1) / tn;
+    for (int mt = 0; mt < nmt; ++mt)
+      for (int nt = 0; nt < nnt; ++nt) wl.push_back({g, mt, nt, 0});
+    // B-resident kernel: 64 x 64 or 128 x 32 tiles, several row tiles, the
+    // whole K in one slot-table pass (at most 32 segments, K <= 192)
+    const int bres = (tmi == 1 && tni == 3) ? 0 : ((tmi == 2 && tni == 2) ? 1 : -1);
+    if (bres >= 0 && nmt >= 2 && G.nseg <= 32 && ktot[g] <= kBresMaxK) {
+      const int nruns = (nmt + kBresRun - 1) / kBresRun;
+      const int len = (nmt + nruns - 1) / nruns;
+      for (int nt = 0; nt < nnt; ++nt)
+        for (int mt = 0; mt < nmt; mt += len) wtcb[bres].push_back({g, mt, nt, std::min(len, nmt - mt)});
+    } else {
+      for (int mt = 0; mt < nmt; ++mt)
+        for (int nt = 0; nt < nnt; ++nt) wtc4[tmi][tni].push_back({g, mt, nt, 0});
+    }
   }
   st.nwork_fp64 = (int64_t)w64.size();
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 4; ++j) st.nwork_tc[i][j] = (int64_t)wtc[i][j].size();
+    for (int j = 0; j < 4; ++j) {
+      st.nwork_tc[i][j] = (int64_t)wtc[i][j].size();
+      st.nwork_tc4[i][j] = (int64_t)wtc4[i][j].size();
+    }
+  for (int i = 0; i < 2; ++i) st.nwork_tcb[i] = (int64_t)wtcb[i].size();
   auto up = [](auto **dptr, const auto &v) -> cudaError_t {
     using T = typename std::remove_reference<decltype(v)>::type::value_type;
     if (v.empty()) {
@@ -879,7 +899,11 @@ static int upload_step(Step &st) {
   CUDA_TRY(up(&st.d_segb, st.segb));
   CUDA_TRY(up(&st.d_work_fp64, w64));
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 4; ++j) CUDA_TRY(up(&st.d_work_tc[i][j], wtc[i][j]));
+    for (int j = 0; j < 4; ++j) {
+      CUDA_TRY(up(&st.d_work_tc[i][j], wtc[i][j]));
+      CUDA_TRY(up(&st.d_work_tc4[i][j], wtc4[i][j]));
+    }
+  for (int i = 0; i < 2; ++i) CUDA_TRY(up(&st.d_work_tcb[i], wtcb[i]));
   CUDA_TRY(up(&st.d_reds, st.reds));
   if (st.part_elems > 0) CUDA_TRY(cudaMalloc((void **)&st.d_part, st.part_elems * sizeof(double)));
   // keep the host mirror of groups (sizes) but free the bulky segment copy
@@ -902,8 +926,14 @@ static void free_step(Step &st) {
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 4; ++j) {
       cudaFree(st.d_work_tc[i][j]);
+      cudaFree(st.d_work_tc4[i][j]);
       st.d_work_tc[i][j] = nullptr;
+      st.d_work_tc4[i][j] = nullptr;
     }
+  for (int i = 0; i < 2; ++i) {
+    cudaFree(st.d_work_tcb[i]);
+    st.d_work_tcb[i] = nullptr;
+  }
   cudaFree(st.d_reds);
   cudaFree(st.d_part);
   st.d_reds = nullptr;
@@ -1467,8 +1497,10 @@ int zmpo_plan_kernel_count(zmpo_engine *e, int plan_id, int precision, int *coun
     if (precision == ZMPO_PREC_FP64) {
       n += s.nwork_fp64 > 0;
     } else {
+      const bool s4 = precision == ZMPO_PREC_SPLIT;
       for (int a = 0; a < 3; ++a)
-        for (int c = 0; c < 4; ++c) n += s.nwork_tc[a][c] > 0;
+        for (int c = 0; c < 4; ++c) n += (s4 ? s.nwork_tc4[a][c] : s.nwork_tc[a][c]) > 0;
+      if (s4) n += (s.nwork_tcb[0] > 0) + (s.nwork_tcb[1] > 0);
     }
     n += s.red_elems > 0;
   }
