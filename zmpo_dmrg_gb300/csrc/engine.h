@@ -60,8 +60,8 @@ struct Reduction {
 
 struct Work {
   int32_t group;
-  int32_t mt, nt;   // tile coordinates inside the group
-  int32_t pad;
+  int32_t mt, nt;   // first row and first column of the tile inside the group
+  int32_t pad;      // B-resident kernel: row tiles of the item (from row mt)
 };
 
 constexpr int kMaxBufs = 8;

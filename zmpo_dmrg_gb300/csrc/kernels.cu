@@ -96,7 +96,7 @@ k_step_fp64(const Work *__restrict__ work, int64_t nwork, const Group *__restric
   for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
     const Work wk = work[w];
     const Group g = groups[wk.group];
-    const int m0 = wk.mt * F_TM, n0 = wk.nt * F_TN;
+    const int m0 = wk.mt, n0 = wk.nt;
     if (g.ncb) tile_cblocks(cbl, g, n0, F_TN, cbj, cbrel);
     __syncthreads();
     double c00 = 0.0, c01 = 0.0, c10 = 0.0, c11 = 0.0;
@@ -592,7 +592,7 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
   for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
     const Work wk = work[w];
     const Group g = groups[wk.group];
-    const int m0 = wk.mt * TM, n0 = wk.nt * TN;
+    const int m0 = wk.mt, n0 = wk.nt;
     const int rowa = m0 + ra, colb = n0 + cb;
     float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
     if (tid == 0) {
@@ -673,7 +673,7 @@ k_step_tcb(const Work *__restrict__ work, int64_t nwork, const Group *__restrict
   for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
     const Work wk = work[w];
     const Group g = groups[wk.group];
-    const int n0 = wk.nt * TN, colb = n0 + cb;
+    const int n0 = wk.nt, colb = n0 + cb;
     if (tid == 0) {
       ctl[0] = 0;
       ctl[1] = 0;
@@ -688,7 +688,7 @@ k_step_tcb(const Work *__restrict__ work, int64_t nwork, const Group *__restrict
       cut_b<S, TN, TPC, KPB, T_PAD>(slots + ch * TK, ctl[3 + ch], colb, g, segb, jb, colrel, Bp + ch * BPL,
                                     Eb + ch * EBN, cb, partb);
     for (int mi = 0; mi < wk.pad; ++mi) {
-      const int m0 = (wk.mt + mi) * TM, rowa = m0 + ra;
+      const int m0 = wk.mt + mi * TM, rowa = m0 + ra;
       float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
       for (int ch = 0; ch < nch; ++ch) {
         cut_a<S, TM, TPR, KPA, T_PAD>(slots + ch * TK, ctl[3 + ch], rowa, g.M, Ap, Ea, ra, parta);

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -848,32 +849,48 @@ static int upload_step(Step &st) {
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
   for (int g : order) {
     const Group &G = st.groups[g];
-    for (int mt = 0; mt * kTileFP64M < G.M; ++mt)
-      for (int nt = 0; nt * kTileFP64N < G.N; ++nt) w64.push_back({g, mt, nt, 0});
-    int tni = G.N <= 8 ? 0 : (G.N <= 16 ? 1 : (G.N <= 32 ? 2 : 3));
-    // 64-column tiles cut K in 64-slot chunks: a group with K <= 32 would
-    // leave half of every chunk empty, so it takes 32-column tiles (32-slot
-    // chunks, up to 128 rows) instead
-    if (tni == 3 && ktot[g] <= 32) tni = 2;
-    const int tn = 8 << tni;
-    int tmi = G.M <= 32 ? 0 : (G.M <= 64 ? 1 : 2);
-    if (tni == 3 && tmi == 2) tmi = 1;  // 64-column tiles: 32 or 64 rows (1024 threads at most)
-    const int tm = 32 << tmi;
-    auto &wl = wtc[tmi][tni];
-    const int nmt = (G.M + tm - 1) / tm, nnt = (G.N + tn - 1) / tn;
-    for (int mt = 0; mt < nmt; ++mt)
-      for (int nt = 0; nt < nnt; ++nt) wl.push_back({g, mt, nt, 0});
-    // B-resident kernel: 64 x 64 or 128 x 32 tiles, several row tiles, the
-    // whole K in one slot-table pass (at most 32 segments, K <= 192)
-    const int bres = (tmi == 1 && tni == 3) ? 0 : ((tmi == 2 && tni == 2) ? 1 : -1);
-    if (bres >= 0 && nmt >= 2 && G.nseg <= 32 && ktot[g] <= kBresMaxK) {
-      const int nruns = (nmt + kBresRun - 1) / kBresRun;
-      const int len = (nmt + nruns - 1) / nruns;
-      for (int nt = 0; nt < nnt; ++nt)
-        for (int mt = 0; mt < nmt; mt += len) wtcb[bres].push_back({g, mt, nt, std::min(len, nmt - mt)});
-    } else {
-      for (int mt = 0; mt < nmt; ++mt)
-        for (int nt = 0; nt < nnt; ++nt) wtc4[tmi][tni].push_back({g, mt, nt, 0});
+    for (int m0 = 0; m0 < G.M; m0 += kTileFP64M)
+      for (int n0 = 0; n0 < G.N; n0 += kTileFP64N) w64.push_back({g, m0, n0, 0});
+    // Tensor-core tiles.  Columns: full pieces of the widest tile, then one
+    // narrower tile for the rest (the smallest of 8/16/32/64 that holds it),
+    // so a group of 74 columns takes 64 + 16 instead of 64 + 64.  64-column
+    // tiles cut K in 64-slot chunks: a group with K <= 32 would leave half
+    // of every chunk empty, so it takes 32-column tiles (32-slot chunks)
+    // instead.  Rows: likewise with 128-row tiles (64 under 64-column tiles,
+    // 1024 threads at most) and a 32/64/128-row tile for the rest.
+    const int wmax = ktot[g] <= 32 ? 32 : 64;
+    for (int n0 = 0; n0 < G.N;) {
+      const int rem = G.N - n0;
+      const int tn = rem >= wmax ? wmax : (rem <= 8 ? 8 : (rem <= 16 ? 16 : (rem <= 32 ? 32 : 64)));
+      const int tni = tn == 8 ? 0 : (tn == 16 ? 1 : (tn == 32 ? 2 : 3));
+      const int hmax = tn == 64 ? 64 : 128;
+      std::vector<std::pair<int, int>> rows;  // (first row, tile height)
+      for (int m0 = 0; m0 < G.M;) {
+        const int rm = G.M - m0;
+        const int tm = rm >= hmax ? hmax : (rm <= 32 ? 32 : (rm <= 64 ? 64 : 128));
+        rows.push_back({m0, tm});
+        m0 += tm;
+      }
+      // B-resident kernel: 64 x 64 or 128 x 32 tiles, a run of at least two
+      // full-height row tiles, the whole K in one slot-table pass (at most
+      // 32 segments, K <= kBresMaxK)
+      const int bres = tn == 64 ? 0 : (tn == 32 ? 1 : -1);
+      size_t nfull = 0;
+      if (bres >= 0 && G.nseg <= 32 && ktot[g] <= kBresMaxK)
+        while (nfull < rows.size() && rows[nfull].second == hmax) ++nfull;
+      if (nfull < 2) nfull = 0;
+      if (nfull) {
+        const int nruns = (int)((nfull + kBresRun - 1) / kBresRun);
+        const int len = (int)((nfull + nruns - 1) / nruns);
+        for (int r = 0; r < (int)nfull; r += len)
+          wtcb[bres].push_back({g, rows[r].first, n0, std::min(len, (int)nfull - r)});
+      }
+      for (size_t r = 0; r < rows.size(); ++r) {
+        const int tmi = rows[r].second == 32 ? 0 : (rows[r].second == 64 ? 1 : 2);
+        wtc[tmi][tni].push_back({g, rows[r].first, n0, 0});
+        if (r >= nfull) wtc4[tmi][tni].push_back({g, rows[r].first, n0, 0});
+      }
+      n0 += tn;
     }
   }
   st.nwork_fp64 = (int64_t)w64.size();
@@ -1301,6 +1318,35 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
     P->flops += ch.ref_flops;
   }
   P->ws_elems = ws;
+  // Structurally zero intermediate blocks: an output block of an
+  // intermediate step whose every task reads such a block (or that has no
+  // task) is zero for any operand values.  It is neither written nor read:
+  // its works are dropped and so are the tasks that read it.  src_step[s] =
+  // the steps whose outputs step s reads as A and B (-1: a caller operand).
+  static const int src2[4][2] = {{-1, -1}, {-1, -1}, {1, 0}, {2, -1}};
+  static const int src1[3][2] = {{-1, -1}, {0, -1}, {1, -1}};
+  auto src_step = [&](int s, int which) { return d->ncsite == 2 ? src2[s][which] : src1[s][which]; };
+  std::vector<std::vector<std::vector<char>>> alive(d->nclass);
+  for (int c = 0; c < d->nclass; ++c) {
+    if (!chains[c].built) continue;
+    alive[c].resize(nstep);
+    for (int s = 0; s < nstep - 1; ++s) {
+      const Contraction *C = e->contractions[chains[c].c[s].contr].get();
+      const int sa = src_step(s, 0), sb = src_step(s, 1);
+      const size_t nob = C->task_start.size() - 1;
+      alive[c][s].assign(nob, 0);
+      for (size_t ob = 0; ob < nob; ++ob)
+        for (int64_t t = C->task_start[ob]; t < C->task_start[ob + 1]; ++t)
+          if ((sa < 0 || alive[c][sa][C->tasks[t].ab]) && (sb < 0 || alive[c][sb][C->tasks[t].bb])) {
+            alive[c][s][ob] = 1;
+            break;
+          }
+    }
+  }
+  auto live_task = [&](int c, int s, const Task &t) {
+    const int sa = src_step(s, 0), sb = src_step(s, 1);
+    return (sa < 0 || alive[c][sa][t.ab]) && (sb < 0 || alive[c][sb][t.bb]);
+  };
   // buffers: 0 L, 1 R, 2 W, 3 x, 4 y, 5 workspace
   // operand sources per executed step (two-site: O, T1, T3, sigma).  The
   // steps' task lists are independent: their output works are collected
@@ -1334,6 +1380,7 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
         src(op, true, abuf, abase);
         src(op, false, bbuf, bbase);
         for (size_t ob = 0; ob < O->pk->flat.size(); ++ob) {
+          if (!alive[d->op_class[op]][s][ob]) continue;
           OutWork w;
           w.lo = O;
           w.ob = (int32_t)ob;
@@ -1343,7 +1390,8 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
           // (two-site), so the sum over terms reads unscaled operands
           const double wgt = (d->ncsite == 2 && s == 0) ? d->wts[op] : 1.0;
           for (int64_t t = C->task_start[ob]; t < C->task_start[ob + 1]; ++t)
-            w.tasks.push_back({C, A, B, O, C->tasks[t].ab, C->tasks[t].bb, abase, bbase, abuf, bbuf, wgt});
+            if (live_task(d->op_class[op], s, C->tasks[t]))
+              w.tasks.push_back({C, A, B, O, C->tasks[t].ab, C->tasks[t].bb, abase, bbase, abuf, bbuf, wgt});
           works.push_back(std::move(w));
         }
       }
@@ -1367,8 +1415,9 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
         src(op, false, bbuf, bbase);
         for (size_t ob = 0; ob < O->pk->flat.size(); ++ob)
           for (int64_t t = C->task_start[ob]; t < C->task_start[ob + 1]; ++t)
-            works[ob].tasks.push_back({C, A, B, O, C->tasks[t].ab, C->tasks[t].bb, abase, bbase, abuf,
-                                       bbuf, d->ncsite == 2 ? 1.0 : d->wts[op]});
+            if (live_task(d->op_class[op], s, C->tasks[t]))
+              works[ob].tasks.push_back({C, A, B, O, C->tasks[t].ab, C->tasks[t].bb, abase, bbase, abuf,
+                                         bbuf, d->ncsite == 2 ? 1.0 : d->wts[op]});
       }
     }
   }
@@ -1614,6 +1663,23 @@ int zmpo_renorm_plan(zmpo_engine *e, const zmpo_renorm_desc *d, int *plan_id) {
   }
   P->out_total = tot;
   P->ws_elems = ws;
+  // structurally zero blocks of T1 and T2 (as in the sigma plan): step 1
+  // reads T1 as B, step 2 reads T2 as A
+  std::vector<std::array<std::vector<char>, 2>> alive(d->nclass);
+  for (int c = 0; c < d->nclass; ++c) {
+    if (!ch[c].built) continue;
+    const Contraction *C1 = e->contractions[ch[c].c1].get(), *C2 = e->contractions[ch[c].c2].get();
+    alive[c][0].assign(C1->task_start.size() - 1, 0);
+    for (size_t ob = 0; ob + 1 < C1->task_start.size(); ++ob)
+      alive[c][0][ob] = C1->task_start[ob + 1] > C1->task_start[ob];
+    alive[c][1].assign(C2->task_start.size() - 1, 0);
+    for (size_t ob = 0; ob + 1 < C2->task_start.size(); ++ob)
+      for (int64_t t = C2->task_start[ob]; t < C2->task_start[ob + 1]; ++t)
+        if (alive[c][0][C2->tasks[t].bb]) {
+          alive[c][1][ob] = 1;
+          break;
+        }
+  }
   // buffers: 0 env, 2 W, 3 site, 4 out, 5 workspace
   std::vector<std::vector<OutWork>> step_works(3);
   for (int s = 0; s < 3; ++s) {
@@ -1634,14 +1700,19 @@ int zmpo_renorm_plan(zmpo_engine *e, const zmpo_renorm_desc *d, int *plan_id) {
       } else {
         abuf = 5; abase = w2[op]; bbuf = 3; bbase = 0; cbuf = 4; cbase = P->out_off[op];
       }
+      P->flops += contraction_flops(e, C);
       for (size_t ob = 0; ob < O->pk->flat.size(); ++ob) {
+        if (s < 2 && !alive[c][s][ob]) continue;  // zero intermediate block
         OutWork w;
         w.lo = O;
         w.ob = (int32_t)ob;
         w.c_base = cbase;
         w.cbuf = cbuf;
-        for (int64_t t = C->task_start[ob]; t < C->task_start[ob + 1]; ++t)
-          w.tasks.push_back({C, A, B, O, C->tasks[t].ab, C->tasks[t].bb, abase, bbase, abuf, bbuf, 1.0});
+        for (int64_t t = C->task_start[ob]; t < C->task_start[ob + 1]; ++t) {
+          const Task &tk = C->tasks[t];
+          if ((s == 1 && !alive[c][0][tk.bb]) || (s == 2 && !alive[c][1][tk.ab])) continue;
+          w.tasks.push_back({C, A, B, O, tk.ab, tk.bb, abase, bbase, abuf, bbuf, 1.0});
+        }
         works.push_back(std::move(w));
       }
     }
@@ -1650,7 +1721,7 @@ int zmpo_renorm_plan(zmpo_engine *e, const zmpo_renorm_desc *d, int *plan_id) {
     int rc = build_steps_parallel(P.get(), step_works);
     if (rc) return rc;
     for (auto &st : P->steps) {
-      P->flops += st.flops;
+      P->exec_flops += st.flops;
       P->ntasks += st.ntasks;
     }
   }
