@@ -307,6 +307,18 @@ __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x) {
   lo += e;
 }
 
+// ldmatrix: four (two) 8x8 b16 matrices from shared memory in mma fragment
+// order; lane l gives the address of row l & 7 of matrix l >> 3 (16-byte
+// aligned rows)
+__device__ __forceinline__ void ldsm_x4(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(addr));
+}
+__device__ __forceinline__ void ldsm_x2(uint32_t addr, uint32_t &r0, uint32_t &r1) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0, %1}, [%2];\n" : "=r"(r0), "=r"(r1) : "r"(addr));
+}
+
 __device__ __forceinline__ void mma_bf16(float *c, const uint32_t *a, const uint32_t *b) {
   asm volatile(
       "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
@@ -519,23 +531,26 @@ __device__ __forceinline__ void mma_fold(const __nv_bfloat16 *Ap, const __nv_bfl
   for (int l = 0; l < S; ++l)
 #pragma unroll
     for (int i = 0; i < 4; ++i) acc[l][i] = 0.f;
+  // ldmatrix row addresses of this lane: lane l points at row l & 7 of 8x8
+  // matrix l >> 3.  A (x4): matrices (rows 0-7 | 8-15) x (k 0-7 | 8-15) in
+  // fragment order; B (x4 over two levels): (level sb | sb+1) x (k 0-7 | 8-15).
+  const int lane = gq * 4 + tq;
+  const uint32_t a_base = (uint32_t)__cvta_generic_to_shared(
+      Ap + (wm + (lane & 7) + ((lane >> 3) & 1) * 8) * T_PAD + (lane >> 4) * 8);
+  const uint32_t b_base = (uint32_t)__cvta_generic_to_shared(
+      Bp + ((lane >> 4) * TN + wn + (lane & 7)) * T_PAD + ((lane >> 3) & 1) * 8);
+  constexpr uint32_t A_LEVEL = TM * T_PAD * 2, B_LEVEL = TN * T_PAD * 2;  // bytes per plane
 #pragma unroll
   for (int kk = 0; kk < TK; kk += 16) {
     uint32_t bf[S][2];
 #pragma unroll
-    for (int sb = 0; sb < S; ++sb) {
-      const __nv_bfloat16 *bp = Bp + (sb * TN + wn + gq) * T_PAD + kk;
-      bf[sb][0] = *reinterpret_cast<const uint32_t *>(bp + 2 * tq);
-      bf[sb][1] = *reinterpret_cast<const uint32_t *>(bp + 2 * tq + 8);
-    }
+    for (int sb = 0; sb + 1 < S; sb += 2)
+      ldsm_x4(b_base + sb * B_LEVEL + kk * 2, bf[sb][0], bf[sb][1], bf[sb + 1][0], bf[sb + 1][1]);
+    if constexpr (S % 2 == 1) ldsm_x2(b_base + (S - 1) * B_LEVEL + kk * 2, bf[S - 1][0], bf[S - 1][1]);
 #pragma unroll
     for (int sa = 0; sa < S; ++sa) {
       uint32_t af[4];
-      const __nv_bfloat16 *ap = Ap + (sa * TM + wm) * T_PAD + kk;
-      af[0] = *reinterpret_cast<const uint32_t *>(ap + gq * T_PAD + 2 * tq);
-      af[1] = *reinterpret_cast<const uint32_t *>(ap + (gq + 8) * T_PAD + 2 * tq);
-      af[2] = *reinterpret_cast<const uint32_t *>(ap + gq * T_PAD + 2 * tq + 8);
-      af[3] = *reinterpret_cast<const uint32_t *>(ap + (gq + 8) * T_PAD + 2 * tq + 8);
+      ldsm_x4(a_base + sa * A_LEVEL + kk * 2, af[0], af[1], af[2], af[3]);
 #pragma unroll
       for (int sb = 0; sb + sa < S; ++sb) mma_bf16(acc[sa + sb], af, bf[sb]);
     }
