@@ -353,11 +353,12 @@ __device__ __forceinline__ double load_b_cb(const Slot &sl, const SegB *__restri
 // segment cur+l; the inclusive scan places every segment's k range in the
 // slot sequence, chunk c holding slots [c*TK, (c+1)*TK)).  A chunk may be
 // shorter than TK (end of the 32 segments a pass sees): sums are unchanged.
-// nslot[c] = slots of chunk c; *nchunk = chunks filled (0 = done).
+// nslot[c] = slots of chunk c; *nchunk = chunks filled (0 = done);
+// *scaled = some slot of the pass has a weight other than 1.
 template <int TK, int NCH>
 __device__ __forceinline__ void build_slots_multi(const Group &g, const Seg *__restrict__ segs,
                                                   const Bufs &bufs, Slot *slots, int *cursor,
-                                                  int *nslot, int *nchunk, int lane) {
+                                                  int *nslot, int *nchunk, int *scaled, int lane) {
   constexpr int CAP = TK * NCH;
   const int cur = cursor[0], curk = cursor[1];
   if (cur >= g.nseg) {
@@ -396,6 +397,7 @@ __device__ __forceinline__ void build_slots_multi(const Group &g, const Seg *__r
       sl.kk = kk;
     }
   }
+  const unsigned wscaled = __ballot_sync(0xffffffffu, avail > 0 && excl < CAP && sg.alpha != 1.0);
   const unsigned reach = __ballot_sync(0xffffffffu, incl >= CAP && avail > 0);
   const int total = __shfl_sync(0xffffffffu, incl, 31);
   const int lstop = reach ? (__ffs(reach) - 1) : -1;
@@ -422,6 +424,7 @@ __device__ __forceinline__ void build_slots_multi(const Group &g, const Seg *__r
     const int nch = (filled + TK - 1) / TK;
     for (int c = 0; c < nch; ++c) nslot[c] = min(TK, filled - c * TK);
     *nchunk = nch;
+    *scaled = wscaled != 0u;
   }
 }
 
@@ -454,10 +457,13 @@ struct TcShape {
 };
 
 // Cut of one chunk of A: TPR threads per row, KPA slots each; the row's
-// chunk exponent (max over its TPR threads) and its S digit planes.
+// chunk exponent (max over its TPR threads) and its S digit planes.  Slot
+// weights other than 1 are applied only in passes that have one (scaled is
+// the same for the whole CTA: the other passes issue no FP64 multiply -- the
+// FP64 pipe is narrow on GB300).
 template <int S, int TM, int TPR, int KPA, int T_PAD>
 __device__ __forceinline__ void cut_a(const Slot *slt, int ns, int rowa, int M, __nv_bfloat16 *Ap, int *Ea,
-                                      int ra, int parta) {
+                                      int ra, int parta, bool scaled) {
   double v[KPA];
   int emax = 0;
 #pragma unroll
@@ -467,11 +473,18 @@ __device__ __forceinline__ void cut_a(const Slot *slt, int ns, int rowa, int M, 
     if (j < ns && rowa < M) {
       const Slot &sl = slt[j];
       x = __ldg(sl.a + (int64_t)rowa * sl.sam);
-      if (sl.scaled) x *= sl.alpha;
     }
     v[t] = x;
-    emax = max(emax, dexp(x));
   }
+  if (scaled) {
+#pragma unroll
+    for (int t = 0; t < KPA; ++t) {
+      const int j = parta * KPA + t;
+      if (j < ns && slt[j].scaled) v[t] *= slt[j].alpha;
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < KPA; ++t) emax = max(emax, dexp(v[t]));
 #pragma unroll
   for (int o = 1; o < TPR; o <<= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
   if (parta == 0) Ea[ra] = emax;
@@ -595,7 +608,7 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
   int *Ea = reinterpret_cast<int *>(Bp + S * TN * T_PAD);           // [TM]
   int *Eb = Ea + TM;                                                // [TN]
   Slot *slots = reinterpret_cast<Slot *>(Eb + (TN < 16 ? 16 : TN));  // [NCH][TK] (Eb holds TN ints)
-  int *ctl = reinterpret_cast<int *>(slots + Sh::NCH * TK);  // cursor[2], nchunk, nslot[NCH]
+  int *ctl = reinterpret_cast<int *>(slots + Sh::NCH * TK);  // cursor[2], nchunk, nslot[NCH], scaled
 
   __shared__ int cbj[TN], cbrel[TN];  // column-block map of the tile
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -618,14 +631,16 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
     __syncthreads();
     const int jb = g.ncb ? cbj[cb] : -1, colrel = g.ncb ? cbrel[cb] : 0;
     while (true) {
-      if (warp == 0) build_slots_multi<TK, Sh::NCH>(g, segs, bufs, slots, ctl, ctl + 3, ctl + 2, lane);
+      if (warp == 0)
+        build_slots_multi<TK, Sh::NCH>(g, segs, bufs, slots, ctl, ctl + 3, ctl + 2, ctl + 3 + Sh::NCH, lane);
       __syncthreads();
       const int nch = ctl[2];
       if (nch == 0) break;
+      const bool scaled = ctl[3 + Sh::NCH] != 0;
       for (int ch = 0; ch < nch; ++ch) {
         const int ns = ctl[3 + ch];
         const Slot *slt = slots + ch * TK;
-        cut_a<S, TM, TPR, KPA, T_PAD>(slt, ns, rowa, g.M, Ap, Ea, ra, parta);
+        cut_a<S, TM, TPR, KPA, T_PAD>(slt, ns, rowa, g.M, Ap, Ea, ra, parta, scaled);
         cut_b<S, TN, TPC, KPB, T_PAD>(slt, ns, colb, g, segb, jb, colrel, Bp, Eb, cb, partb);
         __syncthreads();
         mma_fold<S, TM, TN, TK, T_PAD>(Ap, Bp, Ea, Eb, wm, wn, gq, tq, hi, lo);
@@ -655,7 +670,7 @@ struct TcbShape {
   static constexpr int EBN = TN < 16 ? 16 : TN;
   static constexpr size_t smem() {
     return (size_t)4 * TM * Sh::PAD * 2 + (size_t)CHB * 4 * TN * Sh::PAD * 2 + (size_t)TM * 4 +
-           (size_t)CHB * EBN * 4 + (size_t)CHB * Sh::TK * sizeof(Slot) + (3 + CHB) * 4 + 16;
+           (size_t)CHB * EBN * 4 + (size_t)CHB * Sh::TK * sizeof(Slot) + (4 + CHB) * 4 + 16;
   }
 };
 
@@ -676,7 +691,7 @@ k_step_tcb(const Work *__restrict__ work, int64_t nwork, const Group *__restrict
   int *Ea = reinterpret_cast<int *>(Bp + CHB * BPL);                // [TM]
   int *Eb = Ea + TM;                                                // [CHB][EBN]
   Slot *slots = reinterpret_cast<Slot *>(Eb + CHB * EBN);          // [CHB][TK]
-  int *ctl = reinterpret_cast<int *>(slots + CHB * TK);             // cursor[2], nchunk, nslot[CHB]
+  int *ctl = reinterpret_cast<int *>(slots + CHB * TK);             // cursor[2], nchunk, nslot[CHB], scaled
 
   __shared__ int cbj[TN], cbrel[TN];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -696,9 +711,10 @@ k_step_tcb(const Work *__restrict__ work, int64_t nwork, const Group *__restrict
     if (g.ncb) tile_cblocks(cbl, g, n0, TN, cbj, cbrel);
     __syncthreads();
     const int jb = g.ncb ? cbj[cb] : -1, colrel = g.ncb ? cbrel[cb] : 0;
-    if (warp == 0) build_slots_multi<TK, CHB>(g, segs, bufs, slots, ctl, ctl + 3, ctl + 2, lane);
+    if (warp == 0) build_slots_multi<TK, CHB>(g, segs, bufs, slots, ctl, ctl + 3, ctl + 2, ctl + 3 + CHB, lane);
     __syncthreads();
     const int nch = ctl[2];  // the planner routes only groups that one pass covers
+    const bool scaled = ctl[3 + CHB] != 0;
     for (int ch = 0; ch < nch; ++ch)
       cut_b<S, TN, TPC, KPB, T_PAD>(slots + ch * TK, ctl[3 + ch], colb, g, segb, jb, colrel, Bp + ch * BPL,
                                     Eb + ch * EBN, cb, partb);
@@ -706,7 +722,7 @@ k_step_tcb(const Work *__restrict__ work, int64_t nwork, const Group *__restrict
       const int m0 = wk.mt + mi * TM, rowa = m0 + ra;
       float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
       for (int ch = 0; ch < nch; ++ch) {
-        cut_a<S, TM, TPR, KPA, T_PAD>(slots + ch * TK, ctl[3 + ch], rowa, g.M, Ap, Ea, ra, parta);
+        cut_a<S, TM, TPR, KPA, T_PAD>(slots + ch * TK, ctl[3 + ch], rowa, g.M, Ap, Ea, ra, parta, scaled);
         __syncthreads();
         mma_fold<S, TM, TN, TK, T_PAD>(Ap, Bp + ch * BPL, Ea, Eb + ch * EBN, wm, wn, gq, tq, hi, lo);
         __syncthreads();
@@ -743,7 +759,7 @@ static int launch_tc_t(const Work *work, int64_t nwork, const Step &s, const Buf
   using Sh = TcShape<S, TM, TN>;
   const size_t smem = (size_t)S * (TM + TN) * Sh::PAD * sizeof(__nv_bfloat16) +
                       (size_t)(TM + (TN < 16 ? 16 : TN)) * sizeof(int) + Sh::NCH * Sh::TK * sizeof(Slot) +
-                      (3 + Sh::NCH) * sizeof(int) + 16;
+                      (4 + Sh::NCH) * sizeof(int) + 16;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_step_tc<S, TM, TN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
