@@ -220,32 +220,45 @@ __device__ __forceinline__ uint32_t aligned32(double x, int E) {
 }
 
 // byte k of X as the bit pattern of the float 2^23 + byte (PRMT), then the
-// exact float value of the byte (one FADD)
-template <int K>
+// exact float value of the byte minus OFF (one FADD)
+template <int K, int OFF>
 __device__ __forceinline__ float byte_to_float(uint32_t X) {
-  return __uint_as_float(__byte_perm(X, 0x4B000000u, 0x7440u | K)) - 8388608.0f;
+  return __uint_as_float(__byte_perm(X, 0x4B000000u, 0x7440u | K)) - (8388608.0f + (float)OFF);
 }
 
-// four digit planes of two neighbouring elements (same row, k and k+1) as
-// packed bf16 pairs: the bf16 of a byte-valued float is its upper half
+// S = 4 digits, balanced: the 31 most significant bits X of |x| aligned to
+// the chunk exponent E are written X = d0 2^24 + d1 2^16 + d2 2^8 + d3 with
+// d1..d3 in [-128, 127] and d0 in [0, 128]: Y = X + 0x808080 has the bytes
+// d1+128, d2+128, d3+128 and d0 on top (X < 2^31, so d0 <= 128).  Every
+// digit is an integer of magnitude <= 128 (exact in bf16); a digit product
+// is at most 2^14 in magnitude, so a level (at most four products per k)
+// stays exact in FP32 (< 2^24) for up to 256 slots.  The element's sign
+// flips every digit.
+__device__ __forceinline__ uint32_t balanced31(double x, int E) { return (aligned32(x, E) >> 1) + 0x808080u; }
+
+// bf16 digit planes of two neighbouring elements (same row, k and k+1) as
+// packed pairs: the bf16 of a small integer-valued float is its upper half
 __device__ __forceinline__ void digits4_pair(double x0, double x1, int E, uint32_t *d, int stride_u32) {
-  const uint32_t X0 = aligned32(x0, E), X1 = aligned32(x1, E);
+  const uint32_t Y0 = balanced31(x0, E), Y1 = balanced31(x1, E);
   const uint32_t sg = ((unsigned)__double2hiint(x0) >> 16 & 0x8000u) | ((unsigned)__double2hiint(x1) & 0x80000000u);
-  d[0] = __byte_perm(__float_as_uint(byte_to_float<3>(X0)), __float_as_uint(byte_to_float<3>(X1)), 0x7632u) | sg;
-  d[stride_u32] = __byte_perm(__float_as_uint(byte_to_float<2>(X0)), __float_as_uint(byte_to_float<2>(X1)), 0x7632u) | sg;
-  d[2 * stride_u32] = __byte_perm(__float_as_uint(byte_to_float<1>(X0)), __float_as_uint(byte_to_float<1>(X1)), 0x7632u) | sg;
-  d[3 * stride_u32] = __byte_perm(__float_as_uint(byte_to_float<0>(X0)), __float_as_uint(byte_to_float<0>(X1)), 0x7632u) | sg;
+  d[0] = __byte_perm(__float_as_uint(byte_to_float<3, 0>(Y0)), __float_as_uint(byte_to_float<3, 0>(Y1)), 0x7632u) ^ sg;
+  d[stride_u32] =
+      __byte_perm(__float_as_uint(byte_to_float<2, 128>(Y0)), __float_as_uint(byte_to_float<2, 128>(Y1)), 0x7632u) ^ sg;
+  d[2 * stride_u32] =
+      __byte_perm(__float_as_uint(byte_to_float<1, 128>(Y0)), __float_as_uint(byte_to_float<1, 128>(Y1)), 0x7632u) ^ sg;
+  d[3 * stride_u32] =
+      __byte_perm(__float_as_uint(byte_to_float<0, 128>(Y0)), __float_as_uint(byte_to_float<0, 128>(Y1)), 0x7632u) ^ sg;
 }
 
 // single element variant (one bf16 per plane)
 __device__ __forceinline__ void digits4_one(double x, int E, __nv_bfloat16 *d, int stride) {
-  const uint32_t X = aligned32(x, E);
+  const uint32_t Y = balanced31(x, E);
   const unsigned short sg = (unsigned short)((unsigned)__double2hiint(x) >> 16 & 0x8000u);
   unsigned short *u = reinterpret_cast<unsigned short *>(d);
-  u[0] = (unsigned short)(__float_as_uint(byte_to_float<3>(X)) >> 16) | sg;
-  u[stride] = (unsigned short)(__float_as_uint(byte_to_float<2>(X)) >> 16) | sg;
-  u[2 * stride] = (unsigned short)(__float_as_uint(byte_to_float<1>(X)) >> 16) | sg;
-  u[3 * stride] = (unsigned short)(__float_as_uint(byte_to_float<0>(X)) >> 16) | sg;
+  u[0] = (unsigned short)(__float_as_uint(byte_to_float<3, 0>(Y)) >> 16) ^ sg;
+  u[stride] = (unsigned short)(__float_as_uint(byte_to_float<2, 128>(Y)) >> 16) ^ sg;
+  u[2 * stride] = (unsigned short)(__float_as_uint(byte_to_float<1, 128>(Y)) >> 16) ^ sg;
+  u[3 * stride] = (unsigned short)(__float_as_uint(byte_to_float<0, 128>(Y)) >> 16) ^ sg;
 }
 
 // 2^k as a float for k in the float range (subnormal powers of two are exact;
@@ -435,12 +448,13 @@ __device__ __forceinline__ void build_slots_multi(const Group &g, const Seg *__r
 // to digit planes, digit products, scaled sums; three barriers.
 template <int S, int TM, int TN>
 struct TcShape {
-  // k slots per chunk.  A level sums at most S products of at most 255^2 per
-  // k, so S = 4 stays exact in FP32 (< 2^24) up to 64 slots and S = 7 up to
-  // 32.  The 64-column tiles (16 threads per row of A, 4 slots each) take
-  // 64-slot chunks with S = 4: half the barriers and level folds per k.  The
-  // narrower tiles keep 32 (64 slots there mean more registers per thread,
-  // measured slower).
+  // k slots per chunk.  S = 4 (balanced digits, |digit| <= 128, at most 4
+  // products per level and k) stays exact in FP32 (< 2^24) up to 256 slots;
+  // S = 7 (digits 0..255, at most 7 products) up to 32.  The 64-column tiles
+  // take 64-slot chunks with S = 4 (half the barriers and level folds per
+  // k); the narrower tiles keep 32 (64 slots there mean more registers per
+  // thread, measured slower).  128-slot chunks in 64 x 64 tiles measured
+  // slower too (more registers; the last chunk of a group wastes more).
   static constexpr int TK = (S == 4 && TN == 64) ? 64 : 32;
   static constexpr int PAD = TK + 8;          // bf16 per plane row in shared memory
   static constexpr int NCH = 8;               // chunks per slot-table pass (4, 8, 16 measured: 8 best)
@@ -533,12 +547,15 @@ __device__ __forceinline__ void cut_b(const Slot *slt, int ns, int colb, const G
   }
 }
 
-// Digit products of one chunk for this warp's m16 x n8 piece (exact in FP32
-// per level), then the levels scaled by 2^(Ea + Eb - 2044 - 8(l+2)) into the
-// two-float sums.
+// Digit products of one chunk of ns slots for this warp's m16 x n8 piece
+// (exact in FP32 per level; k steps past the chunk's slots are skipped), then
+// the levels scaled by 2^(Ea + Eb - 2044 - 8(l+2)) (S = 7) or
+// 2^(Ea + Eb - 2058 - 8l) (S = 4, 31-bit balanced digits) into the two-float
+// sums.
 template <int S, int TM, int TN, int TK, int T_PAD>
 __device__ __forceinline__ void mma_fold(const __nv_bfloat16 *Ap, const __nv_bfloat16 *Bp, const int *Ea,
-                                         const int *Eb, int wm, int wn, int gq, int tq, float *hi, float *lo) {
+                                         const int *Eb, int ns, int wm, int wn, int gq, int tq, float *hi,
+                                         float *lo) {
   float acc[S][4];
 #pragma unroll
   for (int l = 0; l < S; ++l)
@@ -555,6 +572,7 @@ __device__ __forceinline__ void mma_fold(const __nv_bfloat16 *Ap, const __nv_bfl
   constexpr uint32_t A_LEVEL = TM * T_PAD * 2, B_LEVEL = TN * T_PAD * 2;  // bytes per plane
 #pragma unroll
   for (int kk = 0; kk < TK; kk += 16) {
+    if (kk >= ns) break;  // the same for the whole CTA
     uint32_t bf[S][2];
 #pragma unroll
     for (int sb = 0; sb + 1 < S; sb += 2)
@@ -582,7 +600,7 @@ __device__ __forceinline__ void mma_fold(const __nv_bfloat16 *Ap, const __nv_bfl
       two_sum(acc[0][i], acc[1][i] * 0x1p-8f, h, e);
       e = fmaf(acc[2][i], 0x1p-16f, e);
       e = fmaf(acc[3][i], 0x1p-24f, e);
-      const float sc = pow2f(base - 16);
+      const float sc = pow2f(base - 14);  // 31-bit X: one more power of two than 32
       float s2, e2;
       two_sum(hi[i], h * sc, s2, e2);
       hi[i] = s2;
@@ -643,7 +661,7 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
         cut_a<S, TM, TPR, KPA, T_PAD>(slt, ns, rowa, g.M, Ap, Ea, ra, parta, scaled);
         cut_b<S, TN, TPC, KPB, T_PAD>(slt, ns, colb, g, segb, jb, colrel, Bp, Eb, cb, partb);
         __syncthreads();
-        mma_fold<S, TM, TN, TK, T_PAD>(Ap, Bp, Ea, Eb, wm, wn, gq, tq, hi, lo);
+        mma_fold<S, TM, TN, TK, T_PAD>(Ap, Bp, Ea, Eb, ns, wm, wn, gq, tq, hi, lo);
         __syncthreads();
       }
     }
@@ -666,7 +684,7 @@ k_step_tc(const Work *__restrict__ work, int64_t nwork, const Group *__restrict_
 template <int TM, int TN>
 struct TcbShape {
   using Sh = TcShape<4, TM, TN>;
-  static constexpr int CHB = 192 / Sh::TK;      // K up to 192
+  static constexpr int CHB = 256 / Sh::TK;      // K up to 256
   static constexpr int EBN = TN < 16 ? 16 : TN;
   static constexpr size_t smem() {
     return (size_t)4 * TM * Sh::PAD * 2 + (size_t)CHB * 4 * TN * Sh::PAD * 2 + (size_t)TM * 4 +
@@ -724,7 +742,8 @@ k_step_tcb(const Work *__restrict__ work, int64_t nwork, const Group *__restrict
       for (int ch = 0; ch < nch; ++ch) {
         cut_a<S, TM, TPR, KPA, T_PAD>(slots + ch * TK, ctl[3 + ch], rowa, g.M, Ap, Ea, ra, parta, scaled);
         __syncthreads();
-        mma_fold<S, TM, TN, TK, T_PAD>(Ap, Bp + ch * BPL, Ea, Eb + ch * EBN, wm, wn, gq, tq, hi, lo);
+        mma_fold<S, TM, TN, TK, T_PAD>(Ap, Bp + ch * BPL, Ea, Eb + ch * EBN, ctl[3 + ch], wm, wn, gq, tq, hi,
+                                       lo);
         __syncthreads();
       }
 #pragma unroll

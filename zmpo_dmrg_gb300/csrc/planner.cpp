@@ -749,9 +749,9 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
 
 // tile sizes of the two kernels (must match kernels.cu)
 constexpr int kTileFP64M = 32, kTileFP64N = 32;
-// B-resident kernel (kernels.cu, k_step_tcb): largest K it holds (three
-// 64-slot or six 32-slot chunks) and the row tiles of one work item
-constexpr int kBresMaxK = 192, kBresRun = 8;
+// B-resident kernel (kernels.cu, k_step_tcb): largest K it holds (four
+// 64-slot or eight 32-slot chunks) and the row tiles of one work item
+constexpr int kBresMaxK = 256, kBresRun = 16;
 
 // Cut groups whose summed K exceeds kSplitK into parts of about kSplitK (at
 // segment boundaries, or inside a long segment); parts go to scratch and a
