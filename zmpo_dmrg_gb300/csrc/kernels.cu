@@ -692,6 +692,18 @@ struct TcbShape {
   }
 };
 
+// Barrier of the NTH threads of one half of the CTA (ids 1, 2; id 0 is
+// __syncthreads): both halves run the same number of row-tile chunks, so
+// every half barrier is reached by all of its threads.
+__device__ __forceinline__ void bar_half(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// The CTA's two halves (512 threads each) take the upper and lower TM/2 rows
+// of each row tile against the same resident B planes, each with its own A
+// planes and its own barrier: the halves drift apart, so one half's digit
+// products overlap the other half's loads and cuts (the phases of a single
+// 1024-thread loop are otherwise in lockstep).
 template <int TM, int TN>
 __global__ void __launch_bounds__(TcShape<4, TM, TN>::NT, TcShape<4, TM, TN>::THREADS_SM / TcShape<4, TM, TN>::NT)
 k_step_tcb(const Work *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
@@ -700,23 +712,30 @@ k_step_tcb(const Work *__restrict__ work, int64_t nwork, const Group *__restrict
   constexpr int S = 4;
   using Sh = TcShape<S, TM, TN>;
   using Bh = TcbShape<TM, TN>;
-  constexpr int TPR = Sh::TPR, KPA = Sh::KPA, TPC = Sh::TPC, KPB = Sh::KPB;
+  constexpr int TPC = Sh::TPC, KPB = Sh::KPB;
   constexpr int TK = Sh::TK, T_PAD = Sh::PAD, CHB = Bh::CHB, EBN = Bh::EBN;
   constexpr int BPL = S * TN * T_PAD;  // bf16 per chunk of B planes
+  // one half: TMH rows, NTH threads, warps WMH x WN of m16 x n8 pieces
+  constexpr int TMH = TM / 2, NTH = Sh::NT / 2, WMH = TMH / 16;
+  constexpr int TPRH = NTH / TMH, KPAH = TK / TPRH;
+  static_assert(WMH * Sh::WN * 32 == NTH && TPRH * KPAH == TK && TPRH <= 32, "half shape");
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __nv_bfloat16 *Ap = reinterpret_cast<__nv_bfloat16 *>(smem_raw);  // [S][TM][PAD]
+  __nv_bfloat16 *Ap = reinterpret_cast<__nv_bfloat16 *>(smem_raw);  // [2][S][TMH][PAD]
   __nv_bfloat16 *Bp = Ap + S * TM * T_PAD;                          // [CHB][S][TN][PAD]
-  int *Ea = reinterpret_cast<int *>(Bp + CHB * BPL);                // [TM]
+  int *Ea = reinterpret_cast<int *>(Bp + CHB * BPL);                // [2][TMH]
   int *Eb = Ea + TM;                                                // [CHB][EBN]
   Slot *slots = reinterpret_cast<Slot *>(Eb + CHB * EBN);          // [CHB][TK]
   int *ctl = reinterpret_cast<int *>(slots + CHB * TK);             // cursor[2], nchunk, nslot[CHB], scaled
 
   __shared__ int cbj[TN], cbrel[TN];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = (warp % Sh::WM) * 16, wn = (warp / Sh::WM) * 8;
+  const int half = tid / NTH, tidh = tid % NTH, warph = tidh >> 5;
+  const int wm = (warph % WMH) * 16, wn = (warph / WMH) * 8;
   const int gq = lane >> 2, tq = lane & 3;
-  const int ra = tid / TPR, parta = tid % TPR;
+  const int ra = tidh / TPRH, parta = tidh % TPRH;
   const int cb = tid / TPC, partb = tid % TPC;
+  __nv_bfloat16 *Aph = Ap + half * S * TMH * T_PAD;
+  int *Eah = Ea + half * TMH;
 
   for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
     const Work wk = work[w];
@@ -736,15 +755,16 @@ k_step_tcb(const Work *__restrict__ work, int64_t nwork, const Group *__restrict
     for (int ch = 0; ch < nch; ++ch)
       cut_b<S, TN, TPC, KPB, T_PAD>(slots + ch * TK, ctl[3 + ch], colb, g, segb, jb, colrel, Bp + ch * BPL,
                                     Eb + ch * EBN, cb, partb);
+    __syncthreads();  // B planes of every chunk ready for both halves
     for (int mi = 0; mi < wk.pad; ++mi) {
-      const int m0 = wk.mt + mi * TM, rowa = m0 + ra;
+      const int m0 = wk.mt + mi * TM + half * TMH, rowa = m0 + ra;
       float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
       for (int ch = 0; ch < nch; ++ch) {
-        cut_a<S, TM, TPR, KPA, T_PAD>(slots + ch * TK, ctl[3 + ch], rowa, g.M, Ap, Ea, ra, parta, scaled);
-        __syncthreads();
-        mma_fold<S, TM, TN, TK, T_PAD>(Ap, Bp + ch * BPL, Ea, Eb + ch * EBN, ctl[3 + ch], wm, wn, gq, tq, hi,
-                                       lo);
-        __syncthreads();
+        cut_a<S, TMH, TPRH, KPAH, T_PAD>(slots + ch * TK, ctl[3 + ch], rowa, g.M, Aph, Eah, ra, parta, scaled);
+        bar_half(1 + half, NTH);
+        mma_fold<S, TMH, TN, TK, T_PAD>(Aph, Bp + ch * BPL, Eah, Eb + ch * EBN, ctl[3 + ch], wm, wn, gq, tq,
+                                        hi, lo);
+        bar_half(1 + half, NTH);
       }
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
