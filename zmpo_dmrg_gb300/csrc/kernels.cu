@@ -692,18 +692,20 @@ struct TcbShape {
   }
 };
 
-// Barrier of the NTH threads of one half of the CTA (ids 1, 2; id 0 is
-// __syncthreads): both halves run the same number of row-tile chunks, so
-// every half barrier is reached by all of its threads.
-__device__ __forceinline__ void bar_half(int id, int nthreads) {
+// Barrier of the NTH threads of one part of the CTA (ids 1 .. NPART; id 0 is
+// __syncthreads): all parts run the same number of row-tile chunks, so every
+// part barrier is reached by all of its threads.
+__device__ __forceinline__ void bar_part(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-// The CTA's two halves (512 threads each) take the upper and lower TM/2 rows
-// of each row tile against the same resident B planes, each with its own A
-// planes and its own barrier: the halves drift apart, so one half's digit
-// products overlap the other half's loads and cuts (the phases of a single
-// 1024-thread loop are otherwise in lockstep).
+// The CTA's NPART parts (256 threads each) take TM/NPART rows of each row
+// tile against the same resident B planes, each with its own A planes and
+// its own barrier: the parts drift apart, so one part's digit products
+// overlap another part's loads and cuts (the phases of a single 1024-thread
+// loop are otherwise in lockstep).  2 parts: -3 % sigma time, 4: -7 %.
+constexpr int NPART = 4;
+
 template <int TM, int TN>
 __global__ void __launch_bounds__(TcShape<4, TM, TN>::NT, TcShape<4, TM, TN>::THREADS_SM / TcShape<4, TM, TN>::NT)
 k_step_tcb(const Work *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
@@ -715,27 +717,27 @@ k_step_tcb(const Work *__restrict__ work, int64_t nwork, const Group *__restrict
   constexpr int TPC = Sh::TPC, KPB = Sh::KPB;
   constexpr int TK = Sh::TK, T_PAD = Sh::PAD, CHB = Bh::CHB, EBN = Bh::EBN;
   constexpr int BPL = S * TN * T_PAD;  // bf16 per chunk of B planes
-  // one half: TMH rows, NTH threads, warps WMH x WN of m16 x n8 pieces
-  constexpr int TMH = TM / 2, NTH = Sh::NT / 2, WMH = TMH / 16;
+  // one of NPART parts: TMH rows, NTH threads, warps WMH x WN of m16 x n8 pieces
+  constexpr int TMH = TM / NPART, NTH = Sh::NT / NPART, WMH = TMH / 16;
   constexpr int TPRH = NTH / TMH, KPAH = TK / TPRH;
-  static_assert(WMH * Sh::WN * 32 == NTH && TPRH * KPAH == TK && TPRH <= 32, "half shape");
+  static_assert(WMH * Sh::WN * 32 == NTH && TPRH * KPAH == TK && TPRH <= 32, "part shape");
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __nv_bfloat16 *Ap = reinterpret_cast<__nv_bfloat16 *>(smem_raw);  // [2][S][TMH][PAD]
+  __nv_bfloat16 *Ap = reinterpret_cast<__nv_bfloat16 *>(smem_raw);  // [NPART][S][TMH][PAD]
   __nv_bfloat16 *Bp = Ap + S * TM * T_PAD;                          // [CHB][S][TN][PAD]
-  int *Ea = reinterpret_cast<int *>(Bp + CHB * BPL);                // [2][TMH]
+  int *Ea = reinterpret_cast<int *>(Bp + CHB * BPL);                // [NPART][TMH]
   int *Eb = Ea + TM;                                                // [CHB][EBN]
   Slot *slots = reinterpret_cast<Slot *>(Eb + CHB * EBN);          // [CHB][TK]
   int *ctl = reinterpret_cast<int *>(slots + CHB * TK);             // cursor[2], nchunk, nslot[CHB], scaled
 
   __shared__ int cbj[TN], cbrel[TN];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int half = tid / NTH, tidh = tid % NTH, warph = tidh >> 5;
+  const int part = tid / NTH, tidh = tid % NTH, warph = tidh >> 5;
   const int wm = (warph % WMH) * 16, wn = (warph / WMH) * 8;
   const int gq = lane >> 2, tq = lane & 3;
   const int ra = tidh / TPRH, parta = tidh % TPRH;
   const int cb = tid / TPC, partb = tid % TPC;
-  __nv_bfloat16 *Aph = Ap + half * S * TMH * T_PAD;
-  int *Eah = Ea + half * TMH;
+  __nv_bfloat16 *Aph = Ap + part * S * TMH * T_PAD;
+  int *Eah = Ea + part * TMH;
 
   for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
     const Work wk = work[w];
@@ -755,16 +757,16 @@ k_step_tcb(const Work *__restrict__ work, int64_t nwork, const Group *__restrict
     for (int ch = 0; ch < nch; ++ch)
       cut_b<S, TN, TPC, KPB, T_PAD>(slots + ch * TK, ctl[3 + ch], colb, g, segb, jb, colrel, Bp + ch * BPL,
                                     Eb + ch * EBN, cb, partb);
-    __syncthreads();  // B planes of every chunk ready for both halves
+    __syncthreads();  // B planes of every chunk ready for all parts
     for (int mi = 0; mi < wk.pad; ++mi) {
-      const int m0 = wk.mt + mi * TM + half * TMH, rowa = m0 + ra;
+      const int m0 = wk.mt + mi * TM + part * TMH, rowa = m0 + ra;
       float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
       for (int ch = 0; ch < nch; ++ch) {
         cut_a<S, TMH, TPRH, KPAH, T_PAD>(slots + ch * TK, ctl[3 + ch], rowa, g.M, Aph, Eah, ra, parta, scaled);
-        bar_half(1 + half, NTH);
+        bar_part(1 + part, NTH);
         mma_fold<S, TMH, TN, TK, T_PAD>(Aph, Bp + ch * BPL, Eah, Eb + ch * EBN, ctl[3 + ch], wm, wn, gq, tq,
                                         hi, lo);
-        bar_half(1 + half, NTH);
+        bar_part(1 + part, NTH);
       }
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
