@@ -351,3 +351,33 @@ def test_sigma_task_lists_compute_the_oracle_sigma():
     ref = oracle_sigma(P, x)
     assert numpy.linalg.norm(y - ref) <= 1e-12 * numpy.linalg.norm(ref)
     eng.destroy_plan(pid)
+
+
+def test_sigma_plan_key_is_structural():
+    """Sigma plans are reused across sweeps by a content key: equal for
+    environments of the same block structure and offsets (new buffers),
+    different when any structure, offset or the wavefunction layout differs."""
+    from types import SimpleNamespace
+    from zmpo_dmrg_gb300.mpo_dmrg_kernel import EnvSet, _sigma_key
+    qa = numpy.array([[0, 0], [1, .5], [1, -.5]], dtype=float)
+    qb = numpy.array([[0, 0], [1, .5]], dtype=float)
+
+    def tens(q, d):
+        t = pq([True, False, True])
+        t.fromQsyms(3, [q, q, q], [d, d, d], ifallocate=False)
+        return t
+
+    def env(d, off1=7):
+        t = tens(qa, d)
+        return EnvSet(None, [0, off1, -1], [t.layout] * 3, [t, t, None])
+
+    psi = tens(qb, [2, 3])
+    dmrg = SimpleNamespace(mpo_store=SimpleNamespace(uid=1), ifs2proj=False, nops=3, qkey=[2.0, 0.0],
+                           hpwts=numpy.ones(3), qtmp=psi)
+    k0 = _sigma_key(dmrg, 1, 2, env([1, 2, 2]), env([3, 1, 1]))
+    assert k0 == _sigma_key(dmrg, 1, 2, env([1, 2, 2]), env([3, 1, 1]))      # new EnvSets, same structure
+    assert k0 != _sigma_key(dmrg, 1, 2, env([1, 2, 3]), env([3, 1, 1]))      # a sector dimension
+    assert k0 != _sigma_key(dmrg, 1, 2, env([1, 2, 2], 8), env([3, 1, 1]))   # an offset
+    assert k0 != _sigma_key(dmrg, 2, 2, env([1, 2, 2]), env([3, 1, 1]))      # the dot
+    dmrg.qtmp = tens(qb, [2, 4])
+    assert k0 != _sigma_key(dmrg, 1, 2, env([1, 2, 2]), env([3, 1, 1]))      # the wavefunction layout

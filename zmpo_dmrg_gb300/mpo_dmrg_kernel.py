@@ -14,6 +14,8 @@ Vectors may be NumPy (copied to and from the device) or float64 CUDA tensors
 (kept on the device).  Every product runs in the engine; there is no host
 fallback.
 """
+import collections
+import hashlib
 import itertools
 
 import numpy
@@ -76,9 +78,24 @@ def _flip_layout(dmrg, t):
     return lid
 
 
+def _shared_workspace(dmrg, nelem):
+    """The sigma plans of one driver run one after the other on one stream:
+    they share one workspace buffer, grown on demand (cached plans hold none)."""
+    torch = _torch()
+    buf = dmrg.__dict__.get("_sigma_ws")
+    if buf is None or buf.numel() < nelem:
+        dmrg._sigma_ws = None
+        buf = torch.empty(nelem, dtype=torch.float64, device="cuda")
+        dmrg._sigma_ws = buf
+    return buf[:nelem]
+
+
 class SigmaPlan:
+    released = False
+
     def __init__(self, dmrg, isite, ncsite, fL, fR):
         from .mpo import op_class
+        self.dmrg = dmrg
         eng = _engine.get()
         mpo = dmrg.mpo_store
         ops = [iop for iop in range(dmrg.nops) if fL.present(iop) and fR.present(iop)]
@@ -143,11 +160,20 @@ class SigmaPlan:
             nb *= 2
         self.pids = pids
         self.pid = pids[0]
-        self.workspace = torch.empty(max(max(wss) // 8, 1), dtype=torch.float64, device="cuda")
+        self.ws_elems = max(max(wss) // 8, 1)
         stats = [eng.plan_stats(pid) for pid in pids]
         self.flops = sum(x[0] for x in stats)
         self.ntasks = sum(x[1] for x in stats)
         self.nlaunch = stats[0][2]
+        self.fL, self.fR = fL, fR
+        self.graphs = {}
+
+    @property
+    def workspace(self):
+        return _shared_workspace(self.dmrg, self.ws_elems)
+
+    def rebind(self, fL, fR):
+        """Reuse for environments of the same structure (new device buffers)."""
         self.fL, self.fR = fL, fR
         self.graphs = {}
 
@@ -181,6 +207,8 @@ class SigmaPlan:
             return
         torch = _torch()
         rec = self.graphs.get(precision)
+        if rec is not None and rec[3] != self.workspace.data_ptr():
+            rec = None  # the shared workspace was reallocated since the recording
         if rec is None:
             xs = torch.empty_like(x)
             ys = torch.empty_like(y)
@@ -191,9 +219,9 @@ class SigmaPlan:
             graph = torch.cuda.CUDAGraph()
             with torch.cuda.graph(graph):
                 eng.sigma(self.pid, self.fL.buf, self.fR.buf, W, xs, ys, self.workspace, precision)
-            rec = (graph, xs, ys)
+            rec = (graph, xs, ys, self.workspace.data_ptr())
             self.graphs[precision] = rec
-        graph, xs, ys = rec
+        graph, xs, ys, _ = rec
         xs.copy_(x)
         graph.replay()
         y.copy_(ys)
@@ -209,6 +237,7 @@ class SigmaPlan:
                 d += tmp
 
     def release(self):
+        self.released = True
         self.graphs = {}
         if self.pid is not None:
             for pid in self.pids:
@@ -217,17 +246,65 @@ class SigmaPlan:
             self.pids = []
 
 
+def _qt_signature(h, t):
+    h.update(numpy.asarray(t.status, dtype=numpy.int8).tobytes())
+    for q, d in zip(t.qsyms, t.ndims):
+        q = numpy.ascontiguousarray(q, dtype=numpy.float64)
+        d = numpy.ascontiguousarray(d, dtype=numpy.int64)
+        h.update(numpy.int64(q.size).tobytes())
+        h.update(q.tobytes())
+        h.update(numpy.int64(d.size).tobytes())
+        h.update(d.tobytes())
+
+
+def _sigma_key(dmrg, isite, ncsite, fL, fR):
+    """Content key of a sigma plan: everything its task lists depend on (the
+    dot, the MPO and its term weights, the target label, the wavefunction
+    block structure, the block structures and offsets of every environment).
+    Equal keys give identical plans, so a later sweep that meets the same
+    structures at a dot reuses the plan with the new environment buffers."""
+    h = hashlib.blake2b(digest_size=24)
+    h.update(repr((isite, ncsite, dmrg.mpo_store.uid, bool(dmrg.ifs2proj), dmrg.nops,
+                   getattr(dmrg, "workspace_budget", None))).encode())
+    h.update(numpy.ascontiguousarray(dmrg.qkey, dtype=numpy.float64).tobytes())
+    h.update(numpy.ascontiguousarray(dmrg.hpwts, dtype=numpy.float64).tobytes())
+    _qt_signature(h, dmrg.qtmp)
+    for env in (fL, fR):
+        off = numpy.asarray(env.off, dtype=numpy.int64)
+        h.update(off.tobytes())
+        for iop in numpy.nonzero(off >= 0)[0]:
+            _qt_signature(h, env.tensors[iop])
+    return h.digest()
+
+
+# cached sigma plans per driver: at most this many block tasks in total
+# (the plans' device task lists; their workspace is shared)
+_SIGMA_CACHE_TASKS = 60_000_000
+
+
 def _sigma_plan(info):
     dmrg, isite, ncsite, flst, status, ifsym = info
     fL, fR = flst[0][0:2]
-    key = (fL.uid, fR.uid, isite, ncsite, dmrg.qtmp_psi_layout, dmrg.mpo_store.uid)
+    fast = (fL.uid, fR.uid, isite, ncsite, dmrg.qtmp_psi_layout, dmrg.mpo_store.uid,
+            getattr(dmrg, "workspace_budget", None))
     cur = getattr(dmrg, "_sigma_plan", None)
-    if cur is None or cur[0] != key:
-        if cur is not None:
-            cur[1].release()
-        cur = (key, SigmaPlan(dmrg, isite, ncsite, fL, fR))
-        dmrg._sigma_plan = cur
-    return cur[1]
+    if cur is not None and cur[0] == fast and not cur[1].released:
+        return cur[1]
+    key = _sigma_key(dmrg, isite, ncsite, fL, fR)
+    cache = dmrg.__dict__.setdefault("_sigma_cache", collections.OrderedDict())
+    plan = cache.pop(key, None)
+    if plan is None or plan.released:
+        plan = SigmaPlan(dmrg, isite, ncsite, fL, fR)
+    else:
+        plan.rebind(fL, fR)
+    cache[key] = plan
+    total = sum(getattr(p, "ntasks", 0) for p in cache.values())
+    while total > _SIGMA_CACHE_TASKS and len(cache) > 1:
+        _, old = cache.popitem(last=False)
+        total -= getattr(old, "ntasks", 0)
+        old.release()
+    dmrg._sigma_plan = (fast, plan)
+    return plan
 
 
 def HVec(vec0, info, ndim0, prjmap):
