@@ -342,7 +342,6 @@ def HDiag(info, ndim0, prjmap):
 def renorm(dmrg, isite, ncsite, flst, flstN, site, status):
     """New environments of every operator term after the site update; the
     result EnvSet is stored in ``flstN[0][0]`` (a one-element list)."""
-    from .mpo import op_class
     eng = _engine.get()
     torch = _torch()
     mpo = dmrg.mpo_store
@@ -357,37 +356,58 @@ def renorm(dmrg, isite, ncsite, flst, flstN, site, status):
         fE = flst[0][1]
         jsite = isite + ncsite - 1
     ops = [iop for iop in range(dmrg.nops) if fE.present(iop)]
-    classes = {}
-    op_cls, lay_env, lay_W, off_env, off_W = [], [], [], [], []
-    for iop in ops:
-        c0 = op_class(dmrg.opers[iop][0], jsite)
-        if c0 not in classes:
-            classes[c0] = len(classes)
-            lay_env.append(fE.layouts[iop])
-            wt = mpo.tensors[jsite][iop]
-            if status == 'L':
-                lay_W.append(wt.layout)
-            else:
-                st = wt.status.copy()
-                st[0], st[1] = not st[0], not st[1]
-                lay_W.append(eng.derive(wt.layout, [-wt.qsyms[0], -wt.qsyms[1], wt.qsyms[2],
-                                                    wt.qsyms[3]], st))
-        op_cls.append(classes[c0])
-        off_env.append(fE.off[iop])
-        off_W.append(mpo.off[jsite][iop])
     nop = dmrg.nops
-    off = numpy.full(nop, -1, dtype=numpy.int64)
-    lays = numpy.full(nop, -1, dtype=numpy.int64)
-    tens = [None] * nop
     if not ops:
         buf = torch.zeros(1, dtype=torch.float64, device="cuda")
+        flstN[0][0] = EnvSet(buf, numpy.full(nop, -1, dtype=numpy.int64), numpy.full(nop, -1, dtype=numpy.int64),
+                             [None] * nop)
     else:
-        pid, lay_out, off_out, total, ws = eng.renorm_plan(status, op_cls, lay_env, lay_W,
-                                                           qsite.layout, off_env, off_W)
-        buf = torch.empty(max(total, 1), dtype=torch.float64, device="cuda")
-        work = torch.empty(max(ws // 8, 1), dtype=torch.float64, device="cuda")
+        rp = _renorm_plan(dmrg, status, jsite, fE, qsite, ops)
+        buf = torch.empty(max(rp.total, 1), dtype=torch.float64, device="cuda")
+        work = torch.empty(max(rp.ws // 8, 1), dtype=torch.float64, device="cuda")
         sval, _ = _to_device(qsite.value)
-        eng.renorm(pid, fE.buf, mpo.buf, sval, buf, work, getattr(dmrg, "precision_renorm", "fp64"))
+        eng.renorm(rp.pid, fE.buf, mpo.buf, sval, buf, work, getattr(dmrg, "precision_renorm", "fp64"))
+        flstN[0][0] = EnvSet(buf, rp.off.copy(), rp.lays.copy(), list(rp.tens))
+    if dmrg.ifs2proj:
+        from .spinproj import renorm_S00
+        renorm_S00(dmrg, isite, ncsite, flst, flstN, site, status)
+    return 0
+
+
+class RenormPlan:
+    """A renormalisation plan and the host structure of its outputs (block
+    structure and offset of every term's new environment)."""
+    released = False
+
+    def __init__(self, dmrg, status, jsite, fE, qsite, ops):
+        from .mpo import op_class
+        eng = _engine.get()
+        mpo = dmrg.mpo_store
+        classes = {}
+        op_cls, lay_env, lay_W, off_env, off_W = [], [], [], [], []
+        for iop in ops:
+            c0 = op_class(dmrg.opers[iop][0], jsite)
+            if c0 not in classes:
+                classes[c0] = len(classes)
+                lay_env.append(fE.layouts[iop])
+                wt = mpo.tensors[jsite][iop]
+                if status == 'L':
+                    lay_W.append(wt.layout)
+                else:
+                    st = wt.status.copy()
+                    st[0], st[1] = not st[0], not st[1]
+                    lay_W.append(eng.derive(wt.layout, [-wt.qsyms[0], -wt.qsyms[1], wt.qsyms[2],
+                                                        wt.qsyms[3]], st))
+            op_cls.append(classes[c0])
+            off_env.append(fE.off[iop])
+            off_W.append(mpo.off[jsite][iop])
+        nop = dmrg.nops
+        self.off = numpy.full(nop, -1, dtype=numpy.int64)
+        self.lays = numpy.full(nop, -1, dtype=numpy.int64)
+        self.tens = [None] * nop
+        self.pid, lay_out, off_out, self.total, self.ws = eng.renorm_plan(status, op_cls, lay_env, lay_W,
+                                                                          qsite.layout, off_env, off_W)
+        self.ntasks = eng.plan_stats(self.pid)[1]
         # host structure of each output (layout id per class)
         struct = {}
         for k, iop in enumerate(ops):
@@ -397,15 +417,40 @@ def renorm(dmrg, isite, ncsite, flst, flstN, site, status):
             if c not in struct:
                 struct[c] = _env_structure(dmrg, status, qsite, mpo.tensors[jsite][iop], fE.tensors[iop],
                                            int(lay_out[c]))
-            off[iop] = off_out[k]
-            lays[iop] = struct[c].layout
-            tens[iop] = struct[c]
-        eng.destroy_plan(pid)
-    flstN[0][0] = EnvSet(buf, off, lays, tens)
-    if dmrg.ifs2proj:
-        from .spinproj import renorm_S00
-        renorm_S00(dmrg, isite, ncsite, flst, flstN, site, status)
-    return 0
+            self.off[iop] = off_out[k]
+            self.lays[iop] = struct[c].layout
+            self.tens[iop] = struct[c]
+
+    def release(self):
+        if not self.released:
+            self.released = True
+            _engine.get().destroy_plan(self.pid)
+
+
+def _renorm_plan(dmrg, status, jsite, fE, qsite, ops):
+    """Renormalisation plan for this site update, reused when a later sweep
+    meets the same structures (key: the side, the site, the MPO, the site
+    tensor's block structure and the block structures and offsets of the
+    environments it extends)."""
+    h = hashlib.blake2b(digest_size=24)
+    h.update(repr((status, jsite, dmrg.mpo_store.uid, bool(dmrg.ifs2proj), dmrg.nops)).encode())
+    _qt_signature(h, qsite)
+    off = numpy.asarray(fE.off, dtype=numpy.int64)
+    h.update(off.tobytes())
+    for iop in ops:
+        _qt_signature(h, fE.tensors[iop])
+    key = h.digest()
+    cache = dmrg.__dict__.setdefault("_renorm_cache", collections.OrderedDict())
+    rp = cache.pop(key, None)
+    if rp is None or rp.released:
+        rp = RenormPlan(dmrg, status, jsite, fE, qsite, ops)
+    cache[key] = rp
+    total = sum(p.ntasks for p in cache.values())
+    while total > _SIGMA_CACHE_TASKS and len(cache) > 1:
+        _, old = cache.popitem(last=False)
+        total -= old.ntasks
+        old.release()
+    return rp
 
 
 def SVec(vec0, info, ndim0, prjmap):
