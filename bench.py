@@ -501,7 +501,8 @@ def main():
         "gpu_launches": args.steps * sum(eng.kernel_count(pid, args.precision) for pid in plan.pids),
         "clocks": clocks_rec,
         "launches": launches,
-        "roofline": {"bound": "hbm", "kernel": "k_step_tc (all tile shapes) of step %d of %d" % (top, plan.nlaunch),
+        "roofline": {"bound": "hbm", "kernel": "tensor-core kernels (k_step_tcb, k_step_tc) of step %d of %d" %
+                               (top, plan.nlaunch),
                      "achieved": launches[top]["GBs"], "peak": hbm, "unit": "GB/s",
                      "frac": (launches[top]["GBs"] or 0.0) / hbm,
                      "traffic": (T3_TRAFFIC_RATIO * launches[top]["alg_bytes"] / len(plan.pids)
