@@ -38,11 +38,12 @@ LARGE_WORKSPACE = 64e9
 # points (320 terms [p, g]), H.psi with the N-only relabelling
 SPCFG = dict(K=20, nelec=20, D=512, isite=9, seed=2024, npts=8, sval=0.0)
 # DRAM bytes (read + write) over algorithmic bytes of the T3 step, measured
-# with ncu (dram__bytes_read.sum + dram__bytes_write.sum of every launch in
-# the step's NVTX range) on the K=16, D=256 two-site dot: 1.890 GB against
-# 1.934 GB.  The full-size traffic is this ratio times the step's algorithmic
-# bytes (the step's traffic grows with the operand and output sizes).
-T3_TRAFFIC_RATIO = 1.890 / 1.934
+# with ncu (dram__bytes_read.sum + dram__bytes_write.sum of every split-path
+# launch in the step's NVTX range, 18 executions) on the K=16, D=256 two-site
+# dot: 2.334 GB per execution against 1.930 GB algorithmic.  The full-size
+# traffic is this ratio times the step's algorithmic bytes (the step's traffic
+# grows with the operand and output sizes).
+T3_TRAFFIC_RATIO = 2.334 / 1.930
 METRIC = "sweep s & sigma-vec TFLOP/s, split-BF16 vs FP64 on 1 GB300 at ΔE≤1e-8 Eh"
 
 
