@@ -358,25 +358,6 @@ static void rowmajor_strides(const int64_t *d, int r, int64_t *st) {
   }
 }
 
-// merge adjacent legs (outer first) when contiguous in both operands
-static std::vector<Leg2> merge_legs(const std::vector<Leg2> &in) {
-  std::vector<Leg2> out;
-  for (const auto &l : in) {
-    if (l.d == 1) continue;
-    if (!out.empty()) {
-      Leg2 &o = out.back();
-      if (o.s0 == l.d * l.s0 && o.s1 == l.d * l.s1) {
-        o.d *= l.d;
-        o.s0 = l.s0;
-        o.s1 = l.s1;
-        continue;
-      }
-    }
-    out.push_back(l);
-  }
-  return out;
-}
-
 // Expand all output works of one launch into groups / segments.
 constexpr int64_t kSplitK = 2048;
 
