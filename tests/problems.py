@@ -364,3 +364,32 @@ def product_sdiag(P):
     from zmpo_dmrg_gb300.mpo_dmrg_kernel import SDiag
     m = P.p
     return SDiag([m, P.isite, 2, m.flst, 'L', True], P.ndim0, None).cpu().numpy()
+
+
+def b_resident_tiles(P):
+    """Column tiles of the problem's sigma plan that the planner gives to the
+    B-resident kernel (its rule: 64-column tiles over two or more 64-row
+    tiles, or 32-column tiles over two or more 128-row tiles, K <= 256 in at
+    most 32 segments).  Reads the task lists before the plan's first run."""
+    from zmpo_dmrg_gb300 import engine as E
+    from zmpo_dmrg_gb300.mpo_dmrg_kernel import _sigma_plan
+    m = P.p
+    plan = _sigma_plan([m, P.isite, 2, m.flst, 'L', True])
+    eng = E.get()
+    n = 0
+    for pid in plan.pids:
+        for st in range(plan.nlaunch):
+            G, Sg, _, _ = eng.step_tasks(pid, st)
+            cs = numpy.concatenate([[0], numpy.cumsum(Sg['K'].astype(numpy.int64))])
+            kt = cs[G['seg0'] + G['nseg']] - cs[G['seg0']]
+            for M, N, k, ns in zip(G['M'], G['N'], kt, G['nseg']):
+                wmax = 32 if k <= 32 else 64
+                n0 = 0
+                while n0 < N:
+                    rem = N - n0
+                    tn = wmax if rem >= wmax else (8 if rem <= 8 else 16 if rem <= 16 else 32 if rem <= 32 else 64)
+                    hmax = 64 if tn == 64 else 128
+                    if tn in (32, 64) and ns <= 32 and k <= 256 and M // hmax >= 2:
+                        n += 1
+                    n0 += tn
+    return n

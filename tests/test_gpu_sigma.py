@@ -7,7 +7,7 @@ import pytest
 
 from tests.problems import (random_problem, oracle_sigma, product_sigma, oracle_hdiag,
                             product_hdiag, oracle_renorm, product_renorm, oracle_prdm,
-                            product_prdm)
+                            product_prdm, b_resident_tiles)
 
 pytestmark = pytest.mark.gpu
 
@@ -44,6 +44,21 @@ def test_sigma_split(gpu, case, precision, tol):
     P = prob(case)
     x = numpy.random.default_rng(8).standard_normal(P.ndim0)
     assert rel(product_sigma(P, x, precision), oracle_sigma(P, x)) < tol
+
+
+# large enough that whole groups span several 64-row tiles: the B-resident
+# kernel (k_step_tcb, four independent parts) carries most of T1 and T3
+BRES_CASE = dict(K=10, nelec=10, D=128, isite=4, seed=7)
+
+
+def test_sigma_b_resident_kernel(gpu):
+    P = prob(BRES_CASE)
+    assert b_resident_tiles(P) > 100
+    x = numpy.random.default_rng(12).standard_normal(P.ndim0)
+    ref = oracle_sigma(P, x)
+    assert rel(product_sigma(P, x, "fp64"), ref) < 1e-10
+    assert rel(product_sigma(P, x, "split"), ref) < 1e-8
+    assert rel(product_sigma(P, x, "emu64"), ref) < 1e-10
 
 
 @pytest.mark.parametrize("case", CASES)
