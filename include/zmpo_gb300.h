@@ -150,6 +150,11 @@ int zmpo_plan_step_tasks(zmpo_engine *e, int plan_id, int step, int64_t *counts,
  * precision (grouped GEMM launches per tile shape plus split-K sums).  No
  * reference counterpart: it reports what the engine will launch. */
 int zmpo_plan_kernel_count(zmpo_engine *e, int plan_id, int precision, int *count);
+/* Multiply-adds the tiles of each step issue at this precision (tile padding
+ * included, a group's K rounded up to 16), macs[step] for step < nmax; the
+ * tensor-core paths issue 10 (split) or 28 (emu64) digit products per
+ * multiply-add.  No reference counterpart: the roofline of the executed work. */
+int zmpo_plan_mma_macs(zmpo_engine *e, int plan_id, int precision, int nmax, double *macs);
 /* y = H x (ndim0 = size of lay_psi).  d_x, d_y device vectors. */
 int zmpo_sigma(zmpo_engine *e, int plan_id, const double *d_L,
                const double *d_R, const double *d_W, const double *d_x,

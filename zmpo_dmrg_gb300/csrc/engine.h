@@ -93,6 +93,10 @@ struct Step {
   int64_t nwork_tcb[2] = {};
   int64_t nwork_tc4[3][4] = {};
   double flops = 0.0;            // sum of 2*m*n*k of the reference tasks
+  // multiply-adds the tiles of the step issue (tile padding included, K of a
+  // group rounded up to the 16-slot MMA step): FP64 tiles, 4-slice and
+  // 7-slice tensor-core tiles (times the digit products per multiply-add)
+  double mma_macs[3] = {0.0, 0.0, 0.0};
   int64_t ntasks = 0;
   bool uploaded = false;         // device copies are made on first use
   std::vector<Reduction> reds;   // split-K reductions (host)

@@ -828,10 +828,15 @@ static int upload_step(Step &st) {
     ktot[g] = k;
   }
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  st.mma_macs[0] = st.mma_macs[1] = st.mma_macs[2] = 0.0;
   for (int g : order) {
     const Group &G = st.groups[g];
+    const double k16 = (double)((ktot[g] + 15) / 16 * 16);
     for (int m0 = 0; m0 < G.M; m0 += kTileFP64M)
-      for (int n0 = 0; n0 < G.N; n0 += kTileFP64N) w64.push_back({g, m0, n0, 0});
+      for (int n0 = 0; n0 < G.N; n0 += kTileFP64N) {
+        w64.push_back({g, m0, n0, 0});
+        st.mma_macs[0] += (double)kTileFP64M * kTileFP64N * k16;
+      }
     // Tensor-core tiles.  Columns: full pieces of the widest tile, then one
     // narrower tile for the rest (the smallest of 8/16/32/64 that holds it),
     // so a group of 74 columns takes 64 + 16 instead of 64 + 64.  64-column
@@ -870,6 +875,9 @@ static int upload_step(Step &st) {
         const int tmi = rows[r].second == 32 ? 0 : (rows[r].second == 64 ? 1 : 2);
         wtc[tmi][tni].push_back({g, rows[r].first, n0, 0});
         if (r >= nfull) wtc4[tmi][tni].push_back({g, rows[r].first, n0, 0});
+        const double macs = (double)rows[r].second * tn * k16;
+        st.mma_macs[1] += macs;  // the same tiles, B-resident or not
+        st.mma_macs[2] += macs;
       }
       n0 += tn;
     }
@@ -1535,6 +1543,20 @@ int zmpo_plan_kernel_count(zmpo_engine *e, int plan_id, int precision, int *coun
     n += s.red_elems > 0;
   }
   *count = n;
+  return ZMPO_OK;
+}
+
+int zmpo_plan_mma_macs(zmpo_engine *e, int plan_id, int precision, int nmax, double *macs) {
+  Plan *P = get_plan(e, plan_id, 0);
+  if (!P) return fail(ZMPO_E_ID, "plan_mma_macs: unknown plan");
+  if (!macs || nmax < 0) return fail(ZMPO_E_ARG, "plan_mma_macs: bad output");
+  const int which = precision == ZMPO_PREC_FP64 ? 0 : (precision == ZMPO_PREC_SPLIT ? 1 : 2);
+  for (int i = 0; i < nmax; ++i) macs[i] = 0.0;
+  for (size_t i = 0; i < P->steps.size(); ++i) {
+    int rc = upload_step(P->steps[i]);
+    if (rc) return rc;
+    if ((int)i < nmax) macs[i] = P->steps[i].mma_macs[which];
+  }
   return ZMPO_OK;
 }
 

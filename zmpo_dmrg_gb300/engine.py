@@ -143,6 +143,12 @@ class Engine:
               "plan_kernel_count")
         return n.value
 
+    def mma_macs(self, pid, precision="split", nmax=8):
+        """Multiply-adds the tiles of each step issue at ``precision``."""
+        macs = numpy.zeros(nmax)
+        check(_lib.lib().zmpo_plan_mma_macs(self.h, pid, _lib.PREC[precision], nmax, dptr(macs)), "plan_mma_macs")
+        return macs
+
     def profile(self, on=True):
         check(_lib.lib().zmpo_profile(self.h, 1 if on else 0), "profile")
 
