@@ -374,11 +374,15 @@ struct MergeInfo {
 
 static void merge_column_blocks(Step &st, const std::vector<MergeInfo> &info) {
   std::unordered_map<std::string, std::vector<int>> buckets;
-  std::vector<int> order_keys;
   for (size_t g = 0; g < st.groups.size(); ++g)
     if (info[g].ok) buckets[info[g].key].push_back((int)g);
+  bool any = false;
+  for (const auto &kv : buckets) any = any || kv.second.size() >= 2;
+  if (!any) return;  // nothing to join: the groups stay as they are
   std::vector<Group> groups;
   std::vector<Seg> segs;
+  groups.reserve(st.groups.size());
+  segs.reserve(st.segs.size());
   std::vector<char> done(st.groups.size(), 0);
   auto emit_plain = [&](int gi) {
     Group g = st.groups[gi];
