@@ -61,6 +61,8 @@ struct Packing {
   std::vector<int64_t> flat;     // allowed blocks, ascending flat index
   std::vector<int64_t> off;      // packed offset of each allowed block
   std::vector<int32_t> lookup;   // flat -> ordinal, -1 if not allowed
+  std::vector<int32_t> bsec;     // [ordinal][leg] sector of each allowed block
+  std::vector<int64_t> bdim;     // [ordinal][leg] dimension of each allowed block
 };
 
 struct Layout {
@@ -87,47 +89,79 @@ struct Layout {
     for (int j = 0; j < rank; ++j) f = f * nsec[j] + sec[j];
     return f;
   }
+  // sectors and dimensions of an allowed block (tables made with the packing)
+  void block_sectors(int64_t ord, int *sec) const {
+    const int32_t *p = pk->bsec.data() + (size_t)ord * rank;
+    for (int j = 0; j < rank; ++j) sec[j] = p[j];
+  }
   void block_dims(int64_t ord, int64_t *d) const {
-    int sec[16];
-    sectors(pk->flat[ord], sec);
-    for (int j = 0; j < rank; ++j) d[j] = dim[j][sec[j]];
+    const int64_t *p = pk->bdim.data() + (size_t)ord * rank;
+    for (int j = 0; j < rank; ++j) d[j] = p[j];
   }
 };
 
-// allowed iff sum_k |sum_{status 0} q_k - sum_{status 1} q_k| < 1e-10
+// allowed iff sum_k |sum_{status 0} q_k - sum_{status 1} q_k| < 1e-10.
+// Blocks are visited in ascending flat order by an odometer over legs
+// 0 .. rank-2 that keeps the signed charge sums and the dimension products of
+// the leading legs (accumulated leg by leg in the same order as a direct sum,
+// so the test is bit-for-bit the direct one), with the last leg innermost.
+// The sectors and dimensions of every allowed block are tabulated.
 static void build_packing(Layout &L) {
   auto pk = std::make_shared<Packing>();
   int64_t nb = 1;
   for (int j = 0; j < L.rank; ++j) nb *= L.nsec[j];
   pk->nblks = nb;
   pk->lookup.assign((size_t)nb, -1);
-  std::vector<int> sec(L.rank, 0);
-  std::vector<double> diff(L.nq);
-  int64_t off = 0;
-  for (int64_t f = 0; f < nb; ++f) {
-    if (L.rank > 0) {
-      int64_t t = f;
-      for (int j = L.rank - 1; j >= 0; --j) {
-        sec[j] = (int)(t % L.nsec[j]);
-        t /= L.nsec[j];
+  const int R = L.rank, nq = L.nq;
+  if (R == 0) {
+    pk->lookup[0] = 0;
+    pk->flat.push_back(0);
+    pk->off.push_back(0);
+    pk->size = 1;
+    L.pk = pk;
+    return;
+  }
+  for (int j = 0; j < R; ++j)
+    if (L.nsec[j] == 0) {
+      L.pk = pk;
+      return;
+    }
+  std::vector<int> sec(R, 0);
+  std::vector<double> part((size_t)R * nq, 0.0);  // part[j] = signed charge sum of legs < j
+  std::vector<int64_t> dprod(R, 1);               // dprod[j] = dimension product of legs < j
+  auto set_leg = [&](int j) {  // part[j+1], dprod[j+1] from leg j's sector
+    const double sg = L.status[j] ? -1.0 : 1.0;
+    const double *qq = &L.q[j][(size_t)sec[j] * nq];
+    for (int k = 0; k < nq; ++k) part[(size_t)(j + 1) * nq + k] = part[(size_t)j * nq + k] + sg * qq[k];
+    dprod[j + 1] = dprod[j] * L.dim[j][sec[j]];
+  };
+  for (int j = 0; j + 1 < R; ++j) set_leg(j);
+  const int last = R - 1;
+  const double sgl = L.status[last] ? -1.0 : 1.0;
+  int64_t f = 0, off = 0;
+  while (true) {
+    const double *pre = &part[(size_t)last * nq];
+    for (int s = 0; s < L.nsec[last]; ++s, ++f) {
+      const double *qq = &L.q[last][(size_t)s * nq];
+      double dtot = 0.0;
+      for (int k = 0; k < nq; ++k) dtot += std::fabs(pre[k] + sgl * qq[k]);
+      if (dtot < 1e-10) {
+        pk->lookup[(size_t)f] = (int32_t)pk->flat.size();
+        pk->flat.push_back(f);
+        pk->off.push_back(off);
+        off += dprod[last] * L.dim[last][s];
+        for (int j = 0; j < last; ++j) {
+          pk->bsec.push_back(sec[j]);
+          pk->bdim.push_back(L.dim[j][sec[j]]);
+        }
+        pk->bsec.push_back(s);
+        pk->bdim.push_back(L.dim[last][s]);
       }
     }
-    std::fill(diff.begin(), diff.end(), 0.0);
-    for (int j = 0; j < L.rank; ++j) {
-      const double *qq = &L.q[j][(size_t)sec[j] * L.nq];
-      double sg = L.status[j] ? -1.0 : 1.0;
-      for (int k = 0; k < L.nq; ++k) diff[k] += sg * qq[k];
-    }
-    double dtot = 0.0;
-    for (int k = 0; k < L.nq; ++k) dtot += std::fabs(diff[k]);
-    if (dtot < 1e-10) {
-      int64_t n = 1;
-      for (int j = 0; j < L.rank; ++j) n *= L.dim[j][sec[j]];
-      pk->lookup[(size_t)f] = (int32_t)pk->flat.size();
-      pk->flat.push_back(f);
-      pk->off.push_back(off);
-      off += n;
-    }
+    int j = last - 1;
+    while (j >= 0 && ++sec[j] == L.nsec[j]) sec[j--] = 0;
+    if (j < 0) break;
+    for (int t = j; t < last; ++t) set_leg(t);
   }
   pk->size = off;
   L.pk = pk;
@@ -286,7 +320,7 @@ static int build_contraction(zmpo_engine *e, int ia, int ib, int naxes, const in
   {
     int sec[16];
     for (size_t ob = 0; ob < A->pk->flat.size(); ++ob) {
-      A->sectors(A->pk->flat[ob], sec);
+      A->block_sectors((int64_t)ob, sec);
       int64_t ef = 0, inf = 0;
       for (int j : C->e1) ef = ef * A->nsec[j] + sec[j];
       for (int j : C->i1) inf = inf * A->nsec[j] + sec[j];
@@ -298,7 +332,7 @@ static int build_contraction(zmpo_engine *e, int ia, int ib, int naxes, const in
   int osec[16], bsec[16], isec[16];
   for (size_t ob = 0; ob < O->pk->flat.size(); ++ob) {
     C->task_start[ob] = (int64_t)C->tasks.size();
-    O->sectors(O->pk->flat[ob], osec);
+    O->block_sectors((int64_t)ob, osec);
     int64_t ef = 0;
     for (int t = 0; t < ne1; ++t) ef = ef * A->nsec[C->e1[t]] + osec[t];
     auto it = amap.find(ef);
@@ -601,7 +635,7 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
     mi.ok = nsub == 1 && !w.tasks.empty();
     if (mi.ok) {
       int sec[16];
-      O.sectors(O.pk->flat[w.ob], sec);
+      O.block_sectors(w.ob, sec);
       const auto &t0 = w.tasks[0];
       // binary key: output layout, A tensor (layout, buffer, base), output
       // buffer, M and the row-leg sectors
@@ -1426,7 +1460,7 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
   {
     int psec[16];
     for (size_t ob = 0; ob < Psi->pk->flat.size(); ++ob) {
-      Psi->sectors(Psi->pk->flat[ob], psec);
+      Psi->block_sectors((int64_t)ob, psec);
       DiagBlock db;
       db.out_off = Psi->pk->off[ob];
       db.dl = (int32_t)Psi->dim[0][psec[0]];
