@@ -401,13 +401,39 @@ constexpr int64_t kSplitK = 2048;
 // each (segment, column block) pair keeps its own B part, or none.  Only
 // groups made of one region with one segment per task take part, and only
 // while the joined K stays below the split-K length.
+// Key of the A rows an output block reads: output layout, A tensor (layout,
+// buffer, base), output buffer, M and the row-leg sectors (fixed size, no
+// heap allocation per group).
+struct MergeKey {
+  int64_t w[6 + 16];
+  int n = 0;
+  bool operator==(const MergeKey &o) const {
+    if (n != o.n) return false;
+    for (int i = 0; i < n; ++i)
+      if (w[i] != o.w[i]) return false;
+    return true;
+  }
+};
+struct MergeKeyHash {
+  size_t operator()(const MergeKey &k) const {
+    uint64_t h = 0x9e3779b97f4a7c15ull ^ (uint64_t)k.n;
+    for (int i = 0; i < k.n; ++i) {
+      uint64_t x = (uint64_t)k.w[i] + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
+      x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+      x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+      h ^= x ^ (x >> 31);
+    }
+    return (size_t)h;
+  }
+};
 struct MergeInfo {
   bool ok = false;
-  std::string key;
+  MergeKey key;
 };
 
 static void merge_column_blocks(Step &st, const std::vector<MergeInfo> &info) {
-  std::unordered_map<std::string, std::vector<int>> buckets;
+  std::unordered_map<MergeKey, std::vector<int>, MergeKeyHash> buckets;
+  buckets.reserve(st.groups.size());
   for (size_t g = 0; g < st.groups.size(); ++g)
     if (info[g].ok) buckets[info[g].key].push_back((int)g);
   bool any = false;
@@ -637,9 +663,7 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
       int sec[16];
       O.block_sectors(w.ob, sec);
       const auto &t0 = w.tasks[0];
-      // binary key: output layout, A tensor (layout, buffer, base), output
-      // buffer, M and the row-leg sectors
-      int64_t kw[8 + 16];
+      int64_t *kw = mi.key.w;
       kw[0] = (int64_t)(intptr_t)w.lo;
       kw[1] = (int64_t)(intptr_t)t0.la;
       kw[2] = t0.abuf;
@@ -647,7 +671,7 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
       kw[4] = t0.a_base;
       kw[5] = M;
       for (int j = 0; j < ne1; ++j) kw[6 + j] = sec[j];
-      mi.key.assign(reinterpret_cast<const char *>(kw), (size_t)(6 + ne1) * sizeof(int64_t));
+      mi.key.n = 6 + ne1;
       for (auto &t : w.tasks)
         if (t.la != t0.la || t.abuf != t0.abuf || t.a_base != t0.a_base) mi.ok = false;
     }
