@@ -6,16 +6,18 @@
 // arithmetic paths share the task lists:
 //
 //   k_step_fp64   FP64 FMA on the CUDA cores (reference arithmetic).
-//   k_step_split  FP64 operands cut into S exact 8-bit digit planes per
-//                 K-chunk (a shared power-of-two scale per row of A and per
-//                 column of B, Ozaki-style), digit products on the BF16
+//   k_step_tc     the split path: FP64 operands cut into S exact digit planes
+//   k_step_tcb    per K-chunk (a shared power-of-two scale per row of A and
+//                 per column of B, Ozaki-style), digit products on the BF16
 //                 tensor cores (mma.sync m16n8k16, FP32 accumulate, exact:
 //                 every per-level sum stays below 2^24), per-chunk results
 //                 scaled by powers of two and summed in a two-float (hi+lo)
 //                 accumulator on the FP32 pipes; FP64 only for the final
-//                 store.  S = 4 keeps pairs s+t <= 5 (10 products, ~2^-32
-//                 relative to the row/column maximum); S = 7 keeps 28
-//                 products (~2^-56).
+//                 store.  S = 4 (balanced digits of 31 bits, |digit| <= 128)
+//                 keeps the level pairs s+t <= 3 (10 products, ~2^-31
+//                 relative to the row/column maximum); S = 7 (unsigned
+//                 bytes) keeps 28 products (~2^-56).  k_step_tcb is the
+//                 B-resident variant for groups whose K fits one pass.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -165,14 +167,14 @@ int launch_step_fp64(const Step &s, const Bufs &b, void *stream) {
 }
 
 // ------------------------------------------------------- split (tensor core)
-// Tile: 128 rows (one thread per row of A) x TN (8 or 16) columns, K packed
-// in chunks of 32 slots: consecutive segments of the group fill the slots of
-// a chunk (a short block product does not waste a whole chunk).  Per chunk:
-// shared power-of-two scale per row of A / column of B over the chunk, S
-// exact 8-bit digit planes in shared memory, digit products per level on the
-// BF16 tensor cores (exact in FP32: level sums < 2^24), level sums scaled and
-// added to a two-float accumulator.  Integer->float conversions stay 32-bit:
-// 64-bit conversions issue on the FP64 pipe, which is narrow on GB300.
+// Tiles of TM x TN outputs (TcShape), K packed in chunks of TK slots:
+// consecutive segments of the group fill the slots of a chunk (a short block
+// product does not waste a whole chunk).  Per chunk: shared power-of-two
+// scale per row of A / column of B over the chunk, S exact digit planes in
+// shared memory, digit products per level on the BF16 tensor cores (exact in
+// FP32: level sums < 2^24), level sums scaled and added to a two-float
+// accumulator.  Integer->float conversions stay 32-bit: 64-bit conversions
+// issue on the FP64 pipe, which is narrow on GB300.
 
 // biased exponent of a double (0 for zero / denormal)
 __device__ __forceinline__ int dexp(double x) {
@@ -184,8 +186,8 @@ __device__ __forceinline__ float small_u2f(unsigned d) {
   return __uint_as_float(0x4B000000u | d) - 8388608.0f;
 }
 
-// S signed 8-bit digits of |x| / 2^(E-1022), most significant first, packed
-// as bf16 (exact: |digit| <= 255).
+// S = 7: S unsigned 8-bit digits of |x| / 2^(E-1022), most significant
+// first, the element's sign on each, packed as bf16 (exact: |digit| <= 255).
 template <int S>
 __device__ __forceinline__ void digits_bf16(double x, int E, __nv_bfloat16 *d, int stride) {
   const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
@@ -209,9 +211,8 @@ __device__ __forceinline__ void digits_bf16(double x, int E, __nv_bfloat16 *d, i
 }
 
 // S = 4: the 32 most significant bits of |x|'s significand aligned to the
-// chunk exponent E (E >= exponent of x), truncated -- the same bits the
-// 64-bit path keeps -- using 32-bit integer operations only.  Its four bytes
-// are the four digits, most significant first.
+// chunk exponent E (E >= exponent of x), truncated, using 32-bit integer
+// operations only (balanced31 below recodes its top 31 bits into digits).
 __device__ __forceinline__ uint32_t aligned32(double x, int E) {
   const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
   const int e = (int)((hi >> 20) & 0x7ffu);
