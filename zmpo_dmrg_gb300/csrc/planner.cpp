@@ -1313,7 +1313,7 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
     ClassChain &ch = chains[c];
     if (ch.built) continue;
     ch.built = true;
-    int lo, ci, rc, l1, c1;
+    int lo = -1, ci = -1, rc = 0, l1 = -1, c1 = -1;
     rc = build_contraction(e, d->lay_L[c], d->lay_psi, 1, ax1a, ax1b, &l1, &c1);
     if (rc) return rc;
     ch.ref_flops += contraction_flops(e, e->contractions[c1].get());
