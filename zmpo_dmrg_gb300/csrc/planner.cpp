@@ -1217,7 +1217,7 @@ int zmpo_contract_plan(zmpo_engine *e, int lay_a, int lay_b, int naxes, const in
                        const int *axes_b, int *lay_out, int *plan_id) {
   if (!e || !lay_out || !plan_id || naxes < 0 || (naxes > 0 && (!axes_a || !axes_b)))
     return fail(ZMPO_E_ARG, "contract_plan: bad arguments");
-  int lo, ci;
+  int lo = -1, ci = -1;
   const size_t c0 = e->contractions.size(), l0 = e->layouts.size();
   int rc = build_contraction(e, lay_a, lay_b, naxes, axes_a, axes_b, &lo, &ci);
   if (rc) return rc;
