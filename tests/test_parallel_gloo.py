@@ -5,7 +5,6 @@ import os
 import socket
 
 import numpy
-import pytest
 
 from zmpo_dmrg_gb300.parallel import partition_sites, partition_ops
 

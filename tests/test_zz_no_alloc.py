@@ -8,7 +8,6 @@ a row and checks both results against the regular ``zmpo_contract_exec`` on
 the same plan, for the FP64 and the split tensor-core path, and checks that a
 plan needing more scratch than the array holds is refused.  This file is
 collected last so that a failure here does not stop the other tests."""
-import ctypes
 
 import numpy
 import pytest
