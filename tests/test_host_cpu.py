@@ -381,3 +381,55 @@ def test_sigma_plan_key_is_structural():
     assert k0 != _sigma_key(dmrg, 2, 2, env([1, 2, 2]), env([3, 1, 1]))      # the dot
     dmrg.qtmp = tens(qb, [2, 4])
     assert k0 != _sigma_key(dmrg, 1, 2, env([1, 2, 2]), env([3, 1, 1]))      # the wavefunction layout
+
+
+def test_transposed_builder_equals_autograd_of_the_builder():
+    """The energy gradient's chain rule (adjoint.integral_gradients: the
+    transposed MPO builder, the site tensors being linear in the integrals)
+    equals torch autograd through the builder, and the exact change of the
+    linear functional sum_j,p <G_p(j), W_p(j)(h, g)> along a random direction."""
+    import torch
+    from zmpo_dmrg_gb300.mpo_dmrg_class import mpo_dmrg
+    from zmpo_dmrg_gb300 import adjoint
+    K = 5
+    m = mpo_dmrg(seed=1)
+    m.nsite, m.sbas, m.isym = K, 2 * K, 2
+    m.build()
+    m.partition()
+    h, eri, _ = pint.synthetic(K, 3)
+    i1, i2 = pint.spin_orbital(h, eri)
+    rng = numpy.random.default_rng(0)
+    grads = [[None] * m.nops for _ in range(K)]
+    for j in range(K):
+        for iop in range(m.nops):
+            if rng.random() < 0.8:
+                W = pm.hp_spatial_site(m.opers[iop], m.sbas, j, i1[m.pidx], i2[m.pidx], None, m.pdic)
+                grads[j][iop] = rng.standard_normal(W.shape)
+    a1, a2 = adjoint.integral_gradients(m, h, eri, grads)
+    hh = torch.tensor(h, requires_grad=True)
+    gg = torch.tensor(eri, requires_grad=True)
+    t1, t2 = adjoint.spin_orbital_torch(hh, gg)
+    t1, t2 = t1[m.pidx], t2[m.pidx]
+    tot = torch.zeros((), dtype=torch.float64)
+    for j in range(K):
+        for iop in range(m.nops):
+            if grads[j][iop] is not None:
+                W = pm.hp_spatial_site(m.opers[iop], m.sbas, j, t1, t2, None, m.pdic)
+                tot = tot + (W * torch.from_numpy(grads[j][iop])).sum()
+    tot.backward()
+    assert numpy.allclose(a1, hh.grad.numpy(), rtol=1e-13, atol=1e-13)
+    assert numpy.allclose(a2, gg.grad.numpy(), rtol=1e-13, atol=1e-13)
+
+    def energy(hv, ev):
+        j1, j2 = pint.spin_orbital(hv, ev)
+        return sum(float((pm.hp_spatial_site(m.opers[iop], m.sbas, j, j1[m.pidx], j2[m.pidx], None, m.pdic)
+                          * grads[j][iop]).sum())
+                   for j in range(K) for iop in range(m.nops) if grads[j][iop] is not None)
+    dh = rng.standard_normal(h.shape)
+    dh = dh + dh.T
+    de = rng.standard_normal(eri.shape)
+    de = de + de.transpose(1, 0, 2, 3)
+    de = de + de.transpose(0, 1, 3, 2)
+    de = de + de.transpose(2, 3, 0, 1)
+    change = energy(h + dh, eri + de) - energy(h, eri)
+    assert abs(change - float((a1 * dh).sum() + (a2 * de).sum())) <= 1e-12 * abs(change)

@@ -9,9 +9,10 @@ every MPO site tensor W_p(j), so
 with L and R the environments of the same MPS (exact for any gauge: the
 left-canonical sites of the last sweep serve for both sides).  These site
 gradients are engine contractions (three per term and site, block-sparse,
-FP64 on the GPU); the chain rule through the MPO construction and the
-spin-orbital expansion of the integrals is the torch autograd of the same
-builder (``mpo.hp_spatial_site`` with torch tensors).  ``EnergyGradient`` is
+FP64 on the GPU); the chain rule through the MPO construction is the
+transposed builder (``mpo.hp_spatial_site_adjoint``: every site tensor is
+linear in the integrals) and through the spin-orbital expansion of the
+integrals torch autograd.  ``EnergyGradient`` is
 the ``torch.autograd.Function`` wrapping it: forward returns E, backward
 dE/dh1e (K x K) and dE/d(pq|rs) (K^4).
 
@@ -157,22 +158,30 @@ def site_gradients(dmrg, fmps=None):
 
 def integral_gradients(dmrg, h1e, eri, grads):
     """Chain rule from the site gradients to dE/dh1e and dE/d(pq|rs)
-    (spatial orbitals) through the torch build of every W_p(j)."""
+    (spatial orbitals).  Every W_p(j) is linear in the spin-orbital rows
+    int1e[p], int2e[p], so their gradients are the transposed builder applied
+    to the site gradients (``mpo.hp_spatial_site_adjoint``, NumPy); the small
+    spin-orbital expansion of the spatial integrals is differentiated by
+    torch autograd."""
     torch = _torch()
+    from .integrals import spin_orbital
+    i1, i2 = spin_orbital(numpy.asarray(h1e, dtype=float), numpy.asarray(eri, dtype=float))
+    i1, i2 = i1[dmrg.pidx], i2[dmrg.pidx]
+    d1 = numpy.zeros_like(i1)
+    d2 = numpy.zeros_like(i2)
+    for j in range(dmrg.nsite):
+        for iop in range(dmrg.nops):
+            G = grads[j][iop]
+            if G is None:
+                continue
+            idx, dh, dv = _mpo.hp_spatial_site_adjoint(dmrg.opers[iop], dmrg.sbas, j, i1, i2, G, dmrg.pdic)
+            d1[idx] += dh
+            d2[idx] += dv
     with torch.enable_grad():   # also when called from a Function's backward
         h = torch.tensor(numpy.asarray(h1e, dtype=float), requires_grad=True)
         g = torch.tensor(numpy.asarray(eri, dtype=float), requires_grad=True)
         int1e, int2e = spin_orbital_torch(h, g)
-        int1e = int1e[dmrg.pidx]
-        int2e = int2e[dmrg.pidx]
-        total = torch.zeros((), dtype=torch.float64)
-        for j in range(dmrg.nsite):
-            for iop in range(dmrg.nops):
-                G = grads[j][iop]
-                if G is None:
-                    continue
-                W = _mpo.hp_spatial_site(dmrg.opers[iop], dmrg.sbas, j, int1e, int2e, None, dmrg.pdic)
-                total = total + (W * torch.from_numpy(G)).sum()
+        total = (int1e[dmrg.pidx] * torch.from_numpy(d1)).sum() + (int2e[dmrg.pidx] * torch.from_numpy(d2)).sum()
         total.backward()
     return h.grad.numpy().copy(), g.grad.numpy().copy()
 

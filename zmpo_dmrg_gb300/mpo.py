@@ -101,6 +101,64 @@ def spin_site(nsite, k, h, v):
     return W
 
 
+def spin_site_adjoint(nsite, k, G):
+    """Gradient of <G, spin_site(nsite, k, h, v)> with respect to h and v
+    (spin_site is linear in them): the transpose of its assignments, as
+    NumPy arrays dh [nsite], dv [nsite, nsite, nsite]."""
+    dh = numpy.zeros(nsite)
+    dv = numpy.zeros((nsite, nsite, nsite))
+    nr = 1 if k == nsite - 1 else 2 * (nsite + 1)
+    L, R = k, nsite - k - 1
+    right = numpy.arange(k + 1, nsite)
+    left = numpy.arange(k)
+    rr = numpy.arange(R)
+    last = nr - 1
+
+    def ip(X, M):  # <X[..., i, j], M[i, j]>
+        return numpy.tensordot(X, M, axes=([-2, -1], [0, 1]))
+
+    if k == nsite - 1:
+        dh[k] += ip(G[0, 0], _A)
+        dv[k, left, k] += ip(G[3 + left, 0], _N)
+        return dh, dv
+    dv[k, k, right] += ip(G[0, 1 + R + rr], -_N)
+    dh[k] += ip(G[0, last], _A)
+    if k == 0:
+        return dh, dv
+    o6 = 3 + 2 * R
+    for li in range(L):
+        dv[right, li, k] += ip(G[o6 + li, 1 + rr], _A)       # -v * (-A)
+        dv[k, li, right] += ip(G[o6 + li, 1 + R + rr], _C)
+        dv[k, li, k] += ip(G[o6 + li, last], _N)
+    o7 = 3 + 2 * R + L
+    for li in range(L):
+        dv[li, k, right] += ip(G[o7 + li, 1 + R + rr], -_A)
+    return dh, dv
+
+
+def hp_spatial_site_adjoint(pindx, nspin, isite, int1e, int2e, G, pdic=None):
+    """Gradient of <G, hp_spatial_site(...)> with respect to the spin-orbital
+    rows int1e[idx] and int2e[idx] of term p (the site is linear in them):
+    G [Dw_l, Dw_r, 4, 4] in the builder's bond order.  Returns (idx, dh, dv)."""
+    p, ipt = pindx
+    if ipt is not None:
+        raise NotImplementedError("adjoint of the spin-projected site")
+    idx = p if pdic is None else pdic[p]
+    h, v = int1e[idx], int2e[idx]
+    k0, k1 = 2 * isite, 2 * isite + 1
+    e0, e1 = _elem(p, k0), _elem(p, k1)
+    W1 = numpy.matmul(e0, spin_site(nspin, k0, h, v))
+    W2 = numpy.matmul(e1, spin_site(nspin, k1, h, v))
+    # link: W[a, c, (i k), (j l)] = sum_b W1[a, b, i, j] W2[b, c, k, l]
+    G6 = G.reshape(G.shape[0], G.shape[1], 2, 2, 2, 2)        # [a, c, i, k, j, l]
+    dW1 = numpy.einsum('acikjl,bckl->abij', G6, W2, optimize=True)
+    dW2 = numpy.einsum('acikjl,abij->bckl', G6, W1, optimize=True)
+    # hp_spin_site: e @ W over the row index of the local operator
+    dh0, dv0 = spin_site_adjoint(nspin, k0, numpy.matmul(e0.T, dW1))
+    dh1, dv1 = spin_site_adjoint(nspin, k1, numpy.matmul(e1.T, dW2))
+    return idx, dh0 + dh1, dv0 + dv1
+
+
 def _elem(p, k):
     if k < p:
         return _Z
