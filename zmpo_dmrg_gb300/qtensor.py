@@ -134,12 +134,20 @@ class qtensor:
         return val
 
     def prjmap(self, idlst):
+        """Dense (row-major, full shape) index of every packed element: per
+        block the outer sum of each leg's indices times its dense stride."""
         shape = tuple(int(x) for x in self.shape)
+        strides = [1] * self.rank
+        for i in range(self.rank - 2, -1, -1):
+            strides[i] = strides[i + 1] * shape[i + 1]
+        scaled = [[numpy.asarray(ix, dtype=numpy.int64) * strides[i] for ix in idlst[i]]
+                  for i in range(self.rank)]
         out = []
         for sec, dims, off in self.blocks():
-            grids = numpy.meshgrid(*[numpy.asarray(idlst[i][sec[i]]) for i in range(self.rank)],
-                                   indexing='ij')
-            out.append(numpy.ravel_multi_index(tuple(g.reshape(-1) for g in grids), shape))
+            acc = numpy.zeros((), dtype=numpy.int64)
+            for i in range(self.rank):
+                acc = numpy.add.outer(acc, scaled[i][sec[i]])
+            out.append(acc.reshape(-1))
         return numpy.concatenate(out) if out else numpy.zeros(0, dtype=numpy.int64)
 
     def copy_structure(self, other, qsyms=None, status=None):
