@@ -99,6 +99,10 @@ class qtensor:
 
     def fromDense(self, val, idlst):
         val = numpy.asarray(val)
+        if val.shape == tuple(int(x) for x in self.shape):
+            # one gather through the packed -> dense index map
+            self.value = val.reshape(-1)[self.prjmap(idlst)].astype(numpy.float64, copy=False)
+            return 0
         out = numpy.zeros(self.size_allowed)
         for sec, dims, off in self.blocks():
             ix = numpy.ix_(*[idlst[i][sec[i]] for i in range(self.rank)])
@@ -117,9 +121,7 @@ class qtensor:
     def toDenseTensor(self, idlst):
         v = self._host_value()
         val = numpy.zeros(tuple(int(x) for x in self.shape))
-        for sec, dims, off in self.blocks():
-            ix = numpy.ix_(*[idlst[i][sec[i]] for i in range(self.rank)])
-            val[ix] = v[off:off + int(numpy.prod(dims))].reshape(dims)
+        val.reshape(-1)[self.prjmap(idlst)] = v   # one scatter through the index map
         return val
 
     def toDenseDiag(self, idlst):
