@@ -433,3 +433,28 @@ def test_transposed_builder_equals_autograd_of_the_builder():
     de = de + de.transpose(2, 3, 0, 1)
     change = energy(h + dh, eri + de) - energy(h, eri)
     assert abs(change - float((a1 * dh).sum() + (a2 * de).sum())) <= 1e-12 * abs(change)
+
+
+def test_plan_caches_are_released_with_their_driver():
+    """Cached sigma / renorm plans hold device task lists: they are released
+    when the driver that owns the cache is collected."""
+    import gc
+    from zmpo_dmrg_gb300.mpo_dmrg_kernel import _plan_cache
+
+    class Driver:
+        pass
+
+    class Plan:
+        released = 0
+
+        def release(self):
+            Plan.released += 1
+
+    d = Driver()
+    cache = _plan_cache(d, "_sigma_cache")
+    assert _plan_cache(d, "_sigma_cache") is cache
+    cache["a"] = Plan()
+    cache["b"] = Plan()
+    del d
+    gc.collect()
+    assert Plan.released == 2 and not cache

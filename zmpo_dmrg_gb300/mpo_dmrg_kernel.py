@@ -17,6 +17,7 @@ fallback.
 import collections
 import hashlib
 import itertools
+import weakref
 
 import numpy
 
@@ -95,7 +96,7 @@ class SigmaPlan:
 
     def __init__(self, dmrg, isite, ncsite, fL, fR):
         from .mpo import op_class
-        self.dmrg = dmrg
+        self._dmrg = weakref.ref(dmrg)  # the driver owns the shared workspace (no cycle)
         eng = _engine.get()
         mpo = dmrg.mpo_store
         ops = [iop for iop in range(dmrg.nops) if fL.present(iop) and fR.present(iop)]
@@ -170,7 +171,7 @@ class SigmaPlan:
 
     @property
     def workspace(self):
-        return _shared_workspace(self.dmrg, self.ws_elems)
+        return _shared_workspace(self._dmrg(), self.ws_elems)
 
     def rebind(self, fL, fR):
         """Reuse for environments of the same structure (new device buffers)."""
@@ -282,6 +283,26 @@ def _sigma_key(dmrg, isite, ncsite, fL, fR):
 _SIGMA_CACHE_TASKS = 60_000_000
 
 
+def _release_all(cache):
+    for plan in list(cache.values()):
+        try:
+            plan.release()
+        except Exception:  # the engine may already be gone at interpreter exit
+            pass
+    cache.clear()
+
+
+def _plan_cache(dmrg, name):
+    """The driver's plan cache ``name``; its plans (device task lists) are
+    released when the driver is collected."""
+    cache = dmrg.__dict__.get(name)
+    if cache is None:
+        cache = collections.OrderedDict()
+        dmrg.__dict__[name] = cache
+        weakref.finalize(dmrg, _release_all, cache)
+    return cache
+
+
 def _sigma_plan(info):
     dmrg, isite, ncsite, flst, status, ifsym = info
     fL, fR = flst[0][0:2]
@@ -291,7 +312,7 @@ def _sigma_plan(info):
     if cur is not None and cur[0] == fast and not cur[1].released:
         return cur[1]
     key = _sigma_key(dmrg, isite, ncsite, fL, fR)
-    cache = dmrg.__dict__.setdefault("_sigma_cache", collections.OrderedDict())
+    cache = _plan_cache(dmrg, "_sigma_cache")
     plan = cache.pop(key, None)
     if plan is None or plan.released:
         plan = SigmaPlan(dmrg, isite, ncsite, fL, fR)
@@ -440,7 +461,7 @@ def _renorm_plan(dmrg, status, jsite, fE, qsite, ops):
     for iop in ops:
         _qt_signature(h, fE.tensors[iop])
     key = h.digest()
-    cache = dmrg.__dict__.setdefault("_renorm_cache", collections.OrderedDict())
+    cache = _plan_cache(dmrg, "_renorm_cache")
     rp = cache.pop(key, None)
     if rp is None or rp.released:
         rp = RenormPlan(dmrg, status, jsite, fE, qsite, ops)
