@@ -463,17 +463,14 @@ static void merge_column_blocks(Step &st, const std::vector<MergeInfo> &info) {
       emit_plain((int)gi);
       continue;
     }
-    // union of A parts, in first-seen order
-    struct PartKey {
-      int64_t a_off, sam, sak;
-      double alpha;
-      int32_t K;
-      int8_t abuf;
-      bool operator<(const PartKey &o) const {
-        return std::tie(a_off, sam, sak, alpha, K, abuf) < std::tie(o.a_off, o.sam, o.sak, o.alpha, o.K, o.abuf);
-      }
+    // union of A parts, in first-seen order (parts with the same A offset
+    // are chained from a hash of that offset; the full part is compared)
+    auto same_part = [](const Seg &x, const Seg &y) {
+      return x.a_off == y.a_off && x.sam == y.sam && x.sak == y.sak && x.alpha == y.alpha && x.K == y.K &&
+             x.abuf == y.abuf;
     };
-    std::map<PartKey, int> pidx;
+    std::unordered_map<int64_t, int> first_part;
+    std::vector<int> next_part;
     std::vector<Seg> parts;
     struct Use {
       int part, blk;
@@ -494,16 +491,20 @@ static void merge_column_blocks(Step &st, const std::vector<MergeInfo> &info) {
           ok = false;
           break;
         }
-        PartKey k{sg.a_off, sg.sam, sg.sak, sg.alpha, sg.K, sg.abuf};
-        auto it = pidx.find(k);
-        int p;
-        if (it == pidx.end()) {
+        int p = -1;
+        auto it = first_part.find(sg.a_off);
+        if (it != first_part.end())
+          for (int q = it->second; q >= 0; q = next_part[q])
+            if (same_part(parts[q], sg)) {
+              p = q;
+              break;
+            }
+        if (p < 0) {
           p = (int)parts.size();
-          pidx[k] = p;
+          next_part.push_back(it != first_part.end() ? it->second : -1);
+          first_part[sg.a_off] = p;
           parts.push_back(sg);
           ktot += sg.K;
-        } else {
-          p = it->second;
         }
         uses.push_back({p, (int)j, {sg.b_off, sg.sbk, sg.sbn}});
       }
