@@ -70,3 +70,62 @@ def test_two_rank_sum_equals_full_product():
         assert p.exitcode == 0
     for r in range(2):
         assert numpy.allclose(out[r], full, atol=1e-12)
+
+
+def _oracle_worker(rank, size, port, case, x, out):
+    """Rank-local sigma of the oracle (the reference's HVecQt restated) over
+    this rank's contiguous range of operator terms, summed over ranks."""
+    import copy
+    import torch
+    import torch.distributed as dist
+    from oracle import kernel as ok
+    from tests.problems import random_problem
+    from zmpo_dmrg_gb300.parallel import DistributedHVec, partition_sites
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=size)
+    P = random_problem(device=False, **case)
+    m = P.o
+    mine = partition_sites(m.nops, size, rank)
+    view = copy.copy(m)     # this rank's terms, renumbered 0..len(mine)-1
+    view.fhop = {"nsite": m.fhop["nsite"], "nops": len(mine), "wts": numpy.asarray(m.hpwts)[mine]}
+    for i in range(m.nsite):
+        for k, iop in enumerate(mine):
+            view.fhop["site%d/op%d" % (i, k)] = m.fhop["site%d/op%d" % (i, iop)]
+    view.opers = [m.opers[iop] for iop in mine]
+    view.hpwts = numpy.asarray(m.hpwts)[mine]
+    view.nops = len(mine)
+    view._hvec_templates = None
+    fL = {"opers%d" % k: m.flst[0][0]["opers%d" % iop] for k, iop in enumerate(mine)}
+    fR = {"opers%d" % k: m.flst[0][1]["opers%d" % iop] for k, iop in enumerate(mine)}
+
+    def local(v):
+        return torch.as_tensor(ok.HVecQt(v.numpy(), [view, P.isite, 2, [[fL, fR]], "L", True], P.ndim0, None))
+
+    y = DistributedHVec(local)(torch.as_tensor(x))
+    out[rank] = y.numpy().copy()
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_rank_oracle_sigma_equals_full_sigma():
+    """The operator partition of a real two-site dot: each rank's oracle sigma
+    over its terms, all-reduced, equals the oracle sigma over all terms."""
+    import torch.multiprocessing as mp
+    from tests.problems import random_problem, oracle_sigma
+    case = dict(K=4, nelec=4, D=8, isite=1, seed=5)
+    P = random_problem(device=False, **case)
+    x = numpy.random.default_rng(4).standard_normal(P.ndim0)
+    full = oracle_sigma(P, x)
+    ctx = mp.get_context("spawn")
+    mgr = ctx.Manager()
+    out = mgr.dict()
+    port = _free_port()
+    procs = [ctx.Process(target=_oracle_worker, args=(r, 2, port, case, x, out)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(300)
+        assert p.exitcode == 0
+    for r in range(2):
+        assert numpy.allclose(out[r], full, rtol=1e-12, atol=1e-12)
