@@ -85,10 +85,17 @@ class qtensor:
     def blocks(self):
         """Yield (sector multi-index, block dims, offset) of allowed blocks."""
         nsyms = tuple(int(x) for x in self.nsyms)
-        for f, off in zip(self.blk_flat, self.blk_off):
-            sec = numpy.unravel_index(int(f), nsyms)
-            dims = tuple(int(self.ndims[i][sec[i]]) for i in range(self.rank))
-            yield sec, dims, int(off)
+        flat = numpy.asarray(self.blk_flat, dtype=numpy.int64)
+        if self.rank == 0:
+            for off in self.blk_off:
+                yield (), (), int(off)
+            return
+        secs = numpy.unravel_index(flat, nsyms)        # all blocks at once
+        dims = [numpy.asarray(self.ndims[i])[secs[i]] for i in range(self.rank)]
+        secs = numpy.stack(secs, axis=1).tolist()
+        dims = numpy.stack(dims, axis=1).tolist()
+        for b, off in enumerate(self.blk_off):
+            yield tuple(secs[b]), tuple(dims[b]), int(off)
 
     def fromDenseTensor(self, val, qnums, ifcollect=None):
         rank, qsyms, ndims, idlst = fromQnums(qnums, ifcollect)
