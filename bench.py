@@ -13,7 +13,9 @@ lists) and t the device time per step with inputs resident in HBM; ``e2e`` =
 the same through the C ABI with host input/output vectors (H2D + D2H inside
 the timed region); ``roofline`` for the dominant launch; ``cpu_baseline`` =
 the oracle (the reference's NumPy kernel restated) on a bounded sample of the
-same workload.  ``--impl reference`` times only that CPU path.
+same workload; ``parity_vs_oracle`` = the engine's sigma against the oracle's
+over that sample.  ``--impl reference`` times only the oracle, on a dot built
+on the host without any engine code.
 """
 import argparse
 import json
@@ -69,12 +71,24 @@ class Clocks:
         self.path = os.environ.get("ZMPO_CLOCKS_CSV",
                                    os.path.join(tempfile.gettempdir(), "zmpo_clocks_bench.csv"))
 
+    @staticmethod
+    def device_id():
+        """nvidia-smi ignores CUDA_VISIBLE_DEVICES: select the GPU this process
+        runs on by its UUID (read-only query)."""
+        try:
+            import torch
+            u = str(torch.cuda.get_device_properties(torch.cuda.current_device()).uuid)
+            return u if u.startswith("GPU-") else "GPU-" + u
+        except Exception:
+            return "0"
+
     def start(self):
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                                       "-i", "0", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                                       "-i", self.device_id(), "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
 
@@ -115,55 +129,102 @@ def build_problem(with_oracle=False, small=False, medium=False, large=False, sp=
     return P, time.perf_counter() - t0
 
 
-def oracle_sample(P, nops_sample=2, budget_s=25.0):
-    """Time the oracle's HVecQt on a bounded subset of operator terms built
-    from the GPU environments (same packed values), F_ref / t."""
-    from oracle import dmrg as od, kernel as ok, qtensor as oq
-    m = od.mpo_dmrg(seed=0)
-    m.nsite, m.sbas, m.isym, m.ifQt = P.K, 2 * P.K, 2, True
-    m.build()
-    m.partition()
-    m.loadInts(P.int1e, P.int2e)
-    pm = P.p
-    isite = P.isite
-    fL, fR = pm.flst[0]
-    Lb = fL.buf.cpu().numpy()
-    Rb = fR.buf.cpu().numpy()
-    from oracle import qtensor_opers
-    # pick operator terms from distinct classes, up to nops_sample
-    chosen, seen = [], set()
-    for iop in range(m.nops):
-        c = qtensor_opers.case(m.opers[iop][0], isite, 2)
-        if c not in seen and fL.present(iop) and fR.present(iop):
-            seen.add(c)
-            chosen.append(iop)
-        if len(chosen) >= nops_sample:
-            break
-    m.fhop = {'nops': len(chosen)}
-    m.opers = [m.opers[i] for i in chosen]
-    m.hpwts = numpy.ones(len(chosen))
+def oracle_rate(m, terms_per_step, nsteps, isite, x):
+    """The oracle's HVecQt (the reference's NumPy algorithm, all host cores
+    through BLAS) over rotating subsets of ``terms_per_step`` operator terms,
+    ``nsteps`` times: step i takes terms i*s .. i*s+s-1 (mod the term count),
+    so enough steps visit every term.  Returns per-step (F_ref, seconds) and
+    the set of terms visited; F_ref counts 2mnk over the reference's task
+    lists of the terms evaluated."""
+    from oracle import kernel as ok, qtensor as oq
+    fL, fR = m.flst[0][0:2]
+    allops = list(range(m.fhop['nops']))
+    out, seen = [], set()
+    for i in range(nsteps):
+        chosen = [allops[(i * terms_per_step + j) % len(allops)] for j in range(terms_per_step)]
+        seen.update(chosen)
+        sub = _oracle_view(m, chosen)
+        oq.reset_flops()
+        t0 = time.perf_counter()
+        ok.HVecQt(x, [sub, isite, 2, sub.flst, 'L', True], sub.qtmp.size_allowed, None)
+        dt = time.perf_counter() - t0
+        out.append((float(oq.FLOPS["count"]), dt))
+    return out, seen
+
+
+def _oracle_view(m, chosen):
+    """Oracle driver restricted to the terms ``chosen`` (same environments,
+    MPO sites and packed wavefunction layout)."""
+    import copy
+    sub = copy.copy(m)
+    fL, fR = m.flst[0][0:2]
+    sub.opers = [m.opers[i] for i in chosen]
+    sub.hpwts = numpy.asarray([m.hpwts[i] for i in chosen])
+    sub.fhop = {'nops': len(chosen)}
     fLo, fRo = {}, {}
-    for k, iop in enumerate(chosen):
-        for src, dst, buf in ((fL, fLo, Lb), (fR, fRo, Rb)):
-            t = src.tensors[iop]
-            q = oq.qtensor(t.status)
-            q.fromQsyms(3, t.qsyms, t.ndims)
-            q.value = buf[src.off[iop]:src.off[iop] + q.size_allowed].copy()
-            q.idlst = None
-            dst['opers%d' % k] = q
-        for s in (isite, isite + 1):
-            m.fhop['site%d/op%d' % (s, k)] = qtensor_opers.genHRfacSpatialQt(
-                m.opers[k], m.sbas, s, m.int1e, m.int2e, None, m.pdic)
-    m.qlst = [P.qnuml[isite], pm.qlst[1], pm.qlst[2], P.qnumr[isite + 2]]
-    m.setupQtmpCI(2, P.key)
-    x = numpy.random.default_rng(1).standard_normal(m.qtmp.size_allowed)
-    info = [m, isite, 2, [[fLo, fRo]], 'L', True]
+    for k, i in enumerate(chosen):
+        fLo['opers%d' % k] = fL['opers%d' % i]
+        fRo['opers%d' % k] = fR['opers%d' % i]
+        for st in (m._dot_isite, m._dot_isite + 1):
+            sub.fhop['site%d/op%d' % (st, k)] = m.fhop['site%d/op%d' % (st, i)]
+    sub.flst = [[fLo, fRo]]
+    sub._hvec_templates = None
+    return sub
+
+
+def reference_dot(cfg):
+    """The dot of ``cfg`` for the reference arm, built on the host by the
+    oracle alone (no engine code): the same seeded integrals and random MPS as
+    the engine arm, environments of every operator term renormalised site by
+    site with the oracle's renormQt_H00 (the reference's algorithm), so both
+    arms contract the same environments (to FP64 rounding)."""
+    from tests.problems import random_problem
+    P = random_problem(device=False, with_oracle=True, **cfg)
+    m = P.o
+    m._dot_isite = P.isite
+    return m
+
+
+def cpu_leg(P, cfg, budget_terms=12):
+    """Engine arm, rank 0: (1) ``cpu_baseline`` = the oracle's HVecQt on the
+    host cores over a bounded sample of the dot's terms (``budget_terms``, two
+    per operator class), fed the environments the engine built; (2)
+    ``parity_vs_oracle`` = the engine's sigma over the same terms against that
+    oracle sigma, FP64 / split / 56-bit emulation, relative norm error."""
+    from tests.problems import class_covering_terms, oracle_subset_driver, product_sigma_subset
+    from oracle import kernel as ok, qtensor as oq
+    terms, classes = class_covering_terms(P, 2)
+    terms = terms[:budget_terms]
+    m = oracle_subset_driver(P, terms)
+    x = numpy.random.default_rng(6).standard_normal(P.ndim0)
     oq.reset_flops()
     t0 = time.perf_counter()
-    m._hvec_templates = None
-    ok.HVecQt(x, info, m.qtmp.size_allowed, None)
+    ref = ok.HVecQt(x, [m, P.isite, 2, m.flst, 'L', True], m.qtmp.size_allowed, None)
     dt = time.perf_counter() - t0
-    return oq.FLOPS["count"], dt, chosen
+    fl = float(oq.FLOPS["count"])
+    base = {"value": fl / dt / 1e12, "unit": "TFLOP/s", "cores": cpu_threads(), "kind": "port",
+            "sample": "oracle HVecQt over %d of the %d operator terms (two per operator class, %d classes), "
+                      "environments copied from the engine's dot, %.1f s, F_ref/t" %
+                      (len(terms), P.p.nops, len(classes), dt),
+            "mpi": MPI_NOTE}
+    par = {"terms": terms, "classes": classes}
+    for prec in ("fp64", "split", "emu64"):
+        y = product_sigma_subset(P, terms, x, prec)
+        par[prec] = float(numpy.linalg.norm(y - ref) / numpy.linalg.norm(ref))
+    par["tolerance"] = {"fp64": 1e-10, "split": 1e-8, "emu64": 1e-10}
+    return base, par
+
+
+def workload_config(cfg, ndim0, nterms):
+    """``config`` of both arms' JSON lines (identical for the same workload)."""
+    w = "two-site H.psi, K=%d N=%d Sz=0 D=%d, %d terms, (N,Sz) blocks" % (cfg["K"], cfg["nelec"], cfg["D"], nterms)
+    if cfg.get("npts"):
+        w += ", spin-projected S=0 with %d quadrature points (N-only terms)" % cfg["npts"]
+    return {"workload": w, "ndim0": int(ndim0), "terms": int(nterms), "middle_dot": int(cfg["isite"])}
+
+
+MPI_NOTE = ("the reference's MPI operator partition (mpirun over mpi4py) is unavailable on this box: "
+            "mpi4py and an MPI launcher are absent; one process with multithreaded BLAS on every host core")
 
 
 def sweep_metrics(K=10, nelec=10, D=64, nsweep=10, seed=2024):
@@ -331,25 +392,35 @@ def cpu_threads():
 
 
 def run_reference(args):
-    """--impl reference: the oracle (reference algorithm) on host cores."""
+    """--impl reference: the reference's algorithm (the oracle's restatement
+    of HVecQt, NumPy/BLAS FP64) on the host cores, on the same workload.  No
+    engine code is imported: the dot is built on the host (``reference_dot``)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    import torch
-    torch.cuda.set_device(0)
-    P, _ = build_problem()
-    vals = []
-    for i in range(args.warmup + args.steps):
-        fl, dt, ch = oracle_sample(P)
-        if i >= args.warmup:
-            vals.append(fl / dt / 1e12)
-    v = float(numpy.mean(vals))
+    cfg = WORKLOAD
+    t0 = time.perf_counter()
+    m = reference_dot(cfg)
+    t_setup = time.perf_counter() - t0
+    n = m.qtmp.size_allowed
+    x = numpy.random.default_rng(5).standard_normal(n)
+    nops = m.fhop['nops']
+    # three terms a step: the driver's 20 timed steps visit all 48 terms
+    per = 3
+    oracle_rate(m, per, args.warmup, cfg["isite"], x)
+    res, seen = oracle_rate(m, per, args.steps, cfg["isite"], x)
+    fl = sum(r[0] for r in res)
+    tt = sum(r[1] for r in res)
+    v = fl / tt / 1e12
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-           "config": {"workload": "two-site H.psi, K=24 N=24 Sz=0 D=512, 48 terms, (N,Sz) blocks"},
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tt / len(res),
+           "higher_is_better": True, "config": workload_config(cfg, n, nops),
            "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": cpu_threads(), "kind": "port",
-                            "sample": "oracle HVecQt (reference NumPy algorithm) over %d of 48 operator "
-                                      "terms per step, F_ref/t" % len(ch)},
+                            "sample": "oracle HVecQt (the reference's NumPy algorithm, FP64) over %d of the %d "
+                                      "operator terms per step, rotating (%d distinct terms timed), F_ref/t; "
+                                      "environments built by the oracle's renormalisation on the host "
+                                      "(%.0f s)" % (per, nops, len(seen), t_setup),
+                            "mpi": MPI_NOTE, "setup_s": t_setup},
            "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
     return 0
@@ -392,6 +463,8 @@ def main():
     from zmpo_dmrg_gb300.mpo_dmrg_kernel import HVec, _sigma_plan
 
     P, t_build = build_problem(small=args.small, medium=args.medium, large=args.large, sp=args.sp)
+    cfg = SMALL if args.small else (MEDIUM if args.medium else (LARGE if args.large else
+                                                                 (SPCFG if args.sp else WORKLOAD)))
     pm = P.p
     if args.large or args.sp:
         pm.workspace_budget = LARGE_WORKSPACE
@@ -492,14 +565,11 @@ def main():
         "warmup": max(args.warmup, 3), "ms_per_step": tmax * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 (bf16 digit slices, fp32 accumulate)",
         "data": "synthetic (seeded integrals + seeded random block-sparse MPS)",
-        "config": {"workload": ("two-site H.psi, K=%d N=%d Sz=0 D=%d, %d terms, (N,Sz) blocks" %
-                                (P.K, P.nelec, P.D, pm.nops)) +
-                               (", spin-projected S=0 with %d quadrature points (N-only terms)" % pm.npts
-                                if pm.ifs2proj else ""),
-                   "ndim0": n, "F_ref_flops": flops, "tasks": plan.ntasks, "precision": args.precision,
-                   "term_batches": len(plan.pids),
-                   "l2": "inputs larger than L2 (environments %.2f GB)" % ((L.numel() + R.numel()) * 8 / 1e9),
-                   "build_s": t_build},
+        "config": workload_config(cfg, n, pm.nops),
+        "plan": {"F_ref_flops": flops, "tasks": plan.ntasks, "precision": args.precision,
+                 "term_batches": len(plan.pids),
+                 "l2": "inputs larger than L2 (environments %.2f GB)" % ((L.numel() + R.numel()) * 8 / 1e9),
+                 "build_s": t_build},
         "fp64": {"value": flops / t_fp64 / 1e12, "ms_per_step": t_fp64 * 1e3},
         "split_vs_fp64_rel_err": err_split,
         "e2e": {"value": flops / t_e2e / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": n * 8,
@@ -534,12 +604,8 @@ def main():
         result["gradient"] = gradient_metrics()
     if rank == 0 and args.sweep_large:
         result["sweep_large"] = sweep_large()
-    if rank == 0 and not args.no_cpu:
-        fl, dt, ch = oracle_sample(P)
-        result["cpu_baseline"] = {"value": fl / dt / 1e12, "unit": "TFLOP/s", "cores": cpu_threads(),
-                                  "kind": "port",
-                                  "sample": "oracle HVecQt over %d of 48 operator terms (%.1f s), F_ref/t" %
-                                            (len(ch), dt)}
+    if rank == 0 and not args.no_cpu and not (args.large or args.sp):
+        result["cpu_baseline"], result["parity_vs_oracle"] = cpu_leg(P, cfg)
     if rank == 0:
         print(json.dumps(result))
     if dist:

@@ -7,10 +7,11 @@ as the checker for the GPU engine in ``zmpo_dmrg_gb300``.  Only ``tests/``,
 of ``bench.py`` may import it.  The product package never imports it.
 
 Pinning (how the restatement is tied to the reference):
-  * ``qsym.py`` block-selection rule == the reference's own C ``symAllowed``
+  * ``qtensor.py`` block-selection rule == the reference's own C ``symAllowed``
     (``ctypes/qsym.c``), compiled from the reference sources into
     ``oracle/_ref/libqsym.so`` by ``oracle/Makefile`` (tests skip when absent);
-  * sum_p MPO_p contracted over the chain == exact Jordan-Wigner H (``fci.py``);
+  * sum_p MPO_p contracted over the chain == exact Jordan-Wigner H
+    (``integrals.py``);
   * Qt MPO blocks == dense MPO (reference self-test ``testHRfacSpatial``);
   * H built column-by-column from HVec is symmetric and its diagonal equals
     HDiag (reference debug switch ``checkDiagNQt`` / ``checkDiagQt``);

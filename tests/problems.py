@@ -215,6 +215,63 @@ def _product_side(P):
     return m
 
 
+def oracle_dense_side(P):
+    """The oracle in its dense ("NQt") mode on the same dot: dense MPO sites,
+    dense environments renormalised from the same random sites, ``dims`` as the
+    reference's ``ci_solver`` sets them (normal problems only)."""
+    from oracle import dmrg as od, kernel as ok
+    assert P.npts is None
+    m = od.mpo_dmrg(seed=P.seed)
+    m.nsite, m.sbas, m.isym, m.ifQt = P.K, 2 * P.K, 2, False
+    m.build()
+    m.partition()
+    m.loadInts(P.int1e, P.int2e)
+    m.dumpMPO()
+    fL = m._boundary('lop', -1)
+    for i in range(P.isite):
+        fN = {}
+        ok.renorm(m, i, 1, [[fL, None]], [[fN]], P.lsites[i], 'L')
+        fL = fN
+    fR = m._boundary('rop', P.K)
+    for i in range(P.K - 1, P.isite + 1, -1):
+        fN = {}
+        ok.renorm(m, i, 1, [[None, fR]], [[fN]], P.rsites[i], 'R')
+        fR = fN
+    m.flst = [[fL, fR]]
+    ldim, rdim = len(P.qnuml[P.isite]), len(P.qnumr[P.isite + 2])
+    m.dims = (ldim, 16, rdim, ldim * 16 * rdim)
+    return m
+
+
+def nqt_prjmap(P):
+    """Dense indices of the (ldim, 4, 4, rdim) elements carrying the target
+    label, ascending: the reference's NQt basis of the dot
+    (``mpo_dmrg_dotutil.dptSymmetry``, 102-145)."""
+    ql = numpy.asarray(P.qnuml[P.isite], dtype=float)
+    qr = numpy.asarray(P.qnumr[P.isite + 2], dtype=float)
+    qp = numpy.asarray(QPHYS, dtype=float)
+    qt = (ql[:, None, None, None, :] + qp[None, :, None, None, :] + qp[None, None, :, None, :] +
+          qr[None, None, None, :, :]).reshape(-1, ql.shape[1])
+    key = numpy.asarray(P.key, dtype=float)
+    return numpy.nonzero(numpy.abs(qt - key).sum(axis=1) < 1e-10)[0]
+
+
+def packed_to_nqt(P, prj):
+    """pos[i] = position in the NQt vector of packed element i."""
+    m = P.o if getattr(P, "o", None) is not None else P.p
+    dense_of_packed = numpy.asarray(m.qtmp.prjmap(m.idlstCI))
+    inv = numpy.full(int(prj.max()) + 1, -1)
+    inv[prj] = numpy.arange(prj.size)
+    return inv[dense_of_packed]
+
+
+def oracle_sigma_nqt(P, x, m=None):
+    from oracle import kernel as ok
+    m = m or oracle_dense_side(P)
+    prj = nqt_prjmap(P)
+    return ok.HVecNQt(numpy.asarray(x, dtype=float), [m, P.isite, 2, m.flst, 'L', True], prj.size, prj)
+
+
 def oracle_sigma(P, x):
     from oracle import kernel as ok
     m = P.o
@@ -393,3 +450,99 @@ def b_resident_tiles(P):
                         n += 1
                     n0 += tn
     return n
+
+
+# ------------------------------------------- parity over a subset of terms
+# At the benchmark sizes (K=24 D=512, K=20 D=512 with 8 quadrature points)
+# the oracle cannot build the environments in reasonable time, so the check
+# runs on the environments the engine built: the oracle's HVecQt over a subset
+# of operator terms, fed the same environment values (copied from the device),
+# against the engine's sigma over the same terms.
+
+def class_covering_terms(P, per_class=1):
+    """Operator terms of the dot with both environments, ``per_class`` of
+    each operator class the dot meets (``qtensor_opers.case``, the unit the
+    reference builds its task-list templates for, mpo_dmrg_kernelQt.py:196-236),
+    evenly spaced within the class (for a spin-projected problem this varies
+    the rotation angle from class to class), in term order."""
+    from oracle import qtensor_opers
+    m = P.p
+    fL, fR = m.flst[0][0:2]
+    by_class = {}
+    for iop in range(m.nops):
+        if fL.present(iop) and fR.present(iop):
+            by_class.setdefault(qtensor_opers.case(m.opers[iop][0], P.isite, 2), []).append(iop)
+    chosen = []
+    for c, lst in by_class.items():
+        n = min(per_class, len(lst))
+        chosen += [lst[int((j + 0.5) * len(lst) / n)] for j in range(n)]
+    return sorted(chosen), sorted(by_class)
+
+
+def _oracle_qt_from_device(env, iop, host_buf):
+    from oracle.qtensor import qtensor
+    t = env.tensors[iop]
+    q = qtensor(t.status)
+    q.fromQsyms(3, t.qsyms, t.ndims)
+    q.value = host_buf[env.off[iop]:env.off[iop] + q.size_allowed].copy()
+    return q
+
+
+def oracle_subset_driver(P, terms):
+    """Oracle driver whose operator list is ``terms`` of the engine's driver,
+    environments copied from the engine's EnvSets, MPO sites from the
+    oracle's own builder."""
+    from oracle import dmrg as od, qtensor_opers
+    from oracle import spinproj as osp
+    pm = P.p
+    m = od.mpo_dmrg(seed=0)
+    m.nsite, m.sbas, m.isym, m.ifQt = P.K, 2 * P.K, 2, True
+    if P.npts is not None:
+        m.ifs2proj, m.npts = True, P.npts
+        osp.s2quad(m, P.sval, P.sz)
+    m.build()
+    m.partition()
+    m.loadInts(P.int1e, P.int2e)
+    fL, fR = pm.flst[0][0:2]
+    Lb = fL.buf.cpu().numpy()
+    Rb = fR.buf.cpu().numpy()
+    opers = [m.opers[i] for i in terms]
+    hpwts = numpy.array([m.hpwts[i] for i in terms])
+    m.opers = opers
+    m.hpwts = hpwts
+    m.fhop = {'nops': len(terms)}
+    fLo, fRo = {}, {}
+    for k, iop in enumerate(terms):
+        fLo['opers%d' % k] = _oracle_qt_from_device(fL, iop, Lb)
+        fRo['opers%d' % k] = _oracle_qt_from_device(fR, iop, Rb)
+        for s in (P.isite, P.isite + 1):
+            m.fhop['site%d/op%d' % (s, k)] = qtensor_opers.genHRfacSpatialQt(
+                opers[k], m.sbas, s, m.int1e, m.int2e, m.qpts, m.pdic)
+    m.flst = [[fLo, fRo]]
+    m.qlst = [P.qnuml[P.isite], QPHYS, QPHYS, P.qnumr[P.isite + 2]]
+    m.setupQtmpCI(2, P.key)
+    m._hvec_templates = None
+    return m
+
+
+def oracle_sigma_subset(P, terms, x, m=None):
+    from oracle import kernel as ok
+    m = m or oracle_subset_driver(P, terms)
+    return ok.HVecQt(numpy.asarray(x, dtype=float), [m, P.isite, 2, m.flst, 'L', True],
+                     m.qtmp.size_allowed, None)
+
+
+def product_sigma_subset(P, terms, x, precision="fp64"):
+    """The engine's HVec over ``terms`` only: views of the environment sets
+    in which every other term is absent (a plan over exactly those terms)."""
+    from zmpo_dmrg_gb300.mpo_dmrg_kernel import HVec, EnvSet
+    m = P.p
+    keep = numpy.zeros(m.nops, dtype=bool)
+    keep[list(terms)] = True
+    views = []
+    for env in m.flst[0][0:2]:
+        off = numpy.where(keep, env.off, -1)
+        views.append(EnvSet(env.buf, off, env.layouts, env.tensors))
+    flst = [views + list(m.flst[0][2:])]
+    m.precision = precision
+    return HVec(numpy.asarray(x, dtype=float), [m, P.isite, 2, flst, 'L', True], P.ndim0, None)

@@ -62,7 +62,7 @@ def test_error_convention():
     assert "unknown layout" in _lib.last_error()
 
 
-def test_integrals_match_oracle():
+def test_integrals_match_oracle(tmp_path):
     for K, seed, hop in [(4, 1, 1.0), (6, 9, 0.7)]:
         a = pint.synthetic(K, seed, hop)
         b = oint.synthetic(K, seed, hop)
@@ -73,8 +73,7 @@ def test_integrals_match_oracle():
     fd = os.path.join(ROOT, "tests", "golden", "h6p_doublet_fcidump.npz")
     z = numpy.load(fd)
     # round trip through the FCIDUMP text format
-    path = os.path.join(ROOT, "_work", "rt.FCIDUMP")
-    os.makedirs(os.path.dirname(path), exist_ok=True)
+    path = str(tmp_path / "rt.FCIDUMP")
     n = z["h1e"].shape[0]
     with open(path, "w") as f:
         f.write(" &FCI NORB=%d,NELEC=%d,MS2=%d,\n  ORBSYM=%s\n  ISYM=1,\n &END\n"
@@ -265,15 +264,19 @@ def test_n_only_relabel_matches_oracle():
     assert numpy.abs(a.qwts - b.qwts).max() < 1e-13
 
 
-def _run_tasks_on_host(eng, pid, nsteps, bufs):
+def _run_tasks_on_host(eng, pid, nsteps, bufs, gemm=None):
     """Execute a plan's task records with NumPy (test-only model of the
-    kernels' semantics, incl. column-block groups); returns the buffers."""
+    kernels' semantics, incl. column-block groups); returns the buffers.
+    ``gemm(A, B)``, when given, computes each group's product from its
+    segments joined along K (A scaled by the segment weights) -- a model of
+    a kernel's arithmetic; it may return None to keep the FP64 sum."""
     for st in range(nsteps):
         groups, segs, cbl, segb = eng.step_tasks(pid, st)
         for g in groups:
             M, N = int(g["M"]), int(g["N"])
             acc = numpy.zeros((M, N))
             mi = numpy.arange(M)
+            As, Bs = [], []
             for si in range(int(g["nseg"])):
                 s = segs[g["seg0"] + si]
                 K = int(s["K"])
@@ -293,6 +296,13 @@ def _run_tasks_on_host(eng, pid, nsteps, bufs):
                         B[:, cb["n0"]:cb["n0"] + cb["n"]] = bufs[int(s["bbuf"])][
                             sb["b_off"] + ki[:, None] * sb["sbk"] + ni[None, :] * sb["sbn"]]
                 acc += s["alpha"] * (A @ B)
+                if gemm is not None:
+                    As.append(A * s["alpha"] if s["alpha"] != 1.0 else A)
+                    Bs.append(B)
+            if gemm is not None and As:
+                got = gemm(numpy.concatenate(As, axis=1), numpy.concatenate(Bs, axis=0))
+                if got is not None:
+                    acc = got
             out = bufs[int(g["cbuf"])]
             if g["ncb"] == 0:
                 ni = numpy.arange(N)
@@ -306,13 +316,10 @@ def _run_tasks_on_host(eng, pid, nsteps, bufs):
     return bufs
 
 
-def test_sigma_task_lists_compute_the_oracle_sigma():
-    """The engine's sigma plan (O = Wi.Wj, T1 = L.psi, T3 = T1.O, sigma = T3.R
-    with column-block groups) executed from its task records by a NumPy model
-    of the kernels equals the oracle's HVecQt (FP64, 1e-12): checks the
-    planner's addressing on the CPU, before any kernel runs."""
-    from tests.problems import random_problem, oracle_sigma
-    P = random_problem(K=6, nelec=6, D=16, isite=2, seed=1, device=False)
+def _host_sigma(P, gemm=None):
+    """The engine's sigma plan for the oracle side of ``P`` executed on the
+    host from its task records; returns (sigma, oracle sigma, groups)."""
+    from tests.problems import oracle_sigma
     m = P.o
     eng = E.get()
     fL, fR = m.flst[0]
@@ -346,11 +353,46 @@ def test_sigma_task_lists_compute_the_oracle_sigma():
             numpy.zeros(P.ndim0), numpy.zeros(max(ws // 8, 1)), numpy.zeros(1), numpy.zeros(1)]
     _, _, nl = eng.plan_stats(pid)
     groups_all = [eng.step_tasks(pid, st)[0] for st in range(nl)]
-    assert any((g["ncb"] > 0).any() for g in groups_all)      # column-block groups are in use
-    y = _run_tasks_on_host(eng, pid, nl, bufs)[4]
+    y = _run_tasks_on_host(eng, pid, nl, bufs, gemm)[4]
     ref = oracle_sigma(P, x)
-    assert numpy.linalg.norm(y - ref) <= 1e-12 * numpy.linalg.norm(ref)
     eng.destroy_plan(pid)
+    return y, ref, groups_all
+
+
+def test_sigma_task_lists_compute_the_oracle_sigma():
+    """The engine's sigma plan (O = Wi.Wj, T1 = L.psi, T3 = T1.O, sigma = T3.R
+    with column-block groups) executed from its task records by a NumPy model
+    of the kernels equals the oracle's HVecQt (FP64, 1e-12): checks the
+    planner's addressing on the CPU, before any kernel runs."""
+    from tests.problems import random_problem
+    P = random_problem(K=6, nelec=6, D=16, isite=2, seed=1, device=False)
+    y, ref, groups_all = _host_sigma(P)
+    assert any((g["ncb"] > 0).any() for g in groups_all)      # column-block groups are in use
+    assert numpy.linalg.norm(y - ref) <= 1e-12 * numpy.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("case", [dict(K=8, nelec=8, D=32, isite=3, seed=4),
+                                  dict(K=10, nelec=10, D=64, isite=4, seed=7)])
+def test_sigma_one_pass_split_model_error(case):
+    """Sigma with every group whose K fits one pass (K <= 256) multiplied by
+    the exact model of the one-pass split arithmetic (whole-K row and column
+    exponents, tests/split_model.py): within the split path's 1e-8 of the
+    oracle's FP64 sigma."""
+    from tests.problems import random_problem
+    from tests.split_model import one_pass_gemm
+    P = random_problem(device=False, **case)
+    used = []
+
+    def gemm(A, B):
+        if A.shape[1] > 256:
+            return None
+        used.append(A.shape)
+        return one_pass_gemm(A, B)
+
+    y, ref, _ = _host_sigma(P, gemm)
+    assert len(used) > 100
+    err = numpy.linalg.norm(y - ref) / numpy.linalg.norm(ref)
+    assert err < 1e-8, err
 
 
 def test_sigma_plan_key_is_structural():

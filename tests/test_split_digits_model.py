@@ -110,3 +110,33 @@ def test_split_dot_error_bound():
         got = split_dot(list(a), list(b))
         worst = max(worst, abs(got - ref) / float(numpy.dot(numpy.abs(a), numpy.abs(b))))
     assert worst < 1e-8
+
+
+# ------------------------------------------------ one-pass (whole-K) scheme
+def test_one_pass_model_matches_slot_model():
+    """The vectorised one-pass model (tests/split_model.py) equals the scalar
+    digit model above with a single chunk covering all of K."""
+    from tests.split_model import one_pass_gemm
+    rng = numpy.random.default_rng(3)
+    for n in (1, 5, 64, 200, 256):
+        a = rng.standard_normal(n) * numpy.exp(rng.uniform(-6, 6, n))
+        b = rng.standard_normal(n)
+        got = one_pass_gemm(a[None, :], b[:, None])[0, 0]
+        ref = split_dot(list(a), list(b), TK=256)
+        assert abs(got - ref) <= 2e-7 * abs(ref) + 1e-300   # the scalar model folds in two floats
+
+
+def test_one_pass_model_error_bound():
+    """Error of the one-pass product: below 2^-29 K max_k|a_ik| max_k|b_kj|
+    per element (every digit cut is relative to its row's or column's largest
+    element), also for rows and columns with a wide dynamic range."""
+    from tests.split_model import one_pass_gemm
+    rng = numpy.random.default_rng(11)
+    for trial in range(6):
+        M, K, N = 37, int(rng.integers(1, 257)), 23
+        A = rng.standard_normal((M, K)) * numpy.exp(rng.uniform(-10, 10, (M, K)) * (trial % 2))
+        B = rng.standard_normal((K, N)) * numpy.exp(rng.uniform(-4, 4, (K, N)))
+        got = one_pass_gemm(A, B)
+        ref = (A.astype(numpy.longdouble) @ B.astype(numpy.longdouble)).astype(numpy.float64)
+        scale = K * numpy.abs(A).max(axis=1)[:, None] * numpy.abs(B).max(axis=0)[None, :]
+        assert (numpy.abs(got - ref) <= 2.0 ** -29 * scale + 1e-300).all()

@@ -129,6 +129,8 @@ class mpo_dmrg:
         self.opers = []
         self.nops = None
         self.ifQt = True
+        # this driver keeps Davidson vectors and diagonals on the device
+        self.device_vectors = True
         self.qkey = None
         self.qlst = None
         self.qtmp = None

@@ -13,6 +13,18 @@ L_p or R_p for every operator term, in the reference's packed block order),
 Vectors may be NumPy (copied to and from the device) or float64 CUDA tensors
 (kept on the device).  Every product runs in the engine; there is no host
 fallback.
+
+Vector order follows ``dmrg.ifQt`` as in the reference (``HVec`` 121-124,
+``HDiag`` 45-48): with ``ifQt`` (the default) a vector is the packed block
+order of ``dmrg.qtmp``; with ``ifQt = False`` it is the caller's dense order,
+element j at dense index ``prjmap[j]`` of the (ldim, 4, 4, rdim) tensor
+(``HVecNQt`` 138-181).  The environments stay block-sparse either way: the
+dense-ordered vector is gathered into the packed order on the device and the
+result scattered back.  ``HDiag`` returns NumPy (as the reference's
+``genHDiag`` expects) unless the driver keeps its vectors on the device
+(``dmrg.device_vectors``).  The perturbation-theory variant of the
+reference's ``HVec`` (``dmrg.ifpt``: H0 - E0 through ``fdopXfhop``, 118-135)
+is not part of this path and raises ``NotImplementedError``.
 """
 import collections
 import hashlib
@@ -328,36 +340,108 @@ def _sigma_plan(info):
     return plan
 
 
+def _check_path(dmrg):
+    if getattr(dmrg, "ifpt", False):
+        raise NotImplementedError("the perturbation-theory H0 - E0 form of HVec (dmrg.ifpt) is not part "
+                                  "of this engine's sigma-vector path")
+
+
+def _nqt_positions(info, ndim0, prjmap):
+    """For ``dmrg.ifQt = False``: position in the caller's dense-ordered
+    vector of every packed block element, as a device index tensor (None in
+    the packed-order case).  ``prjmap`` lists the dense indices of the
+    caller's elements (the reference's ``dptSymmetry`` dictionary entry,
+    ``mpo_dmrg_dotutil.py:102-145``); the target label is read from it, the
+    packed layout set up for that label, and the map cached per driver."""
+    dmrg, isite, ncsite = info[0], info[1], info[2]
+    if getattr(dmrg, "ifQt", True):
+        return None
+    if prjmap is None:
+        raise ValueError("HVec/HDiag with dmrg.ifQt = False need prjmap (dense index of each element)")
+    torch = _torch()
+    prj = numpy.asarray(prjmap, dtype=numpy.int64).reshape(-1)
+    if prj.size != ndim0:
+        raise ValueError("prjmap has %d entries, ndim0 is %d" % (prj.size, ndim0))
+    qlst = [numpy.asarray(q, dtype=float) for q in dmrg.qlst]
+    dims = [len(q) for q in qlst]
+    ndim = int(numpy.prod(dims))
+    if prj.size == 0 or prj.min() < 0 or prj.max() >= ndim:
+        raise ValueError("prjmap entries outside the dense (%s) tensor" % ",".join(map(str, dims)))
+    h = hashlib.blake2b(prj.tobytes(), digest_size=16)
+    for q in qlst:
+        h.update(q.tobytes())
+    key = (isite, ncsite, h.digest())
+    cache = dmrg.__dict__.setdefault("_nqt_pos_cache", {})
+    hit = cache.get(key)
+    if hit is not None:
+        if dmrg.qtmp_psi_layout != hit[1]:
+            dmrg.setupQtmpCI(ncsite, list(hit[2]))
+        return hit[0]
+    # total label of the caller's elements, from the first one
+    idx0 = numpy.unravel_index(int(prj[0]), dims)
+    qkey = sum(qlst[i][idx0[i]] for i in range(len(qlst)))
+    dmrg.setupQtmpCI(ncsite, [float(v) for v in numpy.atleast_1d(qkey)])
+    dense_of_packed = numpy.asarray(dmrg.qtmp.prjmap(dmrg.idlstCI), dtype=numpy.int64)
+    inv = numpy.full(ndim, -1, dtype=numpy.int64)
+    inv[prj] = numpy.arange(prj.size)
+    pos = inv[dense_of_packed]
+    if dense_of_packed.size != prj.size or (pos < 0).any():
+        raise ValueError("prjmap does not span the symmetry sector of its first element")
+    if len(cache) > 64:
+        cache.clear()
+    pos_d = torch.as_tensor(pos, device="cuda")
+    cache[key] = (pos_d, dmrg.qtmp_psi_layout, tuple(float(v) for v in numpy.atleast_1d(qkey)))
+    return pos_d
+
+
 def HVec(vec0, info, ndim0, prjmap):
     """y = H x over every operator term of the dot, on the GPU."""
     dmrg = info[0]
+    _check_path(dmrg)
     torch = _torch()
+    pos = _nqt_positions(info, ndim0, prjmap)
     plan = _sigma_plan(info)
     x, was_host = _to_device(vec0)
+    if pos is not None:
+        x = x.index_select(0, pos)
     y = torch.empty(ndim0, dtype=torch.float64, device=x.device)
     if plan.pid is None:
         y.zero_()
     else:
         plan.run(dmrg, x, y, getattr(dmrg, "precision", "fp64"), getattr(dmrg, "use_graph", False))
+    if pos is not None:
+        yd = torch.empty_like(y)
+        yd[pos] = y
+        y = yd
     return y.cpu().numpy() if was_host else y
 
 
+def _diag_out(dmrg, d, pos):
+    if pos is not None:
+        dd = _torch().empty_like(d)
+        dd[pos] = d
+        d = dd
+    return d if getattr(dmrg, "device_vectors", False) else d.cpu().numpy()
+
+
 def HDiag(info, ndim0, prjmap):
-    """diag(H) in the packed wavefunction order (Davidson preconditioner)."""
+    """diag(H) (Davidson preconditioner) in the caller's vector order."""
     dmrg = info[0]
+    _check_path(dmrg)
     torch = _torch()
+    pos = _nqt_positions(info, ndim0, prjmap)
     plan = _sigma_plan(info)
     d = torch.zeros(ndim0, dtype=torch.float64, device="cuda")
     if plan.pid is None:
-        return d
+        return _diag_out(dmrg, d, pos)
     if plan.nmap is not None:
         idx, nN = plan.nmap
         dN = torch.zeros(nN, dtype=torch.float64, device="cuda")
         plan.hdiag(dmrg, dN)
         torch.index_select(dN, 0, idx, out=d)
-        return d
+        return _diag_out(dmrg, d, pos)
     plan.hdiag(dmrg, d)
-    return d
+    return _diag_out(dmrg, d, pos)
 
 
 def renorm(dmrg, isite, ncsite, flst, flstN, site, status):
@@ -477,12 +561,21 @@ def _renorm_plan(dmrg, status, jsite, fE, qsite, ops):
 def SVec(vec0, info, ndim0, prjmap):
     """S psi for the spin-projected problem (``mpo_dmrg_kernel.SVec``, 226-231)."""
     from .spinproj import SVec as _svec
-    return _svec(vec0, info, ndim0, prjmap)
+    pos = _nqt_positions(info, ndim0, prjmap)
+    if pos is None:
+        return _svec(vec0, info, ndim0, prjmap)
+    x, was_host = _to_device(vec0)
+    y = _svec(x.index_select(0, pos), info, ndim0, prjmap)
+    yd = _torch().empty_like(y)
+    yd[pos] = y
+    return yd.cpu().numpy() if was_host else yd
 
 
 def SDiag(info, ndim0, prjmap):
+    """diag(S) in the caller's vector order (``SDiag``, 185-224)."""
     from .spinproj import SDiag as _sdiag
-    return _sdiag(info, ndim0, prjmap)
+    pos = _nqt_positions(info, ndim0, prjmap)
+    return _diag_out(info[0], _sdiag(info, ndim0, prjmap), pos)
 
 
 def _env_structure(dmrg, status, qsite, wt, env, lay_out):
