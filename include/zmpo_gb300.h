@@ -35,7 +35,10 @@ extern "C" {
 
 /* Precision of the block contractions (argument `precision`). */
 #define ZMPO_PREC_FP64 0     /* FP64 FMA on the CUDA cores                 */
-#define ZMPO_PREC_SPLIT 1    /* BF16 tensor cores, 4 exact digit slices    */
+#define ZMPO_PREC_SPLIT 1    /* BF16 tensor cores, 4 exact digit slices;
+                                groups whose whole K fits one exact pass
+                                (K <= 256) run on tcgen05 with exponents
+                                per row / column over that K              */
 #define ZMPO_PREC_EMU64 2    /* BF16 tensor cores, 7 exact digit slices    */
 
 typedef struct zmpo_engine zmpo_engine;
@@ -206,6 +209,14 @@ int zmpo_plan_launch_times(zmpo_engine *e, int plan_id, int nmax, double *ms_avg
  * of block products and summed K (used to choose tile shapes). */
 int zmpo_plan_groups(zmpo_engine *e, int plan_id, int step, int64_t *ngroups,
                      int32_t *M, int32_t *N, int32_t *nseg, int64_t *ktot);
+
+/* Error word of the device kernels (no reference counterpart).  The
+ * tensor-core kernels bound every wait between their warps in time; a wait
+ * that runs out records a code here (100 + the wait's site) and the kernel
+ * returns early without hanging the GPU, leaving its output incomplete.
+ * *code = 0 when no kernel has reported an error; reset != 0 clears it.
+ * Synchronises with the device. */
+int zmpo_device_status(zmpo_engine *e, int *code, int reset);
 
 /* Release a contraction / sigma / renorm plan. */
 int zmpo_plan_destroy(zmpo_engine *e, int plan_id);

@@ -546,3 +546,66 @@ def product_sigma_subset(P, terms, x, precision="fp64"):
     flst = [views + list(m.flst[0][2:])]
     m.precision = precision
     return HVec(numpy.asarray(x, dtype=float), [m, P.isite, 2, flst, 'L', True], P.ndim0, None)
+
+
+# ------------------------------------------ host model of a plan's tasks
+def run_tasks_on_host(eng, pid, nsteps, bufs, gemm=None, written=None):
+    """Execute a plan's task records with NumPy (test-only model of the
+    kernels' semantics, incl. column-block groups); returns the buffers.
+    ``gemm(A, B)``, when given, computes each group's product from its
+    segments joined along K (A scaled by the segment weights) -- a model of
+    a kernel's arithmetic; it may return None to keep the FP64 sum.
+    ``written``, when given, collects (buffer, flat indices, values) of the
+    groups whose product came from ``gemm``."""
+    for st in range(nsteps):
+        groups, segs, cbl, segb = eng.step_tasks(pid, st)
+        for g in groups:
+            M, N = int(g["M"]), int(g["N"])
+            acc = numpy.zeros((M, N))
+            mi = numpy.arange(M)
+            As, Bs = [], []
+            for si in range(int(g["nseg"])):
+                s = segs[g["seg0"] + si]
+                K = int(s["K"])
+                ki = numpy.arange(K)
+                A = bufs[int(s["abuf"])][s["a_off"] + mi[:, None] * s["sam"] + ki[None, :] * s["sak"]]
+                if g["ncb"] == 0:
+                    ni = numpy.arange(N)
+                    B = bufs[int(s["bbuf"])][s["b_off"] + ki[:, None] * s["sbk"] + ni[None, :] * s["sbn"]]
+                else:
+                    B = numpy.zeros((K, N))
+                    for j in range(int(g["ncb"])):
+                        cb = cbl[g["cb0"] + j]
+                        sb = segb[g["sb0"] + si * g["ncb"] + j]
+                        if sb["b_off"] < 0:
+                            continue
+                        ni = numpy.arange(int(cb["n"]))
+                        B[:, cb["n0"]:cb["n0"] + cb["n"]] = bufs[int(s["bbuf"])][
+                            sb["b_off"] + ki[:, None] * sb["sbk"] + ni[None, :] * sb["sbn"]]
+                acc += s["alpha"] * (A @ B)
+                if gemm is not None:
+                    As.append(A * s["alpha"] if s["alpha"] != 1.0 else A)
+                    Bs.append(B)
+            modelled = False
+            if gemm is not None and As:
+                got = gemm(numpy.concatenate(As, axis=1), numpy.concatenate(Bs, axis=0))
+                if got is not None:
+                    acc = got
+                    modelled = True
+            out = bufs[int(g["cbuf"])]
+            if g["ncb"] == 0:
+                ni = numpy.arange(N)
+                idx = g["c_off"] + mi[:, None] * g["scm"] + ni[None, :] * g["scn"]
+                out[idx] = acc
+                if modelled and written is not None:
+                    written.append((int(g["cbuf"]), idx.ravel(), acc.ravel()))
+            else:
+                for j in range(int(g["ncb"])):
+                    cb = cbl[g["cb0"] + j]
+                    ni = numpy.arange(int(cb["n"]))
+                    idx = cb["c_off"] + mi[:, None] * cb["scm"] + ni[None, :] * cb["scn"]
+                    part = acc[:, cb["n0"]:cb["n0"] + cb["n"]]
+                    out[idx] = part
+                    if modelled and written is not None:
+                        written.append((int(g["cbuf"]), idx.ravel(), part.ravel()))
+    return bufs

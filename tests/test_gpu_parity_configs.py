@@ -8,10 +8,15 @@
   <= 1e-10 relative (norm of the difference over the norm).
 * K=20, 20 electrons, D=512, singlet projection with 8 quadrature points:
   the same check on the spin-projected H.psi (N-only relabelled terms).
-* K=10, 10 electrons, D=64, the reference's default two-site schedule, 4
+* K=10, 10 electrons, D=64, the reference's default two-site schedule from
+  the occupation-number state (its initial one-site sweep included), 4
   sweeps: the energy of every dot and the final energy of the GPU driver
   against the oracle driver's (frozen in ``tests/golden/sweep_k10_d64.npz``
-  by ``tests/golden/make_oracle_fixtures.py``), within 1e-8 Eh.
+  by ``tests/golden/make_oracle_fixtures.py``), within 1e-8 Eh.  The
+  reference builds a first MPS only in its dense-vector mode, so the driver
+  runs with ``ifQt = False``: Davidson vectors (and their random start
+  noise) in the reference's dense order, the engine's block-sparse products
+  underneath.
 """
 import os
 
@@ -73,6 +78,7 @@ def test_sweep_k10_d64_matches_oracle_driver(gpu, precision):
     m.occun = numpy.array([1., 1.] * (nelec // 2) + [0., 0.] * (K - nelec // 2))
     m.qsectors = {str([float(nelec), 0.0]): 1}
     m.precision = precision
+    m.ifQt = False
     m.partition()
     m.loadInts((i1, i2))
     m.dumpMPO()

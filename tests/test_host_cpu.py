@@ -14,6 +14,7 @@ from zmpo_dmrg_gb300 import _lib, engine as E, mpo as pm, integrals as pint
 from zmpo_dmrg_gb300.mpo_dmrg_schedule import schedule as pschedule
 from zmpo_dmrg_gb300.mpo_dmrg_class import rdm_blkdiag as p_rdm_blkdiag
 from zmpo_dmrg_gb300.qtensor import qtensor as pq
+from tests.problems import run_tasks_on_host as _run_tasks_on_host
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "zmpo_gb300.h")
@@ -262,58 +263,6 @@ def test_n_only_relabel_matches_oracle():
     osp.s2quad(b, 1.5, 0.5)
     assert numpy.abs(a.qpts - b.qpts).max() < 1e-14
     assert numpy.abs(a.qwts - b.qwts).max() < 1e-13
-
-
-def _run_tasks_on_host(eng, pid, nsteps, bufs, gemm=None):
-    """Execute a plan's task records with NumPy (test-only model of the
-    kernels' semantics, incl. column-block groups); returns the buffers.
-    ``gemm(A, B)``, when given, computes each group's product from its
-    segments joined along K (A scaled by the segment weights) -- a model of
-    a kernel's arithmetic; it may return None to keep the FP64 sum."""
-    for st in range(nsteps):
-        groups, segs, cbl, segb = eng.step_tasks(pid, st)
-        for g in groups:
-            M, N = int(g["M"]), int(g["N"])
-            acc = numpy.zeros((M, N))
-            mi = numpy.arange(M)
-            As, Bs = [], []
-            for si in range(int(g["nseg"])):
-                s = segs[g["seg0"] + si]
-                K = int(s["K"])
-                ki = numpy.arange(K)
-                A = bufs[int(s["abuf"])][s["a_off"] + mi[:, None] * s["sam"] + ki[None, :] * s["sak"]]
-                if g["ncb"] == 0:
-                    ni = numpy.arange(N)
-                    B = bufs[int(s["bbuf"])][s["b_off"] + ki[:, None] * s["sbk"] + ni[None, :] * s["sbn"]]
-                else:
-                    B = numpy.zeros((K, N))
-                    for j in range(int(g["ncb"])):
-                        cb = cbl[g["cb0"] + j]
-                        sb = segb[g["sb0"] + si * g["ncb"] + j]
-                        if sb["b_off"] < 0:
-                            continue
-                        ni = numpy.arange(int(cb["n"]))
-                        B[:, cb["n0"]:cb["n0"] + cb["n"]] = bufs[int(s["bbuf"])][
-                            sb["b_off"] + ki[:, None] * sb["sbk"] + ni[None, :] * sb["sbn"]]
-                acc += s["alpha"] * (A @ B)
-                if gemm is not None:
-                    As.append(A * s["alpha"] if s["alpha"] != 1.0 else A)
-                    Bs.append(B)
-            if gemm is not None and As:
-                got = gemm(numpy.concatenate(As, axis=1), numpy.concatenate(Bs, axis=0))
-                if got is not None:
-                    acc = got
-            out = bufs[int(g["cbuf"])]
-            if g["ncb"] == 0:
-                ni = numpy.arange(N)
-                out[g["c_off"] + mi[:, None] * g["scm"] + ni[None, :] * g["scn"]] = acc
-            else:
-                for j in range(int(g["ncb"])):
-                    cb = cbl[g["cb0"] + j]
-                    ni = numpy.arange(int(cb["n"]))
-                    out[cb["c_off"] + mi[:, None] * cb["scm"] + ni[None, :] * cb["scn"]] = \
-                        acc[:, cb["n0"]:cb["n0"] + cb["n"]]
-    return bufs
 
 
 def _host_sigma(P, gemm=None):

@@ -13,6 +13,7 @@ import os
 import pytest
 
 SRC = os.path.join(os.path.dirname(__file__), "..", "zmpo_dmrg_gb300", "csrc", "kernels.cu")
+COMMON = os.path.join(os.path.dirname(__file__), "..", "zmpo_dmrg_gb300", "csrc", "device_common.cuh")
 SLOT = 56              # sizeof(Slot): 2 pointers, 2 int64, 1 double, 4 int
 LIMIT = 232448         # dynamic + static shared memory per CTA
 NPART = 4              # independent parts of a B-resident CTA
@@ -34,14 +35,18 @@ MIRRORED = [
     "constexpr int TPRH = NTH / TMH, KPAH = TK / TPRH;",
     "(size_t)CHB * EBN * 4 + (size_t)CHB * Sh::TK * sizeof(Slot) + (4 + CHB) * 4 + 16;",
     "(4 + Sh::NCH) * sizeof(int) + 16;",
-    "int pad;\n};",
 ]
+# the slot record lives in the header both kernel files include
+MIRRORED_COMMON = ["int pad;\n};"]
 
 
 def test_mirrored_constants_match_the_kernel_source():
     src = open(SRC).read()
     for line in MIRRORED:
         assert line in src, "kernels.cu changed: update this mirror (%s)" % line
+    common = open(COMMON).read()
+    for line in MIRRORED_COMMON:
+        assert line in common, "device_common.cuh changed: update this mirror (%s)" % line
 
 
 def shape(S, TM, TN):

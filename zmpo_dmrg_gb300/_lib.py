@@ -72,6 +72,7 @@ EXPORTS = {
                                ctypes.c_int),
     "zmpo_plan_groups": ([c_void_p, ctypes.c_int, ctypes.c_int, c_i64_p, c_int_p, c_int_p, c_int_p,
                           c_i64_p], ctypes.c_int),
+    "zmpo_device_status": ([c_void_p, c_int_p, ctypes.c_int], ctypes.c_int),
     "zmpo_plan_destroy": ([c_void_p, ctypes.c_int], ctypes.c_int),
 }
 

@@ -1,7 +1,7 @@
 """Build ``libzmpo_gb300.so`` (the engine's C ABI) in-tree with nvcc for sm_103a.
 
 Run as ``python -m zmpo_dmrg_gb300.build``; ``__graft_entry__.build()`` calls
-``build()``.  Two translation units are compiled in parallel and linked
+``build()``.  Three translation units are compiled in parallel and linked
 against the shared CUDA runtime.  Rebuilds only when a source is newer than
 the library.
 """
@@ -14,8 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libzmpo_gb300.so")
-SOURCES = ["planner.cpp", "kernels.cu"]
-HEADERS = [os.path.join(CSRC, "engine.h"),
+SOURCES = ["planner.cpp", "kernels.cu", "kernels_umma.cu"]
+HEADERS = [os.path.join(CSRC, "engine.h"), os.path.join(CSRC, "device_common.cuh"),
            os.path.join(os.path.dirname(HERE), "include", "zmpo_gb300.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

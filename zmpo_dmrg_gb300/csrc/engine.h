@@ -88,6 +88,11 @@ struct Step {
   // nt, row tiles mt .. mt+pad-1) and the tiles of all other groups
   Work *d_work_tcb[2] = {};    // [64 x 64 tiles, 128 x 32 tiles]
   Work *d_work_tc4[3][4] = {};
+  // 4 digit slices, groups whose whole K fits one exact pass (1 <= K <= 256,
+  // at least 64 rows): tensor-core (tcgen05) work items, Work::pad = row
+  // tiles | K << 8, by column tile 16 / 32 / 64
+  Work *d_work_um[3] = {};
+  int64_t nwork_um[3] = {};
   int64_t nwork_fp64 = 0;
   int64_t nwork_tc[3][4] = {};
   int64_t nwork_tcb[2] = {};
@@ -116,6 +121,9 @@ struct Step {
 int launch_step_fp64(const Step &s, const Bufs &b, void *stream);
 int launch_step_split(const Step &s, const Bufs &b, int nslices, void *stream);
 int launch_reduce(const Step &s, const Bufs &b, void *stream);
+// tcgen05 one-pass kernels (kernels_umma.cu) and their error word
+int launch_step_umma(const Step &s, const Bufs &b, void *stream);
+int umma_device_status(int *code, int reset);
 
 // Diagonal terms for HDiag: out[l, r] += alpha * sum_{a,b,c} Ld[a,l] Wi[a,b]
 // Wj[b,c] Rd[c,r] for one psi block; Ld/Rd are diagonal blocks of the

@@ -1,0 +1,665 @@
+// One-pass split-precision grouped GEMM on the 5th-generation tensor cores
+// (tcgen05 + TMEM), for the groups of a step whose whole K fits one exact
+// pass (1 <= K <= 256 slots).
+//
+// Arithmetic (exact model: tests/split_model.py).  Every FP64 element of a
+// row i of A (column j of B) is cut relative to the row's (column's) largest
+// biased exponent over the group's whole K into four balanced 8-bit digits
+// (X = d0 2^24 + d1 2^16 + d2 2^8 + d3 = floor(|x| / 2^(E-1053)) < 2^31,
+// |digit| <= 128, the element's sign on every digit), held as bf16 planes in
+// shared memory.  The tensor cores form the level sums
+//   L_l = sum_{s+t=l} A_s B_t^T,  l = 0..3  (10 digit products),
+// in FP32 in tensor memory; a digit product is at most 2^14 and a level takes
+// at most four per slot, so for K <= 256 every level is an exact integer
+// below 2^24.  The epilogue combines the levels once per tile into the exact
+// integer S = L0 2^24 + L1 2^16 + L2 2^8 + L3 (< 2^48) and writes
+// S 2^(Ea_i + Eb_j - 2082) as FP64 with integer operations.  The result is
+// a deterministic function of the inputs, bit-identical to the model.
+//
+// Level products on the tensor cores: the B planes of a column tile of TN
+// columns are stacked along N as B' = [B0 | B1 | B2 | B3] (4 TN rows of a
+// K-major operand), and the four level accumulators of a row tile lie side
+// by side in TMEM ([L0 | L1 | L2 | L3], TN columns each), so per 16-slot k
+// step four MMAs  A_a x B'[0, (4-a) TN)  ->  TMEM columns [a TN, 4 TN)
+// (N = 4TN, 3TN, 2TN, TN) issue all ten products.
+//
+// Work item = one column tile of one group and a run of up to 16 row tiles
+// of 128 rows (the TMEM lanes).  The column tile's B is cut once per item
+// and stays in shared memory (all K); A streams through two stages of 32
+// slots.  Warp roles (416 threads):
+//   warps 0-3   epilogue: warp w reads TMEM lanes 32w..32w+31 (one output
+//               row per thread), folds and stores the tile;
+//   warps 4-11  producers: slot table, B cut, per row tile the A row
+//               exponents and the A cut into swizzled planes;
+//   warp 12     TMEM allocation; lane 0 issues the MMAs and commits.
+// Producer -> MMA -> epilogue hand-offs go through mbarriers; the two TMEM
+// accumulator buffers let the epilogue of one row tile overlap the MMAs of
+// the next.  Every wait is bounded in time (2 s): on expiry the kernel
+// records an error code (zmpo_device_status), every role stops at its next
+// item boundary, the MMA issuer's outstanding work is waited for (bounded)
+// and the tensor memory is released before the kernel returns.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/zmpo_gb300.h"
+#include "device_common.cuh"
+#include "engine.h"
+
+namespace zmpo {
+
+__device__ int g_umma_error = 0;
+
+namespace umma {
+
+// ----------------------------------------------------------- constants
+constexpr int TM = 128;             // rows per tile (TMEM lanes)
+constexpr int KMAX = 256;           // slots of one exact pass
+constexpr int KB_SLOTS = 32;        // slots per k block (one 64-byte swizzle row)
+constexpr int NKB_MAX = KMAX / KB_SLOTS;
+constexpr int ROW_BYTES = 64;       // K-major rows of 32 bf16, 64-byte swizzle
+constexpr int A_PLANE = TM * ROW_BYTES;       // 8 KB: one digit plane of a stage
+constexpr int A_STAGE = 4 * A_PLANE;          // 32 KB: four planes
+constexpr int NSTAGE = 2;
+constexpr int NTHREADS = 416;
+constexpr int EPI_WARPS = 4, PROD_WARP0 = 4, PROD_WARPS = 8, MMA_WARP = 12;
+constexpr int NPROD = PROD_WARPS * 32;        // 256 producer threads
+constexpr int BIAS = 2082;
+constexpr uint64_t WAIT_NS = 2000000000ull;   // 2 s bound on every wait
+
+// error codes recorded in g_umma_error (first one wins)
+constexpr int ERR_TIMEOUT_BASE = 100;         // + site of the wait
+
+template <int TN>
+struct Layout {
+  static constexpr int B_KB = 4 * TN * ROW_BYTES;     // one k block of the four B planes
+  static constexpr int OFF_B = 0;
+  static constexpr int OFF_A = OFF_B + NKB_MAX * B_KB;
+  static constexpr int OFF_SLOTS = OFF_A + NSTAGE * A_STAGE;
+  static constexpr int OFF_REC = OFF_SLOTS + KMAX * (int)sizeof(Slot);
+  // tile record (one per TMEM buffer): row exponents, column exponents,
+  // output address of (row 0, column c) and the row stride, rows and buffer
+  static constexpr int REC_EA = 0;
+  static constexpr int REC_EB = REC_EA + TM * 4;
+  static constexpr int REC_CB = REC_EB + TN * 4;           // int64 colbase[TN]
+  static constexpr int REC_RS = REC_CB + TN * 8;           // int64 rowstride[TN]
+  static constexpr int REC_INFO = REC_RS + TN * 8;         // int m0, M, cbuf, pad
+  static constexpr int REC_BYTES = REC_INFO + 16;
+  static constexpr int OFF_ITEM = OFF_REC + 2 * REC_BYTES; // item: ebmax[TN], colbase[TN], rowstride[TN]
+  static constexpr int ITEM_BYTES = TN * 4 + TN * 16;
+  static constexpr int OFF_BAR = (OFF_ITEM + ITEM_BYTES + 7) / 8 * 8;
+  static constexpr int NBAR = 15;
+  static constexpr int OFF_MISC = OFF_BAR + NBAR * 8;      // tmem base, abort flag, ktot, scaled
+  static constexpr int BYTES = OFF_MISC + 16;
+  static constexpr int SMEM = BYTES + 1024;                // + alignment of the base to 1024
+  static constexpr int TMEM_COLS = 8 * TN;                 // two buffers of four levels
+  static_assert(TN == 16 || TN == 32 || TN == 64, "column tile");
+  static_assert(OFF_A % 1024 == 0 && A_STAGE % 1024 == 0 && B_KB % 512 == 0, "swizzle atoms");
+  static_assert(OFF_SLOTS % 16 == 0 && OFF_REC % 16 == 0 && REC_BYTES % 16 == 0, "alignment");
+  static_assert(SMEM <= 232448, "shared memory");
+};
+
+// barrier indices
+enum {
+  BAR_A_FULL = 0,    // [2] producers (256 arrivals) -> MMA
+  BAR_A_EMPTY = 2,   // [2] MMA commit -> producers
+  BAR_T_FULL = 4,    // [2] MMA commit (tile done) -> epilogue
+  BAR_T_EMPTY = 6,   // [2] epilogue (128) -> MMA
+  BAR_E_FULL = 8,    // [2] tile record written, producers (256) -> epilogue
+  BAR_E_EMPTY = 10,  // [2] tile record read, epilogue (128) -> producers
+  BAR_B_FULL = 12,   // B planes of the item cut, producers (256) -> MMA
+  BAR_B_FREE = 13,   // MMA commit after the item -> producers
+  BAR_DONE = 14      // MMA commit at the end (teardown)
+};
+
+// ------------------------------------------------------------- PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void bar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void bar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool bar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred P1;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
+      "selp.b32 %0, 1, 0, P1;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Wait for the phase of parity `parity` of barrier `bar` to complete, at most
+// WAIT_NS.  Returns false (at once) when the kernel is aborting, or after
+// recording a timeout at `site` and raising the abort flag.
+__device__ __noinline__ bool wait_bounded(uint32_t bar, uint32_t parity, volatile int *abort_flag, int site,
+                                          bool heed_abort = true) {
+  if (bar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  while (true) {
+    if (bar_try_wait(bar, parity)) return true;
+    if (heed_abort && *abort_flag) return false;
+    if (globaltimer() - t0 > WAIT_NS) {
+      *abort_flag = 1;
+      atomicCAS(&g_umma_error, 0, ERR_TIMEOUT_BASE + site);
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// barrier of the producer warps (id 1) or epilogue warps (id 2) that also
+// returns the OR of `v` over the participating threads
+__device__ __forceinline__ bool role_sync_or(int id, int nthreads, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 q, %1, 0;\n\t"
+      "bar.red.or.pred p, %2, %3, q;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(id), "r"(nthreads)
+      : "memory");
+  return r != 0;
+}
+
+__device__ __forceinline__ void role_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 64-byte swizzle (8-row groups of
+// 64-byte rows, 512 bytes apart), version 1.
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)1u << 16) | ((uint64_t)(512u >> 4) << 32) |
+         ((uint64_t)1u << 46) | ((uint64_t)4u << 61);
+}
+
+// Instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major,
+// M = 128, N = n.
+__device__ __forceinline__ uint32_t idesc(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t id, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+      ::"r"(dtmem), "l"(ad), "l"(bd), "r"(id), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *v) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+        "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr)
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// ------------------------------------------------------------ digit cut
+__device__ __forceinline__ int dexp(double x) { return (int)(((unsigned)__double2hiint(x) >> 20) & 0x7ffu); }
+
+// Y = floor(|x| / 2^(E-1053)) + 0x808080 (E >= exponent of x): the bytes of
+// Y are d0, d1+128, d2+128, d3+128
+__device__ __forceinline__ uint32_t balanced(double x, int E) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const int e = (int)((hi >> 20) & 0x7ffu);
+  const uint32_t top = e ? ((((hi & 0xfffffu) | 0x100000u) << 11) | (lo >> 21)) : 0u;
+  return (__funnelshift_rc(top, 0u, (unsigned)(E - e)) >> 1) + 0x808080u;
+}
+
+// byte K of Y minus OFF as the bit pattern of an exact float (PRMT + FADD)
+template <int K, int OFF>
+__device__ __forceinline__ float byte_f(uint32_t Y) {
+  return __uint_as_float(__byte_perm(Y, 0x4B000000u, 0x7440u | K)) - (8388608.0f + (float)OFF);
+}
+
+// digit planes of two elements (k, k+1) as packed bf16 pairs: the bf16 of a
+// small integer-valued float is its upper half; the sign flips every digit
+__device__ __forceinline__ void cut_pair(double x0, double x1, int E, uint32_t d[4]) {
+  const uint32_t Y0 = balanced(x0, E), Y1 = balanced(x1, E);
+  const uint32_t sg = ((unsigned)__double2hiint(x0) >> 16 & 0x8000u) | ((unsigned)__double2hiint(x1) & 0x80000000u);
+  d[0] = __byte_perm(__float_as_uint(byte_f<3, 0>(Y0)), __float_as_uint(byte_f<3, 0>(Y1)), 0x7632u) ^ sg;
+  d[1] = __byte_perm(__float_as_uint(byte_f<2, 128>(Y0)), __float_as_uint(byte_f<2, 128>(Y1)), 0x7632u) ^ sg;
+  d[2] = __byte_perm(__float_as_uint(byte_f<1, 128>(Y0)), __float_as_uint(byte_f<1, 128>(Y1)), 0x7632u) ^ sg;
+  d[3] = __byte_perm(__float_as_uint(byte_f<0, 128>(Y0)), __float_as_uint(byte_f<0, 128>(Y1)), 0x7632u) ^ sg;
+}
+
+// Cut 8 consecutive slots (one 16-byte chunk per plane) of one row of a
+// K-major plane set: rowaddr = byte address of row 0 of plane 0 plus
+// row * 64, plane stride in bytes, chunk = slot / 8 within the k block.
+__device__ __forceinline__ void cut8_store(const double *v, int E, unsigned char *plane0, int plane_bytes, int row,
+                                           int chunk) {
+  uint32_t d[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    uint32_t p[4];
+    cut_pair(v[2 * i], v[2 * i + 1], E, p);
+#pragma unroll
+    for (int s = 0; s < 4; ++s) d[s][i] = p[s];
+  }
+  const int off = row * ROW_BYTES + ((chunk ^ ((row >> 1) & 3)) << 4);
+#pragma unroll
+  for (int s = 0; s < 4; ++s)
+    *reinterpret_cast<uint4 *>(plane0 + s * plane_bytes + off) = make_uint4(d[s][0], d[s][1], d[s][2], d[s][3]);
+}
+
+// S 2^e as FP64 with integer operations (|S| < 2^53: exact); results below
+// the normal range are flushed to zero
+__device__ __forceinline__ double scaled_int_to_double(long long S, int e) {
+  if (S == 0) return 0.0;
+  const unsigned long long sign = S < 0 ? 0x8000000000000000ull : 0ull;
+  const unsigned long long A = (unsigned long long)(S < 0 ? -S : S);
+  const int n = 63 - __clzll((long long)A);
+  const int be = n + e + 1023;
+  if (be <= 0) return 0.0;
+  const unsigned long long mant = (A << (52 - n)) & 0xfffffffffffffull;
+  return __longlong_as_double((long long)(sign | ((unsigned long long)be << 52) | mant));
+}
+
+__device__ __forceinline__ long long lvl(uint32_t bits) { return (long long)__float2int_rz(__uint_as_float(bits)); }
+
+// Slot table of all K slots of a group (one warp): lanes take segments 32 at
+// a time, an inclusive scan places each segment's k range.  Returns K; sets
+// *scaled when some slot has a weight other than 1.
+__device__ int build_slots(const Group &g, const Seg *__restrict__ segs, const Bufs &bufs, Slot *slots, int lane,
+                           int *scaled) {
+  int base = 0;
+  unsigned sc = 0;
+  for (int s0 = 0; s0 < g.nseg; s0 += 32) {
+    const int sidx = s0 + lane;
+    Seg sg;
+    int k = 0;
+    if (sidx < g.nseg) {
+      sg = segs[g.seg0 + sidx];
+      k = sg.K;
+    }
+    int incl = k;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const int excl = incl - k;
+    if (k > 0 && base + incl <= KMAX) {
+      const double *A = bufs.p[sg.abuf] + sg.a_off;
+      const double *B = g.ncb ? bufs.p[sg.bbuf] : bufs.p[sg.bbuf] + sg.b_off;
+      for (int j = 0; j < k; ++j) {
+        Slot &sl = slots[base + excl + j];
+        sl.a = A + (int64_t)j * sg.sak;
+        sl.b = g.ncb ? B : B + (int64_t)j * sg.sbk;
+        sl.sam = sg.sam;
+        sl.sbn = sg.sbn;
+        sl.alpha = sg.alpha;
+        sl.scaled = sg.alpha != 1.0;
+        sl.seg = sidx;
+        sl.kk = j;
+      }
+    }
+    sc |= __ballot_sync(0xffffffffu, k > 0 && sg.alpha != 1.0);
+    base += __shfl_sync(0xffffffffu, incl, 31);
+  }
+  *scaled = sc != 0u;
+  return base;
+}
+
+}  // namespace umma
+
+// ------------------------------------------------------------------ kernel
+template <int TN>
+__global__ void __launch_bounds__(umma::NTHREADS, 1)
+k_step_umma(const Work *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
+            const Seg *__restrict__ segs, const ColBlock *__restrict__ cbl, const SegB *__restrict__ segb,
+            Bufs bufs) {
+  using namespace umma;
+  using LY = Layout<TN>;
+  extern __shared__ unsigned char smem_raw[];
+  const uint32_t raw_s = smem_u32(smem_raw);
+  const uint32_t base_s = (raw_s + 1023u) & ~1023u;
+  unsigned char *sm = smem_raw + (base_s - raw_s);
+  unsigned char *Bpl = sm + LY::OFF_B;
+  unsigned char *Ast = sm + LY::OFF_A;
+  Slot *slots = reinterpret_cast<Slot *>(sm + LY::OFF_SLOTS);
+  unsigned char *rec0 = sm + LY::OFF_REC;
+  int *it_eb = reinterpret_cast<int *>(sm + LY::OFF_ITEM);
+  long long *it_cb = reinterpret_cast<long long *>(sm + LY::OFF_ITEM + TN * 4);
+  long long *it_rs = it_cb + TN;
+  const uint32_t bar0 = base_s + LY::OFF_BAR;
+  uint32_t *misc = reinterpret_cast<uint32_t *>(sm + LY::OFF_MISC);  // [0] tmem, [1] abort, [2] K, [3] scaled
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(misc + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  auto bar = [&](int i) { return bar0 + 8u * (uint32_t)i; };
+
+  if (warp == MMA_WARP) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(misc)),
+                 "r"(LY::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < 2; ++s) {
+      bar_init(bar(BAR_A_FULL + s), NPROD);
+      bar_init(bar(BAR_A_EMPTY + s), 1);
+      bar_init(bar(BAR_T_FULL + s), 1);
+      bar_init(bar(BAR_T_EMPTY + s), EPI_WARPS * 32);
+      bar_init(bar(BAR_E_FULL + s), NPROD);
+      bar_init(bar(BAR_E_EMPTY + s), EPI_WARPS * 32);
+    }
+    bar_init(bar(BAR_B_FULL), NPROD);
+    bar_init(bar(BAR_B_FREE), 1);
+    bar_init(bar(BAR_DONE), 1);
+    misc[1] = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = misc[0];
+
+  if (warp >= PROD_WARP0 && warp < PROD_WARP0 + PROD_WARPS) {
+    // ================================================================ producers
+    const int pt = tid - PROD_WARP0 * 32;  // 0..255
+    const int arow = pt >> 1, half = pt & 1;
+    uint32_t q = 0, t = 0, item = 0;
+    for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x, ++item) {
+      if (role_sync_or(1, NPROD, *abort_flag != 0)) break;
+      const Work wk = work[w];
+      const Group g = groups[wk.group];
+      const int nrt = wk.pad & 0xff;
+      const int n0 = wk.nt;
+      if (pt < 32) {
+        int sc;
+        const int K = build_slots(g, segs, bufs, slots, lane, &sc);
+        if (lane == 0) {
+          misc[2] = (uint32_t)K;
+          misc[3] = (uint32_t)sc;
+        }
+      }
+      // column map of the tile: output address of (row 0, column c), row stride
+      for (int c = pt; c < TN; c += NPROD) {
+        const int col = n0 + c;
+        long long cbase = -1, rs = 0;
+        if (col < g.N) {
+          if (g.ncb == 0) {
+            cbase = g.c_off + (long long)col * g.scn;
+            rs = g.scm;
+          } else {
+            int rel;
+            const int j = find_cblock(cbl, g, col, rel);
+            if (j >= 0) {
+              const ColBlock cb = cbl[g.cb0 + j];
+              cbase = cb.c_off + (long long)rel * cb.scn;
+              rs = cb.scm;
+            }
+          }
+        }
+        it_cb[c] = cbase;
+        it_rs[c] = rs;
+        it_eb[c] = 0;
+      }
+      role_sync(1, NPROD);
+      const int K = (int)misc[2];
+      const bool scaled = misc[3] != 0;
+      const int nkb = (K + KB_SLOTS - 1) / KB_SLOTS;
+      // ---- B of the column tile: column exponents over all K, then the cut
+      wait_bounded(bar(BAR_B_FREE), (item & 1) ^ 1, abort_flag, 1);
+      const int ngrp = nkb * 4;  // 8-slot groups per column
+      for (int idx = pt; idx < TN * ngrp; idx += NPROD) {
+        const int c = idx % TN, g8 = idx / TN, col = n0 + c;
+        int jb = -1, rel = 0;
+        if (g.ncb && col < g.N) jb = find_cblock(cbl, g, col, rel);
+        int em = 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int j = g8 * 8 + i;
+          double x = 0.0;
+          if (j < K && col < g.N)
+            x = g.ncb ? load_b_cb(slots[j], segb, g, jb, rel) : __ldg(slots[j].b + (int64_t)col * slots[j].sbn);
+          em = max(em, dexp(x));
+        }
+        atomicMax(it_eb + c, em);
+      }
+      role_sync(1, NPROD);
+      for (int idx = pt; idx < TN * ngrp; idx += NPROD) {
+        const int c = idx % TN, g8 = idx / TN, col = n0 + c;
+        int jb = -1, rel = 0;
+        if (g.ncb && col < g.N) jb = find_cblock(cbl, g, col, rel);
+        double v[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int j = g8 * 8 + i;
+          double x = 0.0;
+          if (j < K && col < g.N)
+            x = g.ncb ? load_b_cb(slots[j], segb, g, jb, rel) : __ldg(slots[j].b + (int64_t)col * slots[j].sbn);
+          v[i] = x;
+        }
+        // k block g8/4, chunk g8%4; B' row of plane s = s*TN + c
+        cut8_store(v, it_eb[c], Bpl + (g8 >> 2) * LY::B_KB, TN * ROW_BYTES, c, g8 & 3);
+      }
+      fence_proxy_async();
+      bar_arrive(bar(BAR_B_FULL));
+      // ---- row tiles
+      for (int r = 0; r < nrt; ++r, ++t) {
+        const int m0 = wk.mt + r * TM, grow = m0 + arow;
+        const bool rv = grow < g.M;
+        int em = 0;
+        if (rv) {
+          for (int j = half; j < K; j += 2) {
+            double x = __ldg(slots[j].a + (int64_t)grow * slots[j].sam);
+            if (scaled && slots[j].scaled) x *= slots[j].alpha;
+            em = max(em, dexp(x));
+          }
+        }
+        em = max(em, __shfl_xor_sync(0xffffffffu, em, 1));
+        const uint32_t b = t & 1, u = t >> 1;
+        wait_bounded(bar(BAR_E_EMPTY + b), (u & 1) ^ 1, abort_flag, 2);
+        unsigned char *rec = rec0 + b * LY::REC_BYTES;
+        if (half == 0) reinterpret_cast<int *>(rec + LY::REC_EA)[arow] = em;
+        for (int c = pt; c < TN; c += NPROD) {
+          reinterpret_cast<int *>(rec + LY::REC_EB)[c] = it_eb[c];
+          reinterpret_cast<long long *>(rec + LY::REC_CB)[c] = it_cb[c];
+          reinterpret_cast<long long *>(rec + LY::REC_RS)[c] = it_rs[c];
+        }
+        if (pt == 0) {
+          int *info = reinterpret_cast<int *>(rec + LY::REC_INFO);
+          info[0] = m0;
+          info[1] = g.M;
+          info[2] = g.cbuf;
+        }
+        bar_arrive(bar(BAR_E_FULL + b));
+        for (int kb = 0; kb < nkb; ++kb, ++q) {
+          const uint32_t s = q & 1, us = q >> 1;
+          wait_bounded(bar(BAR_A_EMPTY + s), (us & 1) ^ 1, abort_flag, 3);
+          unsigned char *st = Ast + s * A_STAGE;
+#pragma unroll
+          for (int cc = 0; cc < 2; ++cc) {
+            double v[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+              const int j = kb * KB_SLOTS + half * 16 + cc * 8 + i;
+              double x = 0.0;
+              if (rv && j < K) {
+                x = __ldg(slots[j].a + (int64_t)grow * slots[j].sam);
+                if (scaled && slots[j].scaled) x *= slots[j].alpha;
+              }
+              v[i] = x;
+            }
+            cut8_store(v, em, st, A_PLANE, arow, half * 2 + cc);
+          }
+          fence_proxy_async();
+          bar_arrive(bar(BAR_A_FULL + s));
+        }
+      }
+      // the slot table and the item arrays are rewritten by the next item
+      role_sync(1, NPROD);
+    }
+  } else if (warp == MMA_WARP) {
+    // ====================================================================== MMA
+    if (lane == 0) {
+      uint32_t q = 0, t = 0, item = 0;
+      for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x, ++item) {
+        if (*abort_flag) break;
+        const Work wk = work[w];
+        const int nrt = wk.pad & 0xff, K = wk.pad >> 8;
+        const int nkb = (K + KB_SLOTS - 1) / KB_SLOTS;
+        wait_bounded(bar(BAR_B_FULL), item & 1, abort_flag, 4);
+        tc_fence_after();
+        for (int r = 0; r < nrt; ++r, ++t) {
+          const uint32_t b = t & 1, u = t >> 1;
+          wait_bounded(bar(BAR_T_EMPTY + b), (u & 1) ^ 1, abort_flag, 5);
+          tc_fence_after();
+          for (int kb = 0; kb < nkb; ++kb, ++q) {
+            const uint32_t s = q & 1, us = q >> 1;
+            const bool ok = wait_bounded(bar(BAR_A_FULL + s), us & 1, abort_flag, 6);
+            tc_fence_after();
+            if (ok) {
+              const uint32_t a_s = base_s + LY::OFF_A + s * A_STAGE;
+              const uint32_t b_s = base_s + LY::OFF_B + kb * LY::B_KB;
+#pragma unroll
+              for (int k16 = 0; k16 < 2; ++k16) {
+                if (kb * KB_SLOTS + k16 * 16 >= K) break;
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                  const uint32_t d = tmem + b * (4 * TN) + a * TN;
+                  mma(d, sdesc(a_s + a * A_PLANE + k16 * 32), sdesc(b_s + k16 * 32), idesc((4 - a) * TN),
+                      (kb | k16 | a) != 0);
+                }
+              }
+            }
+            commit(bar(BAR_A_EMPTY + s));
+          }
+          commit(bar(BAR_T_FULL + b));
+        }
+        commit(bar(BAR_B_FREE));
+      }
+      commit(bar(BAR_DONE));
+    }
+    __syncwarp();
+  } else {
+    // ================================================================= epilogue
+    const int e = tid;  // row of the tile, warp e/32 reads TMEM lanes 32(e/32)..
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    uint32_t t = 0;
+    for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+      if (role_sync_or(2, EPI_WARPS * 32, *abort_flag != 0)) break;
+      const Work wk = work[w];
+      const int nrt = wk.pad & 0xff;
+      for (int r = 0; r < nrt; ++r, ++t) {
+        const uint32_t b = t & 1, u = t >> 1;
+        wait_bounded(bar(BAR_E_FULL + b), u & 1, abort_flag, 7);
+        const unsigned char *rec = rec0 + b * LY::REC_BYTES;
+        const int *info = reinterpret_cast<const int *>(rec + LY::REC_INFO);
+        const int m0 = info[0], M = info[1], cbuf = info[2];
+        const int ea = reinterpret_cast<const int *>(rec + LY::REC_EA)[e];
+        const int *eb = reinterpret_cast<const int *>(rec + LY::REC_EB);
+        const long long *cb = reinterpret_cast<const long long *>(rec + LY::REC_CB);
+        const long long *rs = reinterpret_cast<const long long *>(rec + LY::REC_RS);
+        const int row = m0 + e;
+        const bool ok = wait_bounded(bar(BAR_T_FULL + b), u & 1, abort_flag, 8);
+        tc_fence_after();
+        double *out = bufs.p[cbuf];
+#pragma unroll 1
+        for (int c0 = 0; c0 < TN; c0 += 16) {
+          uint32_t v[4][16];
+          const uint32_t ta = tmem + lane_base + b * (4 * TN) + c0;
+#pragma unroll
+          for (int l = 0; l < 4; ++l) tmem_ld16(ta + l * TN, v[l]);
+          tmem_ld_wait();
+          if (ok && row < M) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+              const long long base = cb[c0 + i];
+              if (base < 0) continue;
+              const long long S = (lvl(v[0][i]) << 24) + (lvl(v[1][i]) << 16) + (lvl(v[2][i]) << 8) + lvl(v[3][i]);
+              out[base + (long long)row * rs[c0 + i]] = scaled_int_to_double(S, ea + eb[c0 + i] - BIAS);
+            }
+          }
+        }
+        tc_fence_before();
+        bar_arrive(bar(BAR_T_EMPTY + b));
+        bar_arrive(bar(BAR_E_EMPTY + b));
+      }
+    }
+  }
+
+  // ---- teardown: wait for the MMA issuer's last commit, release TMEM
+  tc_fence_before();
+  __syncthreads();
+  if (warp == MMA_WARP) {
+    tc_fence_after();
+    // the issuer's last commit completes once every MMA it issued has
+    // finished writing TMEM (waited for even when aborting)
+    if (lane == 0) wait_bounded(bar(BAR_DONE), 0, abort_flag, 9, false);
+    __syncwarp();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(LY::TMEM_COLS)
+                 : "memory");
+  }
+}
+
+template <int TN>
+static int launch_umma_t(const Work *work, int64_t nwork, const Step &s, const Bufs &b, void *stream) {
+  if (nwork == 0) return ZMPO_OK;
+  constexpr int smem = umma::Layout<TN>::SMEM;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_step_umma<TN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return record_cuda_error("k_step_umma: shared memory attribute", (int)e);
+    attr = true;
+  }
+  int dev = 0, nsm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int grid = (int)(nwork < nsm ? nwork : nsm);
+  k_step_umma<TN><<<grid, umma::NTHREADS, smem, (cudaStream_t)stream>>>(work, nwork, s.d_groups, s.d_segs,
+                                                                        s.d_cblocks, s.d_segb, b);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? ZMPO_OK : record_cuda_error("k_step_umma", (int)e);
+}
+
+int launch_step_umma(const Step &s, const Bufs &b, void *stream) {
+  int rc;
+  if ((rc = launch_umma_t<64>(s.d_work_um[2], s.nwork_um[2], s, b, stream))) return rc;
+  if ((rc = launch_umma_t<32>(s.d_work_um[1], s.nwork_um[1], s, b, stream))) return rc;
+  return launch_umma_t<16>(s.d_work_um[0], s.nwork_um[0], s, b, stream);
+}
+
+int umma_device_status(int *code, int reset) {
+  int v = 0;
+  cudaError_t e = cudaMemcpyFromSymbol(&v, g_umma_error, sizeof(int));
+  if (e != cudaSuccess) return record_cuda_error("device_status", (int)e);
+  if (code) *code = v;
+  if (reset && v) {
+    const int z = 0;
+    e = cudaMemcpyToSymbol(g_umma_error, &z, sizeof(int));
+    if (e != cudaSuccess) return record_cuda_error("device_status reset", (int)e);
+  }
+  return ZMPO_OK;
+}
+
+}  // namespace zmpo

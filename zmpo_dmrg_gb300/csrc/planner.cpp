@@ -13,6 +13,7 @@
 #include <array>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <tuple>
@@ -873,10 +874,23 @@ static void split_long_groups(Step &st) {
   st.part_elems = part;
 }
 
+// Groups the one-pass tensor-core kernel (kernels_umma.cu) takes in the
+// 4-slice path: the whole K in one exact pass, at least half a row tile.
+// ZMPO_SPLIT_LEGACY=1 in the environment keeps every group on the mma.sync
+// kernels (for comparisons).
+constexpr int kUmmaMaxK = 256, kUmmaMinM = 64, kUmmaTM = 128, kUmmaRun = 16;
+static bool umma_enabled() {
+  static const bool on = [] {
+    const char *v = std::getenv("ZMPO_SPLIT_LEGACY");
+    return !(v && v[0] == '1');
+  }();
+  return on;
+}
+
 static int upload_step(Step &st) {
   if (st.uploaded) return ZMPO_OK;
   split_long_groups(st);
-  std::vector<Work> w64, wtc[3][4], wtc4[3][4], wtcb[2];
+  std::vector<Work> w64, wtc[3][4], wtc4[3][4], wtcb[2], wum[3];
   // order groups by cost (longest first) for load balance
   std::vector<int> order(st.groups.size());
   std::iota(order.begin(), order.end(), 0);
@@ -892,6 +906,7 @@ static int upload_step(Step &st) {
   }
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
   st.mma_macs[0] = st.mma_macs[1] = st.mma_macs[2] = 0.0;
+  const bool um = umma_enabled();
   for (int g : order) {
     const Group &G = st.groups[g];
     const double k16 = (double)((ktot[g] + 15) / 16 * 16);
@@ -900,6 +915,25 @@ static int upload_step(Step &st) {
         w64.push_back({g, m0, n0, 0});
         st.mma_macs[0] += (double)kTileFP64M * kTileFP64N * k16;
       }
+    // one-pass tensor-core items: full 64-column tiles, then a 16/32/64 tile
+    // for the rest; runs of at most kUmmaRun row tiles of 128, balanced
+    const bool one_pass = um && ktot[g] >= 1 && ktot[g] <= kUmmaMaxK && G.M >= kUmmaMinM && G.N >= 1;
+    if (one_pass) {
+      const int nrt = (G.M + kUmmaTM - 1) / kUmmaTM;
+      const int nruns = (nrt + kUmmaRun - 1) / kUmmaRun;
+      const int len = (nrt + nruns - 1) / nruns;
+      for (int n0 = 0; n0 < G.N;) {
+        const int rem = G.N - n0;
+        const int tn = rem >= 64 ? 64 : (rem <= 16 ? 16 : (rem <= 32 ? 32 : 64));
+        const int ti = tn == 16 ? 0 : (tn == 32 ? 1 : 2);
+        for (int r = 0; r < nrt; r += len) {
+          const int n = std::min(len, nrt - r);
+          wum[ti].push_back({g, r * kUmmaTM, n0, n | ((int32_t)ktot[g] << 8)});
+        }
+        st.mma_macs[1] += (double)nrt * kUmmaTM * tn * k16;
+        n0 += tn;
+      }
+    }
     // Tensor-core tiles.  Columns: full pieces of the widest tile, then one
     // narrower tile for the rest (the smallest of 8/16/32/64 that holds it),
     // so a group of 74 columns takes 64 + 16 instead of 64 + 64.  64-column
@@ -927,7 +961,7 @@ static int upload_step(Step &st) {
       size_t nfull = 0;
       if (bres >= 0 && G.nseg <= 32 && ktot[g] <= kBresMaxK)
         while (nfull < rows.size() && rows[nfull].second == hmax) ++nfull;
-      if (nfull < 2) nfull = 0;
+      if (nfull < 2 || one_pass) nfull = 0;
       if (nfull) {
         const int nruns = (int)((nfull + kBresRun - 1) / kBresRun);
         const int len = (int)((nfull + nruns - 1) / nruns);
@@ -937,9 +971,9 @@ static int upload_step(Step &st) {
       for (size_t r = 0; r < rows.size(); ++r) {
         const int tmi = rows[r].second == 32 ? 0 : (rows[r].second == 64 ? 1 : 2);
         wtc[tmi][tni].push_back({g, rows[r].first, n0, 0});
-        if (r >= nfull) wtc4[tmi][tni].push_back({g, rows[r].first, n0, 0});
+        if (r >= nfull && !one_pass) wtc4[tmi][tni].push_back({g, rows[r].first, n0, 0});
         const double macs = (double)rows[r].second * tn * k16;
-        st.mma_macs[1] += macs;  // the same tiles, B-resident or not
+        if (!one_pass) st.mma_macs[1] += macs;  // the same tiles, B-resident or not
         st.mma_macs[2] += macs;
       }
       n0 += tn;
@@ -952,6 +986,7 @@ static int upload_step(Step &st) {
       st.nwork_tc4[i][j] = (int64_t)wtc4[i][j].size();
     }
   for (int i = 0; i < 2; ++i) st.nwork_tcb[i] = (int64_t)wtcb[i].size();
+  for (int i = 0; i < 3; ++i) st.nwork_um[i] = (int64_t)wum[i].size();
   auto up = [](auto **dptr, const auto &v) -> cudaError_t {
     using T = typename std::remove_reference<decltype(v)>::type::value_type;
     if (v.empty()) {
@@ -973,6 +1008,7 @@ static int upload_step(Step &st) {
       CUDA_TRY(up(&st.d_work_tc4[i][j], wtc4[i][j]));
     }
   for (int i = 0; i < 2; ++i) CUDA_TRY(up(&st.d_work_tcb[i], wtcb[i]));
+  for (int i = 0; i < 3; ++i) CUDA_TRY(up(&st.d_work_um[i], wum[i]));
   CUDA_TRY(up(&st.d_reds, st.reds));
   if (st.part_elems > 0) CUDA_TRY(cudaMalloc((void **)&st.d_part, st.part_elems * sizeof(double)));
   // keep the host mirror of groups (sizes) but free the bulky segment copy
@@ -1002,6 +1038,10 @@ static void free_step(Step &st) {
   for (int i = 0; i < 2; ++i) {
     cudaFree(st.d_work_tcb[i]);
     st.d_work_tcb[i] = nullptr;
+  }
+  for (int i = 0; i < 3; ++i) {
+    cudaFree(st.d_work_um[i]);
+    st.d_work_um[i] = nullptr;
   }
   cudaFree(st.d_reds);
   cudaFree(st.d_part);
@@ -1601,7 +1641,8 @@ int zmpo_plan_kernel_count(zmpo_engine *e, int plan_id, int precision, int *coun
       const bool s4 = precision == ZMPO_PREC_SPLIT;
       for (int a = 0; a < 3; ++a)
         for (int c = 0; c < 4; ++c) n += (s4 ? s.nwork_tc4[a][c] : s.nwork_tc[a][c]) > 0;
-      if (s4) n += (s.nwork_tcb[0] > 0) + (s.nwork_tcb[1] > 0);
+      if (s4) n += (s.nwork_tcb[0] > 0) + (s.nwork_tcb[1] > 0) + (s.nwork_um[0] > 0) + (s.nwork_um[1] > 0) +
+                   (s.nwork_um[2] > 0);
     }
     n += s.red_elems > 0;
   }
@@ -1898,6 +1939,11 @@ int zmpo_plan_step_tasks(zmpo_engine *e, int plan_id, int step, int64_t *counts,
   if (cblocks) memcpy(cblocks, st.cblocks.data(), st.cblocks.size() * sizeof(ColBlock));
   if (segb) memcpy(segb, st.segb.data(), st.segb.size() * sizeof(SegB));
   return ZMPO_OK;
+}
+
+int zmpo_device_status(zmpo_engine *e, int *code, int reset) {
+  if (!e || !code) return fail(ZMPO_E_ARG, "device_status: null argument");
+  return umma_device_status(code, reset);
 }
 
 int zmpo_plan_destroy(zmpo_engine *e, int plan_id) {

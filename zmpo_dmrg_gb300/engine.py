@@ -173,6 +173,12 @@ class Engine:
         k = n.value
         return M[:k], N[:k], S[:k], Kt[:k]
 
+    def device_status(self, reset=False):
+        """Error word of the device kernels (0: none); see zmpo_device_status."""
+        code = ctypes.c_int()
+        check(_lib.lib().zmpo_device_status(self.h, ctypes.byref(code), 1 if reset else 0), "device_status")
+        return code.value
+
     def destroy_plan(self, pid):
         check(_lib.lib().zmpo_plan_destroy(self.h, pid), "plan_destroy")
 

@@ -52,6 +52,21 @@ def init_spatial_orb(norb, isym=2):
     return [q.copy() for _ in range(norb)]
 
 
+def dense_sector(qlst, key):
+    """Ascending dense indices of the elements of the tensor with legs
+    ``qlst`` whose labels add up to ``key``."""
+    qs = [numpy.asarray(q, dtype=float) for q in qlst]
+    nq = qs[0].shape[1]
+    tot = numpy.zeros([len(q) for q in qs] + [nq])
+    for i, q in enumerate(qs):
+        shape = [1] * len(qs) + [nq]
+        shape[i] = len(q)
+        tot = tot + q.reshape(shape)
+    tot = tot.reshape(-1, nq)
+    k = numpy.asarray(key, dtype=float).reshape(-1)[:nq]
+    return numpy.flatnonzero(numpy.abs(tot - k).sum(axis=1) < 1e-10)
+
+
 def rdm_blkdiag(rho0, classes, thresh, Dcut=-1):
     """Block eigen-decomposition of the reduced density matrix by sector and
     truncation (mpo_dmrg_qparser.rdm_blkdiag, mpo_dmrg_qparser.py:106-183)."""
@@ -129,6 +144,9 @@ class mpo_dmrg:
         self.opers = []
         self.nops = None
         self.ifQt = True
+        # first MPS from occun when default() gets none (mpo_dmrg_class.py:113-115)
+        self.initNsweep = 0
+        self.initNcsite = 1
         # this driver keeps Davidson vectors and diagonals on the device
         self.device_vectors = True
         self.qkey = None
@@ -273,6 +291,40 @@ class mpo_dmrg:
             fmps['qnum%d' % i] = qn[i]
         return fmps
 
+    def product_mps_right(self):
+        """The same occupation-number product state as right-canonical sites
+        [l, n, r] (status [T, F, F]) with the reference's right labels
+        qnumr[i] = (N - N_left(i), Sz - Sz_left(i)) (mps0occun, 118-155)."""
+        left = self.product_mps()
+        qn = [numpy.asarray(left['qnum%d' % i], dtype=float) for i in range(self.nsite + 1)]
+        tot = qn[-1]
+        qr = [tot - q for q in qn]
+        fmps = {'nsite': self.nsite}
+        for i in range(self.nsite):
+            d = numpy.asarray(left['site%d' % i].toDenseTensor(left['site%d' % i].idlst))
+            fmps['site%d' % i] = self.site_qt(i, d, [qr[i], self.qphys[i], qr[i + 1]], [True, False, False])
+        return qn, qr, fmps
+
+    def initMPS(self):
+        """Initial MPS when no MPS is given (mpo_dmrg_util.initMPS, 158-190):
+        the occupation-number product state, its right environments, then one
+        left sweep of ``initNcsite``-site dots under the first schedule entry
+        (the perturbed density matrix grows the bond dimension), plus
+        ``initNsweep`` further sweep pairs."""
+        qn, qr, fmps0 = self.product_mps_right()
+        self.qnuml = [q.copy() for q in qn]
+        self.qnumr = [q.copy() for q in qr]
+        self.envs[('lop', -1)] = self.boundary_env()
+        if self.ifs2proj:
+            self.envs[('lpop', -1)] = spinproj.boundary_pops(self)
+        self.genHops(fmps0, 'rop')
+        sitelst = list(range(self.nsite))
+        self.sweep(sitelst, self.initNcsite, 'L')
+        for _ in range(self.initNsweep):
+            self.sweep(sitelst, self.initNcsite, 'R')
+            self.sweep(sitelst, self.initNcsite, 'L')
+        return 0
+
     def _flst(self, lsite, rsite):
         """Environments of a dot: [L, R] or, spin-projected, [L, R, L_P, R_P]."""
         f = [self.envs.get(('lop', lsite)), self.envs.get(('rop', rsite))]
@@ -373,8 +425,16 @@ class mpo_dmrg:
             neig = self.qsectors[qkey]
             key = [float(x) for x in eval(qkey)]
             self.setupQtmpCI(ncsite, key)
-            prjmap = self.qtmp.prjmap(self.idlstCI)
-            ndim0 = self.qtmp.size_allowed
+            if self.ifQt:
+                prjmap = self.qtmp.prjmap(self.idlstCI)
+                ndim0 = self.qtmp.size_allowed
+            else:
+                # the reference's dense ("NQt") basis of the sector: every
+                # element of the (ldim, c, rdim) tensor with the target label,
+                # ascending (mpo_dmrg_dotutil.dptSymmetry, 102-145); vectors in
+                # this order, the engine gathers them into its block order
+                prjmap = dense_sector(self.qlst, self.qkey)
+                ndim0 = prjmap.size
             if ndim0 == 0:
                 raise RuntimeError('no basis in symmetry sector %s' % qkey)
             if self.ifprecond:
@@ -559,10 +619,17 @@ class mpo_dmrg:
         self.flmps = {'nsite': self.nsite, 'qnum0': self.qnuml[0]}
         self.frmps = {'nsite': self.nsite, 'qnum%d' % self.nsite: self.qnumr[-1]}
         if fmps is None:
-            fmps = self.product_mps()
-        self.qnuml = [numpy.asarray(fmps['qnum%d' % i]) for i in range(self.nsite + 1)]
-        self.flmps.update(fmps)
-        self.initOps(fmps)
+            # the reference builds the first MPS by a sweep under the first
+            # schedule entry (mpo_dmrg_class.py:359-367)
+            self.status = 'init'
+            self.Dmax = sc.MaxMs[0]
+            self.crit_e = sc.Tols[0]
+            self.noise = sc.Noises[0]
+            self.initMPS()
+        else:
+            self.qnuml = [numpy.asarray(fmps['qnum%d' % i]) for i in range(self.nsite + 1)]
+            self.flmps.update(fmps)
+            self.initOps(fmps)
         self.psi0 = None
         sitelst = list(range(self.nsite))
         eold, deltaE, ifconv, isweep = 1.e3, 1.e3, False, -1
