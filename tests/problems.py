@@ -609,3 +609,51 @@ def run_tasks_on_host(eng, pid, nsteps, bufs, gemm=None, written=None):
                     if modelled and written is not None:
                         written.append((int(g["cbuf"]), idx.ravel(), part.ravel()))
     return bufs
+
+
+def host_sigma_terms(P, terms, x, gemm=None):
+    """The engine's sigma plan over the operator terms ``terms`` of the
+    oracle side of ``P`` (its environments and MPO sites as the operands),
+    built by the engine's planner and executed on the host from the task
+    records (NumPy model of the kernels); returns (sigma, groups per step).
+    Needs no GPU."""
+    from zmpo_dmrg_gb300 import engine as E, mpo as pm
+    m = P.o
+    eng = E.get()
+    fL, fR = m.flst[0]
+
+    def lay(t):
+        return eng.layout(t.qsyms, t.ndims, t.status)
+
+    Lv, Rv, Wv = [], [], []
+    offL, offR, offWi, offWj, wts = [], [], [], [], []
+    classes, op_cls, lL, lWi, lWj, lRf = {}, [], [], [], [], []
+    pos = {"L": 0, "R": 0, "W": 0}
+    for iop in terms:
+        Lt, Rt = fL['opers%d' % iop], fR['opers%d' % iop]
+        if Lt is None or Rt is None:
+            continue
+        Wi = m.fhop['site%d/op%d' % (P.isite, iop)]
+        Wj = m.fhop['site%d/op%d' % (P.isite + 1, iop)]
+        offL.append(pos["L"]); Lv.append(Lt.value); pos["L"] += Lt.value.size
+        offR.append(pos["R"]); Rv.append(Rt.value); pos["R"] += Rt.value.size
+        offWi.append(pos["W"]); Wv.append(Wi.value); pos["W"] += Wi.value.size
+        offWj.append(pos["W"]); Wv.append(Wj.value); pos["W"] += Wj.value.size
+        wts.append(m.hpwts[iop])
+        c0 = pm.op_class(m.opers[iop][0], P.isite, 2)
+        if c0 not in classes:
+            classes[c0] = len(classes)
+            lL.append(lay(Lt)); lWi.append(lay(Wi)); lWj.append(lay(Wj))
+            lRf.append(eng.derive(lay(Rt), [-Rt.qsyms[0], m.qkey - Rt.qsyms[1], m.qkey - Rt.qsyms[2]],
+                                  Rt.status))
+        op_cls.append(classes[c0])
+    if not op_cls:
+        return numpy.zeros(P.ndim0), []
+    pid, ws = eng.sigma_plan(2, op_cls, lL, lWi, lWj, lRf, lay(m.qtmp), offL, offR, offWi, offWj, wts)
+    bufs = [numpy.concatenate(Lv), numpy.concatenate(Rv), numpy.concatenate(Wv), numpy.asarray(x, dtype=float),
+            numpy.zeros(P.ndim0), numpy.zeros(max(ws // 8, 1)), numpy.zeros(1), numpy.zeros(1)]
+    _, _, nl = eng.plan_stats(pid)
+    groups_all = [eng.step_tasks(pid, st)[0] for st in range(nl)]
+    y = run_tasks_on_host(eng, pid, nl, bufs, gemm)[4]
+    eng.destroy_plan(pid)
+    return y, groups_all

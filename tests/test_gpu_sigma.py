@@ -117,6 +117,41 @@ def test_perturbed_rdm(gpu, case, status):
     assert numpy.abs(noise_part).max() > 1e-6   # the noise term is exercised
 
 
+@pytest.mark.parametrize("case", CASES[1:4])
+@pytest.mark.parametrize("status", ["L", "R"])
+def test_perturbed_rdm_one_site(gpu, case, status):
+    """Noise density matrix of a one-site dot (the reference's first sweep
+    from the occupation-number state uses one-site dots with noise):
+    'L' at the dot's first site, 'R' at its second."""
+    from oracle import dmrg as od
+    from zmpo_dmrg_gb300 import prdm
+    from zmpo_dmrg_gb300.mpo_dmrg_class import dense_sector
+    from tests.problems import QPHYS
+    P = prob(case)
+    i = P.isite if status == 'L' else P.isite + 1
+    qlst = [numpy.asarray(P.qnuml[i], dtype=float), QPHYS, numpy.asarray(P.qnumr[i + 1], dtype=float)]
+    dims = [len(q) for q in qlst]
+    civec = numpy.zeros(int(numpy.prod(dims)))
+    sel = dense_sector(qlst, P.key)
+    civec[sel] = numpy.random.default_rng(5).standard_normal(sel.size)
+    civec = civec.reshape(1, *dims)
+    o, m = P.o, P.p
+    o.noise, o.inoise = 1e-4, 0
+    m.noise, m.inoise = 1e-4, 0
+    saved = m.qlst
+    m.qlst, m.qkey = qlst, numpy.array(P.key)
+    b = od.pRDM(civec, [o, i, 1, o.flst, status, True])
+    try:
+        a = prdm.pRDM(civec, [m, i, 1, m.flst, status, True])
+    finally:
+        m.qlst = saved
+    assert a.shape == b.shape
+    assert numpy.abs(a - b).max() <= 1e-12 * max(1.0, numpy.abs(b).max())
+    # the noise term is exercised
+    o.noise = 1.0
+    assert numpy.abs(od.pRDM(civec, [o, i, 1, o.flst, status, True]) - b).max() > 1e-6
+
+
 @pytest.mark.parametrize("precision", ["fp64", "split"])
 def test_sigma_term_batches(gpu, precision):
     """With a workspace budget the terms run in batches (summed on the

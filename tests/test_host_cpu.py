@@ -268,44 +268,10 @@ def test_n_only_relabel_matches_oracle():
 def _host_sigma(P, gemm=None):
     """The engine's sigma plan for the oracle side of ``P`` executed on the
     host from its task records; returns (sigma, oracle sigma, groups)."""
-    from tests.problems import oracle_sigma
-    m = P.o
-    eng = E.get()
-    fL, fR = m.flst[0]
-
-    def lay(t):
-        return eng.layout(t.qsyms, t.ndims, t.status)
-
-    nops = m.nops
-    Lv, Rv, Wv = [], [], []
-    offL, offR, offWi, offWj = [], [], [], []
-    classes, op_cls, lL, lWi, lWj, lRf = {}, [], [], [], [], []
-    pos = {"L": 0, "R": 0, "W": 0}
-    for iop in range(nops):
-        Lt, Rt = fL['opers%d' % iop], fR['opers%d' % iop]
-        Wi = m.fhop['site%d/op%d' % (P.isite, iop)]
-        Wj = m.fhop['site%d/op%d' % (P.isite + 1, iop)]
-        offL.append(pos["L"]); Lv.append(Lt.value); pos["L"] += Lt.value.size
-        offR.append(pos["R"]); Rv.append(Rt.value); pos["R"] += Rt.value.size
-        offWi.append(pos["W"]); Wv.append(Wi.value); pos["W"] += Wi.value.size
-        offWj.append(pos["W"]); Wv.append(Wj.value); pos["W"] += Wj.value.size
-        c0 = pm.op_class(m.opers[iop][0], P.isite, 2)
-        if c0 not in classes:
-            classes[c0] = len(classes)
-            lL.append(lay(Lt)); lWi.append(lay(Wi)); lWj.append(lay(Wj))
-            lRf.append(eng.derive(lay(Rt), [-Rt.qsyms[0], m.qkey - Rt.qsyms[1], m.qkey - Rt.qsyms[2]], Rt.status))
-        op_cls.append(classes[c0])
-    pid, ws = eng.sigma_plan(2, op_cls, lL, lWi, lWj, lRf, lay(m.qtmp), offL, offR, offWi, offWj,
-                             m.hpwts)
+    from tests.problems import oracle_sigma, host_sigma_terms
     x = numpy.random.default_rng(3).standard_normal(P.ndim0)
-    bufs = [numpy.concatenate(Lv), numpy.concatenate(Rv), numpy.concatenate(Wv), x,
-            numpy.zeros(P.ndim0), numpy.zeros(max(ws // 8, 1)), numpy.zeros(1), numpy.zeros(1)]
-    _, _, nl = eng.plan_stats(pid)
-    groups_all = [eng.step_tasks(pid, st)[0] for st in range(nl)]
-    y = _run_tasks_on_host(eng, pid, nl, bufs, gemm)[4]
-    ref = oracle_sigma(P, x)
-    eng.destroy_plan(pid)
-    return y, ref, groups_all
+    y, groups_all = host_sigma_terms(P, range(P.o.nops), x, gemm)
+    return y, oracle_sigma(P, x), groups_all
 
 
 def test_sigma_task_lists_compute_the_oracle_sigma():

@@ -129,3 +129,39 @@ def test_two_rank_oracle_sigma_equals_full_sigma():
         assert p.exitcode == 0
     for r in range(2):
         assert numpy.allclose(out[r], full, rtol=1e-12, atol=1e-12)
+
+
+def _product_plan_worker(rank, size, port, case, x, out):
+    """One CPU rank: the engine's own sigma plan over this rank's operator
+    terms (``partition_ops``, the reference's partitionSites rule), executed
+    on the host by the NumPy model of the kernels, then summed over ranks."""
+    import torch
+    import torch.distributed as dist
+    from zmpo_dmrg_gb300.parallel import DistributedHVec, partition_ops
+    from tests.problems import random_problem, host_sigma_terms
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=size)
+    P = random_problem(device=False, **case)
+    mine = [o[0] for o in partition_ops(P.o.sbas, size, rank)]
+    hv = DistributedHVec(lambda v: torch.as_tensor(host_sigma_terms(P, mine, v.numpy())[0]))
+    out[rank] = hv(torch.as_tensor(x)).numpy().copy()
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_rank_product_plans_sum_to_the_oracle_sigma():
+    """Each rank plans and runs (on the host) the engine's sigma over its
+    range of operator terms; the all-reduced result equals the oracle's
+    sigma over every term of the dot."""
+    import torch.multiprocessing as mp
+    from tests.problems import random_problem, oracle_sigma
+    case = dict(K=6, nelec=6, D=16, isite=2, seed=1)
+    P = random_problem(device=False, **case)
+    x = numpy.random.default_rng(11).standard_normal(P.ndim0)
+    ref = oracle_sigma(P, x)
+    mgr = mp.Manager()
+    out = mgr.dict()
+    mp.spawn(_product_plan_worker, args=(2, _free_port(), case, x, out), nprocs=2, join=True)
+    for r in range(2):
+        assert numpy.linalg.norm(out[r] - ref) <= 1e-12 * numpy.linalg.norm(ref)

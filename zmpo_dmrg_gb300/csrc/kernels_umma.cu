@@ -572,7 +572,7 @@ k_step_umma(const Work *__restrict__ work, int64_t nwork, const Group *__restric
       const int nrt = wk.pad & 0xff;
       for (int r = 0; r < nrt; ++r, ++t) {
         const uint32_t b = t & 1, u = t >> 1;
-        wait_bounded(bar(BAR_E_FULL + b), u & 1, abort_flag, 7);
+        const bool ok_rec = wait_bounded(bar(BAR_E_FULL + b), u & 1, abort_flag, 7);
         const unsigned char *rec = rec0 + b * LY::REC_BYTES;
         const int *info = reinterpret_cast<const int *>(rec + LY::REC_INFO);
         const int m0 = info[0], M = info[1], cbuf = info[2];
@@ -581,7 +581,10 @@ k_step_umma(const Work *__restrict__ work, int64_t nwork, const Group *__restric
         const long long *cb = reinterpret_cast<const long long *>(rec + LY::REC_CB);
         const long long *rs = reinterpret_cast<const long long *>(rec + LY::REC_RS);
         const int row = m0 + e;
-        const bool ok = wait_bounded(bar(BAR_T_FULL + b), u & 1, abort_flag, 8);
+        // stores only when the tile record and the accumulators are both this
+        // tile's (an aborting MMA issuer commits without having multiplied)
+        const bool ok_acc = wait_bounded(bar(BAR_T_FULL + b), u & 1, abort_flag, 8);
+        const bool ok = ok_rec && ok_acc && *abort_flag == 0;
         tc_fence_after();
         double *out = bufs.p[cbuf];
 #pragma unroll 1

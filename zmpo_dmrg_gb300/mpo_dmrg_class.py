@@ -457,7 +457,8 @@ class mpo_dmrg:
             solver.hvec_eps = {"fp64": 0.0, "emu64": 1e-14, "split": 1e-8}[self.precision]
             v0 = None
             if self.psi0 is not None:
-                v0 = self.psi0[ioff:ioff + neig][:, prjmap].copy()
+                idx = torch.as_tensor(numpy.asarray(prjmap, dtype=numpy.int64), device=self.psi0.device)
+                v0 = self.psi0[ioff:ioff + neig].index_select(1, idx)
             eig, vec, nmvp = solver.solve_iter(v0=v0, iop=4)
             if self.precision == "split":
                 # energy error is second order in the vector error: one
@@ -470,13 +471,13 @@ class mpo_dmrg:
                     sv = SVec(v, info, ndim0, prjmap) if self.ifs2proj else v
                     eig[i] = float(torch.dot(v, hv) / torch.dot(v, sv))
                 self.precision = saved
-            civec = numpy.zeros((neig, ndim))
-            civec[:, prjmap] = vec.cpu().numpy()
+            civec = torch.zeros((neig, ndim), dtype=torch.float64, device="cuda")
+            civec[:, torch.as_tensor(numpy.asarray(prjmap, dtype=numpy.int64), device="cuda")] = vec
             civecs.append(civec)
             eigs += list(eig)
             nmvps += nmvp
             ioff += neig
-        civecs = numpy.vstack(civecs)
+        civecs = torch.cat(civecs, dim=0)
         eigs = numpy.array(eigs)
         sigs, dwts, qred, site, srotR = self.decimation(civecs, info)
         if self.ifguess:
@@ -484,6 +485,14 @@ class mpo_dmrg:
         return nmvps, eigs, sigs, dwts, qred, site, srotR
 
     def decimation(self, civecs, info):
+        """Reduced density matrix (with the perturbation noise), its block
+        eigen-decomposition and truncation, the new site and the rotated
+        wavefunction (mpo_dmrg_dotutil.decimation, 259-345).  ``civecs``
+        (neig, ndim) live on the device; the dense products (rho = C C^T and
+        the rotation of C) run there, the block eigen-decomposition of rho on
+        the host (it decides which states are kept, with LAPACK as in the
+        reference)."""
+        torch = _torch()
         dmrg, isite, ncsite, flst, status, ifsym = info
         ldim, cdim, rdim, ndim = self.dims
         neig = civecs.shape[0]
@@ -497,17 +506,22 @@ class mpo_dmrg:
             cdimc = cdim // dim
             lcdim, crdim = ldim * cdimc, dim * rdim
         if self.noise >= 1.e-10 and self.inoise == 1:
-            civecs = civecs + self.rng.uniform(-1, 1, size=civecs.shape) * 10.0 * self.noise
+            nz = self.rng.uniform(-1, 1, size=tuple(civecs.shape)) * 10.0 * self.noise
+            civecs = civecs + torch.as_tensor(nz, device=civecs.device)
         mats = civecs.reshape(neig, lcdim, crdim)
         if status == 'L':
             shaped = civecs.reshape(neig, ldim, dim, crdim)
         else:
             shaped = civecs.reshape(neig, lcdim, dim, rdim)
         rdm1 = prdm.pRDM(shaped, info)
-        tr = numpy.trace(rdm1)
+        tr = float(torch.trace(rdm1))
         if tr < -1e-12:
             raise RuntimeError('RDM should be positive definite')
-        rdm1 = rdm1 + numpy.identity(rdm1.shape[0]) / rdm1.shape[0] if tr < 1e-12 else rdm1 / tr
+        if tr < 1e-12:
+            rdm1 = rdm1 + torch.eye(rdm1.shape[0], dtype=rdm1.dtype, device=rdm1.device) / rdm1.shape[0]
+        else:
+            rdm1 = rdm1 / tr
+        rdm1 = rdm1.cpu().numpy()
         Dcut = self.Dmax
         if ncsite == 1 and ((status == 'L' and isite == self.nsite - 1) or (status == 'R' and isite == 0)):
             Dcut = 1
@@ -518,7 +532,8 @@ class mpo_dmrg:
             dwts, qred, rotL, sigs = rdm_blkdiag(rdm1, classes, self.thresh, Dcut)
             nres = len(qred)
             site = rotL.reshape(ldim, dim, nres).copy()
-            srotR = numpy.matmul(rotL.T, mats).reshape(neig, nres, cdimc, rdim)
+            rot = torch.from_numpy(numpy.ascontiguousarray(rotL)).cuda()
+            srotR = torch.matmul(rot.T, mats).reshape(neig, nres, cdimc, rdim)
         else:
             jsite = isite + ncsite - 1
             if self.Dcut is not None:
@@ -527,24 +542,28 @@ class mpo_dmrg:
             dwts, qred, rotL, sigs = rdm_blkdiag(rdm1, classes, self.thresh, Dcut)
             nres = len(qred)
             site = rotL.reshape(dim, rdim, nres).transpose(2, 0, 1).copy()
-            srotR = numpy.matmul(mats, rotL).reshape(neig, ldim, cdimc, nres)
+            rot = torch.from_numpy(numpy.ascontiguousarray(rotL)).cuda()
+            srotR = torch.matmul(mats, rot).reshape(neig, ldim, cdimc, nres)
         return sigs, dwts, qred, site, srotR
 
     def genGuess(self, isite, ncsite, actlst, civecs, srotR, status):
+        """Guess for the next dot (mpo_dmrg_dotutil.guess, 498-559): the
+        rotated wavefunction times the neighbouring site, on the device."""
+        torch = _torch()
         if isite == actlst[-1]:
-            self.psi0 = civecs.copy()
+            self.psi0 = civecs.clone()
             return 0
         if status == 'R':
             t = self.flmps.get('site%d' % (isite - 1))
             if t is not None:
-                d = t.toDenseTensor(t.idlst)
-                self.psi0 = numpy.array([numpy.tensordot(d, srotR[e], axes=([2], [0])).reshape(-1)
+                d = torch.from_numpy(t.toDenseTensor(t.idlst)).cuda()
+                self.psi0 = torch.stack([torch.tensordot(d, srotR[e], dims=([2], [0])).reshape(-1)
                                          for e in range(self.neig)])
         else:
             t = self.frmps.get('site%d' % (isite + ncsite))
             if t is not None:
-                d = t.toDenseTensor(t.idlst)
-                self.psi0 = numpy.array([numpy.tensordot(srotR[e], d, axes=([2], [0])).reshape(-1)
+                d = torch.from_numpy(t.toDenseTensor(t.idlst)).cuda()
+                self.psi0 = torch.stack([torch.tensordot(srotR[e], d, dims=([2], [0])).reshape(-1)
                                          for e in range(self.neig)])
         return 0
 
@@ -573,7 +592,8 @@ class mpo_dmrg:
         if ncsite != 2:
             return 0
         key = numpy.array([float(x) for x in eval(next(iter(self.qsectors)))])
-        smat = srotR[0] / numpy.linalg.norm(srotR[0])
+        s0 = srotR[0].cpu().numpy() if hasattr(srotR, "cpu") else srotR[0]
+        smat = s0 / numpy.linalg.norm(s0)
         if status == 'L' and sitelst[-1] == self.nsite - 1:
             self.flmps['qnum%d' % self.nsite] = key[None, :]
             self.flmps['site%d' % (self.nsite - 1)] = self.site_qt(

@@ -98,7 +98,8 @@ class eigenSolver:
         if v0 is None:
             vbas = self.genV0(self.neig)
         else:
-            vbas = torch.as_tensor(numpy.asarray(v0), dtype=torch.float64, device=dev).clone()
+            vbas = (v0 if torch.is_tensor(v0) else torch.as_tensor(numpy.asarray(v0))).to(
+                device=dev, dtype=torch.float64).clone()
         if self.noise:
             nz = self.rng.uniform(-1, 1, size=(self.neig, self.ndim))
             vbas = vbas + self.nz * torch.as_tensor(nz, device=dev)

@@ -47,32 +47,38 @@ class _Chain:
 
 
 def pRDM(civecs, info):
-    """civecs: (neig, diml, dimc, dimr) as reshaped by the decimation."""
+    """civecs: (neig, diml, dimc, dimr) as reshaped by the decimation, a NumPy
+    array or a float64 CUDA tensor; the result is of the same kind."""
     dmrg, isite, ncsite, flst, status, ifsym = info
     torch = _torch()
-    neig, diml, dimc, dimr = civecs.shape
-    # sum_e C_e C_e^T as one BLAS product (the states side by side)
+    on_device = torch.is_tensor(civecs)
+    cv = civecs if on_device else torch.from_numpy(numpy.ascontiguousarray(civecs, dtype=numpy.float64)).cuda()
+    neig, diml, dimc, dimr = cv.shape
+    # sum_e C_e C_e^T as one dense product on the device (the states side by side)
     if status == 'L':
-        mats = civecs.reshape(neig, diml * dimc, dimr)
-        cat = mats.transpose(1, 0, 2).reshape(diml * dimc, neig * dimr)
+        cat = cv.reshape(neig, diml * dimc, dimr).permute(1, 0, 2).reshape(diml * dimc, neig * dimr)
         rho = cat @ cat.T
     else:
-        mats = civecs.reshape(neig * diml, dimc * dimr)
+        mats = cv.reshape(neig * diml, dimc * dimr)
         rho = mats.T @ mats
     if not (dmrg.inoise == 0 and dmrg.noise >= 1.e-10):
-        return rho
-    if ncsite != 2:
-        raise NotImplementedError("perturbed RDM is built for the two-site dot")
+        return rho if on_device else rho.cpu().numpy()
     eng = _engine.get()
     qkey = numpy.asarray(dmrg.qkey, dtype=float)
-    ql, qc1, qc2, qr = dmrg.qlst
+    # the dot as three legs [l, n, r] around the site being decimated: a
+    # two-site dot merges the other site into its outer leg, a one-site dot
+    # is already in that form (pRDMNQt, mpo_dmrg_kernel.py:290-340)
+    if ncsite == 2:
+        ql, qc1, qc2, qr = dmrg.qlst
+        ql3, qc3, qr3 = (ql, qc1, _dpt(qc2, qr)) if status == 'L' else (_dpt(ql, qc1), qc2, qr)
+    else:
+        ql3, qc3, qr3 = dmrg.qlst
+    qn = [ql3, qc3, qkey - numpy.asarray(qr3, dtype=float)]
     if status == 'L':
-        qn = [ql, qc1, qkey - _dpt(qc2, qr)]
         qn2 = [qn[0], qn[1], qn[0], qn[1]]
         env = flst[0][0]
         jsite = isite
     else:
-        qn = [_dpt(ql, qc1), qc2, qkey - qr]
         qn2 = [qn[1], qn[2], qn[1], qn[2]]
         env = flst[0][1]
         jsite = isite + ncsite - 1
@@ -87,15 +93,18 @@ def pRDM(civecs, info):
         lay_psi, nmap = psiN.layout, (idx, psiN.size_allowed)
     mpo = dmrg.mpo_store
     from .mpo import op_class
-    # the packed wavefunction of every state, on the device once
+    # the packed wavefunction of every state: a device gather of the dense
+    # vector through the packing's index map
+    dense_idx = torch.as_tensor(numpy.asarray(psi.prjmap(idlst), dtype=numpy.int64), device="cuda")
+    flat = cv.reshape(neig, -1)
     xs = []
     for e in range(neig):
-        psi.fromDense(civecs[e], idlst)
-        xv = psi.value
+        xv = flat[e].index_select(0, dense_idx)
         if nmap is not None:
-            xv = numpy.zeros(nmap[1])
-            xv[nmap[0]] = psi.value
-        xs.append(torch.from_numpy(numpy.ascontiguousarray(xv)).cuda())
+            xN = torch.zeros(nmap[1], dtype=torch.float64, device="cuda")
+            xN[torch.as_tensor(nmap[0], device="cuda")] = xv
+            xv = xN
+        xs.append(xv.contiguous())
     chains = {}
     acc = None
     for iop in range(dmrg.nops):
@@ -134,7 +143,7 @@ def pRDM(civecs, info):
     for ch in chains.values():
         ch.release(eng)
     if acc is None:
-        return rho
+        return rho if on_device else rho.cpu().numpy()
     # block structure of the summed T T^T (legs of the last contraction)
     et = next(env.tensors[i] for i in range(dmrg.nops) if env.present(i))
     qp = mpo.tensors[jsite][0].qsyms[2]
@@ -151,7 +160,10 @@ def pRDM(civecs, info):
     _, _, _, idlst2 = fromQnums(qn2)
     if out.size_allowed != acc.numel():
         raise RuntimeError("perturbed RDM layout mismatch")
-    out.value = acc.cpu().numpy()
-    dense = out.toDenseTensor(idlst2)
-    n = dense.shape[0] * dense.shape[1]
-    return rho + dmrg.noise * dense.reshape(n, n)
+    # scatter the summed blocks into the dense (n, n) matrix on the device
+    n = int(numpy.prod([len(x) for x in qn2[:2]]))
+    didx = torch.as_tensor(numpy.asarray(out.prjmap(idlst2), dtype=numpy.int64), device="cuda")
+    noise_dense = torch.zeros(n * n, dtype=torch.float64, device="cuda")
+    noise_dense[didx] = acc
+    rho = rho + dmrg.noise * noise_dense.reshape(n, n)
+    return rho if on_device else rho.cpu().numpy()
