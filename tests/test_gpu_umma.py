@@ -49,10 +49,13 @@ def test_dense_one_pass_bit_exact(gpu, M, K, N):
         got = out.cpu().numpy().reshape(M, N)
         ref = one_pass_gemm(A, B)
         assert numpy.array_equal(got, ref), (spread, numpy.abs(got - ref).max())
-        # and close to the FP64 product
+        # and close to the FP64 product: per product a.b the digits drop at
+        # most 2^-31 P of each operand (P = 2^(E-1022) <= 2 max|row| or
+        # 2 max|column|) and the levels 4-6 at most 3.05 2^-32 Pa Pb, so
+        # |error| <= 1.76 2^-30 Pa Pb <= 2^-27 K max|A_i.| max|B_.j|
         exact = A @ B
         scale = K * numpy.abs(A).max(axis=1)[:, None] * numpy.abs(B).max(axis=0)[None, :]
-        assert (numpy.abs(got - exact) <= 2.0 ** -29 * scale + 1e-300).all()
+        assert (numpy.abs(got - exact) <= 2.0 ** -27 * scale + 1e-300).all()
         eng.destroy_plan(pid)
     assert eng.device_status() == 0
 
