@@ -1,13 +1,20 @@
-"""CPU checks of the tcgen05 one-pass kernel's shared-memory, descriptor and
-tensor-memory arithmetic (csrc/kernels_umma.cu), mirrored here and asserted
-against the source constants, so that every address the kernel forms is
-checked before it runs on a GPU:
+"""CPU checks of the tcgen05 one-pass path's shared-memory, plane-record,
+descriptor and tensor-memory arithmetic (csrc/kernels_umma.cu, the record
+sizes in csrc/engine.h), mirrored here and asserted against the source
+constants, so that every address the kernels form is checked before it runs
+on a GPU:
 
 * shared-memory regions lie inside the dynamic allocation, do not overlap and
-  are aligned as the 64-byte swizzle (512-byte atoms) and the barriers need;
-* the producers' swizzled 16-byte digit stores land exactly where the
-  tensor core reads element (row, k) of a K-major, 64-byte-swizzled operand
-  through the kernel's descriptors (start address, SBO = 512, k16 offset);
+  are aligned as the 64-byte swizzle (512-byte atoms), the bulk copies
+  (16 bytes) and the barriers need;
+* the prepare kernels' swizzled 16-byte digit stores into a tile record land,
+  once the record is bulk-copied into its shared-memory stage, exactly where
+  the tensor core reads element (row, k) of a K-major, 64-byte-swizzled
+  operand through the kernel's descriptors (start address, SBO = 512, k16
+  offset);
+* the exponent / column-map parts of the records land in the tile record's
+  fields; every bulk copy is 16-byte aligned and sized, and the bytes a
+  barrier phase expects stay within the transaction-count range;
 * every MMA's shared-memory reads stay inside its plane / stage region and
   its TMEM columns inside the allocation; N is a legal kind::f16 width for
   M = 128; the instruction and matrix descriptor fields hold what they encode;
@@ -20,46 +27,56 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = open(os.path.join(ROOT, "zmpo_dmrg_gb300", "csrc", "kernels_umma.cu")).read()
-COMMON = open(os.path.join(ROOT, "zmpo_dmrg_gb300", "csrc", "device_common.cuh")).read()
+ENGINE = open(os.path.join(ROOT, "zmpo_dmrg_gb300", "csrc", "engine.h")).read()
 
-TM, KMAX, KB_SLOTS, ROW_BYTES, NSTAGE, NTHREADS = 128, 256, 32, 64, 2, 416
-EPI_WARPS, PROD_WARP0, PROD_WARPS, MMA_WARP = 4, 4, 8, 12
-SLOT_BYTES = 56
+TM, KMAX, KB_SLOTS, ROW_BYTES, NTHREADS = 128, 256, 32, 64, 192
+EPI_WARPS, PROD_WARP, MMA_WARP = 4, 4, 5
 SMEM_MAX = 232448
+TX_MAX = (1 << 20) - 1
+
+
+def nstage(TN):
+    return 2 if TN == 64 else 4
 
 
 def test_constants_match_source():
-    for name, val in [("TM", TM), ("KMAX", KMAX), ("KB_SLOTS", KB_SLOTS), ("ROW_BYTES", ROW_BYTES),
-                      ("NSTAGE", NSTAGE), ("NTHREADS", NTHREADS)]:
+    assert "constexpr int kUmmaTM = 128, kUmmaMaxK = 256, kUmmaKB = 32;" in ENGINE
+    for name, val in [("ROW_BYTES", ROW_BYTES), ("NTHREADS", NTHREADS)]:
         assert re.search(r"constexpr int %s = %d;" % (name, val), SRC), name
-    assert "EPI_WARPS = 4, PROD_WARP0 = 4, PROD_WARPS = 8, MMA_WARP = 12" in SRC
-    assert (EPI_WARPS + PROD_WARPS + 1) * 32 == NTHREADS
-    # Slot: two pointers, two int64, one double, four ints
-    body = re.search(r"struct Slot \{(.*?)\};", COMMON, re.S).group(1)
-    assert re.findall(r"const double \*(\w+);", body) == ["a", "b"]
-    assert "int64_t sam, sbn;" in body and "double alpha;" in body
-    assert len(re.findall(r"\bint (\w+);", body)) == 4
+    assert "EPI_WARPS = 4, PROD_WARP = 4, MMA_WARP = 5" in SRC
+    assert (EPI_WARPS + 2) * 32 == NTHREADS
+    assert "static constexpr int NSTAGE = TN == 64 ? 2 : 4;" in SRC
+    # record sizes (engine.h) = the layout mirrored below
+    assert "umma_a_tile_bytes(int nkb) { return nkb * kUmmaAKB + kUmmaTM * 4; }" in ENGINE
+    assert "umma_b_kb_bytes(int tn) { return 4 * (int64_t)tn * 64; }" in ENGINE
+    assert "umma_b_tile_bytes(int nkb, int tn) { return nkb * umma_b_kb_bytes(tn) + (int64_t)tn * 20; }" in ENGINE
+
+
+def a_tile_bytes(nkb):
+    return nkb * 4 * TM * ROW_BYTES + TM * 4
+
+
+def b_tile_bytes(nkb, tn):
+    return nkb * 4 * tn * ROW_BYTES + tn * 20
 
 
 def layout(TN):
-    L = {}
+    L = {"NSTAGE": nstage(TN)}
     L["B_KB"] = 4 * TN * ROW_BYTES
     L["OFF_B"] = 0
     L["OFF_A"] = L["OFF_B"] + (KMAX // KB_SLOTS) * L["B_KB"]
     L["A_PLANE"] = TM * ROW_BYTES
     L["A_STAGE"] = 4 * L["A_PLANE"]
-    L["OFF_SLOTS"] = L["OFF_A"] + NSTAGE * L["A_STAGE"]
-    L["OFF_REC"] = L["OFF_SLOTS"] + KMAX * SLOT_BYTES
+    L["OFF_REC"] = L["OFF_A"] + L["NSTAGE"] * L["A_STAGE"]
     L["REC_EA"] = 0
     L["REC_EB"] = TM * 4
     L["REC_CB"] = L["REC_EB"] + TN * 4
     L["REC_RS"] = L["REC_CB"] + TN * 8
     L["REC_INFO"] = L["REC_RS"] + TN * 8
     L["REC_BYTES"] = L["REC_INFO"] + 16
-    L["OFF_ITEM"] = L["OFF_REC"] + 2 * L["REC_BYTES"]
-    L["ITEM_BYTES"] = TN * 4 + TN * 16
-    L["OFF_BAR"] = (L["OFF_ITEM"] + L["ITEM_BYTES"] + 7) // 8 * 8
-    L["OFF_MISC"] = L["OFF_BAR"] + 15 * 8
+    L["OFF_BAR"] = L["OFF_REC"] + 2 * L["REC_BYTES"]
+    L["NBAR"] = 11 + 2 * L["NSTAGE"]
+    L["OFF_MISC"] = L["OFF_BAR"] + L["NBAR"] * 8
     L["BYTES"] = L["OFF_MISC"] + 16
     L["SMEM"] = L["BYTES"] + 1024
     L["TMEM_COLS"] = 8 * TN
@@ -68,12 +85,12 @@ def layout(TN):
 
 def test_layout_formulas_match_source():
     for expr in ["B_KB = 4 * TN * ROW_BYTES", "OFF_A = OFF_B + NKB_MAX * B_KB",
-                 "OFF_SLOTS = OFF_A + NSTAGE * A_STAGE", "OFF_REC = OFF_SLOTS + KMAX * (int)sizeof(Slot)",
+                 "OFF_REC = OFF_A + NSTAGE * A_STAGE",
                  "REC_EB = REC_EA + TM * 4", "REC_CB = REC_EB + TN * 4", "REC_RS = REC_CB + TN * 8",
-                 "REC_INFO = REC_RS + TN * 8", "REC_BYTES = REC_INFO + 16", "OFF_ITEM = OFF_REC + 2 * REC_BYTES",
-                 "ITEM_BYTES = TN * 4 + TN * 16", "OFF_BAR = (OFF_ITEM + ITEM_BYTES + 7) / 8 * 8",
-                 "NBAR = 15", "OFF_MISC = OFF_BAR + NBAR * 8", "BYTES = OFF_MISC + 16", "SMEM = BYTES + 1024",
-                 "TMEM_COLS = 8 * TN", "A_PLANE = TM * ROW_BYTES", "A_STAGE = 4 * A_PLANE"]:
+                 "REC_INFO = REC_RS + TN * 8", "REC_BYTES = REC_INFO + 16", "OFF_BAR = OFF_REC + 2 * REC_BYTES",
+                 "BAR_A_EMPTY = BAR_A_FULL + NSTAGE", "NBAR = BAR_A_FULL + 2 * NSTAGE",
+                 "OFF_MISC = OFF_BAR + NBAR * 8", "BYTES = OFF_MISC + 16", "SMEM = BYTES + 1024",
+                 "TMEM_COLS = 8 * TN", "A_PLANE = TM * ROW_BYTES", "A_STAGE = 4 * A_PLANE", "BAR_A_FULL = 11"]:
         assert expr in SRC, expr
 
 
@@ -81,23 +98,80 @@ def test_layout_formulas_match_source():
 def test_shared_memory_regions(TN):
     L = layout(TN)
     assert L["SMEM"] <= SMEM_MAX
-    regions = [("B", L["OFF_B"], L["OFF_A"]), ("A", L["OFF_A"], L["OFF_SLOTS"]),
-               ("slots", L["OFF_SLOTS"], L["OFF_REC"]), ("rec", L["OFF_REC"], L["OFF_REC"] + 2 * L["REC_BYTES"]),
-               ("item", L["OFF_ITEM"], L["OFF_ITEM"] + L["ITEM_BYTES"]),
-               ("bar", L["OFF_BAR"], L["OFF_BAR"] + 15 * 8), ("misc", L["OFF_MISC"], L["OFF_MISC"] + 16)]
+    regions = [("B", L["OFF_B"], L["OFF_A"]), ("A", L["OFF_A"], L["OFF_REC"]),
+               ("rec", L["OFF_REC"], L["OFF_REC"] + 2 * L["REC_BYTES"]),
+               ("bar", L["OFF_BAR"], L["OFF_BAR"] + L["NBAR"] * 8), ("misc", L["OFF_MISC"], L["OFF_MISC"] + 16)]
     for (_, a0, a1), (_, b0, b1) in zip(regions, regions[1:]):
         assert a0 <= a1 <= b0 <= b1
     assert regions[-1][2] <= L["BYTES"]
     # base aligned to 1024 at run time: 1023 bytes of slack at most
     assert L["BYTES"] + 1023 <= L["SMEM"]
-    assert L["OFF_A"] % 1024 == 0 and L["A_STAGE"] % 1024 == 0 and L["B_KB"] % 512 == 0
+    assert L["OFF_A"] % 1024 == 0 and L["A_STAGE"] % 1024 == 0 and L["B_KB"] % 1024 == 0
     assert L["A_PLANE"] % 512 == 0 and (TN * ROW_BYTES) % 512 == 0
-    assert L["OFF_BAR"] % 8 == 0 and L["OFF_SLOTS"] % 16 == 0 and L["OFF_REC"] % 16 == 0
-    assert (L["OFF_REC"] + L["REC_CB"]) % 8 == 0 and (L["OFF_ITEM"] + TN * 4) % 8 == 0
+    # bulk-copy destinations 16-byte aligned; int64 fields 8-byte aligned
+    for b in range(2):
+        rec = L["OFF_REC"] + b * L["REC_BYTES"]
+        assert (rec + L["REC_EA"]) % 16 == 0 and (rec + L["REC_EB"]) % 16 == 0
+        assert (rec + L["REC_CB"]) % 8 == 0 and (rec + L["REC_RS"]) % 8 == 0
+    assert L["OFF_BAR"] % 8 == 0
     # one CTA per SM: two would need more shared memory than an SM has, or
     # fit in TMEM together (no blocking allocation)
     assert 2 * L["SMEM"] > 228 * 1024 or 2 * L["TMEM_COLS"] <= 512
     assert L["TMEM_COLS"] in (32, 64, 128, 256, 512)
+
+
+@pytest.mark.parametrize("TN", [16, 32, 64])
+@pytest.mark.parametrize("nkb", [1, 2, 7, 8])
+def test_bulk_copies(TN, nkb):
+    """Every copy the producer issues: source offset inside the tile record,
+    size a multiple of 16, destination inside its region; the bytes armed on
+    a barrier phase equal the bytes copied and stay within range."""
+    L = layout(TN)
+    A, B = a_tile_bytes(nkb), b_tile_bytes(nkb, TN)
+    assert A % 16 == 0 and B % 16 == 0
+    # B planes of the item
+    size = nkb * L["B_KB"]
+    assert size % 16 == 0 and size <= L["OFF_A"] - L["OFF_B"] and size <= TX_MAX
+    # per row tile: row exponents (end of the A tile) + column part (end of the B tile)
+    ea_src, eb_src = nkb * L["A_STAGE"], nkb * L["B_KB"]
+    assert ea_src % 16 == 0 and ea_src + TM * 4 == A
+    assert eb_src % 16 == 0 and eb_src + TN * 20 == B
+    assert L["REC_EA"] + TM * 4 == L["REC_EB"] and L["REC_EB"] + TN * 20 == L["REC_INFO"]
+    assert (TM * 4) % 16 == 0 and (TN * 20) % 16 == 0
+    # A k blocks into the stage ring
+    for kb in range(nkb):
+        assert (kb * L["A_STAGE"]) % 16 == 0 and (kb + 1) * L["A_STAGE"] <= nkb * L["A_STAGE"]
+    assert L["A_STAGE"] <= TX_MAX
+    # the column part's fields inside the B record
+    tail = eb_src
+    assert tail + TN * 4 + TN * 8 + TN * 8 == B and (tail + TN * 4) % 8 == 0 and (tail + TN * 12) % 8 == 0
+
+
+def test_planner_plane_offsets_are_aligned():
+    """Tile records are packed A tiles first, then B tiles from a 256-byte
+    aligned offset: every record start is a multiple of 16."""
+    import random
+    rnd = random.Random(3)
+    a = 0
+    starts = []
+    groups = [(rnd.randint(64, 3000), rnd.randint(1, 500), rnd.randint(1, 256)) for _ in range(200)]
+    for M, N, K in groups:
+        nkb, nrt = (K + 31) // 32, (M + 127) // 128
+        for _ in range(nrt):
+            starts.append(a)
+            a += a_tile_bytes(nkb)
+    b0 = (a + 255) // 256 * 256
+    b = 0
+    for M, N, K in groups:
+        nkb = (K + 31) // 32
+        n0 = 0
+        while n0 < N:
+            rem = N - n0
+            tn = 64 if rem >= 64 else (16 if rem <= 16 else (32 if rem <= 32 else 64))
+            starts.append(b0 + b)
+            b += b_tile_bytes(nkb, tn)
+            n0 += tn
+    assert all(s % 16 == 0 for s in starts)
 
 
 def store_offset(row, chunk):
@@ -118,23 +192,28 @@ def tensor_core_read(start, row, k):
 def test_swizzled_stores_match_descriptor_reads(TN):
     L = layout(TN)
     base = 1024 * 7   # any 1024-aligned dynamic-smem base
-    # A: stage s, plane p, row r, slot j
-    for s in range(NSTAGE):
-        for p in range(4):
-            plane = base + L["OFF_A"] + s * L["A_STAGE"] + p * L["A_PLANE"]
-            for r in range(TM):
-                for j in range(KB_SLOTS):
-                    w = plane + store_offset(r, j // 8) + (j % 8) * 2
-                    k16, k = divmod(j, 16)
-                    assert tensor_core_read(plane + k16 * 32, r, k) == w
-                    assert plane <= w < plane + L["A_PLANE"]
-    # B': k block kb, plane p, column c -> operand row p*TN + c
+    # A: record k block kb -> stage s; plane p, row r, slot j
+    for s in range(L["NSTAGE"]):
+        for kb in (0, 3):
+            for p in range(4):
+                for r in range(TM):
+                    for j in range(KB_SLOTS):
+                        rec_off = kb * L["A_STAGE"] + p * L["A_PLANE"] + store_offset(r, j // 8) + (j % 8) * 2
+                        # the bulk copy moves k block kb's bytes unchanged to the stage
+                        w = base + L["OFF_A"] + s * L["A_STAGE"] + (rec_off - kb * L["A_STAGE"])
+                        plane = base + L["OFF_A"] + s * L["A_STAGE"] + p * L["A_PLANE"]
+                        k16, k = divmod(j, 16)
+                        assert tensor_core_read(plane + k16 * 32, r, k) == w
+                        assert plane <= w < plane + L["A_PLANE"]
+    # B': record k block kb, plane p, column c -> operand row p*TN + c; the
+    # whole record's planes are copied to OFF_B
     for kb in range(KMAX // KB_SLOTS):
         blk = base + L["OFF_B"] + kb * L["B_KB"]
         for p in range(4):
             for c in range(TN):
                 for j in range(KB_SLOTS):
-                    w = blk + p * TN * ROW_BYTES + store_offset(c, j // 8) + (j % 8) * 2
+                    rec_off = kb * L["B_KB"] + p * TN * ROW_BYTES + store_offset(c, j // 8) + (j % 8) * 2
+                    w = base + L["OFF_B"] + rec_off
                     k16, k = divmod(j, 16)
                     assert tensor_core_read(blk + k16 * 32, p * TN + c, k) == w
                     assert blk <= w < blk + L["B_KB"]

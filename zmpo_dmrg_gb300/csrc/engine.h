@@ -64,8 +64,43 @@ struct Work {
   int32_t pad;      // B-resident kernel: row tiles of the item (from row mt)
 };
 
+// One-pass tensor-core path (kernels_umma.cu): groups whose whole K fits one
+// exact pass.  Their operand tiles are cut by prepare kernels into the digit
+// planes the tensor cores read (K-major, 64-byte swizzle, the shared-memory
+// image), in a plane buffer:
+//   A tile (group, row tile of 128 rows): nkb k blocks of 32 slots, each four
+//     planes of 128 rows x 64 bytes, then 128 int32 row exponents;
+//   B tile (group, column tile of tn columns): nkb k blocks, each four planes
+//     of tn rows x 64 bytes (plane s holds rows s*tn .. s*tn+tn-1), then tn
+//     int32 column exponents, tn int64 output offsets of (row 0, column c)
+//     (-1: no such column) and tn int64 output row strides.
+// Every record size is a multiple of 16 bytes (bulk-copy granularity).
+constexpr int kUmmaTM = 128, kUmmaMaxK = 256, kUmmaKB = 32;
+constexpr int64_t kUmmaAPlane = 128 * 64;           // one digit plane of a k block
+constexpr int64_t kUmmaAKB = 4 * kUmmaAPlane;       // four planes
+constexpr int64_t umma_a_tile_bytes(int nkb) { return nkb * kUmmaAKB + kUmmaTM * 4; }
+constexpr int64_t umma_b_kb_bytes(int tn) { return 4 * (int64_t)tn * 64; }
+constexpr int64_t umma_b_tile_bytes(int nkb, int tn) { return nkb * umma_b_kb_bytes(tn) + (int64_t)tn * 20; }
+
+struct PrepA {      // cut one A tile: rows m0 .. m0+127 of the group
+  int64_t rec;      // byte offset of the tile record in the plane buffer
+  int32_t group, m0;
+};
+struct PrepB {      // cut one B tile: columns n0 .. n0+tn-1 of the group
+  int64_t rec;
+  int32_t group, n0, tn, pad;
+};
+struct UWork {      // tcgen05 work item: one column tile, a run of row tiles
+  int64_t a_rec;    // record of the run's first A tile (a group's A tiles are consecutive)
+  int64_t b_rec;    // record of the column tile's B tile
+  int32_t group, m0;
+  int32_t nrt_k;    // row tiles of the run | K << 8
+  int32_t pad;
+};
+
 constexpr int kMaxBufs = 8;
 constexpr int kPartialBuf = 6;   // buffer slot of the split-K scratch
+constexpr int kWorkspaceBuf = 5; // buffer slot of a sigma / renorm plan's workspace
 struct Bufs {
   double *p[kMaxBufs];
 };
@@ -89,10 +124,21 @@ struct Step {
   Work *d_work_tcb[2] = {};    // [64 x 64 tiles, 128 x 32 tiles]
   Work *d_work_tc4[3][4] = {};
   // 4 digit slices, groups whose whole K fits one exact pass (1 <= K <= 256,
-  // at least 64 rows): tensor-core (tcgen05) work items, Work::pad = row
-  // tiles | K << 8, by column tile 16 / 32 / 64
-  Work *d_work_um[3] = {};
+  // at least 64 rows): the prepare items (A and B tiles) and the tensor-core
+  // (tcgen05) work items by column tile 16 / 32 / 64
+  PrepA *d_prep_a = nullptr;
+  PrepB *d_prep_b = nullptr;
+  int64_t nprep_a = 0, nprep_b = 0;
+  UWork *d_work_um[3] = {};
   int64_t nwork_um[3] = {};
+  int64_t plane_bytes = 0;          // A tiles, then B tiles (from plane_b0)
+  int64_t plane_b0 = 0;
+  // where the plane buffer lives: a byte offset into the workspace buffer
+  // (sigma and renorm plans; every step of a plan shares one region), or
+  // step-owned memory (plane_ws_off < 0: contraction plans, allocated when
+  // the step's task lists are uploaded)
+  int64_t plane_ws_off = -1;
+  unsigned char *d_planes_own = nullptr;
   int64_t nwork_fp64 = 0;
   int64_t nwork_tc[3][4] = {};
   int64_t nwork_tcb[2] = {};
@@ -117,12 +163,20 @@ struct Step {
   int64_t ncalls = 0;
 };
 
+// the prepared-plane buffer of a step for the buffers of this call
+inline unsigned char *step_planes(const Step &s, const Bufs &b) {
+  return s.plane_ws_off >= 0 ? reinterpret_cast<unsigned char *>(b.p[kWorkspaceBuf]) + s.plane_ws_off
+                             : s.d_planes_own;
+}
+
 // Launchers (kernels.cu)
 int launch_step_fp64(const Step &s, const Bufs &b, void *stream);
 int launch_step_split(const Step &s, const Bufs &b, int nslices, void *stream);
 int launch_reduce(const Step &s, const Bufs &b, void *stream);
-// tcgen05 one-pass kernels (kernels_umma.cu) and their error word
-int launch_step_umma(const Step &s, const Bufs &b, void *stream);
+// tcgen05 one-pass kernels (kernels_umma.cu) and their error word: the
+// prepare kernels cut the step's one-pass operand tiles into `planes`, then
+// the tensor-core kernels multiply them
+int launch_step_umma(const Step &s, const Bufs &b, unsigned char *planes, void *stream);
 int umma_device_status(int *code, int reset);
 
 // Diagonal terms for HDiag: out[l, r] += alpha * sum_{a,b,c} Ld[a,l] Wi[a,b]

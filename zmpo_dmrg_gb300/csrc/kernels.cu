@@ -771,7 +771,7 @@ static int launch_split_all(const Step &s, const Bufs &b, void *stream) {
   Work *const(*wl)[4] = S == 4 ? s.d_work_tc4 : s.d_work_tc;
   const int64_t(*nw)[4] = S == 4 ? s.nwork_tc4 : s.nwork_tc;
   if (S == 4) {
-    if ((rc = launch_step_umma(s, b, stream))) return rc;
+    if ((rc = launch_step_umma(s, b, step_planes(s, b), stream))) return rc;
     if ((rc = launch_tcb_t<64, 64>(s.d_work_tcb[0], s.nwork_tcb[0], s, b, stream))) return rc;
     if ((rc = launch_tcb_t<128, 32>(s.d_work_tcb[1], s.nwork_tcb[1], s, b, stream))) return rc;
   }

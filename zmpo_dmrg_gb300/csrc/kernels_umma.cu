@@ -6,8 +6,8 @@
 // row i of A (column j of B) is cut relative to the row's (column's) largest
 // biased exponent over the group's whole K into four balanced 8-bit digits
 // (X = d0 2^24 + d1 2^16 + d2 2^8 + d3 = floor(|x| / 2^(E-1053)) < 2^31,
-// |digit| <= 128, the element's sign on every digit), held as bf16 planes in
-// shared memory.  The tensor cores form the level sums
+// |digit| <= 128, the element's sign on every digit), held as bf16 planes.
+// The tensor cores form the level sums
 //   L_l = sum_{s+t=l} A_s B_t^T,  l = 0..3  (10 digit products),
 // in FP32 in tensor memory; a digit product is at most 2^14 and a level takes
 // at most four per slot, so for K <= 256 every level is an exact integer
@@ -16,28 +16,35 @@
 // S 2^(Ea_i + Eb_j - 2082) as FP64 with integer operations.  The result is
 // a deterministic function of the inputs, bit-identical to the model.
 //
-// Level products on the tensor cores: the B planes of a column tile of TN
-// columns are stacked along N as B' = [B0 | B1 | B2 | B3] (4 TN rows of a
-// K-major operand), and the four level accumulators of a row tile lie side
-// by side in TMEM ([L0 | L1 | L2 | L3], TN columns each), so per 16-slot k
-// step four MMAs  A_a x B'[0, (4-a) TN)  ->  TMEM columns [a TN, 4 TN)
-// (N = 4TN, 3TN, 2TN, TN) issue all ten products.
-//
-// Work item = one column tile of one group and a run of up to 16 row tiles
-// of 128 rows (the TMEM lanes).  The column tile's B is cut once per item
-// and stays in shared memory (all K); A streams through two stages of 32
-// slots.  Warp roles (416 threads):
-//   warps 0-3   epilogue: warp w reads TMEM lanes 32w..32w+31 (one output
-//               row per thread), folds and stores the tile;
-//   warps 4-11  producers: slot table, B cut, per row tile the A row
-//               exponents and the A cut into swizzled planes;
-//   warp 12     TMEM allocation; lane 0 issues the MMAs and commits.
-// Producer -> MMA -> epilogue hand-offs go through mbarriers; the two TMEM
-// accumulator buffers let the epilogue of one row tile overlap the MMAs of
-// the next.  Every wait is bounded in time (2 s): on expiry the kernel
-// records an error code (zmpo_device_status), every role stops at its next
-// item boundary, the MMA issuer's outstanding work is waited for (bounded)
-// and the tensor memory is released before the kernel returns.
+// Two phases per step.
+//  1. Prepare kernels (k_prep_a, k_prep_b) cut every operand tile once: an A
+//     tile is 128 rows of a group over its whole K, a B tile is a column tile
+//     of 16 / 32 / 64 columns.  Each tile record in the plane buffer is the
+//     exact shared-memory image the tensor cores read (K-major, 64-byte
+//     swizzle, k blocks of 32 slots) followed by the exponents (and, for B,
+//     the output offset and row stride of every column).  These are plain
+//     streaming kernels with many warps per SM, so the gathers of the
+//     block-sparse operands run with enough loads in flight.
+//  2. k_step_umma moves records into shared memory with bulk copies
+//     (cp.async.bulk, completion counted on mbarriers) and multiplies:
+//       warps 0-3  epilogue: warp w reads TMEM lanes 32w..32w+31 (one output
+//                  row per thread), folds the levels and stores the tile;
+//       warp 4     producer: lane 0 issues the bulk copies (B tile of the
+//                  work item, per row tile its exponents and column map, A
+//                  k blocks through a ring of stages);
+//       warp 5     TMEM allocation; lane 0 issues the MMAs and commits.
+//     Level products: the B planes of a column tile of TN columns are stacked
+//     along N as B' = [B0 | B1 | B2 | B3] (4 TN rows of a K-major operand)
+//     and the four level accumulators of a row tile lie side by side in TMEM
+//     ([L0 | L1 | L2 | L3], TN columns each), so per 16-slot k step four MMAs
+//     A_a x B'[0, (4-a) TN) -> TMEM columns [a TN, 4 TN) (N = 4TN, 3TN, 2TN,
+//     TN) issue all ten products.  Two TMEM accumulator buffers let the
+//     epilogue of one row tile overlap the MMAs of the next.
+// Every wait is bounded in time (2 s): on expiry the kernel records an error
+// code (zmpo_device_status), every role stops at its next item boundary,
+// the producer waits (bounded) for the bulk copies it issued, the MMA
+// issuer's outstanding work is waited for (bounded) and the tensor memory is
+// released before the kernel returns.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -53,63 +60,64 @@ __device__ int g_umma_error = 0;
 namespace umma {
 
 // ----------------------------------------------------------- constants
-constexpr int TM = 128;             // rows per tile (TMEM lanes)
-constexpr int KMAX = 256;           // slots of one exact pass
-constexpr int KB_SLOTS = 32;        // slots per k block (one 64-byte swizzle row)
+constexpr int TM = kUmmaTM;                   // rows per tile (TMEM lanes)
+constexpr int KMAX = kUmmaMaxK;               // slots of one exact pass
+constexpr int KB_SLOTS = kUmmaKB;             // slots per k block (one 64-byte swizzle row)
 constexpr int NKB_MAX = KMAX / KB_SLOTS;
-constexpr int ROW_BYTES = 64;       // K-major rows of 32 bf16, 64-byte swizzle
-constexpr int A_PLANE = TM * ROW_BYTES;       // 8 KB: one digit plane of a stage
+constexpr int ROW_BYTES = 64;                 // K-major rows of 32 bf16, 64-byte swizzle
+constexpr int A_PLANE = TM * ROW_BYTES;       // 8 KB: one digit plane of a k block
 constexpr int A_STAGE = 4 * A_PLANE;          // 32 KB: four planes
-constexpr int NSTAGE = 2;
-constexpr int NTHREADS = 416;
-constexpr int EPI_WARPS = 4, PROD_WARP0 = 4, PROD_WARPS = 8, MMA_WARP = 12;
-constexpr int NPROD = PROD_WARPS * 32;        // 256 producer threads
+constexpr int NTHREADS = 192;
+constexpr int EPI_WARPS = 4, PROD_WARP = 4, MMA_WARP = 5;
+constexpr int PREP_THREADS = 256;
 constexpr int BIAS = 2082;
 constexpr uint64_t WAIT_NS = 2000000000ull;   // 2 s bound on every wait
+static_assert(A_PLANE == kUmmaAPlane && A_STAGE == kUmmaAKB, "plane record layout");
 
 // error codes recorded in g_umma_error (first one wins)
 constexpr int ERR_TIMEOUT_BASE = 100;         // + site of the wait
 
-template <int TN>
-struct Layout {
-  static constexpr int B_KB = 4 * TN * ROW_BYTES;     // one k block of the four B planes
-  static constexpr int OFF_B = 0;
-  static constexpr int OFF_A = OFF_B + NKB_MAX * B_KB;
-  static constexpr int OFF_SLOTS = OFF_A + NSTAGE * A_STAGE;
-  static constexpr int OFF_REC = OFF_SLOTS + KMAX * (int)sizeof(Slot);
-  // tile record (one per TMEM buffer): row exponents, column exponents,
-  // output address of (row 0, column c) and the row stride, rows and buffer
-  static constexpr int REC_EA = 0;
-  static constexpr int REC_EB = REC_EA + TM * 4;
-  static constexpr int REC_CB = REC_EB + TN * 4;           // int64 colbase[TN]
-  static constexpr int REC_RS = REC_CB + TN * 8;           // int64 rowstride[TN]
-  static constexpr int REC_INFO = REC_RS + TN * 8;         // int m0, M, cbuf, pad
-  static constexpr int REC_BYTES = REC_INFO + 16;
-  static constexpr int OFF_ITEM = OFF_REC + 2 * REC_BYTES; // item: ebmax[TN], colbase[TN], rowstride[TN]
-  static constexpr int ITEM_BYTES = TN * 4 + TN * 16;
-  static constexpr int OFF_BAR = (OFF_ITEM + ITEM_BYTES + 7) / 8 * 8;
-  static constexpr int NBAR = 15;
-  static constexpr int OFF_MISC = OFF_BAR + NBAR * 8;      // tmem base, abort flag, ktot, scaled
-  static constexpr int BYTES = OFF_MISC + 16;
-  static constexpr int SMEM = BYTES + 1024;                // + alignment of the base to 1024
-  static constexpr int TMEM_COLS = 8 * TN;                 // two buffers of four levels
-  static_assert(TN == 16 || TN == 32 || TN == 64, "column tile");
-  static_assert(OFF_A % 1024 == 0 && A_STAGE % 1024 == 0 && B_KB % 512 == 0, "swizzle atoms");
-  static_assert(OFF_SLOTS % 16 == 0 && OFF_REC % 16 == 0 && REC_BYTES % 16 == 0, "alignment");
-  static_assert(SMEM <= 232448, "shared memory");
+// barrier indices (A ring after the fixed ones)
+enum {
+  BAR_T_FULL = 0,    // [2] MMA commit (tile done) -> epilogue
+  BAR_T_EMPTY = 2,   // [2] epilogue (128) -> MMA
+  BAR_E_FULL = 4,    // [2] tile record copied (+ producer's arrival) -> epilogue
+  BAR_E_EMPTY = 6,   // [2] tile record read, epilogue (128) -> producer
+  BAR_B_FULL = 8,    // B tile of the item copied -> MMA
+  BAR_B_FREE = 9,    // MMA commit after the item -> producer
+  BAR_DONE = 10,     // MMA commit at the end (teardown)
+  BAR_A_FULL = 11    // [NSTAGE] A k block copied -> MMA; then [NSTAGE] A_EMPTY (MMA commit -> producer)
 };
 
-// barrier indices
-enum {
-  BAR_A_FULL = 0,    // [2] producers (256 arrivals) -> MMA
-  BAR_A_EMPTY = 2,   // [2] MMA commit -> producers
-  BAR_T_FULL = 4,    // [2] MMA commit (tile done) -> epilogue
-  BAR_T_EMPTY = 6,   // [2] epilogue (128) -> MMA
-  BAR_E_FULL = 8,    // [2] tile record written, producers (256) -> epilogue
-  BAR_E_EMPTY = 10,  // [2] tile record read, epilogue (128) -> producers
-  BAR_B_FULL = 12,   // B planes of the item cut, producers (256) -> MMA
-  BAR_B_FREE = 13,   // MMA commit after the item -> producers
-  BAR_DONE = 14      // MMA commit at the end (teardown)
+template <int TN>
+struct Layout {
+  static constexpr int NSTAGE = TN == 64 ? 2 : 4;        // A k-block ring
+  static constexpr int B_KB = 4 * TN * ROW_BYTES;         // one k block of the four B planes
+  static constexpr int OFF_B = 0;
+  static constexpr int OFF_A = OFF_B + NKB_MAX * B_KB;
+  static constexpr int OFF_REC = OFF_A + NSTAGE * A_STAGE;
+  // tile record (one per TMEM buffer): row exponents (copied from the A
+  // tile), column exponents, output offsets of (row 0, column c) and row
+  // strides (copied from the B tile, in that order), then m0, M, cbuf
+  static constexpr int REC_EA = 0;
+  static constexpr int REC_EB = REC_EA + TM * 4;
+  static constexpr int REC_CB = REC_EB + TN * 4;          // int64 colbase[TN]
+  static constexpr int REC_RS = REC_CB + TN * 8;          // int64 rowstride[TN]
+  static constexpr int REC_INFO = REC_RS + TN * 8;        // int m0, M, cbuf, pad
+  static constexpr int REC_BYTES = REC_INFO + 16;
+  static constexpr int OFF_BAR = OFF_REC + 2 * REC_BYTES;
+  static constexpr int BAR_A_EMPTY = BAR_A_FULL + NSTAGE;
+  static constexpr int NBAR = BAR_A_FULL + 2 * NSTAGE;
+  static constexpr int OFF_MISC = OFF_BAR + NBAR * 8;     // tmem base, abort flag
+  static constexpr int BYTES = OFF_MISC + 16;
+  static constexpr int SMEM = BYTES + 1024;               // + alignment of the base to 1024
+  static constexpr int TMEM_COLS = 8 * TN;                // two buffers of four levels
+  static_assert(TN == 16 || TN == 32 || TN == 64, "column tile");
+  static_assert(B_KB == umma_b_kb_bytes(TN), "plane record layout");
+  static_assert(OFF_A % 1024 == 0 && A_STAGE % 1024 == 0 && B_KB % 1024 == 0, "swizzle atoms");
+  static_assert(OFF_REC % 16 == 0 && REC_EB % 16 == 0 && REC_BYTES % 16 == 0, "bulk-copy alignment");
+  static_assert(REC_INFO - REC_EB == TN * 20, "column part of a B tile record");
+  static_assert(SMEM <= 232448, "shared memory");
 };
 
 // ------------------------------------------------------------- PTX helpers
@@ -127,6 +135,19 @@ __device__ __forceinline__ void bar_init(uint32_t bar, uint32_t count) {
 
 __device__ __forceinline__ void bar_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// one arrival that also expects `bytes` of bulk-copy completions this phase
+__device__ __forceinline__ void bar_arrive_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// global -> shared bulk copy (16-byte aligned, size a multiple of 16), its
+// bytes counted on `bar`
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
 }
 
 __device__ __forceinline__ bool bar_try_wait(uint32_t bar, uint32_t parity) {
@@ -159,12 +180,11 @@ __device__ __noinline__ bool wait_bounded(uint32_t bar, uint32_t parity, volatil
   }
 }
 
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// barrier of the producer warps (id 1) or epilogue warps (id 2) that also
-// returns the OR of `v` over the participating threads
+// barrier of the epilogue warps (id 2) that also returns the OR of `v` over
+// the participating threads
 __device__ __forceinline__ bool role_sync_or(int id, int nthreads, bool v) {
   uint32_t r;
   asm volatile(
@@ -176,10 +196,6 @@ __device__ __forceinline__ bool role_sync_or(int id, int nthreads, bool v) {
       : "r"((uint32_t)v), "r"(id), "r"(nthreads)
       : "memory");
   return r != 0;
-}
-
-__device__ __forceinline__ void role_sync(int id, int nthreads) {
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
 // Shared-memory matrix descriptor: K-major, 64-byte swizzle (8-row groups of
@@ -251,8 +267,10 @@ __device__ __forceinline__ void cut_pair(double x0, double x1, int E, uint32_t d
 }
 
 // Cut 8 consecutive slots (one 16-byte chunk per plane) of one row of a
-// K-major plane set: rowaddr = byte address of row 0 of plane 0 plus
-// row * 64, plane stride in bytes, chunk = slot / 8 within the k block.
+// K-major plane set: plane0 = row 0 of plane 0 of the k block, planes
+// plane_bytes apart, chunk = slot / 8 within the k block.  The 16-byte chunk
+// index is XORed with bits 1-2 of the row (the 64-byte swizzle of an image
+// whose 8-row groups start at multiples of 512 bytes).
 __device__ __forceinline__ void cut8_store(const double *v, int E, unsigned char *plane0, int plane_bytes, int row,
                                            int chunk) {
   uint32_t d[4][4];
@@ -328,29 +346,182 @@ __device__ int build_slots(const Group &g, const Seg *__restrict__ segs, const B
   return base;
 }
 
+// A(row, slot j), with the slot's weight when the group has weights
+__device__ __forceinline__ double load_a(const Slot &sl, int row, bool scaled) {
+  double x = __ldg(sl.a + (int64_t)row * sl.sam);
+  if (scaled && sl.scaled) x *= sl.alpha;
+  return x;
+}
+
 }  // namespace umma
+
+// ------------------------------------------------------------ prepare kernels
+// One A tile per item: the row exponents of rows m0 .. m0+127 over the
+// group's K (two threads per row, eight loads in flight each), then the four
+// digit planes of every k block (a warp writes 8 rows x 4 chunks = 512
+// contiguous bytes of each plane), then the exponents after the planes.
+__global__ void __launch_bounds__(umma::PREP_THREADS)
+k_prep_a(const PrepA *__restrict__ items, int64_t nitems, const Group *__restrict__ groups,
+         const Seg *__restrict__ segs, Bufs bufs, unsigned char *__restrict__ planes) {
+  using namespace umma;
+  __shared__ Slot slots[KMAX];
+  __shared__ int s_ctl[2];
+  __shared__ int s_ea[TM];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int64_t it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const PrepA p = items[it];
+    const Group g = groups[p.group];
+    if (warp == 0) {
+      int sc;
+      const int K = build_slots(g, segs, bufs, slots, lane, &sc);
+      if (lane == 0) {
+        s_ctl[0] = K;
+        s_ctl[1] = sc;
+      }
+    }
+    __syncthreads();
+    const int K = s_ctl[0];
+    const bool scaled = s_ctl[1] != 0;
+    const int nkb = (K + KB_SLOTS - 1) / KB_SLOTS;
+    {
+      const int row = tid >> 1, half = tid & 1, grow = p.m0 + row;
+      int em = 0;
+      if (grow < g.M) {
+        for (int j0 = half; j0 < K; j0 += 16) {
+          double v[8];
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const int j = j0 + 2 * i;
+            v[i] = j < K ? load_a(slots[j], grow, scaled) : 0.0;
+          }
+#pragma unroll
+          for (int i = 0; i < 8; ++i) em = max(em, dexp(v[i]));
+        }
+      }
+      em = max(em, __shfl_xor_sync(0xffffffffu, em, 1));
+      if (half == 0) s_ea[row] = em;
+    }
+    __syncthreads();
+    unsigned char *rec = planes + p.rec;
+    if (tid < TM) reinterpret_cast<int *>(rec + (int64_t)nkb * A_STAGE)[tid] = s_ea[tid];
+    for (int u = tid; u < nkb * TM * 4; u += PREP_THREADS) {
+      const int kb = u / (TM * 4), row = (u >> 2) & (TM - 1), ch = u & 3;
+      const int grow = p.m0 + row;
+      double v[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int j = kb * KB_SLOTS + ch * 8 + i;
+        v[i] = (grow < g.M && j < K) ? load_a(slots[j], grow, scaled) : 0.0;
+      }
+      cut8_store(v, s_ea[row], rec + (int64_t)kb * A_STAGE, A_PLANE, row, ch);
+    }
+    __syncthreads();  // the slot table and the exponents are rewritten by the next item
+  }
+}
+
+// One B tile per item (columns n0 .. n0+tn-1): the column map (output offset
+// of row 0 and row stride of each column, column-block lookups once per
+// column), the column exponents over the group's K, the four digit planes of
+// every k block (plane s holds rows s*tn + c), then exponents, offsets and
+// strides after the planes.
+__global__ void __launch_bounds__(umma::PREP_THREADS)
+k_prep_b(const PrepB *__restrict__ items, int64_t nitems, const Group *__restrict__ groups,
+         const Seg *__restrict__ segs, const ColBlock *__restrict__ cbl, const SegB *__restrict__ segb, Bufs bufs,
+         unsigned char *__restrict__ planes) {
+  using namespace umma;
+  __shared__ Slot slots[KMAX];
+  __shared__ int s_ctl[2];
+  __shared__ int s_eb[64], s_jb[64], s_rel[64];
+  __shared__ long long s_cb[64], s_rs[64];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int64_t it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const PrepB p = items[it];
+    const Group g = groups[p.group];
+    const int tn = p.tn;
+    if (warp == 0) {
+      int sc;
+      const int K = build_slots(g, segs, bufs, slots, lane, &sc);
+      if (lane == 0) {
+        s_ctl[0] = K;
+        s_ctl[1] = sc;
+      }
+    }
+    for (int c = tid; c < tn; c += PREP_THREADS) {
+      const int col = p.n0 + c;
+      long long cbase = -1, rs = 0;
+      int jb = -1, rel = 0;
+      if (col < g.N) {
+        if (g.ncb == 0) {
+          cbase = g.c_off + (long long)col * g.scn;
+          rs = g.scm;
+        } else {
+          jb = find_cblock(cbl, g, col, rel);
+          if (jb >= 0) {
+            const ColBlock cb = cbl[g.cb0 + jb];
+            cbase = cb.c_off + (long long)rel * cb.scn;
+            rs = cb.scm;
+          }
+        }
+      }
+      s_jb[c] = jb;
+      s_rel[c] = rel;
+      s_cb[c] = cbase;
+      s_rs[c] = rs;
+      s_eb[c] = 0;
+    }
+    __syncthreads();
+    const int K = s_ctl[0];
+    const int nkb = (K + KB_SLOTS - 1) / KB_SLOTS;
+    auto load_b = [&](int j, int c) -> double {
+      const int col = p.n0 + c;
+      if (j >= K || col >= g.N) return 0.0;
+      return g.ncb ? load_b_cb(slots[j], segb, g, s_jb[c], s_rel[c])
+                   : __ldg(slots[j].b + (int64_t)col * slots[j].sbn);
+    };
+    for (int u = tid; u < tn * nkb * 4; u += PREP_THREADS) {
+      const int c = u % tn, g8 = u / tn;
+      double v[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) v[i] = load_b(g8 * 8 + i, c);
+      int em = 0;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) em = max(em, dexp(v[i]));
+      if (em) atomicMax(s_eb + c, em);
+    }
+    __syncthreads();
+    unsigned char *rec = planes + p.rec;
+    unsigned char *tail = rec + (int64_t)nkb * umma_b_kb_bytes(tn);
+    for (int c = tid; c < tn; c += PREP_THREADS) {
+      reinterpret_cast<int *>(tail)[c] = s_eb[c];
+      reinterpret_cast<long long *>(tail + tn * 4)[c] = s_cb[c];
+      reinterpret_cast<long long *>(tail + tn * 12)[c] = s_rs[c];
+    }
+    for (int u = tid; u < nkb * tn * 4; u += PREP_THREADS) {
+      const int kb = u / (tn * 4), c = (u >> 2) % tn, ch = u & 3;
+      double v[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) v[i] = load_b(kb * KB_SLOTS + ch * 8 + i, c);
+      cut8_store(v, s_eb[c], rec + (int64_t)kb * umma_b_kb_bytes(tn), tn * ROW_BYTES, c, ch);
+    }
+    __syncthreads();  // the slot table and the column arrays are rewritten by the next item
+  }
+}
 
 // ------------------------------------------------------------------ kernel
 template <int TN>
 __global__ void __launch_bounds__(umma::NTHREADS, 1)
-k_step_umma(const Work *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
-            const Seg *__restrict__ segs, const ColBlock *__restrict__ cbl, const SegB *__restrict__ segb,
-            Bufs bufs) {
+k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
+            const unsigned char *__restrict__ planes, Bufs bufs) {
   using namespace umma;
   using LY = Layout<TN>;
+  constexpr int NSTAGE = LY::NSTAGE;
   extern __shared__ unsigned char smem_raw[];
   const uint32_t raw_s = smem_u32(smem_raw);
   const uint32_t base_s = (raw_s + 1023u) & ~1023u;
   unsigned char *sm = smem_raw + (base_s - raw_s);
-  unsigned char *Bpl = sm + LY::OFF_B;
-  unsigned char *Ast = sm + LY::OFF_A;
-  Slot *slots = reinterpret_cast<Slot *>(sm + LY::OFF_SLOTS);
   unsigned char *rec0 = sm + LY::OFF_REC;
-  int *it_eb = reinterpret_cast<int *>(sm + LY::OFF_ITEM);
-  long long *it_cb = reinterpret_cast<long long *>(sm + LY::OFF_ITEM + TN * 4);
-  long long *it_rs = it_cb + TN;
   const uint32_t bar0 = base_s + LY::OFF_BAR;
-  uint32_t *misc = reinterpret_cast<uint32_t *>(sm + LY::OFF_MISC);  // [0] tmem, [1] abort, [2] K, [3] scaled
+  uint32_t *misc = reinterpret_cast<uint32_t *>(sm + LY::OFF_MISC);  // [0] tmem, [1] abort
   volatile int *abort_flag = reinterpret_cast<volatile int *>(misc + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -364,16 +535,18 @@ k_step_umma(const Work *__restrict__ work, int64_t nwork, const Group *__restric
   }
   if (tid == 0) {
     for (int s = 0; s < 2; ++s) {
-      bar_init(bar(BAR_A_FULL + s), NPROD);
-      bar_init(bar(BAR_A_EMPTY + s), 1);
       bar_init(bar(BAR_T_FULL + s), 1);
       bar_init(bar(BAR_T_EMPTY + s), EPI_WARPS * 32);
-      bar_init(bar(BAR_E_FULL + s), NPROD);
+      bar_init(bar(BAR_E_FULL + s), 1);
       bar_init(bar(BAR_E_EMPTY + s), EPI_WARPS * 32);
     }
-    bar_init(bar(BAR_B_FULL), NPROD);
+    bar_init(bar(BAR_B_FULL), 1);
     bar_init(bar(BAR_B_FREE), 1);
     bar_init(bar(BAR_DONE), 1);
+    for (int s = 0; s < NSTAGE; ++s) {
+      bar_init(bar(BAR_A_FULL + s), 1);
+      bar_init(bar(LY::BAR_A_EMPTY + s), 1);
+    }
     misc[1] = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -382,163 +555,79 @@ k_step_umma(const Work *__restrict__ work, int64_t nwork, const Group *__restric
   tc_fence_after();
   const uint32_t tmem = misc[0];
 
-  if (warp >= PROD_WARP0 && warp < PROD_WARP0 + PROD_WARPS) {
-    // ================================================================ producers
-    const int pt = tid - PROD_WARP0 * 32;  // 0..255
-    const int arow = pt >> 1, half = pt & 1;
-    uint32_t q = 0, t = 0, item = 0;
-    for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x, ++item) {
-      if (role_sync_or(1, NPROD, *abort_flag != 0)) break;
-      const Work wk = work[w];
-      const Group g = groups[wk.group];
-      const int nrt = wk.pad & 0xff;
-      const int n0 = wk.nt;
-      if (pt < 32) {
-        int sc;
-        const int K = build_slots(g, segs, bufs, slots, lane, &sc);
-        if (lane == 0) {
-          misc[2] = (uint32_t)K;
-          misc[3] = (uint32_t)sc;
-        }
-      }
-      // column map of the tile: output address of (row 0, column c), row stride
-      for (int c = pt; c < TN; c += NPROD) {
-        const int col = n0 + c;
-        long long cbase = -1, rs = 0;
-        if (col < g.N) {
-          if (g.ncb == 0) {
-            cbase = g.c_off + (long long)col * g.scn;
-            rs = g.scm;
-          } else {
-            int rel;
-            const int j = find_cblock(cbl, g, col, rel);
-            if (j >= 0) {
-              const ColBlock cb = cbl[g.cb0 + j];
-              cbase = cb.c_off + (long long)rel * cb.scn;
-              rs = cb.scm;
-            }
-          }
-        }
-        it_cb[c] = cbase;
-        it_rs[c] = rs;
-        it_eb[c] = 0;
-      }
-      role_sync(1, NPROD);
-      const int K = (int)misc[2];
-      const bool scaled = misc[3] != 0;
-      const int nkb = (K + KB_SLOTS - 1) / KB_SLOTS;
-      // ---- B of the column tile: column exponents over all K, then the cut
-      wait_bounded(bar(BAR_B_FREE), (item & 1) ^ 1, abort_flag, 1);
-      const int ngrp = nkb * 4;  // 8-slot groups per column
-      for (int idx = pt; idx < TN * ngrp; idx += NPROD) {
-        const int c = idx % TN, g8 = idx / TN, col = n0 + c;
-        int jb = -1, rel = 0;
-        if (g.ncb && col < g.N) jb = find_cblock(cbl, g, col, rel);
-        int em = 0;
+  if (warp == PROD_WARP) {
+    // ================================================================ producer
+    if (lane == 0) {
+      uint32_t t = 0, q = 0, item = 0;
+      uint32_t nA[NSTAGE], nE[2] = {0u, 0u}, nB = 0;  // phases armed per barrier (for the drain)
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int j = g8 * 8 + i;
-          double x = 0.0;
-          if (j < K && col < g.N)
-            x = g.ncb ? load_b_cb(slots[j], segb, g, jb, rel) : __ldg(slots[j].b + (int64_t)col * slots[j].sbn);
-          em = max(em, dexp(x));
-        }
-        atomicMax(it_eb + c, em);
-      }
-      role_sync(1, NPROD);
-      for (int idx = pt; idx < TN * ngrp; idx += NPROD) {
-        const int c = idx % TN, g8 = idx / TN, col = n0 + c;
-        int jb = -1, rel = 0;
-        if (g.ncb && col < g.N) jb = find_cblock(cbl, g, col, rel);
-        double v[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int j = g8 * 8 + i;
-          double x = 0.0;
-          if (j < K && col < g.N)
-            x = g.ncb ? load_b_cb(slots[j], segb, g, jb, rel) : __ldg(slots[j].b + (int64_t)col * slots[j].sbn);
-          v[i] = x;
-        }
-        // k block g8/4, chunk g8%4; B' row of plane s = s*TN + c
-        cut8_store(v, it_eb[c], Bpl + (g8 >> 2) * LY::B_KB, TN * ROW_BYTES, c, g8 & 3);
-      }
-      fence_proxy_async();
-      bar_arrive(bar(BAR_B_FULL));
-      // ---- row tiles
-      for (int r = 0; r < nrt; ++r, ++t) {
-        const int m0 = wk.mt + r * TM, grow = m0 + arow;
-        const bool rv = grow < g.M;
-        int em = 0;
-        if (rv) {
-          for (int j = half; j < K; j += 2) {
-            double x = __ldg(slots[j].a + (int64_t)grow * slots[j].sam);
-            if (scaled && slots[j].scaled) x *= slots[j].alpha;
-            em = max(em, dexp(x));
-          }
-        }
-        em = max(em, __shfl_xor_sync(0xffffffffu, em, 1));
-        const uint32_t b = t & 1, u = t >> 1;
-        wait_bounded(bar(BAR_E_EMPTY + b), (u & 1) ^ 1, abort_flag, 2);
-        unsigned char *rec = rec0 + b * LY::REC_BYTES;
-        if (half == 0) reinterpret_cast<int *>(rec + LY::REC_EA)[arow] = em;
-        for (int c = pt; c < TN; c += NPROD) {
-          reinterpret_cast<int *>(rec + LY::REC_EB)[c] = it_eb[c];
-          reinterpret_cast<long long *>(rec + LY::REC_CB)[c] = it_cb[c];
-          reinterpret_cast<long long *>(rec + LY::REC_RS)[c] = it_rs[c];
-        }
-        if (pt == 0) {
+      for (int s = 0; s < NSTAGE; ++s) nA[s] = 0;
+      bool ok = true;
+      for (int64_t w = blockIdx.x; ok && w < nwork; w += gridDim.x, ++item) {
+        if (*abort_flag) break;
+        const UWork wk = work[w];
+        const Group g = groups[wk.group];
+        const int nrt = wk.nrt_k & 0xff, K = wk.nrt_k >> 8;
+        const int nkb = (K + KB_SLOTS - 1) / KB_SLOTS;
+        const unsigned char *brec = planes + wk.b_rec;
+        if (!(ok = wait_bounded(bar(BAR_B_FREE), (item & 1) ^ 1, abort_flag, 1))) break;
+        bar_arrive_tx(bar(BAR_B_FULL), (uint32_t)(nkb * LY::B_KB));
+        bulk_g2s(base_s + LY::OFF_B, brec, (uint32_t)(nkb * LY::B_KB), bar(BAR_B_FULL));
+        ++nB;
+        const unsigned char *arec = planes + wk.a_rec;
+        for (int r = 0; r < nrt; ++r, ++t) {
+          const uint32_t b = t & 1, u = t >> 1;
+          if (!(ok = wait_bounded(bar(BAR_E_EMPTY + b), (u & 1) ^ 1, abort_flag, 2))) break;
+          unsigned char *rec = rec0 + b * LY::REC_BYTES;
+          const uint32_t rec_s = base_s + LY::OFF_REC + b * LY::REC_BYTES;
           int *info = reinterpret_cast<int *>(rec + LY::REC_INFO);
-          info[0] = m0;
+          info[0] = wk.m0 + r * TM;
           info[1] = g.M;
           info[2] = g.cbuf;
-        }
-        bar_arrive(bar(BAR_E_FULL + b));
-        for (int kb = 0; kb < nkb; ++kb, ++q) {
-          const uint32_t s = q & 1, us = q >> 1;
-          wait_bounded(bar(BAR_A_EMPTY + s), (us & 1) ^ 1, abort_flag, 3);
-          unsigned char *st = Ast + s * A_STAGE;
-#pragma unroll
-          for (int cc = 0; cc < 2; ++cc) {
-            double v[8];
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-              const int j = kb * KB_SLOTS + half * 16 + cc * 8 + i;
-              double x = 0.0;
-              if (rv && j < K) {
-                x = __ldg(slots[j].a + (int64_t)grow * slots[j].sam);
-                if (scaled && slots[j].scaled) x *= slots[j].alpha;
-              }
-              v[i] = x;
-            }
-            cut8_store(v, em, st, A_PLANE, arow, half * 2 + cc);
+          bar_arrive_tx(bar(BAR_E_FULL + b), (uint32_t)(TM * 4 + TN * 20));
+          bulk_g2s(rec_s + LY::REC_EA, arec + (int64_t)nkb * A_STAGE, TM * 4, bar(BAR_E_FULL + b));
+          bulk_g2s(rec_s + LY::REC_EB, brec + (int64_t)nkb * LY::B_KB, TN * 20, bar(BAR_E_FULL + b));
+          ++nE[b];
+          for (int kb = 0; kb < nkb; ++kb, ++q) {
+            const uint32_t s = q % NSTAGE, use = q / NSTAGE;
+            if (!(ok = wait_bounded(bar(LY::BAR_A_EMPTY + s), (use & 1) ^ 1, abort_flag, 3))) break;
+            bar_arrive_tx(bar(BAR_A_FULL + s), A_STAGE);
+            bulk_g2s(base_s + LY::OFF_A + s * A_STAGE, arec + (int64_t)kb * A_STAGE, A_STAGE, bar(BAR_A_FULL + s));
+            ++nA[s];
           }
-          fence_proxy_async();
-          bar_arrive(bar(BAR_A_FULL + s));
+          if (!ok) break;
+          arec += umma_a_tile_bytes(nkb);
         }
       }
-      // the slot table and the item arrays are rewritten by the next item
-      role_sync(1, NPROD);
+      // drain: every bulk copy issued has landed before the CTA may exit
+#pragma unroll
+      for (int s = 0; s < NSTAGE; ++s)
+        if (nA[s]) wait_bounded(bar(BAR_A_FULL + s), (nA[s] - 1) & 1, abort_flag, 10, false);
+      for (int b = 0; b < 2; ++b)
+        if (nE[b]) wait_bounded(bar(BAR_E_FULL + b), (nE[b] - 1) & 1, abort_flag, 11, false);
+      if (nB) wait_bounded(bar(BAR_B_FULL), (nB - 1) & 1, abort_flag, 12, false);
     }
+    __syncwarp();
   } else if (warp == MMA_WARP) {
     // ====================================================================== MMA
     if (lane == 0) {
       uint32_t q = 0, t = 0, item = 0;
       for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x, ++item) {
         if (*abort_flag) break;
-        const Work wk = work[w];
-        const int nrt = wk.pad & 0xff, K = wk.pad >> 8;
+        const UWork wk = work[w];
+        const int nrt = wk.nrt_k & 0xff, K = wk.nrt_k >> 8;
         const int nkb = (K + KB_SLOTS - 1) / KB_SLOTS;
-        wait_bounded(bar(BAR_B_FULL), item & 1, abort_flag, 4);
+        const bool okb = wait_bounded(bar(BAR_B_FULL), item & 1, abort_flag, 4);
         tc_fence_after();
         for (int r = 0; r < nrt; ++r, ++t) {
           const uint32_t b = t & 1, u = t >> 1;
           wait_bounded(bar(BAR_T_EMPTY + b), (u & 1) ^ 1, abort_flag, 5);
           tc_fence_after();
           for (int kb = 0; kb < nkb; ++kb, ++q) {
-            const uint32_t s = q & 1, us = q >> 1;
-            const bool ok = wait_bounded(bar(BAR_A_FULL + s), us & 1, abort_flag, 6);
+            const uint32_t s = q % NSTAGE, use = q / NSTAGE;
+            const bool ok = wait_bounded(bar(BAR_A_FULL + s), use & 1, abort_flag, 6);
             tc_fence_after();
-            if (ok) {
+            if (ok && okb && !*abort_flag) {
               const uint32_t a_s = base_s + LY::OFF_A + s * A_STAGE;
               const uint32_t b_s = base_s + LY::OFF_B + kb * LY::B_KB;
 #pragma unroll
@@ -552,7 +641,7 @@ k_step_umma(const Work *__restrict__ work, int64_t nwork, const Group *__restric
                 }
               }
             }
-            commit(bar(BAR_A_EMPTY + s));
+            commit(bar(LY::BAR_A_EMPTY + s));
           }
           commit(bar(BAR_T_FULL + b));
         }
@@ -568,8 +657,8 @@ k_step_umma(const Work *__restrict__ work, int64_t nwork, const Group *__restric
     uint32_t t = 0;
     for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
       if (role_sync_or(2, EPI_WARPS * 32, *abort_flag != 0)) break;
-      const Work wk = work[w];
-      const int nrt = wk.pad & 0xff;
+      const UWork wk = work[w];
+      const int nrt = wk.nrt_k & 0xff;
       for (int r = 0; r < nrt; ++r, ++t) {
         const uint32_t b = t & 1, u = t >> 1;
         const bool ok_rec = wait_bounded(bar(BAR_E_FULL + b), u & 1, abort_flag, 7);
@@ -586,7 +675,7 @@ k_step_umma(const Work *__restrict__ work, int64_t nwork, const Group *__restric
         const bool ok_acc = wait_bounded(bar(BAR_T_FULL + b), u & 1, abort_flag, 8);
         const bool ok = ok_rec && ok_acc && *abort_flag == 0;
         tc_fence_after();
-        double *out = bufs.p[cbuf];
+        double *out = bufs.p[ok ? cbuf : 0];
 #pragma unroll 1
         for (int c0 = 0; c0 < TN; c0 += 16) {
           uint32_t v[4][16];
@@ -626,7 +715,8 @@ k_step_umma(const Work *__restrict__ work, int64_t nwork, const Group *__restric
 }
 
 template <int TN>
-static int launch_umma_t(const Work *work, int64_t nwork, const Step &s, const Bufs &b, void *stream) {
+static int launch_umma_t(const UWork *work, int64_t nwork, const Step &s, const Bufs &b,
+                         const unsigned char *planes, int nsm, void *stream) {
   if (nwork == 0) return ZMPO_OK;
   constexpr int smem = umma::Layout<TN>::SMEM;
   static bool attr = false;
@@ -635,21 +725,35 @@ static int launch_umma_t(const Work *work, int64_t nwork, const Step &s, const B
     if (e != cudaSuccess) return record_cuda_error("k_step_umma: shared memory attribute", (int)e);
     attr = true;
   }
-  int dev = 0, nsm = 152;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const int grid = (int)(nwork < nsm ? nwork : nsm);
-  k_step_umma<TN><<<grid, umma::NTHREADS, smem, (cudaStream_t)stream>>>(work, nwork, s.d_groups, s.d_segs,
-                                                                        s.d_cblocks, s.d_segb, b);
+  k_step_umma<TN><<<grid, umma::NTHREADS, smem, (cudaStream_t)stream>>>(work, nwork, s.d_groups, planes, b);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? ZMPO_OK : record_cuda_error("k_step_umma", (int)e);
 }
 
-int launch_step_umma(const Step &s, const Bufs &b, void *stream) {
+int launch_step_umma(const Step &s, const Bufs &b, unsigned char *planes, void *stream) {
+  if (s.nprep_a == 0 && s.nprep_b == 0) return ZMPO_OK;
+  if (!planes) return record_arg_error("one-pass tensor-core groups without a plane buffer");
+  int dev = 0, nsm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t cap = (int64_t)nsm * 8;
+  if (s.nprep_a) {
+    k_prep_a<<<(int)(s.nprep_a < cap ? s.nprep_a : cap), umma::PREP_THREADS, 0, (cudaStream_t)stream>>>(
+        s.d_prep_a, s.nprep_a, s.d_groups, s.d_segs, b, planes);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return record_cuda_error("k_prep_a", (int)e);
+  }
+  if (s.nprep_b) {
+    k_prep_b<<<(int)(s.nprep_b < cap ? s.nprep_b : cap), umma::PREP_THREADS, 0, (cudaStream_t)stream>>>(
+        s.d_prep_b, s.nprep_b, s.d_groups, s.d_segs, s.d_cblocks, s.d_segb, b, planes);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return record_cuda_error("k_prep_b", (int)e);
+  }
   int rc;
-  if ((rc = launch_umma_t<64>(s.d_work_um[2], s.nwork_um[2], s, b, stream))) return rc;
-  if ((rc = launch_umma_t<32>(s.d_work_um[1], s.nwork_um[1], s, b, stream))) return rc;
-  return launch_umma_t<16>(s.d_work_um[0], s.nwork_um[0], s, b, stream);
+  if ((rc = launch_umma_t<64>(s.d_work_um[2], s.nwork_um[2], s, b, planes, nsm, stream))) return rc;
+  if ((rc = launch_umma_t<32>(s.d_work_um[1], s.nwork_um[1], s, b, planes, nsm, stream))) return rc;
+  return launch_umma_t<16>(s.d_work_um[0], s.nwork_um[0], s, b, planes, nsm, stream);
 }
 
 int umma_device_status(int *code, int reset) {

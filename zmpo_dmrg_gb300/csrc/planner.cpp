@@ -878,7 +878,7 @@ static void split_long_groups(Step &st) {
 // 4-slice path: the whole K in one exact pass, at least half a row tile.
 // ZMPO_SPLIT_LEGACY=1 in the environment keeps every group on the mma.sync
 // kernels (for comparisons).
-constexpr int kUmmaMaxK = 256, kUmmaMinM = 64, kUmmaTM = 128, kUmmaRun = 16;
+constexpr int kUmmaMinM = 64, kUmmaRun = 16;
 static bool umma_enabled() {
   static const bool on = [] {
     const char *v = std::getenv("ZMPO_SPLIT_LEGACY");
@@ -887,10 +887,66 @@ static bool umma_enabled() {
   return on;
 }
 
+// Split-K parts (written to the partial-sum scratch) stay on the chunked
+// kernels, so the one-pass set is the same before and after the split.
+static bool umma_one_pass(const Group &G, int64_t ktot) {
+  return umma_enabled() && ktot >= 1 && ktot <= kUmmaMaxK && G.M >= kUmmaMinM && G.N >= 1 &&
+         G.cbuf != kPartialBuf;
+}
+
+// column tiles of a one-pass group: full 64-column tiles, then the smallest
+// of 16 / 32 / 64 that holds the rest
+static int umma_tn(int rem) { return rem >= 64 ? 64 : (rem <= 16 ? 16 : (rem <= 32 ? 32 : 64)); }
+
+static int64_t group_k(const Step &st, const Group &G) {
+  int64_t k = 0;
+  for (int i = 0; i < G.nseg; ++i) k += st.segs[G.seg0 + i].K;
+  return k;
+}
+
+// Bytes of the prepared digit planes of a step's one-pass groups: every A
+// tile, then (from *b0, 256-byte aligned) every B tile.
+static int64_t umma_plane_bytes(const Step &st, int64_t *b0) {
+  int64_t a = 0, b = 0;
+  for (const Group &G : st.groups) {
+    const int64_t k = group_k(st, G);
+    if (!umma_one_pass(G, k)) continue;
+    const int nkb = (int)((k + kUmmaKB - 1) / kUmmaKB);
+    const int nrt = (G.M + kUmmaTM - 1) / kUmmaTM;
+    a += nrt * umma_a_tile_bytes(nkb);
+    for (int n0 = 0; n0 < G.N;) {
+      const int tn = umma_tn(G.N - n0);
+      b += umma_b_tile_bytes(nkb, tn);
+      n0 += tn;
+    }
+  }
+  a = (a + 255) & ~int64_t(255);
+  if (b0) *b0 = a;
+  return a + b;
+}
+
+// Sigma and renorm plans: one plane region at the end of the workspace,
+// shared by the plan's steps (they run one after another).
+static void reserve_plane_region(Plan *P) {
+  int64_t need = 0;
+  for (auto &st : P->steps) {
+    st.plane_bytes = umma_plane_bytes(st, &st.plane_b0);
+    need = std::max(need, st.plane_bytes);
+  }
+  if (need == 0) return;
+  const int64_t off = ((P->ws_elems * (int64_t)sizeof(double)) + 255) & ~int64_t(255);
+  for (auto &st : P->steps) st.plane_ws_off = off;
+  P->ws_elems = ((off + need + 255) & ~int64_t(255)) / (int64_t)sizeof(double);
+}
+
 static int upload_step(Step &st) {
   if (st.uploaded) return ZMPO_OK;
   split_long_groups(st);
-  std::vector<Work> w64, wtc[3][4], wtc4[3][4], wtcb[2], wum[3];
+  std::vector<Work> w64, wtc[3][4], wtc4[3][4], wtcb[2];
+  std::vector<UWork> wum[3];
+  std::vector<PrepA> prep_a;
+  std::vector<PrepB> prep_b;
+  int64_t abytes = 0, bbytes = 0;
   // order groups by cost (longest first) for load balance
   std::vector<int> order(st.groups.size());
   std::iota(order.begin(), order.end(), 0);
@@ -915,21 +971,31 @@ static int upload_step(Step &st) {
         w64.push_back({g, m0, n0, 0});
         st.mma_macs[0] += (double)kTileFP64M * kTileFP64N * k16;
       }
-    // one-pass tensor-core items: full 64-column tiles, then a 16/32/64 tile
-    // for the rest; runs of at most kUmmaRun row tiles of 128, balanced
-    const bool one_pass = um && ktot[g] >= 1 && ktot[g] <= kUmmaMaxK && G.M >= kUmmaMinM && G.N >= 1;
+    // one-pass tensor-core items: every row tile of 128 and every column
+    // tile (umma_tn) is cut once into the plane buffer by a prepare item;
+    // work items = one column tile and a run of at most kUmmaRun row tiles
+    // (runs balanced)
+    const bool one_pass = um && umma_one_pass(G, ktot[g]);
     if (one_pass) {
+      const int K = (int)ktot[g];
+      const int nkb = (K + kUmmaKB - 1) / kUmmaKB;
       const int nrt = (G.M + kUmmaTM - 1) / kUmmaTM;
       const int nruns = (nrt + kUmmaRun - 1) / kUmmaRun;
       const int len = (nrt + nruns - 1) / nruns;
+      const int64_t a0 = abytes;
+      for (int r = 0; r < nrt; ++r) {
+        prep_a.push_back({abytes, g, r * kUmmaTM});
+        abytes += umma_a_tile_bytes(nkb);
+      }
       for (int n0 = 0; n0 < G.N;) {
-        const int rem = G.N - n0;
-        const int tn = rem >= 64 ? 64 : (rem <= 16 ? 16 : (rem <= 32 ? 32 : 64));
+        const int tn = umma_tn(G.N - n0);
         const int ti = tn == 16 ? 0 : (tn == 32 ? 1 : 2);
+        prep_b.push_back({bbytes, g, n0, tn, 0});  // B offsets are relative until the A total is known
         for (int r = 0; r < nrt; r += len) {
           const int n = std::min(len, nrt - r);
-          wum[ti].push_back({g, r * kUmmaTM, n0, n | ((int32_t)ktot[g] << 8)});
+          wum[ti].push_back({a0 + r * umma_a_tile_bytes(nkb), bbytes, g, r * kUmmaTM, n | (K << 8), 0});
         }
+        bbytes += umma_b_tile_bytes(nkb, tn);
         st.mma_macs[1] += (double)nrt * kUmmaTM * tn * k16;
         n0 += tn;
       }
@@ -986,6 +1052,21 @@ static int upload_step(Step &st) {
       st.nwork_tc4[i][j] = (int64_t)wtc4[i][j].size();
     }
   for (int i = 0; i < 2; ++i) st.nwork_tcb[i] = (int64_t)wtcb[i].size();
+  // plane buffer: A tiles, then B tiles from the 256-aligned A total (the
+  // layout umma_plane_bytes sizes)
+  {
+    const int64_t b0 = (abytes + 255) & ~int64_t(255);
+    for (auto &p : prep_b) p.rec += b0;
+    for (int i = 0; i < 3; ++i)
+      for (auto &w : wum[i]) w.b_rec += b0;
+    const int64_t total = (abytes + bbytes) > 0 ? b0 + bbytes : 0;
+    if (st.plane_ws_off >= 0 && (total != st.plane_bytes || b0 != st.plane_b0))
+      return fail(ZMPO_E_ARG, "upload: prepared-plane size differs from the plan's reservation");
+    st.plane_bytes = total;
+    st.plane_b0 = b0;
+  }
+  st.nprep_a = (int64_t)prep_a.size();
+  st.nprep_b = (int64_t)prep_b.size();
   for (int i = 0; i < 3; ++i) st.nwork_um[i] = (int64_t)wum[i].size();
   auto up = [](auto **dptr, const auto &v) -> cudaError_t {
     using T = typename std::remove_reference<decltype(v)>::type::value_type;
@@ -1009,6 +1090,10 @@ static int upload_step(Step &st) {
     }
   for (int i = 0; i < 2; ++i) CUDA_TRY(up(&st.d_work_tcb[i], wtcb[i]));
   for (int i = 0; i < 3; ++i) CUDA_TRY(up(&st.d_work_um[i], wum[i]));
+  CUDA_TRY(up(&st.d_prep_a, prep_a));
+  CUDA_TRY(up(&st.d_prep_b, prep_b));
+  if (st.plane_ws_off < 0 && st.plane_bytes > 0)
+    CUDA_TRY(cudaMalloc((void **)&st.d_planes_own, st.plane_bytes));
   CUDA_TRY(up(&st.d_reds, st.reds));
   if (st.part_elems > 0) CUDA_TRY(cudaMalloc((void **)&st.d_part, st.part_elems * sizeof(double)));
   // keep the host mirror of groups (sizes) but free the bulky segment copy
@@ -1043,6 +1128,12 @@ static void free_step(Step &st) {
     cudaFree(st.d_work_um[i]);
     st.d_work_um[i] = nullptr;
   }
+  cudaFree(st.d_prep_a);
+  cudaFree(st.d_prep_b);
+  cudaFree(st.d_planes_own);
+  st.d_prep_a = nullptr;
+  st.d_prep_b = nullptr;
+  st.d_planes_own = nullptr;
   cudaFree(st.d_reds);
   cudaFree(st.d_part);
   st.d_reds = nullptr;
@@ -1520,6 +1611,7 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
       P->exec_flops += st.flops;
       P->ntasks += st.ntasks;
     }
+    reserve_plane_region(P.get());
   }
   // ---- HDiag terms: out[l,r] += w * sum Ld[a,l] Wi[a,b] (Wj[b,c]) Rd[c,r]
   {
@@ -1831,6 +1923,7 @@ int zmpo_renorm_plan(zmpo_engine *e, const zmpo_renorm_desc *d, int *plan_id) {
       P->exec_flops += st.flops;
       P->ntasks += st.ntasks;
     }
+    reserve_plane_region(P.get());
   }
   e->plans.push_back(std::move(P));
   {
