@@ -387,6 +387,96 @@ def sweep_large(K=24, nelec=24, D=512, seed=2024):
     return out
 
 
+def sweep_converged(K=24, nelec=24, D=512, seed=2024, max_pairs=6, tol=1e-8):
+    """Sweep seconds at K=24, 24 electrons, Sz=0, D=512 (the split-vs-FP64
+    configuration).  Phase 1: split-precision two-site sweep pairs (right,
+    then left; D=512, Davidson crit_e 1e-9, no noise) from a seeded random
+    left-canonical MPS until the energy changes by less than ``tol`` between
+    pairs.  Phase 2: from that converged MPS (environments rebuilt from it for
+    each arm, so both arms start from identical states), one FP64 sweep pair
+    and one split sweep pair, timed alone; reported: seconds per sweep pair
+    and per half sweep, matvecs, energies, their difference, and whether each
+    arm stayed within ``tol`` of the converged energy."""
+    import torch
+    from tests.problems import bond_structure, random_left_site, QPHYS
+    from zmpo_dmrg_gb300 import integrals as I
+    from zmpo_dmrg_gb300.mpo_dmrg_class import mpo_dmrg
+    from zmpo_dmrg_gb300.mpo_dmrg_schedule import schedule
+    from zmpo_dmrg_gb300.qtensor import qtensor
+    h, eri, _ = I.synthetic(K, seed)
+    rng = numpy.random.default_rng(seed)
+    qnuml, _ = bond_structure(K, nelec, 0.0, D, rng)
+    qnuml[K] = numpy.array([[float(nelec), 0.0]])
+    fmps = {'nsite': K}
+    for i in range(K):
+        t = qtensor([False, False, True])
+        t.fromDenseTensor(random_left_site(qnuml[i], qnuml[i + 1], rng), [qnuml[i], QPHYS, qnuml[i + 1]])
+        fmps['site%d' % i] = t
+    for i in range(K + 1):
+        fmps['qnum%d' % i] = qnuml[i]
+    m = mpo_dmrg(seed=1)
+    m.nsite, m.sbas, m.isym = K, 2 * K, 2
+    m.build()
+    m.qsectors = {str([float(nelec), 0.0]): 1}
+    m.initStates()
+    m.partition()
+    m.loadInts(I.spin_orbital(h, eri))
+    m.dumpMPO()
+    sc = schedule(maxM=D, tol=1e-9, maxiter=1)
+    sc.fixed(ncsite=2, maxM=D, tol=1e-9, maxiter=1, noise=0.0)
+
+    def start(mps, prec):
+        m.precision = prec
+        m.precision_renorm = "emu64" if prec == "split" else "fp64"
+        m.flmps = {'nsite': K, 'qnum0': m.qnuml[0]}
+        m.frmps = {'nsite': K, 'qnum%d' % K: m.qnumr[-1]}
+        m.qnuml = [numpy.asarray(mps['qnum%d' % i]) for i in range(K + 1)]
+        m.flmps.update(mps)
+        m.initOps(mps)
+        m.psi0 = None
+        sc.getParameters(m, 0)
+        m.crit_e = 1e-9
+
+    def pair():
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r1 = m.sweep(list(range(K)), 2, 'R')
+        r2 = m.sweep(list(range(K)), 2, 'L')
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, min(float(r1[2]), float(r2[2])), int(r1[0] + r2[0])
+
+    def snapshot():
+        mps = {k: v for k, v in m.flmps.items() if k.startswith('site') or k.startswith('qnum')}
+        mps['nsite'] = K
+        return mps
+
+    out = {"workload": "K=%d N=%d Sz=0 D=%d, two-site sweep pairs (right + left, %d dots each), Davidson crit_e "
+                       "1e-9, no noise; converged by split sweeps from a seeded random left-canonical MPS, then one "
+                       "sweep pair per arm from the same converged MPS" % (K, nelec, D, K - 1)}
+    start(fmps, "split")
+    hist, eold, conv = [], None, False
+    for _ in range(max_pairs):
+        dt, e, nmv = pair()
+        hist.append({"s": dt, "energy": e, "matvecs": nmv})
+        if eold is not None and abs(e - eold) < tol:
+            conv = True
+            break
+        eold = e
+    out["converge"] = {"pairs": hist, "converged": conv, "energy": hist[-1]["energy"]}
+    e_conv = hist[-1]["energy"]
+    mps = snapshot()
+    for prec in ("fp64", "split"):
+        start(mps, prec)
+        dt, e, nmv = pair()
+        out[prec] = {"s_per_sweep": dt, "s_per_half_sweep": dt / 2, "energy": e, "matvecs": nmv,
+                     "converged": abs(e - e_conv) < tol}
+    out["dE_split_fp64"] = abs(out["split"]["energy"] - out["fp64"]["energy"])
+    out["sweep_speedup_split_vs_fp64"] = out["fp64"]["s_per_sweep"] / out["split"]["s_per_sweep"]
+    del m
+    torch.cuda.empty_cache()
+    return out
+
+
 def cpu_threads():
     return os.cpu_count() or 1
 
@@ -599,7 +689,8 @@ def main():
                             "peak_source": peak_kind} if args.precision != "fp64" else None,
     }
     if rank == 0 and not args.no_sweep:
-        result["sweep"] = sweep_metrics()
+        result["sweep"] = sweep_converged()
+        result["sweep_k10"] = sweep_metrics()
     if rank == 0 and args.gradient:
         result["gradient"] = gradient_metrics()
     if rank == 0 and args.sweep_large:

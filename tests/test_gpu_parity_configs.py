@@ -9,14 +9,18 @@
 * K=20, 20 electrons, D=512, singlet projection with 8 quadrature points:
   the same check on the spin-projected H.psi (N-only relabelled terms).
 * K=10, 10 electrons, D=64, the reference's default two-site schedule from
-  the occupation-number state (its initial one-site sweep included), 4
-  sweeps: the energy of every dot and the final energy of the GPU driver
-  against the oracle driver's (frozen in ``tests/golden/sweep_k10_d64.npz``
-  by ``tests/golden/make_oracle_fixtures.py``), within 1e-8 Eh.  The
-  reference builds a first MPS only in its dense-vector mode, so the driver
-  runs with ``ifQt = False``: Davidson vectors (and their random start
-  noise) in the reference's dense order, the engine's block-sparse products
-  underneath.
+  the occupation-number state (its initial one-site sweep included), 12
+  sweeps: the energy of every noise-free sweep (the sixth on) and the final
+  energy of the GPU driver against the oracle driver's (frozen in
+  ``tests/golden/sweep_k10_d64.npz`` by
+  ``tests/golden/make_oracle_fixtures.py``), within 1e-8 Eh.  The first
+  sweeps add random noise to the density matrix and stop Davidson at 1e-4,
+  so their energies depend on the noise draws (oracle runs with two noise
+  seeds differ there by up to 2e-6 and agree to 1e-10 from the sixth sweep
+  on); they are not compared.  The reference builds a first MPS only in its
+  dense-vector mode, so the driver runs with ``ifQt = False``: Davidson
+  vectors (and their random start noise) in the reference's dense order, the
+  engine's block-sparse products underneath.
 """
 import os
 
@@ -86,8 +90,8 @@ def test_sweep_k10_d64_matches_oracle_driver(gpu, precision):
     sc.normal(2)
     m.default(sc)
     assert m.nsweep == int(z["nsweep"])
-    dots = numpy.array([float(numpy.asarray(e).ravel()[0]) for e in m.esweeps])
-    ref = z["dot_energies"]
-    assert dots.shape == ref.shape
-    assert numpy.abs(dots - ref).max() < 1e-8
+    got = numpy.array([float(e) for e in m.eav])
+    ref = z["sweep_energies"]
+    assert got.shape == ref.shape
+    assert numpy.abs(got[5:] - ref[5:]).max() < 1e-8, (got - ref)
     assert abs(float(m.Energy) - float(z["energy"])) < 1e-8
