@@ -100,9 +100,10 @@ int zmpo_contract_exec(zmpo_engine *e, int plan_id, const double *d_a,
  * (1048576 float64) compiled into this library instead of memory the plan
  * allocates.  Every GPU that loads the library holds that array until the
  * process exits.  The call allocates nothing: the plan must have run once
- * through zmpo_contract_exec during set-up (that call builds the plan's device
- * task lists), and a plan that needs more scratch than the array holds is
- * rejected with ZMPO_E_SIZE.  The first call on a device looks up the array's
+ * through zmpo_contract_exec during set-up, with the precision of the later
+ * calls (that call builds the plan's device task lists and, for the split
+ * precision, the plan's own buffer of prepared digit planes), and a plan that
+ * needs more scratch than the array holds is rejected with ZMPO_E_SIZE.  The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress, with that device current); make that
  * first call before any stream capture.  All calls share the one array and it
  * keeps the last call's contents (every partial is overwritten before it is

@@ -17,6 +17,12 @@ digit products:
 ``one_pass_gemm`` computes that result exactly (int64 products); the
 tensor-core kernel that runs a group in one pass must reproduce it bit for
 bit.  Results below the normal FP64 range are flushed to zero in both.
+
+``long_gemm``: a group with a longer K runs in passes of 256 slots (each
+exact as above, with its own exponents) whose results are added in FP64 in
+pass order, starting from zero; a group longer than 2048 slots is first cut
+into parts of 2048 (the last one shorter) whose results are added in FP64 in
+part order, starting from zero (the split-K sum).
 """
 import numpy
 
@@ -77,3 +83,31 @@ def one_pass_gemm(A, B):
     out[tiny] = 0.0
     out[(Ea[:, None] == 0) | (Eb[None, :] == 0)] = 0.0
     return out
+
+
+PASS, PART = 256, 2048
+
+
+def passes_gemm(A, B):
+    """FP64 sum, in pass order from zero, of the one-pass products of the
+    256-slot passes of A (M x K) and B (K x N)."""
+    A = numpy.asarray(A, dtype=numpy.float64)
+    B = numpy.asarray(B, dtype=numpy.float64)
+    acc = numpy.zeros((A.shape[0], B.shape[1]))
+    for k0 in range(0, A.shape[1], PASS):
+        acc = acc + one_pass_gemm(A[:, k0:k0 + PASS], B[k0:k0 + PASS])
+    return acc
+
+
+def long_gemm(A, B):
+    """The long tcgen05 route: parts of 2048 slots, each a pass sum; the parts
+    added in order from zero when there is more than one."""
+    A = numpy.asarray(A, dtype=numpy.float64)
+    B = numpy.asarray(B, dtype=numpy.float64)
+    K = A.shape[1]
+    if K <= PART:
+        return passes_gemm(A, B)
+    acc = numpy.zeros((A.shape[0], B.shape[1]))
+    for k0 in range(0, K, PART):
+        acc = acc + passes_gemm(A[:, k0:k0 + PART], B[k0:k0 + PART])
+    return acc

@@ -1,7 +1,9 @@
-"""The one-pass tcgen05 kernel (csrc/kernels_umma.cu) against its exact model
+"""The tcgen05 kernels (csrc/kernels_umma.cu) against their exact model
 (tests/split_model.py): every group whose whole K fits one exact pass (1 <= K
 <= 256) and that has at least 64 rows runs on the tensor cores with
-whole-K row and column exponents; its output must equal the model bit for bit.
+whole-K row and column exponents; longer groups (and the split-K parts of
+groups longer than 2048 slots) run in exact passes of 256 slots summed in
+FP64; the output must equal the model bit for bit.
 Dense products over the edge shapes (K = 1 and 256, ragged rows and columns,
 one to several column tiles and row-tile runs) and block-sparse contractions
 of a DMRG dot (column-block groups, strided operands).  The kernel's error
@@ -10,7 +12,7 @@ import numpy
 import pytest
 
 from tests.problems import random_problem, run_tasks_on_host
-from tests.split_model import one_pass_gemm
+from tests.split_model import one_pass_gemm, long_gemm
 
 pytestmark = pytest.mark.gpu
 
@@ -19,6 +21,17 @@ UMMA_MAX_K, UMMA_MIN_M = 256, 64
 
 def routed(A, B):
     return A.shape[1] <= UMMA_MAX_K and A.shape[1] >= 1 and A.shape[0] >= UMMA_MIN_M
+
+
+def model(A, B):
+    """The tcgen05 routes' result for a group of the task model, None for a
+    group the chunked kernels run (K <= 256 with fewer than 64 rows)."""
+    K = A.shape[1]
+    if K == 0:
+        return None
+    if K > UMMA_MAX_K:
+        return long_gemm(A, B)
+    return one_pass_gemm(A, B) if routed(A, B) else None
 
 
 def _dense(eng, M, K, N, rng, spread):
@@ -60,17 +73,25 @@ def test_dense_one_pass_bit_exact(gpu, M, K, N):
     assert eng.device_status() == 0
 
 
-def test_dense_beyond_one_pass_uses_the_chunked_kernels(gpu):
-    """K = 257 is not one pass: the chunked kernels run it (close to FP64)."""
+@pytest.mark.parametrize("M,K,N", [(200, 257, 40), (24, 300, 17), (100, 1000, 64), (130, 2048, 70),
+                                   (64, 2049, 33), (7, 5000, 130), (300, 700, 16)])
+def test_dense_long_k_bit_exact(gpu, M, K, N):
+    """K > 256: exact passes of 256 slots summed in FP64 (and parts of 2048
+    slots summed by the split-K reduction beyond that), any row count."""
     from zmpo_dmrg_gb300 import engine as E
     eng = E.get()
-    rng = numpy.random.default_rng(5)
-    pid, A, B, a, b, out = _dense(eng, 200, 257, 40, rng, 0.0)
-    eng.contract_exec(pid, a, b, out, "split")
-    got = out.cpu().numpy().reshape(200, 40)
-    exact = A @ B
-    assert numpy.linalg.norm(got - exact) / numpy.linalg.norm(exact) < 1e-8
-    eng.destroy_plan(pid)
+    rng = numpy.random.default_rng(M + 3 * K + 7 * N)
+    for spread in (0.0, 6.0):
+        pid, A, B, a, b, out = _dense(eng, M, K, N, rng, spread)
+        eng.contract_exec(pid, a, b, out, "split")
+        got = out.cpu().numpy().reshape(M, N)
+        ref = long_gemm(A, B)
+        assert numpy.array_equal(got, ref), (spread, numpy.abs(got - ref).max())
+        exact = A @ B
+        scale = K * numpy.abs(A).max(axis=1)[:, None] * numpy.abs(B).max(axis=0)[None, :]
+        assert (numpy.abs(got - exact) <= 2.0 ** -27 * scale + 1e-300).all()
+        eng.destroy_plan(pid)
+    assert eng.device_status() == 0
 
 
 def _dot_contraction(P, which):
@@ -122,8 +143,7 @@ def test_dot_contractions_bit_exact_on_routed_groups(gpu, which):
             cb = cbl[g["cb0"] + j]
             outn = max(outn, int(cb["c_off"] + (g["M"] - 1) * cb["scm"] + (cb["n"] - 1) * cb["scn"]) + 1)
     host_bufs[4] = numpy.full(outn, numpy.nan)
-    run_tasks_on_host(eng, pid, 1, host_bufs, lambda A, B: one_pass_gemm(A, B) if routed(A, B) else None,
-                      written)
+    run_tasks_on_host(eng, pid, 1, host_bufs, model, written)
     assert len(written) > 10
     out = torch.full((outn,), numpy.nan, dtype=torch.float64, device="cuda")
     eng.contract_exec(pid, a, b, out, "split")

@@ -29,8 +29,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = open(os.path.join(ROOT, "zmpo_dmrg_gb300", "csrc", "kernels_umma.cu")).read()
 ENGINE = open(os.path.join(ROOT, "zmpo_dmrg_gb300", "csrc", "engine.h")).read()
 
-TM, KMAX, KB_SLOTS, ROW_BYTES, NTHREADS = 128, 256, 32, 64, 192
-EPI_WARPS, PROD_WARP, MMA_WARP = 4, 4, 5
+TM, KMAX, KB_SLOTS, ROW_BYTES, NTHREADS = 128, 256, 32, 64, 320
+EPI_WARPS, PROD_WARP, MMA_WARP = 8, 8, 9
+STG_BYTES = EPI_WARPS * 32 * 8 * 8
 SMEM_MAX = 232448
 TX_MAX = (1 << 20) - 1
 
@@ -43,17 +44,20 @@ def test_constants_match_source():
     assert "constexpr int kUmmaTM = 128, kUmmaMaxK = 256, kUmmaKB = 32;" in ENGINE
     for name, val in [("ROW_BYTES", ROW_BYTES), ("NTHREADS", NTHREADS)]:
         assert re.search(r"constexpr int %s = %d;" % (name, val), SRC), name
-    assert "EPI_WARPS = 4, PROD_WARP = 4, MMA_WARP = 5" in SRC
+    assert "EPI_WARPS = 8, PROD_WARP = 8, MMA_WARP = 9" in SRC
+    assert "STG_BYTES = EPI_WARPS * 32 * 8 * 8;" in SRC
     assert (EPI_WARPS + 2) * 32 == NTHREADS
     assert "static constexpr int NSTAGE = TN == 64 ? 2 : 4;" in SRC
     # record sizes (engine.h) = the layout mirrored below
-    assert "umma_a_tile_bytes(int nkb) { return nkb * kUmmaAKB + kUmmaTM * 4; }" in ENGINE
+    assert "umma_a_rec_bytes(int nkb, int tm8) { return (int64_t)nkb * 256 * tm8 + kUmmaTM * 4; }" in ENGINE
     assert "umma_b_kb_bytes(int tn) { return 4 * (int64_t)tn * 64; }" in ENGINE
-    assert "umma_b_tile_bytes(int nkb, int tn) { return nkb * umma_b_kb_bytes(tn) + (int64_t)tn * 20; }" in ENGINE
+    assert "umma_b_rec_bytes(int nkb, int tn) { return nkb * umma_b_kb_bytes(tn) + (int64_t)tn * 20; }" in ENGINE
+    assert "constexpr int kUmmaLongMaxK = 2048;" in ENGINE
+    assert "static constexpr int NSTAGE = 4;" in SRC and "STAGE = umma::A_STAGE + B_KB;" in SRC
 
 
-def a_tile_bytes(nkb):
-    return nkb * 4 * TM * ROW_BYTES + TM * 4
+def a_tile_bytes(nkb, tm8=TM):
+    return nkb * 4 * tm8 * ROW_BYTES + TM * 4
 
 
 def b_tile_bytes(nkb, tn):
@@ -74,7 +78,8 @@ def layout(TN):
     L["REC_RS"] = L["REC_CB"] + TN * 8
     L["REC_INFO"] = L["REC_RS"] + TN * 8
     L["REC_BYTES"] = L["REC_INFO"] + 16
-    L["OFF_BAR"] = L["OFF_REC"] + 2 * L["REC_BYTES"]
+    L["OFF_STG"] = L["OFF_REC"] + 2 * L["REC_BYTES"]
+    L["OFF_BAR"] = L["OFF_STG"] + STG_BYTES
     L["NBAR"] = 11 + 2 * L["NSTAGE"]
     L["OFF_MISC"] = L["OFF_BAR"] + L["NBAR"] * 8
     L["BYTES"] = L["OFF_MISC"] + 16
@@ -87,7 +92,8 @@ def test_layout_formulas_match_source():
     for expr in ["B_KB = 4 * TN * ROW_BYTES", "OFF_A = OFF_B + NKB_MAX * B_KB",
                  "OFF_REC = OFF_A + NSTAGE * A_STAGE",
                  "REC_EB = REC_EA + TM * 4", "REC_CB = REC_EB + TN * 4", "REC_RS = REC_CB + TN * 8",
-                 "REC_INFO = REC_RS + TN * 8", "REC_BYTES = REC_INFO + 16", "OFF_BAR = OFF_REC + 2 * REC_BYTES",
+                 "REC_INFO = REC_RS + TN * 8", "REC_BYTES = REC_INFO + 16", "OFF_STG = OFF_REC + 2 * REC_BYTES",
+                 "OFF_BAR = OFF_STG + STG_BYTES",
                  "BAR_A_EMPTY = BAR_A_FULL + NSTAGE", "NBAR = BAR_A_FULL + 2 * NSTAGE",
                  "OFF_MISC = OFF_BAR + NBAR * 8", "BYTES = OFF_MISC + 16", "SMEM = BYTES + 1024",
                  "TMEM_COLS = 8 * TN", "A_PLANE = TM * ROW_BYTES", "A_STAGE = 4 * A_PLANE", "BAR_A_FULL = 11"]:
@@ -100,7 +106,9 @@ def test_shared_memory_regions(TN):
     assert L["SMEM"] <= SMEM_MAX
     regions = [("B", L["OFF_B"], L["OFF_A"]), ("A", L["OFF_A"], L["OFF_REC"]),
                ("rec", L["OFF_REC"], L["OFF_REC"] + 2 * L["REC_BYTES"]),
+               ("stg", L["OFF_STG"], L["OFF_STG"] + STG_BYTES),
                ("bar", L["OFF_BAR"], L["OFF_BAR"] + L["NBAR"] * 8), ("misc", L["OFF_MISC"], L["OFF_MISC"] + 16)]
+    assert L["OFF_STG"] % 8 == 0
     for (_, a0, a1), (_, b0, b1) in zip(regions, regions[1:]):
         assert a0 <= a1 <= b0 <= b1
     assert regions[-1][2] <= L["BYTES"]
@@ -122,29 +130,74 @@ def test_shared_memory_regions(TN):
 
 @pytest.mark.parametrize("TN", [16, 32, 64])
 @pytest.mark.parametrize("nkb", [1, 2, 7, 8])
-def test_bulk_copies(TN, nkb):
-    """Every copy the producer issues: source offset inside the tile record,
-    size a multiple of 16, destination inside its region; the bytes armed on
-    a barrier phase equal the bytes copied and stay within range."""
+@pytest.mark.parametrize("tm8", [8, 64, 120, 128])
+def test_bulk_copies(TN, nkb, tm8):
+    """Every copy the producers issue: source offset inside the record, size a
+    multiple of 16, destination inside its region; the bytes armed on a
+    barrier phase equal the bytes copied and stay within range."""
     L = layout(TN)
-    A, B = a_tile_bytes(nkb), b_tile_bytes(nkb, TN)
-    assert A % 16 == 0 and B % 16 == 0
-    # B planes of the item
+    akb = 4 * tm8 * ROW_BYTES
+    A, B = a_tile_bytes(nkb, tm8), b_tile_bytes(nkb, TN)
+    assert A % 16 == 0 and B % 16 == 0 and akb % 512 == 0
+    # B planes of a one-pass item
     size = nkb * L["B_KB"]
     assert size % 16 == 0 and size <= L["OFF_A"] - L["OFF_B"] and size <= TX_MAX
-    # per row tile: row exponents (end of the A tile) + column part (end of the B tile)
-    ea_src, eb_src = nkb * L["A_STAGE"], nkb * L["B_KB"]
+    # per row tile / pass: row exponents (end of the A record) + column part (end of the B record)
+    ea_src, eb_src = nkb * akb, nkb * L["B_KB"]
     assert ea_src % 16 == 0 and ea_src + TM * 4 == A
     assert eb_src % 16 == 0 and eb_src + TN * 20 == B
     assert L["REC_EA"] + TM * 4 == L["REC_EB"] and L["REC_EB"] + TN * 20 == L["REC_INFO"]
     assert (TM * 4) % 16 == 0 and (TN * 20) % 16 == 0
-    # A k blocks into the stage ring
-    for kb in range(nkb):
-        assert (kb * L["A_STAGE"]) % 16 == 0 and (kb + 1) * L["A_STAGE"] <= nkb * L["A_STAGE"]
-    assert L["A_STAGE"] <= TX_MAX
+    # A k blocks into a stage (tm8-row planes, 128 rows read from each)
+    assert akb <= L["A_STAGE"] and 3 * (akb // 4) + TM * ROW_BYTES <= L["A_STAGE"]
+    # long kernel: one stage = A k block + B k block
+    G = long_layout(TN)
+    assert akb + G["B_KB"] <= TX_MAX and akb <= G["A_STAGE"]
     # the column part's fields inside the B record
     tail = eb_src
     assert tail + TN * 4 + TN * 8 + TN * 8 == B and (tail + TN * 4) % 8 == 0 and (tail + TN * 12) % 8 == 0
+
+
+def long_layout(TN):
+    L = {"NSTAGE": 4, "A_STAGE": 4 * TM * ROW_BYTES}
+    L["B_KB"] = 4 * TN * ROW_BYTES
+    L["STAGE"] = L["A_STAGE"] + L["B_KB"]
+    L["OFF_S"] = 0
+    L["OFF_REC"] = L["NSTAGE"] * L["STAGE"]
+    L["REC_BYTES"] = TM * 4 + TN * 20 + 16
+    L["OFF_STG"] = L["OFF_REC"] + 2 * L["REC_BYTES"]
+    L["OFF_BAR"] = L["OFF_STG"] + STG_BYTES
+    L["NBAR"] = 9 + 2 * L["NSTAGE"]
+    L["OFF_MISC"] = L["OFF_BAR"] + L["NBAR"] * 8
+    L["BYTES"] = L["OFF_MISC"] + 16
+    L["SMEM"] = L["BYTES"] + 1024
+    L["TMEM_COLS"] = 8 * TN
+    return L
+
+
+def test_long_layout_formulas_match_source():
+    for expr in ["STAGE = umma::A_STAGE + B_KB", "OFF_REC = OFF_S + NSTAGE * STAGE",
+                 "OFF_STG = OFF_REC + 2 * REC_BYTES", "OFF_BAR = OFF_STG + umma::STG_BYTES",
+                 "BAR_DONE = 8, BAR_S_FULL = 9, BAR_S_EMPTY = BAR_S_FULL + NSTAGE",
+                 "NBAR = BAR_S_EMPTY + NSTAGE"]:
+        assert expr in SRC, expr
+
+
+@pytest.mark.parametrize("TN", [16, 32, 64])
+def test_long_kernel_shared_memory(TN):
+    L = long_layout(TN)
+    assert L["SMEM"] <= SMEM_MAX and L["BYTES"] + 1023 <= L["SMEM"]
+    assert L["STAGE"] % 1024 == 0 and L["B_KB"] % 1024 == 0 and L["OFF_REC"] % 16 == 0
+    assert L["OFF_BAR"] % 8 == 0
+    # B k block of a stage right after its 32 KB A part; the MMAs read from
+    # the stage's A part (planes tm8 rows apart, 128 rows each) and B part
+    for s in range(L["NSTAGE"]):
+        st = s * L["STAGE"]
+        for tm8 in (8, 64, 128):
+            pl = tm8 * ROW_BYTES
+            assert st + 3 * pl + TM * ROW_BYTES <= st + L["A_STAGE"]
+        assert st + L["A_STAGE"] + 4 * TN * ROW_BYTES <= st + L["STAGE"] <= L["OFF_REC"]
+    assert 2 * L["SMEM"] > 228 * 1024 or 2 * L["TMEM_COLS"] <= 512
 
 
 def test_planner_plane_offsets_are_aligned():
@@ -192,19 +245,23 @@ def tensor_core_read(start, row, k):
 def test_swizzled_stores_match_descriptor_reads(TN):
     L = layout(TN)
     base = 1024 * 7   # any 1024-aligned dynamic-smem base
-    # A: record k block kb -> stage s; plane p, row r, slot j
-    for s in range(L["NSTAGE"]):
-        for kb in (0, 3):
-            for p in range(4):
-                for r in range(TM):
-                    for j in range(KB_SLOTS):
-                        rec_off = kb * L["A_STAGE"] + p * L["A_PLANE"] + store_offset(r, j // 8) + (j % 8) * 2
-                        # the bulk copy moves k block kb's bytes unchanged to the stage
-                        w = base + L["OFF_A"] + s * L["A_STAGE"] + (rec_off - kb * L["A_STAGE"])
-                        plane = base + L["OFF_A"] + s * L["A_STAGE"] + p * L["A_PLANE"]
-                        k16, k = divmod(j, 16)
-                        assert tensor_core_read(plane + k16 * 32, r, k) == w
-                        assert plane <= w < plane + L["A_PLANE"]
+    # A: record k block kb (planes tm8 rows apart) -> stage s; plane p, row
+    # r < tm8, slot j (the prepare kernel's cut8_store(row=r) into a plane of
+    # tm8 * 64 bytes)
+    for tm8 in (8, 56, 128):
+        pl = tm8 * ROW_BYTES
+        for s in range(L["NSTAGE"]):
+            for kb in (0, 3):
+                for p in range(4):
+                    for r in range(tm8):
+                        for j in range(KB_SLOTS):
+                            rec_off = kb * 4 * pl + p * pl + store_offset(r, j // 8) + (j % 8) * 2
+                            # the bulk copy moves k block kb's bytes unchanged to the stage
+                            w = base + L["OFF_A"] + s * L["A_STAGE"] + (rec_off - kb * 4 * pl)
+                            plane = base + L["OFF_A"] + s * L["A_STAGE"] + p * pl
+                            k16, k = divmod(j, 16)
+                            assert tensor_core_read(plane + k16 * 32, r, k) == w
+                            assert plane <= w < plane + pl
     # B': record k block kb, plane p, column c -> operand row p*TN + c; the
     # whole record's planes are copied to OFF_B
     for kb in range(KMAX // KB_SLOTS):
@@ -257,3 +314,40 @@ def test_descriptor_encodings():
         assert d & 0b1111 == 0 and (d >> 13) & 3 == 0 and (d >> 23) & 1 == 0 and d >> 29 == 0
     sd = re.search(r"uint64_t sdesc\(uint32_t addr\) \{(.*?)\}", SRC, re.S).group(1)
     assert "((uint64_t)(512u >> 4) << 32)" in sd and "((uint64_t)1u << 46)" in sd and "((uint64_t)4u << 61)" in sd
+
+
+def test_epilogue_staging_and_tmem_chunks():
+    """Epilogue warp w: TMEM lane quarter w % 4, 8-column chunks from 8 (w / 4)
+    in steps of 16; its 2 KB staging area holds 32 rows x 8 float64; the
+    swizzled writes (lane = row) and reads (4 rows x 8 columns per
+    instruction) cover the area exactly once each."""
+    assert "tcgen05.ld.sync.aligned.32x32b.x8.b32" in SRC
+    assert "const int quarter = warp & 3, half = warp >> 2;" in SRC
+    for TN in (16, 32, 64):
+        cover = {}
+        for w in range(EPI_WARPS):
+            q, h = w & 3, w >> 2
+            for c0 in range(8 * h, TN, 16):
+                for lane in range(32):
+                    for i in range(8):
+                        key = (q * 32 + lane, c0 + i)
+                        cover[key] = cover.get(key, 0) + 1
+        assert len(cover) == TM * TN and set(cover.values()) == {1}
+    widx = lambda lane, i: lane * 8 + (i ^ ((lane >> 1) & 7))
+    ridx = lambda r, col: r * 8 + (col ^ ((r >> 1) & 7))
+    assert "stg[lane * 8 + (i ^ ((lane >> 1) & 7))] = val[i];" in SRC
+    assert "stg[r * 8 + (col ^ ((r >> 1) & 7))];" in SRC
+    writes = sorted(widx(lane, i) for lane in range(32) for i in range(8))
+    reads = sorted(ridx(k * 4 + (lane >> 3), lane & 7) for k in range(8) for lane in range(32))
+    assert writes == list(range(256)) and reads == list(range(256))
+    # a read instruction: 4 rows x 8 columns, 4 distinct rows, all 8 columns each
+    for k in range(8):
+        rows = {k * 4 + (lane >> 3) for lane in range(32)}
+        assert len(rows) == 4
+    # no bank conflicts: an 8-byte access is served per half warp (128 bytes);
+    # its 16 lanes must hit 16 different bank pairs
+    for hw in (range(0, 16), range(16, 32)):
+        for i in range(8):
+            assert len({widx(lane, i) % 16 for lane in hw}) == 16
+        for k in range(8):
+            assert len({ridx(k * 4 + (lane >> 3), lane & 7) % 16 for lane in hw}) == 16

@@ -64,37 +64,42 @@ struct Work {
   int32_t pad;      // B-resident kernel: row tiles of the item (from row mt)
 };
 
-// One-pass tensor-core path (kernels_umma.cu): groups whose whole K fits one
-// exact pass.  Their operand tiles are cut by prepare kernels into the digit
-// planes the tensor cores read (K-major, 64-byte swizzle, the shared-memory
-// image), in a plane buffer:
-//   A tile (group, row tile of 128 rows): nkb k blocks of 32 slots, each four
-//     planes of 128 rows x 64 bytes, then 128 int32 row exponents;
-//   B tile (group, column tile of tn columns): nkb k blocks, each four planes
-//     of tn rows x 64 bytes (plane s holds rows s*tn .. s*tn+tn-1), then tn
-//     int32 column exponents, tn int64 output offsets of (row 0, column c)
-//     (-1: no such column) and tn int64 output row strides.
+// tcgen05 path (kernels_umma.cu), split precision.  Groups whose whole K
+// fits one exact pass (1 <= K <= 256, at least 64 rows) are multiplied in one
+// pass per tile; groups with 256 < K <= 2048 and the split-K parts of longer
+// groups in passes of 256 slots, each pass exact with its own exponents,
+// summed in FP64 in pass order.  Prepare kernels cut the operand tiles of
+// every pass once per launch into records that are the shared-memory image
+// the tensor cores read (K-major, 64-byte swizzle), in a plane buffer:
+//   A record (row tile of tm8 rows, tm8 = the tile's rows rounded up to 8, one
+//     pass): nkb k blocks of 32 slots, each four planes of tm8 rows x 64
+//     bytes, then 128 int32 row exponents;
+//   B record (column tile of tn columns, one pass): nkb k blocks, each four
+//     planes of tn rows x 64 bytes (plane s holds rows s*tn .. s*tn+tn-1),
+//     then tn int32 column exponents, tn int64 output offsets of (row 0,
+//     column c) (-1: no such column) and tn int64 output row strides.
 // Every record size is a multiple of 16 bytes (bulk-copy granularity).
 constexpr int kUmmaTM = 128, kUmmaMaxK = 256, kUmmaKB = 32;
-constexpr int64_t kUmmaAPlane = 128 * 64;           // one digit plane of a k block
-constexpr int64_t kUmmaAKB = 4 * kUmmaAPlane;       // four planes
-constexpr int64_t umma_a_tile_bytes(int nkb) { return nkb * kUmmaAKB + kUmmaTM * 4; }
+constexpr int kUmmaLongMaxK = 2048;                 // K of a long item (passes of kUmmaMaxK)
+constexpr int64_t kUmmaAPlane = 128 * 64;           // one 128-row digit plane of a k block
+constexpr int64_t kUmmaAKB = 4 * kUmmaAPlane;       // four planes (shared-memory stage)
+constexpr int64_t umma_a_rec_bytes(int nkb, int tm8) { return (int64_t)nkb * 256 * tm8 + kUmmaTM * 4; }
 constexpr int64_t umma_b_kb_bytes(int tn) { return 4 * (int64_t)tn * 64; }
-constexpr int64_t umma_b_tile_bytes(int nkb, int tn) { return nkb * umma_b_kb_bytes(tn) + (int64_t)tn * 20; }
+constexpr int64_t umma_b_rec_bytes(int nkb, int tn) { return nkb * umma_b_kb_bytes(tn) + (int64_t)tn * 20; }
 
-struct PrepA {      // cut one A tile: rows m0 .. m0+127 of the group
-  int64_t rec;      // byte offset of the tile record in the plane buffer
-  int32_t group, m0;
+struct PrepA {      // cut one A record: rows m0 .., slots k0 .. k0+kc-1 of the group
+  int64_t rec;      // byte offset of the record in the plane buffer
+  int32_t group, m0, k0, kc;
 };
-struct PrepB {      // cut one B tile: columns n0 .. n0+tn-1 of the group
+struct PrepB {      // cut one B record: columns n0 .. n0+tn-1, slots k0 .. k0+kc-1
   int64_t rec;
-  int32_t group, n0, tn, pad;
+  int32_t group, n0, tn, k0, kc, pad;
 };
-struct UWork {      // tcgen05 work item: one column tile, a run of row tiles
-  int64_t a_rec;    // record of the run's first A tile (a group's A tiles are consecutive)
-  int64_t b_rec;    // record of the column tile's B tile
+struct UWork {      // tcgen05 work item: one column tile, a run of row tiles (one-pass)
+  int64_t a_rec;    // or one row tile and every pass of its K (long); first A record
+  int64_t b_rec;    // first B record of the column tile
   int32_t group, m0;
-  int32_t nrt_k;    // row tiles of the run | K << 8
+  int32_t nrt_k;    // row tiles of the run (1 for long items) | K << 8
   int32_t pad;
 };
 
@@ -123,20 +128,22 @@ struct Step {
   // nt, row tiles mt .. mt+pad-1) and the tiles of all other groups
   Work *d_work_tcb[2] = {};    // [64 x 64 tiles, 128 x 32 tiles]
   Work *d_work_tc4[3][4] = {};
-  // 4 digit slices, groups whose whole K fits one exact pass (1 <= K <= 256,
-  // at least 64 rows): the prepare items (A and B tiles) and the tensor-core
-  // (tcgen05) work items by column tile 16 / 32 / 64
+  // 4 digit slices, the tcgen05 groups: the prepare items (A and B records)
+  // and the work items of the one-pass kernel by column tile 16 / 32 / 64
   PrepA *d_prep_a = nullptr;
   PrepB *d_prep_b = nullptr;
   int64_t nprep_a = 0, nprep_b = 0;
   UWork *d_work_um[3] = {};
   int64_t nwork_um[3] = {};
+  UWork *d_work_ul[3] = {};         // long items (passes), by column tile 16 / 32 / 64
+  int64_t nwork_ul[3] = {};
+  bool split_done = false;          // split-K parts made (split_long_groups)
   int64_t plane_bytes = 0;          // A tiles, then B tiles (from plane_b0)
   int64_t plane_b0 = 0;
   // where the plane buffer lives: a byte offset into the workspace buffer
-  // (sigma and renorm plans; every step of a plan shares one region), or
-  // step-owned memory (plane_ws_off < 0: contraction plans, allocated when
-  // the step's task lists are uploaded)
+  // (sigma plans; every step of a plan shares one region), or step-owned
+  // memory (plane_ws_off < 0: renormalisation and contraction plans,
+  // allocated at the step's first split-precision run)
   int64_t plane_ws_off = -1;
   unsigned char *d_planes_own = nullptr;
   int64_t nwork_fp64 = 0;

@@ -928,6 +928,10 @@ extern "C" int zmpo_contract_exec_noalloc(zmpo_engine *e, int plan_id, const dou
   zmpo::Step *st = nullptr;
   int rc = zmpo::contract_step_for(e, plan_id, &st);
   if (rc) return rc;
+  if (precision == ZMPO_PREC_SPLIT && st->plane_bytes > 0 && st->plane_ws_off < 0 && !st->d_planes_own)
+    return zmpo::record_arg_error(
+        "contract_exec_noalloc: run the plan once with the split precision through zmpo_contract_exec "
+        "during set-up (that call makes the plan's digit-plane buffer)");
   if (st->part_elems > kNoAllocScratchElems)
     return zmpo::record_size_error(
         "contract_exec_noalloc: the plan needs more split-K scratch than the fixed 8 MiB "

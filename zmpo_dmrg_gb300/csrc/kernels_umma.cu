@@ -67,8 +67,9 @@ constexpr int NKB_MAX = KMAX / KB_SLOTS;
 constexpr int ROW_BYTES = 64;                 // K-major rows of 32 bf16, 64-byte swizzle
 constexpr int A_PLANE = TM * ROW_BYTES;       // 8 KB: one digit plane of a k block
 constexpr int A_STAGE = 4 * A_PLANE;          // 32 KB: four planes
-constexpr int NTHREADS = 192;
-constexpr int EPI_WARPS = 4, PROD_WARP = 4, MMA_WARP = 5;
+constexpr int NTHREADS = 320;
+constexpr int EPI_WARPS = 8, PROD_WARP = 8, MMA_WARP = 9;
+constexpr int STG_BYTES = EPI_WARPS * 32 * 8 * 8;  // per epilogue warp: 32 rows x 8 float64
 constexpr int PREP_THREADS = 256;
 constexpr int BIAS = 2082;
 constexpr uint64_t WAIT_NS = 2000000000ull;   // 2 s bound on every wait
@@ -105,7 +106,8 @@ struct Layout {
   static constexpr int REC_RS = REC_CB + TN * 8;          // int64 rowstride[TN]
   static constexpr int REC_INFO = REC_RS + TN * 8;        // int m0, M, cbuf, pad
   static constexpr int REC_BYTES = REC_INFO + 16;
-  static constexpr int OFF_BAR = OFF_REC + 2 * REC_BYTES;
+  static constexpr int OFF_STG = OFF_REC + 2 * REC_BYTES;  // epilogue staging, 2 KB per warp
+  static constexpr int OFF_BAR = OFF_STG + STG_BYTES;
   static constexpr int BAR_A_EMPTY = BAR_A_FULL + NSTAGE;
   static constexpr int NBAR = BAR_A_FULL + 2 * NSTAGE;
   static constexpr int OFF_MISC = OFF_BAR + NBAR * 8;     // tmem base, abort flag
@@ -235,6 +237,13 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *v) {
       : "memory");
 }
 
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t *v) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+               : "r"(taddr)
+               : "memory");
+}
+
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // ------------------------------------------------------------ digit cut
@@ -302,14 +311,44 @@ __device__ __forceinline__ double scaled_int_to_double(long long S, int e) {
 
 __device__ __forceinline__ long long lvl(uint32_t bits) { return (long long)__float2int_rz(__uint_as_float(bits)); }
 
-// Slot table of all K slots of a group (one warp): lanes take segments 32 at
-// a time, an inclusive scan places each segment's k range.  Returns K; sets
-// *scaled when some slot has a weight other than 1.
-__device__ int build_slots(const Group &g, const Seg *__restrict__ segs, const Bufs &bufs, Slot *slots, int lane,
-                           int *scaled) {
+// The epilogue warp's 32 x 8 chunk (lane = row row0 + lane, val[i] =
+// column i) stored through the warp's 2 KB staging area: each store
+// instruction then writes 4 rows x 8 consecutive columns (64 contiguous bytes
+// per row when the columns are in one output block).  The chunk's columns
+// are cb[i] (output offset of row 0, < 0: none) and rs[i] (row stride).  The
+// staging index is XOR-swizzled by bits 1-3 of the row, so the 16 lanes of a
+// half warp touch 16 different 8-byte bank pairs (no bank conflicts).
+// Called by every lane of the warp.
+__device__ __forceinline__ void store_chunk(double *stg, const double *val, int lane, int row0, int M,
+                                            const long long *cb, const long long *rs, double *out, bool ok) {
+#pragma unroll
+  for (int i = 0; i < 8; ++i) stg[lane * 8 + (i ^ ((lane >> 1) & 7))] = val[i];
+  __syncwarp();
+  if (ok) {
+    const int col = lane & 7;
+    const long long base = cb[col], stride = rs[col];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int r = k * 4 + (lane >> 3);
+      const double x = stg[r * 8 + (col ^ ((r >> 1) & 7))];
+      if (row0 + r < M && base >= 0) out[base + (long long)(row0 + r) * stride] = x;
+    }
+  }
+  __syncwarp();
+}
+
+// Slot table of the slots k0 .. k0+kc-1 of a group (one warp; kc <= KMAX):
+// lanes take segments 32 at a time, an inclusive scan places each segment's
+// k range, and the part of it inside the window is written.  Returns the
+// number of slots in the window; sets *scaled when one of them has a weight
+// other than 1.
+__device__ int build_slots_window(const Group &g, const Seg *__restrict__ segs, const Bufs &bufs, Slot *slots,
+                                  int lane, int k0, int kc, int *scaled) {
+  kc = min(kc, KMAX);
+  const int k1 = k0 + kc;
   int base = 0;
   unsigned sc = 0;
-  for (int s0 = 0; s0 < g.nseg; s0 += 32) {
+  for (int s0 = 0; s0 < g.nseg && base < k1; s0 += 32) {
     const int sidx = s0 + lane;
     Seg sg;
     int k = 0;
@@ -323,12 +362,15 @@ __device__ int build_slots(const Group &g, const Seg *__restrict__ segs, const B
       const int t = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += t;
     }
-    const int excl = incl - k;
-    if (k > 0 && base + incl <= KMAX) {
+    const int first = base + incl - k;  // global slot of the segment's k = 0
+    const int lo = max(first, k0), hi = min(first + k, k1);
+    const bool in = k > 0 && lo < hi;
+    if (in) {
       const double *A = bufs.p[sg.abuf] + sg.a_off;
       const double *B = g.ncb ? bufs.p[sg.bbuf] : bufs.p[sg.bbuf] + sg.b_off;
-      for (int j = 0; j < k; ++j) {
-        Slot &sl = slots[base + excl + j];
+      for (int gj = lo; gj < hi; ++gj) {
+        const int j = gj - first;
+        Slot &sl = slots[gj - k0];
         sl.a = A + (int64_t)j * sg.sak;
         sl.b = g.ncb ? B : B + (int64_t)j * sg.sbk;
         sl.sam = sg.sam;
@@ -339,12 +381,15 @@ __device__ int build_slots(const Group &g, const Seg *__restrict__ segs, const B
         sl.kk = j;
       }
     }
-    sc |= __ballot_sync(0xffffffffu, k > 0 && sg.alpha != 1.0);
+    sc |= __ballot_sync(0xffffffffu, in && sg.alpha != 1.0);
     base += __shfl_sync(0xffffffffu, incl, 31);
   }
   *scaled = sc != 0u;
-  return base;
+  return max(0, min(kc, base - k0));
 }
+
+// rows of a row tile rounded up to 8 (the rows an A record holds)
+__device__ __forceinline__ int tile_rows8(int M, int m0) { return (min(TM, M - m0) + 7) & ~7; }
 
 // A(row, slot j), with the slot's weight when the group has weights
 __device__ __forceinline__ double load_a(const Slot &sl, int row, bool scaled) {
@@ -356,10 +401,11 @@ __device__ __forceinline__ double load_a(const Slot &sl, int row, bool scaled) {
 }  // namespace umma
 
 // ------------------------------------------------------------ prepare kernels
-// One A tile per item: the row exponents of rows m0 .. m0+127 over the
-// group's K (two threads per row, eight loads in flight each), then the four
-// digit planes of every k block (a warp writes 8 rows x 4 chunks = 512
-// contiguous bytes of each plane), then the exponents after the planes.
+// One A record per item (rows m0 .. m0+tm8-1, slots k0 .. k0+kc-1 of the
+// group): the row exponents over the window (two threads per row, eight
+// loads in flight each), then the four digit planes of tm8 rows of every k
+// block (a warp writes 8 rows x 4 chunks = 512 contiguous bytes of each
+// plane), then the 128 exponents after the planes.
 __global__ void __launch_bounds__(umma::PREP_THREADS)
 k_prep_a(const PrepA *__restrict__ items, int64_t nitems, const Group *__restrict__ groups,
          const Seg *__restrict__ segs, Bufs bufs, unsigned char *__restrict__ planes) {
@@ -373,7 +419,7 @@ k_prep_a(const PrepA *__restrict__ items, int64_t nitems, const Group *__restric
     const Group g = groups[p.group];
     if (warp == 0) {
       int sc;
-      const int K = build_slots(g, segs, bufs, slots, lane, &sc);
+      const int K = build_slots_window(g, segs, bufs, slots, lane, p.k0, p.kc, &sc);
       if (lane == 0) {
         s_ctl[0] = K;
         s_ctl[1] = sc;
@@ -383,6 +429,7 @@ k_prep_a(const PrepA *__restrict__ items, int64_t nitems, const Group *__restric
     const int K = s_ctl[0];
     const bool scaled = s_ctl[1] != 0;
     const int nkb = (K + KB_SLOTS - 1) / KB_SLOTS;
+    const int tm8 = tile_rows8(g.M, p.m0), PL = tm8 * ROW_BYTES;
     {
       const int row = tid >> 1, half = tid & 1, grow = p.m0 + row;
       int em = 0;
@@ -403,9 +450,9 @@ k_prep_a(const PrepA *__restrict__ items, int64_t nitems, const Group *__restric
     }
     __syncthreads();
     unsigned char *rec = planes + p.rec;
-    if (tid < TM) reinterpret_cast<int *>(rec + (int64_t)nkb * A_STAGE)[tid] = s_ea[tid];
-    for (int u = tid; u < nkb * TM * 4; u += PREP_THREADS) {
-      const int kb = u / (TM * 4), row = (u >> 2) & (TM - 1), ch = u & 3;
+    if (tid < TM) reinterpret_cast<int *>(rec + (int64_t)nkb * 4 * PL)[tid] = s_ea[tid];
+    for (int u = tid; u < nkb * tm8 * 4; u += PREP_THREADS) {
+      const int kb = u / (tm8 * 4), rem = u - kb * (tm8 * 4), row = rem >> 2, ch = rem & 3;
       const int grow = p.m0 + row;
       double v[8];
 #pragma unroll
@@ -413,17 +460,17 @@ k_prep_a(const PrepA *__restrict__ items, int64_t nitems, const Group *__restric
         const int j = kb * KB_SLOTS + ch * 8 + i;
         v[i] = (grow < g.M && j < K) ? load_a(slots[j], grow, scaled) : 0.0;
       }
-      cut8_store(v, s_ea[row], rec + (int64_t)kb * A_STAGE, A_PLANE, row, ch);
+      cut8_store(v, s_ea[row], rec + (int64_t)kb * 4 * PL, PL, row, ch);
     }
     __syncthreads();  // the slot table and the exponents are rewritten by the next item
   }
 }
 
-// One B tile per item (columns n0 .. n0+tn-1): the column map (output offset
-// of row 0 and row stride of each column, column-block lookups once per
-// column), the column exponents over the group's K, the four digit planes of
-// every k block (plane s holds rows s*tn + c), then exponents, offsets and
-// strides after the planes.
+// One B record per item (columns n0 .. n0+tn-1, slots k0 .. k0+kc-1): the
+// column map (output offset of row 0 and row stride of each column,
+// column-block look-ups once per column), the column exponents over the
+// window, the four digit planes of every k block (plane s holds rows
+// s*tn + c), then exponents, offsets and strides after the planes.
 __global__ void __launch_bounds__(umma::PREP_THREADS)
 k_prep_b(const PrepB *__restrict__ items, int64_t nitems, const Group *__restrict__ groups,
          const Seg *__restrict__ segs, const ColBlock *__restrict__ cbl, const SegB *__restrict__ segb, Bufs bufs,
@@ -440,7 +487,7 @@ k_prep_b(const PrepB *__restrict__ items, int64_t nitems, const Group *__restric
     const int tn = p.tn;
     if (warp == 0) {
       int sc;
-      const int K = build_slots(g, segs, bufs, slots, lane, &sc);
+      const int K = build_slots_window(g, segs, bufs, slots, lane, p.k0, p.kc, &sc);
       if (lane == 0) {
         s_ctl[0] = K;
         s_ctl[1] = sc;
@@ -577,26 +624,27 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
         const unsigned char *arec = planes + wk.a_rec;
         for (int r = 0; r < nrt; ++r, ++t) {
           const uint32_t b = t & 1, u = t >> 1;
+          const int m0 = wk.m0 + r * TM, akb = 4 * tile_rows8(g.M, m0) * ROW_BYTES;  // bytes of an A k block
           if (!(ok = wait_bounded(bar(BAR_E_EMPTY + b), (u & 1) ^ 1, abort_flag, 2))) break;
           unsigned char *rec = rec0 + b * LY::REC_BYTES;
           const uint32_t rec_s = base_s + LY::OFF_REC + b * LY::REC_BYTES;
           int *info = reinterpret_cast<int *>(rec + LY::REC_INFO);
-          info[0] = wk.m0 + r * TM;
+          info[0] = m0;
           info[1] = g.M;
           info[2] = g.cbuf;
           bar_arrive_tx(bar(BAR_E_FULL + b), (uint32_t)(TM * 4 + TN * 20));
-          bulk_g2s(rec_s + LY::REC_EA, arec + (int64_t)nkb * A_STAGE, TM * 4, bar(BAR_E_FULL + b));
+          bulk_g2s(rec_s + LY::REC_EA, arec + (int64_t)nkb * akb, TM * 4, bar(BAR_E_FULL + b));
           bulk_g2s(rec_s + LY::REC_EB, brec + (int64_t)nkb * LY::B_KB, TN * 20, bar(BAR_E_FULL + b));
           ++nE[b];
           for (int kb = 0; kb < nkb; ++kb, ++q) {
             const uint32_t s = q % NSTAGE, use = q / NSTAGE;
             if (!(ok = wait_bounded(bar(LY::BAR_A_EMPTY + s), (use & 1) ^ 1, abort_flag, 3))) break;
-            bar_arrive_tx(bar(BAR_A_FULL + s), A_STAGE);
-            bulk_g2s(base_s + LY::OFF_A + s * A_STAGE, arec + (int64_t)kb * A_STAGE, A_STAGE, bar(BAR_A_FULL + s));
+            bar_arrive_tx(bar(BAR_A_FULL + s), (uint32_t)akb);
+            bulk_g2s(base_s + LY::OFF_A + s * A_STAGE, arec + (int64_t)kb * akb, (uint32_t)akb, bar(BAR_A_FULL + s));
             ++nA[s];
           }
           if (!ok) break;
-          arec += umma_a_tile_bytes(nkb);
+          arec += (int64_t)nkb * akb + TM * 4;
         }
       }
       // drain: every bulk copy issued has landed before the CTA may exit
@@ -615,12 +663,16 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
       for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x, ++item) {
         if (*abort_flag) break;
         const UWork wk = work[w];
+        const int M = groups[wk.group].M;
         const int nrt = wk.nrt_k & 0xff, K = wk.nrt_k >> 8;
         const int nkb = (K + KB_SLOTS - 1) / KB_SLOTS;
         const bool okb = wait_bounded(bar(BAR_B_FULL), item & 1, abort_flag, 4);
         tc_fence_after();
         for (int r = 0; r < nrt; ++r, ++t) {
           const uint32_t b = t & 1, u = t >> 1;
+          // planes of the A record are tm8 rows apart; the MMA reads 128 rows
+          // from each (rows past tm8 land in TMEM lanes the epilogue skips)
+          const uint32_t PL = (uint32_t)(tile_rows8(M, wk.m0 + r * TM) * ROW_BYTES);
           wait_bounded(bar(BAR_T_EMPTY + b), (u & 1) ^ 1, abort_flag, 5);
           tc_fence_after();
           for (int kb = 0; kb < nkb; ++kb, ++q) {
@@ -636,7 +688,7 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
 #pragma unroll
                 for (int a = 0; a < 4; ++a) {
                   const uint32_t d = tmem + b * (4 * TN) + a * TN;
-                  mma(d, sdesc(a_s + a * A_PLANE + k16 * 32), sdesc(b_s + k16 * 32), idesc((4 - a) * TN),
+                  mma(d, sdesc(a_s + a * PL + k16 * 32), sdesc(b_s + k16 * 32), idesc((4 - a) * TN),
                       (kb | k16 | a) != 0);
                 }
               }
@@ -652,8 +704,12 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
     __syncwarp();
   } else {
     // ================================================================= epilogue
-    const int e = tid;  // row of the tile, warp e/32 reads TMEM lanes 32(e/32)..
-    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    // warp w reads TMEM lanes 32(w%4).. (tile rows) and every other 8-column
+    // chunk (from column 8(w/4))
+    const int quarter = warp & 3, half = warp >> 2;
+    const int e = quarter * 32 + lane;
+    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+    double *stg = reinterpret_cast<double *>(sm + LY::OFF_STG) + warp * 256;
     uint32_t t = 0;
     for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
       if (role_sync_or(2, EPI_WARPS * 32, *abort_flag != 0)) break;
@@ -669,7 +725,6 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
         const int *eb = reinterpret_cast<const int *>(rec + LY::REC_EB);
         const long long *cb = reinterpret_cast<const long long *>(rec + LY::REC_CB);
         const long long *rs = reinterpret_cast<const long long *>(rec + LY::REC_RS);
-        const int row = m0 + e;
         // stores only when the tile record and the accumulators are both this
         // tile's (an aborting MMA issuer commits without having multiplied)
         const bool ok_acc = wait_bounded(bar(BAR_T_FULL + b), u & 1, abort_flag, 8);
@@ -677,21 +732,19 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
         tc_fence_after();
         double *out = bufs.p[ok ? cbuf : 0];
 #pragma unroll 1
-        for (int c0 = 0; c0 < TN; c0 += 16) {
-          uint32_t v[4][16];
+        for (int c0 = 8 * half; c0 < TN; c0 += 16) {
+          uint32_t v[4][8];
           const uint32_t ta = tmem + lane_base + b * (4 * TN) + c0;
 #pragma unroll
-          for (int l = 0; l < 4; ++l) tmem_ld16(ta + l * TN, v[l]);
+          for (int l = 0; l < 4; ++l) tmem_ld8(ta + l * TN, v[l]);
           tmem_ld_wait();
-          if (ok && row < M) {
+          double val[8];
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
-              const long long base = cb[c0 + i];
-              if (base < 0) continue;
-              const long long S = (lvl(v[0][i]) << 24) + (lvl(v[1][i]) << 16) + (lvl(v[2][i]) << 8) + lvl(v[3][i]);
-              out[base + (long long)row * rs[c0 + i]] = scaled_int_to_double(S, ea + eb[c0 + i] - BIAS);
-            }
+          for (int i = 0; i < 8; ++i) {
+            const long long S = (lvl(v[0][i]) << 24) + (lvl(v[1][i]) << 16) + (lvl(v[2][i]) << 8) + lvl(v[3][i]);
+            val[i] = scaled_int_to_double(S, ea + eb[c0 + i] - BIAS);
           }
+          store_chunk(stg, val, lane, m0 + quarter * 32, M, cb + c0, rs + c0, out, ok);
         }
         tc_fence_before();
         bar_arrive(bar(BAR_T_EMPTY + b));
@@ -712,6 +765,265 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(LY::TMEM_COLS)
                  : "memory");
   }
+}
+
+// ------------------------------------------------------------- long kernel
+// Groups with a longer K than one pass (at most kUmmaLongMaxK slots: the
+// split-K parts of longer groups): a work item is one row tile and one
+// column tile over every pass of 256 slots.  Each pass has its own A and B
+// records (own exponents), so a stage of the ring carries one k block of
+// both; the tile's result of a pass, exact as in the one-pass kernel, is
+// added in FP64 (pass order) to the epilogue's per-thread accumulators, and
+// the sum is stored once after the last pass.
+template <int TN>
+struct LongLayout {
+  static constexpr int NSTAGE = 4;
+  static constexpr int B_KB = 4 * TN * umma::ROW_BYTES;
+  static constexpr int STAGE = umma::A_STAGE + B_KB;      // A k block (128-row planes) + B k block
+  static constexpr int OFF_S = 0;
+  static constexpr int OFF_REC = OFF_S + NSTAGE * STAGE;
+  static constexpr int REC_EA = 0;
+  static constexpr int REC_EB = REC_EA + umma::TM * 4;
+  static constexpr int REC_CB = REC_EB + TN * 4;
+  static constexpr int REC_RS = REC_CB + TN * 8;
+  static constexpr int REC_INFO = REC_RS + TN * 8;
+  static constexpr int REC_BYTES = REC_INFO + 16;
+  static constexpr int OFF_STG = OFF_REC + 2 * REC_BYTES;  // epilogue staging, 2 KB per warp
+  static constexpr int OFF_BAR = OFF_STG + umma::STG_BYTES;
+  // barriers: T_FULL[2], T_EMPTY[2], E_FULL[2], E_EMPTY[2], DONE, S_FULL[NSTAGE], S_EMPTY[NSTAGE]
+  static constexpr int BAR_DONE = 8, BAR_S_FULL = 9, BAR_S_EMPTY = BAR_S_FULL + NSTAGE;
+  static constexpr int NBAR = BAR_S_EMPTY + NSTAGE;
+  static constexpr int OFF_MISC = OFF_BAR + NBAR * 8;
+  static constexpr int BYTES = OFF_MISC + 16;
+  static constexpr int SMEM = BYTES + 1024;
+  static constexpr int TMEM_COLS = 8 * TN;
+  static_assert(TN == 16 || TN == 32 || TN == 64, "column tile");
+  static_assert(STAGE % 1024 == 0 && B_KB % 1024 == 0, "swizzle atoms");
+  static_assert(OFF_REC % 16 == 0 && REC_EB % 16 == 0 && REC_BYTES % 16 == 0, "bulk-copy alignment");
+  static_assert(SMEM <= 232448, "shared memory");
+};
+
+template <int TN>
+__global__ void __launch_bounds__(umma::NTHREADS, 1)
+k_step_umma_long(const UWork *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
+                 const unsigned char *__restrict__ planes, Bufs bufs) {
+  using namespace umma;
+  using LY = LongLayout<TN>;
+  constexpr int NSTAGE = LY::NSTAGE;
+  extern __shared__ unsigned char smem_raw[];
+  const uint32_t raw_s = smem_u32(smem_raw);
+  const uint32_t base_s = (raw_s + 1023u) & ~1023u;
+  unsigned char *sm = smem_raw + (base_s - raw_s);
+  unsigned char *rec0 = sm + LY::OFF_REC;
+  const uint32_t bar0 = base_s + LY::OFF_BAR;
+  uint32_t *misc = reinterpret_cast<uint32_t *>(sm + LY::OFF_MISC);  // [0] tmem, [1] abort
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(misc + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  auto bar = [&](int i) { return bar0 + 8u * (uint32_t)i; };
+
+  if (warp == MMA_WARP) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(misc)),
+                 "r"(LY::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < 2; ++s) {
+      bar_init(bar(BAR_T_FULL + s), 1);
+      bar_init(bar(BAR_T_EMPTY + s), EPI_WARPS * 32);
+      bar_init(bar(BAR_E_FULL + s), 1);
+      bar_init(bar(BAR_E_EMPTY + s), EPI_WARPS * 32);
+    }
+    bar_init(bar(LY::BAR_DONE), 1);
+    for (int s = 0; s < NSTAGE; ++s) {
+      bar_init(bar(LY::BAR_S_FULL + s), 1);
+      bar_init(bar(LY::BAR_S_EMPTY + s), 1);
+    }
+    misc[1] = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = misc[0];
+
+  if (warp == PROD_WARP) {
+    // ================================================================ producer
+    if (lane == 0) {
+      uint32_t t = 0, q = 0;
+      uint32_t nS[NSTAGE], nE[2] = {0u, 0u};  // phases armed per barrier (for the drain)
+#pragma unroll
+      for (int s = 0; s < NSTAGE; ++s) nS[s] = 0;
+      bool ok = true;
+      for (int64_t w = blockIdx.x; ok && w < nwork; w += gridDim.x) {
+        if (*abort_flag) break;
+        const UWork wk = work[w];
+        const Group g = groups[wk.group];
+        const int K = wk.nrt_k >> 8, npass = (K + KMAX - 1) / KMAX;
+        const int akb = 4 * tile_rows8(g.M, wk.m0) * ROW_BYTES;
+        const unsigned char *arec = planes + wk.a_rec, *brec = planes + wk.b_rec;
+        for (int j = 0; j < npass; ++j, ++t) {
+          const int kc = min(KMAX, K - j * KMAX), nkb = (kc + KB_SLOTS - 1) / KB_SLOTS;
+          const uint32_t b = t & 1, u = t >> 1;
+          if (!(ok = wait_bounded(bar(BAR_E_EMPTY + b), (u & 1) ^ 1, abort_flag, 2))) break;
+          unsigned char *rec = rec0 + b * LY::REC_BYTES;
+          const uint32_t rec_s = base_s + LY::OFF_REC + b * LY::REC_BYTES;
+          int *info = reinterpret_cast<int *>(rec + LY::REC_INFO);
+          info[0] = wk.m0;
+          info[1] = g.M;
+          info[2] = g.cbuf;
+          info[3] = j == npass - 1;
+          bar_arrive_tx(bar(BAR_E_FULL + b), (uint32_t)(TM * 4 + TN * 20));
+          bulk_g2s(rec_s + LY::REC_EA, arec + (int64_t)nkb * akb, TM * 4, bar(BAR_E_FULL + b));
+          bulk_g2s(rec_s + LY::REC_EB, brec + (int64_t)nkb * LY::B_KB, TN * 20, bar(BAR_E_FULL + b));
+          ++nE[b];
+          for (int kb = 0; kb < nkb; ++kb, ++q) {
+            const uint32_t s = q % NSTAGE, use = q / NSTAGE;
+            if (!(ok = wait_bounded(bar(LY::BAR_S_EMPTY + s), (use & 1) ^ 1, abort_flag, 3))) break;
+            const uint32_t st = base_s + LY::OFF_S + s * LY::STAGE;
+            bar_arrive_tx(bar(LY::BAR_S_FULL + s), (uint32_t)(akb + LY::B_KB));
+            bulk_g2s(st, arec + (int64_t)kb * akb, (uint32_t)akb, bar(LY::BAR_S_FULL + s));
+            bulk_g2s(st + A_STAGE, brec + (int64_t)kb * LY::B_KB, LY::B_KB, bar(LY::BAR_S_FULL + s));
+            ++nS[s];
+          }
+          if (!ok) break;
+          arec += (int64_t)nkb * akb + TM * 4;
+          brec += (int64_t)nkb * LY::B_KB + TN * 20;
+        }
+      }
+      // drain: every bulk copy issued has landed before the CTA may exit
+#pragma unroll
+      for (int s = 0; s < NSTAGE; ++s)
+        if (nS[s]) wait_bounded(bar(LY::BAR_S_FULL + s), (nS[s] - 1) & 1, abort_flag, 10, false);
+      for (int b = 0; b < 2; ++b)
+        if (nE[b]) wait_bounded(bar(BAR_E_FULL + b), (nE[b] - 1) & 1, abort_flag, 11, false);
+    }
+    __syncwarp();
+  } else if (warp == MMA_WARP) {
+    // ====================================================================== MMA
+    if (lane == 0) {
+      uint32_t q = 0, t = 0;
+      for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+        if (*abort_flag) break;
+        const UWork wk = work[w];
+        const int K = wk.nrt_k >> 8, npass = (K + KMAX - 1) / KMAX;
+        const uint32_t PL = (uint32_t)(tile_rows8(groups[wk.group].M, wk.m0) * ROW_BYTES);
+        for (int j = 0; j < npass; ++j, ++t) {
+          const int kc = min(KMAX, K - j * KMAX), nkb = (kc + KB_SLOTS - 1) / KB_SLOTS;
+          const uint32_t b = t & 1, u = t >> 1;
+          wait_bounded(bar(BAR_T_EMPTY + b), (u & 1) ^ 1, abort_flag, 5);
+          tc_fence_after();
+          for (int kb = 0; kb < nkb; ++kb, ++q) {
+            const uint32_t s = q % NSTAGE, use = q / NSTAGE;
+            const bool ok = wait_bounded(bar(LY::BAR_S_FULL + s), use & 1, abort_flag, 6);
+            tc_fence_after();
+            if (ok && !*abort_flag) {
+              const uint32_t a_s = base_s + LY::OFF_S + s * LY::STAGE, b_s = a_s + A_STAGE;
+#pragma unroll
+              for (int k16 = 0; k16 < 2; ++k16) {
+                if (kb * KB_SLOTS + k16 * 16 >= kc) break;
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                  const uint32_t d = tmem + b * (4 * TN) + a * TN;
+                  mma(d, sdesc(a_s + a * PL + k16 * 32), sdesc(b_s + k16 * 32), idesc((4 - a) * TN),
+                      (kb | k16 | a) != 0);
+                }
+              }
+            }
+            commit(bar(LY::BAR_S_EMPTY + s));
+          }
+          commit(bar(BAR_T_FULL + b));
+        }
+      }
+      commit(bar(LY::BAR_DONE));
+    }
+    __syncwarp();
+  } else {
+    // ================================================================= epilogue
+    // warp w reads TMEM lanes 32(w%4).. and every other 8-column chunk (from
+    // column 8(w/4)); its TN/2 sums stay in registers over the passes
+    const int quarter = warp & 3, half = warp >> 2;
+    const int e = quarter * 32 + lane;
+    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+    double *stg = reinterpret_cast<double *>(sm + LY::OFF_STG) + warp * 256;
+    uint32_t t = 0;
+    for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+      if (role_sync_or(2, EPI_WARPS * 32, *abort_flag != 0)) break;
+      const UWork wk = work[w];
+      const int K = wk.nrt_k >> 8, npass = (K + KMAX - 1) / KMAX;
+      double acc[TN / 2];
+#pragma unroll
+      for (int c = 0; c < TN / 2; ++c) acc[c] = 0.0;
+      for (int j = 0; j < npass; ++j, ++t) {
+        const uint32_t b = t & 1, u = t >> 1;
+        const bool ok_rec = wait_bounded(bar(BAR_E_FULL + b), u & 1, abort_flag, 7);
+        const unsigned char *rec = rec0 + b * LY::REC_BYTES;
+        const int *info = reinterpret_cast<const int *>(rec + LY::REC_INFO);
+        const int ea = reinterpret_cast<const int *>(rec + LY::REC_EA)[e];
+        const int *eb = reinterpret_cast<const int *>(rec + LY::REC_EB);
+        const bool ok_acc = wait_bounded(bar(BAR_T_FULL + b), u & 1, abort_flag, 8);
+        const bool ok = __all_sync(0xffffffffu, ok_rec && ok_acc && *abort_flag == 0);
+        tc_fence_after();
+#pragma unroll
+        for (int jc = 0; jc < TN / 16; ++jc) {
+          const int c0 = 8 * half + 16 * jc;
+          uint32_t v[4][8];
+          const uint32_t ta = tmem + lane_base + b * (4 * TN) + c0;
+#pragma unroll
+          for (int l = 0; l < 4; ++l) tmem_ld8(ta + l * TN, v[l]);
+          tmem_ld_wait();
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const long long S = (lvl(v[0][i]) << 24) + (lvl(v[1][i]) << 16) + (lvl(v[2][i]) << 8) + lvl(v[3][i]);
+            acc[8 * jc + i] += scaled_int_to_double(S, ea + eb[c0 + i] - BIAS);
+          }
+        }
+        // the last pass stores the sums (its tile record has the column map)
+        if (ok && info[3]) {
+          double *out = bufs.p[info[2]];
+          const long long *cb = reinterpret_cast<const long long *>(rec + LY::REC_CB);
+          const long long *rs = reinterpret_cast<const long long *>(rec + LY::REC_RS);
+#pragma unroll
+          for (int jc = 0; jc < TN / 16; ++jc) {
+            const int c0 = 8 * half + 16 * jc;
+            store_chunk(stg, acc + 8 * jc, lane, info[0] + quarter * 32, info[1], cb + c0, rs + c0, out, true);
+          }
+        }
+        tc_fence_before();
+        bar_arrive(bar(BAR_T_EMPTY + b));
+        bar_arrive(bar(BAR_E_EMPTY + b));
+      }
+    }
+  }
+
+  // ---- teardown: wait for the MMA issuer's last commit, release TMEM
+  tc_fence_before();
+  __syncthreads();
+  if (warp == MMA_WARP) {
+    tc_fence_after();
+    if (lane == 0) wait_bounded(bar(LY::BAR_DONE), 0, abort_flag, 9, false);
+    __syncwarp();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(LY::TMEM_COLS)
+                 : "memory");
+  }
+}
+
+template <int TN>
+static int launch_umma_long_t(const UWork *work, int64_t nwork, const Step &s, const Bufs &b,
+                              const unsigned char *planes, int nsm, void *stream) {
+  if (nwork == 0) return ZMPO_OK;
+  constexpr int smem = LongLayout<TN>::SMEM;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_step_umma_long<TN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return record_cuda_error("k_step_umma_long: shared memory attribute", (int)e);
+    attr = true;
+  }
+  const int grid = (int)(nwork < nsm ? nwork : nsm);
+  k_step_umma_long<TN><<<grid, umma::NTHREADS, smem, (cudaStream_t)stream>>>(work, nwork, s.d_groups, planes, b);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? ZMPO_OK : record_cuda_error("k_step_umma_long", (int)e);
 }
 
 template <int TN>
@@ -751,6 +1063,9 @@ int launch_step_umma(const Step &s, const Bufs &b, unsigned char *planes, void *
     if (e != cudaSuccess) return record_cuda_error("k_prep_b", (int)e);
   }
   int rc;
+  if ((rc = launch_umma_long_t<64>(s.d_work_ul[2], s.nwork_ul[2], s, b, planes, nsm, stream))) return rc;
+  if ((rc = launch_umma_long_t<32>(s.d_work_ul[1], s.nwork_ul[1], s, b, planes, nsm, stream))) return rc;
+  if ((rc = launch_umma_long_t<16>(s.d_work_ul[0], s.nwork_ul[0], s, b, planes, nsm, stream))) return rc;
   if ((rc = launch_umma_t<64>(s.d_work_um[2], s.nwork_um[2], s, b, planes, nsm, stream))) return rc;
   if ((rc = launch_umma_t<32>(s.d_work_um[1], s.nwork_um[1], s, b, planes, nsm, stream))) return rc;
   return launch_umma_t<16>(s.d_work_um[0], s.nwork_um[0], s, b, planes, nsm, stream);

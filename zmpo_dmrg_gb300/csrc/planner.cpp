@@ -395,6 +395,7 @@ static void rowmajor_strides(const int64_t *d, int r, int64_t *st) {
 
 // Expand all output works of one launch into groups / segments.
 constexpr int64_t kSplitK = 2048;
+static_assert(kSplitK == kUmmaLongMaxK, "a split-K part is one long tcgen05 item");
 
 // Column-block groups: output blocks of one step whose groups read the same A
 // rows (same output layout, same row-leg sectors, same A tensor and term) are
@@ -803,6 +804,8 @@ constexpr int kBresMaxK = 256, kBresRun = 16;
 // reduction sums them in order.
 
 static void split_long_groups(Step &st) {
+  if (st.split_done) return;
+  st.split_done = true;
   std::vector<Group> out;
   std::vector<Seg> segs;
   out.reserve(st.groups.size());
@@ -878,7 +881,7 @@ static void split_long_groups(Step &st) {
 // 4-slice path: the whole K in one exact pass, at least half a row tile.
 // ZMPO_SPLIT_LEGACY=1 in the environment keeps every group on the mma.sync
 // kernels (for comparisons).
-constexpr int kUmmaMinM = 64, kUmmaRun = 16;
+constexpr int kUmmaMinM = 64;
 static bool umma_enabled() {
   static const bool on = [] {
     const char *v = std::getenv("ZMPO_SPLIT_LEGACY");
@@ -887,16 +890,24 @@ static bool umma_enabled() {
   return on;
 }
 
-// Split-K parts (written to the partial-sum scratch) stay on the chunked
-// kernels, so the one-pass set is the same before and after the split.
+// The tcgen05 routes of the split path: one-pass groups (the whole K in one
+// exact pass, at least 64 rows, not a split-K part) and long groups (K up to
+// kUmmaLongMaxK in passes of kUmmaMaxK slots: groups with a longer K than one
+// pass, and every split-K part).
 static bool umma_one_pass(const Group &G, int64_t ktot) {
   return umma_enabled() && ktot >= 1 && ktot <= kUmmaMaxK && G.M >= kUmmaMinM && G.N >= 1 &&
          G.cbuf != kPartialBuf;
 }
+static bool umma_long(const Group &G, int64_t ktot) {
+  return umma_enabled() && ktot >= 1 && ktot <= kUmmaLongMaxK && G.M >= 1 && G.N >= 1 &&
+         (ktot > kUmmaMaxK || G.cbuf == kPartialBuf);
+}
 
-// column tiles of a one-pass group: full 64-column tiles, then the smallest
-// of 16 / 32 / 64 that holds the rest
+// column tiles: full 64-column tiles, then the smallest of 16 / 32 / 64 that
+// holds the rest
 static int umma_tn(int rem) { return rem >= 64 ? 64 : (rem <= 16 ? 16 : (rem <= 32 ? 32 : 64)); }
+static int umma_ti(int tn) { return tn == 16 ? 0 : (tn == 32 ? 1 : 2); }
+static int umma_tm8(int M, int m0) { return (std::min(kUmmaTM, M - m0) + 7) & ~7; }
 
 static int64_t group_k(const Step &st, const Group &G) {
   int64_t k = 0;
@@ -904,29 +915,84 @@ static int64_t group_k(const Step &st, const Group &G) {
   return k;
 }
 
-// Bytes of the prepared digit planes of a step's one-pass groups: every A
-// tile, then (from *b0, 256-byte aligned) every B tile.
-static int64_t umma_plane_bytes(const Step &st, int64_t *b0) {
-  int64_t a = 0, b = 0;
-  for (const Group &G : st.groups) {
-    const int64_t k = group_k(st, G);
-    if (!umma_one_pass(G, k)) continue;
-    const int nkb = (int)((k + kUmmaKB - 1) / kUmmaKB);
-    const int nrt = (G.M + kUmmaTM - 1) / kUmmaTM;
-    a += nrt * umma_a_tile_bytes(nkb);
-    for (int n0 = 0; n0 < G.N;) {
-      const int tn = umma_tn(G.N - n0);
-      b += umma_b_tile_bytes(nkb, tn);
-      n0 += tn;
+// Records and work items of the tcgen05 groups of a step.  With make =
+// false only the byte totals are counted (the plan-time estimate).
+struct UmmaLists {
+  bool make = true;
+  std::vector<PrepA> pa;
+  std::vector<PrepB> pb;            // rec relative to the B part until placed
+  std::vector<UWork> w1[3], wl[3];  // one-pass / long items by column tile
+  int64_t abytes = 0, bbytes = 0;
+  double macs = 0.0;                // multiply-adds the MMAs issue (x10 digit products)
+};
+
+constexpr int kUmmaRunMax = 16;     // row tiles of a one-pass work item
+
+static void umma_add_group(UmmaLists &L, int g, const Group &G, int64_t K) {
+  const bool one = umma_one_pass(G, K);
+  if (!one && !umma_long(G, K)) return;
+  const int nrt = (G.M + kUmmaTM - 1) / kUmmaTM;
+  const int npass = (int)((K + kUmmaMaxK - 1) / kUmmaMaxK);
+  const double k16 = (double)((K + 15) / 16 * 16);
+  // A records: per row tile, per pass (one pass for one-pass groups)
+  std::vector<int64_t> arec(nrt);
+  for (int r = 0; r < nrt; ++r) {
+    const int m0 = r * kUmmaTM, tm8 = umma_tm8(G.M, m0);
+    arec[r] = L.abytes;
+    for (int j = 0; j < npass; ++j) {
+      const int k0 = j * kUmmaMaxK, kc = (int)std::min<int64_t>(kUmmaMaxK, K - k0);
+      if (L.make) L.pa.push_back({L.abytes, g, m0, k0, kc});
+      L.abytes += umma_a_rec_bytes((kc + kUmmaKB - 1) / kUmmaKB, tm8);
     }
   }
-  a = (a + 255) & ~int64_t(255);
-  if (b0) *b0 = a;
-  return a + b;
+  const int nruns = (nrt + kUmmaRunMax - 1) / kUmmaRunMax;
+  const int len = (nrt + nruns - 1) / nruns;
+  for (int n0 = 0; n0 < G.N;) {
+    const int tn = umma_tn(G.N - n0), ti = umma_ti(tn);
+    const int64_t brec = L.bbytes;
+    for (int j = 0; j < npass; ++j) {
+      const int k0 = j * kUmmaMaxK, kc = (int)std::min<int64_t>(kUmmaMaxK, K - k0);
+      if (L.make) L.pb.push_back({L.bbytes, g, n0, tn, k0, kc, 0});
+      L.bbytes += umma_b_rec_bytes((kc + kUmmaKB - 1) / kUmmaKB, tn);
+    }
+    if (L.make) {
+      if (one) {
+        for (int r = 0; r < nrt; r += len)
+          L.w1[ti].push_back({arec[r], brec, g, r * kUmmaTM, std::min(len, nrt - r) | (int32_t)(K << 8), 0});
+      } else {
+        for (int r = 0; r < nrt; ++r) L.wl[ti].push_back({arec[r], brec, g, r * kUmmaTM, 1 | (int32_t)(K << 8), 0});
+      }
+    }
+    L.macs += (double)nrt * kUmmaTM * tn * k16;
+    n0 += tn;
+  }
 }
 
-// Sigma and renorm plans: one plane region at the end of the workspace,
-// shared by the plan's steps (they run one after another).
+// Bytes of the prepared records of a step: every A record, then (from *b0,
+// 256-byte aligned) every B record.  Before the split-K parts exist, a group
+// longer than kSplitK counts as its parts (kSplitK slots each, the rest last).
+static int64_t umma_plane_bytes(const Step &st, int64_t *b0) {
+  UmmaLists L;
+  L.make = false;
+  for (const Group &G : st.groups) {
+    const int64_t k = group_k(st, G);
+    if (!st.split_done && k > kSplitK && G.M > 0 && G.N > 0) {
+      Group part = G;
+      part.cbuf = kPartialBuf;
+      for (int64_t k0 = 0; k0 < k; k0 += kSplitK) umma_add_group(L, 0, part, std::min<int64_t>(kSplitK, k - k0));
+      continue;
+    }
+    umma_add_group(L, 0, G, k);
+  }
+  const int64_t a = (L.abytes + 255) & ~int64_t(255);
+  if (b0) *b0 = a;
+  return L.abytes + L.bbytes > 0 ? a + L.bbytes : 0;
+}
+
+// Sigma plans: one plane region at the end of the workspace, shared by the
+// plan's steps (they run one after another).  Other plans (renormalisation,
+// which runs in FP64 or the 7-slice emulation, and contractions) get a
+// step-owned buffer at their first split-precision run.
 static void reserve_plane_region(Plan *P) {
   int64_t need = 0;
   for (auto &st : P->steps) {
@@ -943,10 +1009,7 @@ static int upload_step(Step &st) {
   if (st.uploaded) return ZMPO_OK;
   split_long_groups(st);
   std::vector<Work> w64, wtc[3][4], wtc4[3][4], wtcb[2];
-  std::vector<UWork> wum[3];
-  std::vector<PrepA> prep_a;
-  std::vector<PrepB> prep_b;
-  int64_t abytes = 0, bbytes = 0;
+  UmmaLists UL;
   // order groups by cost (longest first) for load balance
   std::vector<int> order(st.groups.size());
   std::iota(order.begin(), order.end(), 0);
@@ -962,7 +1025,6 @@ static int upload_step(Step &st) {
   }
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
   st.mma_macs[0] = st.mma_macs[1] = st.mma_macs[2] = 0.0;
-  const bool um = umma_enabled();
   for (int g : order) {
     const Group &G = st.groups[g];
     const double k16 = (double)((ktot[g] + 15) / 16 * 16);
@@ -971,35 +1033,11 @@ static int upload_step(Step &st) {
         w64.push_back({g, m0, n0, 0});
         st.mma_macs[0] += (double)kTileFP64M * kTileFP64N * k16;
       }
-    // one-pass tensor-core items: every row tile of 128 and every column
-    // tile (umma_tn) is cut once into the plane buffer by a prepare item;
-    // work items = one column tile and a run of at most kUmmaRun row tiles
-    // (runs balanced)
-    const bool one_pass = um && umma_one_pass(G, ktot[g]);
-    if (one_pass) {
-      const int K = (int)ktot[g];
-      const int nkb = (K + kUmmaKB - 1) / kUmmaKB;
-      const int nrt = (G.M + kUmmaTM - 1) / kUmmaTM;
-      const int nruns = (nrt + kUmmaRun - 1) / kUmmaRun;
-      const int len = (nrt + nruns - 1) / nruns;
-      const int64_t a0 = abytes;
-      for (int r = 0; r < nrt; ++r) {
-        prep_a.push_back({abytes, g, r * kUmmaTM});
-        abytes += umma_a_tile_bytes(nkb);
-      }
-      for (int n0 = 0; n0 < G.N;) {
-        const int tn = umma_tn(G.N - n0);
-        const int ti = tn == 16 ? 0 : (tn == 32 ? 1 : 2);
-        prep_b.push_back({bbytes, g, n0, tn, 0});  // B offsets are relative until the A total is known
-        for (int r = 0; r < nrt; r += len) {
-          const int n = std::min(len, nrt - r);
-          wum[ti].push_back({a0 + r * umma_a_tile_bytes(nkb), bbytes, g, r * kUmmaTM, n | (K << 8), 0});
-        }
-        bbytes += umma_b_tile_bytes(nkb, tn);
-        st.mma_macs[1] += (double)nrt * kUmmaTM * tn * k16;
-        n0 += tn;
-      }
-    }
+    // tcgen05 groups (records cut once per launch by the prepare kernels)
+    const double macs0 = UL.macs;
+    umma_add_group(UL, g, G, ktot[g]);
+    const bool routed = UL.macs != macs0;
+    st.mma_macs[1] += UL.macs - macs0;
     // Tensor-core tiles.  Columns: full pieces of the widest tile, then one
     // narrower tile for the rest (the smallest of 8/16/32/64 that holds it),
     // so a group of 74 columns takes 64 + 16 instead of 64 + 64.  64-column
@@ -1027,7 +1065,7 @@ static int upload_step(Step &st) {
       size_t nfull = 0;
       if (bres >= 0 && G.nseg <= 32 && ktot[g] <= kBresMaxK)
         while (nfull < rows.size() && rows[nfull].second == hmax) ++nfull;
-      if (nfull < 2 || one_pass) nfull = 0;
+      if (nfull < 2 || routed) nfull = 0;
       if (nfull) {
         const int nruns = (int)((nfull + kBresRun - 1) / kBresRun);
         const int len = (int)((nfull + nruns - 1) / nruns);
@@ -1037,9 +1075,9 @@ static int upload_step(Step &st) {
       for (size_t r = 0; r < rows.size(); ++r) {
         const int tmi = rows[r].second == 32 ? 0 : (rows[r].second == 64 ? 1 : 2);
         wtc[tmi][tni].push_back({g, rows[r].first, n0, 0});
-        if (r >= nfull && !one_pass) wtc4[tmi][tni].push_back({g, rows[r].first, n0, 0});
+        if (r >= nfull && !routed) wtc4[tmi][tni].push_back({g, rows[r].first, n0, 0});
         const double macs = (double)rows[r].second * tn * k16;
-        if (!one_pass) st.mma_macs[1] += macs;  // the same tiles, B-resident or not
+        if (!routed) st.mma_macs[1] += macs;  // the same tiles, B-resident or not
         st.mma_macs[2] += macs;
       }
       n0 += tn;
@@ -1052,22 +1090,27 @@ static int upload_step(Step &st) {
       st.nwork_tc4[i][j] = (int64_t)wtc4[i][j].size();
     }
   for (int i = 0; i < 2; ++i) st.nwork_tcb[i] = (int64_t)wtcb[i].size();
-  // plane buffer: A tiles, then B tiles from the 256-aligned A total (the
-  // layout umma_plane_bytes sizes)
+  // plane buffer: A records, then B records from the 256-aligned A total
+  // (the layout umma_plane_bytes sizes)
   {
-    const int64_t b0 = (abytes + 255) & ~int64_t(255);
-    for (auto &p : prep_b) p.rec += b0;
-    for (int i = 0; i < 3; ++i)
-      for (auto &w : wum[i]) w.b_rec += b0;
-    const int64_t total = (abytes + bbytes) > 0 ? b0 + bbytes : 0;
+    const int64_t b0 = (UL.abytes + 255) & ~int64_t(255);
+    for (auto &p : UL.pb) p.rec += b0;
+    for (int i = 0; i < 3; ++i) {
+      for (auto &w : UL.w1[i]) w.b_rec += b0;
+      for (auto &w : UL.wl[i]) w.b_rec += b0;
+    }
+    const int64_t total = (UL.abytes + UL.bbytes) > 0 ? b0 + UL.bbytes : 0;
     if (st.plane_ws_off >= 0 && (total != st.plane_bytes || b0 != st.plane_b0))
       return fail(ZMPO_E_ARG, "upload: prepared-plane size differs from the plan's reservation");
     st.plane_bytes = total;
     st.plane_b0 = b0;
   }
-  st.nprep_a = (int64_t)prep_a.size();
-  st.nprep_b = (int64_t)prep_b.size();
-  for (int i = 0; i < 3; ++i) st.nwork_um[i] = (int64_t)wum[i].size();
+  st.nprep_a = (int64_t)UL.pa.size();
+  st.nprep_b = (int64_t)UL.pb.size();
+  for (int i = 0; i < 3; ++i) {
+    st.nwork_um[i] = (int64_t)UL.w1[i].size();
+    st.nwork_ul[i] = (int64_t)UL.wl[i].size();
+  }
   auto up = [](auto **dptr, const auto &v) -> cudaError_t {
     using T = typename std::remove_reference<decltype(v)>::type::value_type;
     if (v.empty()) {
@@ -1089,11 +1132,12 @@ static int upload_step(Step &st) {
       CUDA_TRY(up(&st.d_work_tc4[i][j], wtc4[i][j]));
     }
   for (int i = 0; i < 2; ++i) CUDA_TRY(up(&st.d_work_tcb[i], wtcb[i]));
-  for (int i = 0; i < 3; ++i) CUDA_TRY(up(&st.d_work_um[i], wum[i]));
-  CUDA_TRY(up(&st.d_prep_a, prep_a));
-  CUDA_TRY(up(&st.d_prep_b, prep_b));
-  if (st.plane_ws_off < 0 && st.plane_bytes > 0)
-    CUDA_TRY(cudaMalloc((void **)&st.d_planes_own, st.plane_bytes));
+  for (int i = 0; i < 3; ++i) {
+    CUDA_TRY(up(&st.d_work_um[i], UL.w1[i]));
+    CUDA_TRY(up(&st.d_work_ul[i], UL.wl[i]));
+  }
+  CUDA_TRY(up(&st.d_prep_a, UL.pa));
+  CUDA_TRY(up(&st.d_prep_b, UL.pb));
   CUDA_TRY(up(&st.d_reds, st.reds));
   if (st.part_elems > 0) CUDA_TRY(cudaMalloc((void **)&st.d_part, st.part_elems * sizeof(double)));
   // keep the host mirror of groups (sizes) but free the bulky segment copy
@@ -1126,7 +1170,9 @@ static void free_step(Step &st) {
   }
   for (int i = 0; i < 3; ++i) {
     cudaFree(st.d_work_um[i]);
+    cudaFree(st.d_work_ul[i]);
     st.d_work_um[i] = nullptr;
+    st.d_work_ul[i] = nullptr;
   }
   cudaFree(st.d_prep_a);
   cudaFree(st.d_prep_b);
@@ -1177,6 +1223,8 @@ static int run_step(Step &st, const Bufs &b, int precision, void *stream) {
   }
   Bufs bb = b;
   bb.p[kPartialBuf] = st.d_part;
+  if (precision == ZMPO_PREC_SPLIT && st.plane_bytes > 0 && st.plane_ws_off < 0 && !st.d_planes_own)
+    CUDA_TRY(cudaMalloc((void **)&st.d_planes_own, st.plane_bytes));
   if (precision == ZMPO_PREC_FP64)
     rc = launch_step_fp64(st, bb, stream);
   else if (precision == ZMPO_PREC_SPLIT)
@@ -1733,8 +1781,10 @@ int zmpo_plan_kernel_count(zmpo_engine *e, int plan_id, int precision, int *coun
       const bool s4 = precision == ZMPO_PREC_SPLIT;
       for (int a = 0; a < 3; ++a)
         for (int c = 0; c < 4; ++c) n += (s4 ? s.nwork_tc4[a][c] : s.nwork_tc[a][c]) > 0;
-      if (s4) n += (s.nwork_tcb[0] > 0) + (s.nwork_tcb[1] > 0) + (s.nwork_um[0] > 0) + (s.nwork_um[1] > 0) +
-                   (s.nwork_um[2] > 0);
+      if (s4) {
+        n += (s.nwork_tcb[0] > 0) + (s.nwork_tcb[1] > 0) + (s.nprep_a > 0) + (s.nprep_b > 0);
+        for (int i = 0; i < 3; ++i) n += (s.nwork_um[i] > 0) + (s.nwork_ul[i] > 0);
+      }
     }
     n += s.red_elems > 0;
   }
@@ -1923,7 +1973,6 @@ int zmpo_renorm_plan(zmpo_engine *e, const zmpo_renorm_desc *d, int *plan_id) {
       P->exec_flops += st.flops;
       P->ntasks += st.ntasks;
     }
-    reserve_plane_region(P.get());
   }
   e->plans.push_back(std::move(P));
   {
