@@ -163,6 +163,16 @@ int zmpo_plan_mma_macs(zmpo_engine *e, int plan_id, int precision, int nmax, dou
 int zmpo_sigma(zmpo_engine *e, int plan_id, const double *d_L,
                const double *d_R, const double *d_W, const double *d_x,
                double *d_y, void *d_workspace, int precision, void *stream);
+/* Lets the next zmpo_sigma call of this plan (split precision) skip
+ * re-cutting the tensor-core digit planes of the operands that stay fixed
+ * during a Davidson solve (the environments L, R and the MPO W): they are
+ * reused from the plan's previous split-precision call when that call had
+ * the same d_L, d_R, d_W and d_workspace and no other sigma plan ran on
+ * d_workspace since; otherwise the call cuts them as usual.  The caller
+ * guarantees that the contents of d_L, d_R and d_W did not change since that
+ * call.  Applies to the next call only.  No reference counterpart (the
+ * reference has no prepared operands). */
+int zmpo_sigma_reuse_kept(zmpo_engine *e, int plan_id, int reuse);
 /* Davidson preconditioner diag(H) in the packed psi order (replaces
  * HDiagQt, mpo_dmrg_kernelQt.py:30-127). */
 int zmpo_hdiag(zmpo_engine *e, int plan_id, const double *d_L,

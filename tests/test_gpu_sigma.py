@@ -181,3 +181,34 @@ def test_sigma_term_batches(gpu, precision):
     tol = 1e-12 if precision == "fp64" else 1e-8
     assert rel(y2, y1) < tol
     assert rel(d2, d1) < 1e-12
+
+
+def test_sigma_reuses_kept_records_only_while_operands_are_unchanged(gpu):
+    """Within a Davidson solve the environments and the MPO stay fixed: the
+    second split H.psi of a plan reuses the digit planes cut from them on the
+    first call and gives the identical vector.  An in-place change of an
+    environment makes the next call cut them again (the result equals that
+    of a fresh plan on the changed environments)."""
+    import torch
+    from zmpo_dmrg_gb300.mpo_dmrg_kernel import _sigma_plan
+    P = random_problem(**BRES_CASE)
+    m = P.p
+    info = [m, P.isite, 2, m.flst, 'L', True]
+    plan = _sigma_plan(info)
+    x = torch.from_numpy(numpy.random.default_rng(21).standard_normal(P.ndim0)).cuda()
+    y1, y2, y3 = (torch.empty_like(x) for _ in range(3))
+    plan.run(m, x, y1, "split")
+    assert plan._kept_token is not None
+    plan.run(m, x, y2, "split")
+    assert torch.equal(y1, y2)
+    fL = m.flst[0][0]
+    fL.buf.mul_(0.5)                      # in place: the version counter moves
+    plan.run(m, x, y3, "split")
+    plan.rebind(fL, m.flst[0][1])         # forgets the kept records
+    y4 = torch.empty_like(x)
+    plan.run(m, x, y4, "split")
+    assert torch.equal(y3, y4)
+    assert not torch.equal(y3, y1)
+    ref = oracle_sigma(P, x.cpu().numpy())  # the oracle side was not scaled
+    assert rel(2.0 * y3.cpu().numpy(), ref) < 1e-8
+    fL.buf.mul_(2.0)

@@ -138,8 +138,14 @@ struct Step {
   UWork *d_work_ul[3] = {};         // long items (passes), by column tile 16 / 32 / 64
   int64_t nwork_ul[3] = {};
   bool split_done = false;          // split-K parts made (split_long_groups)
-  int64_t plane_bytes = 0;          // A tiles, then B tiles (from plane_b0)
-  int64_t plane_b0 = 0;
+  int64_t nprep_a_kept = 0, nprep_b_kept = 0;  // the first items cut kept records
+  // plane buffer of the step: a kept area (records of the operands in
+  // keep_bufs, which stay fixed between calls) and a per-call area, byte
+  // offsets from the buffer's base
+  uint32_t keep_bufs = 0;
+  int64_t plane_keep_off = 0, plane_keep_bytes = 0;
+  int64_t plane_call_off = 0, plane_call_bytes = 0;
+  int64_t plane_bytes = 0;          // the whole buffer
   // where the plane buffer lives: a byte offset into the workspace buffer
   // (sigma plans; every step of a plan shares one region), or step-owned
   // memory (plane_ws_off < 0: renormalisation and contraction plans,
@@ -178,12 +184,12 @@ inline unsigned char *step_planes(const Step &s, const Bufs &b) {
 
 // Launchers (kernels.cu)
 int launch_step_fp64(const Step &s, const Bufs &b, void *stream);
-int launch_step_split(const Step &s, const Bufs &b, int nslices, void *stream);
+int launch_step_split(const Step &s, const Bufs &b, int nslices, void *stream, bool cut_kept = true);
 int launch_reduce(const Step &s, const Bufs &b, void *stream);
 // tcgen05 one-pass kernels (kernels_umma.cu) and their error word: the
 // prepare kernels cut the step's one-pass operand tiles into `planes`, then
 // the tensor-core kernels multiply them
-int launch_step_umma(const Step &s, const Bufs &b, unsigned char *planes, void *stream);
+int launch_step_umma(const Step &s, const Bufs &b, unsigned char *planes, bool cut_kept, void *stream);
 int umma_device_status(int *code, int reset);
 
 // Diagonal terms for HDiag: out[l, r] += alpha * sum_{a,b,c} Ld[a,l] Wi[a,b]

@@ -764,14 +764,14 @@ static int launch_tc_t(const Work *work, int64_t nwork, const Step &s, const Buf
 }
 
 template <int S>
-static int launch_split_all(const Step &s, const Bufs &b, void *stream) {
+static int launch_split_all(const Step &s, const Bufs &b, void *stream, bool cut_kept) {
   int rc;
   // S = 4: the groups routed to the B-resident kernel are not in the S = 4
   // lists; S = 7 (no B-resident variant) uses the lists of every group
   Work *const(*wl)[4] = S == 4 ? s.d_work_tc4 : s.d_work_tc;
   const int64_t(*nw)[4] = S == 4 ? s.nwork_tc4 : s.nwork_tc;
   if (S == 4) {
-    if ((rc = launch_step_umma(s, b, step_planes(s, b), stream))) return rc;
+    if ((rc = launch_step_umma(s, b, step_planes(s, b), cut_kept, stream))) return rc;
     if ((rc = launch_tcb_t<64, 64>(s.d_work_tcb[0], s.nwork_tcb[0], s, b, stream))) return rc;
     if ((rc = launch_tcb_t<128, 32>(s.d_work_tcb[1], s.nwork_tcb[1], s, b, stream))) return rc;
   }
@@ -788,9 +788,9 @@ static int launch_split_all(const Step &s, const Bufs &b, void *stream) {
   return launch_tc_t<S, 32, 64>(wl[0][3], nw[0][3], s, b, stream);
 }
 
-int launch_step_split(const Step &s, const Bufs &b, int nslices, void *stream) {
-  if (nslices == 4) return launch_split_all<4>(s, b, stream);
-  if (nslices == 7) return launch_split_all<7>(s, b, stream);
+int launch_step_split(const Step &s, const Bufs &b, int nslices, void *stream, bool cut_kept) {
+  if (nslices == 4) return launch_split_all<4>(s, b, stream, cut_kept);
+  if (nslices == 7) return launch_split_all<7>(s, b, stream, true);
   return record_arg_error("unsupported slice count");
 }
 

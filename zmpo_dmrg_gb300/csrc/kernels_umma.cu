@@ -1043,22 +1043,26 @@ static int launch_umma_t(const UWork *work, int64_t nwork, const Step &s, const 
   return e == cudaSuccess ? ZMPO_OK : record_cuda_error("k_step_umma", (int)e);
 }
 
-int launch_step_umma(const Step &s, const Bufs &b, unsigned char *planes, void *stream) {
+int launch_step_umma(const Step &s, const Bufs &b, unsigned char *planes, bool cut_kept, void *stream) {
   if (s.nprep_a == 0 && s.nprep_b == 0) return ZMPO_OK;
-  if (!planes) return record_arg_error("one-pass tensor-core groups without a plane buffer");
+  if (!planes) return record_arg_error("tensor-core groups without a plane buffer");
   int dev = 0, nsm = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const int64_t cap = (int64_t)nsm * 8;
-  if (s.nprep_a) {
-    k_prep_a<<<(int)(s.nprep_a < cap ? s.nprep_a : cap), umma::PREP_THREADS, 0, (cudaStream_t)stream>>>(
-        s.d_prep_a, s.nprep_a, s.d_groups, s.d_segs, b, planes);
+  // the kept records (first items of each list) are cut unless the caller
+  // reuses those of the previous call
+  const int64_t a0 = cut_kept ? 0 : s.nprep_a_kept, b0 = cut_kept ? 0 : s.nprep_b_kept;
+  const int64_t na = s.nprep_a - a0, nb = s.nprep_b - b0;
+  if (na > 0) {
+    k_prep_a<<<(int)(na < cap ? na : cap), umma::PREP_THREADS, 0, (cudaStream_t)stream>>>(
+        s.d_prep_a + a0, na, s.d_groups, s.d_segs, b, planes);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return record_cuda_error("k_prep_a", (int)e);
   }
-  if (s.nprep_b) {
-    k_prep_b<<<(int)(s.nprep_b < cap ? s.nprep_b : cap), umma::PREP_THREADS, 0, (cudaStream_t)stream>>>(
-        s.d_prep_b, s.nprep_b, s.d_groups, s.d_segs, s.d_cblocks, s.d_segb, b, planes);
+  if (nb > 0) {
+    k_prep_b<<<(int)(nb < cap ? nb : cap), umma::PREP_THREADS, 0, (cudaStream_t)stream>>>(
+        s.d_prep_b + b0, nb, s.d_groups, s.d_segs, s.d_cblocks, s.d_segb, b, planes);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return record_cuda_error("k_prep_b", (int)e);
   }

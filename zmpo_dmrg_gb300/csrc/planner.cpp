@@ -212,6 +212,10 @@ struct Plan {
   std::vector<int64_t> out_off;
   int64_t out_total = 0;
   int status = 0;
+  // sigma: kept records (records of the environments and the MPO in the
+  // workspace's plane region) and whether the next call may reuse them
+  bool reuse_next = false, kept_ready = false;
+  const void *kept_ws = nullptr, *kept_L = nullptr, *kept_R = nullptr, *kept_W = nullptr;
   // sigma: the psi size (checked at call time) and HDiag tables
   int64_t ndim0 = 0;
   std::vector<DiagBlock> dblocks;
@@ -231,6 +235,9 @@ struct zmpo_engine {
   std::vector<std::unique_ptr<Layout>> layouts;
   std::vector<std::unique_ptr<Contraction>> contractions;
   std::vector<std::unique_ptr<Plan>> plans;
+  // the sigma plan that last ran on each workspace buffer (a plan's kept
+  // records in a workspace are valid only while no other plan used it)
+  std::unordered_map<const void *, int> ws_user;
 };
 
 namespace zmpo {
@@ -915,22 +922,39 @@ static int64_t group_k(const Step &st, const Group &G) {
   return k;
 }
 
-// Records and work items of the tcgen05 groups of a step.  With make =
-// false only the byte totals are counted (the plan-time estimate).
+// Records and work items of the tcgen05 groups of a step.  A group side
+// (A or B) whose operand buffers are all in the step's keep_bufs mask has
+// its records in the step's kept area (records of operands that stay fixed
+// between calls, which a caller may let the next call reuse), every other
+// side in the per-call area.  Each area holds its A records, then (from a
+// 256-byte aligned offset) its B records.  With make = false only the byte
+// totals are counted (the plan-time estimate).
 struct UmmaLists {
   bool make = true;
-  std::vector<PrepA> pa;
-  std::vector<PrepB> pb;            // rec relative to the B part until placed
-  std::vector<UWork> w1[3], wl[3];  // one-pass / long items by column tile
-  int64_t abytes = 0, bbytes = 0;
-  double macs = 0.0;                // multiply-adds the MMAs issue (x10 digit products)
+  uint32_t keep_bufs = 0;
+  std::vector<PrepA> pa[2];          // [per-call, kept]; rec relative to its part
+  std::vector<PrepB> pb[2];
+  std::vector<UWork> w1[3], wl[3];   // one-pass / long items by column tile; pad = kept sides
+  int64_t abytes[2] = {0, 0}, bbytes[2] = {0, 0};
+  double macs = 0.0;                 // multiply-adds the MMAs issue (x10 digit products)
 };
 
-constexpr int kUmmaRunMax = 16;     // row tiles of a one-pass work item
+constexpr int kUmmaRunMax = 16;      // row tiles of a one-pass work item
 
-static void umma_add_group(UmmaLists &L, int g, const Group &G, int64_t K) {
+static bool side_kept(const Step &st, const Group &G, bool a_side, uint32_t mask) {
+  if (!mask || G.nseg <= 0) return false;
+  for (int i = 0; i < G.nseg; ++i) {
+    const Seg &sg = st.segs[G.seg0 + i];
+    const int buf = a_side ? sg.abuf : sg.bbuf;
+    if (buf < 0 || buf >= 32 || !((mask >> buf) & 1u)) return false;
+  }
+  return true;
+}
+
+static void umma_add_group(UmmaLists &L, int g, const Group &G, int64_t K, bool keep_a, bool keep_b) {
   const bool one = umma_one_pass(G, K);
   if (!one && !umma_long(G, K)) return;
+  const int ka = keep_a ? 1 : 0, kb = keep_b ? 1 : 0;
   const int nrt = (G.M + kUmmaTM - 1) / kUmmaTM;
   const int npass = (int)((K + kUmmaMaxK - 1) / kUmmaMaxK);
   const double k16 = (double)((K + 15) / 16 * 16);
@@ -938,29 +962,31 @@ static void umma_add_group(UmmaLists &L, int g, const Group &G, int64_t K) {
   std::vector<int64_t> arec(nrt);
   for (int r = 0; r < nrt; ++r) {
     const int m0 = r * kUmmaTM, tm8 = umma_tm8(G.M, m0);
-    arec[r] = L.abytes;
+    arec[r] = L.abytes[ka];
     for (int j = 0; j < npass; ++j) {
       const int k0 = j * kUmmaMaxK, kc = (int)std::min<int64_t>(kUmmaMaxK, K - k0);
-      if (L.make) L.pa.push_back({L.abytes, g, m0, k0, kc});
-      L.abytes += umma_a_rec_bytes((kc + kUmmaKB - 1) / kUmmaKB, tm8);
+      if (L.make) L.pa[ka].push_back({L.abytes[ka], g, m0, k0, kc});
+      L.abytes[ka] += umma_a_rec_bytes((kc + kUmmaKB - 1) / kUmmaKB, tm8);
     }
   }
   const int nruns = (nrt + kUmmaRunMax - 1) / kUmmaRunMax;
   const int len = (nrt + nruns - 1) / nruns;
+  const int32_t sides = ka | (kb << 1);
   for (int n0 = 0; n0 < G.N;) {
     const int tn = umma_tn(G.N - n0), ti = umma_ti(tn);
-    const int64_t brec = L.bbytes;
+    const int64_t brec = L.bbytes[kb];
     for (int j = 0; j < npass; ++j) {
       const int k0 = j * kUmmaMaxK, kc = (int)std::min<int64_t>(kUmmaMaxK, K - k0);
-      if (L.make) L.pb.push_back({L.bbytes, g, n0, tn, k0, kc, 0});
-      L.bbytes += umma_b_rec_bytes((kc + kUmmaKB - 1) / kUmmaKB, tn);
+      if (L.make) L.pb[kb].push_back({L.bbytes[kb], g, n0, tn, k0, kc, 0});
+      L.bbytes[kb] += umma_b_rec_bytes((kc + kUmmaKB - 1) / kUmmaKB, tn);
     }
     if (L.make) {
       if (one) {
         for (int r = 0; r < nrt; r += len)
-          L.w1[ti].push_back({arec[r], brec, g, r * kUmmaTM, std::min(len, nrt - r) | (int32_t)(K << 8), 0});
+          L.w1[ti].push_back({arec[r], brec, g, r * kUmmaTM, std::min(len, nrt - r) | (int32_t)(K << 8), sides});
       } else {
-        for (int r = 0; r < nrt; ++r) L.wl[ti].push_back({arec[r], brec, g, r * kUmmaTM, 1 | (int32_t)(K << 8), 0});
+        for (int r = 0; r < nrt; ++r)
+          L.wl[ti].push_back({arec[r], brec, g, r * kUmmaTM, 1 | (int32_t)(K << 8), sides});
       }
     }
     L.macs += (double)nrt * kUmmaTM * tn * k16;
@@ -968,41 +994,61 @@ static void umma_add_group(UmmaLists &L, int g, const Group &G, int64_t K) {
   }
 }
 
-// Bytes of the prepared records of a step: every A record, then (from *b0,
-// 256-byte aligned) every B record.  Before the split-K parts exist, a group
-// longer than kSplitK counts as its parts (kSplitK slots each, the rest last).
-static int64_t umma_plane_bytes(const Step &st, int64_t *b0) {
+static int64_t area_bytes(const UmmaLists &L, int k, int64_t *b0) {
+  const int64_t a = (L.abytes[k] + 255) & ~int64_t(255);
+  if (b0) *b0 = a;
+  return L.abytes[k] + L.bbytes[k] > 0 ? ((a + L.bbytes[k] + 255) & ~int64_t(255)) : 0;
+}
+
+// Bytes of the kept and per-call areas of a step's records.  Before the
+// split-K parts exist, a group longer than kSplitK counts as its parts
+// (kSplitK slots each, the rest last).
+static void umma_plane_bytes(const Step &st, int64_t *keep, int64_t *call) {
   UmmaLists L;
   L.make = false;
   for (const Group &G : st.groups) {
     const int64_t k = group_k(st, G);
+    const bool ka = side_kept(st, G, true, st.keep_bufs), kb = side_kept(st, G, false, st.keep_bufs);
     if (!st.split_done && k > kSplitK && G.M > 0 && G.N > 0) {
       Group part = G;
       part.cbuf = kPartialBuf;
-      for (int64_t k0 = 0; k0 < k; k0 += kSplitK) umma_add_group(L, 0, part, std::min<int64_t>(kSplitK, k - k0));
+      for (int64_t k0 = 0; k0 < k; k0 += kSplitK)
+        umma_add_group(L, 0, part, std::min<int64_t>(kSplitK, k - k0), ka, kb);
       continue;
     }
-    umma_add_group(L, 0, G, k);
+    umma_add_group(L, 0, G, k, ka, kb);
   }
-  const int64_t a = (L.abytes + 255) & ~int64_t(255);
-  if (b0) *b0 = a;
-  return L.abytes + L.bbytes > 0 ? a + L.bbytes : 0;
+  *call = area_bytes(L, 0, nullptr);
+  *keep = area_bytes(L, 1, nullptr);
 }
 
-// Sigma plans: one plane region at the end of the workspace, shared by the
-// plan's steps (they run one after another).  Other plans (renormalisation,
-// which runs in FP64 or the 7-slice emulation, and contractions) get a
-// step-owned buffer at their first split-precision run.
+// Sigma plans: one plane region at the end of the workspace: the kept
+// areas of the steps one after another, then one per-call area shared by
+// the steps (they run one after another).  Records of the environments and
+// the MPO (buffers 0, 1, 2), which stay fixed while a Davidson solve calls
+// the plan, are kept.  Other plans (renormalisation, which runs in FP64 or
+// the 7-slice emulation, and contractions) keep nothing and get a step-owned
+// buffer at their first split-precision run.
 static void reserve_plane_region(Plan *P) {
-  int64_t need = 0;
+  int64_t keep_total = 0, call_max = 0;
   for (auto &st : P->steps) {
-    st.plane_bytes = umma_plane_bytes(st, &st.plane_b0);
-    need = std::max(need, st.plane_bytes);
+    st.keep_bufs = 0x7u;
+    int64_t keep, call;
+    umma_plane_bytes(st, &keep, &call);
+    st.plane_keep_off = keep_total;
+    st.plane_keep_bytes = keep;
+    keep_total += keep;
+    st.plane_call_bytes = call;
+    call_max = std::max(call_max, call);
   }
-  if (need == 0) return;
+  if (keep_total + call_max == 0) return;
   const int64_t off = ((P->ws_elems * (int64_t)sizeof(double)) + 255) & ~int64_t(255);
-  for (auto &st : P->steps) st.plane_ws_off = off;
-  P->ws_elems = ((off + need + 255) & ~int64_t(255)) / (int64_t)sizeof(double);
+  for (auto &st : P->steps) {
+    st.plane_ws_off = off;
+    st.plane_call_off = keep_total;
+    st.plane_bytes = keep_total + call_max;
+  }
+  P->ws_elems = ((off + keep_total + call_max + 255) & ~int64_t(255)) / (int64_t)sizeof(double);
 }
 
 static int upload_step(Step &st) {
@@ -1033,9 +1079,9 @@ static int upload_step(Step &st) {
         w64.push_back({g, m0, n0, 0});
         st.mma_macs[0] += (double)kTileFP64M * kTileFP64N * k16;
       }
-    // tcgen05 groups (records cut once per launch by the prepare kernels)
+    // tcgen05 groups (records cut by the prepare kernels)
     const double macs0 = UL.macs;
-    umma_add_group(UL, g, G, ktot[g]);
+    umma_add_group(UL, g, G, ktot[g], side_kept(st, G, true, st.keep_bufs), side_kept(st, G, false, st.keep_bufs));
     const bool routed = UL.macs != macs0;
     st.mma_macs[1] += UL.macs - macs0;
     // Tensor-core tiles.  Columns: full pieces of the widest tile, then one
@@ -1090,23 +1136,44 @@ static int upload_step(Step &st) {
       st.nwork_tc4[i][j] = (int64_t)wtc4[i][j].size();
     }
   for (int i = 0; i < 2; ++i) st.nwork_tcb[i] = (int64_t)wtcb[i].size();
-  // plane buffer: A records, then B records from the 256-aligned A total
-  // (the layout umma_plane_bytes sizes)
+  // record offsets: kept area at plane_keep_off, per-call area at
+  // plane_call_off (A records, then B records of each area)
   {
-    const int64_t b0 = (UL.abytes + 255) & ~int64_t(255);
-    for (auto &p : UL.pb) p.rec += b0;
-    for (int i = 0; i < 3; ++i) {
-      for (auto &w : UL.w1[i]) w.b_rec += b0;
-      for (auto &w : UL.wl[i]) w.b_rec += b0;
+    int64_t b0[2];
+    const int64_t call = area_bytes(UL, 0, &b0[0]), keep = area_bytes(UL, 1, &b0[1]);
+    if (st.plane_ws_off >= 0) {
+      if (call != st.plane_call_bytes || keep != st.plane_keep_bytes)
+        return fail(ZMPO_E_ARG, "upload: prepared-plane size differs from the plan's reservation");
+    } else {
+      st.plane_keep_off = 0;
+      st.plane_keep_bytes = keep;
+      st.plane_call_off = keep;
+      st.plane_call_bytes = call;
+      st.plane_bytes = keep + call;
     }
-    const int64_t total = (UL.abytes + UL.bbytes) > 0 ? b0 + UL.bbytes : 0;
-    if (st.plane_ws_off >= 0 && (total != st.plane_bytes || b0 != st.plane_b0))
-      return fail(ZMPO_E_ARG, "upload: prepared-plane size differs from the plan's reservation");
-    st.plane_bytes = total;
-    st.plane_b0 = b0;
+    const int64_t abase[2] = {st.plane_call_off, st.plane_keep_off};
+    const int64_t bbase[2] = {st.plane_call_off + b0[0], st.plane_keep_off + b0[1]};
+    for (int k = 0; k < 2; ++k) {
+      for (auto &p : UL.pa[k]) p.rec += abase[k];
+      for (auto &p : UL.pb[k]) p.rec += bbase[k];
+    }
+    for (int i = 0; i < 3; ++i)
+      for (auto *wv : {&UL.w1[i], &UL.wl[i]})
+        for (auto &w : *wv) {
+          w.a_rec += abase[w.pad & 1];
+          w.b_rec += bbase[(w.pad >> 1) & 1];
+          w.pad = 0;
+        }
   }
-  st.nprep_a = (int64_t)UL.pa.size();
-  st.nprep_b = (int64_t)UL.pb.size();
+  // prepare items: kept ones first (a call that reuses them skips them)
+  std::vector<PrepA> prep_a(UL.pa[1]);
+  prep_a.insert(prep_a.end(), UL.pa[0].begin(), UL.pa[0].end());
+  std::vector<PrepB> prep_b(UL.pb[1]);
+  prep_b.insert(prep_b.end(), UL.pb[0].begin(), UL.pb[0].end());
+  st.nprep_a = (int64_t)prep_a.size();
+  st.nprep_b = (int64_t)prep_b.size();
+  st.nprep_a_kept = (int64_t)UL.pa[1].size();
+  st.nprep_b_kept = (int64_t)UL.pb[1].size();
   for (int i = 0; i < 3; ++i) {
     st.nwork_um[i] = (int64_t)UL.w1[i].size();
     st.nwork_ul[i] = (int64_t)UL.wl[i].size();
@@ -1136,8 +1203,8 @@ static int upload_step(Step &st) {
     CUDA_TRY(up(&st.d_work_um[i], UL.w1[i]));
     CUDA_TRY(up(&st.d_work_ul[i], UL.wl[i]));
   }
-  CUDA_TRY(up(&st.d_prep_a, UL.pa));
-  CUDA_TRY(up(&st.d_prep_b, UL.pb));
+  CUDA_TRY(up(&st.d_prep_a, prep_a));
+  CUDA_TRY(up(&st.d_prep_b, prep_b));
   CUDA_TRY(up(&st.d_reds, st.reds));
   if (st.part_elems > 0) CUDA_TRY(cudaMalloc((void **)&st.d_part, st.part_elems * sizeof(double)));
   // keep the host mirror of groups (sizes) but free the bulky segment copy
@@ -1202,7 +1269,7 @@ static void profile_collect(Step &st) {
   st.ev_pending = false;
 }
 
-static int run_step(Step &st, const Bufs &b, int precision, void *stream) {
+static int run_step(Step &st, const Bufs &b, int precision, void *stream, bool cut_kept = true) {
   int rc = upload_step(st);
   if (rc) return rc;
   // one NVTX range per step ("zmpo.step<i>"), so a profiler can select the
@@ -1228,7 +1295,7 @@ static int run_step(Step &st, const Bufs &b, int precision, void *stream) {
   if (precision == ZMPO_PREC_FP64)
     rc = launch_step_fp64(st, bb, stream);
   else if (precision == ZMPO_PREC_SPLIT)
-    rc = launch_step_split(st, bb, 4, stream);
+    rc = launch_step_split(st, bb, 4, stream, cut_kept);
   else if (precision == ZMPO_PREC_EMU64)
     rc = launch_step_split(st, bb, 7, stream);
   else
@@ -1819,10 +1886,32 @@ int zmpo_sigma(zmpo_engine *e, int plan_id, const double *d_L, const double *d_R
   b.p[3] = const_cast<double *>(d_x);
   b.p[4] = d_y;
   b.p[5] = (double *)d_workspace;
+  // the kept records are reused when the caller asked for it and they are
+  // this plan's, from its last split call on the same buffers, with no other
+  // plan run on this workspace since
+  const bool reuse = P->reuse_next && P->kept_ready && P->kept_ws == d_workspace && P->kept_L == d_L &&
+                     P->kept_R == d_R && P->kept_W == d_W && e->ws_user[d_workspace] == plan_id;
+  P->reuse_next = false;
+  e->ws_user[d_workspace] = plan_id;
+  if (precision == ZMPO_PREC_SPLIT) P->kept_ready = false;
   for (auto &s : P->steps) {
-    int rc = run_step(s, b, precision, stream);
+    int rc = run_step(s, b, precision, stream, !reuse);
     if (rc) return rc;
   }
+  if (precision == ZMPO_PREC_SPLIT) {
+    P->kept_ready = true;
+    P->kept_ws = d_workspace;
+    P->kept_L = d_L;
+    P->kept_R = d_R;
+    P->kept_W = d_W;
+  }
+  return ZMPO_OK;
+}
+
+int zmpo_sigma_reuse_kept(zmpo_engine *e, int plan_id, int reuse) {
+  Plan *P = get_plan(e, plan_id, 2);
+  if (!P) return fail(ZMPO_E_ID, "sigma_reuse_kept: unknown plan");
+  P->reuse_next = reuse != 0;
   return ZMPO_OK;
 }
 

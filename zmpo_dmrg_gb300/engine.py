@@ -205,6 +205,11 @@ class Engine:
                                     device_ptr(workspace) if workspace is not None else None,
                                     _lib.PREC[precision], current_stream()), "sigma")
 
+    def sigma_reuse_kept(self, pid, reuse):
+        """The next sigma call of plan ``pid`` may reuse the digit planes of
+        its fixed operands (environments, MPO) from its previous call."""
+        check(_lib.lib().zmpo_sigma_reuse_kept(self.h, pid, 1 if reuse else 0), "sigma_reuse_kept")
+
     def hdiag(self, pid, L, R, W, diag):
         check(_lib.lib().zmpo_hdiag(self.h, pid, device_ptr(L), device_ptr(R), device_ptr(W),
                                     device_ptr(diag), current_stream()), "hdiag")

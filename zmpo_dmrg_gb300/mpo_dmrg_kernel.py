@@ -180,6 +180,7 @@ class SigmaPlan:
         self.nlaunch = stats[0][2]
         self.fL, self.fR = fL, fR
         self.graphs = {}
+        self._kept_token = None
 
     @property
     def workspace(self):
@@ -189,6 +190,15 @@ class SigmaPlan:
         """Reuse for environments of the same structure (new device buffers)."""
         self.fL, self.fR = fL, fR
         self.graphs = {}
+        self._kept_token = None
+
+    def _fixed_token(self, W):
+        """Identity and in-place-write counters of the operands that stay
+        fixed during a Davidson solve (environments, MPO) and the workspace:
+        equal tokens on two calls mean the engine may reuse the digit planes
+        it cut from them on the first call."""
+        ts = (self.fL.buf, self.fR.buf, W)
+        return tuple((id(t), t.data_ptr(), t._version) for t in ts) + (self.workspace.data_ptr(),)
 
     def run(self, dmrg, x, y, precision, use_graph=False):
         """y = H x.  With ``use_graph`` the launches of this plan are recorded
@@ -216,7 +226,14 @@ class SigmaPlan:
                 y += tmp
             return
         if not use_graph:
+            tok = None
+            if precision == "split":
+                tok = self._fixed_token(W)
+                eng.sigma_reuse_kept(self.pid, tok == self._kept_token)
+                self._kept_token = None
             eng.sigma(self.pid, self.fL.buf, self.fR.buf, W, x, y, self.workspace, precision)
+            if tok is not None:
+                self._kept_token = tok
             return
         torch = _torch()
         rec = self.graphs.get(precision)
