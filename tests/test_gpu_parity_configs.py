@@ -10,14 +10,17 @@
   the same check on the spin-projected H.psi (N-only relabelled terms).
 * K=10, 10 electrons, D=64, the reference's default two-site schedule from
   the occupation-number state (its initial one-site sweep included), 12
-  sweeps: the energy of every noise-free sweep (the sixth on) and the final
-  energy of the GPU driver against the oracle driver's (frozen in
+  sweeps: the energies of the converged sweeps and the final energy of the
+  GPU driver against the oracle driver's (frozen in
   ``tests/golden/sweep_k10_d64.npz`` by
-  ``tests/golden/make_oracle_fixtures.py``), within 1e-8 Eh.  The first
-  sweeps add random noise to the density matrix and stop Davidson at 1e-4,
-  so their energies depend on the noise draws (oracle runs with two noise
-  seeds differ there by up to 2e-6 and agree to 1e-10 from the sixth sweep
-  on); they are not compared.  The reference builds a first MPS only in its
+  ``tests/golden/make_oracle_fixtures.py``), within 1e-8 Eh.  The schedule
+  adds density-matrix noise in the first four sweeps and tightens the
+  Davidson tolerance from 1e-4 to 1e-9 over the next four (sweeps 3-7), so
+  until then a sweep's energy is only as sharp as its tolerance and depends
+  on the noise draws and on the rounding of the products (the GPU driver
+  differs from the oracle by up to 6e-7 at the 1e-7 sweep); the sweeps from
+  the ninth on (tolerance 1e-9 after a sweep at 1e-9) and the final energy
+  are compared.  The reference builds a first MPS only in its
   dense-vector mode, so the driver runs with ``ifQt = False``: Davidson
   vectors (and their random start noise) in the reference's dense order, the
   engine's block-sparse products underneath.
@@ -93,5 +96,5 @@ def test_sweep_k10_d64_matches_oracle_driver(gpu, precision):
     got = numpy.array([float(e) for e in m.eav])
     ref = z["sweep_energies"]
     assert got.shape == ref.shape
-    assert numpy.abs(got[5:] - ref[5:]).max() < 1e-8, (got - ref)
+    assert numpy.abs(got[8:] - ref[8:]).max() < 1e-8, (got - ref)
     assert abs(float(m.Energy) - float(z["energy"])) < 1e-8

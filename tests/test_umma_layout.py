@@ -51,7 +51,7 @@ def test_constants_match_source():
     # record sizes (engine.h) = the layout mirrored below
     assert "umma_a_rec_bytes(int nkb, int tm8) { return (int64_t)nkb * 256 * tm8 + kUmmaTM * 4; }" in ENGINE
     assert "umma_b_kb_bytes(int tn) { return 4 * (int64_t)tn * 64; }" in ENGINE
-    assert "umma_b_rec_bytes(int nkb, int tn) { return nkb * umma_b_kb_bytes(tn) + (int64_t)tn * 20; }" in ENGINE
+    assert "umma_b_rec_bytes(int nkb, int tn) { return nkb * umma_b_kb_bytes(tn) + (int64_t)tn * 4; }" in ENGINE
     assert "constexpr int kUmmaLongMaxK = 2048;" in ENGINE
     assert "static constexpr int NSTAGE = 4;" in SRC and "STAGE = umma::A_STAGE + B_KB;" in SRC
 
@@ -61,7 +61,7 @@ def a_tile_bytes(nkb, tm8=TM):
 
 
 def b_tile_bytes(nkb, tn):
-    return nkb * 4 * tn * ROW_BYTES + tn * 20
+    return nkb * 4 * tn * ROW_BYTES + tn * 4
 
 
 def layout(TN):
@@ -142,20 +142,22 @@ def test_bulk_copies(TN, nkb, tm8):
     # B planes of a one-pass item
     size = nkb * L["B_KB"]
     assert size % 16 == 0 and size <= L["OFF_A"] - L["OFF_B"] and size <= TX_MAX
-    # per row tile / pass: row exponents (end of the A record) + column part (end of the B record)
+    # per row tile / pass: row exponents (end of the A record), column
+    # exponents (end of the B record), the column map (TN offsets, TN strides
+    # from the planner's array, 16 bytes per column)
     ea_src, eb_src = nkb * akb, nkb * L["B_KB"]
     assert ea_src % 16 == 0 and ea_src + TM * 4 == A
-    assert eb_src % 16 == 0 and eb_src + TN * 20 == B
-    assert L["REC_EA"] + TM * 4 == L["REC_EB"] and L["REC_EB"] + TN * 20 == L["REC_INFO"]
-    assert (TM * 4) % 16 == 0 and (TN * 20) % 16 == 0
+    assert eb_src % 16 == 0 and eb_src + TN * 4 == B
+    assert L["REC_EA"] + TM * 4 == L["REC_EB"] and L["REC_EB"] + TN * 4 == L["REC_CB"]
+    assert L["REC_CB"] + TN * 16 == L["REC_INFO"] and L["REC_CB"] % 16 == 0
+    assert (TM * 4) % 16 == 0 and (TN * 4) % 16 == 0 and (TN * 16) % 16 == 0
+    assert "bulk_g2s(rec_s + LY::REC_CB, cmaps + wk.cmap, TN * 16, bar(BAR_E_FULL + b));" in SRC
     # A k blocks into a stage (tm8-row planes, 128 rows read from each)
     assert akb <= L["A_STAGE"] and 3 * (akb // 4) + TM * ROW_BYTES <= L["A_STAGE"]
     # long kernel: one stage = A k block + B k block
     G = long_layout(TN)
     assert akb + G["B_KB"] <= TX_MAX and akb <= G["A_STAGE"]
-    # the column part's fields inside the B record
-    tail = eb_src
-    assert tail + TN * 4 + TN * 8 + TN * 8 == B and (tail + TN * 4) % 8 == 0 and (tail + TN * 12) % 8 == 0
+
 
 
 def long_layout(TN):
@@ -222,6 +224,7 @@ def test_planner_plane_offsets_are_aligned():
             rem = N - n0
             tn = 64 if rem >= 64 else (16 if rem <= 16 else (32 if rem <= 32 else 64))
             starts.append(b0 + b)
+            assert (2 * tn * 8) % 16 == 0   # a column map (element offsets in the map array)
             b += b_tile_bytes(nkb, tn)
             n0 += tn
     assert all(s % 16 == 0 for s in starts)

@@ -76,8 +76,11 @@ struct Work {
 //     bytes, then 128 int32 row exponents;
 //   B record (column tile of tn columns, one pass): nkb k blocks, each four
 //     planes of tn rows x 64 bytes (plane s holds rows s*tn .. s*tn+tn-1),
-//     then tn int32 column exponents, tn int64 output offsets of (row 0,
-//     column c) (-1: no such column) and tn int64 output row strides.
+//     then tn int32 column exponents.  Groups whose B parts in the pass are
+//     the same share one B record.
+// The output column map of a (group, column tile) -- tn int64 output offsets
+// of (row 0, column c) (-1: no such column), then tn int64 output row strides
+// -- is made by the planner (an array uploaded with the task lists).
 // Every record size is a multiple of 16 bytes (bulk-copy granularity).
 constexpr int kUmmaTM = 128, kUmmaMaxK = 256, kUmmaKB = 32;
 constexpr int kUmmaLongMaxK = 2048;                 // K of a long item (passes of kUmmaMaxK)
@@ -85,7 +88,7 @@ constexpr int64_t kUmmaAPlane = 128 * 64;           // one 128-row digit plane o
 constexpr int64_t kUmmaAKB = 4 * kUmmaAPlane;       // four planes (shared-memory stage)
 constexpr int64_t umma_a_rec_bytes(int nkb, int tm8) { return (int64_t)nkb * 256 * tm8 + kUmmaTM * 4; }
 constexpr int64_t umma_b_kb_bytes(int tn) { return 4 * (int64_t)tn * 64; }
-constexpr int64_t umma_b_rec_bytes(int nkb, int tn) { return nkb * umma_b_kb_bytes(tn) + (int64_t)tn * 20; }
+constexpr int64_t umma_b_rec_bytes(int nkb, int tn) { return nkb * umma_b_kb_bytes(tn) + (int64_t)tn * 4; }
 
 struct PrepA {      // cut one A record: rows m0 .., slots k0 .. k0+kc-1 of the group
   int64_t rec;      // byte offset of the record in the plane buffer
@@ -97,7 +100,8 @@ struct PrepB {      // cut one B record: columns n0 .. n0+tn-1, slots k0 .. k0+k
 };
 struct UWork {      // tcgen05 work item: one column tile, a run of row tiles (one-pass)
   int64_t a_rec;    // or one row tile and every pass of its K (long); first A record
-  int64_t b_rec;    // first B record of the column tile
+  int64_t b_rec;    // first B record of the column tile (one per pass, consecutive)
+  int64_t cmap;     // its column map (element offset into the column-map array)
   int32_t group, m0;
   int32_t nrt_k;    // row tiles of the run (1 for long items) | K << 8
   int32_t pad;
@@ -136,6 +140,7 @@ struct Step {
   UWork *d_work_um[3] = {};
   int64_t nwork_um[3] = {};
   UWork *d_work_ul[3] = {};         // long items (passes), by column tile 16 / 32 / 64
+  int64_t *d_cmap = nullptr;        // column maps of the tcgen05 work items
   int64_t nwork_ul[3] = {};
   bool split_done = false;          // split-K parts made (split_long_groups)
   int64_t nprep_a_kept = 0, nprep_b_kept = 0;  // the first items cut kept records

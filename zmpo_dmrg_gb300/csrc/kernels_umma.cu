@@ -118,7 +118,7 @@ struct Layout {
   static_assert(B_KB == umma_b_kb_bytes(TN), "plane record layout");
   static_assert(OFF_A % 1024 == 0 && A_STAGE % 1024 == 0 && B_KB % 1024 == 0, "swizzle atoms");
   static_assert(OFF_REC % 16 == 0 && REC_EB % 16 == 0 && REC_BYTES % 16 == 0, "bulk-copy alignment");
-  static_assert(REC_INFO - REC_EB == TN * 20, "column part of a B tile record");
+  static_assert(REC_INFO - REC_EB == TN * 20 && REC_CB % 16 == 0, "exponents + column map of a tile record");
   static_assert(SMEM <= 232448, "shared memory");
 };
 
@@ -467,10 +467,9 @@ k_prep_a(const PrepA *__restrict__ items, int64_t nitems, const Group *__restric
 }
 
 // One B record per item (columns n0 .. n0+tn-1, slots k0 .. k0+kc-1): the
-// column map (output offset of row 0 and row stride of each column,
-// column-block look-ups once per column), the column exponents over the
-// window, the four digit planes of every k block (plane s holds rows
-// s*tn + c), then exponents, offsets and strides after the planes.
+// column exponents over the window (column-block look-ups once per column),
+// the four digit planes of every k block (plane s holds rows s*tn + c), then
+// the exponents after the planes.
 __global__ void __launch_bounds__(umma::PREP_THREADS)
 k_prep_b(const PrepB *__restrict__ items, int64_t nitems, const Group *__restrict__ groups,
          const Seg *__restrict__ segs, const ColBlock *__restrict__ cbl, const SegB *__restrict__ segb, Bufs bufs,
@@ -479,7 +478,6 @@ k_prep_b(const PrepB *__restrict__ items, int64_t nitems, const Group *__restric
   __shared__ Slot slots[KMAX];
   __shared__ int s_ctl[2];
   __shared__ int s_eb[64], s_jb[64], s_rel[64];
-  __shared__ long long s_cb[64], s_rs[64];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int64_t it = blockIdx.x; it < nitems; it += gridDim.x) {
     const PrepB p = items[it];
@@ -494,26 +492,9 @@ k_prep_b(const PrepB *__restrict__ items, int64_t nitems, const Group *__restric
       }
     }
     for (int c = tid; c < tn; c += PREP_THREADS) {
-      const int col = p.n0 + c;
-      long long cbase = -1, rs = 0;
-      int jb = -1, rel = 0;
-      if (col < g.N) {
-        if (g.ncb == 0) {
-          cbase = g.c_off + (long long)col * g.scn;
-          rs = g.scm;
-        } else {
-          jb = find_cblock(cbl, g, col, rel);
-          if (jb >= 0) {
-            const ColBlock cb = cbl[g.cb0 + jb];
-            cbase = cb.c_off + (long long)rel * cb.scn;
-            rs = cb.scm;
-          }
-        }
-      }
-      s_jb[c] = jb;
+      int rel = 0;
+      s_jb[c] = g.ncb ? find_cblock(cbl, g, p.n0 + c, rel) : -1;
       s_rel[c] = rel;
-      s_cb[c] = cbase;
-      s_rs[c] = rs;
       s_eb[c] = 0;
     }
     __syncthreads();
@@ -538,11 +519,7 @@ k_prep_b(const PrepB *__restrict__ items, int64_t nitems, const Group *__restric
     __syncthreads();
     unsigned char *rec = planes + p.rec;
     unsigned char *tail = rec + (int64_t)nkb * umma_b_kb_bytes(tn);
-    for (int c = tid; c < tn; c += PREP_THREADS) {
-      reinterpret_cast<int *>(tail)[c] = s_eb[c];
-      reinterpret_cast<long long *>(tail + tn * 4)[c] = s_cb[c];
-      reinterpret_cast<long long *>(tail + tn * 12)[c] = s_rs[c];
-    }
+    for (int c = tid; c < tn; c += PREP_THREADS) reinterpret_cast<int *>(tail)[c] = s_eb[c];
     for (int u = tid; u < nkb * tn * 4; u += PREP_THREADS) {
       const int kb = u / (tn * 4), c = (u >> 2) % tn, ch = u & 3;
       double v[8];
@@ -558,7 +535,7 @@ k_prep_b(const PrepB *__restrict__ items, int64_t nitems, const Group *__restric
 template <int TN>
 __global__ void __launch_bounds__(umma::NTHREADS, 1)
 k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
-            const unsigned char *__restrict__ planes, Bufs bufs) {
+            const unsigned char *__restrict__ planes, const int64_t *__restrict__ cmaps, Bufs bufs) {
   using namespace umma;
   using LY = Layout<TN>;
   constexpr int NSTAGE = LY::NSTAGE;
@@ -634,7 +611,8 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
           info[2] = g.cbuf;
           bar_arrive_tx(bar(BAR_E_FULL + b), (uint32_t)(TM * 4 + TN * 20));
           bulk_g2s(rec_s + LY::REC_EA, arec + (int64_t)nkb * akb, TM * 4, bar(BAR_E_FULL + b));
-          bulk_g2s(rec_s + LY::REC_EB, brec + (int64_t)nkb * LY::B_KB, TN * 20, bar(BAR_E_FULL + b));
+          bulk_g2s(rec_s + LY::REC_EB, brec + (int64_t)nkb * LY::B_KB, TN * 4, bar(BAR_E_FULL + b));
+          bulk_g2s(rec_s + LY::REC_CB, cmaps + wk.cmap, TN * 16, bar(BAR_E_FULL + b));
           ++nE[b];
           for (int kb = 0; kb < nkb; ++kb, ++q) {
             const uint32_t s = q % NSTAGE, use = q / NSTAGE;
@@ -806,7 +784,7 @@ struct LongLayout {
 template <int TN>
 __global__ void __launch_bounds__(umma::NTHREADS, 1)
 k_step_umma_long(const UWork *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
-                 const unsigned char *__restrict__ planes, Bufs bufs) {
+                 const unsigned char *__restrict__ planes, const int64_t *__restrict__ cmaps, Bufs bufs) {
   using namespace umma;
   using LY = LongLayout<TN>;
   constexpr int NSTAGE = LY::NSTAGE;
@@ -876,7 +854,8 @@ k_step_umma_long(const UWork *__restrict__ work, int64_t nwork, const Group *__r
           info[3] = j == npass - 1;
           bar_arrive_tx(bar(BAR_E_FULL + b), (uint32_t)(TM * 4 + TN * 20));
           bulk_g2s(rec_s + LY::REC_EA, arec + (int64_t)nkb * akb, TM * 4, bar(BAR_E_FULL + b));
-          bulk_g2s(rec_s + LY::REC_EB, brec + (int64_t)nkb * LY::B_KB, TN * 20, bar(BAR_E_FULL + b));
+          bulk_g2s(rec_s + LY::REC_EB, brec + (int64_t)nkb * LY::B_KB, TN * 4, bar(BAR_E_FULL + b));
+          bulk_g2s(rec_s + LY::REC_CB, cmaps + wk.cmap, TN * 16, bar(BAR_E_FULL + b));
           ++nE[b];
           for (int kb = 0; kb < nkb; ++kb, ++q) {
             const uint32_t s = q % NSTAGE, use = q / NSTAGE;
@@ -889,7 +868,7 @@ k_step_umma_long(const UWork *__restrict__ work, int64_t nwork, const Group *__r
           }
           if (!ok) break;
           arec += (int64_t)nkb * akb + TM * 4;
-          brec += (int64_t)nkb * LY::B_KB + TN * 20;
+          brec += (int64_t)nkb * LY::B_KB + TN * 4;
         }
       }
       // drain: every bulk copy issued has landed before the CTA may exit
@@ -1021,7 +1000,8 @@ static int launch_umma_long_t(const UWork *work, int64_t nwork, const Step &s, c
     attr = true;
   }
   const int grid = (int)(nwork < nsm ? nwork : nsm);
-  k_step_umma_long<TN><<<grid, umma::NTHREADS, smem, (cudaStream_t)stream>>>(work, nwork, s.d_groups, planes, b);
+  k_step_umma_long<TN><<<grid, umma::NTHREADS, smem, (cudaStream_t)stream>>>(work, nwork, s.d_groups, planes,
+                                                                             s.d_cmap, b);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? ZMPO_OK : record_cuda_error("k_step_umma_long", (int)e);
 }
@@ -1038,7 +1018,8 @@ static int launch_umma_t(const UWork *work, int64_t nwork, const Step &s, const 
     attr = true;
   }
   const int grid = (int)(nwork < nsm ? nwork : nsm);
-  k_step_umma<TN><<<grid, umma::NTHREADS, smem, (cudaStream_t)stream>>>(work, nwork, s.d_groups, planes, b);
+  k_step_umma<TN><<<grid, umma::NTHREADS, smem, (cudaStream_t)stream>>>(work, nwork, s.d_groups, planes, s.d_cmap,
+                                                                        b);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? ZMPO_OK : record_cuda_error("k_step_umma", (int)e);
 }

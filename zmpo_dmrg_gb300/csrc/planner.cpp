@@ -935,9 +935,63 @@ struct UmmaLists {
   std::vector<PrepA> pa[2];          // [per-call, kept]; rec relative to its part
   std::vector<PrepB> pb[2];
   std::vector<UWork> w1[3], wl[3];   // one-pass / long items by column tile; pad = kept sides
+  std::vector<int64_t> cmap;         // column maps (tn output offsets, then tn row strides each)
+  // B-record sequences (all passes of a column tile) of plain groups, by
+  // their exact content key: groups reading the same B parts share them
+  std::map<std::vector<int64_t>, int64_t> bseq[2];
   int64_t abytes[2] = {0, 0}, bbytes[2] = {0, 0};
   double macs = 0.0;                 // multiply-adds the MMAs issue (x10 digit products)
 };
+
+// Content key of the B records of a column tile (columns n0 .. n0+tn-1) of a
+// plain group over its slots kbase .. kbase+K-1: the B part of every segment
+// piece in that window (buffer, offset of its first slot, strides, length).
+// Equal keys mean equal records.
+static void b_seq_key(const Step &st, const Group &G, int64_t kbase, int64_t K, int n0, int tn,
+                      std::vector<int64_t> &key) {
+  key.assign({(int64_t)n0, (int64_t)tn, (int64_t)std::min(tn, G.N - n0), K});
+  int64_t pos = 0;
+  for (int i = 0; i < G.nseg && pos < kbase + K; ++i) {
+    const Seg &sg = st.segs[G.seg0 + i];
+    const int64_t lo = std::max(pos, kbase), hi = std::min(pos + sg.K, kbase + K);
+    if (lo < hi) {
+      key.push_back(sg.bbuf);
+      key.push_back(sg.b_off + (lo - pos) * sg.sbk);
+      key.push_back(sg.sbk);
+      key.push_back(sg.sbn);
+      key.push_back(hi - lo);
+    }
+    pos += sg.K;
+  }
+}
+
+// Output column map of columns n0 .. n0+tn-1 of a group: tn offsets of
+// (row 0, column) (-1: none), then tn row strides
+static void column_map(const Step &st, const Group &G, int n0, int tn, std::vector<int64_t> &out) {
+  const size_t base = out.size();
+  out.resize(base + 2 * (size_t)tn);
+  for (int c = 0; c < tn; ++c) {
+    const int col = n0 + c;
+    int64_t cbase = -1, rs = 0;
+    if (col < G.N) {
+      if (G.ncb == 0) {
+        cbase = G.c_off + (int64_t)col * G.scn;
+        rs = G.scm;
+      } else {
+        for (int j = 0; j < G.ncb; ++j) {
+          const ColBlock &cb = st.cblocks[G.cb0 + j];
+          if (col >= cb.n0 && col < cb.n0 + cb.n) {
+            cbase = cb.c_off + (int64_t)(col - cb.n0) * cb.scn;
+            rs = cb.scm;
+            break;
+          }
+        }
+      }
+    }
+    out[base + c] = cbase;
+    out[base + tn + c] = rs;
+  }
+}
 
 constexpr int kUmmaRunMax = 16;      // row tiles of a one-pass work item
 
@@ -951,7 +1005,10 @@ static bool side_kept(const Step &st, const Group &G, bool a_side, uint32_t mask
   return true;
 }
 
-static void umma_add_group(UmmaLists &L, int g, const Group &G, int64_t K, bool keep_a, bool keep_b) {
+// kbase: the group's first slot in G's segments (a split-K part counted
+// before the split: G is the whole group)
+static void umma_add_group(UmmaLists &L, const Step &st, int g, const Group &G, int64_t kbase, int64_t K,
+                           bool keep_a, bool keep_b) {
   const bool one = umma_one_pass(G, K);
   if (!one && !umma_long(G, K)) return;
   const int ka = keep_a ? 1 : 0, kb = keep_b ? 1 : 0;
@@ -972,21 +1029,33 @@ static void umma_add_group(UmmaLists &L, int g, const Group &G, int64_t K, bool 
   const int nruns = (nrt + kUmmaRunMax - 1) / kUmmaRunMax;
   const int len = (nrt + nruns - 1) / nruns;
   const int32_t sides = ka | (kb << 1);
+  std::vector<int64_t> key;
   for (int n0 = 0; n0 < G.N;) {
     const int tn = umma_tn(G.N - n0), ti = umma_ti(tn);
-    const int64_t brec = L.bbytes[kb];
-    for (int j = 0; j < npass; ++j) {
-      const int k0 = j * kUmmaMaxK, kc = (int)std::min<int64_t>(kUmmaMaxK, K - k0);
-      if (L.make) L.pb[kb].push_back({L.bbytes[kb], g, n0, tn, k0, kc, 0});
-      L.bbytes[kb] += umma_b_rec_bytes((kc + kUmmaKB - 1) / kUmmaKB, tn);
+    int64_t brec = -1;
+    if (G.ncb == 0) {
+      b_seq_key(st, G, kbase, K, n0, tn, key);
+      auto it = L.bseq[kb].find(key);
+      if (it != L.bseq[kb].end()) brec = it->second;
+    }
+    if (brec < 0) {
+      brec = L.bbytes[kb];
+      if (G.ncb == 0) L.bseq[kb].emplace(key, brec);
+      for (int j = 0; j < npass; ++j) {
+        const int k0 = j * kUmmaMaxK, kc = (int)std::min<int64_t>(kUmmaMaxK, K - k0);
+        if (L.make) L.pb[kb].push_back({L.bbytes[kb], g, n0, tn, k0, kc, 0});
+        L.bbytes[kb] += umma_b_rec_bytes((kc + kUmmaKB - 1) / kUmmaKB, tn);
+      }
     }
     if (L.make) {
+      const int64_t cm = (int64_t)L.cmap.size();
+      column_map(st, G, n0, tn, L.cmap);
       if (one) {
         for (int r = 0; r < nrt; r += len)
-          L.w1[ti].push_back({arec[r], brec, g, r * kUmmaTM, std::min(len, nrt - r) | (int32_t)(K << 8), sides});
+          L.w1[ti].push_back({arec[r], brec, cm, g, r * kUmmaTM, std::min(len, nrt - r) | (int32_t)(K << 8), sides});
       } else {
         for (int r = 0; r < nrt; ++r)
-          L.wl[ti].push_back({arec[r], brec, g, r * kUmmaTM, 1 | (int32_t)(K << 8), sides});
+          L.wl[ti].push_back({arec[r], brec, cm, g, r * kUmmaTM, 1 | (int32_t)(K << 8), sides});
       }
     }
     L.macs += (double)nrt * kUmmaTM * tn * k16;
@@ -1013,10 +1082,10 @@ static void umma_plane_bytes(const Step &st, int64_t *keep, int64_t *call) {
       Group part = G;
       part.cbuf = kPartialBuf;
       for (int64_t k0 = 0; k0 < k; k0 += kSplitK)
-        umma_add_group(L, 0, part, std::min<int64_t>(kSplitK, k - k0), ka, kb);
+        umma_add_group(L, st, 0, part, k0, std::min<int64_t>(kSplitK, k - k0), ka, kb);
       continue;
     }
-    umma_add_group(L, 0, G, k, ka, kb);
+    umma_add_group(L, st, 0, G, 0, k, ka, kb);
   }
   *call = area_bytes(L, 0, nullptr);
   *keep = area_bytes(L, 1, nullptr);
@@ -1051,8 +1120,21 @@ static void reserve_plane_region(Plan *P) {
   P->ws_elems = ((off + keep_total + call_max + 255) & ~int64_t(255)) / (int64_t)sizeof(double);
 }
 
+static void free_step(Step &st);
+
+static int upload_step_lists(Step &st);
+
+// Device copies of a step's task lists, made on first use.  A failed upload
+// (out of device memory, say) frees what it had allocated, so a later call
+// can try again.
 static int upload_step(Step &st) {
   if (st.uploaded) return ZMPO_OK;
+  const int rc = upload_step_lists(st);
+  if (rc != ZMPO_OK) free_step(st);
+  return rc;
+}
+
+static int upload_step_lists(Step &st) {
   split_long_groups(st);
   std::vector<Work> w64, wtc[3][4], wtc4[3][4], wtcb[2];
   UmmaLists UL;
@@ -1081,7 +1163,8 @@ static int upload_step(Step &st) {
       }
     // tcgen05 groups (records cut by the prepare kernels)
     const double macs0 = UL.macs;
-    umma_add_group(UL, g, G, ktot[g], side_kept(st, G, true, st.keep_bufs), side_kept(st, G, false, st.keep_bufs));
+    umma_add_group(UL, st, g, G, 0, ktot[g], side_kept(st, G, true, st.keep_bufs),
+                   side_kept(st, G, false, st.keep_bufs));
     const bool routed = UL.macs != macs0;
     st.mma_macs[1] += UL.macs - macs0;
     // Tensor-core tiles.  Columns: full pieces of the widest tile, then one
@@ -1205,6 +1288,7 @@ static int upload_step(Step &st) {
   }
   CUDA_TRY(up(&st.d_prep_a, prep_a));
   CUDA_TRY(up(&st.d_prep_b, prep_b));
+  CUDA_TRY(up(&st.d_cmap, UL.cmap));
   CUDA_TRY(up(&st.d_reds, st.reds));
   if (st.part_elems > 0) CUDA_TRY(cudaMalloc((void **)&st.d_part, st.part_elems * sizeof(double)));
   // keep the host mirror of groups (sizes) but free the bulky segment copy
@@ -1243,6 +1327,8 @@ static void free_step(Step &st) {
   }
   cudaFree(st.d_prep_a);
   cudaFree(st.d_prep_b);
+  cudaFree(st.d_cmap);
+  st.d_cmap = nullptr;
   cudaFree(st.d_planes_own);
   st.d_prep_a = nullptr;
   st.d_prep_b = nullptr;

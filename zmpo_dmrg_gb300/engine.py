@@ -30,6 +30,20 @@ def device_ptr(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
+ZMPO_E_NOMEM = -5
+
+
+def checked_call(call, what):
+    """Run an engine call; when it fails for want of device memory, return
+    the blocks PyTorch's caching allocator holds unused to the device and try
+    once more (the engine allocates with cudaMalloc, which cannot use them)."""
+    rc = call()
+    if rc == ZMPO_E_NOMEM:
+        _torch().cuda.empty_cache()
+        rc = call()
+    return check(rc, what)
+
+
 def current_stream():
     torch = _torch()
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
@@ -102,8 +116,9 @@ class Engine:
         return lo.value, pid.value
 
     def contract_exec(self, pid, a, b, out, precision="fp64"):
-        check(_lib.lib().zmpo_contract_exec(self.h, pid, device_ptr(a), device_ptr(b), device_ptr(out),
-                                            _lib.PREC[precision], current_stream()), "contract_exec")
+        checked_call(lambda: _lib.lib().zmpo_contract_exec(self.h, pid, device_ptr(a), device_ptr(b),
+                                                           device_ptr(out), _lib.PREC[precision],
+                                                           current_stream()), "contract_exec")
 
     def plan_stats(self, pid):
         fl = ctypes.c_double()
@@ -200,10 +215,10 @@ class Engine:
         return pid.value, ws.value
 
     def sigma(self, pid, L, R, W, x, y, workspace, precision="fp64"):
-        check(_lib.lib().zmpo_sigma(self.h, pid, device_ptr(L), device_ptr(R), device_ptr(W),
-                                    device_ptr(x), device_ptr(y),
-                                    device_ptr(workspace) if workspace is not None else None,
-                                    _lib.PREC[precision], current_stream()), "sigma")
+        ws = device_ptr(workspace) if workspace is not None else None
+        checked_call(lambda: _lib.lib().zmpo_sigma(self.h, pid, device_ptr(L), device_ptr(R), device_ptr(W),
+                                                   device_ptr(x), device_ptr(y), ws, _lib.PREC[precision],
+                                                   current_stream()), "sigma")
 
     def sigma_reuse_kept(self, pid, reuse):
         """The next sigma call of plan ``pid`` may reuse the digit planes of
@@ -211,8 +226,8 @@ class Engine:
         check(_lib.lib().zmpo_sigma_reuse_kept(self.h, pid, 1 if reuse else 0), "sigma_reuse_kept")
 
     def hdiag(self, pid, L, R, W, diag):
-        check(_lib.lib().zmpo_hdiag(self.h, pid, device_ptr(L), device_ptr(R), device_ptr(W),
-                                    device_ptr(diag), current_stream()), "hdiag")
+        checked_call(lambda: _lib.lib().zmpo_hdiag(self.h, pid, device_ptr(L), device_ptr(R), device_ptr(W),
+                                                   device_ptr(diag), current_stream()), "hdiag")
 
     # -------------------------------------------------------------- renorm
     def renorm_plan(self, status, op_class, lay_env, lay_W, lay_site, off_env, off_W):
@@ -233,10 +248,10 @@ class Engine:
         return pid.value, lay_out, off_out, tot.value, ws.value
 
     def renorm(self, pid, env, W, site, out, workspace, precision="fp64"):
-        check(_lib.lib().zmpo_renorm(self.h, pid, device_ptr(env), device_ptr(W), device_ptr(site),
-                                     device_ptr(out),
-                                     device_ptr(workspace) if workspace is not None else None,
-                                     _lib.PREC[precision], current_stream()), "renorm")
+        ws = device_ptr(workspace) if workspace is not None else None
+        checked_call(lambda: _lib.lib().zmpo_renorm(self.h, pid, device_ptr(env), device_ptr(W), device_ptr(site),
+                                                    device_ptr(out), ws, _lib.PREC[precision],
+                                                    current_stream()), "renorm")
 
 
 def get(device=0):
