@@ -402,10 +402,17 @@ __device__ __forceinline__ double load_a(const Slot &sl, int row, bool scaled) {
 
 // ------------------------------------------------------------ prepare kernels
 // One A record per item (rows m0 .. m0+tm8-1, slots k0 .. k0+kc-1 of the
-// group): the row exponents over the window (two threads per row, eight
-// loads in flight each), then the four digit planes of tm8 rows of every k
-// block (a warp writes 8 rows x 4 chunks = 512 contiguous bytes of each
-// plane), then the 128 exponents after the planes.
+// group), 16 rows at a time: the raw FP64 values of the rows over the
+// window are staged in shared memory (threads laid along the rows when a
+// slot's rows are contiguous, along the slots otherwise, so the CTA's loads
+// cover each row's span together), the row exponents are taken there, and
+// the rows are cut from there into the four digit planes of every k block
+// (a warp writes 8 rows x 4 chunks = 512 contiguous bytes of each plane);
+// the 128 exponents follow the planes.  Every value is read once.
+constexpr int PREP_RB = 16;                   // rows per staging block
+// staging row pitch in float64: = 2 (mod 16), so the 16 lanes of a half warp
+// reading (4 rows x 4 chunks) in the cut meet at most 2-way bank conflicts
+constexpr int PREP_STRIDE = umma::KMAX + 2;
 __global__ void __launch_bounds__(umma::PREP_THREADS)
 k_prep_a(const PrepA *__restrict__ items, int64_t nitems, const Group *__restrict__ groups,
          const Seg *__restrict__ segs, Bufs bufs, unsigned char *__restrict__ planes) {
@@ -413,6 +420,7 @@ k_prep_a(const PrepA *__restrict__ items, int64_t nitems, const Group *__restric
   __shared__ Slot slots[KMAX];
   __shared__ int s_ctl[2];
   __shared__ int s_ea[TM];
+  extern __shared__ double stage[];  // PREP_RB x PREP_STRIDE
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int64_t it = blockIdx.x; it < nitems; it += gridDim.x) {
     const PrepA p = items[it];
@@ -425,43 +433,50 @@ k_prep_a(const PrepA *__restrict__ items, int64_t nitems, const Group *__restric
         s_ctl[1] = sc;
       }
     }
+    if (tid < TM) s_ea[tid] = 0;
     __syncthreads();
     const int K = s_ctl[0];
     const bool scaled = s_ctl[1] != 0;
-    const int nkb = (K + KB_SLOTS - 1) / KB_SLOTS;
+    const int nkb = (K + KB_SLOTS - 1) / KB_SLOTS, kpad = nkb * KB_SLOTS;
     const int tm8 = tile_rows8(g.M, p.m0), PL = tm8 * ROW_BYTES;
-    {
-      const int row = tid >> 1, half = tid & 1, grow = p.m0 + row;
-      int em = 0;
-      if (grow < g.M) {
-        for (int j0 = half; j0 < K; j0 += 16) {
-          double v[8];
-#pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            const int j = j0 + 2 * i;
-            v[i] = j < K ? load_a(slots[j], grow, scaled) : 0.0;
-          }
-#pragma unroll
-          for (int i = 0; i < 8; ++i) em = max(em, dexp(v[i]));
-        }
-      }
-      em = max(em, __shfl_xor_sync(0xffffffffu, em, 1));
-      if (half == 0) s_ea[row] = em;
-    }
-    __syncthreads();
+    // rows contiguous for a slot (unit row stride): threads along the rows
+    const bool rows_fast = K > 0 && slots[0].sam == 1;
     unsigned char *rec = planes + p.rec;
-    if (tid < TM) reinterpret_cast<int *>(rec + (int64_t)nkb * 4 * PL)[tid] = s_ea[tid];
-    for (int u = tid; u < nkb * tm8 * 4; u += PREP_THREADS) {
-      const int kb = u / (tm8 * 4), rem = u - kb * (tm8 * 4), row = rem >> 2, ch = rem & 3;
-      const int grow = p.m0 + row;
-      double v[8];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const int j = kb * KB_SLOTS + ch * 8 + i;
-        v[i] = (grow < g.M && j < K) ? load_a(slots[j], grow, scaled) : 0.0;
+    for (int rb = 0; rb < tm8; rb += PREP_RB) {
+      const int nr = min(PREP_RB, tm8 - rb);
+      for (int u = tid; u < nr * kpad; u += PREP_THREADS) {
+        int r, j;
+        if (rows_fast) {
+          r = u % nr;
+          j = u / nr;
+        } else {
+          j = u % kpad;
+          r = u / kpad;
+        }
+        const int grow = p.m0 + rb + r;
+        stage[r * PREP_STRIDE + j] = (j < K && grow < g.M) ? load_a(slots[j], grow, scaled) : 0.0;
       }
-      cut8_store(v, s_ea[row], rec + (int64_t)kb * 4 * PL, PL, row, ch);
+      __syncthreads();
+      {  // row exponents: 16 threads per row
+        const int r = tid >> 4, part = tid & 15;
+        int em = 0;
+        if (r < nr)
+          for (int j = part; j < kpad; j += 16) em = max(em, dexp(stage[r * PREP_STRIDE + j]));
+#pragma unroll
+        for (int o = 8; o >= 1; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o));
+        if (r < nr && part == 0) s_ea[rb + r] = em;
+      }
+      __syncthreads();
+      for (int u = tid; u < nkb * nr * 4; u += PREP_THREADS) {
+        const int ch = u & 3, q = u >> 2, r = q % nr, kb = q / nr;
+        double v[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] = stage[r * PREP_STRIDE + kb * KB_SLOTS + ch * 8 + i];
+        cut8_store(v, s_ea[rb + r], rec + (int64_t)kb * 4 * PL, PL, rb + r, ch);
+      }
+      __syncthreads();  // the staging block is refilled
     }
+    if (tid < TM) reinterpret_cast<int *>(rec + (int64_t)nkb * 4 * PL)[tid] = s_ea[tid];
     __syncthreads();  // the slot table and the exponents are rewritten by the next item
   }
 }
@@ -1036,7 +1051,8 @@ int launch_step_umma(const Step &s, const Bufs &b, unsigned char *planes, bool c
   const int64_t a0 = cut_kept ? 0 : s.nprep_a_kept, b0 = cut_kept ? 0 : s.nprep_b_kept;
   const int64_t na = s.nprep_a - a0, nb = s.nprep_b - b0;
   if (na > 0) {
-    k_prep_a<<<(int)(na < cap ? na : cap), umma::PREP_THREADS, 0, (cudaStream_t)stream>>>(
+    constexpr int stage_bytes = PREP_RB * PREP_STRIDE * (int)sizeof(double);
+    k_prep_a<<<(int)(na < cap ? na : cap), umma::PREP_THREADS, stage_bytes, (cudaStream_t)stream>>>(
         s.d_prep_a + a0, na, s.d_groups, s.d_segs, b, planes);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return record_cuda_error("k_prep_a", (int)e);
