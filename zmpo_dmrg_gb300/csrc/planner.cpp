@@ -1248,6 +1248,11 @@ static int upload_step_lists(Step &st) {
           w.pad = 0;
         }
   }
+  // long items that share a B-record sequence run one after another (their
+  // second and later reads of it come from L2)
+  for (int i = 0; i < 3; ++i)
+    std::stable_sort(UL.wl[i].begin(), UL.wl[i].end(),
+                     [](const UWork &x, const UWork &y) { return x.b_rec < y.b_rec; });
   // prepare items: kept ones first (a call that reuses them skips them)
   std::vector<PrepA> prep_a(UL.pa[1]);
   prep_a.insert(prep_a.end(), UL.pa[0].begin(), UL.pa[0].end());
