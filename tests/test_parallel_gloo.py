@@ -165,3 +165,27 @@ def test_two_rank_product_plans_sum_to_the_oracle_sigma():
     mp.spawn(_product_plan_worker, args=(2, _free_port(), case, x, out), nprocs=2, join=True)
     for r in range(2):
         assert numpy.linalg.norm(out[r] - ref) <= 1e-12 * numpy.linalg.norm(ref)
+
+
+def test_driver_partition_covers_every_term_once():
+    """mpo_dmrg.partition(rank, size): the ranks' operator terms are disjoint
+    contiguous blocks that together give every term (with and without spin
+    projection), with the matching weights."""
+    from zmpo_dmrg_gb300.mpo_dmrg_class import mpo_dmrg
+    for npts, sbas, size in [(None, 12, 2), (None, 20, 3), (None, 48, 8), (4, 12, 3)]:
+        seen = []
+        for rank in range(size):
+            m = mpo_dmrg()
+            m.nsite, m.sbas, m.isym = sbas // 2, sbas, 2
+            if npts:
+                m.npts = npts
+                m.qwts = numpy.arange(1.0, npts + 1.0)
+            m.partition(rank, size)
+            assert (m.rank, m.size) == (rank, size)
+            assert len(m.hpwts) == len(m.opers) == m.nops
+            if npts:
+                assert all(w == m.qwts[o[1]] for w, o in zip(m.hpwts, m.opers))
+            flat = [o[0] * (npts or 1) + (o[1] or 0) for o in m.opers]
+            assert flat == list(range(flat[0], flat[0] + len(flat))) if flat else True
+            seen += flat
+        assert sorted(seen) == list(range(sbas * (npts or 1)))

@@ -21,6 +21,7 @@ import time
 import numpy
 
 from . import mpo as _mpo
+from . import parallel
 from . import pdvdson
 from . import pgdvdson
 from . import prdm
@@ -165,6 +166,8 @@ class mpo_dmrg:
         # replay each site's H.psi launches from a CUDA graph
         self.use_graph = False
         self.rng = numpy.random.default_rng(seed)
+        # operator-term partition over ranks (partition())
+        self.rank, self.size, self.group = 0, 1, None
         # device state
         self.mpo_store = None
         self.pop_store = None
@@ -196,14 +199,23 @@ class mpo_dmrg:
         s2quad(self, sval, sz)
         return 0
 
-    def partition(self):
+    def partition(self, rank=None, size=None, group=None):
+        """This rank's operator terms H_p (mpo_dmrg_class.partition, 206-246;
+        tools/parallel_util.partitionSites): a contiguous block of the 2K
+        terms (npts * 2K with spin projection) per rank.  ``rank`` / ``size``
+        default to the torch.distributed process group (one rank without it).
+        With several ranks every sum over terms (H.psi, its diagonal, the
+        noise density matrix, the energy of an MPS) is summed over the ranks;
+        the Davidson subspace and the decimation are replicated."""
         if self.sbas is None:
             raise ValueError('sbas is not defined')
+        if rank is None or size is None:
+            rank, size = parallel.world(group)
+        self.rank, self.size, self.group = rank, size, group
+        self.opers = parallel.partition_ops(self.sbas, size, rank, self.npts)
         if self.npts is None:
-            self.opers = [[x, None] for x in range(self.sbas)]
-            self.hpwts = numpy.ones(self.sbas)
+            self.hpwts = numpy.ones(len(self.opers))
         else:
-            self.opers = [[x // self.npts, x % self.npts] for x in range(self.npts * self.sbas)]
             self.hpwts = numpy.array([self.qwts[x[1]] for x in self.opers])
         self.nops = len(self.opers)
         self.pidx = sorted(set(x[0] for x in self.opers))
@@ -386,6 +398,9 @@ class mpo_dmrg:
         fmps = self.flmps if fbra is None else fbra
         exphop = self.genHops(fmps, 'lop')
         esum = float(numpy.dot(self.hpwts, exphop))
+        if getattr(self, "size", 1) > 1:
+            t = _torch().tensor([esum], dtype=_torch().float64)
+            esum = float(parallel.allreduce_(t, self.group)[0])
         if self.ifs2proj:
             psum = float(numpy.dot(self.qwts, self.exppop))
             return esum / psum, esum, 1.0, psum
@@ -439,14 +454,18 @@ class mpo_dmrg:
                 raise RuntimeError('no basis in symmetry sector %s' % qkey)
             if self.ifprecond:
                 diag = HDiag(info, ndim0, prjmap)
+                if getattr(self, "size", 1) > 1:
+                    parallel.allreduce_(diag, self.group)
             else:
                 diag = torch.ones(ndim0, dtype=torch.float64, device="cuda")
+            # H.psi over this rank's terms, summed over the ranks
+            hvec = parallel.DistributedHVec(HVec, self.group) if getattr(self, "size", 1) > 1 else HVec
             if not self.ifs2proj:
                 solver = pdvdson.eigenSolver(self.rng)
-                solver.HVec = pdvdson.mask([info, ndim0, prjmap], HVec).matvec
+                solver.HVec = pdvdson.mask([info, ndim0, prjmap], hvec).matvec
             else:
                 solver = pgdvdson.eigenSolver(self.rng)
-                solver.HVec = pgdvdson.mask([info, ndim0, prjmap], HVec).matvec
+                solver.HVec = pgdvdson.mask([info, ndim0, prjmap], hvec).matvec
                 solver.SVec = pgdvdson.mask([info, ndim0, prjmap], SVec).matvec
             solver.crit_e = self.crit_e
             solver.crit_vec = self.crit_vec
@@ -467,7 +486,7 @@ class mpo_dmrg:
                 self.precision = self.precision_final
                 for i in range(neig):
                     v = vec[i].contiguous()
-                    hv = HVec(v, info, ndim0, prjmap)
+                    hv = hvec(v, info, ndim0, prjmap)
                     sv = SVec(v, info, ndim0, prjmap) if self.ifs2proj else v
                     eig[i] = float(torch.dot(v, hv) / torch.dot(v, sv))
                 self.precision = saved

@@ -7,7 +7,8 @@ its own environments and computes a partial H.psi over its terms; one sum over
 ranks per product (the reference's ``comm.Reduce``, tools/pdvdson.py:75) gives
 the full vector on every rank, so the Davidson subspace work is replicated
 instead of broadcast.  Renormalisation needs no communication.  On GPUs the sum
-is an NCCL all-reduce of the float64 vector.
+is an NCCL all-reduce of the float64 vector; with the gloo backend (CPU ranks,
+or ranks sharing a device) the vector goes through host memory.
 """
 
 
@@ -53,10 +54,40 @@ class DistributedHVec:
 
     def __call__(self, vec, *info):
         import torch
-        import torch.distributed as dist
         y = self.local(vec, *info)
         was_numpy = not isinstance(y, torch.Tensor)
         t = torch.as_tensor(y) if was_numpy else y
-        if dist.is_available() and dist.is_initialized() and dist.get_world_size(self.group) > 1:
-            dist.all_reduce(t, op=dist.ReduceOp.SUM, group=self.group)
+        allreduce_(t, self.group)
         return t.numpy() if was_numpy else t
+
+
+def world(group=None):
+    """(rank, size) of this process in ``group`` (0, 1 without torch.distributed)."""
+    try:
+        import torch.distributed as dist
+    except ImportError:
+        return 0, 1
+    if not (dist.is_available() and dist.is_initialized()):
+        return 0, 1
+    return dist.get_rank(group), dist.get_world_size(group)
+
+
+def allreduce_(t, group=None):
+    """Sum ``t`` (a torch tensor or a NumPy array) over the ranks of
+    ``group``, in place; a no-op on one rank.  Under the gloo backend a
+    device tensor is summed through a host copy."""
+    import torch
+    import torch.distributed as dist
+    rank, size = world(group)
+    if size <= 1:
+        return t
+    if not isinstance(t, torch.Tensor):
+        dist.all_reduce(torch.from_numpy(t), op=dist.ReduceOp.SUM, group=group)
+        return t
+    if t.is_cuda and dist.get_backend(group) == "gloo":
+        h = t.cpu()
+        dist.all_reduce(h, op=dist.ReduceOp.SUM, group=group)
+        t.copy_(h)
+    else:
+        dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+    return t

@@ -142,28 +142,34 @@ def pRDM(civecs, info):
             acc += buf3
     for ch in chains.values():
         ch.release(eng)
-    if acc is None:
-        return rho if on_device else rho.cpu().numpy()
-    # block structure of the summed T T^T (legs of the last contraction)
-    et = next(env.tensors[i] for i in range(dmrg.nops) if env.present(i))
-    qp = mpo.tensors[jsite][0].qsyms[2]
-    dp = mpo.tensors[jsite][0].ndims[2]
-    if status == 'L':
-        legs_q = [et.qsyms[1], qp, et.qsyms[1], qp]
-        legs_d = [et.ndims[1], dp, et.ndims[1], dp]
-    else:
-        qb = et.qsyms[1] - qkey[:et.qsyms[1].shape[1]]
-        legs_q = [qp, qb, qp, qb]
-        legs_d = [dp, et.ndims[1], dp, et.ndims[1]]
-    out = qtensor([False, False, True, True])
-    out.fromQsyms(4, legs_q, legs_d, ifallocate=False)
-    _, _, _, idlst2 = fromQnums(qn2)
-    if out.size_allowed != acc.numel():
-        raise RuntimeError("perturbed RDM layout mismatch")
-    # scatter the summed blocks into the dense (n, n) matrix on the device
     n = int(numpy.prod([len(x) for x in qn2[:2]]))
-    didx = torch.as_tensor(numpy.asarray(out.prjmap(idlst2), dtype=numpy.int64), device="cuda")
     noise_dense = torch.zeros(n * n, dtype=torch.float64, device="cuda")
-    noise_dense[didx] = acc
+    if acc is not None:
+        # block structure of the summed T T^T (legs of the last contraction)
+        et = next(env.tensors[i] for i in range(dmrg.nops) if env.present(i))
+        qp = mpo.tensors[jsite][0].qsyms[2]
+        dp = mpo.tensors[jsite][0].ndims[2]
+        if status == 'L':
+            legs_q = [et.qsyms[1], qp, et.qsyms[1], qp]
+            legs_d = [et.ndims[1], dp, et.ndims[1], dp]
+        else:
+            qb = et.qsyms[1] - qkey[:et.qsyms[1].shape[1]]
+            legs_q = [qp, qb, qp, qb]
+            legs_d = [dp, et.ndims[1], dp, et.ndims[1]]
+        out = qtensor([False, False, True, True])
+        out.fromQsyms(4, legs_q, legs_d, ifallocate=False)
+        _, _, _, idlst2 = fromQnums(qn2)
+        if out.size_allowed != acc.numel():
+            raise RuntimeError("perturbed RDM layout mismatch")
+        # scatter the summed blocks into the dense (n, n) matrix on the device
+        didx = torch.as_tensor(numpy.asarray(out.prjmap(idlst2), dtype=numpy.int64), device="cuda")
+        noise_dense[didx] = acc
+    if getattr(dmrg, "size", 1) > 1:
+        # the noise term sums over the operator terms of every rank (a rank
+        # may hold no term at this site: its share is zero)
+        from .parallel import allreduce_
+        allreduce_(noise_dense, dmrg.group)
+    elif acc is None:
+        return rho if on_device else rho.cpu().numpy()
     rho = rho + dmrg.noise * noise_dense.reshape(n, n)
     return rho if on_device else rho.cpu().numpy()
