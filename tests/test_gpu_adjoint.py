@@ -137,3 +137,20 @@ def test_rdm12_properties(converged):
     assert abs(g1.trace() - 6.0) < 1e-9
     assert numpy.abs(g1 - one).max() < 1e-8
     assert numpy.abs(g2 - two).max() < 1e-8
+
+
+def test_rdm1_matches_reference_brute_force(converged):
+    """The product's 1-RDM (site gradients of the H MPO through the adjoint
+    contractions) against the restatement of the reference's brute-force
+    eval_rdm1BF (an E_pq MPO per element, properties/mpo_dmrg_propsItrf.py:
+    204-263) on the same left-canonical MPS, element by element."""
+    from oracle.properties import eval_rdm1BF
+    from zmpo_dmrg_gb300 import properties
+    m, K = converged["m"], converged["K"]
+    sites = []
+    for i in range(K):
+        t = m.flmps['site%d' % i]
+        sites.append(t.toDenseTensor(t.idlst) if hasattr(t, "toDenseTensor") else numpy.asarray(t))
+    ref_t, _ = eval_rdm1BF(sites)
+    got = properties.rdm1(m, converged["h"], converged["eri"])
+    assert numpy.abs(got - ref_t).max() < 1e-10

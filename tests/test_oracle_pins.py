@@ -222,3 +222,32 @@ def test_spin_projected_kernels_equal_dense_operators():
     eye = numpy.eye(P.ndim0)
     sd_ref = numpy.array([down(Pd @ up(eye[i]))[i] for i in range(P.ndim0)])
     assert numpy.abs(sd - sd_ref).max() < 1e-10
+
+
+def test_rdm1_brute_force_restatement_equals_fock_space():
+    """The restated eval_rdm1BF (reference properties/mpo_dmrg_propsItrf.py:
+    204-263) on a random left-canonical MPS equals <psi|a+_p a_q|psi> from the
+    Jordan-Wigner operators of the Fock space."""
+    from oracle import properties as op
+    rng = numpy.random.default_rng(8)
+    K, D = 4, 6
+    dims = [1] + [min(4 ** i, 4 ** (K - i), D) for i in range(1, K)] + [1]
+    sites = []
+    for i in range(K):
+        a = rng.standard_normal((dims[i] * 4, dims[i + 1]))
+        q, _ = numpy.linalg.qr(a)
+        sites.append(q.reshape(dims[i], 4, dims[i + 1]))
+    psi = op.mps_to_fock(sites)
+    assert abs(psi @ psi - 1.0) < 1e-12
+    a = integrals._jw_ops(2 * K)
+    ref_t = numpy.zeros((K, K))
+    ref_s = numpy.zeros((K, K))
+    for p in range(K):
+        for q in range(K):
+            al = psi @ (a[2 * p].T @ (a[2 * q] @ psi))
+            be = psi @ (a[2 * p + 1].T @ (a[2 * q + 1] @ psi))
+            ref_t[p, q] = al + be
+            ref_s[p, q] = 0.5 * (al - be)
+    got_t, got_s = op.eval_rdm1BF(sites)
+    assert numpy.abs(got_t - ref_t).max() < 1e-12
+    assert numpy.abs(got_s - ref_s).max() < 1e-12
