@@ -39,13 +39,6 @@ LARGE_WORKSPACE = 64e9
 # the spin-projected configuration: singlet projection with 8 Gauss-Legendre
 # points (320 terms [p, g]), H.psi with the N-only relabelling
 SPCFG = dict(K=20, nelec=20, D=512, isite=9, seed=2024, npts=8, sval=0.0)
-# DRAM bytes (read + write) over algorithmic bytes of the T3 step, measured
-# with ncu (dram__bytes_read.sum + dram__bytes_write.sum of every split-path
-# launch in the step's NVTX range, 18 executions) on the K=16, D=256 two-site
-# dot: 2.334 GB per execution against 1.930 GB algorithmic.  The full-size
-# traffic is this ratio times the step's algorithmic bytes (the step's traffic
-# grows with the operand and output sizes).
-T3_TRAFFIC_RATIO = 2.334 / 1.930
 METRIC = "sweep s & sigma-vec TFLOP/s, split-BF16 vs FP64 on 1 GB300 at ΔE≤1e-8 Eh"
 
 
@@ -707,25 +700,27 @@ def main():
         "gpu_launches": args.steps * sum(eng.kernel_count(pid, args.precision) for pid in plan.pids),
         "clocks": clocks_rec,
         "launches": launches,
-        "roofline": {"bound": "hbm", "kernel": "tensor-core kernels (k_step_tcb, k_step_tc) of step %d of %d" %
-                               (top, plan.nlaunch),
+        "roofline": {"bound": "hbm",
+                     "kernel": "step %d of %d: prepare kernels (k_prep_a / k_prep_b), tcgen05 kernels "
+                               "(k_step_umma / k_step_umma_long), split-K sum" % (top, plan.nlaunch),
                      "achieved": launches[top]["GBs"], "peak": hbm, "unit": "GB/s",
                      "frac": (launches[top]["GBs"] or 0.0) / hbm,
-                     "traffic": (T3_TRAFFIC_RATIO * launches[top]["alg_bytes"] / len(plan.pids)
-                                 if top == 2 and args.precision == "split" else None),
-                     "traffic_note": "bytes per launch of the step, scaled from the ncu capture of the K=16 D=256 "
-                                     "dot (ratio %.3f to algorithmic bytes)" % T3_TRAFFIC_RATIO,
+                     "traffic": None,
+                     "traffic_note": "DRAM bytes of the step's kernels: see the ncu summaries (profiles/); the "
+                                     "algorithmic bytes count every operand tensor read once and every output "
+                                     "written once",
                      "peak_source": peak_kind},
-        # the tensor-pipe view of the same step: BF16 digit products actually
-        # issued (products per multiply-add x the step's tile multiply-adds)
-        # over the measured sustained bf16 GEMM rate
-        "roofline_tensor": {"bound": "tensor", "kernel": "tensor-core kernels of step %d" % top,
+        # the tensor-pipe view of the same step: BF16 digit products the
+        # tcgen05 MMAs issue (10 per FP64 multiply-add, 128-row tiles and
+        # 16-slot steps included) over the measured sustained bf16 GEMM rate
+        "roofline_tensor": {"bound": "tensor", "kernel": "tcgen05 kernels of step %d" % top,
                             "achieved": 2.0 * products * macs[top] / (ms[top] * 1e-3) / 1e12 if ms[top] > 0 else None,
                             "peak": bf16, "unit": "TFLOP/s",
                             "frac": (2.0 * products * macs[top] / (ms[top] * 1e-3) / 1e12 / bf16) if ms[top] > 0 else None,
                             "executed_flops_per_launch": 2.0 * products * macs[top] / len(plan.pids),
-                            "note": "mma.sync m16n8k16 BF16 digit products (%d per FP64 multiply-add), tile padding "
-                                    "included; peak = cuBLAS bf16 sustained" % products,
+                            "note": "tcgen05.mma kind::f16 BF16 digit products (%d per FP64 multiply-add), tile "
+                                    "padding included, over the step's whole time (prepare kernels included); "
+                                    "peak = cuBLAS bf16 sustained" % products,
                             "peak_source": peak_kind} if args.precision != "fp64" else None,
     }
     if world > 1:
