@@ -80,6 +80,23 @@ def test_renorm(gpu, case, status):
             assert numpy.abs(x - y).max() <= 1e-12 * max(1.0, numpy.abs(y).max())
 
 
+@pytest.mark.parametrize("case", CASES[1:])
+@pytest.mark.parametrize("status", ["L", "R"])
+@pytest.mark.parametrize("precision,tol", [("emu64", 1e-12), ("split", 1e-8)])
+def test_renorm_tensor_core_paths(gpu, case, status, precision, tol):
+    """The renormalisation in the 56-bit emulation and the split precision
+    (relative to the largest element of each new environment)."""
+    P = prob(case)
+    a = product_renorm(P, status, precision)
+    b = oracle_renorm(P, status)
+    P.p.precision_renorm = "fp64"
+    assert len(a) == len(b)
+    for x, y in zip(a, b):
+        assert x.shape == y.shape
+        if y.size:
+            assert numpy.abs(x - y).max() <= tol * max(1.0, numpy.abs(y).max())
+
+
 def test_sigma_deterministic(gpu):
     P = prob(CASES[1])
     x = numpy.random.default_rng(9).standard_normal(P.ndim0)
