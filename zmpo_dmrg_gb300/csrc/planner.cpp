@@ -1248,11 +1248,23 @@ static int upload_step_lists(Step &st) {
           w.pad = 0;
         }
   }
-  // long items that share a B-record sequence run one after another (their
-  // second and later reads of it come from L2)
-  for (int i = 0; i < 3; ++i)
-    std::stable_sort(UL.wl[i].begin(), UL.wl[i].end(),
-                     [](const UWork &x, const UWork &y) { return x.b_rec < y.b_rec; });
+  // long items: groups whose first column tile shares a B-record sequence
+  // run one after another, and a group's column tiles next to each other (the
+  // repeated reads of a shared B sequence, and of a group's A records, come
+  // from L2)
+  {
+    std::unordered_map<int, int64_t> first_b;
+    for (int i = 2; i >= 0; --i)
+      for (const UWork &w : UL.wl[i]) {
+        auto it = first_b.find(w.group);
+        if (it == first_b.end() || w.b_rec < it->second) first_b[w.group] = w.b_rec;
+      }
+    for (int i = 0; i < 3; ++i)
+      std::stable_sort(UL.wl[i].begin(), UL.wl[i].end(), [&](const UWork &x, const UWork &y) {
+        const int64_t bx = first_b[x.group], by = first_b[y.group];
+        return bx != by ? bx < by : x.group < y.group;
+      });
+  }
   // prepare items: kept ones first (a call that reuses them skips them)
   std::vector<PrepA> prep_a(UL.pa[1]);
   prep_a.insert(prep_a.end(), UL.pa[0].begin(), UL.pa[0].end());
