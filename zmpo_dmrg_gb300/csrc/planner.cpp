@@ -1031,7 +1031,9 @@ static void umma_add_group(UmmaLists &L, const Step &st, int g, const Group &G, 
   const int32_t sides = ka | (kb << 1);
   std::vector<int64_t> key;
   for (int n0 = 0; n0 < G.N;) {
-    const int tn = umma_tn(G.N - n0), ti = umma_ti(tn);
+    // long groups wider than one tile take 64-column tiles only, so their
+    // tiles run in one launch next to each other (A re-read from L2)
+    const int tn = (!one && G.N > 64) ? 64 : umma_tn(G.N - n0), ti = umma_ti(tn);
     int64_t brec = -1;
     if (G.ncb == 0) {
       b_seq_key(st, G, kbase, K, n0, tn, key);
