@@ -220,46 +220,6 @@ MPI_NOTE = ("the reference's MPI operator partition (mpirun over mpi4py) is unav
             "mpi4py and an MPI launcher are absent; one process with multithreaded BLAS on every host core")
 
 
-def sweep_metrics(K=10, nelec=10, D=64, nsweep=10, seed=2024):
-    """Seconds per two-site sweep of the GPU driver on the small configuration
-    (K=10, 10 electrons, Sz=0, D=64, seeded synthetic integrals) with the
-    reference's default two-site schedule (M ramp, perturbed density-matrix
-    noise 1e-4 in the first sweeps, convergence 1e-9, at most 10 sweeps), FP64
-    vs split path, and the difference of their converged energies."""
-    import torch
-    from zmpo_dmrg_gb300 import integrals as I
-    from zmpo_dmrg_gb300.mpo_dmrg_class import mpo_dmrg
-    from zmpo_dmrg_gb300.mpo_dmrg_schedule import schedule
-    h, eri, _ = I.synthetic(K, seed)
-    i1, i2 = I.spin_orbital(h, eri)
-    out = {"workload": "K=%d N=%d Sz=0 D=%d, default two-site schedule (noise 1e-4, tol 1e-9, <= %d "
-                       "sweeps) from the Aufbau product state" % (K, nelec, D, nsweep)}
-    for prec in ("fp64", "split"):
-        m = mpo_dmrg(seed=1)
-        m.nsite, m.sbas, m.isym = K, 2 * K, 2
-        m.build()
-        m.occun = I.closed_shell_occun(K, nelec)
-        m.qsectors = {str([float(nelec), 0.0]): 1}
-        m.precision = prec
-        m.precision_renorm = "emu64" if prec == "split" else "fp64"
-        m.use_graph = False  # graph replay measured no faster here (1.30 vs 1.34 s per split sweep)
-        m.partition()
-        m.loadInts((i1, i2))
-        m.dumpMPO()
-        sc = schedule(maxM=D, tol=1e-9, maxiter=nsweep)
-        sc.normal(2)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        m.default(sc)
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        out[prec] = {"s_per_sweep": dt / max(m.nsweep, 1), "sweeps": m.nsweep, "energy": float(m.Energy),
-                     "converged": bool(m.ifconv), "matvecs": int(sum(m.nmvp))}
-    out["dE_split_fp64"] = abs(out["split"]["energy"] - out["fp64"]["energy"])
-    out["sweep_speedup_split_vs_fp64"] = out["fp64"]["s_per_sweep"] / out["split"]["s_per_sweep"]
-    return out
-
-
 def gradient_metrics(K=16, nelec=16, D=256, seed=2024):
     """Energy gradient (dE/dh1e, dE/d(pq|rs)) at a seeded random left-canonical
     MPS of K=16, 16 electrons, D=256 (the adjoint configuration's sizes; the
@@ -312,113 +272,55 @@ def gradient_metrics(K=16, nelec=16, D=256, seed=2024):
             "fd_directional": fd, "adjoint_directional": an, "abs_diff": abs(fd - an)}
 
 
-def sweep_large(K=24, nelec=24, D=512, seed=2024):
-    """One right-to-left two-site sweep (K-1 dots) at K=24, 24 electrons,
-    D=512 from the same seeded random left-canonical MPS, FP64 vs split
-    (schedule: D=512, Davidson crit_e 1e-9, no noise): seconds, matvecs and
-    the energies reached."""
+def sweep_converged(K=24, nelec=24, D=512, seed=2024, maxiter=14, tol=1e-8, hop=1.0):
+    """Sweep seconds of the split path against the FP64 path at the same
+    converged state (K=24, 24 electrons, Sz=0, D=512 by default).
+
+    Phase 1: the reference's default two-site schedule (mpo_dmrg_schedule
+    normal(2): bond dimension ramp from 1.5 sqrt(D), density-matrix noise
+    1e-4 in the ramp, Davidson tolerance 1e-4 down to 1e-9) from the
+    occupation-number state, split precision, until the schedule's
+    convergence test (energy change below ``tol`` after the ramp) or
+    ``maxiter`` sweep pairs.  Phase 2: from that MPS (environments rebuilt
+    from it for each arm, so both arms start from identical states), one FP64
+    sweep pair and one split sweep pair at D, Davidson 1e-9, no noise, each
+    timed alone: seconds per sweep pair and half sweep, matvecs, energies,
+    their difference, and whether each arm stayed within ``tol`` of the
+    phase-1 energy.  (The noisy ramp amplifies any perturbation, even one of
+    1e-15 in an environment, into a different truncation, so two runs of the
+    whole schedule are compared only through this common state.)"""
     import torch
-    from tests.problems import bond_structure, random_left_site, QPHYS
     from zmpo_dmrg_gb300 import integrals as I
     from zmpo_dmrg_gb300.mpo_dmrg_class import mpo_dmrg
     from zmpo_dmrg_gb300.mpo_dmrg_schedule import schedule
-    from zmpo_dmrg_gb300.qtensor import qtensor
-    h, eri, _ = I.synthetic(K, seed)
-    ints = I.spin_orbital(h, eri)
-    out = {"workload": "K=%d N=%d Sz=0 D=%d, one right-to-left two-site sweep (%d dots) from a seeded random "
-                       "left-canonical MPS, Davidson crit_e 1e-9, no noise" % (K, nelec, D, K - 1)}
-    for prec in ("split", "fp64"):
-        rng = numpy.random.default_rng(seed)
-        qnuml, _ = bond_structure(K, nelec, 0.0, D, rng)
-        qnuml[K] = numpy.array([[float(nelec), 0.0]])
-        m = mpo_dmrg(seed=1)
-        m.nsite, m.sbas, m.isym = K, 2 * K, 2
-        m.build()
-        m.qsectors = {str([float(nelec), 0.0]): 1}
-        m.initStates()
-        m.precision = prec
-        # the split configuration renormalises with the 7-slice emulation
-        # (~2^-56 relative), the FP64 configuration with FP64
-        m.precision_renorm = "emu64" if prec == "split" else "fp64"
-        m.partition()
-        m.loadInts(ints)
-        m.dumpMPO()
-        fmps = {'nsite': K}
-        for i in range(K):
-            t = qtensor([False, False, True])
-            t.fromDenseTensor(random_left_site(qnuml[i], qnuml[i + 1], rng), [qnuml[i], QPHYS, qnuml[i + 1]])
-            fmps['site%d' % i] = t
-        for i in range(K + 1):
-            fmps['qnum%d' % i] = qnuml[i]
-        m.flmps = {'nsite': K, 'qnum0': qnuml[0]}
-        m.frmps = {'nsite': K, 'qnum%d' % K: m.qnumr[-1]}
-        m.qnuml = [numpy.asarray(fmps['qnum%d' % i]) for i in range(K + 1)]
-        m.flmps.update(fmps)
-        m.initOps(fmps)
-        m.psi0 = None
-        sc = schedule(maxM=D, tol=1e-9, maxiter=1)
-        sc.fixed(ncsite=2, maxM=D, tol=1e-9, maxiter=1, noise=0.0)
-        sc.getParameters(m, 0)
-        m.crit_e = 1e-9
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        r = m.sweep(list(range(K)), 2, 'R')
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        tdav = sum(x[2] for x in m.timings)
-        tren = sum(x[3] for x in m.timings)
-        out[prec] = {"s_per_half_sweep": dt, "s_local_solver": tdav, "s_renorm": tren, "matvecs": int(r[0]),
-                     "energy": float(r[2]), "energy_first_dot": float(numpy.asarray(r[4][0]).ravel()[0])}
-        del m
-        torch.cuda.empty_cache()
-    out["dE_split_fp64"] = abs(out["split"]["energy"] - out["fp64"]["energy"])
-    # the first dot sees identical environments in both runs: its energy
-    # difference is the precision effect alone; later dots inherit different
-    # truncations of a far-from-converged random state
-    out["dE_first_dot"] = abs(out["split"]["energy_first_dot"] - out["fp64"]["energy_first_dot"])
-    out["speedup_split_vs_fp64"] = out["fp64"]["s_per_half_sweep"] / out["split"]["s_per_half_sweep"]
-    return out
-
-
-def sweep_converged(K=24, nelec=24, D=512, seed=2024, max_pairs=6, tol=1e-8):
-    """Sweep seconds at K=24, 24 electrons, Sz=0, D=512 (the split-vs-FP64
-    configuration).  Phase 1: split-precision two-site sweep pairs (right,
-    then left; D=512, Davidson crit_e 1e-9, no noise) from a seeded random
-    left-canonical MPS until the energy changes by less than ``tol`` between
-    pairs.  Phase 2: from that converged MPS (environments rebuilt from it for
-    each arm, so both arms start from identical states), one FP64 sweep pair
-    and one split sweep pair, timed alone; reported: seconds per sweep pair
-    and per half sweep, matvecs, energies, their difference, and whether each
-    arm stayed within ``tol`` of the converged energy."""
-    import torch
-    from tests.problems import bond_structure, random_left_site, QPHYS
-    from zmpo_dmrg_gb300 import integrals as I
-    from zmpo_dmrg_gb300.mpo_dmrg_class import mpo_dmrg
-    from zmpo_dmrg_gb300.mpo_dmrg_schedule import schedule
-    from zmpo_dmrg_gb300.qtensor import qtensor
-    h, eri, _ = I.synthetic(K, seed)
-    rng = numpy.random.default_rng(seed)
-    qnuml, _ = bond_structure(K, nelec, 0.0, D, rng)
-    qnuml[K] = numpy.array([[float(nelec), 0.0]])
-    fmps = {'nsite': K}
-    for i in range(K):
-        t = qtensor([False, False, True])
-        t.fromDenseTensor(random_left_site(qnuml[i], qnuml[i + 1], rng), [qnuml[i], QPHYS, qnuml[i + 1]])
-        fmps['site%d' % i] = t
-    for i in range(K + 1):
-        fmps['qnum%d' % i] = qnuml[i]
+    h, eri, _ = I.synthetic(K, seed, hop)
     m = mpo_dmrg(seed=1)
     m.nsite, m.sbas, m.isym = K, 2 * K, 2
     m.build()
+    m.occun = I.closed_shell_occun(K, nelec)
     m.qsectors = {str([float(nelec), 0.0]): 1}
-    m.initStates()
+    m.precision, m.precision_renorm = "split", "emu64"
     m.partition()
     m.loadInts(I.spin_orbital(h, eri))
     m.dumpMPO()
-    sc = schedule(maxM=D, tol=1e-9, maxiter=1)
-    sc.fixed(ncsite=2, maxM=D, tol=1e-9, maxiter=1, noise=0.0)
-
-    def start(mps, prec):
+    out = {"workload": "K=%d N=%d Sz=0 D=%d: default two-site schedule from the occupation-number state (split "
+                       "precision), then one sweep pair (right + left, %d dots each, Davidson 1e-9, no noise) per "
+                       "arm from the same converged MPS" % (K, nelec, D, K - 1)}
+    sc = schedule(maxM=D, tol=tol, maxiter=maxiter)
+    sc.normal(2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    m.default(sc)
+    torch.cuda.synchronize()
+    out["converge"] = {"s": time.perf_counter() - t0, "sweeps": m.nsweep, "converged": bool(m.ifconv),
+                       "energy": float(m.Energy), "energies": [float(e) for e in m.eav],
+                       "matvecs": int(sum(m.nmvp))}
+    e_conv = float(m.Energy)
+    mps = {k: v for k, v in m.flmps.items() if k.startswith('site') or k.startswith('qnum')}
+    mps['nsite'] = K
+    fixed = schedule(maxM=D, tol=1e-9, maxiter=1)
+    fixed.fixed(ncsite=2, maxM=D, tol=1e-9, maxiter=1, noise=0.0)
+    for prec in ("fp64", "split"):
         m.precision = prec
         m.precision_renorm = "emu64" if prec == "split" else "fp64"
         m.flmps = {'nsite': K, 'qnum0': m.qnuml[0]}
@@ -427,42 +329,18 @@ def sweep_converged(K=24, nelec=24, D=512, seed=2024, max_pairs=6, tol=1e-8):
         m.flmps.update(mps)
         m.initOps(mps)
         m.psi0 = None
-        sc.getParameters(m, 0)
+        fixed.getParameters(m, 0)
         m.crit_e = 1e-9
-
-    def pair():
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         r1 = m.sweep(list(range(K)), 2, 'R')
         r2 = m.sweep(list(range(K)), 2, 'L')
         torch.cuda.synchronize()
-        return time.perf_counter() - t0, min(float(r1[2]), float(r2[2])), int(r1[0] + r2[0])
-
-    def snapshot():
-        mps = {k: v for k, v in m.flmps.items() if k.startswith('site') or k.startswith('qnum')}
-        mps['nsite'] = K
-        return mps
-
-    out = {"workload": "K=%d N=%d Sz=0 D=%d, two-site sweep pairs (right + left, %d dots each), Davidson crit_e "
-                       "1e-9, no noise; converged by split sweeps from a seeded random left-canonical MPS, then one "
-                       "sweep pair per arm from the same converged MPS" % (K, nelec, D, K - 1)}
-    start(fmps, "split")
-    hist, eold, conv = [], None, False
-    for _ in range(max_pairs):
-        dt, e, nmv = pair()
-        hist.append({"s": dt, "energy": e, "matvecs": nmv})
-        if eold is not None and abs(e - eold) < tol:
-            conv = True
-            break
-        eold = e
-    out["converge"] = {"pairs": hist, "converged": conv, "energy": hist[-1]["energy"]}
-    e_conv = hist[-1]["energy"]
-    mps = snapshot()
-    for prec in ("fp64", "split"):
-        start(mps, prec)
-        dt, e, nmv = pair()
-        out[prec] = {"s_per_sweep": dt, "s_per_half_sweep": dt / 2, "energy": e, "matvecs": nmv,
-                     "converged": abs(e - e_conv) < tol}
+        dt = time.perf_counter() - t0
+        e = min(float(r1[2]), float(r2[2]))
+        out[prec] = {"s_per_sweep": dt, "s_per_half_sweep": dt / 2, "energy": e, "matvecs": int(r1[0] + r2[0]),
+                     "converged": bool(out["converge"]["converged"]) and abs(e - e_conv) < tol,
+                     "dE_vs_converged": e - e_conv}
     out["dE_split_fp64"] = abs(out["split"]["energy"] - out["fp64"]["energy"])
     out["sweep_speedup_split_vs_fp64"] = out["fp64"]["s_per_sweep"] / out["split"]["s_per_sweep"]
     del m
@@ -520,10 +398,8 @@ def main():
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--small", action="store_true", help="K=12, D=128 case (profiling)")
     ap.add_argument("--medium", action="store_true", help="K=16, D=256 case (profiling)")
-    ap.add_argument("--sweep-large", action="store_true",
-                    help="also time one two-site sweep at K=24, D=512 (split vs FP64)")
-    ap.add_argument("--gradient", action="store_true",
-                    help="also time the energy gradient at K=16, D=256 (adjoint configuration)")
+    ap.add_argument("--no-gradient", action="store_true",
+                    help="skip the energy-gradient timing at K=16, D=256 (adjoint configuration)")
     ap.add_argument("--sp", action="store_true",
                     help="spin-projected H.psi, K=20, D=512, 8 quadrature points (terms in batches)")
     ap.add_argument("--large", action="store_true",
@@ -728,11 +604,9 @@ def main():
                                            "all-reduce of sigma per step" % world)
     if rank == 0 and not args.no_sweep:
         result["sweep"] = sweep_converged()
-        result["sweep_k10"] = sweep_metrics()
-    if rank == 0 and args.gradient:
+        result["sweep_k10"] = sweep_converged(K=10, nelec=10, D=64, maxiter=16)
+    if rank == 0 and not args.no_gradient and not (args.small or args.medium or args.large or args.sp):
         result["gradient"] = gradient_metrics()
-    if rank == 0 and args.sweep_large:
-        result["sweep_large"] = sweep_large()
     if rank == 0 and not args.no_cpu and not (args.large or args.sp):
         result["cpu_baseline"], result["parity_vs_oracle"] = cpu_leg(P, cfg)
     if rank == 0:
