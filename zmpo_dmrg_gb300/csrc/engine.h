@@ -144,10 +144,10 @@ struct Step {
   int64_t nwork_ul[3] = {};
   bool split_done = false;          // split-K parts made (split_long_groups)
   int64_t nprep_a_kept = 0, nprep_b_kept = 0;  // the first items cut kept records
-  // plane buffer of the step: a kept area (records of the operands in
-  // keep_bufs, which stay fixed between calls) and a per-call area, byte
-  // offsets from the buffer's base
-  uint32_t keep_bufs = 0;
+  // plane buffer of the step: a kept area (records of the operand sides in
+  // keep_side -- bit 0 A, bit 1 B -- which stay fixed between calls) and a
+  // per-call area, byte offsets from the buffer's base
+  uint8_t keep_side = 0;
   int64_t plane_keep_off = 0, plane_keep_bytes = 0;
   int64_t plane_call_off = 0, plane_call_bytes = 0;
   int64_t plane_bytes = 0;          // the whole buffer

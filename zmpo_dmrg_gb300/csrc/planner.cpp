@@ -923,15 +923,14 @@ static int64_t group_k(const Step &st, const Group &G) {
 }
 
 // Records and work items of the tcgen05 groups of a step.  A group side
-// (A or B) whose operand buffers are all in the step's keep_bufs mask has
-// its records in the step's kept area (records of operands that stay fixed
+// (A or B) that the step's keep_side marks (bit 0: A, bit 1: B) has its
+// records in the step's kept area (records of operands that stay fixed
 // between calls, which a caller may let the next call reuse), every other
 // side in the per-call area.  Each area holds its A records, then (from a
 // 256-byte aligned offset) its B records.  With make = false only the byte
 // totals are counted (the plan-time estimate).
 struct UmmaLists {
   bool make = true;
-  uint32_t keep_bufs = 0;
   std::vector<PrepA> pa[2];          // [per-call, kept]; rec relative to its part
   std::vector<PrepB> pb[2];
   std::vector<UWork> w1[3], wl[3];   // one-pass / long items by column tile; pad = kept sides
@@ -995,15 +994,7 @@ static void column_map(const Step &st, const Group &G, int n0, int tn, std::vect
 
 constexpr int kUmmaRunMax = 16;      // row tiles of a one-pass work item
 
-static bool side_kept(const Step &st, const Group &G, bool a_side, uint32_t mask) {
-  if (!mask || G.nseg <= 0) return false;
-  for (int i = 0; i < G.nseg; ++i) {
-    const Seg &sg = st.segs[G.seg0 + i];
-    const int buf = a_side ? sg.abuf : sg.bbuf;
-    if (buf < 0 || buf >= 32 || !((mask >> buf) & 1u)) return false;
-  }
-  return true;
-}
+static bool side_kept(const Step &st, bool a_side) { return (st.keep_side >> (a_side ? 0 : 1)) & 1u; }
 
 // kbase: the group's first slot in G's segments (a split-K part counted
 // before the split: G is the whole group)
@@ -1079,7 +1070,7 @@ static void umma_plane_bytes(const Step &st, int64_t *keep, int64_t *call) {
   L.make = false;
   for (const Group &G : st.groups) {
     const int64_t k = group_k(st, G);
-    const bool ka = side_kept(st, G, true, st.keep_bufs), kb = side_kept(st, G, false, st.keep_bufs);
+    const bool ka = side_kept(st, true), kb = side_kept(st, false);
     if (!st.split_done && k > kSplitK && G.M > 0 && G.N > 0) {
       Group part = G;
       part.cbuf = kPartialBuf;
@@ -1095,15 +1086,20 @@ static void umma_plane_bytes(const Step &st, int64_t *keep, int64_t *call) {
 
 // Sigma plans: one plane region at the end of the workspace: the kept
 // areas of the steps one after another, then one per-call area shared by
-// the steps (they run one after another).  Records of the environments and
-// the MPO (buffers 0, 1, 2), which stay fixed while a Davidson solve calls
-// the plan, are kept.  Other plans (renormalisation, which runs in FP64 or
-// the 7-slice emulation, and contractions) keep nothing and get a step-owned
+// the steps (they run one after another).  The records of operands that
+// stay fixed while a Davidson solve calls the plan are kept: the
+// environments, the MPO and, two-site, the MPO product O that step 0
+// writes (keep_side per step, bit 0 = A, bit 1 = B; two-site: O = Wi Wj,
+// T1 = L psi, T3 = T1 O, sigma = T3 R; one-site: T1 = L psi, T2 = T1 W,
+// sigma = T2 R).  Other plans (renormalisation, which runs in FP64 or the
+// 7-slice emulation, and contractions) keep nothing and get a step-owned
 // buffer at their first split-precision run.
-static void reserve_plane_region(Plan *P) {
+static void reserve_plane_region(Plan *P, int ncsite) {
+  static const uint8_t kTwo[4] = {3, 1, 2, 2}, kOne[3] = {1, 2, 2};
   int64_t keep_total = 0, call_max = 0;
   for (auto &st : P->steps) {
-    st.keep_bufs = 0x7u;
+    const size_t i = (size_t)st.idx;
+    st.keep_side = ncsite == 2 ? (i < 4 ? kTwo[i] : 0) : (i < 3 ? kOne[i] : 0);
     int64_t keep, call;
     umma_plane_bytes(st, &keep, &call);
     st.plane_keep_off = keep_total;
@@ -1165,8 +1161,7 @@ static int upload_step_lists(Step &st) {
       }
     // tcgen05 groups (records cut by the prepare kernels)
     const double macs0 = UL.macs;
-    umma_add_group(UL, st, g, G, 0, ktot[g], side_kept(st, G, true, st.keep_bufs),
-                   side_kept(st, G, false, st.keep_bufs));
+    umma_add_group(UL, st, g, G, 0, ktot[g], side_kept(st, true), side_kept(st, false));
     const bool routed = UL.macs != macs0;
     st.mma_macs[1] += UL.macs - macs0;
     // Tensor-core tiles.  Columns: full pieces of the widest tile, then one
@@ -1831,7 +1826,7 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
       P->exec_flops += st.flops;
       P->ntasks += st.ntasks;
     }
-    reserve_plane_region(P.get());
+    reserve_plane_region(P.get(), d->ncsite);
   }
   // ---- HDiag terms: out[l,r] += w * sum Ld[a,l] Wi[a,b] (Wj[b,c]) Rd[c,r]
   {
