@@ -272,7 +272,7 @@ def gradient_metrics(K=16, nelec=16, D=256, seed=2024):
             "fd_directional": fd, "adjoint_directional": an, "abs_diff": abs(fd - an)}
 
 
-def sweep_converged(K=24, nelec=24, D=512, seed=2024, maxiter=14, tol=1e-8, hop=1.0):
+def sweep_converged(K=24, nelec=24, D=512, seed=2024, maxiter=14, tol=1e-8, hop=1.0, phases=True):
     """Sweep seconds of the split path against the FP64 path at the same
     converged state (K=24, 24 electrons, Sz=0, D=512 by default).
 
@@ -331,6 +331,10 @@ def sweep_converged(K=24, nelec=24, D=512, seed=2024, maxiter=14, tol=1e-8, hop=
         m.psi0 = None
         fixed.getParameters(m, 0)
         m.crit_e = 1e-9
+        # seconds per phase of the dots (plan building, diagonal, Davidson,
+        # final Rayleigh quotient, decimation, guess, renormalisation ...);
+        # each phase boundary synchronises the device
+        m.phase_times = {} if phases else None
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         r1 = m.sweep(list(range(K)), 2, 'R')
@@ -341,6 +345,9 @@ def sweep_converged(K=24, nelec=24, D=512, seed=2024, maxiter=14, tol=1e-8, hop=
         out[prec] = {"s_per_sweep": dt, "s_per_half_sweep": dt / 2, "energy": e, "matvecs": int(r1[0] + r2[0]),
                      "converged": bool(out["converge"]["converged"]) and abs(e - e_conv) < tol,
                      "dE_vs_converged": e - e_conv}
+        if phases:
+            out[prec]["phases_s"] = {k: round(v, 4) for k, v in sorted(m.phase_times.items(), key=lambda kv: -kv[1])}
+        m.phase_times = None
     out["dE_split_fp64"] = abs(out["split"]["energy"] - out["fp64"]["energy"])
     out["sweep_speedup_split_vs_fp64"] = out["fp64"]["s_per_sweep"] / out["split"]["s_per_sweep"]
     del m

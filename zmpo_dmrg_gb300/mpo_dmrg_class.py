@@ -26,7 +26,7 @@ from . import pdvdson
 from . import pgdvdson
 from . import prdm
 from . import spinproj
-from .mpo_dmrg_kernel import EnvSet, MPOStore, HVec, HDiag, SVec, renorm
+from .mpo_dmrg_kernel import EnvSet, MPOStore, HVec, HDiag, SVec, renorm, _sigma_plan
 from .qtensor import qtensor, fromQnums
 
 
@@ -180,6 +180,22 @@ class mpo_dmrg:
         self.dwt = []
         self.esweeps = []
         self.timings = []
+        # seconds per phase of the sweep, summed over dots, when set to a
+        # dict (each phase boundary then synchronises the device)
+        self.phase_times = None
+        self._phase_t0 = 0.0
+
+    def tick(self, name):
+        """Adds the seconds since the previous tick to phase ``name`` of
+        ``phase_times`` (no-op unless ``phase_times`` is a dict)."""
+        pt = self.phase_times
+        if pt is None:
+            return
+        _torch().cuda.synchronize()
+        t = time.perf_counter()
+        if name is not None:
+            pt[name] = pt.get(name, 0.0) + t - self._phase_t0
+        self._phase_t0 = t
 
     # ------------------------------------------------------------ set-up
     def build(self):
@@ -452,6 +468,10 @@ class mpo_dmrg:
                 ndim0 = prjmap.size
             if ndim0 == 0:
                 raise RuntimeError('no basis in symmetry sector %s' % qkey)
+            self.tick("setup")
+            if self.phase_times is not None:
+                _sigma_plan(info)
+                self.tick("sigma_plan")
             if self.ifprecond:
                 diag = HDiag(info, ndim0, prjmap)
                 if getattr(self, "size", 1) > 1:
@@ -474,11 +494,13 @@ class mpo_dmrg:
             solver.diag = diag
             solver.noise = self.ifdvdnz and (self.noise > 1.e-10)
             solver.hvec_eps = {"fp64": 0.0, "emu64": 1e-14, "split": 1e-8}[self.precision]
+            self.tick("hdiag")
             v0 = None
             if self.psi0 is not None:
                 idx = torch.as_tensor(numpy.asarray(prjmap, dtype=numpy.int64), device=self.psi0.device)
                 v0 = self.psi0[ioff:ioff + neig].index_select(1, idx)
             eig, vec, nmvp = solver.solve_iter(v0=v0, iop=4)
+            self.tick("davidson")
             if self.precision == "split":
                 # energy error is second order in the vector error: one
                 # Rayleigh quotient per vector with the 56-bit product
@@ -490,6 +512,7 @@ class mpo_dmrg:
                     sv = SVec(v, info, ndim0, prjmap) if self.ifs2proj else v
                     eig[i] = float(torch.dot(v, hv) / torch.dot(v, sv))
                 self.precision = saved
+                self.tick("rayleigh")
             civec = torch.zeros((neig, ndim), dtype=torch.float64, device="cuda")
             civec[:, torch.as_tensor(numpy.asarray(prjmap, dtype=numpy.int64), device="cuda")] = vec
             civecs.append(civec)
@@ -498,9 +521,12 @@ class mpo_dmrg:
             ioff += neig
         civecs = torch.cat(civecs, dim=0)
         eigs = numpy.array(eigs)
+        self.tick("setup")
         sigs, dwts, qred, site, srotR = self.decimation(civecs, info)
+        self.tick("decimation")
         if self.ifguess:
             self.genGuess(isite, ncsite, actlst, civecs, srotR, status)
+            self.tick("guess")
         return nmvps, eigs, sigs, dwts, qred, site, srotR
 
     def decimation(self, civecs, info):
@@ -630,19 +656,24 @@ class mpo_dmrg:
         nmvp = 0
         for isite in actlst:
             t0 = time.perf_counter()
+            self.tick(None)
             flst = self._flst(isite - 1, isite + ncsite)
             nmvps, eigs, sigs, dwts, qred, site, srotR = self.ci_solver(isite, ncsite, actlst, flst, status, ifsym)
             t1 = time.perf_counter()
             nmvp += nmvps
             elst.append(eigs)
             dlst.append(dwts)
+            self.tick(None)
             siteN = self.updateSite(isite, ncsite, qred, site, status)
+            self.tick("site_update")
             fN = [[None, None]]
             renorm(self, isite, ncsite, flst, fN, siteN, status)
+            self.tick("renorm")
             if status == 'L':
                 self._store_envs('lop', isite, fN)
             else:
                 self._store_envs('rop', isite + ncsite - 1, fN)
+            self.tick("store_envs")
             torch.cuda.synchronize()
             self.timings.append((status, isite, t1 - t0, time.perf_counter() - t1, nmvps))
         self.updateBoundary(ncsite, sitelst, qred, srotR, status)

@@ -485,6 +485,9 @@ def renorm(dmrg, isite, ncsite, flst, flstN, site, status):
                              [None] * nop)
     else:
         rp = _renorm_plan(dmrg, status, jsite, fE, qsite, ops)
+        tick = getattr(dmrg, "tick", None)
+        if tick is not None:
+            tick("renorm_plan")
         buf = torch.empty(max(rp.total, 1), dtype=torch.float64, device="cuda")
         work = torch.empty(max(rp.ws // 8, 1), dtype=torch.float64, device="cuda")
         sval, _ = _to_device(qsite.value)
