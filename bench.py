@@ -18,6 +18,7 @@ over that sample.  ``--impl reference`` times only the oracle, on a dot built
 on the host without any engine code.
 """
 import argparse
+import collections
 import json
 import os
 import subprocess
@@ -335,6 +336,7 @@ def sweep_converged(K=24, nelec=24, D=512, seed=2024, maxiter=14, tol=1e-8, hop=
         # final Rayleigh quotient, decimation, guess, renormalisation ...);
         # each phase boundary synchronises the device
         m.phase_times = {} if phases else None
+        m.plan_counts = collections.Counter()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         r1 = m.sweep(list(range(K)), 2, 'R')
@@ -347,6 +349,8 @@ def sweep_converged(K=24, nelec=24, D=512, seed=2024, maxiter=14, tol=1e-8, hop=
                      "dE_vs_converged": e - e_conv}
         if phases:
             out[prec]["phases_s"] = {k: round(v, 4) for k, v in sorted(m.phase_times.items(), key=lambda kv: -kv[1])}
+            # plans built for structures not met before, and plans reused
+            out[prec]["plans"] = dict(m.plan_counts)
         m.phase_times = None
     out["dE_split_fp64"] = abs(out["split"]["energy"] - out["fp64"]["energy"])
     out["sweep_speedup_split_vs_fp64"] = out["fp64"]["s_per_sweep"] / out["split"]["s_per_sweep"]

@@ -29,8 +29,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = open(os.path.join(ROOT, "zmpo_dmrg_gb300", "csrc", "kernels_umma.cu")).read()
 ENGINE = open(os.path.join(ROOT, "zmpo_dmrg_gb300", "csrc", "engine.h")).read()
 
-TM, KMAX, KB_SLOTS, ROW_BYTES, NTHREADS = 128, 256, 32, 64, 320
-EPI_WARPS, PROD_WARP, MMA_WARP = 8, 8, 9
+TM, KMAX, KB_SLOTS, ROW_BYTES, NTHREADS = 128, 256, 32, 64, 448
+EPI_WARPS, PROD_WARP, MMA_WARP = 12, 12, 13
 STG_BYTES = EPI_WARPS * 32 * 8 * 8
 SMEM_MAX = 232448
 TX_MAX = (1 << 20) - 1
@@ -44,7 +44,8 @@ def test_constants_match_source():
     assert "constexpr int kUmmaTM = 128, kUmmaMaxK = 256, kUmmaKB = 32;" in ENGINE
     for name, val in [("ROW_BYTES", ROW_BYTES), ("NTHREADS", NTHREADS)]:
         assert re.search(r"constexpr int %s = %d;" % (name, val), SRC), name
-    assert "EPI_WARPS = 8, PROD_WARP = 8, MMA_WARP = 9" in SRC
+    assert "EPI_WARPS = 12, PROD_WARP = 12, MMA_WARP = 13" in SRC
+    assert "EPI_GROUPS = EPI_WARPS / 4;" in SRC and "CHUNK_STEP = 8 * EPI_GROUPS;" in SRC
     assert "STG_BYTES = EPI_WARPS * 32 * 8 * 8;" in SRC
     assert (EPI_WARPS + 2) * 32 == NTHREADS
     assert "static constexpr int NSTAGE = TN == 64 ? 2 : 4;" in SRC
@@ -321,16 +322,24 @@ def test_descriptor_encodings():
 
 def test_epilogue_staging_and_tmem_chunks():
     """Epilogue warp w: TMEM lane quarter w % 4, 8-column chunks from 8 (w / 4)
-    in steps of 16; its 2 KB staging area holds 32 rows x 8 float64; the
+    in steps of 24 (at most NCH per warp, the long kernel's register sums);
+    its 2 KB staging area holds 32 rows x 8 float64; the
     swizzled writes (lane = row) and reads (4 rows x 8 columns per
     instruction) cover the area exactly once each."""
     assert "tcgen05.ld.sync.aligned.32x32b.x8.b32" in SRC
-    assert "const int quarter = warp & 3, half = warp >> 2;" in SRC
+    assert SRC.count("const int quarter = warp & 3, group = warp >> 2;") == 2
+    assert "for (int c0 = 8 * group; c0 < TN; c0 += CHUNK_STEP) {" in SRC
+    assert SRC.count("const int c0 = 8 * group + CHUNK_STEP * jc;") == 2
+    assert "constexpr int NCH = (TN / 8 + EPI_GROUPS - 1) / EPI_GROUPS;" in SRC
+    assert EPI_WARPS % 4 == 0
+    groups = EPI_WARPS // 4
     for TN in (16, 32, 64):
         cover = {}
+        nch = (TN // 8 + groups - 1) // groups
         for w in range(EPI_WARPS):
             q, h = w & 3, w >> 2
-            for c0 in range(8 * h, TN, 16):
+            assert len(range(8 * h, TN, 8 * groups)) <= nch
+            for c0 in range(8 * h, TN, 8 * groups):
                 for lane in range(32):
                     for i in range(8):
                         key = (q * 32 + lane, c0 + i)
@@ -354,3 +363,33 @@ def test_epilogue_staging_and_tmem_chunks():
             assert len({widx(lane, i) % 16 for lane in hw}) == 16
         for k in range(8):
             assert len({ridx(k * 4 + (lane >> 3), lane & 7) % 16 for lane in hw}) == 16
+
+
+def test_prepare_a_thread_maps():
+    """k_prep_a: the 256 threads' 16 loads of a 16-row staging block cover
+    every (row, slot < 256) once in both load maps (along the rows of a slot,
+    along the slots of a row), stay inside the staging pitch, and the cut map
+    covers every (k block, row, chunk) of the block once."""
+    assert "constexpr int PREP_RB = 16;" in SRC and "constexpr int PREP_STRIDE = umma::KMAX + 2;" in SRC
+    assert "const int lr = rows_fast ? (tid & 15) : (warp << 1);" in SRC
+    assert "const int lj = rows_fast ? (tid >> 4) : lane;" in SRC
+    assert "const int r = rows_fast ? lr : lr + (i & 1);" in SRC
+    assert "const int j = rows_fast ? lj + 16 * i : lj + 32 * (i >> 1);" in SRC
+    assert "const int ch = u & 3, r = (u >> 2) & (PREP_RB - 1), kb = u >> 6;" in SRC
+    RB, STRIDE, LOADS = 16, KMAX + 2, 16
+    for rows_fast in (True, False):
+        seen = set()
+        for tid in range(256):
+            warp, lane = tid >> 5, tid & 31
+            lr = (tid & 15) if rows_fast else (warp << 1)
+            lj = (tid >> 4) if rows_fast else lane
+            for i in range(LOADS):
+                r = lr if rows_fast else lr + (i & 1)
+                j = lj + 16 * i if rows_fast else lj + 32 * (i >> 1)
+                assert 0 <= r < RB and 0 <= j < KMAX and r * STRIDE + j < RB * STRIDE
+                seen.add((r, j))
+        assert len(seen) == RB * KMAX
+    for nkb in range(1, KMAX // KB_SLOTS + 1):
+        cut = [((u >> 6), (u >> 2) & 15, u & 3) for u in range(nkb * RB * 4)]
+        assert len(set(cut)) == len(cut) == nkb * RB * 4
+        assert all(kb < nkb and kb * KB_SLOTS + ch * 8 + 7 < KMAX for kb, r, ch in cut)

@@ -27,12 +27,13 @@
 //     block-sparse operands run with enough loads in flight.
 //  2. k_step_umma moves records into shared memory with bulk copies
 //     (cp.async.bulk, completion counted on mbarriers) and multiplies:
-//       warps 0-3  epilogue: warp w reads TMEM lanes 32w..32w+31 (one output
-//                  row per thread), folds the levels and stores the tile;
-//       warp 4     producer: lane 0 issues the bulk copies (B tile of the
+//       warps 0-11 epilogue: warp w reads TMEM lanes 32(w%4).. (one output
+//                  row per thread) and every third 8-column chunk from
+//                  column 8(w/4), folds the levels and stores the tile;
+//       warp 12    producer: lane 0 issues the bulk copies (B tile of the
 //                  work item, per row tile its exponents and column map, A
 //                  k blocks through a ring of stages);
-//       warp 5     TMEM allocation; lane 0 issues the MMAs and commits.
+//       warp 13    TMEM allocation; lane 0 issues the MMAs and commits.
 //     Level products: the B planes of a column tile of TN columns are stacked
 //     along N as B' = [B0 | B1 | B2 | B3] (4 TN rows of a K-major operand)
 //     and the four level accumulators of a row tile lie side by side in TMEM
@@ -67,8 +68,10 @@ constexpr int NKB_MAX = KMAX / KB_SLOTS;
 constexpr int ROW_BYTES = 64;                 // K-major rows of 32 bf16, 64-byte swizzle
 constexpr int A_PLANE = TM * ROW_BYTES;       // 8 KB: one digit plane of a k block
 constexpr int A_STAGE = 4 * A_PLANE;          // 32 KB: four planes
-constexpr int NTHREADS = 320;
-constexpr int EPI_WARPS = 8, PROD_WARP = 8, MMA_WARP = 9;
+constexpr int NTHREADS = 448;
+constexpr int EPI_WARPS = 12, PROD_WARP = 12, MMA_WARP = 13;
+constexpr int EPI_GROUPS = EPI_WARPS / 4;       // epilogue warps per TMEM lane quarter
+constexpr int CHUNK_STEP = 8 * EPI_GROUPS;      // column step between a warp's 8-column chunks
 constexpr int STG_BYTES = EPI_WARPS * 32 * 8 * 8;  // per epilogue warp: 32 rows x 8 float64
 constexpr int PREP_THREADS = 256;
 constexpr int BIAS = 2082;
@@ -403,21 +406,90 @@ __device__ __forceinline__ double load_a(const Slot &sl, int row, bool scaled) {
 // ------------------------------------------------------------ prepare kernels
 // One A record per item (rows m0 .. m0+tm8-1, slots k0 .. k0+kc-1 of the
 // group), 16 rows at a time: the raw FP64 values of the rows over the
-// window are staged in shared memory (threads laid along the rows when a
-// slot's rows are contiguous, along the slots otherwise, so the CTA's loads
-// cover each row's span together), the row exponents are taken there, and
+// window are staged in shared memory, the row exponents are taken there, and
 // the rows are cut from there into the four digit planes of every k block
 // (a warp writes 8 rows x 4 chunks = 512 contiguous bytes of each plane);
 // the 128 exponents follow the planes.  Every value is read once.
+//
+// The loads of the next 16-row block are issued into registers before the
+// current block is cut (16 independent loads per thread in flight under the
+// cut).  A thread's loads run along the rows when a slot's rows are
+// contiguous (16 lanes per slot), along the slots otherwise (32 lanes per
+// row).  The slot table keeps only what the loads need: the address of row
+// 0, the row stride and the weight of every slot of the window.
 constexpr int PREP_RB = 16;                   // rows per staging block
 // staging row pitch in float64: = 2 (mod 16), so the 16 lanes of a half warp
 // reading (4 rows x 4 chunks) in the cut meet at most 2-way bank conflicts
 constexpr int PREP_STRIDE = umma::KMAX + 2;
-__global__ void __launch_bounds__(umma::PREP_THREADS)
+constexpr int PREP_LOADS = PREP_RB * umma::KMAX / umma::PREP_THREADS;  // 16 per thread and block
+static_assert(PREP_RB == 16 && umma::PREP_THREADS == 256 && PREP_LOADS == 16, "prepare-kernel thread map");
+
+namespace umma {
+struct ASlotTable {
+  const double *a[KMAX];   // A(row 0, slot)
+  int64_t sam[KMAX];       // row stride
+  double alpha[KMAX];      // weight
+};
+
+// The table of the slots k0 .. k0+kc-1 of a group, written by one warp
+// (kc <= KMAX): lanes take segments 32 at a time, an inclusive scan places
+// each segment's k range, then the warp writes the window part of each of
+// the 32 segments in turn, one slot per lane.  Returns the number of slots
+// in the window; sets *scaled when one of them has a weight other than 1.
+__device__ int build_a_slots(const Group &g, const Seg *__restrict__ segs, const Bufs &bufs, ASlotTable &t,
+                             int lane, int k0, int kc, int *scaled) {
+  kc = min(kc, KMAX);
+  const int k1 = k0 + kc;
+  int base = 0;
+  unsigned sc = 0;
+  for (int s0 = 0; s0 < g.nseg && base < k1; s0 += 32) {
+    const int sidx = s0 + lane;
+    Seg sg;
+    int k = 0;
+    if (sidx < g.nseg) {
+      sg = segs[g.seg0 + sidx];
+      k = sg.K;
+    }
+    int incl = k;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int first = base + incl - k;  // global slot of the segment's k = 0
+    const int lo = max(first, k0), hi = min(first + k, k1);
+    const bool in = k > 0 && lo < hi;
+    const unsigned inmask = __ballot_sync(0xffffffffu, in);
+    sc |= __ballot_sync(0xffffffffu, in && sg.alpha != 1.0);
+    const double *A = in ? bufs.p[sg.abuf] + sg.a_off : nullptr;
+    const long long sak = in ? sg.sak : 0, sam = in ? sg.sam : 0;
+    const double alpha = in ? sg.alpha : 1.0;
+    for (unsigned m = inmask; m; m &= m - 1) {
+      const int src = __ffs(m) - 1;
+      const int slo = __shfl_sync(0xffffffffu, lo, src), shi = __shfl_sync(0xffffffffu, hi, src);
+      const int sfirst = __shfl_sync(0xffffffffu, first, src);
+      const double *sA = reinterpret_cast<const double *>(
+          __shfl_sync(0xffffffffu, reinterpret_cast<long long>(A), src));
+      const long long ssak = __shfl_sync(0xffffffffu, sak, src), ssam = __shfl_sync(0xffffffffu, sam, src);
+      const double salpha = __shfl_sync(0xffffffffu, alpha, src);
+      for (int gj = slo + lane; gj < shi; gj += 32) {
+        t.a[gj - k0] = sA + (int64_t)(gj - sfirst) * ssak;
+        t.sam[gj - k0] = ssam;
+        t.alpha[gj - k0] = salpha;
+      }
+    }
+    base += __shfl_sync(0xffffffffu, incl, 31);
+  }
+  *scaled = sc != 0u;
+  return max(0, min(kc, base - k0));
+}
+}  // namespace umma
+
+__global__ void __launch_bounds__(umma::PREP_THREADS, 3)
 k_prep_a(const PrepA *__restrict__ items, int64_t nitems, const Group *__restrict__ groups,
          const Seg *__restrict__ segs, Bufs bufs, unsigned char *__restrict__ planes) {
   using namespace umma;
-  __shared__ Slot slots[KMAX];
+  __shared__ ASlotTable tab;
   __shared__ int s_ctl[2];
   __shared__ int s_ea[TM];
   extern __shared__ double stage[];  // PREP_RB x PREP_STRIDE
@@ -427,7 +499,7 @@ k_prep_a(const PrepA *__restrict__ items, int64_t nitems, const Group *__restric
     const Group g = groups[p.group];
     if (warp == 0) {
       int sc;
-      const int K = build_slots_window(g, segs, bufs, slots, lane, p.k0, p.kc, &sc);
+      const int K = build_a_slots(g, segs, bufs, tab, lane, p.k0, p.kc, &sc);
       if (lane == 0) {
         s_ctl[0] = K;
         s_ctl[1] = sc;
@@ -439,40 +511,53 @@ k_prep_a(const PrepA *__restrict__ items, int64_t nitems, const Group *__restric
     const bool scaled = s_ctl[1] != 0;
     const int nkb = (K + KB_SLOTS - 1) / KB_SLOTS, kpad = nkb * KB_SLOTS;
     const int tm8 = tile_rows8(g.M, p.m0), PL = tm8 * ROW_BYTES;
-    // rows contiguous for a slot (unit row stride): threads along the rows
-    const bool rows_fast = K > 0 && slots[0].sam == 1;
-    unsigned char *rec = planes + p.rec;
-    for (int rb = 0; rb < tm8; rb += PREP_RB) {
-      const int nr = min(PREP_RB, tm8 - rb);
-      for (int u = tid; u < nr * kpad; u += PREP_THREADS) {
-        int r, j;
-        if (rows_fast) {
-          r = u % nr;
-          j = u / nr;
-        } else {
-          j = u % kpad;
-          r = u / kpad;
-        }
+    // rows contiguous for a slot (unit row stride): 16 lanes along the rows
+    // of a slot; else 32 lanes along the slots of a row
+    const bool rows_fast = K > 0 && tab.sam[0] == 1;
+    const int lr = rows_fast ? (tid & 15) : (warp << 1);   // row (first of two: + (i & 1))
+    const int lj = rows_fast ? (tid >> 4) : lane;          // first slot
+    auto load_block = [&](double (&v)[PREP_LOADS], int rb) {
+#pragma unroll
+      for (int i = 0; i < PREP_LOADS; ++i) {
+        const int r = rows_fast ? lr : lr + (i & 1);
+        const int j = rows_fast ? lj + 16 * i : lj + 32 * (i >> 1);
         const int grow = p.m0 + rb + r;
-        stage[r * PREP_STRIDE + j] = (j < K && grow < g.M) ? load_a(slots[j], grow, scaled) : 0.0;
+        double x = 0.0;
+        if (j < K && grow < g.M) {
+          x = __ldg(tab.a[j] + (int64_t)grow * tab.sam[j]);
+          if (scaled) x *= tab.alpha[j];
+        }
+        v[i] = x;
+      }
+    };
+    unsigned char *rec = planes + p.rec;
+    double v[PREP_LOADS];
+    load_block(v, 0);
+    for (int rb = 0; rb < tm8; rb += PREP_RB) {
+#pragma unroll
+      for (int i = 0; i < PREP_LOADS; ++i) {
+        const int r = rows_fast ? lr : lr + (i & 1);
+        const int j = rows_fast ? lj + 16 * i : lj + 32 * (i >> 1);
+        if (j < kpad) stage[r * PREP_STRIDE + j] = v[i];
       }
       __syncthreads();
+      if (rb + PREP_RB < tm8) load_block(v, rb + PREP_RB);  // in flight during the cut
       {  // row exponents: 16 threads per row
         const int r = tid >> 4, part = tid & 15;
         int em = 0;
-        if (r < nr)
-          for (int j = part; j < kpad; j += 16) em = max(em, dexp(stage[r * PREP_STRIDE + j]));
+        for (int j = part; j < kpad; j += 16) em = max(em, dexp(stage[r * PREP_STRIDE + j]));
 #pragma unroll
         for (int o = 8; o >= 1; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o));
-        if (r < nr && part == 0) s_ea[rb + r] = em;
+        if (rb + r < tm8 && part == 0) s_ea[rb + r] = em;
       }
       __syncthreads();
-      for (int u = tid; u < nkb * nr * 4; u += PREP_THREADS) {
-        const int ch = u & 3, q = u >> 2, r = q % nr, kb = q / nr;
-        double v[8];
+      for (int u = tid; u < nkb * PREP_RB * 4; u += PREP_THREADS) {
+        const int ch = u & 3, r = (u >> 2) & (PREP_RB - 1), kb = u >> 6;
+        if (rb + r >= tm8) continue;
+        double x[8];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) v[i] = stage[r * PREP_STRIDE + kb * KB_SLOTS + ch * 8 + i];
-        cut8_store(v, s_ea[rb + r], rec + (int64_t)kb * 4 * PL, PL, rb + r, ch);
+        for (int i = 0; i < 8; ++i) x[i] = stage[r * PREP_STRIDE + kb * KB_SLOTS + ch * 8 + i];
+        cut8_store(x, s_ea[rb + r], rec + (int64_t)kb * 4 * PL, PL, rb + r, ch);
       }
       __syncthreads();  // the staging block is refilled
     }
@@ -697,9 +782,9 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
     __syncwarp();
   } else {
     // ================================================================= epilogue
-    // warp w reads TMEM lanes 32(w%4).. (tile rows) and every other 8-column
+    // warp w reads TMEM lanes 32(w%4).. (tile rows) and every third 8-column
     // chunk (from column 8(w/4))
-    const int quarter = warp & 3, half = warp >> 2;
+    const int quarter = warp & 3, group = warp >> 2;
     const int e = quarter * 32 + lane;
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     double *stg = reinterpret_cast<double *>(sm + LY::OFF_STG) + warp * 256;
@@ -725,7 +810,7 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
         tc_fence_after();
         double *out = bufs.p[ok ? cbuf : 0];
 #pragma unroll 1
-        for (int c0 = 8 * half; c0 < TN; c0 += 16) {
+        for (int c0 = 8 * group; c0 < TN; c0 += CHUNK_STEP) {
           uint32_t v[4][8];
           const uint32_t ta = tmem + lane_base + b * (4 * TN) + c0;
 #pragma unroll
@@ -935,9 +1020,11 @@ k_step_umma_long(const UWork *__restrict__ work, int64_t nwork, const Group *__r
     __syncwarp();
   } else {
     // ================================================================= epilogue
-    // warp w reads TMEM lanes 32(w%4).. and every other 8-column chunk (from
-    // column 8(w/4)); its TN/2 sums stay in registers over the passes
-    const int quarter = warp & 3, half = warp >> 2;
+    // warp w reads TMEM lanes 32(w%4).. and every third 8-column chunk (from
+    // column 8(w/4)); its sums (at most NCH chunks) stay in registers over
+    // the passes
+    constexpr int NCH = (TN / 8 + EPI_GROUPS - 1) / EPI_GROUPS;
+    const int quarter = warp & 3, group = warp >> 2;
     const int e = quarter * 32 + lane;
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     double *stg = reinterpret_cast<double *>(sm + LY::OFF_STG) + warp * 256;
@@ -946,9 +1033,9 @@ k_step_umma_long(const UWork *__restrict__ work, int64_t nwork, const Group *__r
       if (role_sync_or(2, EPI_WARPS * 32, *abort_flag != 0)) break;
       const UWork wk = work[w];
       const int K = wk.nrt_k >> 8, npass = (K + KMAX - 1) / KMAX;
-      double acc[TN / 2];
+      double acc[8 * NCH];
 #pragma unroll
-      for (int c = 0; c < TN / 2; ++c) acc[c] = 0.0;
+      for (int c = 0; c < 8 * NCH; ++c) acc[c] = 0.0;
       for (int j = 0; j < npass; ++j, ++t) {
         const uint32_t b = t & 1, u = t >> 1;
         const bool ok_rec = wait_bounded(bar(BAR_E_FULL + b), u & 1, abort_flag, 7);
@@ -960,8 +1047,9 @@ k_step_umma_long(const UWork *__restrict__ work, int64_t nwork, const Group *__r
         const bool ok = __all_sync(0xffffffffu, ok_rec && ok_acc && *abort_flag == 0);
         tc_fence_after();
 #pragma unroll
-        for (int jc = 0; jc < TN / 16; ++jc) {
-          const int c0 = 8 * half + 16 * jc;
+        for (int jc = 0; jc < NCH; ++jc) {
+          const int c0 = 8 * group + CHUNK_STEP * jc;
+          if (c0 >= TN) break;
           uint32_t v[4][8];
           const uint32_t ta = tmem + lane_base + b * (4 * TN) + c0;
 #pragma unroll
@@ -979,8 +1067,9 @@ k_step_umma_long(const UWork *__restrict__ work, int64_t nwork, const Group *__r
           const long long *cb = reinterpret_cast<const long long *>(rec + LY::REC_CB);
           const long long *rs = reinterpret_cast<const long long *>(rec + LY::REC_RS);
 #pragma unroll
-          for (int jc = 0; jc < TN / 16; ++jc) {
-            const int c0 = 8 * half + 16 * jc;
+          for (int jc = 0; jc < NCH; ++jc) {
+            const int c0 = 8 * group + CHUNK_STEP * jc;
+            if (c0 >= TN) break;
             store_chunk(stg, acc + 8 * jc, lane, info[0] + quarter * 32, info[1], cb + c0, rs + c0, out, true);
           }
         }

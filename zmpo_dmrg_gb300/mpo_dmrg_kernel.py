@@ -343,10 +343,13 @@ def _sigma_plan(info):
     key = _sigma_key(dmrg, isite, ncsite, fL, fR)
     cache = _plan_cache(dmrg, "_sigma_cache")
     plan = cache.pop(key, None)
+    counts = dmrg.__dict__.setdefault("plan_counts", collections.Counter())
     if plan is None or plan.released:
         plan = SigmaPlan(dmrg, isite, ncsite, fL, fR)
+        counts["sigma_built"] += 1
     else:
         plan.rebind(fL, fR)
+        counts["sigma_reused"] += 1
     cache[key] = plan
     total = sum(getattr(p, "ntasks", 0) for p in cache.values())
     while total > _SIGMA_CACHE_TASKS and len(cache) > 1:
@@ -567,8 +570,12 @@ def _renorm_plan(dmrg, status, jsite, fE, qsite, ops):
     key = h.digest()
     cache = _plan_cache(dmrg, "_renorm_cache")
     rp = cache.pop(key, None)
+    counts = dmrg.__dict__.setdefault("plan_counts", collections.Counter())
     if rp is None or rp.released:
         rp = RenormPlan(dmrg, status, jsite, fE, qsite, ops)
+        counts["renorm_built"] += 1
+    else:
+        counts["renorm_reused"] += 1
     cache[key] = rp
     total = sum(p.ntasks for p in cache.values())
     while total > _SIGMA_CACHE_TASKS and len(cache) > 1:
