@@ -101,8 +101,9 @@ int zmpo_contract_exec(zmpo_engine *e, int plan_id, const double *d_a,
  * allocates.  Every GPU that loads the library holds that array until the
  * process exits.  The call allocates nothing: the plan must have run once
  * through zmpo_contract_exec during set-up, with the precision of the later
- * calls (that call builds the plan's device task lists and, for the split
- * precision, the plan's own buffer of prepared digit planes), and a plan that
+ * calls (that call builds the plan's device task lists of that precision
+ * and, for the split precision, the plan's own buffer of prepared digit
+ * planes), and a plan that
  * needs more scratch than the array holds is rejected with ZMPO_E_SIZE.  The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress, with that device current); make that
  * first call before any stream capture.  All calls share the one array and it
@@ -143,13 +144,16 @@ int zmpo_sigma_workspace(zmpo_engine *e, int plan_id, int64_t *bytes);
 int zmpo_plan_stats(zmpo_engine *e, int plan_id, double *flops,
                     int64_t *ntasks, int *nlaunch);
 /* Host copy of one step's task records before the plan's first execution
- * (afterwards they live on the device): counts[4] = groups, segments, column
- * blocks, per-(segment, column block) B parts; each output pointer may be NULL
- * and receives the records in the engine's internal layout (csrc/engine.h:
- * Group 56 bytes, Seg 64, ColBlock 32, SegB 24).  For inspection and tests;
- * no reference counterpart. */
+ * (afterwards they live on the device): counts[5] = groups, segments, column
+ * blocks, per-(segment, column block) B parts, split-K sums; each output
+ * pointer may be NULL and receives the records in the engine's internal
+ * layout (csrc/engine.h: Group 56 bytes, Seg 64, ColBlock 32, SegB 24,
+ * Reduction 56).  Groups longer than the split-K length appear as their
+ * parts, which write scratch buffer 6; a split-K sum adds its parts in order
+ * into its destination.  For inspection and tests; no reference
+ * counterpart. */
 int zmpo_plan_step_tasks(zmpo_engine *e, int plan_id, int step, int64_t *counts,
-                         void *groups, void *segs, void *cblocks, void *segb);
+                         void *groups, void *segs, void *cblocks, void *segb, void *reds);
 /* Number of kernel launches one execution of the plan issues at this
  * precision (grouped GEMM launches per tile shape plus split-K sums).  No
  * reference counterpart: it reports what the engine will launch. */
@@ -215,9 +219,9 @@ int zmpo_profile(zmpo_engine *e, int on);
 int zmpo_plan_launch_times(zmpo_engine *e, int plan_id, int nmax, double *ms_avg,
                            double *alg_bytes, int64_t *ncalls);
 
-/* Introspection of a launch of a plan before its first execution: number of
- * output groups and, when M is non-NULL, per group its rows, columns, number
- * of block products and summed K (used to choose tile shapes). */
+/* Introspection of a launch of a plan: number of output groups (groups
+ * longer than the split-K length as their parts) and, when M is non-NULL,
+ * per group its rows, columns, number of block products and summed K. */
 int zmpo_plan_groups(zmpo_engine *e, int plan_id, int step, int64_t *ngroups,
                      int32_t *M, int32_t *N, int32_t *nseg, int64_t *ktot);
 

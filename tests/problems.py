@@ -436,7 +436,7 @@ def b_resident_tiles(P):
     n = 0
     for pid in plan.pids:
         for st in range(plan.nlaunch):
-            G, Sg, _, _ = eng.step_tasks(pid, st)
+            G, Sg = eng.step_tasks(pid, st)[:2]
             cs = numpy.concatenate([[0], numpy.cumsum(Sg['K'].astype(numpy.int64))])
             kt = cs[G['seg0'] + G['nseg']] - cs[G['seg0']]
             for M, N, k, ns in zip(G['M'], G['N'], kt, G['nseg']):
@@ -549,18 +549,27 @@ def product_sigma_subset(P, terms, x, precision="fp64"):
 
 
 # ------------------------------------------ host model of a plan's tasks
-def run_tasks_on_host(eng, pid, nsteps, bufs, gemm=None, written=None):
+def run_tasks_on_host(eng, pid, nsteps, bufs, gemm=None, written=None, part_gemm=None):
     """Execute a plan's task records with NumPy (test-only model of the
-    kernels' semantics, incl. column-block groups); returns the buffers.
-    ``gemm(A, B)``, when given, computes each group's product from its
-    segments joined along K (A scaled by the segment weights) -- a model of
-    a kernel's arithmetic; it may return None to keep the FP64 sum.
-    ``written``, when given, collects (buffer, flat indices, values) of the
-    groups whose product came from ``gemm``."""
+    kernels' semantics, incl. column-block groups and split-K sums); returns
+    the buffers.  ``gemm(A, B)``, when given, computes each group's product
+    from its segments joined along K (A scaled by the segment weights) -- a
+    model of a kernel's arithmetic; it may return None to keep the FP64 sum.
+    ``part_gemm`` (default ``gemm``) does the same for the split-K parts of
+    groups longer than the split-K length, whose results the split-K sums add
+    in order.  ``written``, when given, collects (buffer, flat indices,
+    values) of the groups (and sums of parts) whose product came from the
+    model."""
+    PART = 6  # scratch buffer of the split-K parts
     for st in range(nsteps):
-        groups, segs, cbl, segb = eng.step_tasks(pid, st)
+        groups, segs, cbl, segb, reds = eng.step_tasks(pid, st)
+        if len(reds):
+            bufs = list(bufs)
+            bufs[PART] = numpy.zeros(int(max(r["part_off"] + r["nparts"] * r["M"] * r["N"] for r in reds)))
+        part_modelled = {}
         for g in groups:
             M, N = int(g["M"]), int(g["N"])
+            is_part = int(g["cbuf"]) == PART
             acc = numpy.zeros((M, N))
             mi = numpy.arange(M)
             As, Bs = [], []
@@ -587,8 +596,9 @@ def run_tasks_on_host(eng, pid, nsteps, bufs, gemm=None, written=None):
                     As.append(A * s["alpha"] if s["alpha"] != 1.0 else A)
                     Bs.append(B)
             modelled = False
-            if gemm is not None and As:
-                got = gemm(numpy.concatenate(As, axis=1), numpy.concatenate(Bs, axis=0))
+            f = (part_gemm or gemm) if is_part else gemm
+            if f is not None and As:
+                got = f(numpy.concatenate(As, axis=1), numpy.concatenate(Bs, axis=0))
                 if got is not None:
                     acc = got
                     modelled = True
@@ -597,7 +607,9 @@ def run_tasks_on_host(eng, pid, nsteps, bufs, gemm=None, written=None):
                 ni = numpy.arange(N)
                 idx = g["c_off"] + mi[:, None] * g["scm"] + ni[None, :] * g["scn"]
                 out[idx] = acc
-                if modelled and written is not None:
+                if is_part:
+                    part_modelled[int(g["c_off"])] = modelled
+                elif modelled and written is not None:
                     written.append((int(g["cbuf"]), idx.ravel(), acc.ravel()))
             else:
                 for j in range(int(g["ncb"])):
@@ -608,6 +620,18 @@ def run_tasks_on_host(eng, pid, nsteps, bufs, gemm=None, written=None):
                     out[idx] = part
                     if modelled and written is not None:
                         written.append((int(g["cbuf"]), idx.ravel(), part.ravel()))
+        for r in reds:
+            # the split-K sum: parts added in order (as k_reduce does)
+            M, N, mn = int(r["M"]), int(r["N"]), int(r["M"]) * int(r["N"])
+            acc = numpy.zeros(mn)
+            for t in range(int(r["nparts"])):
+                acc = acc + bufs[PART][int(r["part_off"]) + t * mn:int(r["part_off"]) + (t + 1) * mn]
+            mi, ni = numpy.divmod(numpy.arange(mn), N)
+            idx = r["c_off"] + mi * r["scm"] + ni * r["scn"]
+            bufs[int(r["cbuf"])][idx] = acc
+            if written is not None and all(part_modelled.get(int(r["part_off"]) + t * mn, False)
+                                           for t in range(int(r["nparts"]))):
+                written.append((int(r["cbuf"]), idx, acc))
     return bufs
 
 

@@ -130,20 +130,25 @@ def test_dot_contractions_bit_exact_on_routed_groups(gpu, which):
     import torch
     P = random_problem(K=10, nelec=10, D=128, isite=4, seed=7)
     eng, pid, (a, b) = _dot_contraction(P, which)
-    groups, _, cbl, _ = eng.step_tasks(pid, 0)
+    groups, _, cbl, _, reds = eng.step_tasks(pid, 0)
     written = []
-    # buffers of a contraction plan: 0 = A, 1 = B, 4 = output; the output
-    # size from the furthest element the groups write
+    # buffers of a contraction plan: 0 = A, 1 = B, 4 = output (6: split-K
+    # parts); the output size from the furthest element the groups and the
+    # split-K sums write
     host_bufs = [a.cpu().numpy(), b.cpu().numpy(), None, None, None, None, numpy.zeros(1), numpy.zeros(1)]
     outn = 0
+    for r in reds:
+        outn = max(outn, int(r["c_off"] + (r["M"] - 1) * r["scm"] + (r["N"] - 1) * r["scn"]) + 1)
     for g in groups:
+        if g["cbuf"] == 6:
+            continue
         if g["ncb"] == 0:
             outn = max(outn, int(g["c_off"] + (g["M"] - 1) * g["scm"] + (g["N"] - 1) * g["scn"]) + 1)
         for j in range(int(g["ncb"])):
             cb = cbl[g["cb0"] + j]
             outn = max(outn, int(cb["c_off"] + (g["M"] - 1) * cb["scm"] + (cb["n"] - 1) * cb["scn"]) + 1)
     host_bufs[4] = numpy.full(outn, numpy.nan)
-    run_tasks_on_host(eng, pid, 1, host_bufs, model, written)
+    run_tasks_on_host(eng, pid, 1, host_bufs, model, written, part_gemm=long_gemm)
     assert len(written) > 10
     out = torch.full((outn,), numpy.nan, dtype=torch.float64, device="cuda")
     eng.contract_exec(pid, a, b, out, "split")

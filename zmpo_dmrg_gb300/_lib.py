@@ -57,7 +57,7 @@ EXPORTS = {
     "zmpo_plan_kernel_count": ([c_void_p, ctypes.c_int, ctypes.c_int, c_int_p], ctypes.c_int),
     "zmpo_plan_mma_macs": ([c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_dbl_p], ctypes.c_int),
     "zmpo_plan_step_tasks": ([c_void_p, ctypes.c_int, ctypes.c_int, c_i64_p, c_void_p, c_void_p, c_void_p,
-                              c_void_p], ctypes.c_int),
+                              c_void_p, c_void_p], ctypes.c_int),
     "zmpo_sigma_reuse_kept": ([c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "zmpo_sigma": ([c_void_p, ctypes.c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                     c_void_p, ctypes.c_int, c_void_p], ctypes.c_int),

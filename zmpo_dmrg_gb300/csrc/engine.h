@@ -57,6 +57,7 @@ struct Reduction {
   int32_t nparts, cbuf;
   int64_t elem0;        // prefix of M*N over reductions (thread mapping)
 };
+static_assert(sizeof(Reduction) == 56, "Reduction record layout (zmpo_plan_step_tasks)");
 
 struct Work {
   int32_t group;
@@ -167,7 +168,26 @@ struct Step {
   // 7-slice tensor-core tiles (times the digit products per multiply-add)
   double mma_macs[3] = {0.0, 0.0, 0.0};
   int64_t ntasks = 0;
-  bool uploaded = false;         // device copies are made on first use
+  // Work lists by precision family, made on the host (the split lists of a
+  // sigma plan at plan time, every other list at the first run that needs
+  // it) and copied to the device in one allocation per family: the common
+  // records (segments, groups, column blocks, B parts, split-K sums), the
+  // 4-slice lists (tcgen05 items, column maps, mma.sync tiles), the FP64
+  // tiles, the 7-slice tiles.  gk: each group's K (the lists other than the
+  // 4-slice ones need no segments).
+  struct HostLists {
+    std::vector<Work> w64, wtc[3][4], wtc4[3][4], wtcb[2];
+    std::vector<UWork> um[3], ul[3];
+    std::vector<PrepA> prep_a;   // kept items first
+    std::vector<PrepB> prep_b;
+    std::vector<int64_t> cmap;
+  } hl;
+  std::vector<int64_t> gk;
+  int64_t nsegs = 0;             // segments (the host copy is freed at the first upload)
+  bool lists_split = false, lists_fp64 = false, lists_emu = false;
+  bool up_common = false, up_split = false, up_fp64 = false, up_emu = false;
+  int64_t area_b0[2] = {0, 0};   // B records' offset in the per-call [0] / kept [1] area
+  void *d_lists = nullptr, *d_lists_split = nullptr, *d_lists_fp64 = nullptr, *d_lists_emu = nullptr;
   std::vector<Reduction> reds;   // split-K reductions (host)
   Reduction *d_reds = nullptr;
   int64_t red_elems = 0;         // total output elements of the reductions

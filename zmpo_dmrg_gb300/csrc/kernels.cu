@@ -905,7 +905,7 @@ int launch_hdiag(const DiagBlock *blocks, int64_t nblocks, const DiagTerm *terms
 // declaration in include/zmpo_gb300.h).  Every device that loads the library
 // holds the array until the process exits.
 namespace zmpo {
-int contract_step_for(zmpo_engine *e, int plan_id, Step **out);
+int contract_step_for(zmpo_engine *e, int plan_id, int precision, Step **out);
 }
 
 constexpr int64_t kNoAllocScratchElems = int64_t(1) << 20;  // 8 MiB of float64
@@ -926,7 +926,7 @@ extern "C" int zmpo_contract_exec_noalloc(zmpo_engine *e, int plan_id, const dou
                                           const double *d_b, double *d_out, int precision,
                                           void *stream) {
   zmpo::Step *st = nullptr;
-  int rc = zmpo::contract_step_for(e, plan_id, &st);
+  int rc = zmpo::contract_step_for(e, plan_id, precision, &st);
   if (rc) return rc;
   if (precision == ZMPO_PREC_SPLIT && st->plane_bytes > 0 && st->plane_ws_off < 0 && !st->d_planes_own)
     return zmpo::record_arg_error(

@@ -927,10 +927,8 @@ static int64_t group_k(const Step &st, const Group &G) {
 // records in the step's kept area (records of operands that stay fixed
 // between calls, which a caller may let the next call reuse), every other
 // side in the per-call area.  Each area holds its A records, then (from a
-// 256-byte aligned offset) its B records.  With make = false only the byte
-// totals are counted (the plan-time estimate).
+// 256-byte aligned offset) its B records.
 struct UmmaLists {
-  bool make = true;
   std::vector<PrepA> pa[2];          // [per-call, kept]; rec relative to its part
   std::vector<PrepB> pb[2];
   std::vector<UWork> w1[3], wl[3];   // one-pass / long items by column tile; pad = kept sides
@@ -969,6 +967,18 @@ static void b_seq_key(const Step &st, const Group &G, int64_t kbase, int64_t K, 
 static void column_map(const Step &st, const Group &G, int n0, int tn, std::vector<int64_t> &out) {
   const size_t base = out.size();
   out.resize(base + 2 * (size_t)tn);
+  // column blocks lie side by side in order of n0: find the first one that
+  // ends after n0, then walk along with the columns
+  int j = 0;
+  if (G.ncb > 0) {
+    int lo = 0, hi = G.ncb - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      const ColBlock &cb = st.cblocks[G.cb0 + mid];
+      if (cb.n0 + cb.n <= n0) lo = mid + 1; else hi = mid;
+    }
+    j = lo;
+  }
   for (int c = 0; c < tn; ++c) {
     const int col = n0 + c;
     int64_t cbase = -1, rs = 0;
@@ -977,12 +987,12 @@ static void column_map(const Step &st, const Group &G, int n0, int tn, std::vect
         cbase = G.c_off + (int64_t)col * G.scn;
         rs = G.scm;
       } else {
-        for (int j = 0; j < G.ncb; ++j) {
+        while (j < G.ncb && st.cblocks[G.cb0 + j].n0 + st.cblocks[G.cb0 + j].n <= col) ++j;
+        if (j < G.ncb) {
           const ColBlock &cb = st.cblocks[G.cb0 + j];
-          if (col >= cb.n0 && col < cb.n0 + cb.n) {
+          if (col >= cb.n0) {
             cbase = cb.c_off + (int64_t)(col - cb.n0) * cb.scn;
             rs = cb.scm;
-            break;
           }
         }
       }
@@ -1013,7 +1023,7 @@ static void umma_add_group(UmmaLists &L, const Step &st, int g, const Group &G, 
     arec[r] = L.abytes[ka];
     for (int j = 0; j < npass; ++j) {
       const int k0 = j * kUmmaMaxK, kc = (int)std::min<int64_t>(kUmmaMaxK, K - k0);
-      if (L.make) L.pa[ka].push_back({L.abytes[ka], g, m0, k0, kc});
+      L.pa[ka].push_back({L.abytes[ka], g, m0, k0, kc});
       L.abytes[ka] += umma_a_rec_bytes((kc + kUmmaKB - 1) / kUmmaKB, tm8);
     }
   }
@@ -1036,11 +1046,11 @@ static void umma_add_group(UmmaLists &L, const Step &st, int g, const Group &G, 
       if (G.ncb == 0) L.bseq[kb].emplace(key, brec);
       for (int j = 0; j < npass; ++j) {
         const int k0 = j * kUmmaMaxK, kc = (int)std::min<int64_t>(kUmmaMaxK, K - k0);
-        if (L.make) L.pb[kb].push_back({L.bbytes[kb], g, n0, tn, k0, kc, 0});
+        L.pb[kb].push_back({L.bbytes[kb], g, n0, tn, k0, kc, 0});
         L.bbytes[kb] += umma_b_rec_bytes((kc + kUmmaKB - 1) / kUmmaKB, tn);
       }
     }
-    if (L.make) {
+    {
       const int64_t cm = (int64_t)L.cmap.size();
       column_map(st, G, n0, tn, L.cmap);
       if (one) {
@@ -1062,26 +1072,35 @@ static int64_t area_bytes(const UmmaLists &L, int k, int64_t *b0) {
   return L.abytes[k] + L.bbytes[k] > 0 ? ((a + L.bbytes[k] + 255) & ~int64_t(255)) : 0;
 }
 
-// Bytes of the kept and per-call areas of a step's records.  Before the
-// split-K parts exist, a group longer than kSplitK counts as its parts
-// (kSplitK slots each, the rest last).
-static void umma_plane_bytes(const Step &st, int64_t *keep, int64_t *call) {
-  UmmaLists L;
-  L.make = false;
-  for (const Group &G : st.groups) {
-    const int64_t k = group_k(st, G);
-    const bool ka = side_kept(st, true), kb = side_kept(st, false);
-    if (!st.split_done && k > kSplitK && G.M > 0 && G.N > 0) {
-      Group part = G;
-      part.cbuf = kPartialBuf;
-      for (int64_t k0 = 0; k0 < k; k0 += kSplitK)
-        umma_add_group(L, st, 0, part, k0, std::min<int64_t>(kSplitK, k - k0), ka, kb);
-      continue;
-    }
-    umma_add_group(L, st, 0, G, 0, k, ka, kb);
-  }
-  *call = area_bytes(L, 0, nullptr);
-  *keep = area_bytes(L, 1, nullptr);
+// Where a step's kept and per-call record areas lie in its plane buffer,
+// and the record offsets of its prepare and work items from area-relative
+// to buffer offsets (after build_split_lists).  Kept prepare items come
+// first in their lists; a work item's pad holds its kept sides until then.
+static void place_records(Step &st) {
+  const int64_t abase[2] = {st.plane_call_off, st.plane_keep_off};
+  const int64_t bbase[2] = {st.plane_call_off + st.area_b0[0], st.plane_keep_off + st.area_b0[1]};
+  for (size_t i = 0; i < st.hl.prep_a.size(); ++i)
+    st.hl.prep_a[i].rec += abase[(int64_t)i < st.nprep_a_kept ? 1 : 0];
+  for (size_t i = 0; i < st.hl.prep_b.size(); ++i)
+    st.hl.prep_b[i].rec += bbase[(int64_t)i < st.nprep_b_kept ? 1 : 0];
+  for (int i = 0; i < 3; ++i)
+    for (auto *wv : {&st.hl.um[i], &st.hl.ul[i]})
+      for (auto &w : *wv) {
+        w.a_rec += abase[w.pad & 1];
+        w.b_rec += bbase[(w.pad >> 1) & 1];
+        w.pad = 0;
+      }
+}
+
+// A step-owned plane buffer: the kept area, then the per-call area
+// (renormalisation and contraction plans: allocated at the step's first
+// split-precision run).
+static void place_step_owned(Step &st) {
+  st.plane_ws_off = -1;
+  st.plane_keep_off = 0;
+  st.plane_call_off = st.plane_keep_bytes;
+  st.plane_bytes = st.plane_keep_bytes + st.plane_call_bytes;
+  place_records(st);
 }
 
 // Sigma plans: one plane region at the end of the workspace: the kept
@@ -1092,106 +1111,124 @@ static void umma_plane_bytes(const Step &st, int64_t *keep, int64_t *call) {
 // writes (keep_side per step, bit 0 = A, bit 1 = B; two-site: O = Wi Wj,
 // T1 = L psi, T3 = T1 O, sigma = T3 R; one-site: T1 = L psi, T2 = T1 W,
 // sigma = T2 R).  Other plans (renormalisation, which runs in FP64 or the
-// 7-slice emulation, and contractions) keep nothing and get a step-owned
-// buffer at their first split-precision run.
-static void reserve_plane_region(Plan *P, int ncsite) {
+// 7-slice emulation, and contractions) keep nothing.
+static uint8_t sigma_keep_side(int ncsite, int idx) {
   static const uint8_t kTwo[4] = {3, 1, 2, 2}, kOne[3] = {1, 2, 2};
+  return ncsite == 2 ? (idx < 4 ? kTwo[idx] : 0) : (idx < 3 ? kOne[idx] : 0);
+}
+
+static void reserve_plane_region(Plan *P) {
   int64_t keep_total = 0, call_max = 0;
   for (auto &st : P->steps) {
-    const size_t i = (size_t)st.idx;
-    st.keep_side = ncsite == 2 ? (i < 4 ? kTwo[i] : 0) : (i < 3 ? kOne[i] : 0);
-    int64_t keep, call;
-    umma_plane_bytes(st, &keep, &call);
     st.plane_keep_off = keep_total;
-    st.plane_keep_bytes = keep;
-    keep_total += keep;
-    st.plane_call_bytes = call;
-    call_max = std::max(call_max, call);
+    keep_total += st.plane_keep_bytes;
+    call_max = std::max(call_max, st.plane_call_bytes);
   }
-  if (keep_total + call_max == 0) return;
+  if (keep_total + call_max == 0) {
+    for (auto &st : P->steps) place_step_owned(st);
+    return;
+  }
   const int64_t off = ((P->ws_elems * (int64_t)sizeof(double)) + 255) & ~int64_t(255);
   for (auto &st : P->steps) {
     st.plane_ws_off = off;
     st.plane_call_off = keep_total;
     st.plane_bytes = keep_total + call_max;
+    place_records(st);
   }
   P->ws_elems = ((off + keep_total + call_max + 255) & ~int64_t(255)) / (int64_t)sizeof(double);
 }
 
 static void free_step(Step &st);
 
-static int upload_step_lists(Step &st);
-
-// Device copies of a step's task lists, made on first use.  A failed upload
-// (out of device memory, say) frees what it had allocated, so a later call
-// can try again.
-static int upload_step(Step &st) {
-  if (st.uploaded) return ZMPO_OK;
-  const int rc = upload_step_lists(st);
-  if (rc != ZMPO_OK) free_step(st);
-  return rc;
+// Each group's K after the split-K parts, and the groups in order of cost
+// (longest first, for load balance).
+static void step_group_k(Step &st) {
+  st.gk.assign(st.groups.size(), 0);
+  for (size_t g = 0; g < st.groups.size(); ++g) {
+    int64_t k = 0;
+    for (int s = 0; s < st.groups[g].nseg; ++s) k += st.segs[st.groups[g].seg0 + s].K;
+    st.gk[g] = k;
+  }
+  st.nsegs = (int64_t)st.segs.size();
 }
 
-static int upload_step_lists(Step &st) {
-  split_long_groups(st);
-  std::vector<Work> w64, wtc[3][4], wtc4[3][4], wtcb[2];
-  UmmaLists UL;
-  // order groups by cost (longest first) for load balance
+static std::vector<int> cost_order(const Step &st) {
   std::vector<int> order(st.groups.size());
   std::iota(order.begin(), order.end(), 0);
-  std::vector<int64_t> cost(st.groups.size(), 0), ktot(st.groups.size(), 0);
-  for (size_t g = 0; g < st.groups.size(); ++g) {
-    int64_t c = 0, k = 0;
-    for (int s = 0; s < st.groups[g].nseg; ++s) {
-      c += st.segs[st.groups[g].seg0 + s].K + 16;
-      k += st.segs[st.groups[g].seg0 + s].K;
-    }
-    cost[g] = c;
-    ktot[g] = k;
-  }
+  std::vector<int64_t> cost(st.groups.size());
+  for (size_t g = 0; g < st.groups.size(); ++g) cost[g] = st.gk[g] + 16 * (int64_t)st.groups[g].nseg;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
-  st.mma_macs[0] = st.mma_macs[1] = st.mma_macs[2] = 0.0;
-  for (int g : order) {
+  return order;
+}
+
+// The structure every precision shares: split-K parts, per-group K.
+static void finish_step_structure(Step &st) {
+  split_long_groups(st);
+  step_group_k(st);
+}
+
+// Column tiles of the mma.sync kernels.  Columns: full pieces of the widest
+// tile, then one narrower tile for the rest (the smallest of 8/16/32/64 that
+// holds it), so a group of 74 columns takes 64 + 16 instead of 64 + 64.
+// 64-column tiles cut K in 64-slot chunks: a group with K <= 32 would leave
+// half of every chunk empty, so it takes 32-column tiles (32-slot chunks)
+// instead.  Rows: likewise with 128-row tiles (64 under 64-column tiles,
+// 1024 threads at most) and a 32/64/128-row tile for the rest.
+template <class F>
+static void mma_sync_tiles(const Group &G, int64_t ktot, F &&tile) {
+  const int wmax = ktot <= 32 ? 32 : 64;
+  std::vector<std::pair<int, int>> rows;  // (first row, tile height)
+  for (int n0 = 0; n0 < G.N;) {
+    const int rem = G.N - n0;
+    const int tn = rem >= wmax ? wmax : (rem <= 8 ? 8 : (rem <= 16 ? 16 : (rem <= 32 ? 32 : 64)));
+    const int hmax = tn == 64 ? 64 : 128;
+    rows.clear();
+    for (int m0 = 0; m0 < G.M;) {
+      const int rm = G.M - m0;
+      const int tm = rm >= hmax ? hmax : (rm <= 32 ? 32 : (rm <= 64 ? 64 : 128));
+      rows.push_back({m0, tm});
+      m0 += tm;
+    }
+    tile(n0, tn, hmax, rows);
+    n0 += tn;
+  }
+}
+
+static int tile_index_n(int tn) { return tn == 8 ? 0 : (tn == 16 ? 1 : (tn == 32 ? 2 : 3)); }
+static int tile_index_m(int tm) { return tm == 32 ? 0 : (tm == 64 ? 1 : 2); }
+
+// 4-slice lists (needs the segments): the tcgen05 prepare and work items
+// (record offsets relative to their area until place_records), the column
+// maps, the sizes of the kept and per-call record areas, and the mma.sync
+// tiles (B-resident and plain) of the groups the tcgen05 kernels do not take.
+static void build_split_lists(Step &st) {
+  auto &wtc4 = st.hl.wtc4;
+  auto &wtcb = st.hl.wtcb;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 4; ++j) wtc4[i][j].clear();
+  wtcb[0].clear();
+  wtcb[1].clear();
+  UmmaLists UL;
+  st.mma_macs[1] = 0.0;
+  for (int g : cost_order(st)) {
     const Group &G = st.groups[g];
-    const double k16 = (double)((ktot[g] + 15) / 16 * 16);
-    for (int m0 = 0; m0 < G.M; m0 += kTileFP64M)
-      for (int n0 = 0; n0 < G.N; n0 += kTileFP64N) {
-        w64.push_back({g, m0, n0, 0});
-        st.mma_macs[0] += (double)kTileFP64M * kTileFP64N * k16;
-      }
-    // tcgen05 groups (records cut by the prepare kernels)
+    const int64_t kt = st.gk[g];
+    const double k16 = (double)((kt + 15) / 16 * 16);
     const double macs0 = UL.macs;
-    umma_add_group(UL, st, g, G, 0, ktot[g], side_kept(st, true), side_kept(st, false));
-    const bool routed = UL.macs != macs0;
-    st.mma_macs[1] += UL.macs - macs0;
-    // Tensor-core tiles.  Columns: full pieces of the widest tile, then one
-    // narrower tile for the rest (the smallest of 8/16/32/64 that holds it),
-    // so a group of 74 columns takes 64 + 16 instead of 64 + 64.  64-column
-    // tiles cut K in 64-slot chunks: a group with K <= 32 would leave half
-    // of every chunk empty, so it takes 32-column tiles (32-slot chunks)
-    // instead.  Rows: likewise with 128-row tiles (64 under 64-column tiles,
-    // 1024 threads at most) and a 32/64/128-row tile for the rest.
-    const int wmax = ktot[g] <= 32 ? 32 : 64;
-    for (int n0 = 0; n0 < G.N;) {
-      const int rem = G.N - n0;
-      const int tn = rem >= wmax ? wmax : (rem <= 8 ? 8 : (rem <= 16 ? 16 : (rem <= 32 ? 32 : 64)));
-      const int tni = tn == 8 ? 0 : (tn == 16 ? 1 : (tn == 32 ? 2 : 3));
-      const int hmax = tn == 64 ? 64 : 128;
-      std::vector<std::pair<int, int>> rows;  // (first row, tile height)
-      for (int m0 = 0; m0 < G.M;) {
-        const int rm = G.M - m0;
-        const int tm = rm >= hmax ? hmax : (rm <= 32 ? 32 : (rm <= 64 ? 64 : 128));
-        rows.push_back({m0, tm});
-        m0 += tm;
-      }
+    umma_add_group(UL, st, g, G, 0, kt, side_kept(st, true), side_kept(st, false));
+    if (UL.macs != macs0) {
+      st.mma_macs[1] += UL.macs - macs0;
+      continue;
+    }
+    mma_sync_tiles(G, kt, [&](int n0, int tn, int hmax, const std::vector<std::pair<int, int>> &rows) {
       // B-resident kernel: 64 x 64 or 128 x 32 tiles, a run of at least two
       // full-height row tiles, the whole K in one slot-table pass (at most
       // 32 segments, K <= kBresMaxK)
       const int bres = tn == 64 ? 0 : (tn == 32 ? 1 : -1);
       size_t nfull = 0;
-      if (bres >= 0 && G.nseg <= 32 && ktot[g] <= kBresMaxK)
+      if (bres >= 0 && G.nseg <= 32 && kt <= kBresMaxK)
         while (nfull < rows.size() && rows[nfull].second == hmax) ++nfull;
-      if (nfull < 2 || routed) nfull = 0;
+      if (nfull < 2) nfull = 0;
       if (nfull) {
         const int nruns = (int)((nfull + kBresRun - 1) / kBresRun);
         const int len = (int)((nfull + nruns - 1) / nruns);
@@ -1199,52 +1236,17 @@ static int upload_step_lists(Step &st) {
           wtcb[bres].push_back({g, rows[r].first, n0, std::min(len, (int)nfull - r)});
       }
       for (size_t r = 0; r < rows.size(); ++r) {
-        const int tmi = rows[r].second == 32 ? 0 : (rows[r].second == 64 ? 1 : 2);
-        wtc[tmi][tni].push_back({g, rows[r].first, n0, 0});
-        if (r >= nfull && !routed) wtc4[tmi][tni].push_back({g, rows[r].first, n0, 0});
-        const double macs = (double)rows[r].second * tn * k16;
-        if (!routed) st.mma_macs[1] += macs;  // the same tiles, B-resident or not
-        st.mma_macs[2] += macs;
+        if (r >= nfull) wtc4[tile_index_m(rows[r].second)][tile_index_n(tn)].push_back({g, rows[r].first, n0, 0});
+        st.mma_macs[1] += (double)rows[r].second * tn * k16;  // the same tiles, B-resident or not
       }
-      n0 += tn;
-    }
+    });
   }
-  st.nwork_fp64 = (int64_t)w64.size();
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 4; ++j) {
-      st.nwork_tc[i][j] = (int64_t)wtc[i][j].size();
-      st.nwork_tc4[i][j] = (int64_t)wtc4[i][j].size();
-    }
+    for (int j = 0; j < 4; ++j) st.nwork_tc4[i][j] = (int64_t)wtc4[i][j].size();
   for (int i = 0; i < 2; ++i) st.nwork_tcb[i] = (int64_t)wtcb[i].size();
-  // record offsets: kept area at plane_keep_off, per-call area at
-  // plane_call_off (A records, then B records of each area)
-  {
-    int64_t b0[2];
-    const int64_t call = area_bytes(UL, 0, &b0[0]), keep = area_bytes(UL, 1, &b0[1]);
-    if (st.plane_ws_off >= 0) {
-      if (call != st.plane_call_bytes || keep != st.plane_keep_bytes)
-        return fail(ZMPO_E_ARG, "upload: prepared-plane size differs from the plan's reservation");
-    } else {
-      st.plane_keep_off = 0;
-      st.plane_keep_bytes = keep;
-      st.plane_call_off = keep;
-      st.plane_call_bytes = call;
-      st.plane_bytes = keep + call;
-    }
-    const int64_t abase[2] = {st.plane_call_off, st.plane_keep_off};
-    const int64_t bbase[2] = {st.plane_call_off + b0[0], st.plane_keep_off + b0[1]};
-    for (int k = 0; k < 2; ++k) {
-      for (auto &p : UL.pa[k]) p.rec += abase[k];
-      for (auto &p : UL.pb[k]) p.rec += bbase[k];
-    }
-    for (int i = 0; i < 3; ++i)
-      for (auto *wv : {&UL.w1[i], &UL.wl[i]})
-        for (auto &w : *wv) {
-          w.a_rec += abase[w.pad & 1];
-          w.b_rec += bbase[(w.pad >> 1) & 1];
-          w.pad = 0;
-        }
-  }
+  // area sizes; record offsets stay area-relative until place_records
+  st.plane_call_bytes = area_bytes(UL, 0, &st.area_b0[0]);
+  st.plane_keep_bytes = area_bytes(UL, 1, &st.area_b0[1]);
   // long items: groups whose first column tile shares a B-record sequence
   // run one after another, and a group's column tiles next to each other (the
   // repeated reads of a shared B sequence, and of a group's A records, come
@@ -1263,97 +1265,226 @@ static int upload_step_lists(Step &st) {
       });
   }
   // prepare items: kept ones first (a call that reuses them skips them)
-  std::vector<PrepA> prep_a(UL.pa[1]);
-  prep_a.insert(prep_a.end(), UL.pa[0].begin(), UL.pa[0].end());
-  std::vector<PrepB> prep_b(UL.pb[1]);
-  prep_b.insert(prep_b.end(), UL.pb[0].begin(), UL.pb[0].end());
-  st.nprep_a = (int64_t)prep_a.size();
-  st.nprep_b = (int64_t)prep_b.size();
+  st.hl.prep_a = UL.pa[1];
+  st.hl.prep_a.insert(st.hl.prep_a.end(), UL.pa[0].begin(), UL.pa[0].end());
+  st.hl.prep_b = UL.pb[1];
+  st.hl.prep_b.insert(st.hl.prep_b.end(), UL.pb[0].begin(), UL.pb[0].end());
+  st.nprep_a = (int64_t)st.hl.prep_a.size();
+  st.nprep_b = (int64_t)st.hl.prep_b.size();
   st.nprep_a_kept = (int64_t)UL.pa[1].size();
   st.nprep_b_kept = (int64_t)UL.pb[1].size();
   for (int i = 0; i < 3; ++i) {
     st.nwork_um[i] = (int64_t)UL.w1[i].size();
     st.nwork_ul[i] = (int64_t)UL.wl[i].size();
+    st.hl.um[i].swap(UL.w1[i]);
+    st.hl.ul[i].swap(UL.wl[i]);
   }
-  auto up = [](auto **dptr, const auto &v) -> cudaError_t {
-    using T = typename std::remove_reference<decltype(v)>::type::value_type;
-    if (v.empty()) {
-      *dptr = nullptr;
-      return cudaSuccess;
-    }
-    cudaError_t e = cudaMalloc((void **)dptr, v.size() * sizeof(T));
-    if (e != cudaSuccess) return e;
-    return cudaMemcpy(*dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
-  };
-  CUDA_TRY(up(&st.d_segs, st.segs));
-  CUDA_TRY(up(&st.d_groups, st.groups));
-  CUDA_TRY(up(&st.d_cblocks, st.cblocks));
-  CUDA_TRY(up(&st.d_segb, st.segb));
-  CUDA_TRY(up(&st.d_work_fp64, w64));
+  st.hl.cmap.swap(UL.cmap);
+  st.lists_split = true;
+}
+
+// FP64 tiles (kTileFP64M x kTileFP64N) of every group.
+static void build_fp64_list(Step &st) {
+  st.hl.w64.clear();
+  st.mma_macs[0] = 0.0;
+  for (int g : cost_order(st)) {
+    const Group &G = st.groups[g];
+    const double k16 = (double)((st.gk[g] + 15) / 16 * 16);
+    for (int m0 = 0; m0 < G.M; m0 += kTileFP64M)
+      for (int n0 = 0; n0 < G.N; n0 += kTileFP64N) {
+        st.hl.w64.push_back({g, m0, n0, 0});
+        st.mma_macs[0] += (double)kTileFP64M * kTileFP64N * k16;
+      }
+  }
+  st.nwork_fp64 = (int64_t)st.hl.w64.size();
+  st.lists_fp64 = true;
+}
+
+// 7-slice mma.sync tiles of every group.
+static void build_emu_lists(Step &st) {
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 4; ++j) {
-      CUDA_TRY(up(&st.d_work_tc[i][j], wtc[i][j]));
-      CUDA_TRY(up(&st.d_work_tc4[i][j], wtc4[i][j]));
-    }
-  for (int i = 0; i < 2; ++i) CUDA_TRY(up(&st.d_work_tcb[i], wtcb[i]));
-  for (int i = 0; i < 3; ++i) {
-    CUDA_TRY(up(&st.d_work_um[i], UL.w1[i]));
-    CUDA_TRY(up(&st.d_work_ul[i], UL.wl[i]));
+    for (int j = 0; j < 4; ++j) st.hl.wtc[i][j].clear();
+  st.mma_macs[2] = 0.0;
+  for (int g : cost_order(st)) {
+    const Group &G = st.groups[g];
+    const double k16 = (double)((st.gk[g] + 15) / 16 * 16);
+    mma_sync_tiles(G, st.gk[g], [&](int n0, int tn, int, const std::vector<std::pair<int, int>> &rows) {
+      for (const auto &r : rows) {
+        st.hl.wtc[tile_index_m(r.second)][tile_index_n(tn)].push_back({g, r.first, n0, 0});
+        st.mma_macs[2] += (double)r.second * tn * k16;
+      }
+    });
   }
-  CUDA_TRY(up(&st.d_prep_a, prep_a));
-  CUDA_TRY(up(&st.d_prep_b, prep_b));
-  CUDA_TRY(up(&st.d_cmap, UL.cmap));
-  CUDA_TRY(up(&st.d_reds, st.reds));
-  if (st.part_elems > 0) CUDA_TRY(cudaMalloc((void **)&st.d_part, st.part_elems * sizeof(double)));
-  // keep the host mirror of groups (sizes) but free the bulky segment copy
-  std::vector<Seg>().swap(st.segs);
-  st.uploaded = true;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 4; ++j) st.nwork_tc[i][j] = (int64_t)st.hl.wtc[i][j].size();
+  st.lists_emu = true;
+}
+
+// One device allocation for several host lists, each at a 256-byte aligned
+// offset; *dptr of each list points into it (nullptr for an empty list).
+struct ListUpload {
+  struct Part {
+    void **dst;
+    const void *src;
+    size_t bytes, off;
+  };
+  std::vector<Part> parts;
+  size_t total = 0;
+  template <class T>
+  void add(T **dptr, const std::vector<T> &v) {
+    *dptr = nullptr;
+    if (v.empty()) return;
+    const size_t bytes = v.size() * sizeof(T);
+    parts.push_back({(void **)dptr, v.data(), bytes, total});
+    total += (bytes + 255) & ~size_t(255);
+  }
+  int run(void **dbuf) {
+    if (total == 0) return ZMPO_OK;
+    CUDA_TRY(cudaMalloc(dbuf, total));
+    unsigned char *base = static_cast<unsigned char *>(*dbuf);
+    for (const Part &p : parts) {
+      CUDA_TRY(cudaMemcpy(base + p.off, p.src, p.bytes, cudaMemcpyHostToDevice));
+      *p.dst = base + p.off;
+    }
+    return ZMPO_OK;
+  }
+};
+
+// The host segments again (after the first upload freed them): the 4-slice
+// lists of a plan other than a sigma plan are made at its first 4-slice run.
+static int host_segments(Step &st) {
+  if (!st.segs.empty() || st.nsegs == 0) return ZMPO_OK;
+  if (!st.d_segs) return fail(ZMPO_E_ARG, "task lists: segments neither on the host nor on the device");
+  st.segs.resize((size_t)st.nsegs);
+  CUDA_TRY(cudaMemcpy(st.segs.data(), st.d_segs, st.segs.size() * sizeof(Seg), cudaMemcpyDeviceToHost));
   return ZMPO_OK;
 }
 
+// Host lists of a precision (made when missing).
+static int host_lists(Step &st, int precision) {
+  if (precision == ZMPO_PREC_SPLIT && !st.lists_split) {
+    int rc = host_segments(st);
+    if (rc) return rc;
+    build_split_lists(st);
+    place_step_owned(st);
+    if (st.up_common) std::vector<Seg>().swap(st.segs);
+  } else if (precision == ZMPO_PREC_FP64 && !st.lists_fp64) {
+    build_fp64_list(st);
+  } else if (precision == ZMPO_PREC_EMU64 && !st.lists_emu) {
+    build_emu_lists(st);
+  }
+  return ZMPO_OK;
+}
+
+// Device copies of the lists a run at this precision needs, made on first
+// use (the common records, then the precision's family).  After the common
+// upload the host segments are freed; the groups stay (sizes, the test
+// interfaces).
+static int upload_lists(Step &st, int precision) {
+  if (!st.up_common) {
+    ListUpload U;
+    U.add(&st.d_segs, st.segs);
+    U.add(&st.d_groups, st.groups);
+    U.add(&st.d_cblocks, st.cblocks);
+    U.add(&st.d_segb, st.segb);
+    U.add(&st.d_reds, st.reds);
+    int rc = U.run(&st.d_lists);
+    if (rc) return rc;
+    if (st.part_elems > 0) CUDA_TRY(cudaMalloc((void **)&st.d_part, st.part_elems * sizeof(double)));
+    st.up_common = true;
+    std::vector<Seg>().swap(st.segs);
+  }
+  int rc = host_lists(st, precision);
+  if (rc) return rc;
+  if (precision == ZMPO_PREC_SPLIT && !st.up_split) {
+    ListUpload U;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 4; ++j) U.add(&st.d_work_tc4[i][j], st.hl.wtc4[i][j]);
+    for (int i = 0; i < 2; ++i) U.add(&st.d_work_tcb[i], st.hl.wtcb[i]);
+    for (int i = 0; i < 3; ++i) {
+      U.add(&st.d_work_um[i], st.hl.um[i]);
+      U.add(&st.d_work_ul[i], st.hl.ul[i]);
+    }
+    U.add(&st.d_prep_a, st.hl.prep_a);
+    U.add(&st.d_prep_b, st.hl.prep_b);
+    U.add(&st.d_cmap, st.hl.cmap);
+    rc = U.run(&st.d_lists_split);
+    if (rc) return rc;
+    st.up_split = true;
+  } else if (precision == ZMPO_PREC_FP64 && !st.up_fp64) {
+    ListUpload U;
+    U.add(&st.d_work_fp64, st.hl.w64);
+    rc = U.run(&st.d_lists_fp64);
+    if (rc) return rc;
+    std::vector<Work>().swap(st.hl.w64);
+    st.up_fp64 = true;
+  } else if (precision == ZMPO_PREC_EMU64 && !st.up_emu) {
+    ListUpload U;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 4; ++j) U.add(&st.d_work_tc[i][j], st.hl.wtc[i][j]);
+    rc = U.run(&st.d_lists_emu);
+    if (rc) return rc;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 4; ++j) std::vector<Work>().swap(st.hl.wtc[i][j]);
+    st.up_emu = true;
+  }
+  return ZMPO_OK;
+}
+
+// A failed upload (out of device memory, say) frees every device copy of
+// the step, so a later call can try again from the host lists.
+static int upload_step(Step &st, int precision) {
+  const int rc = upload_lists(st, precision);
+  if (rc != ZMPO_OK) free_step(st);
+  return rc;
+}
+
+// Frees the device copies of every list family not (completely) uploaded.
 static void free_step(Step &st) {
+  if (!st.up_common) {
+    cudaFree(st.d_lists);
+    st.d_lists = nullptr;
+    st.d_segs = nullptr;
+    st.d_groups = nullptr;
+    st.d_cblocks = nullptr;
+    st.d_segb = nullptr;
+    st.d_reds = nullptr;
+    cudaFree(st.d_part);
+    st.d_part = nullptr;
+  }
+  if (!st.up_split) {
+    cudaFree(st.d_lists_split);
+    st.d_lists_split = nullptr;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 4; ++j) st.d_work_tc4[i][j] = nullptr;
+    for (int i = 0; i < 2; ++i) st.d_work_tcb[i] = nullptr;
+    for (int i = 0; i < 3; ++i) st.d_work_um[i] = st.d_work_ul[i] = nullptr;
+    st.d_prep_a = nullptr;
+    st.d_prep_b = nullptr;
+    st.d_cmap = nullptr;
+  }
+  if (!st.up_fp64) {
+    cudaFree(st.d_lists_fp64);
+    st.d_lists_fp64 = nullptr;
+    st.d_work_fp64 = nullptr;
+  }
+  if (!st.up_emu) {
+    cudaFree(st.d_lists_emu);
+    st.d_lists_emu = nullptr;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 4; ++j) st.d_work_tc[i][j] = nullptr;
+  }
+}
+
+// Every device allocation of the step (plan destruction).
+static void release_step(Step &st) {
   if (st.ev0) cudaEventDestroy((cudaEvent_t)st.ev0);
   if (st.ev1) cudaEventDestroy((cudaEvent_t)st.ev1);
   st.ev0 = st.ev1 = nullptr;
-  cudaFree(st.d_segs);
-  cudaFree(st.d_groups);
-  cudaFree(st.d_cblocks);
-  cudaFree(st.d_segb);
-  st.d_cblocks = nullptr;
-  st.d_segb = nullptr;
-  cudaFree(st.d_work_fp64);
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 4; ++j) {
-      cudaFree(st.d_work_tc[i][j]);
-      cudaFree(st.d_work_tc4[i][j]);
-      st.d_work_tc[i][j] = nullptr;
-      st.d_work_tc4[i][j] = nullptr;
-    }
-  for (int i = 0; i < 2; ++i) {
-    cudaFree(st.d_work_tcb[i]);
-    st.d_work_tcb[i] = nullptr;
-  }
-  for (int i = 0; i < 3; ++i) {
-    cudaFree(st.d_work_um[i]);
-    cudaFree(st.d_work_ul[i]);
-    st.d_work_um[i] = nullptr;
-    st.d_work_ul[i] = nullptr;
-  }
-  cudaFree(st.d_prep_a);
-  cudaFree(st.d_prep_b);
-  cudaFree(st.d_cmap);
-  st.d_cmap = nullptr;
+  st.up_common = st.up_split = st.up_fp64 = st.up_emu = false;
+  free_step(st);
   cudaFree(st.d_planes_own);
-  st.d_prep_a = nullptr;
-  st.d_prep_b = nullptr;
   st.d_planes_own = nullptr;
-  cudaFree(st.d_reds);
-  cudaFree(st.d_part);
-  st.d_reds = nullptr;
-  st.d_part = nullptr;
-  st.d_segs = nullptr;
-  st.d_groups = nullptr;
-  st.d_work_fp64 = nullptr;
 }
 
 static bool g_profile = false;
@@ -1370,7 +1501,7 @@ static void profile_collect(Step &st) {
 }
 
 static int run_step(Step &st, const Bufs &b, int precision, void *stream, bool cut_kept = true) {
-  int rc = upload_step(st);
+  int rc = upload_step(st, precision);
   if (rc) return rc;
   // one NVTX range per step ("zmpo.step<i>"), so a profiler can select the
   // launches of one step of a chain
@@ -1425,13 +1556,17 @@ struct ChainStep {
 namespace zmpo {
 // The single launch of a contraction plan whose device task lists exist
 // (used by the allocation-free entry point in kernels.cu).
-int contract_step_for(zmpo_engine *e, int plan_id, Step **out) {
+int contract_step_for(zmpo_engine *e, int plan_id, int precision, Step **out) {
   Plan *P = get_plan(e, plan_id, 1);
   if (!P) return fail(ZMPO_E_ID, "contract_exec_noalloc: unknown contraction plan");
-  if (!P->steps[0].uploaded)
+  const Step &st = P->steps[0];
+  const bool ready = st.up_common && (precision == ZMPO_PREC_SPLIT ? st.up_split
+                                      : precision == ZMPO_PREC_FP64 ? st.up_fp64
+                                                                    : st.up_emu);
+  if (!ready)
     return fail(ZMPO_E_ARG,
-                "contract_exec_noalloc: the plan has no device task lists yet; run it once "
-                "through zmpo_contract_exec during set-up");
+                "contract_exec_noalloc: the plan has no device task lists for this precision yet; run it "
+                "once at this precision through zmpo_contract_exec during set-up");
   *out = &P->steps[0];
   return ZMPO_OK;
 }
@@ -1490,7 +1625,7 @@ int zmpo_engine_destroy(zmpo_engine *e) {
   if (!e) return ZMPO_OK;
   for (auto &p : e->plans) {
     if (!p) continue;
-    for (auto &s : p->steps) free_step(s);
+    for (auto &s : p->steps) release_step(s);
     cudaFree(p->d_dblocks);
     cudaFree(p->d_dterms);
   }
@@ -1587,6 +1722,7 @@ int zmpo_contract_plan(zmpo_engine *e, int lay_a, int lay_b, int naxes, const in
   P->steps.back().idx = (int)P->steps.size() - 1;
   rc = build_step(works, P->steps.back());
   if (rc) return rc;
+  finish_step_structure(P->steps.back());
   P->flops = P->steps.back().flops;
   P->ntasks = P->steps.back().ntasks;
   e->plans.push_back(std::move(P));
@@ -1610,7 +1746,11 @@ int zmpo_contract_exec(zmpo_engine *e, int plan_id, const double *d_a, const dou
 // The steps of a chain have independent task lists: their GEMM mappings are
 // built on one host thread per step (error text is per thread, so it is
 // carried back to the caller's thread).
-static int build_steps_parallel(Plan *P, std::vector<std::vector<OutWork>> &step_works) {
+// The steps of a plan, one host thread per step: groups and segments, then
+// the work lists.  keep_ncsite > 0: a sigma plan of that many dot sites (its
+// steps keep the records of the operands fixed during a solve); 0: nothing
+// kept.
+static int build_steps_parallel(Plan *P, std::vector<std::vector<OutWork>> &step_works, int keep_ncsite) {
   const int nstep = (int)step_works.size();
   P->steps.resize(nstep);
   std::vector<int> rcs(nstep, ZMPO_OK);
@@ -1618,8 +1758,15 @@ static int build_steps_parallel(Plan *P, std::vector<std::vector<OutWork>> &step
   std::vector<std::thread> pool;
   for (int s = 0; s < nstep; ++s) {
     P->steps[s].idx = s;
+    P->steps[s].keep_side = keep_ncsite > 0 ? sigma_keep_side(keep_ncsite, s) : 0;
     pool.emplace_back([&, s]() {
       rcs[s] = build_step(step_works[s], P->steps[s]);
+      if (rcs[s] == ZMPO_OK) {
+        finish_step_structure(P->steps[s]);
+        // sigma plans: the 4-slice lists now (their record areas are placed
+        // in the workspace); other plans at their first 4-slice run
+        if (keep_ncsite > 0) build_split_lists(P->steps[s]);
+      }
       if (rcs[s]) msgs[s] = g_err;
     });
   }
@@ -1820,13 +1967,13 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
     }
   }
   {
-    int rc = build_steps_parallel(P.get(), step_works);
+    int rc = build_steps_parallel(P.get(), step_works, d->ncsite);
     if (rc) return rc;
     for (auto &st : P->steps) {
       P->exec_flops += st.flops;
       P->ntasks += st.ntasks;
     }
-    reserve_plane_region(P.get(), d->ncsite);
+    reserve_plane_region(P.get());
   }
   // ---- HDiag terms: out[l,r] += w * sum Ld[a,l] Wi[a,b] (Wj[b,c]) Rd[c,r]
   {
@@ -1940,7 +2087,7 @@ int zmpo_plan_kernel_count(zmpo_engine *e, int plan_id, int precision, int *coun
   if (!count) return fail(ZMPO_E_ARG, "plan_kernel_count: null output");
   int n = 0;
   for (auto &s : P->steps) {
-    int rc = upload_step(s);
+    int rc = host_lists(s, precision);
     if (rc) return rc;
     if (precision == ZMPO_PREC_FP64) {
       n += s.nwork_fp64 > 0;
@@ -1966,7 +2113,7 @@ int zmpo_plan_mma_macs(zmpo_engine *e, int plan_id, int precision, int nmax, dou
   const int which = precision == ZMPO_PREC_FP64 ? 0 : (precision == ZMPO_PREC_SPLIT ? 1 : 2);
   for (int i = 0; i < nmax; ++i) macs[i] = 0.0;
   for (size_t i = 0; i < P->steps.size(); ++i) {
-    int rc = upload_step(P->steps[i]);
+    int rc = host_lists(P->steps[i], precision);
     if (rc) return rc;
     if ((int)i < nmax) macs[i] = P->steps[i].mma_macs[which];
   }
@@ -2156,7 +2303,7 @@ int zmpo_renorm_plan(zmpo_engine *e, const zmpo_renorm_desc *d, int *plan_id) {
     }
   }
   {
-    int rc = build_steps_parallel(P.get(), step_works);
+    int rc = build_steps_parallel(P.get(), step_works, 0);
     if (rc) return rc;
     for (auto &st : P->steps) {
       P->exec_flops += st.flops;
@@ -2238,16 +2385,13 @@ int zmpo_plan_groups(zmpo_engine *e, int plan_id, int step, int64_t *ngroups, in
   const Step &st = P->steps[step];
   *ngroups = (int64_t)st.groups.size();
   if (!M) return ZMPO_OK;
-  if (st.segs.empty() && !st.groups.empty() && st.uploaded)
-    return fail(ZMPO_E_ARG, "plan_groups: segment list already moved to the device");
   for (size_t g = 0; g < st.groups.size(); ++g) {
     const Group &G = st.groups[g];
     M[g] = G.M;
     N[g] = G.N;
     if (nseg) nseg[g] = G.nseg;
     if (ktot) {
-      int64_t k = 0;
-      for (int i = 0; i < G.nseg; ++i) k += st.segs[G.seg0 + i].K;
+      const int64_t k = st.gk[g];
       ktot[g] = k;
     }
   }
@@ -2255,20 +2399,22 @@ int zmpo_plan_groups(zmpo_engine *e, int plan_id, int step, int64_t *ngroups, in
 }
 
 int zmpo_plan_step_tasks(zmpo_engine *e, int plan_id, int step, int64_t *counts, void *groups, void *segs,
-                         void *cblocks, void *segb) {
+                         void *cblocks, void *segb, void *reds) {
   Plan *P = get_plan(e, plan_id, 0);
   if (!P || step < 0 || step >= (int)P->steps.size() || !counts)
     return fail(ZMPO_E_ID, "plan_step_tasks: unknown plan or step");
   const Step &st = P->steps[step];
-  if (st.uploaded) return fail(ZMPO_E_ARG, "plan_step_tasks: task lists already moved to the device");
+  if (st.up_common) return fail(ZMPO_E_ARG, "plan_step_tasks: task lists already moved to the device");
   counts[0] = (int64_t)st.groups.size();
   counts[1] = (int64_t)st.segs.size();
   counts[2] = (int64_t)st.cblocks.size();
   counts[3] = (int64_t)st.segb.size();
+  counts[4] = (int64_t)st.reds.size();
   if (groups) memcpy(groups, st.groups.data(), st.groups.size() * sizeof(Group));
   if (segs) memcpy(segs, st.segs.data(), st.segs.size() * sizeof(Seg));
   if (cblocks) memcpy(cblocks, st.cblocks.data(), st.cblocks.size() * sizeof(ColBlock));
   if (segb) memcpy(segb, st.segb.data(), st.segb.size() * sizeof(SegB));
+  if (reds) memcpy(reds, st.reds.data(), st.reds.size() * sizeof(Reduction));
   return ZMPO_OK;
 }
 
@@ -2280,7 +2426,7 @@ int zmpo_device_status(zmpo_engine *e, int *code, int reset) {
 int zmpo_plan_destroy(zmpo_engine *e, int plan_id) {
   Plan *P = get_plan(e, plan_id, 0);
   if (!P) return fail(ZMPO_E_ID, "plan_destroy: unknown plan");
-  for (auto &s : P->steps) free_step(s);
+  for (auto &s : P->steps) release_step(s);
   cudaFree(P->d_dblocks);
   cudaFree(P->d_dterms);
   e->plans[plan_id].reset();

@@ -138,14 +138,17 @@ class Engine:
     COLBLOCK = numpy.dtype([("c_off", "i8"), ("scm", "i8"), ("scn", "i8"), ("n0", "i4"), ("n", "i4")],
                            align=True)
     SEGB = numpy.dtype([("b_off", "i8"), ("sbk", "i8"), ("sbn", "i8")], align=True)
+    REDUCTION = numpy.dtype([("c_off", "i8"), ("scm", "i8"), ("scn", "i8"), ("part_off", "i8"), ("M", "i4"),
+                             ("N", "i4"), ("nparts", "i4"), ("cbuf", "i4"), ("elem0", "i8")], align=True)
 
     def step_tasks(self, pid, step):
-        """Host copy of a step's task records (before its first execution)."""
-        cnt = numpy.zeros(4, dtype=numpy.int64)
-        check(_lib.lib().zmpo_plan_step_tasks(self.h, pid, step, lptr(cnt), None, None, None, None),
+        """Host copy of a step's task records (before its first execution):
+        groups, segments, column blocks, B parts, split-K sums."""
+        cnt = numpy.zeros(5, dtype=numpy.int64)
+        check(_lib.lib().zmpo_plan_step_tasks(self.h, pid, step, lptr(cnt), None, None, None, None, None),
               "plan_step_tasks")
         arrs = [numpy.zeros(int(n), dtype=d) for n, d in zip(cnt, (self.GROUP, self.SEG, self.COLBLOCK,
-                                                                   self.SEGB))]
+                                                                   self.SEGB, self.REDUCTION))]
         check(_lib.lib().zmpo_plan_step_tasks(self.h, pid, step, lptr(cnt), *[a.ctypes.data_as(ctypes.c_void_p)
                                                                                for a in arrs]),
               "plan_step_tasks")
