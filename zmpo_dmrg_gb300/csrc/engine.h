@@ -143,7 +143,6 @@ struct Step {
   UWork *d_work_ul[3] = {};         // long items (passes), by column tile 16 / 32 / 64
   int64_t *d_cmap = nullptr;        // column maps of the tcgen05 work items
   int64_t nwork_ul[3] = {};
-  bool split_done = false;          // split-K parts made (split_long_groups)
   int64_t nprep_a_kept = 0, nprep_b_kept = 0;  // the first items cut kept records
   // plane buffer of the step: a kept area (records of the operand sides in
   // keep_side -- bit 0 A, bit 1 B -- which stay fixed between calls) and a

@@ -33,6 +33,7 @@ namespace zmpo {
 
 static thread_local std::string g_err;
 
+
 static int fail(int code, const std::string &msg) {
   g_err = msg;
   return code;
@@ -440,6 +441,11 @@ struct MergeInfo {
   MergeKey key;
 };
 
+// threads of one step's group build, and the block tasks per thread below
+// which fewer are used
+constexpr int kBuildThreads = 4;
+constexpr int64_t kTasksPerThread = 8000;
+
 static void merge_column_blocks(Step &st, const std::vector<MergeInfo> &info) {
   std::unordered_map<MergeKey, std::vector<int>, MergeKeyHash> buckets;
   buckets.reserve(st.groups.size());
@@ -554,43 +560,90 @@ static void merge_column_blocks(Step &st, const std::vector<MergeInfo> &info) {
   st.segs.swap(segs);
 }
 
-static int build_step(std::vector<OutWork> &works, Step &st) {
-  st.segs.clear();
-  st.groups.clear();
-  {
-    // algorithmic traffic: every distinct operand tensor once, every output block once
-    struct Operand {
-      const Layout *l;
-      int64_t base;
-      int buf;
-      bool operator<(const Operand &o) const { return std::tie(l, base, buf) < std::tie(o.l, o.base, o.buf); }
-      bool operator==(const Operand &o) const { return l == o.l && base == o.base && buf == o.buf; }
-    };
-    std::vector<Operand> seen;
-    Operand lastA{nullptr, -1, -1}, lastB{nullptr, -1, -1};
-    double out_elems = 0.0;
-    for (auto &w : works) {
-      int64_t od[16];
-      w.lo->block_dims(w.ob, od);
-      double n = 1;
-      for (int j = 0; j < w.lo->rank; ++j) n *= (double)od[j];
-      out_elems += n;
-      for (auto &t : w.tasks) {
-        const Operand a{t.la, t.a_base, t.abuf}, b{t.lb, t.b_base, t.bbuf};
-        // consecutive tasks mostly read the same tensors: skip repeats early
-        // (the sort below removes the rest)
-        if (!(a == lastA)) seen.push_back(lastA = a);
-        if (!(b == lastB)) seen.push_back(lastB = b);
-      }
-    }
-    std::sort(seen.begin(), seen.end());
-    seen.erase(std::unique(seen.begin(), seen.end()), seen.end());
-    double in_elems = 0.0;
-    for (auto &o : seen) in_elems += (double)o.l->pk->size;
-    st.alg_bytes = 8.0 * (in_elems + out_elems);
-  }
+// Groups and segments of a range of output works (one part of a step, built
+// on its own thread; the parts are joined in order).
+struct GroupPart {
+  std::vector<Seg> segs;
+  std::vector<Group> groups;
   std::vector<MergeInfo> minfo;
-  for (auto &w : works) {
+  std::vector<Reduction> reds;   // offsets (part_off, elem0, part groups' c_off) local to the part
+  int64_t part_elems = 0, red_elems = 0;
+  double flops = 0.0;
+  int64_t ntasks = 0;
+  std::vector<Seg> tmp;
+};
+
+// A group longer than kSplitK slots (the last one built) becomes parts of
+// kSplitK slots (cut at segment boundaries or inside a segment), written to
+// the split-K scratch (buffer kPartialBuf, M x N each, row-major) and summed
+// in order into the group's output by a split-K reduction.
+static void split_last_group(GroupPart &out) {
+  const Group G = out.groups.back();
+  int64_t ktot = 0;
+  for (int i = 0; i < G.nseg; ++i) ktot += out.segs[G.seg0 + i].K;
+  if (ktot <= kSplitK || G.M == 0 || G.N == 0) return;
+  out.groups.pop_back();
+  out.minfo.pop_back();
+  out.tmp.assign(out.segs.begin() + G.seg0, out.segs.begin() + G.seg0 + G.nseg);
+  out.segs.resize(G.seg0);
+  Reduction r;
+  r.c_off = G.c_off;
+  r.scm = G.scm;
+  r.scn = G.scn;
+  r.M = G.M;
+  r.N = G.N;
+  r.cbuf = G.cbuf;
+  r.part_off = out.part_elems;
+  r.nparts = 0;
+  const int64_t mn = (int64_t)G.M * G.N;
+  Group cur{};
+  auto open_part = [&]() {
+    cur = Group{};
+    cur.c_off = out.part_elems;
+    cur.scm = G.N;
+    cur.scn = 1;
+    cur.M = G.M;
+    cur.N = G.N;
+    cur.cbuf = kPartialBuf;
+    cur.seg0 = (int32_t)out.segs.size();
+    cur.nseg = 0;
+    out.part_elems += mn;
+    r.nparts += 1;
+  };
+  auto close_part = [&]() {
+    out.groups.push_back(cur);
+    out.minfo.push_back(MergeInfo{});  // parts are never joined
+  };
+  open_part();
+  int64_t kin = 0;
+  for (const Seg &sgm : out.tmp) {
+    int64_t k0 = 0;
+    while (k0 < sgm.K) {
+      if (kin >= kSplitK) {
+        close_part();
+        open_part();
+        kin = 0;
+      }
+      const int64_t take = std::min<int64_t>(sgm.K - k0, kSplitK - kin);
+      Seg piece = sgm;
+      piece.a_off = sgm.a_off + k0 * sgm.sak;
+      piece.b_off = sgm.b_off + k0 * sgm.sbk;
+      piece.K = (int32_t)take;
+      out.segs.push_back(piece);
+      cur.nseg += 1;
+      kin += take;
+      k0 += take;
+    }
+  }
+  close_part();
+  r.elem0 = out.red_elems;
+  out.red_elems += mn;
+  out.reds.push_back(r);
+}
+
+static int build_groups(std::vector<OutWork> &works, size_t w0, size_t w1, GroupPart &out) {
+  for (size_t wi = w0; wi < w1; ++wi) {
+    OutWork &w = works[wi];
     const Layout &O = *w.lo;
     int64_t od[16], ost[16];
     O.block_dims(w.ob, od);
@@ -706,7 +759,7 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
       g.scn = scn;
       g.M = (int32_t)M;
       g.N = (int32_t)N;
-      g.seg0 = (int32_t)st.segs.size();
+      g.seg0 = (int32_t)out.segs.size();
       g.cbuf = w.cbuf;
       g.ncb = g.cb0 = g.sb0 = 0;
       for (auto &tk : w.tasks) {
@@ -723,8 +776,8 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
           for (int j : e1) m *= (double)ad[j];
           for (int j : e2) n *= (double)bd[j];
           for (int j : i1) k *= (double)ad[j];
-          st.flops += 2.0 * m * n * k;
-          st.ntasks += 1;
+          out.flops += 2.0 * m * n * k;
+          out.ntasks += 1;
         }
         int64_t a0 = tk.a_base + A.pk->off[tk.ab];
         int64_t b0 = tk.b_base + B.pk->off[tk.bb];
@@ -788,12 +841,124 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
           s.abuf = (int8_t)tk.abuf;
           s.bbuf = (int8_t)tk.bbuf;
           s.pad0 = s.pad1 = 0;
-          st.segs.push_back(s);
+          out.segs.push_back(s);
         }
       }
-      g.nseg = (int32_t)st.segs.size() - g.seg0;
-      st.groups.push_back(g);
-      minfo.push_back(mi);
+      g.nseg = (int32_t)out.segs.size() - g.seg0;
+      out.groups.push_back(g);
+      out.minfo.push_back(mi);
+      split_last_group(out);
+    }
+  }
+  return ZMPO_OK;
+}
+
+static int build_step(std::vector<OutWork> &works, Step &st) {
+  st.segs.clear();
+  st.groups.clear();
+  {
+    // algorithmic traffic: every distinct operand tensor once, every output block once
+    struct Operand {
+      const Layout *l;
+      int64_t base;
+      int buf;
+      bool operator<(const Operand &o) const { return std::tie(l, base, buf) < std::tie(o.l, o.base, o.buf); }
+      bool operator==(const Operand &o) const { return l == o.l && base == o.base && buf == o.buf; }
+    };
+    std::vector<Operand> seen;
+    Operand lastA{nullptr, -1, -1}, lastB{nullptr, -1, -1};
+    double out_elems = 0.0;
+    for (auto &w : works) {
+      int64_t od[16];
+      w.lo->block_dims(w.ob, od);
+      double n = 1;
+      for (int j = 0; j < w.lo->rank; ++j) n *= (double)od[j];
+      out_elems += n;
+      for (auto &t : w.tasks) {
+        const Operand a{t.la, t.a_base, t.abuf}, b{t.lb, t.b_base, t.bbuf};
+        // consecutive tasks mostly read the same tensors: skip repeats early
+        // (the sort below removes the rest)
+        if (!(a == lastA)) seen.push_back(lastA = a);
+        if (!(b == lastB)) seen.push_back(lastB = b);
+      }
+    }
+    std::sort(seen.begin(), seen.end());
+    seen.erase(std::unique(seen.begin(), seen.end()), seen.end());
+    double in_elems = 0.0;
+    for (auto &o : seen) in_elems += (double)o.l->pk->size;
+    st.alg_bytes = 8.0 * (in_elems + out_elems);
+  }
+  // parts of about equal task counts on their own threads (large steps)
+  int64_t ntask_all = 0;
+  for (auto &w : works) ntask_all += (int64_t)w.tasks.size();
+  const int nparts = (int)std::max<int64_t>(1, std::min<int64_t>(kBuildThreads, ntask_all / kTasksPerThread));
+  std::vector<size_t> cut(nparts + 1, works.size());
+  cut[0] = 0;
+  {
+    int64_t acc = 0;
+    int p = 1;
+    for (size_t i = 0; i < works.size() && p < nparts; ++i) {
+      acc += (int64_t)works[i].tasks.size();
+      if (acc * nparts >= ntask_all * p) cut[p++] = i + 1;
+    }
+  }
+  std::vector<GroupPart> parts(nparts);
+  std::vector<int> rcs(nparts, ZMPO_OK);
+  std::vector<std::string> msgs(nparts);
+  if (nparts == 1) {
+    rcs[0] = build_groups(works, 0, works.size(), parts[0]);
+    if (rcs[0]) return rcs[0];
+  } else {
+    std::vector<std::thread> pool;
+    for (int p = 0; p < nparts; ++p)
+      pool.emplace_back([&, p]() {
+        rcs[p] = build_groups(works, cut[p], cut[p + 1], parts[p]);
+        if (rcs[p]) msgs[p] = g_err;
+      });
+    for (auto &t : pool) t.join();
+    for (int p = 0; p < nparts; ++p)
+      if (rcs[p]) return fail(rcs[p], msgs[p]);
+  }
+  std::vector<MergeInfo> minfo;
+  st.reds.clear();
+  st.red_elems = st.part_elems = 0;
+  for (auto &p : parts) {
+    for (Reduction r : p.reds) {
+      r.part_off += st.part_elems;
+      r.elem0 += st.red_elems;
+      st.reds.push_back(r);
+    }
+    if (st.part_elems > 0)
+      for (Group &g : p.groups)
+        if (g.cbuf == kPartialBuf) g.c_off += st.part_elems;
+    st.part_elems += p.part_elems;
+    st.red_elems += p.red_elems;
+  }
+  if (nparts == 1) {
+    st.segs.swap(parts[0].segs);
+    st.groups.swap(parts[0].groups);
+    minfo.swap(parts[0].minfo);
+    st.flops += parts[0].flops;
+    st.ntasks += parts[0].ntasks;
+  } else {
+    size_t ns = 0, ng = 0;
+    for (auto &p : parts) {
+      ns += p.segs.size();
+      ng += p.groups.size();
+    }
+    st.segs.reserve(ns);
+    st.groups.reserve(ng);
+    minfo.reserve(ng);
+    for (auto &p : parts) {
+      const int32_t off = (int32_t)st.segs.size();
+      st.segs.insert(st.segs.end(), p.segs.begin(), p.segs.end());
+      for (Group g : p.groups) {
+        g.seg0 += off;
+        st.groups.push_back(g);
+      }
+      minfo.insert(minfo.end(), p.minfo.begin(), p.minfo.end());
+      st.flops += p.flops;
+      st.ntasks += p.ntasks;
     }
   }
   merge_column_blocks(st, minfo);
@@ -806,83 +971,6 @@ constexpr int kTileFP64M = 32, kTileFP64N = 32;
 // 64-slot or eight 32-slot chunks) and the row tiles of one work item
 constexpr int kBresMaxK = 256, kBresRun = 16;
 
-// Cut groups whose summed K exceeds kSplitK into parts of about kSplitK (at
-// segment boundaries, or inside a long segment); parts go to scratch and a
-// reduction sums them in order.
-
-static void split_long_groups(Step &st) {
-  if (st.split_done) return;
-  st.split_done = true;
-  std::vector<Group> out;
-  std::vector<Seg> segs;
-  out.reserve(st.groups.size());
-  segs.reserve(st.segs.size());
-  int64_t part = 0;
-  for (const Group &G : st.groups) {
-    int64_t ktot = 0;
-    for (int i = 0; i < G.nseg; ++i) ktot += st.segs[G.seg0 + i].K;
-    if (ktot <= kSplitK || G.M == 0 || G.N == 0) {
-      Group g = G;
-      g.seg0 = (int32_t)segs.size();
-      for (int i = 0; i < G.nseg; ++i) segs.push_back(st.segs[G.seg0 + i]);
-      out.push_back(g);
-      continue;
-    }
-    Reduction r;
-    r.c_off = G.c_off;
-    r.scm = G.scm;
-    r.scn = G.scn;
-    r.M = G.M;
-    r.N = G.N;
-    r.cbuf = G.cbuf;
-    r.part_off = part;
-    r.nparts = 0;
-    const int64_t mn = (int64_t)G.M * G.N;
-    Group cur{};
-    auto open_part = [&]() {
-      cur = Group{};
-      cur.c_off = part;
-      cur.scm = G.N;
-      cur.scn = 1;
-      cur.M = G.M;
-      cur.N = G.N;
-      cur.cbuf = kPartialBuf;
-      cur.seg0 = (int32_t)segs.size();
-      cur.nseg = 0;
-      part += mn;
-      r.nparts += 1;
-    };
-    open_part();
-    int64_t kin = 0;
-    for (int i = 0; i < G.nseg; ++i) {
-      Seg sgm = st.segs[G.seg0 + i];
-      int64_t k0 = 0;
-      while (k0 < sgm.K) {
-        if (kin >= kSplitK) {
-          out.push_back(cur);
-          open_part();
-          kin = 0;
-        }
-        const int64_t take = std::min<int64_t>(sgm.K - k0, kSplitK - kin);
-        Seg piece = sgm;
-        piece.a_off = sgm.a_off + k0 * sgm.sak;
-        piece.b_off = sgm.b_off + k0 * sgm.sbk;
-        piece.K = (int32_t)take;
-        segs.push_back(piece);
-        cur.nseg += 1;
-        kin += take;
-        k0 += take;
-      }
-    }
-    out.push_back(cur);
-    r.elem0 = st.red_elems;
-    st.red_elems += mn;
-    st.reds.push_back(r);
-  }
-  st.groups.swap(out);
-  st.segs.swap(segs);
-  st.part_elems = part;
-}
 
 // Groups the one-pass tensor-core kernel (kernels_umma.cu) takes in the
 // 4-slice path: the whole K in one exact pass, at least half a row tile.
@@ -1161,11 +1249,8 @@ static std::vector<int> cost_order(const Step &st) {
   return order;
 }
 
-// The structure every precision shares: split-K parts, per-group K.
-static void finish_step_structure(Step &st) {
-  split_long_groups(st);
-  step_group_k(st);
-}
+// The structure every precision shares: per-group K.
+static void finish_step_structure(Step &st) { step_group_k(st); }
 
 // Column tiles of the mma.sync kernels.  Columns: full pieces of the widest
 // tile, then one narrower tile for the rest (the smallest of 8/16/32/64 that
@@ -1210,7 +1295,8 @@ static void build_split_lists(Step &st) {
   wtcb[1].clear();
   UmmaLists UL;
   st.mma_macs[1] = 0.0;
-  for (int g : cost_order(st)) {
+  auto order = cost_order(st);
+  for (int g : order) {
     const Group &G = st.groups[g];
     const int64_t kt = st.gk[g];
     const double k16 = (double)((kt + 15) / 16 * 16);
