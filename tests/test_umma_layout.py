@@ -366,30 +366,72 @@ def test_epilogue_staging_and_tmem_chunks():
 
 
 def test_prepare_a_thread_maps():
-    """k_prep_a: the 256 threads' 16 loads of a 16-row staging block cover
-    every (row, slot < 256) once in both load maps (along the rows of a slot,
-    along the slots of a row), stay inside the staging pitch, and the cut map
-    covers every (k block, row, chunk) of the block once."""
-    assert "constexpr int PREP_RB = 16;" in SRC and "constexpr int PREP_STRIDE = umma::KMAX + 2;" in SRC
-    assert "const int lr = rows_fast ? (tid & 15) : (warp << 1);" in SRC
-    assert "const int lj = rows_fast ? (tid >> 4) : lane;" in SRC
-    assert "const int r = rows_fast ? lr : lr + (i & 1);" in SRC
-    assert "const int j = rows_fast ? lj + 16 * i : lj + 32 * (i >> 1);" in SRC
-    assert "const int ch = u & 3, r = (u >> 2) & (PREP_RB - 1), kb = u >> 6;" in SRC
-    RB, STRIDE, LOADS = 16, KMAX + 2, 16
-    for rows_fast in (True, False):
-        seen = set()
-        for tid in range(256):
-            warp, lane = tid >> 5, tid & 31
-            lr = (tid & 15) if rows_fast else (warp << 1)
-            lj = (tid >> 4) if rows_fast else lane
-            for i in range(LOADS):
-                r = lr if rows_fast else lr + (i & 1)
-                j = lj + 16 * i if rows_fast else lj + 32 * (i >> 1)
-                assert 0 <= r < RB and 0 <= j < KMAX and r * STRIDE + j < RB * STRIDE
-                seen.add((r, j))
-        assert len(seen) == RB * KMAX
+    """k_prep_a: for every block shape (W = the window's slots rounded up to a
+    power of two, RB = 4096 / W rows), the 256 threads' 16 loads cover every
+    (row, slot) of the block once in both load maps (along the rows of a
+    slot, along the slots of a row), stay inside the staging buffer, the
+    exponent map gives each row 256 / RB threads, and the cut map covers every
+    (k block, row, chunk) of the block once."""
+    assert "constexpr int PREP_ELEMS = 4096;" in SRC and "constexpr int PREP_STAGE = 128 * (32 + 2);" in SRC
+    assert "const int lw = nkb <= 1 ? 5 : (nkb <= 2 ? 6 : (nkb <= 4 ? 7 : 8));  // log2 W" in SRC
+    assert "const int W = 1 << lw, lrb = 12 - lw, RB = 1 << lrb, pitch = W + 2;" in SRC
+    assert "const int t_r = rows_fast ? (tid & (RB - 1)) : (tid >> lw);" in SRC
+    assert "const int t_j = rows_fast ? (tid >> lrb) : (tid & (W - 1));" in SRC
+    assert "const int step = rows_fast ? (PREP_THREADS >> lrb) : (PREP_THREADS >> lw);" in SRC
+    assert "const int ch = u & 3, r = (u >> 2) & (RB - 1), kb = u >> (lrb + 2);" in SRC
+    assert "const int ltpr = 8 - lrb, tpr = 1 << ltpr;" in SRC
+    STAGE = 128 * 34
     for nkb in range(1, KMAX // KB_SLOTS + 1):
-        cut = [((u >> 6), (u >> 2) & 15, u & 3) for u in range(nkb * RB * 4)]
+        lw = 5 if nkb <= 1 else (6 if nkb <= 2 else (7 if nkb <= 4 else 8))
+        W, lrb = 1 << lw, 12 - lw
+        RB, pitch = 1 << lrb, W + 2
+        assert nkb * KB_SLOTS <= W and RB * pitch <= STAGE
+        for rows_fast in (True, False):
+            seen = set()
+            for tid in range(256):
+                t_r = (tid & (RB - 1)) if rows_fast else (tid >> lw)
+                t_j = (tid >> lrb) if rows_fast else (tid & (W - 1))
+                step = (256 >> lrb) if rows_fast else (256 >> lw)
+                for i in range(16):
+                    r = t_r if rows_fast else t_r + step * i
+                    j = t_j + step * i if rows_fast else t_j
+                    assert 0 <= r < RB and 0 <= j < W and r * pitch + j < STAGE
+                    seen.add((r, j))
+            assert len(seen) == RB * W
+        tpr = 256 // RB
+        assert {tid >> (8 - lrb) for tid in range(256)} == set(range(RB)) and 32 % tpr == 0
+        cut = [(u >> (lrb + 2), (u >> 2) & (RB - 1), u & 3) for u in range(nkb << (lrb + 2))]
         assert len(set(cut)) == len(cut) == nkb * RB * 4
-        assert all(kb < nkb and kb * KB_SLOTS + ch * 8 + 7 < KMAX for kb, r, ch in cut)
+        assert all(kb < nkb and kb * KB_SLOTS + ch * 8 + 7 < W for kb, r, ch in cut)
+
+
+def test_prepare_a_address_sort():
+    """k_prep_a's bitonic sort (the kernel's loops over size and stride,
+    threads t < W, partner t ^ stride) orders the slots' row-0 addresses,
+    empty slots (key ~0) last, for every power-of-two width."""
+    import random
+    assert "for (int size = 2; size <= W; size <<= 1)" in SRC
+    assert "for (int stride = size >> 1; stride > 0; stride >>= 1) {" in SRC
+    assert "const bool up = (t & size) == 0;" in SRC and "if (up ? kt > kq : kt < kq) {" in SRC
+    rnd = random.Random(5)
+    for W in (32, 64, 128, 256):
+        for K in (1, W // 2 + 3, W - 1, W):
+            K = min(K, W)
+            addr = [rnd.randrange(1 << 40) for _ in range(K)]
+            key = [addr[t] if t < K else (1 << 64) - 1 for t in range(W)]
+            mem = list(range(W))
+            size = 2
+            while size <= W:
+                stride = size >> 1
+                while stride > 0:
+                    for t in range(W):
+                        q = t ^ stride
+                        if q > t:
+                            up = (t & size) == 0
+                            if (key[t] > key[q]) if up else (key[t] < key[q]):
+                                key[t], key[q] = key[q], key[t]
+                                mem[t], mem[q] = mem[q], mem[t]
+                    stride >>= 1
+                size <<= 1
+            assert key == sorted(key)
+            assert sorted(mem[:K]) == list(range(K)) and [addr[m] for m in mem[:K]] == sorted(addr)
