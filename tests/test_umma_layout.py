@@ -403,35 +403,3 @@ def test_prepare_a_thread_maps():
         cut = [(u >> (lrb + 2), (u >> 2) & (RB - 1), u & 3) for u in range(nkb << (lrb + 2))]
         assert len(set(cut)) == len(cut) == nkb * RB * 4
         assert all(kb < nkb and kb * KB_SLOTS + ch * 8 + 7 < W for kb, r, ch in cut)
-
-
-def test_prepare_a_address_sort():
-    """k_prep_a's bitonic sort (the kernel's loops over size and stride,
-    threads t < W, partner t ^ stride) orders the slots' row-0 addresses,
-    empty slots (key ~0) last, for every power-of-two width."""
-    import random
-    assert "for (int size = 2; size <= W; size <<= 1)" in SRC
-    assert "for (int stride = size >> 1; stride > 0; stride >>= 1) {" in SRC
-    assert "const bool up = (t & size) == 0;" in SRC and "if (up ? kt > kq : kt < kq) {" in SRC
-    rnd = random.Random(5)
-    for W in (32, 64, 128, 256):
-        for K in (1, W // 2 + 3, W - 1, W):
-            K = min(K, W)
-            addr = [rnd.randrange(1 << 40) for _ in range(K)]
-            key = [addr[t] if t < K else (1 << 64) - 1 for t in range(W)]
-            mem = list(range(W))
-            size = 2
-            while size <= W:
-                stride = size >> 1
-                while stride > 0:
-                    for t in range(W):
-                        q = t ^ stride
-                        if q > t:
-                            up = (t & size) == 0
-                            if (key[t] > key[q]) if up else (key[t] < key[q]):
-                                key[t], key[q] = key[q], key[t]
-                                mem[t], mem[q] = mem[q], mem[t]
-                    stride >>= 1
-                size <<= 1
-            assert key == sorted(key)
-            assert sorted(mem[:K]) == list(range(K)) and [addr[m] for m in mem[:K]] == sorted(addr)

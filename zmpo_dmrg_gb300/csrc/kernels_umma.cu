@@ -405,24 +405,21 @@ __device__ __forceinline__ double load_a(const Slot &sl, int row, bool scaled) {
 
 // ------------------------------------------------------------ prepare kernels
 // One A record per item (rows m0 .. m0+tm8-1, slots k0 .. k0+kc-1 of the
-// group), a block of 4096 elements at a time: the raw FP64 values are staged
-// in shared memory, the row exponents are taken there, and the rows are cut
-// from there into the four digit planes of every k block (a warp writes 8
-// rows x 4 chunks = 512 contiguous bytes of each plane); the 128 exponents
-// follow the planes.  Every value is read once.
+// group), a block of 4096 elements at a time: the raw FP64 values are copied
+// into shared memory with asynchronous 8-byte copies (cp.async, zero-filled
+// past the rows and slots of the item), the row exponents are taken there,
+// and the rows are cut from there into the four digit planes of every k
+// block (a warp writes 8 rows x 4 chunks = 512 contiguous bytes of each
+// plane); the 128 exponents follow the planes.  Every value is read once.
 //
 // A block is RB rows x W slots with W = the window's slots rounded up to a
 // power of two (32 .. 256) and RB = 4096 / W (128 .. 16 rows), so items with
-// a short K take many rows per block.  Each thread has 16 loads of a block;
-// those of the next block are issued before the current block is cut.  The
-// loads run along the rows when a slot's rows are contiguous (unit row
-// stride), else along the slots in the order of their addresses (a bitonic
-// sort of the slots' row-0 addresses, once per item), so that lanes next to
-// each other read memory next to each other also when the window's slots
-// interleave in memory (a K leg that the planner could not merge becomes a
-// loop of segments one element apart).  The slot table keeps only what the
-// loads need: the address of row 0, the row stride and the weight of every
-// slot of the window.
+// a short K take many rows per block.  The copies run along the rows when a
+// slot's rows are contiguous (unit row stride), else along the slots.  The
+// copies hold no registers, so many blocks per SM keep enough copies in
+// flight.  The slot table keeps what the copies need: the address of row 0,
+// the row stride and the weight of every slot of the window (weights are
+// applied when the staged values are read).
 constexpr int PREP_ELEMS = 4096;              // elements of a staging block
 constexpr int PREP_LOADS = PREP_ELEMS / umma::PREP_THREADS;  // 16 per thread and block
 // staging row pitch in float64: W + 2 (= 2 mod 16), so the 16 lanes of a half
@@ -494,17 +491,16 @@ __device__ int build_a_slots(const Group &g, const Seg *__restrict__ segs, const
 }
 }  // namespace umma
 
-__global__ void __launch_bounds__(umma::PREP_THREADS, 2)
+__global__ void __launch_bounds__(umma::PREP_THREADS, 4)
 k_prep_a(const PrepA *__restrict__ items, int64_t nitems, const Group *__restrict__ groups,
          const Seg *__restrict__ segs, Bufs bufs, unsigned char *__restrict__ planes) {
   using namespace umma;
   __shared__ ASlotTable tab;
-  __shared__ unsigned long long s_key[KMAX];  // row-0 address of a slot (sort key)
-  __shared__ short s_mem[KMAX];               // slots in the order of their addresses
   __shared__ int s_ctl[2];
   __shared__ int s_ea[TM];
   extern __shared__ double stage[];  // PREP_STAGE: RB rows x (W + 2)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t stage_s = smem_u32(stage);
   for (int64_t it = blockIdx.x; it < nitems; it += gridDim.x) {
     const PrepA p = items[it];
     const Group g = groups[p.group];
@@ -525,87 +521,41 @@ k_prep_a(const PrepA *__restrict__ items, int64_t nitems, const Group *__restric
     // block shape: W = kpad rounded up to a power of two, RB = 4096 / W rows
     const int lw = nkb <= 1 ? 5 : (nkb <= 2 ? 6 : (nkb <= 4 ? 7 : 8));  // log2 W
     const int W = 1 << lw, lrb = 12 - lw, RB = 1 << lrb, pitch = W + 2;
-    // rows contiguous for a slot (unit row stride): loads along the rows
+    // rows contiguous for a slot (unit row stride): copies along the rows
     const bool rows_fast = K > 0 && tab.sam[0] == 1;
-    if (!rows_fast && K > 0) {
-      // slots in the order of their row-0 addresses (bitonic sort over W
-      // entries; empty slots sort last)
-      for (int t = tid; t < W; t += PREP_THREADS) {
-        s_key[t] = t < K ? (unsigned long long)tab.a[t] : ~0ull;
-        s_mem[t] = (short)t;
-      }
-      for (int size = 2; size <= W; size <<= 1)
-        for (int stride = size >> 1; stride > 0; stride >>= 1) {
-          __syncthreads();
-          for (int t = tid; t < W; t += PREP_THREADS) {
-            const int q = t ^ stride;
-            if (q > t) {
-              const unsigned long long kt = s_key[t], kq = s_key[q];
-              const bool up = (t & size) == 0;
-              if (up ? kt > kq : kt < kq) {
-                s_key[t] = kq;
-                s_key[q] = kt;
-                const short mt = s_mem[t];
-                s_mem[t] = s_mem[q];
-                s_mem[q] = mt;
-              }
-            }
-          }
-        }
-      __syncthreads();
-    }
     // element e = tid + 256 i of a block: along the rows, the thread's row is
     // tid mod RB and its slots tid / RB + (256 / RB) i; along the slots, its
-    // slot (in address order) is tid mod W and its rows tid / W + (256 / W) i
+    // slot is tid mod W and its rows tid / W + (256 / W) i
     const int t_r = rows_fast ? (tid & (RB - 1)) : (tid >> lw);
     const int t_j = rows_fast ? (tid >> lrb) : (tid & (W - 1));
     const int step = rows_fast ? (PREP_THREADS >> lrb) : (PREP_THREADS >> lw);
-    const int t_slot = (!rows_fast && t_j < K) ? s_mem[t_j] : t_j;  // along the slots: the slot
-    const double *t_a = nullptr;
-    int64_t t_sam = 0;
-    double t_alpha = 1.0;
-    if (!rows_fast && t_j < K) {
-      t_a = tab.a[t_slot];
-      t_sam = tab.sam[t_slot];
-      t_alpha = tab.alpha[t_slot];
-    }
-    auto load_block = [&](double (&v)[PREP_LOADS], int rb) {
-#pragma unroll
-      for (int i = 0; i < PREP_LOADS; ++i) {
-        double x = 0.0;
-        if (rows_fast) {
-          const int j = t_j + step * i, grow = p.m0 + rb + t_r;
-          if (j < K && grow < g.M) {
-            x = __ldg(tab.a[j] + (int64_t)grow * tab.sam[j]);
-            if (scaled) x *= tab.alpha[j];
-          }
-        } else {
-          const int grow = p.m0 + rb + t_r + step * i;
-          if (t_j < K && grow < g.M) {
-            x = __ldg(t_a + (int64_t)grow * t_sam);
-            if (scaled) x *= t_alpha;
-          }
-        }
-        v[i] = x;
-      }
-    };
     unsigned char *rec = planes + p.rec;
-    double v[PREP_LOADS];
-    load_block(v, 0);
     for (int rb = 0; rb < tm8; rb += RB) {
-#pragma unroll
+#pragma unroll 4
       for (int i = 0; i < PREP_LOADS; ++i) {
         const int r = rows_fast ? t_r : t_r + step * i;
-        const int j = rows_fast ? t_j + step * i : t_slot;
-        if (j < kpad && r < RB) stage[r * pitch + j] = v[i];
+        const int j = rows_fast ? t_j + step * i : t_j;
+        if (j >= kpad) continue;
+        const int grow = p.m0 + rb + r;
+        const bool ok = j < K && grow < g.M;
+        // an empty element copies nothing (source size 0, zero fill) from a valid address
+        const double *src = ok ? tab.a[j] + (int64_t)grow * tab.sam[j] : reinterpret_cast<const double *>(planes);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(stage_s + 8u * (uint32_t)(r * pitch + j)),
+                     "l"(src), "r"(ok ? 8 : 0)
+                     : "memory");
       }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
       __syncthreads();
-      if (rb + RB < tm8) load_block(v, rb + RB);  // in flight during the cut
       {  // row exponents: 256 / RB threads per row
         const int ltpr = 8 - lrb, tpr = 1 << ltpr;
         const int r = tid >> ltpr, part = tid & (tpr - 1);
         int em = 0;
-        for (int j = part; j < kpad; j += tpr) em = max(em, dexp(stage[r * pitch + j]));
+        for (int j = part; j < kpad; j += tpr) {
+          double x = stage[r * pitch + j];
+          if (scaled) x *= tab.alpha[j < K ? j : 0];
+          em = max(em, dexp(x));
+        }
         for (int o = tpr >> 1; o >= 1; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o));
         if (rb + r < tm8 && part == 0) s_ea[rb + r] = em;
       }
@@ -615,7 +565,11 @@ k_prep_a(const PrepA *__restrict__ items, int64_t nitems, const Group *__restric
         if (rb + r >= tm8) continue;
         double x[8];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) x[i] = stage[r * pitch + kb * KB_SLOTS + ch * 8 + i];
+        for (int i = 0; i < 8; ++i) {
+          const int j = kb * KB_SLOTS + ch * 8 + i;
+          x[i] = stage[r * pitch + j];
+          if (scaled) x[i] *= tab.alpha[j < K ? j : 0];
+        }
         cut8_store(x, s_ea[rb + r], rec + (int64_t)kb * 4 * PL, PL, rb + r, ch);
       }
       __syncthreads();  // the staging block is refilled

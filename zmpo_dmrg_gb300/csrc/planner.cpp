@@ -1836,8 +1836,9 @@ int zmpo_contract_exec(zmpo_engine *e, int plan_id, const double *d_a, const dou
 // the work lists.  keep_ncsite > 0: a sigma plan of that many dot sites (its
 // steps keep the records of the operands fixed during a solve); 0: nothing
 // kept.
-static int build_steps_parallel(Plan *P, std::vector<std::vector<OutWork>> &step_works, int keep_ncsite) {
-  const int nstep = (int)step_works.size();
+extern "C++" {
+template <class MakeWorks>
+static int build_steps_parallel(Plan *P, int nstep, MakeWorks &&make_works, int keep_ncsite) {
   P->steps.resize(nstep);
   std::vector<int> rcs(nstep, ZMPO_OK);
   std::vector<std::string> msgs(nstep);
@@ -1846,7 +1847,9 @@ static int build_steps_parallel(Plan *P, std::vector<std::vector<OutWork>> &step
     P->steps[s].idx = s;
     P->steps[s].keep_side = keep_ncsite > 0 ? sigma_keep_side(keep_ncsite, s) : 0;
     pool.emplace_back([&, s]() {
-      rcs[s] = build_step(step_works[s], P->steps[s]);
+      std::vector<OutWork> works;
+      make_works(s, works);
+      rcs[s] = build_step(works, P->steps[s]);
       if (rcs[s] == ZMPO_OK) {
         finish_step_structure(P->steps[s]);
         // sigma plans: the 4-slice lists now (their record areas are placed
@@ -1861,6 +1864,7 @@ static int build_steps_parallel(Plan *P, std::vector<std::vector<OutWork>> &step
     if (rcs[s]) return fail(rcs[s], msgs[s]);
   return ZMPO_OK;
 }
+}  // extern "C++"
 
 int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
   if (!e || !d || !plan_id || d->nop < 0 || d->nclass < 1 || (d->ncsite != 1 && d->ncsite != 2))
@@ -1980,11 +1984,9 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
   };
   // buffers: 0 L, 1 R, 2 W, 3 x, 4 y, 5 workspace
   // operand sources per executed step (two-site: O, T1, T3, sigma).  The
-  // steps' task lists are independent: their output works are collected
-  // first and the GEMM mappings built on one host thread per step.
-  std::vector<std::vector<OutWork>> step_works(nstep);
-  for (int s = 0; s < nstep; ++s) {
-    std::vector<OutWork> &works = step_works[s];
+  // steps' task lists are independent: each step's output works and GEMM
+  // mappings are built on a host thread of its own.
+  auto make_works = [&](int s, std::vector<OutWork> &works) {
     auto src = [&](int op, bool isA, int &buf, int64_t &base) {
       if (d->ncsite == 2) {
         switch (s) {
@@ -2051,9 +2053,9 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
                                          bbuf, d->ncsite == 2 ? 1.0 : d->wts[op]});
       }
     }
-  }
+  };
   {
-    int rc = build_steps_parallel(P.get(), step_works, d->ncsite);
+    int rc = build_steps_parallel(P.get(), nstep, make_works, d->ncsite);
     if (rc) return rc;
     for (auto &st : P->steps) {
       P->exec_flops += st.flops;
@@ -2351,10 +2353,15 @@ int zmpo_renorm_plan(zmpo_engine *e, const zmpo_renorm_desc *d, int *plan_id) {
           break;
         }
   }
-  // buffers: 0 env, 2 W, 3 site, 4 out, 5 workspace
-  std::vector<std::vector<OutWork>> step_works(3);
-  for (int s = 0; s < 3; ++s) {
-    std::vector<OutWork> &works = step_works[s];
+  // the reference's work: every task of the three contractions per term
+  for (int op = 0; op < d->nop; ++op) {
+    const int c = d->op_class[op];
+    if (P->out_lay[c] < 0) continue;
+    for (int ci : {ch[c].c1, ch[c].c2, ch[c].c3}) P->flops += contraction_flops(e, e->contractions[ci].get());
+  }
+  // buffers: 0 env, 2 W, 3 site, 4 out, 5 workspace (the works of each step
+  // are made on that step's thread)
+  auto make_works = [&](int s, std::vector<OutWork> &works) {
     for (int op = 0; op < d->nop; ++op) {
       int c = d->op_class[op];
       if (P->out_lay[c] < 0) continue;
@@ -2371,7 +2378,6 @@ int zmpo_renorm_plan(zmpo_engine *e, const zmpo_renorm_desc *d, int *plan_id) {
       } else {
         abuf = 5; abase = w2[op]; bbuf = 3; bbase = 0; cbuf = 4; cbase = P->out_off[op];
       }
-      P->flops += contraction_flops(e, C);
       for (size_t ob = 0; ob < O->pk->flat.size(); ++ob) {
         if (s < 2 && !alive[c][s][ob]) continue;  // zero intermediate block
         OutWork w;
@@ -2387,9 +2393,9 @@ int zmpo_renorm_plan(zmpo_engine *e, const zmpo_renorm_desc *d, int *plan_id) {
         works.push_back(std::move(w));
       }
     }
-  }
+  };
   {
-    int rc = build_steps_parallel(P.get(), step_works, 0);
+    int rc = build_steps_parallel(P.get(), 3, make_works, 0);
     if (rc) return rc;
     for (auto &st : P->steps) {
       P->exec_flops += st.flops;
