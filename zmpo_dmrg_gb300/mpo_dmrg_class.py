@@ -674,7 +674,8 @@ class mpo_dmrg:
             else:
                 self._store_envs('rop', isite + ncsite - 1, fN)
             self.tick("store_envs")
-            torch.cuda.synchronize()
+            # no device synchronisation here: the renormalisation runs on the
+            # GPU while the host sets up the next dot and builds its plans
             self.timings.append((status, isite, t1 - t0, time.perf_counter() - t1, nmvps))
         self.updateBoundary(ncsite, sitelst, qred, srotR, status)
         eavs = numpy.array(elst).dot(self.wts)
