@@ -312,7 +312,16 @@ __device__ __forceinline__ double scaled_int_to_double(long long S, int e) {
   return __longlong_as_double((long long)(sign | ((unsigned long long)be << 52) | mant));
 }
 
-__device__ __forceinline__ long long lvl(uint32_t bits) { return (long long)__float2int_rz(__uint_as_float(bits)); }
+__device__ __forceinline__ int lvl(uint32_t bits) { return __float2int_rz(__uint_as_float(bits)); }
+
+// S = L0 2^24 + L1 2^16 + L2 2^8 + L3 from the four level sums (FP32 bit
+// patterns of exact integers: |L0| <= 2^22, |L1| <= 2^23, |L2| <= 3 2^22,
+// |L3| <= 2^24 for a pass of at most 256 slots of balanced digits, |d| <=
+// 128): L0 2^8 + L1 fits 32 bits, the rest is summed in 64 bits.
+__device__ __forceinline__ long long fold_levels(uint32_t b0, uint32_t b1, uint32_t b2, uint32_t b3) {
+  const int hi = lvl(b0) * 256 + lvl(b1);
+  return (long long)hi * 65536 + (long long)lvl(b2) * 256 + (long long)lvl(b3);
+}
 
 // The epilogue warp's 32 x 8 chunk (lane = row row0 + lane, val[i] =
 // column i) stored through the warp's 2 KB staging area: each store
@@ -832,7 +841,7 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
           double val[8];
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
-            const long long S = (lvl(v[0][i]) << 24) + (lvl(v[1][i]) << 16) + (lvl(v[2][i]) << 8) + lvl(v[3][i]);
+            const long long S = fold_levels(v[0][i], v[1][i], v[2][i], v[3][i]);
             val[i] = scaled_int_to_double(S, ea + eb[c0 + i] - BIAS);
           }
           store_chunk(stg, val, lane, m0 + quarter * 32, M, cb + c0, rs + c0, out, ok);
@@ -1070,7 +1079,7 @@ k_step_umma_long(const UWork *__restrict__ work, int64_t nwork, const Group *__r
           tmem_ld_wait();
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
-            const long long S = (lvl(v[0][i]) << 24) + (lvl(v[1][i]) << 16) + (lvl(v[2][i]) << 8) + lvl(v[3][i]);
+            const long long S = fold_levels(v[0][i], v[1][i], v[2][i], v[3][i]);
             acc[8 * jc + i] += scaled_int_to_double(S, ea + eb[c0 + i] - BIAS);
           }
         }
