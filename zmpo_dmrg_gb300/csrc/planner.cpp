@@ -446,7 +446,8 @@ struct MergeInfo {
 constexpr int kBuildThreads = 4;
 constexpr int64_t kTasksPerThread = 8000;
 
-static void merge_column_blocks(Step &st, const std::vector<MergeInfo> &info) {
+template <class StepLike>
+static void merge_column_blocks(StepLike &st, const std::vector<MergeInfo> &info) {
   std::unordered_map<MergeKey, std::vector<int>, MergeKeyHash> buckets;
   buckets.reserve(st.groups.size());
   for (size_t g = 0; g < st.groups.size(); ++g)
@@ -565,6 +566,8 @@ static void merge_column_blocks(Step &st, const std::vector<MergeInfo> &info) {
 struct GroupPart {
   std::vector<Seg> segs;
   std::vector<Group> groups;
+  std::vector<ColBlock> cblocks;
+  std::vector<SegB> segb;
   std::vector<MergeInfo> minfo;
   std::vector<Reduction> reds;   // offsets (part_off, elem0, part groups' c_off) local to the part
   int64_t part_elems = 0, red_elems = 0;
@@ -901,6 +904,24 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
       acc += (int64_t)works[i].tasks.size();
       if (acc * nparts >= ntask_all * p) cut[p++] = i + 1;
     }
+    // column-block groups join output blocks that read the same A tensor of
+    // one term: a part ends where the term of single-term works changes, so
+    // every join happens inside one part (and each part joins its own)
+    auto term = [&](size_t i, int64_t &base, const Layout *&la) {
+      const auto &t = works[i].tasks;
+      if (t.empty() || t.front().a_base != t.back().a_base || t.front().la != t.back().la) return false;
+      base = t.front().a_base;
+      la = t.front().la;
+      return true;
+    };
+    for (int q = 1; q < nparts; ++q) {
+      if (cut[q] < cut[q - 1]) cut[q] = cut[q - 1];
+      int64_t b0, b1;
+      const Layout *l0, *l1;
+      while (cut[q] > 0 && cut[q] < works.size() && term(cut[q] - 1, b0, l0) && term(cut[q], b1, l1) && b0 == b1 &&
+             l0 == l1)
+        ++cut[q];
+    }
   }
   std::vector<GroupPart> parts(nparts);
   std::vector<int> rcs(nparts, ZMPO_OK);
@@ -908,19 +929,24 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
   if (nparts == 1) {
     rcs[0] = build_groups(works, 0, works.size(), parts[0]);
     if (rcs[0]) return rcs[0];
+    merge_column_blocks(parts[0], parts[0].minfo);
   } else {
     std::vector<std::thread> pool;
     for (int p = 0; p < nparts; ++p)
       pool.emplace_back([&, p]() {
         rcs[p] = build_groups(works, cut[p], cut[p + 1], parts[p]);
+        if (rcs[p] == ZMPO_OK) merge_column_blocks(parts[p], parts[p].minfo);
         if (rcs[p]) msgs[p] = g_err;
       });
     for (auto &t : pool) t.join();
     for (int p = 0; p < nparts; ++p)
       if (rcs[p]) return fail(rcs[p], msgs[p]);
   }
-  std::vector<MergeInfo> minfo;
+  // join the parts in order: segment, column-block, B-part and scratch
+  // offsets shift by what the parts before hold
   st.reds.clear();
+  st.cblocks.clear();
+  st.segb.clear();
   st.red_elems = st.part_elems = 0;
   for (auto &p : parts) {
     for (Reduction r : p.reds) {
@@ -937,31 +963,39 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
   if (nparts == 1) {
     st.segs.swap(parts[0].segs);
     st.groups.swap(parts[0].groups);
-    minfo.swap(parts[0].minfo);
+    st.cblocks.swap(parts[0].cblocks);
+    st.segb.swap(parts[0].segb);
     st.flops += parts[0].flops;
     st.ntasks += parts[0].ntasks;
-  } else {
-    size_t ns = 0, ng = 0;
-    for (auto &p : parts) {
-      ns += p.segs.size();
-      ng += p.groups.size();
-    }
-    st.segs.reserve(ns);
-    st.groups.reserve(ng);
-    minfo.reserve(ng);
-    for (auto &p : parts) {
-      const int32_t off = (int32_t)st.segs.size();
-      st.segs.insert(st.segs.end(), p.segs.begin(), p.segs.end());
-      for (Group g : p.groups) {
-        g.seg0 += off;
-        st.groups.push_back(g);
-      }
-      minfo.insert(minfo.end(), p.minfo.begin(), p.minfo.end());
-      st.flops += p.flops;
-      st.ntasks += p.ntasks;
-    }
+    return ZMPO_OK;
   }
-  merge_column_blocks(st, minfo);
+  size_t ns = 0, ng = 0, nc = 0, nb = 0;
+  for (auto &p : parts) {
+    ns += p.segs.size();
+    ng += p.groups.size();
+    nc += p.cblocks.size();
+    nb += p.segb.size();
+  }
+  st.segs.reserve(ns);
+  st.groups.reserve(ng);
+  st.cblocks.reserve(nc);
+  st.segb.reserve(nb);
+  for (auto &p : parts) {
+    const int32_t soff = (int32_t)st.segs.size(), coff = (int32_t)st.cblocks.size(), boff = (int32_t)st.segb.size();
+    st.segs.insert(st.segs.end(), p.segs.begin(), p.segs.end());
+    st.cblocks.insert(st.cblocks.end(), p.cblocks.begin(), p.cblocks.end());
+    st.segb.insert(st.segb.end(), p.segb.begin(), p.segb.end());
+    for (Group g : p.groups) {
+      g.seg0 += soff;
+      if (g.ncb > 0) {
+        g.cb0 += coff;
+        g.sb0 += boff;
+      }
+      st.groups.push_back(g);
+    }
+    st.flops += p.flops;
+    st.ntasks += p.ntasks;
+  }
   return ZMPO_OK;
 }
 
