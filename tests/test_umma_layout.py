@@ -29,9 +29,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = open(os.path.join(ROOT, "zmpo_dmrg_gb300", "csrc", "kernels_umma.cu")).read()
 ENGINE = open(os.path.join(ROOT, "zmpo_dmrg_gb300", "csrc", "engine.h")).read()
 
-TM, KMAX, KB_SLOTS, ROW_BYTES, NTHREADS = 128, 256, 32, 64, 448
-EPI_WARPS, PROD_WARP, MMA_WARP = 12, 12, 13
-STG_BYTES = EPI_WARPS * 32 * 8 * 8
+TM, KMAX, KB_SLOTS, ROW_BYTES, NTHREADS = 128, 256, 32, 64, 576
+EPI_WARPS, PROD_WARP, MMA_WARP = 16, 16, 17
+STG_BYTES = EPI_WARPS * 32 * 4 * 8
 SMEM_MAX = 232448
 TX_MAX = (1 << 20) - 1
 
@@ -44,9 +44,9 @@ def test_constants_match_source():
     assert "constexpr int kUmmaTM = 128, kUmmaMaxK = 256, kUmmaKB = 32;" in ENGINE
     for name, val in [("ROW_BYTES", ROW_BYTES), ("NTHREADS", NTHREADS)]:
         assert re.search(r"constexpr int %s = %d;" % (name, val), SRC), name
-    assert "EPI_WARPS = 12, PROD_WARP = 12, MMA_WARP = 13" in SRC
+    assert "EPI_WARPS = 16, PROD_WARP = 16, MMA_WARP = 17" in SRC
     assert "EPI_GROUPS = EPI_WARPS / 4;" in SRC and "CHUNK_STEP = 8 * EPI_GROUPS;" in SRC
-    assert "STG_BYTES = EPI_WARPS * 32 * 8 * 8;" in SRC
+    assert "STG_BYTES = EPI_WARPS * 32 * 4 * 8;" in SRC
     assert (EPI_WARPS + 2) * 32 == NTHREADS
     assert "static constexpr int NSTAGE = TN == 64 ? 2 : 4;" in SRC
     # record sizes (engine.h) = the layout mirrored below
@@ -322,15 +322,17 @@ def test_descriptor_encodings():
 
 def test_epilogue_staging_and_tmem_chunks():
     """Epilogue warp w: TMEM lane quarter w % 4, 8-column chunks from 8 (w / 4)
-    in steps of 24 (at most NCH per warp, the long kernel's register sums);
-    its 2 KB staging area holds 32 rows x 8 float64; the
-    swizzled writes (lane = row) and reads (4 rows x 8 columns per
-    instruction) cover the area exactly once each."""
+    in steps of 32 (at most NCH per warp, the long kernel's register sums);
+    its 1 KB staging area holds 32 rows x 4 float64 (a chunk is stored in two
+    halves); the swizzled writes (lane = row) and reads (8 rows x 4 columns
+    per instruction) cover the area exactly once each, without bank
+    conflicts."""
     assert "tcgen05.ld.sync.aligned.32x32b.x8.b32" in SRC
     assert SRC.count("const int quarter = warp & 3, group = warp >> 2;") == 2
     assert "for (int c0 = 8 * group; c0 < TN; c0 += CHUNK_STEP) {" in SRC
     assert SRC.count("const int c0 = 8 * group + CHUNK_STEP * jc;") == 2
     assert "constexpr int NCH = (TN / 8 + EPI_GROUPS - 1) / EPI_GROUPS;" in SRC
+    assert SRC.count("double *stg = reinterpret_cast<double *>(sm + LY::OFF_STG) + warp * 128;") == 2
     assert EPI_WARPS % 4 == 0
     groups = EPI_WARPS // 4
     for TN in (16, 32, 64):
@@ -345,24 +347,24 @@ def test_epilogue_staging_and_tmem_chunks():
                         key = (q * 32 + lane, c0 + i)
                         cover[key] = cover.get(key, 0) + 1
         assert len(cover) == TM * TN and set(cover.values()) == {1}
-    widx = lambda lane, i: lane * 8 + (i ^ ((lane >> 1) & 7))
-    ridx = lambda r, col: r * 8 + (col ^ ((r >> 1) & 7))
-    assert "stg[lane * 8 + (i ^ ((lane >> 1) & 7))] = val[i];" in SRC
-    assert "stg[r * 8 + (col ^ ((r >> 1) & 7))];" in SRC
-    writes = sorted(widx(lane, i) for lane in range(32) for i in range(8))
-    reads = sorted(ridx(k * 4 + (lane >> 3), lane & 7) for k in range(8) for lane in range(32))
-    assert writes == list(range(256)) and reads == list(range(256))
-    # a read instruction: 4 rows x 8 columns, 4 distinct rows, all 8 columns each
-    for k in range(8):
-        rows = {k * 4 + (lane >> 3) for lane in range(32)}
-        assert len(rows) == 4
+    widx = lambda lane, i: lane * 4 + (i ^ ((lane >> 2) & 3))
+    ridx = lambda r, col: r * 4 + (col ^ ((r >> 2) & 3))
+    assert "stg[lane * 4 + (i ^ ((lane >> 2) & 3))] = val[4 * h + i];" in SRC
+    assert "stg[r * 4 + (col ^ ((r >> 2) & 3))];" in SRC
+    assert "const int r = k * 8 + (lane >> 2);" in SRC
+    writes = sorted(widx(lane, i) for lane in range(32) for i in range(4))
+    reads = sorted(ridx(k * 8 + (lane >> 2), lane & 3) for k in range(4) for lane in range(32))
+    assert writes == list(range(128)) and reads == list(range(128))
+    # a read instruction: 8 rows x 4 columns, 8 distinct rows, all 4 columns each
+    for k in range(4):
+        assert len({k * 8 + (lane >> 2) for lane in range(32)}) == 8
     # no bank conflicts: an 8-byte access is served per half warp (128 bytes);
     # its 16 lanes must hit 16 different bank pairs
     for hw in (range(0, 16), range(16, 32)):
-        for i in range(8):
+        for i in range(4):
             assert len({widx(lane, i) % 16 for lane in hw}) == 16
-        for k in range(8):
-            assert len({ridx(k * 4 + (lane >> 3), lane & 7) % 16 for lane in hw}) == 16
+        for k in range(4):
+            assert len({ridx(k * 8 + (lane >> 2), lane & 3) % 16 for lane in hw}) == 16
 
 
 def test_prepare_a_thread_maps():

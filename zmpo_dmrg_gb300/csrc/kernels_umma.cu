@@ -27,13 +27,13 @@
 //     block-sparse operands run with enough loads in flight.
 //  2. k_step_umma moves records into shared memory with bulk copies
 //     (cp.async.bulk, completion counted on mbarriers) and multiplies:
-//       warps 0-11 epilogue: warp w reads TMEM lanes 32(w%4).. (one output
-//                  row per thread) and every third 8-column chunk from
+//       warps 0-15 epilogue: warp w reads TMEM lanes 32(w%4).. (one output
+//                  row per thread) and every fourth 8-column chunk from
 //                  column 8(w/4), folds the levels and stores the tile;
-//       warp 12    producer: lane 0 issues the bulk copies (B tile of the
+//       warp 16    producer: lane 0 issues the bulk copies (B tile of the
 //                  work item, per row tile its exponents and column map, A
 //                  k blocks through a ring of stages);
-//       warp 13    TMEM allocation; lane 0 issues the MMAs and commits.
+//       warp 17    TMEM allocation; lane 0 issues the MMAs and commits.
 //     Level products: the B planes of a column tile of TN columns are stacked
 //     along N as B' = [B0 | B1 | B2 | B3] (4 TN rows of a K-major operand)
 //     and the four level accumulators of a row tile lie side by side in TMEM
@@ -68,11 +68,11 @@ constexpr int NKB_MAX = KMAX / KB_SLOTS;
 constexpr int ROW_BYTES = 64;                 // K-major rows of 32 bf16, 64-byte swizzle
 constexpr int A_PLANE = TM * ROW_BYTES;       // 8 KB: one digit plane of a k block
 constexpr int A_STAGE = 4 * A_PLANE;          // 32 KB: four planes
-constexpr int NTHREADS = 448;
-constexpr int EPI_WARPS = 12, PROD_WARP = 12, MMA_WARP = 13;
+constexpr int NTHREADS = 576;
+constexpr int EPI_WARPS = 16, PROD_WARP = 16, MMA_WARP = 17;
 constexpr int EPI_GROUPS = EPI_WARPS / 4;       // epilogue warps per TMEM lane quarter
 constexpr int CHUNK_STEP = 8 * EPI_GROUPS;      // column step between a warp's 8-column chunks
-constexpr int STG_BYTES = EPI_WARPS * 32 * 8 * 8;  // per epilogue warp: 32 rows x 8 float64
+constexpr int STG_BYTES = EPI_WARPS * 32 * 4 * 8;  // per epilogue warp: 32 rows x 4 float64
 constexpr int PREP_THREADS = 256;
 constexpr int BIAS = 2082;
 constexpr uint64_t WAIT_NS = 2000000000ull;   // 2 s bound on every wait
@@ -324,29 +324,32 @@ __device__ __forceinline__ long long fold_levels(uint32_t b0, uint32_t b1, uint3
 }
 
 // The epilogue warp's 32 x 8 chunk (lane = row row0 + lane, val[i] =
-// column i) stored through the warp's 2 KB staging area: each store
-// instruction then writes 4 rows x 8 consecutive columns (64 contiguous bytes
-// per row when the columns are in one output block).  The chunk's columns
-// are cb[i] (output offset of row 0, < 0: none) and rs[i] (row stride).  The
-// staging index is XOR-swizzled by bits 1-3 of the row, so the 16 lanes of a
-// half warp touch 16 different 8-byte bank pairs (no bank conflicts).
-// Called by every lane of the warp.
+// column i) stored through the warp's 1 KB staging area, four columns at a
+// time: each store instruction then writes 8 rows x 4 consecutive columns
+// (32 contiguous bytes per row when the columns are in one output block).
+// The chunk's columns are cb[i] (output offset of row 0, < 0: none) and
+// rs[i] (row stride).  The staging index is XOR-swizzled by bits 2-3 of the
+// row, so the 16 lanes of a half warp touch 16 different 8-byte bank pairs
+// (no bank conflicts).  Called by every lane of the warp.
 __device__ __forceinline__ void store_chunk(double *stg, const double *val, int lane, int row0, int M,
                                             const long long *cb, const long long *rs, double *out, bool ok) {
 #pragma unroll
-  for (int i = 0; i < 8; ++i) stg[lane * 8 + (i ^ ((lane >> 1) & 7))] = val[i];
-  __syncwarp();
-  if (ok) {
-    const int col = lane & 7;
-    const long long base = cb[col], stride = rs[col];
+  for (int h = 0; h < 2; ++h) {
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const int r = k * 4 + (lane >> 3);
-      const double x = stg[r * 8 + (col ^ ((r >> 1) & 7))];
-      if (row0 + r < M && base >= 0) out[base + (long long)(row0 + r) * stride] = x;
+    for (int i = 0; i < 4; ++i) stg[lane * 4 + (i ^ ((lane >> 2) & 3))] = val[4 * h + i];
+    __syncwarp();
+    if (ok) {
+      const int col = lane & 3;
+      const long long base = cb[4 * h + col], stride = rs[4 * h + col];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int r = k * 8 + (lane >> 2);
+        const double x = stg[r * 4 + (col ^ ((r >> 2) & 3))];
+        if (row0 + r < M && base >= 0) out[base + (long long)(row0 + r) * stride] = x;
+      }
     }
+    __syncwarp();
   }
-  __syncwarp();
 }
 
 // Slot table of the slots k0 .. k0+kc-1 of a group (one warp; kc <= KMAX):
@@ -804,12 +807,12 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
     __syncwarp();
   } else {
     // ================================================================= epilogue
-    // warp w reads TMEM lanes 32(w%4).. (tile rows) and every third 8-column
+    // warp w reads TMEM lanes 32(w%4).. (tile rows) and every fourth 8-column
     // chunk (from column 8(w/4))
     const int quarter = warp & 3, group = warp >> 2;
     const int e = quarter * 32 + lane;
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
-    double *stg = reinterpret_cast<double *>(sm + LY::OFF_STG) + warp * 256;
+    double *stg = reinterpret_cast<double *>(sm + LY::OFF_STG) + warp * 128;
     uint32_t t = 0;
     for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
       if (role_sync_or(2, EPI_WARPS * 32, *abort_flag != 0)) break;
@@ -1042,14 +1045,14 @@ k_step_umma_long(const UWork *__restrict__ work, int64_t nwork, const Group *__r
     __syncwarp();
   } else {
     // ================================================================= epilogue
-    // warp w reads TMEM lanes 32(w%4).. and every third 8-column chunk (from
+    // warp w reads TMEM lanes 32(w%4).. and every fourth 8-column chunk (from
     // column 8(w/4)); its sums (at most NCH chunks) stay in registers over
     // the passes
     constexpr int NCH = (TN / 8 + EPI_GROUPS - 1) / EPI_GROUPS;
     const int quarter = warp & 3, group = warp >> 2;
     const int e = quarter * 32 + lane;
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
-    double *stg = reinterpret_cast<double *>(sm + LY::OFF_STG) + warp * 256;
+    double *stg = reinterpret_cast<double *>(sm + LY::OFF_STG) + warp * 128;
     uint32_t t = 0;
     for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
       if (role_sync_or(2, EPI_WARPS * 32, *abort_flag != 0)) break;
