@@ -5,7 +5,8 @@ digit products:
 
 * every element x of a row i of A (column j of B) is written relative to the
   row's (column's) largest biased exponent E over the whole K of the product:
-  X = floor(|x| / 2^(E - 1053)) < 2^31, and X = d0 2^24 + d1 2^16 + d2 2^8 + d3
+  X = |x| / 2^(E - 1053) rounded to the nearest integer (halves up) <= 2^31,
+  and X = d0 2^24 + d1 2^16 + d2 2^8 + d3
   with d1..d3 in [-128, 127], d0 in [0, 128] (the bytes of X + 0x808080); the
   element's sign goes on every digit (``balanced_digits``);
 * the levels L_l = sum_{s+t=l} Da_s Db_t^T, l = 0..3, are integers below 2^24
@@ -35,15 +36,17 @@ def dexp(x):
 
 
 def aligned31(x, E):
-    """floor(|x| / 2^(E - 1053)) from the 32 leading significand bits, as the
-    kernel computes it (E >= the element's exponent)."""
+    """|x| / 2^(E - 1053) rounded to the nearest integer, halves up, from the
+    53-bit significand m: (m + 2^(s-1)) >> s with s = E - e + 22 capped at 63,
+    as the kernel computes it (E >= the element's exponent e; 0 for zero and
+    subnormals)."""
     b = numpy.ascontiguousarray(x, dtype=numpy.float64).view(numpy.uint64)
-    e = ((b >> 52) & 0x7ff).astype(numpy.int64)
+    e = ((b >> numpy.uint64(52)) & numpy.uint64(0x7ff)).astype(numpy.int64)
     mant = (b & numpy.uint64((1 << 52) - 1)) | numpy.uint64(1 << 52)
-    top32 = numpy.where(e > 0, mant >> numpy.uint64(21), numpy.uint64(0)).astype(numpy.int64)
-    sh = numpy.asarray(E, dtype=numpy.int64) - e
-    out = numpy.where(sh < 32, top32 >> numpy.clip(sh, 0, 63), 0)
-    return out >> 1
+    sh = numpy.minimum(numpy.asarray(E, dtype=numpy.int64) - e + 22, 63)
+    sh, mant = numpy.broadcast_arrays(sh, mant)
+    X = (mant + (numpy.uint64(1) << (sh - 1).astype(numpy.uint64))) >> sh.astype(numpy.uint64)
+    return numpy.where(e > 0, X.astype(numpy.int64), 0)
 
 
 def balanced_digits(x, E):

@@ -5,7 +5,7 @@
 // Arithmetic (exact model: tests/split_model.py).  Every FP64 element of a
 // row i of A (column j of B) is cut relative to the row's (column's) largest
 // biased exponent over the group's whole K into four balanced 8-bit digits
-// (X = d0 2^24 + d1 2^16 + d2 2^8 + d3 = floor(|x| / 2^(E-1053)) < 2^31,
+// (X = d0 2^24 + d1 2^16 + d2 2^8 + d3 = |x| / 2^(E-1053) rounded, <= 2^31,
 // |digit| <= 128, the element's sign on every digit), held as bf16 planes.
 // The tensor cores form the level sums
 //   L_l = sum_{s+t=l} A_s B_t^T,  l = 0..3  (10 digit products),
@@ -252,13 +252,17 @@ __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.
 // ------------------------------------------------------------ digit cut
 __device__ __forceinline__ int dexp(double x) { return (int)(((unsigned)__double2hiint(x) >> 20) & 0x7ffu); }
 
-// Y = floor(|x| / 2^(E-1053)) + 0x808080 (E >= exponent of x): the bytes of
-// Y are d0, d1+128, d2+128, d3+128
+// Y = X + 0x808080 with X = |x| / 2^(E-1053) rounded to the nearest integer
+// (halves up; E >= exponent of x, so X <= 2^31): the bytes of Y are d0, d1+128,
+// d2+128, d3+128.  From the 53-bit significand m: X = (m + 2^(s-1)) >> s with
+// s = E - e + 22 (capped at 63, where X is 0 for any m < 2^53).
 __device__ __forceinline__ uint32_t balanced(double x, int E) {
-  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-  const int e = (int)((hi >> 20) & 0x7ffu);
-  const uint32_t top = e ? ((((hi & 0xfffffu) | 0x100000u) << 11) | (lo >> 21)) : 0u;
-  return (__funnelshift_rc(top, 0u, (unsigned)(E - e)) >> 1) + 0x808080u;
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ffu);
+  const unsigned long long m = (b & 0xfffffffffffffull) | 0x10000000000000ull;
+  const int s = min(E - e + 22, 63);
+  const uint32_t X = e ? (uint32_t)((m + (1ull << (s - 1))) >> s) : 0u;
+  return X + 0x808080u;
 }
 
 // byte K of Y minus OFF as the bit pattern of an exact float (PRMT + FADD)
