@@ -28,6 +28,7 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = open(os.path.join(ROOT, "zmpo_dmrg_gb300", "csrc", "kernels_umma.cu")).read()
 ENGINE = open(os.path.join(ROOT, "zmpo_dmrg_gb300", "csrc", "engine.h")).read()
+PLANNER = open(os.path.join(ROOT, "zmpo_dmrg_gb300", "csrc", "planner.cpp")).read()
 
 TM, KMAX, KB_SLOTS, ROW_BYTES, NTHREADS = 128, 256, 32, 64, 576
 EPI_WARPS, PROD_WARP, MMA_WARP = 16, 16, 17
@@ -36,8 +37,16 @@ SMEM_MAX = 232448
 TX_MAX = (1 << 20) - 1
 
 
-def nstage(TN):
-    return 2 if TN == 64 else 4
+NKBBS = (8, 4, 2)   # B k blocks of the one-pass launches (a launch per class)
+
+
+def nstage(TN, NKBB):
+    """A ring of the one-pass kernel: as many 32 KB stages as the rest of the
+    227 KB leaves (at most 6) next to a B region of NKBB k blocks."""
+    b_kb = 4 * TN * ROW_BYTES
+    rec = TM * 4 + TN * 20 + 16
+    ring = SMEM_MAX - 1024 - NKBB * b_kb - 2 * rec - STG_BYTES - 16 - 8 * (11 + 2 * 6)
+    return min(ring // (4 * TM * ROW_BYTES), 6)
 
 
 def test_constants_match_source():
@@ -48,7 +57,6 @@ def test_constants_match_source():
     assert "EPI_GROUPS = EPI_WARPS / 4;" in SRC and "CHUNK_STEP = 8 * EPI_GROUPS;" in SRC
     assert "STG_BYTES = EPI_WARPS * 32 * 4 * 8;" in SRC
     assert (EPI_WARPS + 2) * 32 == NTHREADS
-    assert "static constexpr int NSTAGE = TN == 64 ? 2 : 4;" in SRC
     # record sizes (engine.h) = the layout mirrored below
     assert "umma_a_rec_bytes(int nkb, int tm8) { return (int64_t)nkb * 256 * tm8 + kUmmaTM * 4; }" in ENGINE
     assert "umma_b_kb_bytes(int tn) { return 4 * (int64_t)tn * 64; }" in ENGINE
@@ -65,11 +73,11 @@ def b_tile_bytes(nkb, tn):
     return nkb * 4 * tn * ROW_BYTES + tn * 4
 
 
-def layout(TN):
-    L = {"NSTAGE": nstage(TN)}
+def layout(TN, NKBB=8):
+    L = {"NSTAGE": nstage(TN, NKBB), "NKBB": NKBB}
     L["B_KB"] = 4 * TN * ROW_BYTES
     L["OFF_B"] = 0
-    L["OFF_A"] = L["OFF_B"] + (KMAX // KB_SLOTS) * L["B_KB"]
+    L["OFF_A"] = L["OFF_B"] + NKBB * L["B_KB"]
     L["A_PLANE"] = TM * ROW_BYTES
     L["A_STAGE"] = 4 * L["A_PLANE"]
     L["OFF_REC"] = L["OFF_A"] + L["NSTAGE"] * L["A_STAGE"]
@@ -90,7 +98,14 @@ def layout(TN):
 
 
 def test_layout_formulas_match_source():
-    for expr in ["B_KB = 4 * TN * ROW_BYTES", "OFF_A = OFF_B + NKB_MAX * B_KB",
+    assert "static constexpr int NSTAGE = RING_BYTES / A_STAGE < 6 ? RING_BYTES / A_STAGE : 6;" in SRC
+    assert ("RING_BYTES = 232448 - 1024 - NKBB * B_KB - 2 * REC_BYTES - STG_BYTES - 16 -\n"
+            "                                    8 * (BAR_A_FULL + 2 * 6);") in SRC
+    assert "return launch_umma_k<TN, 2>(work + ncls[0] + ncls[1], ncls[2], s, b, planes, nsm, stream);" in SRC
+    assert "if (nkb > NKBB) {" in SRC
+    for TN in (16, 32, 64):
+        assert [nstage(TN, k) for k in NKBBS] == {64: [2, 4, 5], 32: [4, 5, 5], 16: [5, 6, 6]}[TN]
+    for expr in ["B_KB = 4 * TN * ROW_BYTES", "OFF_A = OFF_B + NKBB * B_KB",
                  "OFF_REC = OFF_A + NSTAGE * A_STAGE",
                  "REC_EB = REC_EA + TM * 4", "REC_CB = REC_EB + TN * 4", "REC_RS = REC_CB + TN * 8",
                  "REC_INFO = REC_RS + TN * 8", "REC_BYTES = REC_INFO + 16", "OFF_STG = OFF_REC + 2 * REC_BYTES",
@@ -102,8 +117,9 @@ def test_layout_formulas_match_source():
 
 
 @pytest.mark.parametrize("TN", [16, 32, 64])
-def test_shared_memory_regions(TN):
-    L = layout(TN)
+@pytest.mark.parametrize("NKBB", NKBBS)
+def test_shared_memory_regions(TN, NKBB):
+    L = layout(TN, NKBB)
     assert L["SMEM"] <= SMEM_MAX
     regions = [("B", L["OFF_B"], L["OFF_A"]), ("A", L["OFF_A"], L["OFF_REC"]),
                ("rec", L["OFF_REC"], L["OFF_REC"] + 2 * L["REC_BYTES"]),
@@ -136,7 +152,9 @@ def test_bulk_copies(TN, nkb, tm8):
     """Every copy the producers issue: source offset inside the record, size a
     multiple of 16, destination inside its region; the bytes armed on a
     barrier phase equal the bytes copied and stay within range."""
-    L = layout(TN)
+    # the launch the planner routes an item of nkb B k blocks to
+    assert "return nkb > 4 ? 0 : (nkb > 2 ? 1 : 2);" in PLANNER
+    L = layout(TN, 8 if nkb > 4 else (4 if nkb > 2 else 2))
     akb = 4 * tm8 * ROW_BYTES
     A, B = a_tile_bytes(nkb, tm8), b_tile_bytes(nkb, TN)
     assert A % 16 == 0 and B % 16 == 0 and akb % 512 == 0
@@ -246,8 +264,9 @@ def tensor_core_read(start, row, k):
 
 
 @pytest.mark.parametrize("TN", [16, 32, 64])
-def test_swizzled_stores_match_descriptor_reads(TN):
-    L = layout(TN)
+@pytest.mark.parametrize("NKBB", NKBBS)
+def test_swizzled_stores_match_descriptor_reads(TN, NKBB):
+    L = layout(TN, NKBB)
     base = 1024 * 7   # any 1024-aligned dynamic-smem base
     # A: record k block kb (planes tm8 rows apart) -> stage s; plane p, row
     # r < tm8, slot j (the prepare kernel's cut8_store(row=r) into a plane of
@@ -267,8 +286,8 @@ def test_swizzled_stores_match_descriptor_reads(TN):
                             assert tensor_core_read(plane + k16 * 32, r, k) == w
                             assert plane <= w < plane + pl
     # B': record k block kb, plane p, column c -> operand row p*TN + c; the
-    # whole record's planes are copied to OFF_B
-    for kb in range(KMAX // KB_SLOTS):
+    # whole record's planes are copied to OFF_B (at most NKBB k blocks)
+    for kb in range(NKBB):
         blk = base + L["OFF_B"] + kb * L["B_KB"]
         for p in range(4):
             for c in range(TN):
@@ -277,12 +296,13 @@ def test_swizzled_stores_match_descriptor_reads(TN):
                     w = base + L["OFF_B"] + rec_off
                     k16, k = divmod(j, 16)
                     assert tensor_core_read(blk + k16 * 32, p * TN + c, k) == w
-                    assert blk <= w < blk + L["B_KB"]
+                    assert blk <= w < blk + L["B_KB"] and w < base + L["OFF_A"]
 
 
 @pytest.mark.parametrize("TN", [16, 32, 64])
-def test_mma_operand_and_tmem_ranges(TN):
-    L = layout(TN)
+@pytest.mark.parametrize("NKBB", NKBBS)
+def test_mma_operand_and_tmem_ranges(TN, NKBB):
+    L = layout(TN, NKBB)
     for a in range(4):
         n = (4 - a) * TN
         assert n % 16 == 0 and 16 <= n <= 256            # kind::f16, M = 128

@@ -140,6 +140,9 @@ struct Step {
   int64_t nprep_a = 0, nprep_b = 0;
   UWork *d_work_um[3] = {};
   int64_t nwork_um[3] = {};
+  // one-pass items of each column tile by the k blocks of their B tile
+  // (more than 4, 3-4, at most 2), in that order in d_work_um
+  int64_t nwork_um_cls[3][3] = {};
   UWork *d_work_ul[3] = {};         // long items (passes), by column tile 16 / 32 / 64
   int64_t *d_cmap = nullptr;        // column maps of the tcgen05 work items
   int64_t nwork_ul[3] = {};

@@ -80,6 +80,7 @@ static_assert(A_PLANE == kUmmaAPlane && A_STAGE == kUmmaAKB, "plane record layou
 
 // error codes recorded in g_umma_error (first one wins)
 constexpr int ERR_TIMEOUT_BASE = 100;         // + site of the wait
+constexpr int ERR_B_TILE = 90;                // a one-pass item's B tile exceeds its launch's B region
 
 // barrier indices (A ring after the fixed ones)
 enum {
@@ -93,13 +94,14 @@ enum {
   BAR_A_FULL = 11    // [NSTAGE] A k block copied -> MMA; then [NSTAGE] A_EMPTY (MMA commit -> producer)
 };
 
-template <int TN>
+// Shared memory of the one-pass kernel for column tiles of TN and items whose
+// B tile has at most NKBB k blocks: the resident B tile, then a ring of A k
+// blocks as deep as the rest of the 227 KB allows (at most 6 stages), so the
+// A blocks of the next row tiles are copied while the current one is
+// multiplied and folded.
+template <int TN, int NKBB>
 struct Layout {
-  static constexpr int NSTAGE = TN == 64 ? 2 : 4;        // A k-block ring
   static constexpr int B_KB = 4 * TN * ROW_BYTES;         // one k block of the four B planes
-  static constexpr int OFF_B = 0;
-  static constexpr int OFF_A = OFF_B + NKB_MAX * B_KB;
-  static constexpr int OFF_REC = OFF_A + NSTAGE * A_STAGE;
   // tile record (one per TMEM buffer): row exponents (copied from the A
   // tile), column exponents, output offsets of (row 0, column c) and row
   // strides (copied from the B tile, in that order), then m0, M, cbuf
@@ -109,7 +111,13 @@ struct Layout {
   static constexpr int REC_RS = REC_CB + TN * 8;          // int64 rowstride[TN]
   static constexpr int REC_INFO = REC_RS + TN * 8;        // int m0, M, cbuf, pad
   static constexpr int REC_BYTES = REC_INFO + 16;
-  static constexpr int OFF_STG = OFF_REC + 2 * REC_BYTES;  // epilogue staging, 2 KB per warp
+  static constexpr int RING_BYTES = 232448 - 1024 - NKBB * B_KB - 2 * REC_BYTES - STG_BYTES - 16 -
+                                    8 * (BAR_A_FULL + 2 * 6);
+  static constexpr int NSTAGE = RING_BYTES / A_STAGE < 6 ? RING_BYTES / A_STAGE : 6;  // A k-block ring
+  static constexpr int OFF_B = 0;
+  static constexpr int OFF_A = OFF_B + NKBB * B_KB;
+  static constexpr int OFF_REC = OFF_A + NSTAGE * A_STAGE;
+  static constexpr int OFF_STG = OFF_REC + 2 * REC_BYTES;  // epilogue staging, 1 KB per warp
   static constexpr int OFF_BAR = OFF_STG + STG_BYTES;
   static constexpr int BAR_A_EMPTY = BAR_A_FULL + NSTAGE;
   static constexpr int NBAR = BAR_A_FULL + 2 * NSTAGE;
@@ -118,6 +126,8 @@ struct Layout {
   static constexpr int SMEM = BYTES + 1024;               // + alignment of the base to 1024
   static constexpr int TMEM_COLS = 8 * TN;                // two buffers of four levels
   static_assert(TN == 16 || TN == 32 || TN == 64, "column tile");
+  static_assert(NKBB == 2 || NKBB == 4 || NKBB == NKB_MAX, "B k blocks of a launch");
+  static_assert(NSTAGE >= 2, "A ring of at least two stages");
   static_assert(B_KB == umma_b_kb_bytes(TN), "plane record layout");
   static_assert(OFF_A % 1024 == 0 && A_STAGE % 1024 == 0 && B_KB % 1024 == 0, "swizzle atoms");
   static_assert(OFF_REC % 16 == 0 && REC_EB % 16 == 0 && REC_BYTES % 16 == 0, "bulk-copy alignment");
@@ -661,12 +671,12 @@ k_prep_b(const PrepB *__restrict__ items, int64_t nitems, const Group *__restric
 }
 
 // ------------------------------------------------------------------ kernel
-template <int TN>
+template <int TN, int NKBB>
 __global__ void __launch_bounds__(umma::NTHREADS, 1)
 k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restrict__ groups,
             const unsigned char *__restrict__ planes, const int64_t *__restrict__ cmaps, Bufs bufs) {
   using namespace umma;
-  using LY = Layout<TN>;
+  using LY = Layout<TN, NKBB>;
   constexpr int NSTAGE = LY::NSTAGE;
   extern __shared__ unsigned char smem_raw[];
   const uint32_t raw_s = smem_u32(smem_raw);
@@ -723,6 +733,11 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
         const int nrt = wk.nrt_k & 0xff, K = wk.nrt_k >> 8;
         const int nkb = (K + KB_SLOTS - 1) / KB_SLOTS;
         const unsigned char *brec = planes + wk.b_rec;
+        if (nkb > NKBB) {  // the planner routes every item to a launch whose B region holds it
+          *abort_flag = 1;
+          atomicCAS(&g_umma_error, 0, ERR_B_TILE);
+          break;
+        }
         if (!(ok = wait_bounded(bar(BAR_B_FREE), (item & 1) ^ 1, abort_flag, 1))) break;
         bar_arrive_tx(bar(BAR_B_FULL), (uint32_t)(nkb * LY::B_KB));
         bulk_g2s(base_s + LY::OFF_B, brec, (uint32_t)(nkb * LY::B_KB), bar(BAR_B_FULL));
@@ -1139,22 +1154,35 @@ static int launch_umma_long_t(const UWork *work, int64_t nwork, const Step &s, c
   return e == cudaSuccess ? ZMPO_OK : record_cuda_error("k_step_umma_long", (int)e);
 }
 
-template <int TN>
-static int launch_umma_t(const UWork *work, int64_t nwork, const Step &s, const Bufs &b,
+template <int TN, int NKBB>
+static int launch_umma_k(const UWork *work, int64_t nwork, const Step &s, const Bufs &b,
                          const unsigned char *planes, int nsm, void *stream) {
   if (nwork == 0) return ZMPO_OK;
-  constexpr int smem = umma::Layout<TN>::SMEM;
+  constexpr int smem = umma::Layout<TN, NKBB>::SMEM;
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_step_umma<TN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_step_umma<TN, NKBB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return record_cuda_error("k_step_umma: shared memory attribute", (int)e);
     attr = true;
   }
   const int grid = (int)(nwork < nsm ? nwork : nsm);
-  k_step_umma<TN><<<grid, umma::NTHREADS, smem, (cudaStream_t)stream>>>(work, nwork, s.d_groups, planes, s.d_cmap,
-                                                                        b);
+  k_step_umma<TN, NKBB><<<grid, umma::NTHREADS, smem, (cudaStream_t)stream>>>(work, nwork, s.d_groups, planes,
+                                                                              s.d_cmap, b);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? ZMPO_OK : record_cuda_error("k_step_umma", (int)e);
+}
+
+// The one-pass items of a column tile lie in the list by the k blocks of
+// their B tile (more than 4, 3-4, at most 2): one launch per class, with the
+// A ring its B tile leaves room for.
+template <int TN>
+static int launch_umma_t(const UWork *work, const int64_t *ncls, const Step &s, const Bufs &b,
+                         const unsigned char *planes, int nsm, void *stream) {
+  int rc;
+  if ((rc = launch_umma_k<TN, umma::NKB_MAX>(work, ncls[0], s, b, planes, nsm, stream))) return rc;
+  if ((rc = launch_umma_k<TN, 4>(work + ncls[0], ncls[1], s, b, planes, nsm, stream))) return rc;
+  return launch_umma_k<TN, 2>(work + ncls[0] + ncls[1], ncls[2], s, b, planes, nsm, stream);
 }
 
 int launch_step_umma(const Step &s, const Bufs &b, unsigned char *planes, bool cut_kept, void *stream) {
@@ -1185,9 +1213,9 @@ int launch_step_umma(const Step &s, const Bufs &b, unsigned char *planes, bool c
   if ((rc = launch_umma_long_t<64>(s.d_work_ul[2], s.nwork_ul[2], s, b, planes, nsm, stream))) return rc;
   if ((rc = launch_umma_long_t<32>(s.d_work_ul[1], s.nwork_ul[1], s, b, planes, nsm, stream))) return rc;
   if ((rc = launch_umma_long_t<16>(s.d_work_ul[0], s.nwork_ul[0], s, b, planes, nsm, stream))) return rc;
-  if ((rc = launch_umma_t<64>(s.d_work_um[2], s.nwork_um[2], s, b, planes, nsm, stream))) return rc;
-  if ((rc = launch_umma_t<32>(s.d_work_um[1], s.nwork_um[1], s, b, planes, nsm, stream))) return rc;
-  return launch_umma_t<16>(s.d_work_um[0], s.nwork_um[0], s, b, planes, nsm, stream);
+  if ((rc = launch_umma_t<64>(s.d_work_um[2], s.nwork_um_cls[2], s, b, planes, nsm, stream))) return rc;
+  if ((rc = launch_umma_t<32>(s.d_work_um[1], s.nwork_um_cls[1], s, b, planes, nsm, stream))) return rc;
+  return launch_umma_t<16>(s.d_work_um[0], s.nwork_um_cls[0], s, b, planes, nsm, stream);
 }
 
 int umma_device_status(int *code, int reset) {

@@ -1394,6 +1394,16 @@ static void build_split_lists(Step &st) {
   st.nprep_a_kept = (int64_t)UL.pa[1].size();
   st.nprep_b_kept = (int64_t)UL.pb[1].size();
   for (int i = 0; i < 3; ++i) {
+    // one-pass items by the k blocks of their B tile (more than 4, 3-4, at
+    // most 2; the kernel of each class keeps a deeper A ring for a smaller B)
+    auto cls = [](const UWork &w) {
+      const int nkb = ((w.nrt_k >> 8) + kUmmaKB - 1) / kUmmaKB;
+      return nkb > 4 ? 0 : (nkb > 2 ? 1 : 2);
+    };
+    std::stable_sort(UL.w1[i].begin(), UL.w1[i].end(),
+                     [&](const UWork &x, const UWork &y) { return cls(x) < cls(y); });
+    for (int c = 0; c < 3; ++c) st.nwork_um_cls[i][c] = 0;
+    for (const UWork &w : UL.w1[i]) st.nwork_um_cls[i][cls(w)] += 1;
     st.nwork_um[i] = (int64_t)UL.w1[i].size();
     st.nwork_ul[i] = (int64_t)UL.wl[i].size();
     st.hl.um[i].swap(UL.w1[i]);
@@ -2219,7 +2229,10 @@ int zmpo_plan_kernel_count(zmpo_engine *e, int plan_id, int precision, int *coun
         for (int c = 0; c < 4; ++c) n += (s4 ? s.nwork_tc4[a][c] : s.nwork_tc[a][c]) > 0;
       if (s4) {
         n += (s.nwork_tcb[0] > 0) + (s.nwork_tcb[1] > 0) + (s.nprep_a > 0) + (s.nprep_b > 0);
-        for (int i = 0; i < 3; ++i) n += (s.nwork_um[i] > 0) + (s.nwork_ul[i] > 0);
+        for (int i = 0; i < 3; ++i) {
+          n += s.nwork_ul[i] > 0;
+          for (int c = 0; c < 3; ++c) n += s.nwork_um_cls[i][c] > 0;
+        }
       }
     }
     n += s.red_elems > 0;
