@@ -40,13 +40,25 @@ TX_MAX = (1 << 20) - 1
 NKBBS = (8, 4, 2)   # B k blocks of the one-pass launches (a launch per class)
 
 
-def nstage(TN, NKBB):
-    """A ring of the one-pass kernel: as many 32 KB stages as the rest of the
-    227 KB leaves (at most 6) next to a B region of NKBB k blocks."""
+BAR_A_FULL = 13
+
+
+def nbb(TN, NKBB):
+    """B buffers of the one-pass kernel: two when two fit next to a ring of at
+    least two A stages."""
     b_kb = 4 * TN * ROW_BYTES
     rec = TM * 4 + TN * 20 + 16
-    ring = SMEM_MAX - 1024 - NKBB * b_kb - 2 * rec - STG_BYTES - 16 - 8 * (11 + 2 * 6)
-    return min(ring // (4 * TM * ROW_BYTES), 6)
+    free = SMEM_MAX - 1024 - 2 * rec - STG_BYTES - 16 - 8 * (BAR_A_FULL + 2 * 6)
+    return 2 if free - 2 * NKBB * b_kb >= 2 * 4 * TM * ROW_BYTES else 1
+
+
+def nstage(TN, NKBB):
+    """A ring of the one-pass kernel: as many 32 KB stages as the rest of the
+    227 KB leaves (at most 6) next to the B buffers of NKBB k blocks."""
+    b_kb = 4 * TN * ROW_BYTES
+    rec = TM * 4 + TN * 20 + 16
+    free = SMEM_MAX - 1024 - 2 * rec - STG_BYTES - 16 - 8 * (BAR_A_FULL + 2 * 6)
+    return min((free - nbb(TN, NKBB) * NKBB * b_kb) // (4 * TM * ROW_BYTES), 6)
 
 
 def test_constants_match_source():
@@ -74,10 +86,10 @@ def b_tile_bytes(nkb, tn):
 
 
 def layout(TN, NKBB=8):
-    L = {"NSTAGE": nstage(TN, NKBB), "NKBB": NKBB}
+    L = {"NSTAGE": nstage(TN, NKBB), "NKBB": NKBB, "NBB": nbb(TN, NKBB)}
     L["B_KB"] = 4 * TN * ROW_BYTES
     L["OFF_B"] = 0
-    L["OFF_A"] = L["OFF_B"] + NKBB * L["B_KB"]
+    L["OFF_A"] = L["OFF_B"] + L["NBB"] * NKBB * L["B_KB"]
     L["A_PLANE"] = TM * ROW_BYTES
     L["A_STAGE"] = 4 * L["A_PLANE"]
     L["OFF_REC"] = L["OFF_A"] + L["NSTAGE"] * L["A_STAGE"]
@@ -89,7 +101,7 @@ def layout(TN, NKBB=8):
     L["REC_BYTES"] = L["REC_INFO"] + 16
     L["OFF_STG"] = L["OFF_REC"] + 2 * L["REC_BYTES"]
     L["OFF_BAR"] = L["OFF_STG"] + STG_BYTES
-    L["NBAR"] = 11 + 2 * L["NSTAGE"]
+    L["NBAR"] = BAR_A_FULL + 2 * L["NSTAGE"]
     L["OFF_MISC"] = L["OFF_BAR"] + L["NBAR"] * 8
     L["BYTES"] = L["OFF_MISC"] + 16
     L["SMEM"] = L["BYTES"] + 1024
@@ -99,20 +111,24 @@ def layout(TN, NKBB=8):
 
 def test_layout_formulas_match_source():
     assert "static constexpr int NSTAGE = RING_BYTES / A_STAGE < 6 ? RING_BYTES / A_STAGE : 6;" in SRC
-    assert ("RING_BYTES = 232448 - 1024 - NKBB * B_KB - 2 * REC_BYTES - STG_BYTES - 16 -\n"
-            "                                    8 * (BAR_A_FULL + 2 * 6);") in SRC
+    assert ("FREE_BYTES = 232448 - 1024 - 2 * REC_BYTES - STG_BYTES - 16 - 8 * (BAR_A_FULL + 2 * 6);") in SRC
+    assert "NBB = FREE_BYTES - 2 * NKBB * B_KB >= 2 * A_STAGE ? 2 : 1;" in SRC
+    assert "RING_BYTES = FREE_BYTES - NBB * NKBB * B_KB;" in SRC
+    assert "BAR_B_FULL = 8," in SRC and "BAR_B_FREE = 10," in SRC and "BAR_DONE = 12," in SRC
+    for TN in (16, 32, 64):
+        assert [nbb(TN, k) for k in NKBBS] == {64: [1, 2, 2], 32: [2, 2, 2], 16: [2, 2, 2]}[TN]
     assert "return launch_umma_k<TN, 2>(work + ncls[0] + ncls[1], ncls[2], s, b, planes, nsm, stream);" in SRC
     assert "if (nkb > NKBB) {" in SRC
     for TN in (16, 32, 64):
-        assert [nstage(TN, k) for k in NKBBS] == {64: [2, 4, 5], 32: [4, 5, 5], 16: [5, 6, 6]}[TN]
-    for expr in ["B_KB = 4 * TN * ROW_BYTES", "OFF_A = OFF_B + NKBB * B_KB",
+        assert [nstage(TN, k) for k in NKBBS] == {64: [2, 2, 4], 32: [2, 4, 5], 16: [4, 5, 6]}[TN]
+    for expr in ["B_KB = 4 * TN * ROW_BYTES", "OFF_A = OFF_B + NBB * NKBB * B_KB",
                  "OFF_REC = OFF_A + NSTAGE * A_STAGE",
                  "REC_EB = REC_EA + TM * 4", "REC_CB = REC_EB + TN * 4", "REC_RS = REC_CB + TN * 8",
                  "REC_INFO = REC_RS + TN * 8", "REC_BYTES = REC_INFO + 16", "OFF_STG = OFF_REC + 2 * REC_BYTES",
                  "OFF_BAR = OFF_STG + STG_BYTES",
                  "BAR_A_EMPTY = BAR_A_FULL + NSTAGE", "NBAR = BAR_A_FULL + 2 * NSTAGE",
                  "OFF_MISC = OFF_BAR + NBAR * 8", "BYTES = OFF_MISC + 16", "SMEM = BYTES + 1024",
-                 "TMEM_COLS = 8 * TN", "A_PLANE = TM * ROW_BYTES", "A_STAGE = 4 * A_PLANE", "BAR_A_FULL = 11"]:
+                 "TMEM_COLS = 8 * TN", "A_PLANE = TM * ROW_BYTES", "A_STAGE = 4 * A_PLANE", "BAR_A_FULL = 13"]:
         assert expr in SRC, expr
 
 
@@ -160,7 +176,8 @@ def test_bulk_copies(TN, nkb, tm8):
     assert A % 16 == 0 and B % 16 == 0 and akb % 512 == 0
     # B planes of a one-pass item
     size = nkb * L["B_KB"]
-    assert size % 16 == 0 and size <= L["OFF_A"] - L["OFF_B"] and size <= TX_MAX
+    assert size % 16 == 0 and size <= L["NKBB"] * L["B_KB"] and size <= TX_MAX
+    assert L["NBB"] * L["NKBB"] * L["B_KB"] == L["OFF_A"] - L["OFF_B"]
     # per row tile / pass: row exponents (end of the A record), column
     # exponents (end of the B record), the column map (TN offsets, TN strides
     # from the planner's array, 16 bytes per column)
@@ -286,14 +303,16 @@ def test_swizzled_stores_match_descriptor_reads(TN, NKBB):
                             assert tensor_core_read(plane + k16 * 32, r, k) == w
                             assert plane <= w < plane + pl
     # B': record k block kb, plane p, column c -> operand row p*TN + c; the
-    # whole record's planes are copied to OFF_B (at most NKBB k blocks)
-    for kb in range(NKBB):
-        blk = base + L["OFF_B"] + kb * L["B_KB"]
+    # whole record's planes are copied to B buffer bb (at most NKBB k blocks)
+    assert "bulk_g2s(base_s + LY::OFF_B + bb * (NKBB * LY::B_KB), brec, (uint32_t)(nkb * LY::B_KB)," in SRC
+    assert "const uint32_t b_s = base_s + LY::OFF_B + bb * (NKBB * LY::B_KB) + kb * LY::B_KB;" in SRC
+    for bb, kb in [(bb, kb) for bb in range(L["NBB"]) for kb in range(NKBB)]:
+        blk = base + L["OFF_B"] + bb * NKBB * L["B_KB"] + kb * L["B_KB"]
         for p in range(4):
             for c in range(TN):
                 for j in range(KB_SLOTS):
                     rec_off = kb * L["B_KB"] + p * TN * ROW_BYTES + store_offset(c, j // 8) + (j % 8) * 2
-                    w = base + L["OFF_B"] + rec_off
+                    w = base + L["OFF_B"] + bb * NKBB * L["B_KB"] + rec_off
                     k16, k = divmod(j, 16)
                     assert tensor_core_read(blk + k16 * 32, p * TN + c, k) == w
                     assert blk <= w < blk + L["B_KB"] and w < base + L["OFF_A"]

@@ -88,17 +88,18 @@ enum {
   BAR_T_EMPTY = 2,   // [2] epilogue (128) -> MMA
   BAR_E_FULL = 4,    // [2] tile record copied (+ producer's arrival) -> epilogue
   BAR_E_EMPTY = 6,   // [2] tile record read, epilogue (128) -> producer
-  BAR_B_FULL = 8,    // B tile of the item copied -> MMA
-  BAR_B_FREE = 9,    // MMA commit after the item -> producer
-  BAR_DONE = 10,     // MMA commit at the end (teardown)
-  BAR_A_FULL = 11    // [NSTAGE] A k block copied -> MMA; then [NSTAGE] A_EMPTY (MMA commit -> producer)
+  BAR_B_FULL = 8,    // [2] B tile of the item copied -> MMA (one per B buffer)
+  BAR_B_FREE = 10,   // [2] MMA commit after the item -> producer
+  BAR_DONE = 12,     // MMA commit at the end (teardown)
+  BAR_A_FULL = 13    // [NSTAGE] A k block copied -> MMA; then [NSTAGE] A_EMPTY (MMA commit -> producer)
 };
 
 // Shared memory of the one-pass kernel for column tiles of TN and items whose
-// B tile has at most NKBB k blocks: the resident B tile, then a ring of A k
-// blocks as deep as the rest of the 227 KB allows (at most 6 stages), so the
-// A blocks of the next row tiles are copied while the current one is
-// multiplied and folded.
+// B tile has at most NKBB k blocks: two B buffers when two fit next to a ring
+// of at least two A stages (the next item's B tile is copied while the
+// current item's row tiles run), else one; then a ring of A k blocks as deep
+// as the rest of the 227 KB allows (at most 6 stages), so the A blocks of the
+// next row tiles are copied while the current one is multiplied and folded.
 template <int TN, int NKBB>
 struct Layout {
   static constexpr int B_KB = 4 * TN * ROW_BYTES;         // one k block of the four B planes
@@ -111,11 +112,12 @@ struct Layout {
   static constexpr int REC_RS = REC_CB + TN * 8;          // int64 rowstride[TN]
   static constexpr int REC_INFO = REC_RS + TN * 8;        // int m0, M, cbuf, pad
   static constexpr int REC_BYTES = REC_INFO + 16;
-  static constexpr int RING_BYTES = 232448 - 1024 - NKBB * B_KB - 2 * REC_BYTES - STG_BYTES - 16 -
-                                    8 * (BAR_A_FULL + 2 * 6);
+  static constexpr int FREE_BYTES = 232448 - 1024 - 2 * REC_BYTES - STG_BYTES - 16 - 8 * (BAR_A_FULL + 2 * 6);
+  static constexpr int NBB = FREE_BYTES - 2 * NKBB * B_KB >= 2 * A_STAGE ? 2 : 1;  // B buffers
+  static constexpr int RING_BYTES = FREE_BYTES - NBB * NKBB * B_KB;
   static constexpr int NSTAGE = RING_BYTES / A_STAGE < 6 ? RING_BYTES / A_STAGE : 6;  // A k-block ring
-  static constexpr int OFF_B = 0;
-  static constexpr int OFF_A = OFF_B + NKBB * B_KB;
+  static constexpr int OFF_B = 0;                         // buffer b at OFF_B + b * NKBB * B_KB
+  static constexpr int OFF_A = OFF_B + NBB * NKBB * B_KB;
   static constexpr int OFF_REC = OFF_A + NSTAGE * A_STAGE;
   static constexpr int OFF_STG = OFF_REC + 2 * REC_BYTES;  // epilogue staging, 1 KB per warp
   static constexpr int OFF_BAR = OFF_STG + STG_BYTES;
@@ -703,8 +705,10 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
       bar_init(bar(BAR_E_FULL + s), 1);
       bar_init(bar(BAR_E_EMPTY + s), EPI_WARPS * 32);
     }
-    bar_init(bar(BAR_B_FULL), 1);
-    bar_init(bar(BAR_B_FREE), 1);
+    for (int s = 0; s < 2; ++s) {
+      bar_init(bar(BAR_B_FULL + s), 1);
+      bar_init(bar(BAR_B_FREE + s), 1);
+    }
     bar_init(bar(BAR_DONE), 1);
     for (int s = 0; s < NSTAGE; ++s) {
       bar_init(bar(BAR_A_FULL + s), 1);
@@ -722,7 +726,7 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
     // ================================================================ producer
     if (lane == 0) {
       uint32_t t = 0, q = 0, item = 0;
-      uint32_t nA[NSTAGE], nE[2] = {0u, 0u}, nB = 0;  // phases armed per barrier (for the drain)
+      uint32_t nA[NSTAGE], nE[2] = {0u, 0u}, nB[2] = {0u, 0u};  // phases armed per barrier (for the drain)
 #pragma unroll
       for (int s = 0; s < NSTAGE; ++s) nA[s] = 0;
       bool ok = true;
@@ -738,10 +742,13 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
           atomicCAS(&g_umma_error, 0, ERR_B_TILE);
           break;
         }
-        if (!(ok = wait_bounded(bar(BAR_B_FREE), (item & 1) ^ 1, abort_flag, 1))) break;
-        bar_arrive_tx(bar(BAR_B_FULL), (uint32_t)(nkb * LY::B_KB));
-        bulk_g2s(base_s + LY::OFF_B, brec, (uint32_t)(nkb * LY::B_KB), bar(BAR_B_FULL));
-        ++nB;
+        // B buffer of the item and its earlier uses
+        const uint32_t bb = LY::NBB == 2 ? (item & 1) : 0, ub = LY::NBB == 2 ? (item >> 1) : item;
+        if (!(ok = wait_bounded(bar(BAR_B_FREE + bb), (ub & 1) ^ 1, abort_flag, 1))) break;
+        bar_arrive_tx(bar(BAR_B_FULL + bb), (uint32_t)(nkb * LY::B_KB));
+        bulk_g2s(base_s + LY::OFF_B + bb * (NKBB * LY::B_KB), brec, (uint32_t)(nkb * LY::B_KB),
+                 bar(BAR_B_FULL + bb));
+        ++nB[bb];
         const unsigned char *arec = planes + wk.a_rec;
         for (int r = 0; r < nrt; ++r, ++t) {
           const uint32_t b = t & 1, u = t >> 1;
@@ -775,7 +782,8 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
         if (nA[s]) wait_bounded(bar(BAR_A_FULL + s), (nA[s] - 1) & 1, abort_flag, 10, false);
       for (int b = 0; b < 2; ++b)
         if (nE[b]) wait_bounded(bar(BAR_E_FULL + b), (nE[b] - 1) & 1, abort_flag, 11, false);
-      if (nB) wait_bounded(bar(BAR_B_FULL), (nB - 1) & 1, abort_flag, 12, false);
+      for (int b = 0; b < 2; ++b)
+        if (nB[b]) wait_bounded(bar(BAR_B_FULL + b), (nB[b] - 1) & 1, abort_flag, 12, false);
     }
     __syncwarp();
   } else if (warp == MMA_WARP) {
@@ -788,7 +796,8 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
         const int M = groups[wk.group].M;
         const int nrt = wk.nrt_k & 0xff, K = wk.nrt_k >> 8;
         const int nkb = (K + KB_SLOTS - 1) / KB_SLOTS;
-        const bool okb = wait_bounded(bar(BAR_B_FULL), item & 1, abort_flag, 4);
+        const uint32_t bb = LY::NBB == 2 ? (item & 1) : 0, ub = LY::NBB == 2 ? (item >> 1) : item;
+        const bool okb = wait_bounded(bar(BAR_B_FULL + bb), ub & 1, abort_flag, 4);
         tc_fence_after();
         for (int r = 0; r < nrt; ++r, ++t) {
           const uint32_t b = t & 1, u = t >> 1;
@@ -803,7 +812,7 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
             tc_fence_after();
             if (ok && okb && !*abort_flag) {
               const uint32_t a_s = base_s + LY::OFF_A + s * A_STAGE;
-              const uint32_t b_s = base_s + LY::OFF_B + kb * LY::B_KB;
+              const uint32_t b_s = base_s + LY::OFF_B + bb * (NKBB * LY::B_KB) + kb * LY::B_KB;
 #pragma unroll
               for (int k16 = 0; k16 < 2; ++k16) {
                 if (kb * KB_SLOTS + k16 * 16 >= K) break;
@@ -819,7 +828,7 @@ k_step_umma(const UWork *__restrict__ work, int64_t nwork, const Group *__restri
           }
           commit(bar(BAR_T_FULL + b));
         }
-        commit(bar(BAR_B_FREE));
+        commit(bar(BAR_B_FREE + bb));
       }
       commit(bar(BAR_DONE));
     }
