@@ -3,10 +3,12 @@
 Callers that cannot allocate device memory while they run -- work recorded into
 a CUDA graph by stream capture, or a host framework that owns the device
 memory budget -- use this variant: its split-K partial sums live in a fixed
-8 MiB array inside the library.  The test calls it through the C ABI twice in
+8 MiB array inside the library.  The tests call it through the C ABI twice in
 a row and checks both results against the regular ``zmpo_contract_exec`` on
-the same plan, for the FP64 and the split tensor-core path, and checks that a
-plan needing more scratch than the array holds is refused.  This file is
+the same plan, for the FP64 and the split tensor-core path, replay it from a
+CUDA graph recorded by stream capture, and check that a plan needing more
+scratch than the array holds, or a precision the set-up run did not use, is
+refused.  This file is
 collected last so that a failure here does not stop the other tests."""
 
 import numpy
@@ -74,3 +76,41 @@ def test_noalloc_refuses_oversized_scratch(gpu):
                                                E.device_ptr(out), _lib.PREC["fp64"], E.current_stream())
     assert rc == -6
     assert "8 MiB" in _lib.last_error()
+
+
+def test_noalloc_under_stream_capture(gpu):
+    """The use the entry point is for: after a set-up run and one warm call,
+    the call is recorded into a CUDA graph by stream capture and replayed; the
+    replay equals the regular entry point."""
+    import torch
+    from zmpo_dmrg_gb300 import engine as E, _lib
+    ref, outs, eng, pid, a, b = _run(gpu, [40, 24], [5000, 3000], [30, 20], "split", seed=5)
+    out = torch.full_like(ref, float("nan"))
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        rc = _lib.lib().zmpo_contract_exec_noalloc(eng.h, pid, E.device_ptr(a), E.device_ptr(b),
+                                                   E.device_ptr(out), _lib.PREC["split"], E.current_stream())
+    assert rc == 0, _lib.last_error()
+    for _ in range(2):
+        out.fill_(float("nan"))
+        graph.replay()
+        torch.cuda.synchronize()
+        assert torch.isfinite(out).all()
+        assert float(torch.linalg.norm(out - ref) / torch.linalg.norm(ref)) <= 1e-12
+
+
+def test_noalloc_needs_a_set_up_run_at_its_precision(gpu):
+    """Device task lists are made per precision at the first run: a call at a
+    precision the set-up did not use is refused before any launch."""
+    import torch
+    from zmpo_dmrg_gb300 import engine as E, _lib
+    eng = E.get()
+    la, lb = _layouts(eng, [40], [300], [30])
+    lo, pid = eng.contract_plan(la, lb, ([1], [0]))
+    a = torch.ones(40 * 300, dtype=torch.float64, device="cuda")
+    b = torch.ones(300 * 30, dtype=torch.float64, device="cuda")
+    out = torch.empty(40 * 30, dtype=torch.float64, device="cuda")
+    eng.contract_exec(pid, a, b, out, "fp64")
+    rc = _lib.lib().zmpo_contract_exec_noalloc(eng.h, pid, E.device_ptr(a), E.device_ptr(b),
+                                               E.device_ptr(out), _lib.PREC["split"], E.current_stream())
+    assert rc != 0 and "this precision" in _lib.last_error()
