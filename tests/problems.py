@@ -681,3 +681,65 @@ def host_sigma_terms(P, terms, x, gemm=None):
     y = run_tasks_on_host(eng, pid, nl, bufs, gemm)[4]
     eng.destroy_plan(pid)
     return y, groups_all
+
+
+def host_renorm(P, status):
+    """The engine's renormalisation plan for the oracle side of ``P`` (status
+    'L': the left environments extended by the dot's left site; 'R': the
+    right ones by the site right of the dot), built by the engine's planner
+    and executed on the host from the task records (NumPy model of the
+    kernels).  Returns the new environment of every term (empty where absent)
+    and the plan's groups per step.  Needs no GPU."""
+    from zmpo_dmrg_gb300 import engine as E, mpo as pm
+    from oracle.qtensor import qtensor
+    m = P.o
+    eng = E.get()
+
+    def lay(t):
+        return eng.layout(t.qsyms, t.ndims, t.status)
+
+    A, B = _renorm_site(P)
+    if status == 'L':
+        t = qtensor([False, False, True])
+        t.fromDenseTensor(A, [P.qnuml[P.isite], QPHYS, P.qnuml[P.isite + 1]])
+        fE, jsite = m.flst[0][0], P.isite
+    else:
+        t = qtensor([True, False, False])
+        t.fromDenseTensor(B, [P.qnumr[P.isite + 1], QPHYS, P.qnumr[P.isite + 2]])
+        fE, jsite = m.flst[0][1], P.isite + 1
+    ops, Ev, Wv, off_env, off_W = [], [], [], [], []
+    classes, op_cls, lay_env, lay_W = {}, [], [], []
+    pos = {"E": 0, "W": 0}
+    for iop in range(m.nops):
+        Et = fE['opers%d' % iop]
+        if Et is None:
+            continue
+        Wt = m.fhop['site%d/op%d' % (jsite, iop)]
+        ops.append(iop)
+        off_env.append(pos["E"]); Ev.append(Et.value); pos["E"] += Et.value.size
+        off_W.append(pos["W"]); Wv.append(Wt.value); pos["W"] += Wt.value.size
+        c0 = pm.op_class(m.opers[iop][0], jsite)
+        if c0 not in classes:
+            classes[c0] = len(classes)
+            lay_env.append(lay(Et))
+            if status == 'L':
+                lay_W.append(lay(Wt))
+            else:
+                st = numpy.array(Wt.status).copy()
+                st[0], st[1] = not st[0], not st[1]
+                lay_W.append(eng.derive(lay(Wt), [-Wt.qsyms[0], -Wt.qsyms[1], Wt.qsyms[2], Wt.qsyms[3]], st))
+        op_cls.append(classes[c0])
+    pid, lay_out, off_out, total, ws = eng.renorm_plan(status, op_cls, lay_env, lay_W, lay(t), off_env, off_W)
+    bufs = [numpy.concatenate(Ev), numpy.zeros(1), numpy.concatenate(Wv), t.value.copy(), numpy.zeros(max(total, 1)),
+            numpy.zeros(max(ws // 8, 1)), numpy.zeros(1), numpy.zeros(1)]
+    groups_all = [eng.step_tasks(pid, st)[0] for st in range(3)]
+    out = run_tasks_on_host(eng, pid, 3, bufs)[4]
+    envs = [numpy.zeros(0) for _ in range(m.nops)]
+    for k, iop in enumerate(ops):
+        c = op_cls[k]
+        if lay_out[c] < 0 or off_out[k] < 0:
+            continue
+        size = eng.layout_blocks(int(lay_out[c]))[0]
+        envs[iop] = out[off_out[k]:off_out[k] + size]
+    eng.destroy_plan(pid)
+    return envs, groups_all

@@ -415,3 +415,23 @@ def test_plan_caches_are_released_with_their_driver():
     del d
     gc.collect()
     assert Plan.released == 2 and not cache
+
+
+@pytest.mark.parametrize("status", ["L", "R"])
+def test_renorm_task_lists_compute_the_oracle_environments(status):
+    """The engine's renormalisation plan (site . env, W . T1, T2 . site per
+    term, the reference's chain of renormQt_H00) executed from its task
+    records by the NumPy model of the kernels equals the oracle's new
+    environments (FP64, 1e-12 of each term's largest element): checks the
+    planner's addressing of every step on the CPU."""
+    from tests.problems import random_problem, host_renorm, oracle_renorm
+    P = random_problem(K=6, nelec=6, D=16, isite=2, seed=1, device=False)
+    got, groups = host_renorm(P, status)
+    ref = oracle_renorm(P, status)
+    n = 0
+    for g, r in zip(got, ref):
+        assert g.size == r.size
+        if r.size:
+            n += 1
+            assert numpy.abs(g - r).max() <= 1e-12 * max(numpy.abs(r).max(), 1.0)
+    assert n > 10
