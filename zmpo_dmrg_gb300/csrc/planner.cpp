@@ -272,8 +272,11 @@ static bool same_q(const Layout &A, int la, const Layout &B, int lb) {
 }
 
 // tensordotSYM: output layout + task list (qtensor.py:563-637)
-static int build_contraction(zmpo_engine *e, int ia, int ib, int naxes, const int *ax_a,
-                             const int *ax_b, int *out_layout, int *out_contr) {
+// The output layout and the contraction go to the given (existing, empty)
+// slots of the engine's tables, so several contractions can be built at
+// once on different threads into slots reserved in advance.
+static int build_contraction_at(zmpo_engine *e, int ia, int ib, int naxes, const int *ax_a,
+                                const int *ax_b, int lay_slot, int contr_slot) {
   Layout *A = get_layout(e, ia), *B = get_layout(e, ib);
   if (!A || !B) return fail(ZMPO_E_ID, "contract: unknown layout");
   auto C = std::make_unique<Contraction>();
@@ -362,11 +365,25 @@ static int build_contraction(zmpo_engine *e, int ia, int ib, int naxes, const in
     }
   }
   C->task_start[O->pk->flat.size()] = (int64_t)C->tasks.size();
-  int lo = add_layout(e, std::move(O));
-  C->lay_out = lo;
-  e->contractions.push_back(std::move(C));
-  *out_layout = lo;
-  *out_contr = (int)e->contractions.size() - 1;
+  e->layouts[lay_slot] = std::move(O);
+  C->lay_out = lay_slot;
+  e->contractions[contr_slot] = std::move(C);
+  return ZMPO_OK;
+}
+
+static int build_contraction(zmpo_engine *e, int ia, int ib, int naxes, const int *ax_a,
+                             const int *ax_b, int *out_layout, int *out_contr) {
+  e->layouts.emplace_back();
+  e->contractions.emplace_back();
+  const int ls = (int)e->layouts.size() - 1, cs = (int)e->contractions.size() - 1;
+  const int rc = build_contraction_at(e, ia, ib, naxes, ax_a, ax_b, ls, cs);
+  if (rc) {
+    e->layouts.pop_back();
+    e->contractions.pop_back();
+    return rc;
+  }
+  *out_layout = ls;
+  *out_contr = cs;
   return ZMPO_OK;
 }
 
@@ -644,7 +661,22 @@ static void split_last_group(GroupPart &out) {
   out.reds.push_back(r);
 }
 
+// Per-task geometry of one output work, independent of its sub-regions:
+// block dimensions and strides of both operands, the block offsets, the
+// primary M / N / K strides, the K loops left after merging contiguous K
+// legs, and the stride each sub-region loop adds to the A or B offset.
+struct TaskGeo {
+  int64_t ad[16], as[16], bd[16], bs[16];
+  int64_t a0, b0, sam, sbn, sak, sbk, K, nk;
+  int nkloop;
+  Leg2 kloops[16];
+  int64_t ls[16];
+};
+
 static int build_groups(std::vector<OutWork> &works, size_t w0, size_t w1, GroupPart &out) {
+  std::vector<TaskGeo> geo;                          // reused across the works
+  std::vector<std::pair<int, int>> mr, nr, loops;    // merged M / N legs, sub-region loops (range, isM)
+  std::vector<int64_t> lidx;
   for (size_t wi = w0; wi < w1; ++wi) {
     OutWork &w = works[wi];
     const Layout &O = *w.lo;
@@ -657,6 +689,15 @@ static int build_groups(std::vector<OutWork> &works, size_t w0, size_t w1, Group
     int ne1 = w.tasks.empty() ? O.rank : (int)w.tasks[0].c->e1.size();
     for (auto &t : w.tasks)
       if ((int)t.c->e1.size() != ne1) return fail(ZMPO_E_ARG, "mixed contraction split");
+    geo.resize(w.tasks.size());
+    for (size_t ti = 0; ti < w.tasks.size(); ++ti) {
+      const TaskRef &tk = w.tasks[ti];
+      TaskGeo &gt = geo[ti];
+      tk.la->block_dims(tk.ab, gt.ad);
+      tk.lb->block_dims(tk.bb, gt.bd);
+      rowmajor_strides(gt.ad, tk.la->rank, gt.as);
+      rowmajor_strides(gt.bd, tk.lb->rank, gt.bs);
+    }
     // Determine M decomposition valid for C and every task's A; likewise N.
     // Represent each merged leg by its range of original legs.
     auto decompose = [&](int j0, int j1, bool isM, std::vector<std::pair<int, int>> &ranges) {
@@ -674,13 +715,9 @@ static int build_groups(std::vector<OutWork> &works, size_t w0, size_t w1, Group
         // find previous non-unit leg in the range
         while (outer >= rg.first && od[outer] == 1) --outer;
         bool ok = ost[outer] == od[j] * ost[j];
-        for (auto &t : w.tasks) {
-          if (!ok) break;
-          const Layout &X = isM ? *t.la : *t.lb;
-          int32_t xb = isM ? t.ab : t.bb;
-          int64_t xd[16], xs[16];
-          X.block_dims(xb, xd);
-          rowmajor_strides(xd, X.rank, xs);
+        for (size_t ti = 0; ti < w.tasks.size() && ok; ++ti) {
+          const TaskRef &t = w.tasks[ti];
+          const int64_t *xs = isM ? geo[ti].as : geo[ti].bs;
           const std::vector<int> &ex = isM ? t.c->e1 : t.c->e2;
           int jo = isM ? outer : outer - ne1, ji = isM ? j : j - ne1;
           ok = xs[ex[jo]] == od[j] * xs[ex[ji]];
@@ -691,7 +728,6 @@ static int build_groups(std::vector<OutWork> &works, size_t w0, size_t w1, Group
           ranges.push_back({j, j + 1});
       }
     };
-    std::vector<std::pair<int, int>> mr, nr;
     decompose(0, ne1, true, mr);
     decompose(ne1, O.rank, false, nr);
     auto rdim = [&](const std::pair<int, int> &r) {
@@ -710,7 +746,7 @@ static int build_groups(std::vector<OutWork> &works, size_t w0, size_t w1, Group
       if (pm < 0 || rdim(mr[i]) > rdim(mr[pm])) pm = i;
     for (int i = 0; i < (int)nr.size(); ++i)
       if (pn < 0 || rdim(nr[i]) > rdim(nr[pn])) pn = i;
-    std::vector<std::pair<int, int>> loops;  // (range index, isM)
+    loops.clear();
     for (int i = 0; i < (int)mr.size(); ++i)
       if (i != pm) loops.push_back({i, 1});
     for (int i = 0; i < (int)nr.size(); ++i)
@@ -741,16 +777,142 @@ static int build_groups(std::vector<OutWork> &works, size_t w0, size_t w1, Group
       for (auto &t : w.tasks)
         if (t.la != t0.la || t.abuf != t0.abuf || t.a_base != t0.a_base) mi.ok = false;
     }
-    for (int64_t sub = 0; sub < nsub; ++sub) {
-      // multi-index of the sub-region over the loop ranges; each range is a
-      // merged leg so its index maps linearly with the innermost stride
-      std::vector<int64_t> lidx(loops.size());
+    // the rest of each task's geometry (the reference work unit 2 m n k of
+    // the full block product is counted here, once per task)
+    for (size_t ti = 0; ti < w.tasks.size(); ++ti) {
+      const TaskRef &tk = w.tasks[ti];
+      TaskGeo &gt = geo[ti];
+      const int64_t *ad = gt.ad, *as = gt.as, *bd = gt.bd, *bs = gt.bs;
+      const auto &e1 = tk.c->e1, &e2 = tk.c->e2, &i1 = tk.c->i1, &i2 = tk.c->i2;
+      {
+        double m = 1, n = 1, k = 1;
+        for (int j : e1) m *= (double)ad[j];
+        for (int j : e2) n *= (double)bd[j];
+        for (int j : i1) k *= (double)ad[j];
+        out.flops += 2.0 * m * n * k;
+        out.ntasks += 1;
+      }
+      gt.a0 = tk.a_base + tk.la->pk->off[tk.ab];
+      gt.b0 = tk.b_base + tk.lb->pk->off[tk.bb];
+      for (size_t i = 0; i < loops.size(); ++i) {
+        auto &rg = loops[i].second ? mr[loops[i].first] : nr[loops[i].first];
+        int jj = innermost(rg);
+        gt.ls[i] = loops[i].second ? as[e1[jj]] : bs[e2[jj - ne1]];
+      }
+      gt.sam = pm >= 0 ? as[e1[innermost(mr[pm])]] : 0;
+      gt.sbn = pn >= 0 ? bs[e2[innermost(nr[pn]) - ne1]] : 0;
+      // K legs: sort by A stride (descending), merge where contiguous in both
+      Leg2 kraw[16], kl[16];
+      int nraw = 0, nkl = 0;
+      for (size_t k = 0; k < i1.size(); ++k) kraw[nraw++] = {ad[i1[k]], as[i1[k]], bs[i2[k]]};
+      std::sort(kraw, kraw + nraw, [](const Leg2 &x, const Leg2 &y) { return x.s0 > y.s0; });
+      for (int i = 0; i < nraw; ++i) {
+        const Leg2 &l = kraw[i];
+        if (l.d == 1) continue;
+        if (nkl > 0) {
+          Leg2 &o = kl[nkl - 1];
+          if (o.s0 == l.d * l.s0 && o.s1 == l.d * l.s1) {
+            o.d *= l.d;
+            o.s0 = l.s0;
+            o.s1 = l.s1;
+            continue;
+          }
+        }
+        kl[nkl++] = l;
+      }
+      int pk = -1;
+      for (int i = 0; i < nkl; ++i)
+        if (pk < 0 || kl[i].d > kl[pk].d) pk = i;
+      gt.K = pk >= 0 ? kl[pk].d : 1;
+      gt.sak = pk >= 0 ? kl[pk].s0 : 0;
+      gt.sbk = pk >= 0 ? kl[pk].s1 : 0;
+      gt.nkloop = 0;
+      for (int i = 0; i < nkl; ++i)
+        if (i != pk) gt.kloops[gt.nkloop++] = kl[i];
+      gt.nk = 1;
+      for (int i = 0; i < gt.nkloop; ++i) gt.nk *= gt.kloops[i].d;
+      if (gt.nk != 1) mi.ok = false;
+    }
+    lidx.assign(loops.size(), 0);
+    auto sub_index = [&](int64_t sub) {
       int64_t t = sub;
       for (int i = (int)loops.size() - 1; i >= 0; --i) {
         int64_t d = rdim(loops[i].second ? mr[loops[i].first] : nr[loops[i].first]);
         lidx[i] = t % d;
         t /= d;
       }
+    };
+    // Sub-regions that differ only in their columns (every loop is an N
+    // loop: the B operand's N legs are not contiguous, e.g. an environment
+    // [w, bra, ket] read along (w, ket)) all read the same A parts: they
+    // become the column blocks of one group, side by side in N, with one B
+    // part per (segment, column block), when the whole K fits one split-K
+    // part.
+    bool cb_subs = nsub > 1 && !w.tasks.empty() && nsub * N <= INT32_MAX;
+    for (auto &lp : loops)
+      if (lp.second) cb_subs = false;
+    if (cb_subs) {
+      int64_t ktot = 0;
+      for (size_t ti = 0; ti < w.tasks.size(); ++ti) ktot += geo[ti].nk * geo[ti].K;
+      cb_subs = ktot <= kSplitK;
+    }
+    if (cb_subs) {
+      Group g{};
+      g.c_off = 0;
+      g.scm = g.scn = 0;
+      g.M = (int32_t)M;
+      g.N = (int32_t)(nsub * N);
+      g.seg0 = (int32_t)out.segs.size();
+      g.cbuf = w.cbuf;
+      g.ncb = (int32_t)nsub;
+      g.cb0 = (int32_t)out.cblocks.size();
+      g.sb0 = (int32_t)out.segb.size();
+      for (int64_t sub = 0; sub < nsub; ++sub) {
+        sub_index(sub);
+        int64_t coff = c0;
+        for (size_t i = 0; i < loops.size(); ++i) coff += lidx[i] * ost[innermost(nr[loops[i].first])];
+        out.cblocks.push_back({coff, scm, scn, (int32_t)(sub * N), (int32_t)N});
+      }
+      for (size_t ti = 0; ti < w.tasks.size(); ++ti) {
+        const TaskRef &tk = w.tasks[ti];
+        const TaskGeo &gt = geo[ti];
+        for (int64_t ki = 0; ki < gt.nk; ++ki) {
+          int64_t aa = gt.a0, bk = gt.b0, tt = ki;
+          for (int i = gt.nkloop - 1; i >= 0; --i) {
+            int64_t x = tt % gt.kloops[i].d;
+            tt /= gt.kloops[i].d;
+            aa += x * gt.kloops[i].s0;
+            bk += x * gt.kloops[i].s1;
+          }
+          Seg s;
+          s.a_off = aa;
+          s.b_off = -1;
+          s.sam = gt.sam;
+          s.sak = gt.sak;
+          s.sbk = s.sbn = 0;
+          s.alpha = tk.alpha;
+          s.K = (int32_t)gt.K;
+          s.abuf = (int8_t)tk.abuf;
+          s.bbuf = (int8_t)tk.bbuf;
+          s.pad0 = s.pad1 = 0;
+          out.segs.push_back(s);
+          for (int64_t sub = 0; sub < nsub; ++sub) {
+            sub_index(sub);
+            int64_t bb = bk;
+            for (size_t i = 0; i < loops.size(); ++i) bb += lidx[i] * gt.ls[i];
+            out.segb.push_back({bb, gt.sbk, gt.sbn});
+          }
+        }
+      }
+      g.nseg = (int32_t)out.segs.size() - g.seg0;
+      out.groups.push_back(g);
+      out.minfo.push_back(MergeInfo{});  // a column-block group is not joined again
+      continue;
+    }
+    for (int64_t sub = 0; sub < nsub; ++sub) {
+      // multi-index of the sub-region over the loop ranges; each range is a
+      // merged leg so its index maps linearly with the innermost stride
+      sub_index(sub);
       int64_t coff = c0;
       for (size_t i = 0; i < loops.size(); ++i) {
         auto &rg = loops[i].second ? mr[loops[i].first] : nr[loops[i].first];
@@ -765,82 +927,33 @@ static int build_groups(std::vector<OutWork> &works, size_t w0, size_t w1, Group
       g.seg0 = (int32_t)out.segs.size();
       g.cbuf = w.cbuf;
       g.ncb = g.cb0 = g.sb0 = 0;
-      for (auto &tk : w.tasks) {
-        const Layout &A = *tk.la, &B = *tk.lb;
-        int64_t ad[16], as[16], bd[16], bs[16];
-        A.block_dims(tk.ab, ad);
-        B.block_dims(tk.bb, bd);
-        rowmajor_strides(ad, A.rank, as);
-        rowmajor_strides(bd, B.rank, bs);
-        const auto &e1 = tk.c->e1, &e2 = tk.c->e2, &i1 = tk.c->i1, &i2 = tk.c->i2;
-        // reference work unit: 2 * m * n * k of the full block product
-        if (sub == 0) {
-          double m = 1, n = 1, k = 1;
-          for (int j : e1) m *= (double)ad[j];
-          for (int j : e2) n *= (double)bd[j];
-          for (int j : i1) k *= (double)ad[j];
-          out.flops += 2.0 * m * n * k;
-          out.ntasks += 1;
-        }
-        int64_t a0 = tk.a_base + A.pk->off[tk.ab];
-        int64_t b0 = tk.b_base + B.pk->off[tk.bb];
+      for (size_t ti = 0; ti < w.tasks.size(); ++ti) {
+        const TaskRef &tk = w.tasks[ti];
+        const TaskGeo &gt = geo[ti];
+        int64_t a0 = gt.a0, b0 = gt.b0;
         for (size_t i = 0; i < loops.size(); ++i) {
-          auto &rg = loops[i].second ? mr[loops[i].first] : nr[loops[i].first];
-          int jj = innermost(rg);
           if (loops[i].second)
-            a0 += lidx[i] * as[e1[jj]];
+            a0 += lidx[i] * gt.ls[i];
           else
-            b0 += lidx[i] * bs[e2[jj - ne1]];
+            b0 += lidx[i] * gt.ls[i];
         }
-        int64_t sam = pm >= 0 ? as[e1[innermost(mr[pm])]] : 0;
-        int64_t sbn = pn >= 0 ? bs[e2[innermost(nr[pn]) - ne1]] : 0;
-        // K legs: sort by A stride (descending), merge where contiguous in both
-        // (fixed-size arrays: this runs once per block task)
-        Leg2 kraw[16], kl[16], kloops[16];
-        int nraw = 0, nkl = 0, nkloop = 0;
-        for (size_t k = 0; k < i1.size(); ++k) kraw[nraw++] = {ad[i1[k]], as[i1[k]], bs[i2[k]]};
-        std::sort(kraw, kraw + nraw, [](const Leg2 &x, const Leg2 &y) { return x.s0 > y.s0; });
-        for (int i = 0; i < nraw; ++i) {
-          const Leg2 &l = kraw[i];
-          if (l.d == 1) continue;
-          if (nkl > 0) {
-            Leg2 &o = kl[nkl - 1];
-            if (o.s0 == l.d * l.s0 && o.s1 == l.d * l.s1) {
-              o.d *= l.d;
-              o.s0 = l.s0;
-              o.s1 = l.s1;
-              continue;
-            }
-          }
-          kl[nkl++] = l;
-        }
-        int pk = -1;
-        for (int i = 0; i < nkl; ++i)
-          if (pk < 0 || kl[i].d > kl[pk].d) pk = i;
-        int64_t K = pk >= 0 ? kl[pk].d : 1;
-        int64_t sak = pk >= 0 ? kl[pk].s0 : 0, sbk = pk >= 0 ? kl[pk].s1 : 0;
-        for (int i = 0; i < nkl; ++i)
-          if (i != pk) kloops[nkloop++] = kl[i];
-        int64_t nk = 1;
-        for (int i = 0; i < nkloop; ++i) nk *= kloops[i].d;
-        if (nk != 1) mi.ok = false;
-        for (int64_t ki = 0; ki < nk; ++ki) {
+        for (int64_t ki = 0; ki < gt.nk; ++ki) {
           int64_t aa = a0, bb = b0, tt = ki;
-          for (int i = nkloop - 1; i >= 0; --i) {
-            int64_t x = tt % kloops[i].d;
-            tt /= kloops[i].d;
-            aa += x * kloops[i].s0;
-            bb += x * kloops[i].s1;
+          for (int i = gt.nkloop - 1; i >= 0; --i) {
+            int64_t x = tt % gt.kloops[i].d;
+            tt /= gt.kloops[i].d;
+            aa += x * gt.kloops[i].s0;
+            bb += x * gt.kloops[i].s1;
           }
           Seg s;
           s.a_off = aa;
           s.b_off = bb;
-          s.sam = sam;
-          s.sak = sak;
-          s.sbk = sbk;
-          s.sbn = sbn;
+          s.sam = gt.sam;
+          s.sak = gt.sak;
+          s.sbk = gt.sbk;
+          s.sbn = gt.sbn;
           s.alpha = tk.alpha;
-          s.K = (int32_t)K;
+          s.K = (int32_t)gt.K;
           s.abuf = (int8_t)tk.abuf;
           s.bbuf = (int8_t)tk.bbuf;
           s.pad0 = s.pad1 = 0;
@@ -976,26 +1089,50 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
     nc += p.cblocks.size();
     nb += p.segb.size();
   }
-  st.segs.reserve(ns);
-  st.groups.reserve(ng);
-  st.cblocks.reserve(nc);
-  st.segb.reserve(nb);
-  for (auto &p : parts) {
-    const int32_t soff = (int32_t)st.segs.size(), coff = (int32_t)st.cblocks.size(), boff = (int32_t)st.segb.size();
-    st.segs.insert(st.segs.end(), p.segs.begin(), p.segs.end());
-    st.cblocks.insert(st.cblocks.end(), p.cblocks.begin(), p.cblocks.end());
-    st.segb.insert(st.segb.end(), p.segb.begin(), p.segb.end());
-    for (Group g : p.groups) {
-      g.seg0 += soff;
-      if (g.ncb > 0) {
-        g.cb0 += coff;
-        g.sb0 += boff;
-      }
-      st.groups.push_back(g);
+  // each part's records go to their place in the joined arrays on the
+  // part's own thread
+  st.segs.resize(ns);
+  st.groups.resize(ng);
+  st.cblocks.resize(nc);
+  st.segb.resize(nb);
+  struct Off {
+    size_t s, g, c, b;
+  };
+  std::vector<Off> offs(nparts);
+  {
+    Off o{0, 0, 0, 0};
+    for (int q = 0; q < nparts; ++q) {
+      offs[q] = o;
+      o.s += parts[q].segs.size();
+      o.g += parts[q].groups.size();
+      o.c += parts[q].cblocks.size();
+      o.b += parts[q].segb.size();
+      st.flops += parts[q].flops;
+      st.ntasks += parts[q].ntasks;
     }
-    st.flops += p.flops;
-    st.ntasks += p.ntasks;
   }
+  std::vector<std::thread> pool;
+  for (int q = 0; q < nparts; ++q)
+    pool.emplace_back([&st, &parts, &offs, q]() {
+      GroupPart &p = parts[q];
+      const Off o = offs[q];
+      std::copy(p.segs.begin(), p.segs.end(), st.segs.begin() + o.s);
+      std::copy(p.cblocks.begin(), p.cblocks.end(), st.cblocks.begin() + o.c);
+      std::copy(p.segb.begin(), p.segb.end(), st.segb.begin() + o.b);
+      Group *out = st.groups.data() + o.g;
+      for (Group g : p.groups) {
+        g.seg0 += (int32_t)o.s;
+        if (g.ncb > 0) {
+          g.cb0 += (int32_t)o.c;
+          g.sb0 += (int32_t)o.b;
+        }
+        *out++ = g;
+      }
+      // the part's records are released on its thread
+      std::vector<Seg>().swap(p.segs);
+      std::vector<SegB>().swap(p.segb);
+    });
+  for (auto &t : pool) t.join();
   return ZMPO_OK;
 }
 
@@ -1055,32 +1192,41 @@ struct UmmaLists {
   std::vector<PrepB> pb[2];
   std::vector<UWork> w1[3], wl[3];   // one-pass / long items by column tile; pad = kept sides
   std::vector<int64_t> cmap;         // column maps (tn output offsets, then tn row strides each)
-  // B-record sequences (all passes of a column tile) of plain groups, by
-  // their exact content key: groups reading the same B parts share them
-  std::map<std::vector<int64_t>, int64_t> bseq[2];
+  // B-record sequences (all passes of a column tile) of plain groups, by a
+  // hash of the tile and its B parts (candidates compared in full): groups
+  // reading the same B parts share them
+  struct BSeq {
+    int32_t g, n0, tn, ncol;
+    int64_t K, rec;
+  };
+  std::unordered_map<uint64_t, std::vector<BSeq>> bseq[2];
   int64_t abytes[2] = {0, 0}, bbytes[2] = {0, 0};
   double macs = 0.0;                 // multiply-adds the MMAs issue (x10 digit products)
 };
 
-// Content key of the B records of a column tile (columns n0 .. n0+tn-1) of a
-// plain group over its slots kbase .. kbase+K-1: the B part of every segment
-// piece in that window (buffer, offset of its first slot, strides, length).
-// Equal keys mean equal records.
-static void b_seq_key(const Step &st, const Group &G, int64_t kbase, int64_t K, int n0, int tn,
-                      std::vector<int64_t> &key) {
-  key.assign({(int64_t)n0, (int64_t)tn, (int64_t)std::min(tn, G.N - n0), K});
-  int64_t pos = 0;
-  for (int i = 0; i < G.nseg && pos < kbase + K; ++i) {
+// The B records of a column tile (columns n0 .. n0+tn-1, all K slots) of a
+// plain group are fixed by the tile (n0, tn, its columns inside the group),
+// K and the B part of every segment with slots (buffer, offset of its first
+// slot, strides, length).  Equal tiles of two groups have equal records.
+static uint64_t b_parts_hash(const Step &st, const Group &G) {
+  uint64_t h = 0xcbf29ce484222325ull;
+  for (int i = 0; i < G.nseg; ++i) {
     const Seg &sg = st.segs[G.seg0 + i];
-    const int64_t lo = std::max(pos, kbase), hi = std::min(pos + sg.K, kbase + K);
-    if (lo < hi) {
-      key.push_back(sg.bbuf);
-      key.push_back(sg.b_off + (lo - pos) * sg.sbk);
-      key.push_back(sg.sbk);
-      key.push_back(sg.sbn);
-      key.push_back(hi - lo);
-    }
-    pos += sg.K;
+    if (sg.K <= 0) continue;
+    for (int64_t v : {(int64_t)sg.bbuf, sg.b_off, sg.sbk, sg.sbn, (int64_t)sg.K}) h = (h ^ (uint64_t)v) * 0x100000001b3ull;
+  }
+  return h;
+}
+static bool same_b_parts(const Step &st, const Group &X, const Group &Y) {
+  int i = 0, j = 0;
+  while (true) {
+    while (i < X.nseg && st.segs[X.seg0 + i].K <= 0) ++i;
+    while (j < Y.nseg && st.segs[Y.seg0 + j].K <= 0) ++j;
+    if (i == X.nseg || j == Y.nseg) return i == X.nseg && j == Y.nseg;
+    const Seg &a = st.segs[X.seg0 + i], &b = st.segs[Y.seg0 + j];
+    if (a.bbuf != b.bbuf || a.b_off != b.b_off || a.sbk != b.sbk || a.sbn != b.sbn || a.K != b.K) return false;
+    ++i;
+    ++j;
   }
 }
 
@@ -1152,20 +1298,28 @@ static void umma_add_group(UmmaLists &L, const Step &st, int g, const Group &G, 
   const int nruns = (nrt + kUmmaRunMax - 1) / kUmmaRunMax;
   const int len = (nrt + nruns - 1) / nruns;
   const int32_t sides = ka | (kb << 1);
-  std::vector<int64_t> key;
+  const uint64_t hparts = G.ncb == 0 ? b_parts_hash(st, G) : 0;
   for (int n0 = 0; n0 < G.N;) {
     // long groups wider than one tile take 64-column tiles only, so their
     // tiles run in one launch next to each other (A re-read from L2)
     const int tn = (!one && G.N > 64) ? 64 : umma_tn(G.N - n0), ti = umma_ti(tn);
     int64_t brec = -1;
-    if (G.ncb == 0) {
-      b_seq_key(st, G, kbase, K, n0, tn, key);
-      auto it = L.bseq[kb].find(key);
-      if (it != L.bseq[kb].end()) brec = it->second;
+    uint64_t kh = 0;
+    const int ncol = std::min(tn, G.N - n0);
+    if (G.ncb == 0 && kbase == 0) {
+      kh = hparts;
+      for (int64_t v : {(int64_t)n0, (int64_t)tn, (int64_t)ncol, K}) kh = (kh ^ (uint64_t)v) * 0x100000001b3ull;
+      auto it = L.bseq[kb].find(kh);
+      if (it != L.bseq[kb].end())
+        for (const auto &c : it->second)
+          if (c.n0 == n0 && c.tn == tn && c.ncol == ncol && c.K == K && same_b_parts(st, st.groups[c.g], G)) {
+            brec = c.rec;
+            break;
+          }
     }
     if (brec < 0) {
       brec = L.bbytes[kb];
-      if (G.ncb == 0) L.bseq[kb].emplace(key, brec);
+      if (G.ncb == 0 && kbase == 0) L.bseq[kb][kh].push_back({g, n0, tn, ncol, K, brec});
       for (int j = 0; j < npass; ++j) {
         const int k0 = j * kUmmaMaxK, kc = (int)std::min<int64_t>(kUmmaMaxK, K - k0);
         L.pb[kb].push_back({L.bbytes[kb], g, n0, tn, k0, kc, 0});
@@ -1330,6 +1484,22 @@ static void build_split_lists(Step &st) {
   UmmaLists UL;
   st.mma_macs[1] = 0.0;
   auto order = cost_order(st);
+  {
+    // the column maps' final size (tcgen05 groups: 2 tn entries per column
+    // tile), so the array is filled without regrowing
+    size_t ncm = 0;
+    for (size_t g = 0; g < st.groups.size(); ++g) {
+      const Group &G = st.groups[g];
+      const bool one = umma_one_pass(G, st.gk[g]);
+      if (!one && !umma_long(G, st.gk[g])) continue;
+      for (int n0 = 0; n0 < G.N;) {
+        const int tn = (!one && G.N > 64) ? 64 : umma_tn(G.N - n0);
+        ncm += 2 * (size_t)tn;
+        n0 += tn;
+      }
+    }
+    UL.cmap.reserve(ncm);
+  }
   for (int g : order) {
     const Group &G = st.groups[g];
     const int64_t kt = st.gk[g];
@@ -1935,43 +2105,67 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
   static const int ax3a1[2] = {1, 2}, ax3b1[2] = {2, 0};
   static const int axOa[1] = {1}, axOb[1] = {0};
   static const int axTa[3] = {0, 2, 3}, axTb[3] = {0, 2, 5};
-  for (int op = 0; op < d->nop; ++op) {
-    int c = d->op_class[op];
-    if (c < 0 || c >= d->nclass) return fail(ZMPO_E_ARG, "sigma_plan: bad class");
+  // classes in order of first appearance; each class's chain (a fixed
+  // number of contractions) is built on its own thread into table slots
+  // reserved for it, in the order a one-thread build would use them
+  std::vector<int> cls_order;
+  {
+    std::vector<char> seen(d->nclass, 0);
+    for (int op = 0; op < d->nop; ++op) {
+      const int c = d->op_class[op];
+      if (c < 0 || c >= d->nclass) return fail(ZMPO_E_ARG, "sigma_plan: bad class");
+      if (!seen[c]) {
+        seen[c] = 1;
+        cls_order.push_back(c);
+      }
+    }
+  }
+  const int per_chain = d->ncsite == 2 ? 6 : 3;
+  e->layouts.resize(l0 + cls_order.size() * per_chain);
+  e->contractions.resize(c0 + cls_order.size() * per_chain);
+  std::vector<int> chain_rc(cls_order.size(), ZMPO_OK);
+  std::vector<std::string> chain_msg(cls_order.size());
+  auto build_chain = [&](size_t k) -> int {
+    const int c = cls_order[k];
     ClassChain &ch = chains[c];
-    if (ch.built) continue;
     ch.built = true;
+    int next_l = (int)(l0 + k * per_chain), next_c = (int)(c0 + k * per_chain);
+    auto contract = [&](int ia, int ib, int n, const int *aa, const int *ab, int *lo_, int *ci_) {
+      *lo_ = next_l++;
+      *ci_ = next_c++;
+      return build_contraction_at(e, ia, ib, n, aa, ab, *lo_, *ci_);
+    };
     int lo = -1, ci = -1, rc = 0, l1 = -1, c1 = -1;
-    rc = build_contraction(e, d->lay_L[c], d->lay_psi, 1, ax1a, ax1b, &l1, &c1);
+    rc = contract(d->lay_L[c], d->lay_psi, 1, ax1a, ax1b, &l1, &c1);
     if (rc) return rc;
     ch.ref_flops += contraction_flops(e, e->contractions[c1].get());
     if (d->ncsite == 2) {
       int l2, c2, l3, c3;
-      rc = build_contraction(e, l1, d->lay_Wi[c], 2, ax2a, ax2b, &l2, &c2);
+      rc = contract(l1, d->lay_Wi[c], 2, ax2a, ax2b, &l2, &c2);
       if (rc) return rc;
-      rc = build_contraction(e, l2, d->lay_Wj[c], 2, ax3a, ax3b, &l3, &c3);
+      rc = contract(l2, d->lay_Wj[c], 2, ax3a, ax3b, &l3, &c3);
       if (rc) return rc;
       ch.ref_flops += contraction_flops(e, e->contractions[c2].get()) +
                       contraction_flops(e, e->contractions[c3].get());
       int lO, cO;
-      rc = build_contraction(e, d->lay_Wi[c], d->lay_Wj[c], 1, axOa, axOb, &lO, &cO);
+      rc = contract(d->lay_Wi[c], d->lay_Wj[c], 1, axOa, axOb, &lO, &cO);
       if (rc) return rc;
       ch.c.push_back({cO, lO});
       ch.c.push_back({c1, l1});
-      rc = build_contraction(e, l1, lO, 3, axTa, axTb, &lo, &ci);
+      rc = contract(l1, lO, 3, axTa, axTb, &lo, &ci);
       if (rc) return rc;
       const Layout *T3a = get_layout(e, l3), *T3b = get_layout(e, lo);
       if (T3a->pk->flat != T3b->pk->flat || T3a->pk->size != T3b->pk->size)
         return fail(ZMPO_E_SYM, "sigma_plan: fused MPO step layout differs");
       ch.c.push_back({ci, lo});
-      rc = build_contraction(e, lo, d->lay_Rf[c], 2, ax4a, ax4b, &lo, &ci);
+      rc = contract(lo, d->lay_Rf[c], 2, ax4a, ax4b, &lo, &ci);
     } else {
       ch.c.push_back({c1, l1});
-      rc = build_contraction(e, l1, d->lay_Wi[c], 2, ax2a, ax2b, &lo, &ci);
+      rc = contract(l1, d->lay_Wi[c], 2, ax2a, ax2b, &lo, &ci);
       if (rc) return rc;
       ch.ref_flops += contraction_flops(e, e->contractions[ci].get());
       ch.c.push_back({ci, lo});
-      rc = build_contraction(e, lo, d->lay_Rf[c], 2, ax3a1, ax3b1, &lo, &ci);
+      rc = contract(lo, d->lay_Rf[c], 2, ax3a1, ax3b1, &lo, &ci);
     }
     if (rc) return rc;
     ch.ref_flops += contraction_flops(e, e->contractions[ci].get());
@@ -1979,6 +2173,18 @@ int zmpo_sigma_plan(zmpo_engine *e, const zmpo_sigma_desc *d, int *plan_id) {
     const Layout *Out = get_layout(e, lo);
     if (Out->pk->flat != Psi->pk->flat || Out->pk->size != Psi->pk->size)
       return fail(ZMPO_E_SYM, "sigma_plan: H.psi layout differs from psi layout");
+    return ZMPO_OK;
+  };
+  {
+    std::vector<std::thread> pool;
+    for (size_t k = 0; k < cls_order.size(); ++k)
+      pool.emplace_back([&, k]() {
+        chain_rc[k] = build_chain(k);
+        if (chain_rc[k]) chain_msg[k] = g_err;
+      });
+    for (auto &t : pool) t.join();
+    for (size_t k = 0; k < cls_order.size(); ++k)
+      if (chain_rc[k]) return fail(chain_rc[k], chain_msg[k]);
   }
   auto P = std::make_unique<Plan>();
   P->kind = 2;
