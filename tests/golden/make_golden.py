@@ -18,7 +18,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 
-def main(ref="/root/reference"):
+def main(ref=os.environ.get("ZMPO_REFERENCE", "/root/reference")):
     from oracle import integrals
     case = os.path.join(ref, "source", "samps", "example_conversion", "5.h6+_doublet")
     d = integrals.read_fcidump(os.path.join(case, "FCIDUMP"))
