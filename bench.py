@@ -634,13 +634,26 @@ def main():
     if world > 1:
         result["config"]["parallelism"] = ("operator terms partitioned over %d ranks (contiguous blocks), one NCCL "
                                            "all-reduce of sigma per step" % world)
+    # the sections after the sigma measurement each record their own failure
+    # (the JSON line is printed whatever happens in them)
+    def section(name, fn):
+        try:
+            return fn()
+        except Exception as ex:  # noqa: BLE001 -- reported in the result line
+            print("bench: %s failed: %r" % (name, ex), file=sys.stderr)
+            return {"error": "%s: %s" % (type(ex).__name__, ex)}
+
     if rank == 0 and not args.no_sweep:
-        result["sweep"] = sweep_converged()
-        result["sweep_k10"] = sweep_converged(K=10, nelec=10, D=64, maxiter=16)
+        result["sweep"] = section("sweep", sweep_converged)
+        result["sweep_k10"] = section("sweep_k10", lambda: sweep_converged(K=10, nelec=10, D=64, maxiter=16))
     if rank == 0 and not args.no_gradient and not (args.small or args.medium or args.large or args.sp):
-        result["gradient"] = gradient_metrics()
+        result["gradient"] = section("gradient", gradient_metrics)
     if rank == 0 and not args.no_cpu and not (args.large or args.sp):
-        result["cpu_baseline"], result["parity_vs_oracle"] = cpu_leg(P, cfg)
+        leg = section("cpu_baseline", lambda: cpu_leg(P, cfg))
+        if isinstance(leg, dict):
+            result["cpu_baseline"], result["parity_vs_oracle"] = leg, leg
+        else:
+            result["cpu_baseline"], result["parity_vs_oracle"] = leg
     if rank == 0:
         print(json.dumps(result))
     if dist:

@@ -425,15 +425,10 @@ def test_renorm_task_lists_compute_the_oracle_environments(status, case):
     term, the reference's chain of renormQt_H00) executed from its task
     records by the NumPy model of the kernels equals the oracle's new
     environments (FP64, 1e-12 of each term's largest element): checks the
-    planner's addressing of every step on the CPU.  The first two steps read
-    an operand whose N legs are not contiguous (the environment along its
-    MPO bond and ket legs, T1 along its site and ket legs); their
-    sub-regions are the column blocks of one group per output block."""
+    planner's addressing of every step on the CPU."""
     from tests.problems import random_problem, host_renorm, oracle_renorm
     P = random_problem(device=False, **case)
     got, groups = host_renorm(P, status)
-    assert (groups[0]["ncb"] > 1).sum() > 0.9 * len(groups[0])
-    assert (groups[1]["ncb"] > 1).any()
     ref = oracle_renorm(P, status)
     n = 0
     for g, r in zip(got, ref):

@@ -842,73 +842,6 @@ static int build_groups(std::vector<OutWork> &works, size_t w0, size_t w1, Group
         t /= d;
       }
     };
-    // Sub-regions that differ only in their columns (every loop is an N
-    // loop: the B operand's N legs are not contiguous, e.g. an environment
-    // [w, bra, ket] read along (w, ket)) all read the same A parts: they
-    // become the column blocks of one group, side by side in N, with one B
-    // part per (segment, column block), when the whole K fits one split-K
-    // part.
-    bool cb_subs = nsub > 1 && !w.tasks.empty() && nsub * N <= INT32_MAX;
-    for (auto &lp : loops)
-      if (lp.second) cb_subs = false;
-    if (cb_subs) {
-      int64_t ktot = 0;
-      for (size_t ti = 0; ti < w.tasks.size(); ++ti) ktot += geo[ti].nk * geo[ti].K;
-      cb_subs = ktot <= kSplitK;
-    }
-    if (cb_subs) {
-      Group g{};
-      g.c_off = 0;
-      g.scm = g.scn = 0;
-      g.M = (int32_t)M;
-      g.N = (int32_t)(nsub * N);
-      g.seg0 = (int32_t)out.segs.size();
-      g.cbuf = w.cbuf;
-      g.ncb = (int32_t)nsub;
-      g.cb0 = (int32_t)out.cblocks.size();
-      g.sb0 = (int32_t)out.segb.size();
-      for (int64_t sub = 0; sub < nsub; ++sub) {
-        sub_index(sub);
-        int64_t coff = c0;
-        for (size_t i = 0; i < loops.size(); ++i) coff += lidx[i] * ost[innermost(nr[loops[i].first])];
-        out.cblocks.push_back({coff, scm, scn, (int32_t)(sub * N), (int32_t)N});
-      }
-      for (size_t ti = 0; ti < w.tasks.size(); ++ti) {
-        const TaskRef &tk = w.tasks[ti];
-        const TaskGeo &gt = geo[ti];
-        for (int64_t ki = 0; ki < gt.nk; ++ki) {
-          int64_t aa = gt.a0, bk = gt.b0, tt = ki;
-          for (int i = gt.nkloop - 1; i >= 0; --i) {
-            int64_t x = tt % gt.kloops[i].d;
-            tt /= gt.kloops[i].d;
-            aa += x * gt.kloops[i].s0;
-            bk += x * gt.kloops[i].s1;
-          }
-          Seg s;
-          s.a_off = aa;
-          s.b_off = -1;
-          s.sam = gt.sam;
-          s.sak = gt.sak;
-          s.sbk = s.sbn = 0;
-          s.alpha = tk.alpha;
-          s.K = (int32_t)gt.K;
-          s.abuf = (int8_t)tk.abuf;
-          s.bbuf = (int8_t)tk.bbuf;
-          s.pad0 = s.pad1 = 0;
-          out.segs.push_back(s);
-          for (int64_t sub = 0; sub < nsub; ++sub) {
-            sub_index(sub);
-            int64_t bb = bk;
-            for (size_t i = 0; i < loops.size(); ++i) bb += lidx[i] * gt.ls[i];
-            out.segb.push_back({bb, gt.sbk, gt.sbn});
-          }
-        }
-      }
-      g.nseg = (int32_t)out.segs.size() - g.seg0;
-      out.groups.push_back(g);
-      out.minfo.push_back(MergeInfo{});  // a column-block group is not joined again
-      continue;
-    }
     for (int64_t sub = 0; sub < nsub; ++sub) {
       // multi-index of the sub-region over the loop ranges; each range is a
       // merged leg so its index maps linearly with the innermost stride
