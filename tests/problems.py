@@ -635,12 +635,14 @@ def run_tasks_on_host(eng, pid, nsteps, bufs, gemm=None, written=None, part_gemm
     return bufs
 
 
-def host_sigma_terms(P, terms, x, gemm=None):
+def host_sigma_terms(P, terms, x, gemm=None, fill=0.0):
     """The engine's sigma plan over the operator terms ``terms`` of the
     oracle side of ``P`` (its environments and MPO sites as the operands),
     built by the engine's planner and executed on the host from the task
     records (NumPy model of the kernels); returns (sigma, groups per step).
-    Needs no GPU."""
+    ``fill`` is the initial value of the output and of the workspace (NaN:
+    an output element no task writes, or a read of an intermediate no task
+    wrote, shows up as NaN).  Needs no GPU."""
     from zmpo_dmrg_gb300 import engine as E, mpo as pm
     m = P.o
     eng = E.get()
@@ -675,7 +677,7 @@ def host_sigma_terms(P, terms, x, gemm=None):
         return numpy.zeros(P.ndim0), []
     pid, ws = eng.sigma_plan(2, op_cls, lL, lWi, lWj, lRf, lay(m.qtmp), offL, offR, offWi, offWj, wts)
     bufs = [numpy.concatenate(Lv), numpy.concatenate(Rv), numpy.concatenate(Wv), numpy.asarray(x, dtype=float),
-            numpy.zeros(P.ndim0), numpy.zeros(max(ws // 8, 1)), numpy.zeros(1), numpy.zeros(1)]
+            numpy.full(P.ndim0, fill), numpy.full(max(ws // 8, 1), fill), numpy.zeros(1), numpy.zeros(1)]
     _, _, nl = eng.plan_stats(pid)
     groups_all = [eng.step_tasks(pid, st)[0] for st in range(nl)]
     y = run_tasks_on_host(eng, pid, nl, bufs, gemm)[4]
@@ -683,13 +685,14 @@ def host_sigma_terms(P, terms, x, gemm=None):
     return y, groups_all
 
 
-def host_renorm(P, status):
+def host_renorm(P, status, fill=0.0):
     """The engine's renormalisation plan for the oracle side of ``P`` (status
     'L': the left environments extended by the dot's left site; 'R': the
     right ones by the site right of the dot), built by the engine's planner
     and executed on the host from the task records (NumPy model of the
     kernels).  Returns the new environment of every term (empty where absent)
-    and the plan's groups per step.  Needs no GPU."""
+    and the plan's groups per step.  ``fill`` is the initial value of the
+    output and of the workspace (as in ``host_sigma_terms``).  Needs no GPU."""
     from zmpo_dmrg_gb300 import engine as E, mpo as pm
     from oracle.qtensor import qtensor
     m = P.o
@@ -730,8 +733,8 @@ def host_renorm(P, status):
                 lay_W.append(eng.derive(lay(Wt), [-Wt.qsyms[0], -Wt.qsyms[1], Wt.qsyms[2], Wt.qsyms[3]], st))
         op_cls.append(classes[c0])
     pid, lay_out, off_out, total, ws = eng.renorm_plan(status, op_cls, lay_env, lay_W, lay(t), off_env, off_W)
-    bufs = [numpy.concatenate(Ev), numpy.zeros(1), numpy.concatenate(Wv), t.value.copy(), numpy.zeros(max(total, 1)),
-            numpy.zeros(max(ws // 8, 1)), numpy.zeros(1), numpy.zeros(1)]
+    bufs = [numpy.concatenate(Ev), numpy.zeros(1), numpy.concatenate(Wv), t.value.copy(), numpy.full(max(total, 1), fill),
+            numpy.full(max(ws // 8, 1), fill), numpy.zeros(1), numpy.zeros(1)]
     groups_all = [eng.step_tasks(pid, st)[0] for st in range(3)]
     out = run_tasks_on_host(eng, pid, 3, bufs)[4]
     envs = [numpy.zeros(0) for _ in range(m.nops)]

@@ -437,3 +437,55 @@ def test_renorm_task_lists_compute_the_oracle_environments(status, case):
             n += 1
             assert numpy.abs(g - r).max() <= 1e-12 * max(numpy.abs(r).max(), 1.0)
     assert n > 10
+
+
+@pytest.mark.parametrize("isite", [0, 3, 6])
+def test_sigma_task_records_cover_every_output_and_read_only_written_blocks(isite):
+    """Sigma plans of the left-boundary, a middle and the right-boundary dot
+    (K=8, D=32) executed from their task records with the output and the
+    workspace filled with NaN: every element of H.psi is written, no step
+    reads an intermediate block that no task wrote, and the result equals
+    the oracle's HVecQt."""
+    from tests.problems import random_problem, host_sigma_terms, oracle_sigma
+    P = random_problem(K=8, nelec=8, D=32, isite=isite, seed=3, device=False)
+    x = numpy.random.default_rng(1).standard_normal(P.ndim0)
+    y, _ = host_sigma_terms(P, range(P.o.nops), x, fill=numpy.nan)
+    assert not numpy.isnan(y).any()
+    ref = oracle_sigma(P, x)
+    assert numpy.linalg.norm(y - ref) <= 1e-12 * numpy.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("status,isite", [("L", 0), ("L", 3), ("R", 3), ("R", 6)])
+def test_renorm_task_records_cover_every_output_and_read_only_written_blocks(status, isite):
+    """Renormalisation plans next to both chain ends and in the middle (K=8,
+    D=32) with the output and the workspace filled with NaN: every element of
+    every new environment is written and no intermediate block is read
+    unwritten; the environments equal the oracle's."""
+    from tests.problems import random_problem, host_renorm, oracle_renorm
+    P = random_problem(K=8, nelec=8, D=32, isite=isite, seed=3, device=False)
+    got, _ = host_renorm(P, status, fill=numpy.nan)
+    ref = oracle_renorm(P, status)
+    n = 0
+    for g, r in zip(got, ref):
+        assert g.size == r.size and not numpy.isnan(g).any()
+        if r.size:
+            n += 1
+            assert numpy.abs(g - r).max() <= 1e-12 * max(numpy.abs(r).max(), 1.0)
+    assert n > 10
+
+
+def test_threaded_planner_is_deterministic():
+    """The planner builds class chains, steps and step parts on host threads:
+    two builds of the same sigma plan and of the same renormalisation plan
+    give identical task records, step by step."""
+    from tests.problems import random_problem, host_sigma_terms, host_renorm
+    P = random_problem(K=10, nelec=10, D=64, isite=4, seed=7, device=False)
+    x = numpy.random.default_rng(2).standard_normal(P.ndim0)
+    y1, g1 = host_sigma_terms(P, range(P.o.nops), x)
+    y2, g2 = host_sigma_terms(P, range(P.o.nops), x)
+    assert len(g1) == len(g2) and all(numpy.array_equal(a, b) for a, b in zip(g1, g2))
+    assert numpy.array_equal(y1, y2)
+    e1, r1 = host_renorm(P, "L")
+    e2, r2 = host_renorm(P, "L")
+    assert all(numpy.array_equal(a, b) for a, b in zip(r1, r2))
+    assert all(numpy.array_equal(a, b) for a, b in zip(e1, e2))
