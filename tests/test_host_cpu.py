@@ -489,3 +489,27 @@ def test_threaded_planner_is_deterministic():
     e2, r2 = host_renorm(P, "L")
     assert all(numpy.array_equal(a, b) for a, b in zip(r1, r2))
     assert all(numpy.array_equal(a, b) for a, b in zip(e1, e2))
+
+
+def test_adjoint_left_environment_schedule():
+    """Recompute mode of the energy gradient: taking the sites from right to
+    left, every site finds its left environment held (a checkpoint or
+    recomputed in the segment above the nearest checkpoint), at most about
+    2 sqrt(nsite) environments are held at once, and each left environment
+    is recomputed at most once."""
+    from zmpo_dmrg_gb300.adjoint import left_env_schedule, checkpoint_stride
+    for nsite in range(1, 49):
+        stride = checkpoint_stride(nsite)
+        assert stride * stride >= nsite and (stride - 1) ** 2 < nsite
+        checkpoints = {-1} | set(range(stride - 1, nsite, stride))
+        sched = left_env_schedule(nsite, stride)
+        assert len(sched) == nsite
+        recomputed = []
+        for (seg, held), j in zip(sched, range(nsite - 1, -1, -1)):
+            assert j - 1 in held
+            if seg is not None:
+                assert seg - 1 in checkpoints and seg - 1 in held
+                recomputed += list(range(seg, j))
+            assert set(held) <= checkpoints | set(recomputed)
+            assert len(held) <= 2 * stride + 1
+        assert len(recomputed) == len(set(recomputed)) and len(recomputed) < nsite

@@ -95,64 +95,157 @@ def right_environments(dmrg, fmps):
     return envs, qkey
 
 
-def site_gradients(dmrg, fmps=None):
-    """dE/dW_p(j) for every site j and term p as dense [Dw_l, Dw_r, 4, 4]
-    arrays in the builder's bond order, and <H> and <psi|psi> of the MPS."""
+def _left_step(dmrg, j, fL, site):
+    """L(j) from L(j-1) and the left-canonical site j (one renormalisation)."""
+    from .mpo_dmrg_kernel import renorm
+    fN = [[None, None]]
+    renorm(dmrg, j, 1, [[fL, None]], fN, site, 'L')
+    return fN[0][0]
+
+
+def _right_step(dmrg, j, fR, site, qkey):
+    """R(j) from R(j+1) and site j in the right block's labels."""
+    from .mpo_dmrg_kernel import renorm
+    fN = [[None, None]]
+    renorm(dmrg, j, 1, [[None, fR]], fN, _right_convention(site, qkey), 'R')
+    return fN[0][0]
+
+
+def checkpoint_stride(nsite):
+    """Sites between kept left environments when they are recomputed:
+    ceil(sqrt(nsite)), so about 2 sqrt(nsite) environments are held at once."""
+    return max(1, int(numpy.ceil(numpy.sqrt(nsite))))
+
+
+def left_env_schedule(nsite, stride):
+    """The left environments the recompute mode holds.  The forward pass
+    keeps the checkpoints L(c), c = -1 and c = stride-1, 2 stride-1, ...;
+    then the sites are taken from j = nsite-1 down to 0, site j needing
+    L(j-1): when that is not held, the segment L(c+1) .. L(j-1) is
+    recomputed from the nearest checkpoint c below it, and after site j
+    every L(x) with x >= j-1 is dropped (no later site needs it).  Returns,
+    per site j in that order, (the segment's first index, or None when
+    nothing is recomputed; the indices held while site j is taken)."""
+    checkpoints = {-1} | set(range(stride - 1, nsite, stride))
+    held = set(checkpoints)
+    out = []
+    for j in range(nsite - 1, -1, -1):
+        need = j - 1
+        seg = None
+        if need not in held:
+            c = max(x for x in held if x < need)
+            seg = c + 1
+            held |= set(range(seg, need + 1))
+        out.append((seg, sorted(held)))
+        held = {x for x in held if x < need}
+    return out
+
+
+def _site_gradient(dmrg, eng, j, site, fL, fR, qkey, norm2, grads):
+    """dE/dW_p(j) of every term present in both environments."""
     torch = _torch()
+    mpo = dmrg.mpo_store
+    sval = torch.from_numpy(numpy.ascontiguousarray(site.value)).cuda()
+    chains = {}
+    for iop in range(dmrg.nops):
+        if not (fL.present(iop) and fR.present(iop)):
+            continue
+        c0 = op_class(dmrg.opers[iop][0], j)
+        if c0 not in chains:
+            rt = fR.tensors[iop]
+            lay_rf = eng.derive(rt.layout, [-rt.qsyms[0], qkey - rt.qsyms[1], qkey - rt.qsyms[2]],
+                                rt.status)
+            chains[c0] = _GradChain(eng, site.layout, fL.layouts[iop], lay_rf)
+        ch = chains[c0]
+        lv = fL.buf.narrow(0, int(fL.off[iop]), fL.tensors[iop].size_allowed)
+        rv = fR.buf.narrow(0, int(fR.off[iop]), fR.tensors[iop].size_allowed)
+        t1 = torch.empty(max(ch.sizes[0], 1), dtype=torch.float64, device="cuda")
+        t2 = torch.empty(max(ch.sizes[1], 1), dtype=torch.float64, device="cuda")
+        g = torch.empty(max(ch.sizes[2], 1), dtype=torch.float64, device="cuda")
+        eng.contract_exec(ch.p1, sval, lv, t1)
+        eng.contract_exec(ch.p2, t1, sval, t2)
+        eng.contract_exec(ch.p3, t2, rv, g)
+        wt = mpo.tensors[j][iop]
+        # legs [n', a, n, b]: directions follow the contraction (bra
+        # site against the bra leg of L, ket legs against ket legs)
+        out = qtensor([False, False, True, True])
+        out.fromQsyms(4, [site.qsyms[1], wt.qsyms[0], site.qsyms[1], wt.qsyms[1]],
+                      [site.ndims[1], wt.ndims[0], site.ndims[1], wt.ndims[1]], ifallocate=False)
+        size, flat, _ = eng.layout_blocks(ch.lay_out)
+        if size != out.size_allowed or not numpy.array_equal(flat, out.blk_flat):
+            raise RuntimeError("site gradient layout mismatch")
+        out.value = g[:size].cpu().numpy()
+        dense = out.toDenseTensor([site.idlst[1], wt.idlst[0], site.idlst[1], wt.idlst[1]])
+        gq = dense.transpose(1, 3, 0, 2)            # [a, b, n', n] in sorted bond order
+        il, ir = _mpo.bond_order(dmrg.opers[iop], dmrg.sbas, j)
+        gb = numpy.zeros_like(gq)
+        gb[numpy.ix_(il, ir)] = gq
+        grads[j][iop] = dmrg.hpwts[iop] * gb / norm2
+    for ch in chains.values():
+        ch.release(eng)
+
+
+def site_gradients(dmrg, fmps=None, recompute_envs=None):
+    """dE/dW_p(j) for every site j and term p as dense [Dw_l, Dw_r, 4, 4]
+    arrays in the builder's bond order, and <H> and <psi|psi> of the MPS.
+
+    By default every left and right environment of the MPS is made once and
+    kept (2 nsite environment sets on the device).  With ``recompute_envs``
+    (default ``dmrg.adjoint_recompute_envs``, False) they are recomputed
+    where memory requires it: the sites are taken from right to left with
+    one right environment carried along, and the left environments are kept
+    only at checkpoints every ``checkpoint_stride(nsite)`` sites, the ones
+    between recomputed from the nearest checkpoint when they are needed
+    (``left_env_schedule``): about 2 sqrt(nsite) environment sets held and
+    one more left renormalisation per site.  The same renormalisations run
+    on the same inputs, so both modes give the same gradients."""
     if dmrg.ifs2proj:
         raise NotImplementedError("energy gradient of the spin-projected energy")
+    if recompute_envs is None:
+        recompute_envs = bool(getattr(dmrg, "adjoint_recompute_envs", False))
     fmps = dmrg.flmps if fmps is None else fmps
     eng = _engine.get()
     nsite = dmrg.nsite
-    exphop = dmrg.genHops(fmps, 'lop')
-    esum = float(numpy.dot(dmrg.hpwts, exphop))
     last = fmps['site%d' % (nsite - 1)]
     norm2 = float(numpy.dot(last.value, last.value))
-    Lenv = {j: dmrg.envs[('lop', j)] for j in range(-1, nsite)}
-    Renv, qkey = right_environments(dmrg, fmps)
-    mpo = dmrg.mpo_store
     grads = [[None] * dmrg.nops for _ in range(nsite)]
+    if not recompute_envs:
+        exphop = dmrg.genHops(fmps, 'lop')
+        esum = float(numpy.dot(dmrg.hpwts, exphop))
+        Lenv = {j: dmrg.envs[('lop', j)] for j in range(-1, nsite)}
+        Renv, qkey = right_environments(dmrg, fmps)
+        for j in range(nsite):
+            _site_gradient(dmrg, eng, j, fmps['site%d' % j], Lenv[j - 1], Renv[j + 1], qkey, norm2, grads)
+        return grads, esum / norm2, norm2
+    stride = checkpoint_stride(nsite)
+    schedule = left_env_schedule(nsite, stride)
+    checkpoints = {-1} | set(range(stride - 1, nsite, stride))
+    # forward pass: left environments, kept at the checkpoints only
+    L = {-1: dmrg.boundary_env()}
+    fL = L[-1]
     for j in range(nsite):
+        fL = _left_step(dmrg, j, fL, fmps['site%d' % j])
+        if j in checkpoints:
+            L[j] = fL
+    esum = float(numpy.dot(dmrg.hpwts, dmrg._scalars(fL, dmrg.nops)))
+    del fL
+    qkey = numpy.asarray(fmps['qnum%d' % nsite], dtype=float)[0]
+    fR = dmrg.boundary_env()
+    for (seg, held), j in zip(schedule, range(nsite - 1, -1, -1)):
+        if seg is not None:
+            fL = L[seg - 1]
+            for i in range(seg, j):
+                fL = _left_step(dmrg, i, fL, fmps['site%d' % i])
+                L[i] = fL
+            del fL
+        if sorted(L) != held:
+            raise RuntimeError("left environment schedule out of step")
         site = fmps['site%d' % j]
-        sval = torch.from_numpy(numpy.ascontiguousarray(site.value)).cuda()
-        fL, fR = Lenv[j - 1], Renv[j + 1]
-        chains = {}
-        for iop in range(dmrg.nops):
-            if not (fL.present(iop) and fR.present(iop)):
-                continue
-            c0 = op_class(dmrg.opers[iop][0], j)
-            if c0 not in chains:
-                rt = fR.tensors[iop]
-                lay_rf = eng.derive(rt.layout, [-rt.qsyms[0], qkey - rt.qsyms[1], qkey - rt.qsyms[2]],
-                                    rt.status)
-                chains[c0] = _GradChain(eng, site.layout, fL.layouts[iop], lay_rf)
-            ch = chains[c0]
-            lv = fL.buf.narrow(0, int(fL.off[iop]), fL.tensors[iop].size_allowed)
-            rv = fR.buf.narrow(0, int(fR.off[iop]), fR.tensors[iop].size_allowed)
-            t1 = torch.empty(max(ch.sizes[0], 1), dtype=torch.float64, device="cuda")
-            t2 = torch.empty(max(ch.sizes[1], 1), dtype=torch.float64, device="cuda")
-            g = torch.empty(max(ch.sizes[2], 1), dtype=torch.float64, device="cuda")
-            eng.contract_exec(ch.p1, sval, lv, t1)
-            eng.contract_exec(ch.p2, t1, sval, t2)
-            eng.contract_exec(ch.p3, t2, rv, g)
-            wt = mpo.tensors[j][iop]
-            # legs [n', a, n, b]: directions follow the contraction (bra
-            # site against the bra leg of L, ket legs against ket legs)
-            out = qtensor([False, False, True, True])
-            out.fromQsyms(4, [site.qsyms[1], wt.qsyms[0], site.qsyms[1], wt.qsyms[1]],
-                          [site.ndims[1], wt.ndims[0], site.ndims[1], wt.ndims[1]], ifallocate=False)
-            size, flat, _ = eng.layout_blocks(ch.lay_out)
-            if size != out.size_allowed or not numpy.array_equal(flat, out.blk_flat):
-                raise RuntimeError("site gradient layout mismatch")
-            out.value = g[:size].cpu().numpy()
-            dense = out.toDenseTensor([site.idlst[1], wt.idlst[0], site.idlst[1], wt.idlst[1]])
-            gq = dense.transpose(1, 3, 0, 2)            # [a, b, n', n] in sorted bond order
-            il, ir = _mpo.bond_order(dmrg.opers[iop], dmrg.sbas, j)
-            gb = numpy.zeros_like(gq)
-            gb[numpy.ix_(il, ir)] = gq
-            grads[j][iop] = dmrg.hpwts[iop] * gb / norm2
-        for ch in chains.values():
-            ch.release(eng)
+        _site_gradient(dmrg, eng, j, site, L[j - 1], fR, qkey, norm2, grads)
+        for x in [x for x in L if x >= j - 1]:
+            del L[x]
+        if j > 0:
+            fR = _right_step(dmrg, j, fR, site, qkey)
     return grads, esum / norm2, norm2
 
 
