@@ -457,6 +457,28 @@ struct MergeInfo {
   bool ok = false;
   MergeKey key;
 };
+// Merge keys of a part's groups in build order: only groups that may be
+// joined keep a key (most groups of some steps never can, and a key is
+// 184 bytes)
+struct MergeTable {
+  std::vector<int32_t> idx;     // per group: its key, or -1
+  std::vector<MergeKey> keys;
+  bool ok(size_t g) const { return idx[g] >= 0; }
+  const MergeKey &key(size_t g) const { return keys[(size_t)idx[g]]; }
+  void push(const MergeInfo &mi) {
+    if (mi.ok) {
+      idx.push_back((int32_t)keys.size());
+      keys.push_back(mi.key);
+    } else {
+      idx.push_back(-1);
+    }
+  }
+  void push_none() { idx.push_back(-1); }
+  void pop() {
+    if (idx.back() >= 0) keys.pop_back();
+    idx.pop_back();
+  }
+};
 
 // threads of one step's group build, and the block tasks per thread below
 // which fewer are used
@@ -464,11 +486,11 @@ constexpr int kBuildThreads = 4;
 constexpr int64_t kTasksPerThread = 8000;
 
 template <class StepLike>
-static void merge_column_blocks(StepLike &st, const std::vector<MergeInfo> &info) {
+static void merge_column_blocks(StepLike &st, const MergeTable &info) {
   std::unordered_map<MergeKey, std::vector<int>, MergeKeyHash> buckets;
   buckets.reserve(st.groups.size());
   for (size_t g = 0; g < st.groups.size(); ++g)
-    if (info[g].ok) buckets[info[g].key].push_back((int)g);
+    if (info.ok(g)) buckets[info.key(g)].push_back((int)g);
   bool any = false;
   for (const auto &kv : buckets) any = any || kv.second.size() >= 2;
   if (!any) return;  // nothing to join: the groups stay as they are
@@ -486,11 +508,11 @@ static void merge_column_blocks(StepLike &st, const std::vector<MergeInfo> &info
   };
   for (size_t gi = 0; gi < st.groups.size(); ++gi) {
     if (done[gi]) continue;
-    if (!info[gi].ok) {
+    if (!info.ok(gi)) {
       emit_plain((int)gi);
       continue;
     }
-    const std::vector<int> &bk = buckets[info[gi].key];
+    const std::vector<int> &bk = buckets[info.key(gi)];
     for (int x : bk) done[x] = 1;
     if (bk.size() < 2) {
       emit_plain((int)gi);
@@ -585,7 +607,7 @@ struct GroupPart {
   std::vector<Group> groups;
   std::vector<ColBlock> cblocks;
   std::vector<SegB> segb;
-  std::vector<MergeInfo> minfo;
+  MergeTable minfo;
   std::vector<Reduction> reds;   // offsets (part_off, elem0, part groups' c_off) local to the part
   int64_t part_elems = 0, red_elems = 0;
   double flops = 0.0;
@@ -603,7 +625,7 @@ static void split_last_group(GroupPart &out) {
   for (int i = 0; i < G.nseg; ++i) ktot += out.segs[G.seg0 + i].K;
   if (ktot <= kSplitK || G.M == 0 || G.N == 0) return;
   out.groups.pop_back();
-  out.minfo.pop_back();
+  out.minfo.pop();
   out.tmp.assign(out.segs.begin() + G.seg0, out.segs.begin() + G.seg0 + G.nseg);
   out.segs.resize(G.seg0);
   Reduction r;
@@ -632,7 +654,7 @@ static void split_last_group(GroupPart &out) {
   };
   auto close_part = [&]() {
     out.groups.push_back(cur);
-    out.minfo.push_back(MergeInfo{});  // parts are never joined
+    out.minfo.push_none();  // parts are never joined
   };
   open_part();
   int64_t kin = 0;
@@ -895,7 +917,7 @@ static int build_groups(std::vector<OutWork> &works, size_t w0, size_t w1, Group
       }
       g.nseg = (int32_t)out.segs.size() - g.seg0;
       out.groups.push_back(g);
-      out.minfo.push_back(mi);
+      out.minfo.push(mi);
       split_last_group(out);
     }
   }
