@@ -3,10 +3,38 @@
 #pragma once
 #include <cstdint>
 #include <memory>
+#include <new>
 #include <string>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 namespace zmpo {
+
+// Allocator whose resize() leaves new elements default-initialised (no zero
+// fill for the plain record types): the planner sizes its record arrays and
+// then fills them in place, part by part on several threads.
+template <class T>
+struct NoInitAllocator : std::allocator<T> {
+  using value_type = T;
+  template <class U>
+  struct rebind {
+    using other = NoInitAllocator<U>;
+  };
+  NoInitAllocator() noexcept = default;
+  template <class U>
+  NoInitAllocator(const NoInitAllocator<U> &) noexcept {}
+  template <class U>
+  void construct(U *p) noexcept(std::is_nothrow_default_constructible<U>::value) {
+    ::new (static_cast<void *>(p)) U;
+  }
+  template <class U, class... A>
+  void construct(U *p, A &&...a) {
+    ::new (static_cast<void *>(p)) U(std::forward<A>(a)...);
+  }
+};
+template <class T>
+using rec_vector = std::vector<T, NoInitAllocator<T>>;
 
 // Device task records.  A "group" is one dense output sub-matrix
 // C[m*scm + n*scn] (m < M, n < N) of an output block; it is the sum of its
@@ -118,10 +146,10 @@ struct Bufs {
 // One launch worth of tasks (device copies + host mirror of sizes).
 struct Step {
   int idx = 0;                   // position in its plan's chain
-  std::vector<Seg> segs;
-  std::vector<Group> groups;
-  std::vector<ColBlock> cblocks;
-  std::vector<SegB> segb;
+  rec_vector<Seg> segs;
+  rec_vector<Group> groups;
+  rec_vector<ColBlock> cblocks;
+  rec_vector<SegB> segb;
   Seg *d_segs = nullptr;
   Group *d_groups = nullptr;
   ColBlock *d_cblocks = nullptr;

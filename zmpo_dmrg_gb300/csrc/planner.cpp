@@ -494,8 +494,8 @@ static void merge_column_blocks(StepLike &st, const MergeTable &info) {
   bool any = false;
   for (const auto &kv : buckets) any = any || kv.second.size() >= 2;
   if (!any) return;  // nothing to join: the groups stay as they are
-  std::vector<Group> groups;
-  std::vector<Seg> segs;
+  rec_vector<Group> groups;
+  rec_vector<Seg> segs;
   groups.reserve(st.groups.size());
   segs.reserve(st.segs.size());
   std::vector<char> done(st.groups.size(), 0);
@@ -603,10 +603,10 @@ static void merge_column_blocks(StepLike &st, const MergeTable &info) {
 // Groups and segments of a range of output works (one part of a step, built
 // on its own thread; the parts are joined in order).
 struct GroupPart {
-  std::vector<Seg> segs;
-  std::vector<Group> groups;
-  std::vector<ColBlock> cblocks;
-  std::vector<SegB> segb;
+  rec_vector<Seg> segs;
+  rec_vector<Group> groups;
+  rec_vector<ColBlock> cblocks;
+  rec_vector<SegB> segb;
   MergeTable minfo;
   std::vector<Reduction> reds;   // offsets (part_off, elem0, part groups' c_off) local to the part
   int64_t part_elems = 0, red_elems = 0;
@@ -1084,8 +1084,8 @@ static int build_step(std::vector<OutWork> &works, Step &st) {
         *out++ = g;
       }
       // the part's records are released on its thread
-      std::vector<Seg>().swap(p.segs);
-      std::vector<SegB>().swap(p.segb);
+      rec_vector<Seg>().swap(p.segs);
+      rec_vector<SegB>().swap(p.segb);
     });
   for (auto &t : pool) t.join();
   return ZMPO_OK;
@@ -1585,8 +1585,8 @@ struct ListUpload {
   };
   std::vector<Part> parts;
   size_t total = 0;
-  template <class T>
-  void add(T **dptr, const std::vector<T> &v) {
+  template <class T, class A>
+  void add(T **dptr, const std::vector<T, A> &v) {
     *dptr = nullptr;
     if (v.empty()) return;
     const size_t bytes = v.size() * sizeof(T);
@@ -1622,7 +1622,7 @@ static int host_lists(Step &st, int precision) {
     if (rc) return rc;
     build_split_lists(st);
     place_step_owned(st);
-    if (st.up_common) std::vector<Seg>().swap(st.segs);
+    if (st.up_common) rec_vector<Seg>().swap(st.segs);
   } else if (precision == ZMPO_PREC_FP64 && !st.lists_fp64) {
     build_fp64_list(st);
   } else if (precision == ZMPO_PREC_EMU64 && !st.lists_emu) {
@@ -1647,7 +1647,7 @@ static int upload_lists(Step &st, int precision) {
     if (rc) return rc;
     if (st.part_elems > 0) CUDA_TRY(cudaMalloc((void **)&st.d_part, st.part_elems * sizeof(double)));
     st.up_common = true;
-    std::vector<Seg>().swap(st.segs);
+    rec_vector<Seg>().swap(st.segs);
   }
   int rc = host_lists(st, precision);
   if (rc) return rc;
