@@ -380,6 +380,17 @@ def sweep_converged(K=24, nelec=24, D=512, seed=2024, maxiter=14, tol=1e-8, hop=
     return out
 
 
+def section(name, fn):
+    """Run one optional section of the benchmark: its result, or, when it
+    raises, {"error": "<type>: <message>"} (also printed on stderr), so the
+    result line is printed whatever happens in the section."""
+    try:
+        return fn()
+    except Exception as ex:  # noqa: BLE001 -- reported in the result line
+        print("bench: %s failed: %r" % (name, ex), file=sys.stderr)
+        return {"error": "%s: %s" % (type(ex).__name__, ex)}
+
+
 def cpu_threads():
     return os.cpu_count() or 1
 
@@ -644,13 +655,6 @@ def main():
         result["roofline"] = rt
     # the sections after the sigma measurement each record their own failure
     # (the JSON line is printed whatever happens in them)
-    def section(name, fn):
-        try:
-            return fn()
-        except Exception as ex:  # noqa: BLE001 -- reported in the result line
-            print("bench: %s failed: %r" % (name, ex), file=sys.stderr)
-            return {"error": "%s: %s" % (type(ex).__name__, ex)}
-
     if rank == 0 and not args.no_sweep:
         result["sweep"] = section("sweep", sweep_converged)
         result["sweep_k10"] = section("sweep_k10", lambda: sweep_converged(K=10, nelec=10, D=64, maxiter=16))

@@ -513,3 +513,16 @@ def test_adjoint_left_environment_schedule():
             assert set(held) <= checkpoints | set(recomputed)
             assert len(held) <= 2 * stride + 1
         assert len(recomputed) == len(set(recomputed)) and len(recomputed) < nsite
+
+
+def test_bench_section_records_a_failure():
+    """A benchmark section that raises is recorded in the result line as an
+    error entry instead of stopping the run."""
+    import bench
+
+    def boom():
+        raise RuntimeError("Davidson: subspace H not symmetric")
+
+    assert bench.section("ok", lambda: {"s": 1.0}) == {"s": 1.0}
+    rec = bench.section("sweep", boom)
+    assert rec == {"error": "RuntimeError: Davidson: subspace H not symmetric"}
