@@ -286,10 +286,14 @@ def sweep_converged(K=24, nelec=24, D=512, seed=2024, maxiter=14, tol=1e-8, hop=
     from it for each arm, so both arms start from identical states), one FP64
     sweep pair and one split sweep pair at D, Davidson 1e-9, no noise, each
     timed alone: seconds per sweep pair and half sweep, matvecs, energies,
-    their difference, and whether each arm stayed within ``tol`` of the
-    phase-1 energy.  (The noisy ramp amplifies any perturbation, even one of
-    1e-15 in an environment, into a different truncation, so two runs of the
-    whole schedule are compared only through this common state.)"""
+    their difference, the difference of each arm from the phase-1 energy,
+    and whether each arm's pair is converged: its right and left half sweeps
+    end within ``tol`` of each other (the schedule's own test compares whole
+    sweeps; its last sweeps can still be above the fixed point, which the
+    noise-free pair at Davidson 1e-9 then reaches).  (The noisy ramp
+    amplifies any perturbation, even one of 1e-15 in an environment, into a
+    different truncation, so two runs of the whole schedule are compared
+    only through this common state.)"""
     import torch
     from zmpo_dmrg_gb300 import integrals as I
     from zmpo_dmrg_gb300.mpo_dmrg_class import mpo_dmrg
@@ -341,7 +345,8 @@ def sweep_converged(K=24, nelec=24, D=512, seed=2024, maxiter=14, tol=1e-8, hop=
         dt = time.perf_counter() - t0
         e = min(float(r1[2]), float(r2[2]))
         out[prec] = {"s_per_sweep": dt, "s_per_half_sweep": dt / 2, "energy": e, "matvecs": int(r1[0] + r2[0]),
-                     "converged": bool(out["converge"]["converged"]) and abs(e - e_conv) < tol,
+                     "converged": abs(float(r1[2]) - float(r2[2])) < tol,
+                     "dE_half_sweeps": float(r2[2]) - float(r1[2]),
                      "dE_vs_converged": e - e_conv}
         # plans built for structures not met before, and plans reused
         out[prec]["plans"] = dict(m.plan_counts)
