@@ -526,3 +526,34 @@ def test_bench_section_records_a_failure():
     assert bench.section("ok", lambda: {"s": 1.0}) == {"s": 1.0}
     rec = bench.section("sweep", boom)
     assert rec == {"error": "RuntimeError: Davidson: subspace H not symmetric"}
+
+
+def test_buffer_check_names_the_changed_buffer():
+    """The driver's debug integrity check (dmrg.check_buffers) records the
+    checksums of the MPO buffer and of every stored environment set, accepts
+    them unchanged and new sets as they appear, and names the buffer that
+    changed."""
+    import torch
+    from types import SimpleNamespace
+    from zmpo_dmrg_gb300.mpo_dmrg_class import check_buffers
+    from zmpo_dmrg_gb300.mpo_dmrg_kernel import EnvSet
+    rng = numpy.random.default_rng(0)
+
+    def env(n):
+        return EnvSet(torch.from_numpy(rng.standard_normal(n)), numpy.zeros(1, dtype=numpy.int64),
+                      numpy.zeros(1, dtype=numpy.int64), [None])
+
+    d = SimpleNamespace(mpo_store=SimpleNamespace(buf=torch.from_numpy(rng.standard_normal(50))),
+                        envs={('lop', 0): env(10), ('rop', 5): env(1)})
+    check_buffers(d, "at the start")
+    check_buffers(d, "unchanged")
+    d.envs[('lop', 1)] = env(7)          # a new set is recorded, not an error
+    check_buffers(d, "after a renormalisation")
+    d.envs[('rop', 5)].buf[0] += 1.0
+    with pytest.raises(RuntimeError, match="environment rop 5 changed before dot 3"):
+        check_buffers(d, "before dot 3")
+    d2 = SimpleNamespace(mpo_store=SimpleNamespace(buf=torch.ones(4, dtype=torch.float64)), envs={})
+    check_buffers(d2, "first")
+    d2.mpo_store.buf[3] = 2.0
+    with pytest.raises(RuntimeError, match="MPO buffer changed"):
+        check_buffers(d2, "second")

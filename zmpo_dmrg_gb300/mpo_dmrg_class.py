@@ -68,6 +68,39 @@ def dense_sector(qlst, key):
     return numpy.flatnonzero(numpy.abs(tot - k).sum(axis=1) < 1e-10)
 
 
+def check_buffers(dmrg, where):
+    """Integrity check for debugging (``dmrg.check_buffers = True``, off by
+    default): the MPO buffer and every stored environment set must keep the
+    checksums (sum and sum of squares) they had when first seen; an
+    environment set replaced by a new one is checked from then on.  Raises
+    RuntimeError naming the first buffer that changed and ``where``.  Each
+    check reads every stored environment once (a device reduction)."""
+    torch = _torch()
+    seen = dmrg.__dict__.setdefault("_buffer_sums", {})
+
+    def sums(t):
+        t = t.reshape(-1)
+        return (float(t.sum()), float(torch.dot(t, t)))
+
+    items = [("MPO buffer", "mpo", dmrg.mpo_store.buf)]
+    for key in sorted(dmrg.envs, key=lambda k: (k[0], k[1])):
+        env = dmrg.envs[key]
+        if env is not None:
+            items.append(("environment %s %d" % key, ("env", env.uid), env.buf))
+    live = set()
+    for name, tag, buf in items:
+        live.add(tag)
+        cur = sums(buf)
+        old = seen.get(tag)
+        if old is None:
+            seen[tag] = cur
+        elif old != cur:
+            raise RuntimeError("buffer check: %s changed %s (sum %r -> %r, squares %r -> %r)"
+                               % (name, where, old[0], cur[0], old[1], cur[1]))
+    for tag in [t for t in seen if t not in live]:
+        del seen[tag]
+
+
 def rdm_blkdiag(rho0, classes, thresh, Dcut=-1):
     """Block eigen-decomposition of the reduced density matrix by sector and
     truncation (mpo_dmrg_qparser.rdm_blkdiag, mpo_dmrg_qparser.py:106-183)."""
@@ -655,6 +688,8 @@ class mpo_dmrg:
         elst, dlst = [], []
         nmvp = 0
         for isite in actlst:
+            if getattr(self, "check_buffers", False):
+                check_buffers(self, "before the %s-sweep dot at site %d" % (status, isite))
             t0 = time.perf_counter()
             self.tick(None)
             flst = self._flst(isite - 1, isite + ncsite)
