@@ -557,3 +557,18 @@ def test_buffer_check_names_the_changed_buffer():
     d2.mpo_store.buf[3] = 2.0
     with pytest.raises(RuntimeError, match="MPO buffer changed"):
         check_buffers(d2, "second")
+
+
+def test_adjoint_recompute_choice_follows_memory():
+    """Without an explicit choice the energy gradient recomputes its
+    environments when one more full set (the size of the sets the driver
+    holds) would take more than half of the free device memory."""
+    from types import SimpleNamespace
+    import torch
+    from zmpo_dmrg_gb300.adjoint import needs_recompute, _held_env_bytes
+    assert not needs_recompute(10 * 2 ** 30, 200 * 2 ** 30)
+    assert needs_recompute(120 * 2 ** 30, 200 * 2 ** 30)
+    d = SimpleNamespace(envs={('lop', 0): SimpleNamespace(buf=torch.zeros(1000, dtype=torch.float64)),
+                              ('rop', 3): SimpleNamespace(buf=torch.zeros(24, dtype=torch.float64)),
+                              ('lop', 1): None})
+    assert _held_env_bytes(d) == 8 * 1024

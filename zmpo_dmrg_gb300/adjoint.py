@@ -185,6 +185,19 @@ def _site_gradient(dmrg, eng, j, site, fL, fR, qkey, norm2, grads):
         ch.release(eng)
 
 
+def needs_recompute(env_bytes, free_bytes, margin=0.5):
+    """Whether the energy gradient should recompute its environments: the
+    stored mode makes one more full set of environments next to the ones the
+    driver holds (``env_bytes``, estimated by their size); it is used while
+    that stays below ``margin`` of the free device memory."""
+    return env_bytes > margin * free_bytes
+
+
+def _held_env_bytes(dmrg):
+    """Bytes of the environment sets the driver holds (every bond, both sides)."""
+    return sum(int(env.buf.numel()) * 8 for env in dmrg.envs.values() if env is not None)
+
+
 def site_gradients(dmrg, fmps=None, recompute_envs=None):
     """dE/dW_p(j) for every site j and term p as dense [Dw_l, Dw_r, 4, 4]
     arrays in the builder's bond order, and <H> and <psi|psi> of the MPS.
@@ -198,11 +211,17 @@ def site_gradients(dmrg, fmps=None, recompute_envs=None):
     between recomputed from the nearest checkpoint when they are needed
     (``left_env_schedule``): about 2 sqrt(nsite) environment sets held and
     one more left renormalisation per site.  The same renormalisations run
-    on the same inputs, so both modes give the same gradients."""
+    on the same inputs, so both modes give the same gradients.  When neither
+    the argument nor the attribute chooses, the mode follows the memory:
+    recompute when another full set of environments would not fit
+    (``needs_recompute``)."""
     if dmrg.ifs2proj:
         raise NotImplementedError("energy gradient of the spin-projected energy")
     if recompute_envs is None:
-        recompute_envs = bool(getattr(dmrg, "adjoint_recompute_envs", False))
+        recompute_envs = getattr(dmrg, "adjoint_recompute_envs", None)
+    if recompute_envs is None:
+        free, _ = _torch().cuda.mem_get_info()
+        recompute_envs = needs_recompute(_held_env_bytes(dmrg), free)
     fmps = dmrg.flmps if fmps is None else fmps
     eng = _engine.get()
     nsite = dmrg.nsite
